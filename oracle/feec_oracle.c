@@ -1,0 +1,396 @@
+/*
+ * ORACLE — test infrastructure, not product code.
+ *
+ * A plain-C restatement of the FEEC++ reference algorithms on the sparse CSR
+ * Krylov path, used only as the checker by tests/, __graft_entry__.smoke() and
+ * bench.py's CPU-baseline / reference legs. Nothing in the product library
+ * links, loads or calls this file.
+ *
+ * Every function follows the cited reference lines statement by statement,
+ * including loop order and accumulation order, so that at one OpenMP thread
+ * its outputs are bit-identical to the reference's on the same inputs (pinned
+ * by tests/test_oracle.py against fixtures written by the reference itself).
+ * Build with -ffp-contract=off so that no fused multiply-add changes rounding.
+ *
+ * OpenMP is used exactly where the reference uses `parallel for`. The plain CG
+ * direction update (solver/sparsesolver.cpp:179-183) is `omp parallel` without
+ * `for` in the reference, a race that stops convergence with more than one
+ * thread; the restatement runs that loop serially, which is what the reference
+ * computes at one thread.
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+/* base/base.hpp:123, 127-128: machine_epsilon = 2^-52, desired_precision = sqrt(machine_epsilon) */
+static const double ORACLE_MACHINE_EPSILON = 2.220446049250313080847263336181640625e-16;
+static const double ORACLE_DESIRED_PRECISION = 1.490116119384765625e-08;
+
+static double dmax(double a, double b) { return a > b ? a : b; }
+
+/* sparse/matcsr.cpp:216-244: dest = 0; dest[i] += scaling * V[j] * src[C[j]] */
+void oracle_csr_apply(int N, const int* A, const int* C, const double* V,
+                      const double* src, double* dest, double scaling)
+{
+    for (int i = 0; i < N; i++) dest[i] = 0.0;
+    #pragma omp parallel for
+    for (int i = 0; i < N; i++)
+        for (int j = A[i]; j < A[i + 1]; j++)
+            dest[i] += scaling * V[j] * src[C[j]];
+}
+
+/* sparse/matcsr.cpp:266-286: sum of the stored entries with C == row */
+void oracle_csr_diagonal(int N, const int* A, const int* C, const double* V, double* diag)
+{
+    #pragma omp parallel for
+    for (int r = 0; r < N; r++) {
+        diag[r] = 0.0;
+        for (int i = A[r]; i < A[r + 1]; i++)
+            if (C[i] == r) diag[r] += V[i];
+    }
+}
+
+/* sparse/rainbow.cpp:14-130 with do_shuffle = false. F[N], B[N+1] (only
+ * num_colors+1 used), R[N]. Returns num_colors, or -1 on an invalid result. */
+int oracle_rainbow(int N, const int* A, const int* C, int* F, int* B, int* R)
+{
+    int num_colors = 1;                                       /* :35 */
+    for (int r = 0; r < N; r++) F[r] = 0;                     /* :46 */
+    for (int r = 0; r < N; r++) {                             /* :48-75, painting order = identity */
+    again:
+        for (int c = A[r]; c < A[r + 1]; c++) {
+            int j = C[c];
+            if (j == r) continue;
+            if (F[j] == F[r]) { F[r]++; goto again; }
+        }
+        if (F[r] == num_colors) num_colors++;
+    }
+    int* counter = (int*)calloc((size_t)num_colors, sizeof(int));   /* :81-85 */
+    if (!counter) return -1;
+    for (int r = 0; r < N; r++) counter[F[r]]++;
+    B[0] = 0;                                                 /* :91-93 */
+    for (int c = 1; c < num_colors + 1; c++) B[c] = counter[c - 1];
+    for (int c = 1; c < num_colors + 1; c++) B[c] += B[c - 1];
+    for (int r = 0; r < N; r++) R[r] = -1;                    /* :101-117: filled from the top of each color */
+    for (int r = 0; r < N; r++) {
+        int color = F[r];
+        counter[color]--;
+        R[B[color] + counter[color]] = r;
+    }
+    free(counter);
+    return num_colors;
+}
+
+/* solver/sparsesolver.cpp:26-201, unpreconditioned CG; returns K */
+int oracle_cg(int N, double* x, const double* b, const int* A, const int* C, const double* V,
+              double* residual, double precision, int print_modulo)
+{
+    (void)print_modulo;
+    double tolerance = 0.0;                                   /* :45-48 */
+    for (int i = 0; i < N; i++) tolerance += b[i] * b[i];
+    tolerance = precision * sqrt(tolerance);
+    tolerance = dmax(tolerance, ORACLE_DESIRED_PRECISION);
+
+    double* direction = (double*)malloc(sizeof(double) * (size_t)N);   /* :62-63 */
+    double* auxiliary = (double*)malloc(sizeof(double) * (size_t)N);
+    if (!direction || !auxiliary) { free(direction); free(auxiliary); return -1; }
+    for (int i = 0; i < N; i++) direction[i] = auxiliary[i] = NAN;
+
+    double r_r = NAN;
+    int K = 0;
+    while (K < N) {                                           /* :74 */
+        if (K == 0) {                                         /* :76-104 */
+            r_r = 0.0;
+            #pragma omp parallel for reduction(+:r_r)
+            for (int c = 0; c < N; c++) {
+                residual[c] = b[c];
+                for (int d = A[c]; d < A[c + 1]; d++) residual[c] -= V[d] * x[C[d]];
+                direction[c] = residual[c];
+                r_r += residual[c] * residual[c];
+            }
+        }
+        if (fabs(r_r) < tolerance * tolerance) break;        /* :116-119 */
+
+        double d_Ad = 0.0;                                    /* :126-139 */
+        #pragma omp parallel for reduction(+:d_Ad)
+        for (int c = 0; c < N; c++) {
+            auxiliary[c] = 0.0;
+            for (int d = A[c]; d < A[c + 1]; d++) auxiliary[c] += V[d] * direction[C[d]];
+            d_Ad += direction[c] * auxiliary[c];
+        }
+        int numerator_bad = !isfinite(r_r) || r_r < 0.0;      /* :142-155 */
+        int denominator_bad = !isfinite(d_Ad) || d_Ad < 0.0;
+        int denominator_small = sqrt(fabs(d_Ad)) < ORACLE_MACHINE_EPSILON;
+        if (numerator_bad || denominator_bad) break;
+        if (denominator_small) break;
+
+        double alpha = r_r / d_Ad;                            /* :158-173 */
+        double r_r_new = 0.0;
+        #pragma omp parallel for reduction(+:r_r_new)
+        for (int c = 0; c < N; c++) {
+            x[c] += alpha * direction[c];
+            residual[c] -= alpha * auxiliary[c];
+            r_r_new += residual[c] * residual[c];
+        }
+        double beta = r_r_new / r_r;                          /* :175-183 */
+        r_r = r_r_new;
+        for (int c = 0; c < N; c++) direction[c] = residual[c] + beta * direction[c];
+        K++;
+    }
+    free(direction);
+    free(auxiliary);
+    return K;
+}
+
+/* solver/sparsesolver.cpp:446-724, SSOR-preconditioned CG in index order; returns K */
+int oracle_cg_ssor(int N, double* x, const double* b, const int* A, const int* C, const double* V,
+                   double* residual, double precision, int print_modulo,
+                   const double* diagonal, double omega)
+{
+    (void)print_modulo;
+    double tolerance = 0.0;                                   /* :463-466 */
+    for (int i = 0; i < N; i++) tolerance += b[i] * b[i];
+    tolerance = precision * sqrt(tolerance);
+    tolerance = dmax(tolerance, ORACLE_DESIRED_PRECISION);
+
+    double* direction = (double*)calloc((size_t)N, sizeof(double));     /* :479-490 */
+    double* zirconium = (double*)calloc((size_t)N, sizeof(double));
+    double* auxiliary = (double*)calloc((size_t)N, sizeof(double));
+    double* mittlerer = (double*)calloc((size_t)N, sizeof(double));
+    if (!direction || !zirconium || !auxiliary || !mittlerer) {
+        free(direction); free(zirconium); free(auxiliary); free(mittlerer); return -1;
+    }
+    double z_r = NAN;
+    int K = 0;
+    while (K < N) {
+        if (K == 0) {                                         /* :506-588 */
+            #pragma omp parallel for
+            for (int c = 0; c < N; c++) {
+                if (diagonal[c] == 0.0) continue;
+                residual[c] = b[c];
+                for (int d = A[c]; d < A[c + 1]; d++) residual[c] -= V[d] * x[C[d]];
+            }
+            for (int c = 0; c < N; c++) {
+                if (diagonal[c] == 0.0) continue;
+                double aux = residual[c];
+                for (int d = A[c]; d < A[c + 1]; d++)
+                    if (C[d] < c) aux -= V[d] * mittlerer[C[d]];
+                mittlerer[c] = aux * omega / diagonal[c];
+            }
+            #pragma omp parallel for
+            for (int c = 0; c < N; c++) {
+                if (diagonal[c] == 0.0) continue;
+                mittlerer[c] *= diagonal[c];
+                mittlerer[c] *= (2.0 - omega) / omega;
+            }
+            for (int c = N - 1; c >= 0; c--) {
+                if (diagonal[c] == 0.0) continue;
+                double aux = mittlerer[c];
+                for (int d = A[c]; d < A[c + 1]; d++)
+                    if (C[d] > c) aux -= V[d] * zirconium[C[d]];
+                zirconium[c] = aux * omega / diagonal[c];
+            }
+            z_r = 0.0;
+            #pragma omp parallel for reduction(+:z_r)
+            for (int c = 0; c < N; c++) {
+                if (diagonal[c] == 0.0) continue;
+                direction[c] = zirconium[c];
+                z_r += zirconium[c] * residual[c];
+            }
+        }
+        if (fabs(z_r) < tolerance * tolerance) break;        /* :601-604 */
+
+        double d_Ad = 0.0;                                    /* :611-626 */
+        #pragma omp parallel for reduction(+:d_Ad)
+        for (int c = 0; c < N; c++) {
+            auxiliary[c] = 0.0;
+            if (diagonal[c] == 0.0) continue;
+            for (int d = A[c]; d < A[c + 1]; d++) auxiliary[c] += V[d] * direction[C[d]];
+            d_Ad += direction[c] * auxiliary[c];
+        }
+        int numerator_bad = !isfinite(z_r) || z_r < 0.0;
+        int denominator_bad = !isfinite(d_Ad) || d_Ad < 0.0;
+        int denominator_small = sqrt(fabs(d_Ad)) < ORACLE_MACHINE_EPSILON;
+        if (numerator_bad || denominator_bad) break;
+        if (denominator_small) break;
+
+        const double alpha = z_r / d_Ad;                      /* :645-663 */
+        for (int c = 0; c < N; c++) {
+            if (diagonal[c] == 0.0) continue;
+            x[c] += alpha * direction[c];
+            residual[c] -= alpha * auxiliary[c];
+            double aux = residual[c];
+            for (int d = A[c]; d < A[c + 1]; d++)
+                if (C[d] < c) aux -= V[d] * mittlerer[C[d]];
+            mittlerer[c] = aux * omega / diagonal[c];
+        }
+        double z_r_new = 0.0;                                 /* :665-692 */
+        for (int c = N - 1; c >= 0; c--) {
+            if (diagonal[c] == 0.0) continue;
+            mittlerer[c] *= diagonal[c];
+            mittlerer[c] *= (2.0 - omega) / omega;
+            double aux = mittlerer[c];
+            for (int d = A[c]; d < A[c + 1]; d++)
+                if (C[d] > c) aux -= V[d] * zirconium[C[d]];
+            zirconium[c] = aux * omega / diagonal[c];
+            z_r_new += zirconium[c] * residual[c];
+        }
+        const double beta = z_r_new / z_r;                    /* :694-709 */
+        z_r = z_r_new;
+        #pragma omp parallel for
+        for (int c = 0; c < N; c++) {
+            if (diagonal[c] == 0.0) continue;
+            direction[c] = zirconium[c] + beta * direction[c];
+        }
+        K++;
+    }
+    free(direction); free(zirconium); free(auxiliary); free(mittlerer);
+    return K;
+}
+
+/* solver/sparsesolver.cpp:1002-1335, multicolor ("Rainbow") SSOR-PCG; returns K */
+int oracle_cg_rainbow(int N, double* x, const double* b, const int* A, const int* C, const double* V,
+                      double* residual, double precision, int print_modulo,
+                      const double* diagonal, double omega,
+                      int num_colors, const int* F, const int* B, const int* R)
+{
+    (void)print_modulo;
+    double tolerance = 0.0;                                   /* :1030-1033 */
+    for (int i = 0; i < N; i++) tolerance += b[i] * b[i];
+    tolerance = precision * sqrt(tolerance);
+    tolerance = dmax(tolerance, ORACLE_DESIRED_PRECISION);
+
+    double* direction = (double*)calloc((size_t)N, sizeof(double));     /* :1046-1057 */
+    double* zirconium = (double*)calloc((size_t)N, sizeof(double));
+    double* auxiliary = (double*)calloc((size_t)N, sizeof(double));
+    double* mittlerer = (double*)calloc((size_t)N, sizeof(double));
+    if (!direction || !zirconium || !auxiliary || !mittlerer) {
+        free(direction); free(zirconium); free(auxiliary); free(mittlerer); return -1;
+    }
+    double z_r = NAN;
+    int K = 0;
+    while (K < N) {
+        if (K == 0) {                                         /* :1072-1175 */
+            #pragma omp parallel for
+            for (int c = 0; c < N; c++) {
+                if (diagonal[c] == 0.0) continue;
+                residual[c] = b[c];
+                for (int d = A[c]; d < A[c + 1]; d++) residual[c] -= V[d] * x[C[d]];
+            }
+            for (int color = 0; color < num_colors; color++) {
+                #pragma omp parallel for
+                for (int i = B[color]; i < B[color + 1]; i++) {
+                    int c = R[i];
+                    if (diagonal[c] == 0.0) continue;
+                    double aux = residual[c];
+                    for (int d = A[c]; d < A[c + 1]; d++)
+                        if (F[C[d]] < F[c]) aux -= V[d] * mittlerer[C[d]];
+                    mittlerer[c] = aux * omega / diagonal[c];
+                }
+            }
+            #pragma omp parallel for
+            for (int c = 0; c < N; c++) {
+                if (diagonal[c] == 0.0) continue;
+                mittlerer[c] *= diagonal[c];
+                mittlerer[c] *= (2.0 - omega) / omega;
+            }
+            for (int color = num_colors - 1; color >= 0; color--) {
+                #pragma omp parallel for
+                for (int i = B[color]; i < B[color + 1]; i++) {
+                    int c = R[i];
+                    if (diagonal[c] == 0.0) continue;
+                    double aux = mittlerer[c];
+                    for (int d = A[c]; d < A[c + 1]; d++)
+                        if (F[C[d]] > F[c]) aux -= V[d] * zirconium[C[d]];
+                    zirconium[c] = aux * omega / diagonal[c];
+                }
+            }
+            z_r = 0.0;
+            #pragma omp parallel for reduction(+:z_r)
+            for (int c = 0; c < N; c++) {
+                if (diagonal[c] == 0.0) continue;
+                direction[c] = zirconium[c];
+                z_r += zirconium[c] * residual[c];
+            }
+        }
+        if (fabs(z_r) < tolerance * tolerance) break;        /* :1187-1190 */
+
+        double d_Ad = 0.0;                                    /* :1197-1212 */
+        #pragma omp parallel for reduction(+:d_Ad)
+        for (int c = 0; c < N; c++) {
+            auxiliary[c] = 0.0;
+            if (diagonal[c] == 0.0) continue;
+            for (int d = A[c]; d < A[c + 1]; d++) auxiliary[c] += V[d] * direction[C[d]];
+            d_Ad += direction[c] * auxiliary[c];
+        }
+        int numerator_bad = !isfinite(z_r) || z_r < 0.0;
+        int denominator_bad = !isfinite(d_Ad) || d_Ad < 0.0;
+        int denominator_small = sqrt(fabs(d_Ad)) < ORACLE_MACHINE_EPSILON;
+        if (numerator_bad || denominator_bad) break;
+        if (denominator_small) break;
+
+        const double alpha = z_r / d_Ad;                      /* :1230-1261 */
+        for (int color = 0; color < num_colors; color++) {
+            #pragma omp parallel for
+            for (int i = B[color]; i < B[color + 1]; i++) {
+                int c = R[i];
+                if (diagonal[c] == 0.0) continue;
+                x[c] += alpha * direction[c];
+                residual[c] -= alpha * auxiliary[c];
+                double aux = residual[c];
+                for (int d = A[c]; d < A[c + 1]; d++)
+                    if (F[C[d]] < F[c]) aux -= V[d] * mittlerer[C[d]];
+                mittlerer[c] = aux * omega / diagonal[c];
+            }
+        }
+        double z_r_new = 0.0;                                 /* :1263-1307 */
+        for (int color = num_colors - 1; color >= 0; color--) {
+            double z_r_new_local = 0.0;
+            #pragma omp parallel for reduction(+:z_r_new_local)
+            for (int i = B[color]; i < B[color + 1]; i++) {
+                int c = R[i];
+                if (diagonal[c] == 0.0) continue;
+                mittlerer[c] *= diagonal[c];
+                mittlerer[c] *= (2.0 - omega) / omega;
+                double aux = mittlerer[c];
+                for (int d = A[c]; d < A[c + 1]; d++)
+                    if (F[C[d]] > F[c]) aux -= V[d] * zirconium[C[d]];
+                zirconium[c] = aux * omega / diagonal[c];
+                z_r_new_local += zirconium[c] * residual[c];
+            }
+            z_r_new += z_r_new_local;
+        }
+        const double beta = z_r_new / z_r;                    /* :1309-1318 */
+        z_r = z_r_new;
+        #pragma omp parallel for
+        for (int c = 0; c < N; c++) {
+            if (diagonal[c] == 0.0) continue;
+            direction[c] = zirconium[c] + beta * direction[c];
+        }
+        K++;
+    }
+    free(direction); free(zirconium); free(auxiliary); free(mittlerer);
+    return K;
+}
+
+/* Number of OpenMP threads the oracle would use (1 without OpenMP). */
+int oracle_max_threads(void)
+{
+#if defined(_OPENMP)
+    extern int omp_get_max_threads(void);
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
+void oracle_set_threads(int n)
+{
+#if defined(_OPENMP)
+    extern void omp_set_num_threads(int);
+    if (n > 0) omp_set_num_threads(n);
+#else
+    (void)n;
+#endif
+}

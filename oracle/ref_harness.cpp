@@ -1,0 +1,258 @@
+// Test infrastructure, not product code.
+//
+// Drives the unmodified FEEC++ reference (linked from its own object files,
+// built by oracle/Makefile.ref) so that the tests can pin the oracle and the
+// GPU path against the reference's own outputs. Only tests/golden/make_golden.py
+// runs this binary, and only where the reference sources are present.
+//
+// Commands (all files little-endian, formats documented in tests/golden/README):
+//   assemble <dim> <r> <L> <coef_seed> <out.csr>
+//       Mesh UnitSquare2D_simple (mesh/examples2D.hpp:194-210) or UnitCube3D
+//       (mesh/examples3D.hpp:14-37), uniformly refined L times; Lagrange P_r
+//       stiffness + mass assembled through the FEEC route that
+//       tests/solverfem/csrsolver_stiff.cpp:209-243 uses. coef_seed != 0 scales
+//       the broken scalar mass cell by cell with a log-uniform [0.1,10] factor
+//       hashed from the cell position (cell_coefficient below).
+//       Writes the CSR plus the position of every global degree of freedom.
+//   solve <cg|ssor|rainbow> <in.csr> <in.vec b> <in.vec x0> <precision> <omega> <out.sol>
+//       Calls ConjugateGradientSolverCSR{,_SSOR,_Rainbow} (solver/sparsesolver.hpp)
+//       with print_modulo = -3; writes K, x, residual, solve seconds.
+//   rainbow <in.csr> <out.rb>        Rainbow(A) (sparse/rainbow.cpp:14-130)
+//   apply <in.csr> <in.vec> <scaling> <out.vec>   MatrixCSR::apply (sparse/matcsr.cpp:216-244)
+//   diag <in.csr> <out.vec>          MatrixCSR::getDiagonal (sparse/matcsr.cpp:266-286)
+
+#include <chrono>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <random>
+#include <string>
+#include <vector>
+
+#include "base/include.hpp"
+#include "sparse/sparsematrix.hpp"
+#include "sparse/matcsr.hpp"
+#include "sparse/rainbow.hpp"
+#include "mesh/mesh.simplicial2D.hpp"
+#include "mesh/mesh.simplicial3D.hpp"
+#include "mesh/examples2D.hpp"
+#include "mesh/examples3D.hpp"
+#include "solver/sparsesolver.hpp"
+#include "fem/global.inclsullivan.hpp"
+#include "fem/global.massmatrix.hpp"
+#include "fem/global.diffmatrix.hpp"
+#include "combinatorics/generatemultiindices.hpp"
+
+static void die(const char* m) { std::fprintf(stderr, "ref_harness: %s\n", m); std::exit(2); }
+
+struct Csr { int64_t n = 0, ncols = 0, nnz = 0, pdim = 0; std::vector<int> A, C; std::vector<double> V, pos; };
+
+static void write_csr(const char* path, const Csr& m) {
+    FILE* f = std::fopen(path, "wb"); if (!f) die("cannot write csr");
+    const char magic[8] = {'F','E','E','C','C','S','R','1'};
+    std::fwrite(magic, 1, 8, f);
+    int64_t hdr[4] = {m.n, m.ncols, m.nnz, m.pdim};
+    std::fwrite(hdr, 8, 4, f);
+    std::fwrite(m.A.data(), 4, m.n + 1, f);
+    std::fwrite(m.C.data(), 4, m.nnz, f);
+    std::fwrite(m.V.data(), 8, m.nnz, f);
+    if (m.pdim) std::fwrite(m.pos.data(), 8, m.n * m.pdim, f);
+    std::fclose(f);
+}
+
+static Csr read_csr(const char* path) {
+    FILE* f = std::fopen(path, "rb"); if (!f) die("cannot read csr");
+    char magic[8]; if (std::fread(magic, 1, 8, f) != 8 || std::memcmp(magic, "FEECCSR1", 8)) die("bad csr magic");
+    int64_t hdr[4]; if (std::fread(hdr, 8, 4, f) != 4) die("short csr");
+    Csr m; m.n = hdr[0]; m.ncols = hdr[1]; m.nnz = hdr[2]; m.pdim = hdr[3];
+    m.A.resize(m.n + 1); m.C.resize(m.nnz); m.V.resize(m.nnz); m.pos.resize(m.n * m.pdim);
+    if (std::fread(m.A.data(), 4, m.n + 1, f) != (size_t)(m.n + 1)) die("short A");
+    if (std::fread(m.C.data(), 4, m.nnz, f) != (size_t)m.nnz) die("short C");
+    if (std::fread(m.V.data(), 8, m.nnz, f) != (size_t)m.nnz) die("short V");
+    std::fclose(f);
+    return m;
+}
+
+static std::vector<double> read_vec(const char* path, int64_t n) {
+    std::vector<double> v(n);
+    FILE* f = std::fopen(path, "rb"); if (!f) die("cannot read vec");
+    if (std::fread(v.data(), 8, n, f) != (size_t)n) die("short vec");
+    std::fclose(f);
+    return v;
+}
+
+static void write_raw(FILE* f, const void* p, size_t bytes) { if (bytes && std::fwrite(p, 1, bytes, f) != bytes) die("write"); }
+
+static MatrixCSR to_matrix(const Csr& m) {
+    std::vector<int> A(m.A), C(m.C); std::vector<Float> V(m.V.begin(), m.V.end());
+    return MatrixCSR((int)m.n, (int)m.ncols, std::move(A), std::move(C), std::move(V));
+}
+
+static Csr from_matrix(const MatrixCSR& mat) {
+    Csr m; m.n = mat.getdimout(); m.ncols = mat.getdimin(); m.nnz = mat.getnumberofentries();
+    m.A.assign(mat.getA(), mat.getA() + m.n + 1);
+    m.C.assign(mat.getC(), mat.getC() + m.nnz);
+    m.V.assign(mat.getV(), mat.getV() + m.nnz);
+    return m;
+}
+
+// SplitMix64 -> uniform double in [lo, hi); same generator as the package's workload module.
+static uint64_t splitmix64(uint64_t& s) {
+    uint64_t z = (s += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+static double unit_double(uint64_t& s) { return (double)(splitmix64(s) >> 11) * (1.0 / 9007199254740992.0); }
+
+// Coefficient of the cell whose vertex coordinates (in units of the finest
+// lattice spacing) sum to (sx, sy, sz): 10^(2u-1), u uniform in [0,1).
+static double cell_coefficient(uint64_t seed, int64_t sx, int64_t sy, int64_t sz) {
+    uint64_t s = seed ^ ((uint64_t)sx * 0x9E3779B97F4A7C15ull) ^ ((uint64_t)sy * 0xC2B2AE3D27D4EB4Full) ^ ((uint64_t)sz * 0x165667B19E3779F9ull);
+    return std::pow(10.0, 2.0 * unit_double(s) - 1.0);
+}
+
+template <class MeshT>
+static Csr assemble_on(MeshT& M, int n, int r, int L, uint64_t coef_seed) {
+    SparseMatrix M0 = FEECBrokenMassMatrix(M, n, 0, r);
+    SparseMatrix M1 = FEECBrokenMassMatrix(M, n, 1, r - 1);
+    SparseMatrix D  = FEECBrokenDiffMatrix(M, n, 0, r);
+    SparseMatrix I  = FEECSullivanInclusionMatrix(M, n, 0, r);
+    const int nvol = M.count_simplices(n);
+    const int localdim = (int)M0.getdimout() / nvol;
+    if (coef_seed != 0) {
+        // Log-uniform [0.1, 10] per cell. The factor is a hash of the cell's
+        // vertex-coordinate sum on the 2^L lattice, so that any numbering of the
+        // same mesh draws the same field (the package's lattice assembler uses
+        // the identical rule).
+        const auto& cc = M.getCoordinates();
+        const double scale = std::ldexp(1.0, L);
+        for (auto& e : M0.getentries()) {
+            const int s = e.row / localdim;
+            const IndexMap verts = M.get_subsimplices(n, 0, s);
+            int64_t S[3] = {0, 0, 0};
+            for (int v = 0; v <= n; v++)
+                for (int d = 0; d < n; d++) S[d] += (int64_t)std::llround(cc.getdata(verts.at(v), d) * scale);
+            e.value *= cell_coefficient(coef_seed, S[0], S[1], S[2]);
+        }
+    }
+    M0.sortandcompressentries();
+    M1.sortandcompressentries();
+    SparseMatrix opr = D & I;
+    SparseMatrix opl = opr.getTranspose();
+    SparseMatrix stiff = opl & (M1 & opr);
+    stiff.sortentries();
+    SparseMatrix It = I.getTranspose();
+    SparseMatrix mass = It & (M0 & I);
+    mass.sortentries();
+    MatrixCSR sum = MatrixCSR(stiff) + MatrixCSR(mass);
+    Csr out = from_matrix(sum);
+
+    // Positions of the global degrees of freedom, read off the inclusion matrix:
+    // broken row s*localdim + a carries the Bernstein multi-index multis[a] on cell s.
+    const auto multis = generateMultiIndices(IndexRange(0, n), r);
+    if ((int)multis.size() != localdim) die("localdim mismatch");
+    out.pdim = n;
+    out.pos.assign(out.n * n, std::nan(""));
+    const auto& coords = M.getCoordinates();
+    for (const auto& e : I.getentries()) {
+        const int s = e.row / localdim, a = e.row % localdim;
+        const IndexMap verts = M.get_subsimplices(n, 0, s);
+        for (int d = 0; d < n; d++) {
+            double p = 0.0;
+            for (int v = 0; v <= n; v++) p += multis[a].at(v) * coords.getdata(verts.at(v), d);
+            out.pos[(int64_t)e.column * n + d] = p / r;
+        }
+    }
+    return out;
+}
+
+int main(int argc, char** argv) {
+    if (argc < 2) die("usage: see header");
+    const std::string cmd = argv[1];
+    if (cmd == "assemble") {
+        if (argc != 7) die("assemble <dim> <r> <L> <coef_seed> <out.csr>");
+        const int dim = std::atoi(argv[2]), r = std::atoi(argv[3]), L = std::atoi(argv[4]);
+        const uint64_t seed = std::strtoull(argv[5], nullptr, 10);
+        Csr m;
+        if (dim == 2) { auto M = UnitSquare2D_simple(); for (int l = 0; l < L; l++) M.uniformrefinement(); m = assemble_on(M, 2, r, L, seed); }
+        else if (dim == 3) { auto M = UnitCube3D(); for (int l = 0; l < L; l++) M.uniformrefinement(); m = assemble_on(M, 3, r, L, seed); }
+        else die("dim must be 2 or 3");
+        write_csr(argv[6], m);
+        std::printf("N=%lld nnz=%lld\n", (long long)m.n, (long long)m.nnz);
+        return 0;
+    }
+    if (cmd == "solve") {
+        if (argc != 9) die("solve <kind> <in.csr> <b.vec> <x0.vec> <precision> <omega> <out.sol>");
+        const std::string kind = argv[2];
+        Csr m = read_csr(argv[3]);
+        std::vector<double> b = read_vec(argv[4], m.n), x = read_vec(argv[5], m.n);
+        const double precision = std::atof(argv[6]), omega = std::atof(argv[7]);
+        std::vector<double> res(b);
+        MatrixCSR mat = to_matrix(m);
+        int K = -1;
+        double secs = 0.0;
+        if (kind == "cg") {
+            auto t0 = std::chrono::steady_clock::now();
+            K = ConjugateGradientSolverCSR((int)m.n, x.data(), b.data(), mat.getA(), mat.getC(), mat.getV(), res.data(), precision, -3);
+            secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        } else if (kind == "ssor") {
+            FloatVector diag = mat.getDiagonal();
+            auto t0 = std::chrono::steady_clock::now();
+            K = ConjugateGradientSolverCSR_SSOR((int)m.n, x.data(), b.data(), mat.getA(), mat.getC(), mat.getV(), res.data(), precision, -3, diag.raw(), omega);
+            secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        } else if (kind == "rainbow") {
+            FloatVector diag = mat.getDiagonal();
+            Rainbow rb(mat);
+            auto t0 = std::chrono::steady_clock::now();
+            K = ConjugateGradientSolverCSR_Rainbow((int)m.n, x.data(), b.data(), mat.getA(), mat.getC(), mat.getV(), res.data(), precision, -3, diag.raw(), omega,
+                                                   rb.num_colors, rb.F.data(), rb.B.data(), rb.R.data());
+            secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        } else die("unknown solver kind");
+        FILE* f = std::fopen(argv[8], "wb"); if (!f) die("cannot write sol");
+        int64_t hdr[2] = {m.n, K};
+        write_raw(f, hdr, 16); write_raw(f, &secs, 8);
+        write_raw(f, x.data(), 8 * m.n); write_raw(f, res.data(), 8 * m.n);
+        std::fclose(f);
+        std::printf("K=%d secs=%.6f\n", K, secs);
+        return 0;
+    }
+    if (cmd == "rainbow") {
+        if (argc != 4) die("rainbow <in.csr> <out.rb>");
+        Csr m = read_csr(argv[2]);
+        MatrixCSR mat = to_matrix(m);
+        auto t0 = std::chrono::steady_clock::now();
+        Rainbow rb(mat);
+        double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        FILE* f = std::fopen(argv[3], "wb"); if (!f) die("cannot write rb");
+        int64_t hdr[2] = {m.n, rb.num_colors};
+        write_raw(f, hdr, 16);
+        write_raw(f, rb.F.data(), 4 * m.n); write_raw(f, rb.B.data(), 4 * (rb.num_colors + 1)); write_raw(f, rb.R.data(), 4 * m.n);
+        std::fclose(f);
+        std::printf("colors=%d secs=%.6f\n", rb.num_colors, secs);
+        return 0;
+    }
+    if (cmd == "apply") {
+        if (argc != 6) die("apply <in.csr> <in.vec> <scaling> <out.vec>");
+        Csr m = read_csr(argv[2]);
+        MatrixCSR mat = to_matrix(m);
+        std::vector<double> src = read_vec(argv[3], m.ncols);
+        FloatVector s(std::vector<Float>(src.begin(), src.end())), d((int)m.n, 0.0);
+        mat.apply(d, s, std::atof(argv[4]));
+        FILE* f = std::fopen(argv[5], "wb"); if (!f) die("cannot write vec");
+        write_raw(f, d.raw(), 8 * m.n); std::fclose(f);
+        return 0;
+    }
+    if (cmd == "diag") {
+        if (argc != 4) die("diag <in.csr> <out.vec>");
+        Csr m = read_csr(argv[2]);
+        MatrixCSR mat = to_matrix(m);
+        FloatVector d = mat.getDiagonal();
+        FILE* f = std::fopen(argv[3], "wb"); if (!f) die("cannot write vec");
+        write_raw(f, d.raw(), 8 * m.n); std::fclose(f);
+        return 0;
+    }
+    die("unknown command");
+}
