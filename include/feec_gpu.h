@@ -1,0 +1,160 @@
+/*
+ * feec_gpu.h — C ABI of the GB300 sparse-CSR Krylov library (libfeec_gpu.so).
+ *
+ * Drop-in replacement for the CSR hot path of FEEC++ (martinlicht/simplefem):
+ * CSR SpMV, the CG drivers of solver/sparsesolver.hpp and the Rainbow greedy
+ * coloring of sparse/rainbow.hpp. Plain C types only: int32 CSR arrays
+ * (A = row pointers, C = column indices, V = values, as MatrixCSR stores them,
+ * sparse/matcsr.hpp:117-119) and double vectors.
+ *
+ * Every entry point returns a feec_status. The "host" entry points take host
+ * pointers (the reference's raw-pointer convention) and copy to and from the
+ * GPU inside the call; the feec_system_* entry points keep a matrix resident
+ * on the GPU and take device pointers.
+ */
+#ifndef FEEC_GPU_H
+#define FEEC_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum feec_status {
+    FEEC_OK = 0,             /* converged (reference stopping rule or requested rule)        */
+    FEEC_BREAKDOWN = 1,      /* non-finite or negative r.r / z.r / d.Ad (sparsesolver.cpp:148-151) */
+    FEEC_SMALL_ENERGY = 2,   /* sqrt|d.Ad| < machine epsilon (sparsesolver.cpp:153-157)       */
+    FEEC_MAXITER = 3,        /* iteration cap reached without meeting the tolerance            */
+    FEEC_TIMEOUT = 4,        /* a device-side wait gave up; the GPU context stays usable       */
+    FEEC_OOM = 5,            /* device allocation failed or the memory budget was exceeded     */
+    FEEC_BADARG = 6,         /* invalid argument (the reference asserts these)                 */
+    FEEC_CUDA_ERROR = 7,     /* a CUDA runtime call failed                                     */
+    FEEC_NO_DEVICE = 8       /* no usable GPU                                                  */
+} feec_status;
+
+/* Method selectors for feec_system_solve. */
+enum {
+    FEEC_METHOD_CG = 0,        /* ConjugateGradientSolverCSR          (sparsesolver.cpp:26-201)   */
+    FEEC_METHOD_SSOR = 1,      /* ConjugateGradientSolverCSR_SSOR     (sparsesolver.cpp:446-724)  */
+    FEEC_METHOD_RAINBOW = 2    /* ConjugateGradientSolverCSR_Rainbow  (sparsesolver.cpp:1002-1335) */
+};
+
+/* Arithmetic / stopping modes for feec_system_solve. */
+enum {
+    FEEC_MODE_REFERENCE = 0,   /* FP64, the reference's stopping rule: sqrt(r.r) (CG) or |z.r|
+                                  (PCG) below max(precision*||b||, 2^-26), cap N iterations  */
+    FEEC_MODE_FP64 = 1,        /* FP64, stop on the true relative residual ||b-Ax||/||b||
+                                  <= precision, no absolute floor                            */
+    FEEC_MODE_MIXED = 2        /* FP32 inner PCG with compensated dots inside an FP64
+                                  defect-correction loop; stop on the FP64 true relative
+                                  residual <= precision                                      */
+};
+
+typedef struct feec_solve_info {
+    int status;              /* feec_status of the solve                                   */
+    int iterations;          /* K as the reference returns it (inner iterations in MIXED)  */
+    int outer_iterations;    /* FP64 defect-correction steps (MIXED), else 1               */
+    int num_colors;          /* colors / levels used by the preconditioner sweeps          */
+    double tolerance;        /* max(precision*||b||, 2^-26) in REFERENCE mode, else precision */
+    double final_norm;       /* sqrt of the quantity the stopping rule tested               */
+    double true_relres;      /* ||b - A x|| / ||b|| in FP64 after the solve (-1 if skipped) */
+    double device_ms;        /* time of the solve on the device (CUDA events)              */
+    double total_ms;         /* wall time of the call including copies                     */
+    int grid_blocks;         /* persistent grid size used                                  */
+    int lanes_per_row;       /* CSR lanes per row used by the SpMV and sweeps              */
+} feec_solve_info;
+
+/* ---------------------------------------------------------------------------
+ * Drop-in entry points (host pointers). Arguments and return semantics follow
+ * solver/sparsesolver.hpp; the iteration count is returned in info->iterations.
+ * ------------------------------------------------------------------------- */
+
+/* Replaces ConjugateGradientSolverCSR, solver/sparsesolver.hpp:11-19 (sparsesolver.cpp:26-201). */
+int feec_cg_csr(int N, double* x, const double* b,
+                const int* A, const int* C, const double* V,
+                double* residual, double precision, int print_modulo,
+                feec_solve_info* info);
+
+/* Replaces ConjugateGradientSolverCSR_SSOR, solver/sparsesolver.hpp:33-43 (sparsesolver.cpp:446-724). */
+int feec_cg_csr_ssor(int N, double* x, const double* b,
+                     const int* A, const int* C, const double* V,
+                     double* residual, double precision, int print_modulo,
+                     const double* diagonal, double omega,
+                     feec_solve_info* info);
+
+/* Replaces ConjugateGradientSolverCSR_Rainbow, solver/sparsesolver.hpp:59-70 (sparsesolver.cpp:1002-1335). */
+int feec_cg_csr_rainbow(int N, double* x, const double* b,
+                        const int* A, const int* C, const double* V,
+                        double* residual, double precision, int print_modulo,
+                        const double* diagonal, double omega,
+                        int num_colors, const int* F, const int* B, const int* R,
+                        feec_solve_info* info);
+
+/* Replaces MatrixCSR::apply(dest, src, scaling), sparse/matcsr.cpp:216-244:
+ * dest = scaling * A * src (rows x cols matrix, host pointers). */
+int feec_csr_apply(int rows, int cols, const int* A, const int* C, const double* V,
+                   const double* src, double* dest, double scaling);
+
+/* Replaces MatrixCSR::getDiagonal, sparse/matcsr.cpp:266-286 (host pointers). */
+int feec_csr_diagonal(int N, const int* A, const int* C, const double* V, double* diagonal);
+
+/* Replaces Rainbow::Rainbow(mat, do_shuffle = false), sparse/rainbow.cpp:14-130.
+ * F[N], B[N+1] (num_colors+1 entries used), R[N], host pointers; bit-identical
+ * to the reference's greedy coloring. */
+int feec_rainbow(int N, const int* A, const int* C, int* num_colors, int* F, int* B, int* R);
+
+/* Replaces MatrixCSR::check's structural invariants, sparse/matcsr.cpp:178-194:
+ * FEEC_OK if A is non-decreasing from 0 to nnz, 0 <= C < cols and V finite. */
+int feec_csr_check(int rows, int cols, const int* A, const int* C, const double* V);
+
+/* ---------------------------------------------------------------------------
+ * Device-resident systems (device pointers, explicit stream).
+ * ------------------------------------------------------------------------- */
+
+typedef struct feec_system feec_system;
+
+/* Uploads (host_ptrs != 0) or adopts a copy of (host_ptrs == 0, device pointers)
+ * an N x N CSR matrix. `stream` is a cudaStream_t (NULL = the library stream). */
+int feec_system_create(feec_system** sys, int N, const int* A, const int* C, const double* V,
+                       int host_ptrs, void* stream);
+
+/* Prepares the multicolor SSOR layout from a Rainbow coloring (F, B, R as in
+ * sparse/rainbow.hpp:22-30) and the diagonal. Pointers are host pointers if
+ * host_ptrs != 0, else device pointers. */
+int feec_system_set_rainbow(feec_system* sys, const double* diagonal, double omega,
+                            int num_colors, const int* F, const int* B, const int* R, int host_ptrs);
+
+/* Prepares the lexicographic SSOR layout (level-scheduled triangular sweeps). */
+int feec_system_set_ssor(feec_system* sys, const double* diagonal, double omega, int host_ptrs);
+
+/* Solves A x = b on the device. x (in/out, initial guess), b and residual are
+ * device pointers of N doubles (residual may be NULL). max_iter <= 0 means N. */
+int feec_system_solve(feec_system* sys, int method, int mode, double* x, const double* b,
+                      double* residual, double precision, int max_iter,
+                      feec_solve_info* info, void* stream);
+
+/* y = scaling * A * x with device pointers. */
+int feec_system_apply(feec_system* sys, const double* x, double* y, double scaling, void* stream);
+
+/* Bytes of device memory held by the system. */
+int feec_system_memory(const feec_system* sys, size_t* bytes);
+
+int feec_system_destroy(feec_system* sys);
+
+/* ---------------------------------------------------------------------------
+ * Library information.
+ * ------------------------------------------------------------------------- */
+
+/* Number of kernels this library launched since load (all devices). */
+unsigned long long feec_kernel_launches(void);
+
+/* Human-readable name of a status code. */
+const char* feec_status_string(int status);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FEEC_GPU_H */

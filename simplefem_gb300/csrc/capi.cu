@@ -1,0 +1,784 @@
+// Host orchestration and the C ABI of libfeec_gpu.so (declared in include/feec_gpu.h).
+//
+// The drop-in entry points mirror solver/sparsesolver.hpp: they take the
+// caller's host arrays, build a device-resident system, run one persistent
+// cooperative solver launch and copy x and the residual back. The
+// feec_system_* entry points keep everything on the device between calls.
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <vector>
+
+#include "feec_device.cuh"
+#include "feec_internal.h"
+
+namespace feec {
+
+static std::atomic<unsigned long long> g_launches{0};
+void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
+int residual_blocks(int n, int lanes);
+cudaError_t launch_sum_f64(int n, const double* v, double* out, cudaStream_t s);
+
+static const double kDesiredPrecision = 1.490116119384765625e-08;  // base/base.hpp:127-128, sqrt(2^-52)
+
+namespace {
+
+struct DeviceCtx {
+    bool ready = false;
+    cudaStream_t stream = nullptr;
+    int sms = 0;
+};
+
+std::mutex g_ctx_mutex;
+DeviceCtx g_ctx[64];
+
+int init_device(int& dev, cudaStream_t& stream) {
+    if (cudaGetDevice(&dev) != cudaSuccess) return FEEC_NO_DEVICE;
+    if (dev < 0 || dev >= 64) return FEEC_NO_DEVICE;
+    std::lock_guard<std::mutex> lock(g_ctx_mutex);
+    DeviceCtx& c = g_ctx[dev];
+    if (!c.ready) {
+        if (cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking) != cudaSuccess) return FEEC_CUDA_ERROR;
+        cudaMemPool_t pool;
+        if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+            unsigned long long thr = ~0ull;
+            cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+        }
+        cudaDeviceGetAttribute(&c.sms, cudaDevAttrMultiProcessorCount, dev);
+        c.ready = true;
+    }
+    stream = c.stream;
+    return FEEC_OK;
+}
+
+int cuda_status(cudaError_t e) {
+    if (e == cudaSuccess) return FEEC_OK;
+    if (e == cudaErrorMemoryAllocation) return FEEC_OOM;
+    return FEEC_CUDA_ERROR;
+}
+
+// Stream-ordered device allocations owned by one object.
+struct DevArena {
+    std::vector<void*> ptrs;
+    size_t bytes = 0;
+    cudaStream_t stream = nullptr;
+    template <typename T>
+    cudaError_t alloc(T*& p, size_t count) {
+        p = nullptr;
+        if (count == 0) count = 1;
+        void* q = nullptr;
+        cudaError_t e = cudaMallocAsync(&q, count * sizeof(T), stream);
+        if (e != cudaSuccess) return e;
+        ptrs.push_back(q);
+        bytes += count * sizeof(T);
+        p = (T*)q;
+        return cudaSuccess;
+    }
+    void release() {
+        for (void* p : ptrs) cudaFreeAsync(p, stream);
+        ptrs.clear();
+        bytes = 0;
+    }
+};
+
+#define FEEC_TRY(expr)                                   \
+    do {                                                 \
+        cudaError_t _e = (expr);                         \
+        if (_e != cudaSuccess) return cuda_status(_e);   \
+    } while (0)
+
+double host_tolerance(int n, const double* b, double precision) {
+    // solver/sparsesolver.cpp:45-48, the same serial loop
+    double t = 0.0;
+    for (int i = 0; i < n; i++) t += b[i] * b[i];
+    t = precision * std::sqrt(t);
+    return std::max(t, kDesiredPrecision);
+}
+
+}  // namespace
+}  // namespace feec
+
+using namespace feec;
+
+struct feec_system {
+    int dev = 0;
+    int n = 0;
+    int nnz = 0;
+    cudaStream_t stream = nullptr;
+    DevArena mem;      // matrix + layouts
+    DevArena work;     // Krylov workspace
+    int* A = nullptr; int* C = nullptr; double* V = nullptr;   // original CSR
+    float* V32 = nullptr;                                        // FP32 copy for mixed CG
+    int lanes = 4;
+    // preconditioner layout (valid if prepared >= 0)
+    int prepared = -1;
+    int* perm = nullptr; int* iperm = nullptr;
+    int* rp = nullptr; int* ci = nullptr; double* val = nullptr; float* val32 = nullptr;
+    int* lsplit = nullptr; int* usplit = nullptr;
+    double* diag = nullptr; float* diag32 = nullptr;
+    int nf = 0; int* fptr = nullptr;
+    int nbw = 0; int* bptr = nullptr; int* brows = nullptr;
+    double omega = 1.0;
+    int num_levels = 0;
+    // workspace (FP64 permuted vectors + FP32 inner vectors)
+    bool work_ready = false;
+    double *x = nullptr, *r = nullptr, *d = nullptr, *z = nullptr, *m = nullptr, *q = nullptr, *b = nullptr;
+    float *x32 = nullptr, *r32 = nullptr, *d32 = nullptr, *z32 = nullptr, *m32 = nullptr, *q32 = nullptr, *b32 = nullptr;
+    double* partials = nullptr;
+    double* scal = nullptr;   // device scalars
+    DeviceStatus* st = nullptr;
+    int max_blocks = 0;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+};
+
+namespace {
+
+int ensure_work(feec_system* s) {
+    if (s->work_ready) return FEEC_OK;
+    s->work.stream = s->stream;
+    const size_t n = (size_t)s->n;
+    FEEC_TRY(s->work.alloc(s->x, n)); FEEC_TRY(s->work.alloc(s->r, n)); FEEC_TRY(s->work.alloc(s->d, n));
+    FEEC_TRY(s->work.alloc(s->z, n)); FEEC_TRY(s->work.alloc(s->m, n)); FEEC_TRY(s->work.alloc(s->q, n));
+    FEEC_TRY(s->work.alloc(s->b, n));
+    FEEC_TRY(s->work.alloc(s->x32, n)); FEEC_TRY(s->work.alloc(s->r32, n)); FEEC_TRY(s->work.alloc(s->d32, n));
+    FEEC_TRY(s->work.alloc(s->z32, n)); FEEC_TRY(s->work.alloc(s->m32, n)); FEEC_TRY(s->work.alloc(s->q32, n));
+    FEEC_TRY(s->work.alloc(s->b32, n));
+    // partial sums: up to 3 doubles per block of the largest co-resident grid, plus residual blocks
+    int dev_sms = 0;
+    cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, s->dev);
+    const size_t nblk = std::max<size_t>((size_t)dev_sms * 8, (size_t)residual_blocks(s->n, 32));
+    FEEC_TRY(s->work.alloc(s->partials, 3 * nblk + 64));
+    FEEC_TRY(s->work.alloc(s->scal, 16));
+    FEEC_TRY(s->work.alloc(s->st, 1));
+    if (!s->ev0) FEEC_TRY(cudaEventCreate(&s->ev0));
+    if (!s->ev1) FEEC_TRY(cudaEventCreate(&s->ev1));
+    s->work_ready = true;
+    return FEEC_OK;
+}
+
+int read_status(feec_system* s, DeviceStatus& hs) {
+    FEEC_TRY(cudaMemcpyAsync(&hs, s->st, sizeof(DeviceStatus), cudaMemcpyDeviceToHost, s->stream));
+    FEEC_TRY(cudaStreamSynchronize(s->stream));
+    return FEEC_OK;
+}
+
+cudaError_t reset_status(feec_system* s) {
+    return cudaMemsetAsync(s->st, 0, sizeof(DeviceStatus), s->stream);
+}
+
+// ||v||^2 on the device, deterministic, read back to the host.
+int device_norm2(feec_system* s, const double* v, double& out) {
+    FEEC_TRY(launch_sum_sq_f64(s->n, v, s->scal, s->stream));
+    FEEC_TRY(cudaMemcpyAsync(&out, s->scal, sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    FEEC_TRY(cudaStreamSynchronize(s->stream));
+    return FEEC_OK;
+}
+
+// r = b - A x (FP64, permuted layout if prepared else original CSR) and ||r||^2.
+int true_residual(feec_system* s, const double* bb, const double* xx, double* rr, double& norm2, bool permuted) {
+    const int* rp = permuted ? s->rp : s->A;
+    const int* ci = permuted ? s->ci : s->C;
+    const double* v = permuted ? s->val : s->V;
+    const int nb = residual_blocks(s->n, s->lanes);
+    FEEC_TRY(launch_residual_f64(s->n, rp, ci, v, bb, xx, rr, s->partials, s->lanes, s->stream));
+    FEEC_TRY(launch_sum_f64(nb, s->partials, s->scal, s->stream));
+    FEEC_TRY(cudaMemcpyAsync(&norm2, s->scal, sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    FEEC_TRY(cudaStreamSynchronize(s->stream));
+    return FEEC_OK;
+}
+
+template <typename T>
+PcgArgs<T> make_pcg_args(feec_system* s, T* x, T* r, T* d, T* z, T* m, T* q, const T* b, const T* val, const T* diag) {
+    PcgArgs<T> a{};
+    a.n = s->n; a.rp = s->rp; a.ci = s->ci; a.val = val; a.lsplit = s->lsplit; a.usplit = s->usplit;
+    a.diag = diag; a.b = b; a.x = x; a.r = r; a.d = d; a.z = z; a.m = m; a.q = q;
+    a.nf = s->nf; a.fptr = s->fptr; a.nbw = s->nbw; a.bptr = s->bptr; a.brows = s->brows;
+    a.omega = s->omega; a.partials = s->partials; a.st = s->st;
+    return a;
+}
+
+int timed_launch_pcg64(feec_system* s, const PcgArgs<double>& a, LaunchShape& shape, float& ms) {
+    FEEC_TRY(reset_status(s));
+    FEEC_TRY(cudaEventRecord(s->ev0, s->stream));
+    FEEC_TRY(launch_pcg<double>(a, shape, s->stream));
+    FEEC_TRY(cudaEventRecord(s->ev1, s->stream));
+    FEEC_TRY(cudaEventSynchronize(s->ev1));
+    FEEC_TRY(cudaEventElapsedTime(&ms, s->ev0, s->ev1));
+    return FEEC_OK;
+}
+
+void zero_info(feec_solve_info* info) {
+    if (!info) return;
+    std::memset(info, 0, sizeof(*info));
+    info->true_relres = -1.0;
+    info->outer_iterations = 1;
+}
+
+const char* method_title(int method) {
+    switch (method) {
+        case FEEC_METHOD_SSOR: return "Conjugate Gradient CSR (SSOR)";
+        case FEEC_METHOD_RAINBOW: return "Conjugate Gradient CSR (SSOR-Rainbow)";
+        default: return "Conjugate Gradient CSR";
+    }
+}
+
+// Core solve on a prepared system. xx / bb / res: device arrays in the ORIGINAL numbering.
+// tol_override > 0 replaces the tolerance of REFERENCE mode (the drop-in computes it on the host
+// with the reference's own serial loop).
+int solve_core(feec_system* s, int method, int mode, double* xx, const double* bb, double* res, double precision,
+               int max_iter, double tol_override, int print_modulo, feec_solve_info* info) {
+    const int n = s->n;
+    if (method != FEEC_METHOD_CG && s->prepared != method) return FEEC_BADARG;
+    int st = ensure_work(s);
+    if (st != FEEC_OK) return st;
+    if (max_iter <= 0) max_iter = n;
+    const bool permuted = method != FEEC_METHOD_CG;
+    const int* perm = permuted ? s->perm : nullptr;
+
+    // bring b, x (and the caller's residual for rows the sweeps skip) into solver order
+    FEEC_TRY(launch_gather_f64(n, perm, bb, s->b, s->stream));
+    FEEC_TRY(launch_gather_f64(n, perm, xx, s->x, s->stream));
+    if (res) FEEC_TRY(launch_gather_f64(n, perm, res, s->r, s->stream));
+    else FEEC_TRY(cudaMemsetAsync(s->r, 0, sizeof(double) * n, s->stream));
+
+    double bnorm2 = 0.0;
+    st = device_norm2(s, s->b, bnorm2);
+    if (st != FEEC_OK) return st;
+    const double bnorm = std::sqrt(bnorm2);
+    double tolerance = tol_override > 0.0 ? tol_override : std::max(precision * bnorm, kDesiredPrecision);
+    if (mode != FEEC_MODE_REFERENCE) tolerance = precision * bnorm;
+
+    LaunchShape shape;
+    shape.lanes = s->lanes;
+    float ms_total = 0.0f;
+    int K_total = 0, outer = 0, status = FEEC_OK;
+    double final_norm = 0.0;
+    DeviceStatus hs{};
+
+    if (mode == FEEC_MODE_REFERENCE || mode == FEEC_MODE_FP64) {
+        // FP64 mode: run with the recursive-residual rule, then confirm on the true residual and
+        // restart from the current iterate if the recursion drifted (at most a few times).
+        const int max_restarts = (mode == FEEC_MODE_FP64) ? 4 : 1;
+        for (int attempt = 0; attempt < max_restarts; attempt++) {
+            FEEC_TRY(cudaMemsetAsync(s->d, 0, sizeof(double) * n, s->stream));
+            FEEC_TRY(cudaMemsetAsync(s->z, 0, sizeof(double) * n, s->stream));
+            FEEC_TRY(cudaMemsetAsync(s->m, 0, sizeof(double) * n, s->stream));
+            FEEC_TRY(cudaMemsetAsync(s->q, 0, sizeof(double) * n, s->stream));
+            float ms = 0.0f;
+            if (method == FEEC_METHOD_CG) {
+                CgArgs<double> a{};
+                a.n = n; a.rp = s->A; a.ci = s->C; a.val = s->V; a.b = s->b; a.x = s->x; a.r = s->r; a.d = s->d; a.q = s->q;
+                a.tol2 = tolerance * tolerance;
+                a.max_iter = max_iter - K_total;
+                a.print_modulo = print_modulo; a.print_tol = tolerance;
+                a.partials = s->partials; a.st = s->st;
+                FEEC_TRY(reset_status(s));
+                FEEC_TRY(cudaEventRecord(s->ev0, s->stream));
+                FEEC_TRY(launch_cg<double>(a, shape, s->stream));
+                FEEC_TRY(cudaEventRecord(s->ev1, s->stream));
+                FEEC_TRY(cudaEventSynchronize(s->ev1));
+                FEEC_TRY(cudaEventElapsedTime(&ms, s->ev0, s->ev1));
+            } else {
+                PcgArgs<double> a = make_pcg_args<double>(s, s->x, s->r, s->d, s->z, s->m, s->q, s->b, s->val, s->diag);
+                a.tol2 = tolerance * tolerance;
+                a.use_zr_rule = (mode == FEEC_MODE_REFERENCE) ? 1 : 0;
+                a.rr_stop = (mode == FEEC_MODE_FP64) ? tolerance * tolerance : 0.0;
+                a.max_iter = max_iter - K_total;
+                a.print_modulo = print_modulo; a.print_tol = tolerance;
+                st = timed_launch_pcg64(s, a, shape, ms);
+                if (st != FEEC_OK) return st;
+            }
+            ms_total += ms;
+            st = read_status(s, hs);
+            if (st != FEEC_OK) return st;
+            K_total += hs.iterations;
+            status = hs.status;
+            final_norm = std::sqrt(std::fabs(hs.final_value));
+            outer++;
+            if (mode == FEEC_MODE_REFERENCE || status != FEEC_OK) break;
+            double rn2 = 0.0;
+            st = true_residual(s, s->b, s->x, s->d, rn2, permuted);
+            if (st != FEEC_OK) return st;
+            if (std::sqrt(rn2) <= tolerance) break;
+            if (K_total >= max_iter) { status = FEEC_MAXITER; break; }
+        }
+    } else {
+        // MIXED: FP64 defect correction around an FP32 inner solve (compensated FP32 dots).
+        if (method == FEEC_METHOD_CG && !s->V32) return FEEC_BADARG;
+        if (method != FEEC_METHOD_CG && !s->val32) return FEEC_BADARG;
+        const double inner_eta = 2e-5;   // relative reduction asked of one inner solve
+        const int max_outer = 12;
+        double rn2 = 0.0;
+        for (outer = 0; outer < max_outer; outer++) {
+            st = true_residual(s, s->b, s->x, s->r, rn2, permuted);
+            if (st != FEEC_OK) return st;
+            const double rn = std::sqrt(rn2);
+            final_norm = rn;
+            if (!(rn == rn)) { status = FEEC_BREAKDOWN; break; }
+            if (rn <= tolerance) { status = FEEC_OK; break; }
+            if (K_total >= max_iter) { status = FEEC_MAXITER; break; }
+            const double inv = 1.0 / rn;
+            const double scal_h[2] = {inv, rn};
+            FEEC_TRY(cudaMemcpyAsync(s->scal + 2, scal_h, sizeof(scal_h), cudaMemcpyHostToDevice, s->stream));
+            FEEC_TRY(launch_scaled_cast(n, s->r, s->scal + 2, s->b32, s->stream));
+            FEEC_TRY(cudaMemsetAsync(s->x32, 0, sizeof(float) * n, s->stream));
+            FEEC_TRY(cudaMemsetAsync(s->d32, 0, sizeof(float) * n, s->stream));
+            FEEC_TRY(cudaMemsetAsync(s->z32, 0, sizeof(float) * n, s->stream));
+            FEEC_TRY(cudaMemsetAsync(s->m32, 0, sizeof(float) * n, s->stream));
+            FEEC_TRY(cudaMemsetAsync(s->q32, 0, sizeof(float) * n, s->stream));
+            FEEC_TRY(cudaMemsetAsync(s->r32, 0, sizeof(float) * n, s->stream));
+            // do not over-solve the last step: ask only for the reduction still needed (with margin)
+            const double need = 0.3 * tolerance / rn;
+            const double eta = std::max(inner_eta, need);
+            float ms = 0.0f;
+            FEEC_TRY(reset_status(s));
+            FEEC_TRY(cudaEventRecord(s->ev0, s->stream));
+            if (method == FEEC_METHOD_CG) {
+                CgArgs<float> a{};
+                a.n = n; a.rp = s->A; a.ci = s->C; a.val = s->V32; a.b = s->b32; a.x = s->x32; a.r = s->r32;
+                a.d = s->d32; a.q = s->q32;
+                a.tol2 = eta * eta;
+                a.max_iter = max_iter - K_total;
+                a.partials = s->partials; a.st = s->st;
+                FEEC_TRY(launch_cg<float>(a, shape, s->stream));
+            } else {
+                PcgArgs<float> a = make_pcg_args<float>(s, s->x32, s->r32, s->d32, s->z32, s->m32, s->q32, s->b32,
+                                                        s->val32, s->diag32);
+                a.use_zr_rule = 0;
+                a.rr_stop = eta * eta;
+                a.max_iter = max_iter - K_total;
+                FEEC_TRY(launch_pcg<float>(a, shape, s->stream));
+            }
+            FEEC_TRY(cudaEventRecord(s->ev1, s->stream));
+            FEEC_TRY(launch_update_x(n, nullptr, s->x32, s->scal + 3, s->x, s->stream));
+            FEEC_TRY(cudaEventSynchronize(s->ev1));
+            FEEC_TRY(cudaEventElapsedTime(&ms, s->ev0, s->ev1));
+            ms_total += ms;
+            st = read_status(s, hs);
+            if (st != FEEC_OK) return st;
+            K_total += hs.iterations;
+            if (hs.status == FEEC_TIMEOUT) { status = FEEC_TIMEOUT; break; }
+            if (hs.status == FEEC_BREAKDOWN && hs.iterations == 0) { status = FEEC_BREAKDOWN; break; }
+        }
+        if (outer == max_outer) status = FEEC_MAXITER;
+        // leave the FP64 recursive residual array holding the true residual
+        double rn2b = 0.0;
+        st = true_residual(s, s->b, s->x, s->r, rn2b, permuted);
+        if (st != FEEC_OK) return st;
+        final_norm = std::sqrt(rn2b);
+        if (status == FEEC_OK && final_norm > tolerance) status = FEEC_MAXITER;
+    }
+
+    // results back to the caller's numbering
+    FEEC_TRY(launch_scatter_f64(n, perm, s->x, xx, s->stream));
+    if (res) FEEC_TRY(launch_scatter_f64(n, perm, s->r, res, s->stream));
+
+    if (info) {
+        info->status = status;
+        info->iterations = K_total;
+        info->outer_iterations = outer;
+        info->num_colors = method == FEEC_METHOD_CG ? 0 : s->num_levels;
+        info->tolerance = (mode == FEEC_MODE_REFERENCE) ? tolerance : precision;
+        info->final_norm = final_norm;
+        info->device_ms = ms_total;
+        info->grid_blocks = shape.blocks;
+        info->lanes_per_row = shape.lanes;
+        if (mode != FEEC_MODE_REFERENCE) {
+            double rn2 = 0.0;
+            st = true_residual(s, s->b, s->x, s->d, rn2, permuted);
+            if (st != FEEC_OK) return st;
+            info->true_relres = bnorm > 0 ? std::sqrt(rn2) / bnorm : 0.0;
+        }
+    }
+    FEEC_TRY(cudaStreamSynchronize(s->stream));
+    return status;
+}
+
+int build_layout(feec_system* s, int method, const double* diag_dev, double omega, const int* perm_host,
+                 const int* key_dev, const std::vector<int>& fptr, const std::vector<int>& bptr,
+                 const std::vector<int>& brows, int num_levels) {
+    const int n = s->n;
+    cudaStream_t st = s->stream;
+    DevArena& M = s->mem;
+    if (!s->perm) {
+        FEEC_TRY(M.alloc(s->perm, n)); FEEC_TRY(M.alloc(s->iperm, n));
+        FEEC_TRY(M.alloc(s->rp, (size_t)n + 1)); FEEC_TRY(M.alloc(s->ci, (size_t)s->nnz));
+        FEEC_TRY(M.alloc(s->val, (size_t)s->nnz)); FEEC_TRY(M.alloc(s->val32, (size_t)s->nnz));
+        FEEC_TRY(M.alloc(s->lsplit, n)); FEEC_TRY(M.alloc(s->usplit, n));
+        FEEC_TRY(M.alloc(s->diag, n)); FEEC_TRY(M.alloc(s->diag32, n));
+    }
+    // schedules (small, reallocated per preparation)
+    FEEC_TRY(M.alloc(s->fptr, fptr.size())); FEEC_TRY(M.alloc(s->bptr, bptr.size())); FEEC_TRY(M.alloc(s->brows, brows.size()));
+    FEEC_TRY(cudaMemcpyAsync(s->perm, perm_host, sizeof(int) * n, cudaMemcpyHostToDevice, st));
+    FEEC_TRY(cudaMemcpyAsync(s->fptr, fptr.data(), sizeof(int) * fptr.size(), cudaMemcpyHostToDevice, st));
+    FEEC_TRY(cudaMemcpyAsync(s->bptr, bptr.data(), sizeof(int) * bptr.size(), cudaMemcpyHostToDevice, st));
+    FEEC_TRY(cudaMemcpyAsync(s->brows, brows.data(), sizeof(int) * brows.size(), cudaMemcpyHostToDevice, st));
+    FEEC_TRY(launch_inverse_perm(n, s->perm, s->iperm, st));
+    int *len = nullptr, *scratch = nullptr;
+    DevArena tmp; tmp.stream = st;
+    FEEC_TRY(tmp.alloc(len, (size_t)n + 1));
+    FEEC_TRY(tmp.alloc(scratch, scan_scratch_ints(n + 1)));
+    FEEC_TRY(cudaMemsetAsync(len + n, 0, sizeof(int), st));
+    FEEC_TRY(launch_row_lengths(n, s->A, s->perm, len, st));
+    FEEC_TRY(launch_exclusive_scan(n + 1, len, s->rp, scratch, st));
+    FEEC_TRY(launch_permute_split(n, s->A, s->C, s->V, s->perm, s->iperm, key_dev, s->rp, s->ci, s->val, s->val32,
+                                  s->lsplit, s->usplit, st));
+    FEEC_TRY(launch_gather_f64(n, s->perm, diag_dev, s->diag, st));
+    FEEC_TRY(launch_cast_f64_f32((size_t)n, s->diag, s->diag32, st));
+    tmp.release();
+    FEEC_TRY(cudaStreamSynchronize(st));
+    s->nf = (int)fptr.size() - 1;
+    s->nbw = (int)bptr.size() - 1;
+    s->omega = omega;
+    s->num_levels = num_levels;
+    s->prepared = method;
+    return FEEC_OK;
+}
+
+int copy_in_ints(feec_system* s, const int* src, int count, int host_ptrs, std::vector<int>& out) {
+    out.resize((size_t)count);
+    if (count == 0) return FEEC_OK;
+    FEEC_TRY(cudaMemcpyAsync(out.data(), src, sizeof(int) * count, host_ptrs ? cudaMemcpyHostToHost : cudaMemcpyDeviceToHost, s->stream));
+    FEEC_TRY(cudaStreamSynchronize(s->stream));
+    return FEEC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* feec_status_string(int status) {
+    switch (status) {
+        case FEEC_OK: return "ok";
+        case FEEC_BREAKDOWN: return "breakdown";
+        case FEEC_SMALL_ENERGY: return "small gradient energy";
+        case FEEC_MAXITER: return "iteration limit";
+        case FEEC_TIMEOUT: return "device wait timed out";
+        case FEEC_OOM: return "out of device memory";
+        case FEEC_BADARG: return "bad argument";
+        case FEEC_CUDA_ERROR: return "CUDA error";
+        case FEEC_NO_DEVICE: return "no device";
+        default: return "unknown";
+    }
+}
+
+unsigned long long feec_kernel_launches(void) { return g_launches.load(); }
+
+int feec_system_create(feec_system** out, int N, const int* A, const int* C, const double* V, int host_ptrs, void* stream) {
+    if (!out || N <= 0 || !A || !C || !V) return FEEC_BADARG;
+    *out = nullptr;
+    int dev = 0;
+    cudaStream_t lib_stream = nullptr;
+    int st = init_device(dev, lib_stream);
+    if (st != FEEC_OK) return st;
+    feec_system* s = new (std::nothrow) feec_system();
+    if (!s) return FEEC_OOM;
+    s->dev = dev;
+    s->n = N;
+    s->stream = stream ? (cudaStream_t)stream : lib_stream;
+    s->mem.stream = s->stream;
+    s->work.stream = s->stream;
+    int nnz = 0;
+    cudaError_t e = cudaMemcpyAsync(&nnz, A + N, sizeof(int), host_ptrs ? cudaMemcpyHostToHost : cudaMemcpyDeviceToHost, s->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    if (e != cudaSuccess || nnz < 0) { delete s; return e != cudaSuccess ? cuda_status(e) : FEEC_BADARG; }
+    s->nnz = nnz;
+    const cudaMemcpyKind kind = host_ptrs ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
+    if ((e = s->mem.alloc(s->A, (size_t)N + 1)) != cudaSuccess ||
+        (e = s->mem.alloc(s->C, (size_t)nnz)) != cudaSuccess ||
+        (e = s->mem.alloc(s->V, (size_t)nnz)) != cudaSuccess ||
+        (e = s->mem.alloc(s->V32, (size_t)nnz)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(s->A, A, sizeof(int) * ((size_t)N + 1), kind, s->stream)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(s->C, C, sizeof(int) * (size_t)nnz, kind, s->stream)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(s->V, V, sizeof(double) * (size_t)nnz, kind, s->stream)) != cudaSuccess ||
+        (e = launch_cast_f64_f32((size_t)nnz, s->V, s->V32, s->stream)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(s->stream)) != cudaSuccess) {
+        s->mem.release();
+        cudaStreamSynchronize(s->stream);
+        delete s;
+        return cuda_status(e);
+    }
+    // every column index and row pointer is checked before any kernel indexes through them
+    int* bad_d = nullptr;
+    int bad = 0;
+    if ((e = s->mem.alloc(bad_d, 1)) != cudaSuccess || (e = cudaMemsetAsync(bad_d, 0, sizeof(int), s->stream)) != cudaSuccess ||
+        (e = launch_validate_csr(N, nnz, s->A, s->C, bad_d, s->stream)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(&bad, bad_d, sizeof(int), cudaMemcpyDeviceToHost, s->stream)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(s->stream)) != cudaSuccess || bad) {
+        s->mem.release();
+        cudaStreamSynchronize(s->stream);
+        delete s;
+        return e != cudaSuccess ? cuda_status(e) : FEEC_BADARG;
+    }
+    s->lanes = pick_lanes((double)nnz / (double)N);
+    *out = s;
+    return FEEC_OK;
+}
+
+int feec_system_destroy(feec_system* s) {
+    if (!s) return FEEC_OK;
+    s->work.release();
+    s->mem.release();
+    cudaStreamSynchronize(s->stream);
+    if (s->ev0) cudaEventDestroy(s->ev0);
+    if (s->ev1) cudaEventDestroy(s->ev1);
+    delete s;
+    return FEEC_OK;
+}
+
+int feec_system_memory(const feec_system* s, size_t* bytes) {
+    if (!s || !bytes) return FEEC_BADARG;
+    *bytes = s->mem.bytes + s->work.bytes;
+    return FEEC_OK;
+}
+
+int feec_system_set_rainbow(feec_system* s, const double* diagonal, double omega, int num_colors, const int* F,
+                            const int* B, const int* R, int host_ptrs) {
+    if (!s || !diagonal || !F || !B || !R || num_colors < 0 || !(omega > 0.0) || !(omega < 2.0)) return FEEC_BADARG;
+    const int n = s->n;
+    std::vector<int> hB, hR;
+    int st = copy_in_ints(s, B, num_colors + 1, host_ptrs, hB);
+    if (st != FEEC_OK) return st;
+    st = copy_in_ints(s, R, n, host_ptrs, hR);
+    if (st != FEEC_OK) return st;
+    if (hB[0] != 0 || hB[num_colors] != n) return FEEC_BADARG;
+    for (int c = 0; c < num_colors; c++) if (hB[c + 1] < hB[c]) return FEEC_BADARG;
+    std::vector<char> seen((size_t)n, 0);
+    for (int i = 0; i < n; i++) {
+        if (hR[i] < 0 || hR[i] >= n || seen[hR[i]]) return FEEC_BADARG;
+        seen[hR[i]] = 1;
+    }
+    // forward phases: colors ascending (rows are renumbered color by color, so ranges are contiguous);
+    // backward phases: colors descending
+    std::vector<int> fptr(hB.begin(), hB.end());
+    std::vector<int> bptr(1, 0), brows;
+    brows.reserve(n);
+    for (int c = num_colors - 1; c >= 0; c--) {
+        for (int i = hB[c]; i < hB[c + 1]; i++) brows.push_back(i);
+        bptr.push_back((int)brows.size());
+    }
+    DevArena tmp; tmp.stream = s->stream;
+    int* Fd = nullptr; double* Dd = nullptr;
+    FEEC_TRY(tmp.alloc(Fd, n)); FEEC_TRY(tmp.alloc(Dd, n));
+    const cudaMemcpyKind kind = host_ptrs ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
+    FEEC_TRY(cudaMemcpyAsync(Fd, F, sizeof(int) * n, kind, s->stream));
+    FEEC_TRY(cudaMemcpyAsync(Dd, diagonal, sizeof(double) * n, kind, s->stream));
+    st = build_layout(s, FEEC_METHOD_RAINBOW, Dd, omega, hR.data(), Fd, fptr, bptr, brows, num_colors);
+    tmp.release();
+    cudaStreamSynchronize(s->stream);
+    return st;
+}
+
+int feec_system_set_ssor(feec_system* s, const double* diagonal, double omega, int host_ptrs) {
+    if (!s || !diagonal || !(omega > 0.0) || !(omega < 2.0)) return FEEC_BADARG;
+    const int n = s->n;
+    std::vector<int> hA, hC;
+    int st = FEEC_OK;
+    // the level computation needs the pattern on the host
+    hA.resize((size_t)n + 1); hC.resize((size_t)s->nnz);
+    FEEC_TRY(cudaMemcpyAsync(hA.data(), s->A, sizeof(int) * (n + 1), cudaMemcpyDeviceToHost, s->stream));
+    FEEC_TRY(cudaMemcpyAsync(hC.data(), s->C, sizeof(int) * (size_t)s->nnz, cudaMemcpyDeviceToHost, s->stream));
+    FEEC_TRY(cudaStreamSynchronize(s->stream));
+    std::vector<int> flev, blev;
+    int nfl = 0, nbl = 0;
+    triangular_levels(n, hA.data(), hC.data(), true, flev, nfl);
+    triangular_levels(n, hA.data(), hC.data(), false, blev, nbl);
+    // rows renumbered by forward level (stable), backward schedule listed in the new numbering
+    std::vector<int> fcount((size_t)nfl + 1, 0), perm((size_t)n), iperm((size_t)n);
+    for (int i = 0; i < n; i++) fcount[flev[i] + 1]++;
+    for (int l = 0; l < nfl; l++) fcount[l + 1] += fcount[l];
+    std::vector<int> fptr(fcount.begin(), fcount.end());
+    for (int i = 0; i < n; i++) { const int p = fcount[flev[i]]++; perm[p] = i; iperm[i] = p; }
+    std::vector<int> bcount((size_t)nbl + 1, 0), brows((size_t)n);
+    for (int i = 0; i < n; i++) bcount[blev[i] + 1]++;
+    for (int l = 0; l < nbl; l++) bcount[l + 1] += bcount[l];
+    std::vector<int> bptr(bcount.begin(), bcount.end());
+    for (int i = n - 1; i >= 0; i--) brows[bcount[blev[i]]++] = iperm[i];
+    DevArena tmp; tmp.stream = s->stream;
+    double* Dd = nullptr;
+    FEEC_TRY(tmp.alloc(Dd, n));
+    FEEC_TRY(cudaMemcpyAsync(Dd, diagonal, sizeof(double) * n, host_ptrs ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, s->stream));
+    st = build_layout(s, FEEC_METHOD_SSOR, Dd, omega, perm.data(), nullptr, fptr, bptr, brows, nfl);
+    tmp.release();
+    cudaStreamSynchronize(s->stream);
+    return st;
+}
+
+int feec_system_solve(feec_system* s, int method, int mode, double* x, const double* b, double* residual,
+                      double precision, int max_iter, feec_solve_info* info, void* stream) {
+    zero_info(info);
+    if (!s || !x || !b || !(precision > 0.0)) return FEEC_BADARG;
+    if (method < FEEC_METHOD_CG || method > FEEC_METHOD_RAINBOW || mode < FEEC_MODE_REFERENCE || mode > FEEC_MODE_MIXED)
+        return FEEC_BADARG;
+    cudaStream_t keep = s->stream;
+    if (stream) { s->stream = (cudaStream_t)stream; s->work.stream = s->stream; }
+    const auto t0 = std::chrono::steady_clock::now();
+    int st = solve_core(s, method, mode, x, b, residual, precision, max_iter, 0.0, -3, info);
+    if (info) info->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    s->stream = keep; s->work.stream = keep;
+    return st;
+}
+
+int feec_system_apply(feec_system* s, const double* x, double* y, double scaling, void* stream) {
+    if (!s || !x || !y) return FEEC_BADARG;
+    cudaStream_t st = stream ? (cudaStream_t)stream : s->stream;
+    FEEC_TRY(launch_spmv_f64(s->n, s->A, s->C, s->V, x, y, scaling, s->lanes, st));
+    return FEEC_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Drop-in host-pointer entry points
+// ---------------------------------------------------------------------------
+
+static int dropin_solve(int method, int N, double* x, const double* b, const int* A, const int* C, const double* V,
+                        double* residual, double precision, int print_modulo, const double* diagonal, double omega,
+                        int num_colors, const int* F, const int* B, const int* R, feec_solve_info* info) {
+    zero_info(info);
+    // the reference asserts these (sparsesolver.cpp:32-43, 1013-1027)
+    if (N <= 0 || !x || !b || !A || !C || !V || !residual || !(precision > 0.0)) return FEEC_BADARG;
+    if (method != FEEC_METHOD_CG && !diagonal) return FEEC_BADARG;
+    if (method == FEEC_METHOD_RAINBOW && (num_colors < 0 || !F || !B || !R)) return FEEC_BADARG;
+    const auto t0 = std::chrono::steady_clock::now();
+    const double tolerance = host_tolerance(N, b, precision);
+    if (print_modulo >= -1) std::printf("(%d/%d)     BEGIN: %s\n", 0, N, method_title(method));
+
+    feec_system* s = nullptr;
+    int st = feec_system_create(&s, N, A, C, V, 1, nullptr);
+    if (st != FEEC_OK) return st;
+    if (method == FEEC_METHOD_RAINBOW) st = feec_system_set_rainbow(s, diagonal, omega, num_colors, F, B, R, 1);
+    else if (method == FEEC_METHOD_SSOR) st = feec_system_set_ssor(s, diagonal, omega, 1);
+    double *dx = nullptr, *db = nullptr, *dr = nullptr;
+    DevArena io; io.stream = s->stream;
+    if (st == FEEC_OK) {
+        cudaError_t e;
+        if ((e = io.alloc(dx, N)) != cudaSuccess || (e = io.alloc(db, N)) != cudaSuccess || (e = io.alloc(dr, N)) != cudaSuccess ||
+            (e = cudaMemcpyAsync(dx, x, sizeof(double) * N, cudaMemcpyHostToDevice, s->stream)) != cudaSuccess ||
+            (e = cudaMemcpyAsync(db, b, sizeof(double) * N, cudaMemcpyHostToDevice, s->stream)) != cudaSuccess ||
+            (e = cudaMemcpyAsync(dr, residual, sizeof(double) * N, cudaMemcpyHostToDevice, s->stream)) != cudaSuccess)
+            st = cuda_status(e);
+    }
+    feec_solve_info local;
+    feec_solve_info* inf = info ? info : &local;
+    zero_info(inf);
+    if (st == FEEC_OK) st = solve_core(s, method, FEEC_MODE_REFERENCE, dx, db, dr, precision, N, tolerance, print_modulo, inf);
+    const bool solved = st == FEEC_OK || st == FEEC_BREAKDOWN || st == FEEC_SMALL_ENERGY || st == FEEC_MAXITER;
+    if (solved) {
+        cudaError_t e = cudaMemcpyAsync(x, dx, sizeof(double) * N, cudaMemcpyDeviceToHost, s->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(residual, dr, sizeof(double) * N, cudaMemcpyDeviceToHost, s->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+        if (e != cudaSuccess) st = cuda_status(e);
+    }
+    io.release();
+    feec_system_destroy(s);
+    inf->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    inf->tolerance = tolerance;
+    if (solved && print_modulo >= -2) {
+        if (st == FEEC_BREAKDOWN)
+            std::printf("(%d/%d) BREAKDOWN: Gradient energy is unreasonable\n", inf->iterations, N);
+        else if (st == FEEC_SMALL_ENERGY)
+            std::printf("(%d/%d)   WARNING: Gradient energy is small\n", inf->iterations, N);
+    }
+    if (solved && print_modulo >= -1)
+        std::printf("(%d/%d) %9s: Residual norm is %.9le < %.9le\n", inf->iterations, N,
+                    inf->final_norm < tolerance ? "SUCCESS" : "FAILED", inf->final_norm, tolerance);
+    return st;
+}
+
+int feec_cg_csr(int N, double* x, const double* b, const int* A, const int* C, const double* V, double* residual,
+                double precision, int print_modulo, feec_solve_info* info) {
+    return dropin_solve(FEEC_METHOD_CG, N, x, b, A, C, V, residual, precision, print_modulo, nullptr, 1.0, 0, nullptr,
+                        nullptr, nullptr, info);
+}
+
+int feec_cg_csr_ssor(int N, double* x, const double* b, const int* A, const int* C, const double* V, double* residual,
+                     double precision, int print_modulo, const double* diagonal, double omega, feec_solve_info* info) {
+    return dropin_solve(FEEC_METHOD_SSOR, N, x, b, A, C, V, residual, precision, print_modulo, diagonal, omega, 0,
+                        nullptr, nullptr, nullptr, info);
+}
+
+int feec_cg_csr_rainbow(int N, double* x, const double* b, const int* A, const int* C, const double* V,
+                        double* residual, double precision, int print_modulo, const double* diagonal, double omega,
+                        int num_colors, const int* F, const int* B, const int* R, feec_solve_info* info) {
+    return dropin_solve(FEEC_METHOD_RAINBOW, N, x, b, A, C, V, residual, precision, print_modulo, diagonal, omega,
+                        num_colors, F, B, R, info);
+}
+
+int feec_csr_apply(int rows, int cols, const int* A, const int* C, const double* V, const double* src, double* dest,
+                   double scaling) {
+    if (rows < 0 || cols < 0 || !A || (rows > 0 && (!dest)) || (cols > 0 && !src)) return FEEC_BADARG;
+    if (rows == 0) return FEEC_OK;
+    const int nnz = A[rows];
+    if (nnz < 0 || (nnz > 0 && (!C || !V))) return FEEC_BADARG;
+    int dev = 0;
+    cudaStream_t s = nullptr;
+    int st = init_device(dev, s);
+    if (st != FEEC_OK) return st;
+    DevArena m; m.stream = s;
+    int *dA = nullptr, *dC = nullptr; double *dV = nullptr, *dx = nullptr, *dy = nullptr;
+    cudaError_t e;
+    if ((e = m.alloc(dA, (size_t)rows + 1)) == cudaSuccess && (e = m.alloc(dC, (size_t)nnz)) == cudaSuccess &&
+        (e = m.alloc(dV, (size_t)nnz)) == cudaSuccess && (e = m.alloc(dx, (size_t)cols)) == cudaSuccess &&
+        (e = m.alloc(dy, (size_t)rows)) == cudaSuccess &&
+        (e = cudaMemcpyAsync(dA, A, sizeof(int) * ((size_t)rows + 1), cudaMemcpyHostToDevice, s)) == cudaSuccess &&
+        (nnz == 0 || (e = cudaMemcpyAsync(dC, C, sizeof(int) * (size_t)nnz, cudaMemcpyHostToDevice, s)) == cudaSuccess) &&
+        (nnz == 0 || (e = cudaMemcpyAsync(dV, V, sizeof(double) * (size_t)nnz, cudaMemcpyHostToDevice, s)) == cudaSuccess) &&
+        (cols == 0 || (e = cudaMemcpyAsync(dx, src, sizeof(double) * (size_t)cols, cudaMemcpyHostToDevice, s)) == cudaSuccess) &&
+        (e = launch_spmv_f64(rows, dA, dC, dV, dx, dy, scaling, pick_lanes((double)nnz / rows), s)) == cudaSuccess &&
+        (e = cudaMemcpyAsync(dest, dy, sizeof(double) * (size_t)rows, cudaMemcpyDeviceToHost, s)) == cudaSuccess) {
+        e = cudaStreamSynchronize(s);
+    }
+    m.release();
+    cudaStreamSynchronize(s);
+    return cuda_status(e);
+}
+
+int feec_csr_diagonal(int N, const int* A, const int* C, const double* V, double* diagonal) {
+    if (N < 0 || !A || !diagonal) return FEEC_BADARG;
+    if (N == 0) return FEEC_OK;
+    const int nnz = A[N];
+    int dev = 0;
+    cudaStream_t s = nullptr;
+    int st = init_device(dev, s);
+    if (st != FEEC_OK) return st;
+    DevArena m; m.stream = s;
+    int *dA = nullptr, *dC = nullptr; double *dV = nullptr, *dd = nullptr;
+    cudaError_t e;
+    if ((e = m.alloc(dA, (size_t)N + 1)) == cudaSuccess && (e = m.alloc(dC, (size_t)nnz)) == cudaSuccess &&
+        (e = m.alloc(dV, (size_t)nnz)) == cudaSuccess && (e = m.alloc(dd, (size_t)N)) == cudaSuccess &&
+        (e = cudaMemcpyAsync(dA, A, sizeof(int) * ((size_t)N + 1), cudaMemcpyHostToDevice, s)) == cudaSuccess &&
+        (nnz == 0 || (e = cudaMemcpyAsync(dC, C, sizeof(int) * (size_t)nnz, cudaMemcpyHostToDevice, s)) == cudaSuccess) &&
+        (nnz == 0 || (e = cudaMemcpyAsync(dV, V, sizeof(double) * (size_t)nnz, cudaMemcpyHostToDevice, s)) == cudaSuccess) &&
+        (e = launch_diagonal_f64(N, dA, dC, dV, dd, s)) == cudaSuccess &&
+        (e = cudaMemcpyAsync(diagonal, dd, sizeof(double) * (size_t)N, cudaMemcpyDeviceToHost, s)) == cudaSuccess) {
+        e = cudaStreamSynchronize(s);
+    }
+    m.release();
+    cudaStreamSynchronize(s);
+    return cuda_status(e);
+}
+
+int feec_rainbow(int N, const int* A, const int* C, int* num_colors, int* F, int* B, int* R) {
+    if (N < 0 || !A || !num_colors || (N > 0 && (!C || !F || !B || !R))) return FEEC_BADARG;
+    if (N == 0) { *num_colors = 0; if (B) B[0] = 0; return FEEC_OK; }
+    *num_colors = rainbow_host(N, A, C, F, B, R);
+    return FEEC_OK;
+}
+
+int feec_csr_check(int rows, int cols, const int* A, const int* C, const double* V) {
+    if (rows < 0 || cols < 0 || !A) return FEEC_BADARG;
+    if (A[0] != 0) return FEEC_BADARG;
+    for (int p = 1; p <= rows; p++) if (A[p - 1] > A[p]) return FEEC_BADARG;
+    const int nnz = A[rows];
+    for (int i = 0; i < nnz; i++)
+        if (C[i] < 0 || C[i] >= cols || !std::isfinite(V[i])) return FEEC_BADARG;
+    return FEEC_OK;
+}
+
+}  // extern "C"

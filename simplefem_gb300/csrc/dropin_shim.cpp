@@ -1,0 +1,58 @@
+// libfeec_dropin.so: exports the reference's own C++ entry points of the CSR
+// Krylov path (solver/sparsesolver.hpp:11-19, 33-43, 59-70, with Float =
+// double, the reference's default build) so that an application linked
+// against FEEC++'s solver module can link this library instead and run the
+// solves on the GPU unchanged. Each function forwards to the C ABI and returns
+// the iteration count K exactly as the reference does.
+//
+// Error behaviour: the reference guards its arguments with assert()
+// (sparsesolver.cpp:32-43), which aborts in checked builds. A rejected argument
+// or a CUDA failure here prints a message and aborts likewise; numerical
+// breakdowns return the current K after the reference's log lines.
+#include <cstdio>
+#include <cstdlib>
+
+#include "feec_gpu.h"
+
+namespace {
+
+int checked(int status, const feec_solve_info& info, const char* fn) {
+    switch (status) {
+        case FEEC_OK:
+        case FEEC_BREAKDOWN:
+        case FEEC_SMALL_ENERGY:
+        case FEEC_MAXITER:
+            return info.iterations;
+        default:
+            std::fprintf(stderr, "%s: %s (status %d)\n", fn, feec_status_string(status), status);
+            std::abort();
+    }
+}
+
+}  // namespace
+
+int ConjugateGradientSolverCSR(const int N, double* x, const double* b, const int* csrrows, const int* csrcolumns,
+                               const double* csrvalues, double* residual, double precision, int print_modulo) {
+    feec_solve_info info;
+    const int st = feec_cg_csr(N, x, b, csrrows, csrcolumns, csrvalues, residual, precision, print_modulo, &info);
+    return checked(st, info, "ConjugateGradientSolverCSR");
+}
+
+int ConjugateGradientSolverCSR_SSOR(const int N, double* x, const double* b, const int* csrrows,
+                                    const int* csrcolumns, const double* csrvalues, double* residual,
+                                    double precision, int print_modulo, const double* diagonal, double omega) {
+    feec_solve_info info;
+    const int st = feec_cg_csr_ssor(N, x, b, csrrows, csrcolumns, csrvalues, residual, precision, print_modulo,
+                                    diagonal, omega, &info);
+    return checked(st, info, "ConjugateGradientSolverCSR_SSOR");
+}
+
+int ConjugateGradientSolverCSR_Rainbow(const int N, double* x, const double* b, const int* csrrows,
+                                       const int* csrcolumns, const double* csrvalues, double* residual,
+                                       double precision, int print_modulo, const double* diagonal, double omega,
+                                       int num_colors, const int* F, const int* B, const int* R) {
+    feec_solve_info info;
+    const int st = feec_cg_csr_rainbow(N, x, b, csrrows, csrcolumns, csrvalues, residual, precision, print_modulo,
+                                       diagonal, omega, num_colors, F, B, R, &info);
+    return checked(st, info, "ConjugateGradientSolverCSR_Rainbow");
+}

@@ -1,0 +1,99 @@
+// Internal interfaces between the host orchestration (capi.cu), the persistent
+// solver kernels (kernels_krylov.cu), the layout/SpMV kernels (kernels_setup.cu)
+// and the host integer preprocessing (coloring.cpp).
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "feec_gpu.h"
+
+namespace feec {
+
+struct DeviceStatus;
+
+// ---------------------------------------------------------------------------
+// Persistent solver arguments (all pointers are device pointers).
+// ---------------------------------------------------------------------------
+template <typename T>
+struct CgArgs {
+    int n;
+    const int* rp; const int* ci; const T* val;
+    const T* b;
+    T* x; T* r; T* d; T* q;
+    double tol2;        // stop when r.r < tol2 (reference rule) ...
+    int max_iter;       // ... or after max_iter iterations
+    int print_modulo;
+    double print_tol;   // tolerance printed in interim lines
+    double* partials;   // >= 3 * gridDim.x doubles
+    DeviceStatus* st;
+};
+
+template <typename T>
+struct PcgArgs {
+    int n;
+    const int* rp; const int* ci; const T* val;   // rows ordered [L | E | U]
+    const int* lsplit; const int* usplit;         // L = [rp, lsplit), E = [lsplit, usplit), U = [usplit, rp+1)
+    const T* diag; const T* b;
+    T* x; T* r; T* d; T* z; T* m; T* q;
+    int nf; const int* fptr;                      // forward phases: rows [fptr[p], fptr[p+1])
+    int nbw; const int* bptr; const int* brows;   // backward phases: rows brows[bptr[p] .. bptr[p+1])
+    double omega;
+    double tol2;         // reference rule: stop when |z.r| < tol2 (if use_zr_rule)
+    double rr_stop;      // stop when the recursive r.r < rr_stop (if > 0)
+    int use_zr_rule;
+    int max_iter;
+    int print_modulo;
+    double print_tol;
+    double* partials;    // >= 3 * gridDim.x doubles
+    DeviceStatus* st;
+};
+
+struct LaunchShape {
+    int blocks = 0;
+    int threads = 0;
+    int lanes = 0;
+};
+
+// Kernel launchers (kernels_krylov.cu). Return the CUDA error of the launch.
+template <typename T> cudaError_t launch_cg(const CgArgs<T>& a, LaunchShape& shape, cudaStream_t s);
+template <typename T> cudaError_t launch_pcg(const PcgArgs<T>& a, LaunchShape& shape, cudaStream_t s);
+// Largest co-resident grid for the given kernel family and lane count.
+int max_coresident_blocks(int family, int is_float, int lanes, int threads);
+int pick_lanes(double avg_nnz_per_row);
+
+// Setup / utility kernels (kernels_setup.cu).
+cudaError_t launch_spmv_f64(int n, const int* rp, const int* ci, const double* v, const double* x, double* y,
+                            double scaling, int lanes, cudaStream_t s);
+cudaError_t launch_residual_f64(int n, const int* rp, const int* ci, const double* v, const double* b,
+                                const double* x, double* r, double* partial_sq, int lanes, cudaStream_t s);
+cudaError_t launch_sum_sq_f64(int n, const double* v, double* out, cudaStream_t s);
+cudaError_t launch_permute_split(int n, const int* A, const int* C, const double* V, const int* perm,
+                                 const int* iperm, const int* key, const int* new_rp, int* out_ci,
+                                 double* out_v, float* out_v32, int* lsplit, int* usplit, cudaStream_t s);
+cudaError_t launch_validate_csr(int n, int nnz, const int* A, const int* C, int* bad, cudaStream_t s);
+cudaError_t launch_row_lengths(int n, const int* A, const int* perm, int* len, cudaStream_t s);
+cudaError_t launch_exclusive_scan(int n, const int* in, int* out, int* scratch, cudaStream_t s);
+cudaError_t launch_inverse_perm(int n, const int* perm, int* iperm, cudaStream_t s);
+cudaError_t launch_gather_f64(int n, const int* perm, const double* src, double* dst, cudaStream_t s);
+cudaError_t launch_scatter_f64(int n, const int* perm, const double* src, double* dst, cudaStream_t s);
+cudaError_t launch_gather_to_f32(int n, const int* perm, const double* src, float* dst, cudaStream_t s);
+cudaError_t launch_diagonal_f64(int n, const int* A, const int* C, const double* V, double* d, cudaStream_t s);
+cudaError_t launch_cast_f64_f32(size_t n, const double* src, float* dst, cudaStream_t s);
+// Mixed precision helpers.
+cudaError_t launch_scaled_cast(int n, const double* r, const double* inv_norm_dev, float* r32, cudaStream_t s);
+cudaError_t launch_update_x(int n, const int* perm, const float* c32, const double* norm_dev, double* x, cudaStream_t s);
+void note_launch();
+
+// Host integer preprocessing (coloring.cpp).
+int rainbow_host(int n, const int* A, const int* C, int* F, int* B, int* R);
+// Level schedule of the strictly lower (forward) or upper (backward) triangle in
+// index order: level[i] = 1 + max(level of earlier-solved neighbours).
+void triangular_levels(int n, const int* A, const int* C, bool lower, std::vector<int>& level, int& nlevels);
+
+size_t scan_scratch_ints(int n);
+
+}  // namespace feec

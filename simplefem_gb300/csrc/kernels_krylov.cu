@@ -1,0 +1,386 @@
+// Persistent Krylov solvers for sm_103a: one cooperative launch runs a whole
+// solve. Every phase of the reference's iteration becomes a grid-stride sweep
+// over rows, separated by bounded grid barriers; dot products are reduced
+// deterministically (fixed shuffle tree per block, fixed-order sum of the
+// per-block partials), so every block takes the same branch on the same bits.
+//
+//   cg_persistent  — ConjugateGradientSolverCSR   (solver/sparsesolver.cpp:26-201)
+//   pcg_persistent — ConjugateGradientSolverCSR_SSOR (:446-724) and _Rainbow
+//                    (:1002-1335): SSOR sweeps phase by phase over a schedule
+//                    (colors for Rainbow, dependency levels for index-order SSOR)
+//                    on a matrix whose rows are split into [L | E | U] parts.
+//
+// T = double is the drop-in FP64 path; T = float is the inner solver of the
+// mixed-precision mode (FP32 storage, FP32 arithmetic, compensated FP32 dots).
+#include <cmath>
+#include <cstdio>
+
+#include "feec_device.cuh"
+#include "feec_internal.h"
+
+namespace feec {
+
+constexpr int kThreads = 512;
+constexpr double kMachineEpsilon = 2.220446049250313080847263336181640625e-16;  // base/base.hpp:123
+
+// Iterate rows [lo, hi) with LANES lanes per row; the loop trip count is
+// uniform across each warp so the shuffles inside `body` see all 32 lanes.
+#define FEEC_FOR_ROW_GROUPS(lo, hi, row, active)                                                   \
+    for (int _base = (lo) + (int)((blockIdx.x * blockDim.x + threadIdx.x) / 32) * (32 / LANES);    \
+         _base < (hi); _base += (int)(gridDim.x * blockDim.x / 32) * (32 / LANES))                  \
+        for (int row = _base + (int)((threadIdx.x & 31) / LANES), _once = 1; _once; _once = 0)      \
+            for (bool active = row < (hi); _once; _once = 0)
+
+template <typename T, int LANES>
+__device__ __forceinline__ T seg_dot(const int* __restrict__ ci, const T* __restrict__ v, const T* x, int lo, int hi,
+                                     int lane) {
+    T s = T(0);
+    for (int j = lo + lane; j < hi; j += LANES) s = fma(__ldg(&v[j]), x[__ldg(&ci[j])], s);
+    #pragma unroll
+    for (int off = LANES / 2; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off, LANES);
+    return s;
+}
+
+template <typename T>
+__device__ __forceinline__ void write_partials(double* dst, typename AccT<T>::type v0) {
+    typename AccT<T>::type v[1] = {v0};
+    block_reduce<T, 1>(v);
+    if (threadIdx.x == 0) dst[blockIdx.x] = AccT<T>::value(v[0]);
+}
+
+template <typename T>
+__device__ __forceinline__ void write_partials2(double* dst, typename AccT<T>::type v0, typename AccT<T>::type v1) {
+    typename AccT<T>::type v[2] = {v0, v1};
+    block_reduce<T, 2>(v);
+    if (threadIdx.x == 0) {
+        dst[2 * blockIdx.x + 0] = AccT<T>::value(v[0]);
+        dst[2 * blockIdx.x + 1] = AccT<T>::value(v[1]);
+    }
+}
+
+__device__ __forceinline__ void finish(DeviceStatus* st, int status, int K, double fv, double av) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        atomicCAS(&st->status, FEEC_OK, status);
+        st->iterations = K;
+        st->final_value = fv;
+        st->aux_value = av;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Plain CG
+// ---------------------------------------------------------------------------
+template <typename T, int LANES>
+__global__ void __launch_bounds__(kThreads) cg_persistent(CgArgs<T> a) {
+    using AT = AccT<T>;
+    using Acc = typename AT::type;
+    unsigned long long epoch = 0;
+    const int n = a.n;
+    const int lane = threadIdx.x & (LANES - 1);
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nthr = gridDim.x * blockDim.x;
+    double* p_dq = a.partials;
+    double* p_rr = a.partials + gridDim.x;
+
+    // restart (sparsesolver.cpp:76-104): r = b - A x, d = r, r.r
+    Acc acc = AT::zero();
+    FEEC_FOR_ROW_GROUPS(0, n, i, act) {
+        const int lo = act ? __ldg(&a.rp[i]) : 0, hi = act ? __ldg(&a.rp[i + 1]) : 0;
+        const T s = seg_dot<T, LANES>(a.ci, a.val, a.x, lo, hi, lane);
+        if (act && lane == 0) {
+            const T ri = __ldg(&a.b[i]) - s;
+            a.r[i] = ri;
+            a.d[i] = ri;
+            acc = AT::add(acc, ri * ri);
+        }
+    }
+    write_partials<T>(p_rr, acc);
+    if (!grid_barrier(a.st, epoch, 1)) return;
+    double rr[1];
+    grid_sum<1>(p_rr, rr);
+    double r_r = rr[0];
+
+    int K = 0;
+    int status = FEEC_MAXITER;
+    double d_Ad = 0.0;
+    while (K < a.max_iter) {
+        if (a.print_modulo > 0 && K % a.print_modulo == 0 && blockIdx.x == 0 && threadIdx.x == 0)
+            printf("(%d/%d)   INTERIM: Residual norm is %.9le < %.9le\n", K, n, sqrt(r_r), a.print_tol);
+        if (fabs(r_r) < a.tol2) { status = FEEC_OK; break; }                        // :116-119
+
+        // q = A d, d.q                                                               :126-139
+        Acc adq = AT::zero();
+        FEEC_FOR_ROW_GROUPS(0, n, i, act) {
+            const int lo = act ? __ldg(&a.rp[i]) : 0, hi = act ? __ldg(&a.rp[i + 1]) : 0;
+            const T s = seg_dot<T, LANES>(a.ci, a.val, a.d, lo, hi, lane);
+            if (act && lane == 0) {
+                a.q[i] = s;
+                adq = AT::add(adq, a.d[i] * s);
+            }
+        }
+        write_partials<T>(p_dq, adq);
+        if (!grid_barrier(a.st, epoch, 2)) return;
+        double dq[1];
+        grid_sum<1>(p_dq, dq);
+        d_Ad = dq[0];
+
+        if (!isfinite(r_r) || r_r < 0.0 || !isfinite(d_Ad) || d_Ad < 0.0) { status = FEEC_BREAKDOWN; break; }  // :142-151
+        if (sqrt(fabs(d_Ad)) < kMachineEpsilon) { status = FEEC_SMALL_ENERGY; break; }                        // :153-157
+
+        const T alpha = (T)(r_r / d_Ad);
+        Acc arr = AT::zero();
+        for (int i = tid; i < n; i += nthr) {                                          // :158-173
+            const T di = a.d[i];
+            a.x[i] += alpha * di;
+            const T ri = a.r[i] - alpha * a.q[i];
+            a.r[i] = ri;
+            arr = AT::add(arr, ri * ri);
+        }
+        write_partials<T>(p_rr, arr);
+        if (!grid_barrier(a.st, epoch, 3)) return;
+        grid_sum<1>(p_rr, rr);
+        const double r_r_new = rr[0];
+        const T beta = (T)(r_r_new / r_r);                                             // :175-183
+        r_r = r_r_new;
+        for (int i = tid; i < n; i += nthr) a.d[i] = a.r[i] + beta * a.d[i];
+        if (!grid_barrier(a.st, epoch, 4)) return;
+        K++;
+    }
+    finish(a.st, status, K, r_r, d_Ad);
+}
+
+// ---------------------------------------------------------------------------
+// SSOR / multicolor SSOR preconditioned CG
+// ---------------------------------------------------------------------------
+template <typename T, int LANES>
+__global__ void __launch_bounds__(kThreads) pcg_persistent(PcgArgs<T> a) {
+    using AT = AccT<T>;
+    using Acc = typename AT::type;
+    unsigned long long epoch = 0;
+    const int n = a.n;
+    const int lane = threadIdx.x & (LANES - 1);
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nthr = gridDim.x * blockDim.x;
+    double* p_dq = a.partials;
+    double* p_zr = a.partials + gridDim.x;   // (z.r, r.r) pairs
+    const T omega = (T)a.omega;
+    const T two_minus_over = (T)((2.0 - a.omega) / a.omega);
+
+    // ---- restart (sparsesolver.cpp:1072-1175 / 506-588) ----
+    Acc arr = AT::zero();
+    FEEC_FOR_ROW_GROUPS(0, n, i, act) {                      // r = b - A x for rows with D != 0
+        const int lo = act ? __ldg(&a.rp[i]) : 0, hi = act ? __ldg(&a.rp[i + 1]) : 0;
+        const T s = seg_dot<T, LANES>(a.ci, a.val, a.x, lo, hi, lane);
+        if (act && lane == 0 && __ldg(&a.diag[i]) != T(0)) {
+            const T ri = __ldg(&a.b[i]) - s;
+            a.r[i] = ri;
+            arr = AT::add(arr, ri * ri);
+        }
+    }
+    if (!grid_barrier(a.st, epoch, 10)) return;
+    for (int p = 0; p < a.nf; p++) {                          // forward sweep, phase by phase
+        const int lo_r = __ldg(&a.fptr[p]), hi_r = __ldg(&a.fptr[p + 1]);
+        FEEC_FOR_ROW_GROUPS(lo_r, hi_r, i, act) {
+            const int lo = act ? __ldg(&a.rp[i]) : 0, hi = act ? __ldg(&a.lsplit[i]) : 0;
+            const T s = seg_dot<T, LANES>(a.ci, a.val, a.m, lo, hi, lane);
+            if (act && lane == 0) {
+                const T D = __ldg(&a.diag[i]);
+                if (D != T(0)) a.m[i] = (a.r[i] - s) * omega / D;
+            }
+        }
+        if (!grid_barrier(a.st, epoch, 11)) return;
+    }
+    Acc azr = AT::zero();
+    for (int p = 0; p < a.nbw; p++) {                         // scale + backward sweep
+        const int lo_r = __ldg(&a.bptr[p]), hi_r = __ldg(&a.bptr[p + 1]);
+        FEEC_FOR_ROW_GROUPS(lo_r, hi_r, k, act) {
+            const int i = act ? __ldg(&a.brows[k]) : 0;
+            const int lo = act ? __ldg(&a.usplit[i]) : 0, hi = act ? __ldg(&a.rp[i + 1]) : 0;
+            const T s = seg_dot<T, LANES>(a.ci, a.val, a.z, lo, hi, lane);
+            if (act && lane == 0) {
+                const T D = __ldg(&a.diag[i]);
+                if (D != T(0)) {
+                    T mi = a.m[i] * D;
+                    mi *= two_minus_over;
+                    a.m[i] = mi;
+                    const T zi = (mi - s) * omega / D;
+                    a.z[i] = zi;
+                    a.d[i] = zi;
+                    azr = AT::add(azr, zi * a.r[i]);
+                }
+            }
+        }
+        if (p + 1 < a.nbw) {
+            if (!grid_barrier(a.st, epoch, 12)) return;
+        }
+    }
+    write_partials2<T>(p_zr, azr, arr);
+    if (!grid_barrier(a.st, epoch, 13)) return;
+    double zr2[2];
+    grid_sum<2>(p_zr, zr2);
+    double z_r = zr2[0], r_r = zr2[1];
+
+    int K = 0;
+    int status = FEEC_MAXITER;
+    double d_Ad = 0.0;
+    while (K < a.max_iter) {
+        if (a.print_modulo > 0 && K % a.print_modulo == 0 && blockIdx.x == 0 && threadIdx.x == 0)
+            printf("(%d/%d)   INTERIM: Residual norm is %.9le < %.9le\n", K, n, sqrt(z_r), a.print_tol);
+        if (a.use_zr_rule && fabs(z_r) < a.tol2) { status = FEEC_OK; break; }         // :1187-1190
+        if (a.rr_stop > 0.0 && r_r < a.rr_stop) { status = FEEC_OK; break; }
+
+        Acc adq = AT::zero();                                                          // :1197-1212
+        FEEC_FOR_ROW_GROUPS(0, n, i, act) {
+            const int lo = act ? __ldg(&a.rp[i]) : 0, hi = act ? __ldg(&a.rp[i + 1]) : 0;
+            const T s = seg_dot<T, LANES>(a.ci, a.val, a.d, lo, hi, lane);
+            if (act && lane == 0) {
+                const T qi = (__ldg(&a.diag[i]) != T(0)) ? s : T(0);
+                a.q[i] = qi;
+                adq = AT::add(adq, a.d[i] * qi);
+            }
+        }
+        write_partials<T>(p_dq, adq);
+        if (!grid_barrier(a.st, epoch, 14)) return;
+        double dq[1];
+        grid_sum<1>(p_dq, dq);
+        d_Ad = dq[0];
+        if (!isfinite(z_r) || z_r < 0.0 || !isfinite(d_Ad) || d_Ad < 0.0) { status = FEEC_BREAKDOWN; break; }
+        if (sqrt(fabs(d_Ad)) < kMachineEpsilon) { status = FEEC_SMALL_ENERGY; break; }
+
+        const T alpha = (T)(z_r / d_Ad);
+        arr = AT::zero();
+        for (int p = 0; p < a.nf; p++) {                                               // :1230-1261
+            const int lo_r = __ldg(&a.fptr[p]), hi_r = __ldg(&a.fptr[p + 1]);
+            FEEC_FOR_ROW_GROUPS(lo_r, hi_r, i, act) {
+                const int lo = act ? __ldg(&a.rp[i]) : 0, hi = act ? __ldg(&a.lsplit[i]) : 0;
+                const T s = seg_dot<T, LANES>(a.ci, a.val, a.m, lo, hi, lane);
+                if (act && lane == 0) {
+                    const T D = __ldg(&a.diag[i]);
+                    if (D != T(0)) {
+                        a.x[i] += alpha * a.d[i];
+                        const T ri = a.r[i] - alpha * a.q[i];
+                        a.r[i] = ri;
+                        arr = AT::add(arr, ri * ri);
+                        a.m[i] = (ri - s) * omega / D;
+                    }
+                }
+            }
+            if (!grid_barrier(a.st, epoch, 15)) return;
+        }
+        azr = AT::zero();
+        for (int p = 0; p < a.nbw; p++) {                                              // :1263-1307
+            const int lo_r = __ldg(&a.bptr[p]), hi_r = __ldg(&a.bptr[p + 1]);
+            FEEC_FOR_ROW_GROUPS(lo_r, hi_r, k, act) {
+                const int i = act ? __ldg(&a.brows[k]) : 0;
+                const int lo = act ? __ldg(&a.usplit[i]) : 0, hi = act ? __ldg(&a.rp[i + 1]) : 0;
+                const T s = seg_dot<T, LANES>(a.ci, a.val, a.z, lo, hi, lane);
+                if (act && lane == 0) {
+                    const T D = __ldg(&a.diag[i]);
+                    if (D != T(0)) {
+                        T mi = a.m[i] * D;
+                        mi *= two_minus_over;
+                        a.m[i] = mi;
+                        const T zi = (mi - s) * omega / D;
+                        a.z[i] = zi;
+                        azr = AT::add(azr, zi * a.r[i]);
+                    }
+                }
+            }
+            if (p + 1 < a.nbw) {
+                if (!grid_barrier(a.st, epoch, 16)) return;
+            }
+        }
+        write_partials2<T>(p_zr, azr, arr);
+        if (!grid_barrier(a.st, epoch, 17)) return;
+        grid_sum<2>(p_zr, zr2);
+        const double z_r_new = zr2[0];
+        r_r = zr2[1];
+        const T beta = (T)(z_r_new / z_r);                                             // :1309-1318
+        z_r = z_r_new;
+        for (int i = tid; i < n; i += nthr) {
+            if (__ldg(&a.diag[i]) != T(0)) a.d[i] = a.z[i] + beta * a.d[i];
+        }
+        if (!grid_barrier(a.st, epoch, 18)) return;
+        K++;
+    }
+    finish(a.st, status, K, z_r, r_r);
+}
+
+// ---------------------------------------------------------------------------
+// Launchers
+// ---------------------------------------------------------------------------
+template <typename T, int LANES>
+static const void* cg_fn() { return (const void*)cg_persistent<T, LANES>; }
+template <typename T, int LANES>
+static const void* pcg_fn() { return (const void*)pcg_persistent<T, LANES>; }
+
+template <typename T>
+static const void* family_fn(int family, int lanes) {
+    if (family == 0) {
+        switch (lanes) {
+            case 1: return cg_fn<T, 1>(); case 2: return cg_fn<T, 2>(); case 4: return cg_fn<T, 4>();
+            case 8: return cg_fn<T, 8>(); case 16: return cg_fn<T, 16>(); default: return cg_fn<T, 32>();
+        }
+    }
+    switch (lanes) {
+        case 1: return pcg_fn<T, 1>(); case 2: return pcg_fn<T, 2>(); case 4: return pcg_fn<T, 4>();
+        case 8: return pcg_fn<T, 8>(); case 16: return pcg_fn<T, 16>(); default: return pcg_fn<T, 32>();
+    }
+}
+
+int max_coresident_blocks(int family, int is_float, int lanes, int threads) {
+    const void* fn = is_float ? family_fn<float>(family, lanes) : family_fn<double>(family, lanes);
+    int dev = 0, sms = 0, per_sm = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, 0) != cudaSuccess) return 0;
+    return sms * per_sm;
+}
+
+int pick_lanes(double avg) {
+    if (avg <= 3.0) return 2;
+    if (avg <= 10.0) return 4;
+    if (avg <= 24.0) return 8;
+    if (avg <= 48.0) return 16;
+    return 32;
+}
+
+static int pick_blocks(int family, int is_float, int n, LaunchShape& shape) {
+    if (shape.threads <= 0) shape.threads = kThreads;
+    const int maxb = max_coresident_blocks(family, is_float, shape.lanes, shape.threads);
+    if (maxb <= 0) return 0;
+    // enough groups for every row in one sweep, at most the co-resident grid
+    const long long want = ((long long)n * shape.lanes + shape.threads - 1) / shape.threads;
+    int b = shape.blocks > 0 ? shape.blocks : (int)(want < maxb ? want : maxb);
+    if (b > maxb) b = maxb;
+    if (b < 1) b = 1;
+    shape.blocks = b;
+    return b;
+}
+
+template <typename T>
+cudaError_t launch_cg(const CgArgs<T>& a, LaunchShape& shape, cudaStream_t s) {
+    const int is_float = sizeof(T) == 4;
+    if (pick_blocks(0, is_float, a.n, shape) <= 0) return cudaErrorInvalidConfiguration;
+    CgArgs<T> copy = a;
+    void* args[] = {&copy};
+    note_launch();
+    return cudaLaunchCooperativeKernel(family_fn<T>(0, shape.lanes), dim3(shape.blocks), dim3(shape.threads), args, 0, s);
+}
+
+template <typename T>
+cudaError_t launch_pcg(const PcgArgs<T>& a, LaunchShape& shape, cudaStream_t s) {
+    const int is_float = sizeof(T) == 4;
+    if (pick_blocks(1, is_float, a.n, shape) <= 0) return cudaErrorInvalidConfiguration;
+    PcgArgs<T> copy = a;
+    void* args[] = {&copy};
+    note_launch();
+    return cudaLaunchCooperativeKernel(family_fn<T>(1, shape.lanes), dim3(shape.blocks), dim3(shape.threads), args, 0, s);
+}
+
+template cudaError_t launch_cg<double>(const CgArgs<double>&, LaunchShape&, cudaStream_t);
+template cudaError_t launch_cg<float>(const CgArgs<float>&, LaunchShape&, cudaStream_t);
+template cudaError_t launch_pcg<double>(const PcgArgs<double>&, LaunchShape&, cudaStream_t);
+template cudaError_t launch_pcg<float>(const PcgArgs<float>&, LaunchShape&, cudaStream_t);
+
+}  // namespace feec

@@ -1,0 +1,80 @@
+"""The reference's raw-pointer CSR Krylov drivers, running on the GPU.
+
+Same names, argument order and meaning as solver/sparsesolver.hpp:11-70: ``x`` is the
+initial guess and receives the solution, ``residual`` receives the final recursive
+residual, and the return value is the iteration count K. Arrays are NumPy arrays
+(float64 vectors, int32 CSR arrays) standing in for the raw pointers; ``x`` and
+``residual`` are written in place. Where the reference asserts on an argument
+(sparsesolver.cpp:32-43) these functions raise ``FeecError``; numerical breakdowns
+return the current K as the reference does, and the last call's details
+(status, timing, tolerance) are kept in ``last_info()``.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from . import _native
+
+_last_info = None
+
+
+def last_info() -> dict | None:
+    """Details of the most recent solve: status, iterations, tolerance, device time."""
+    return None if _last_info is None else _last_info.as_dict()
+
+
+def _vec(a, name, n=None, writable=False):
+    if not isinstance(a, np.ndarray) or a.dtype != np.float64 or not a.flags.c_contiguous:
+        if writable:
+            raise TypeError(f"{name} must be a C-contiguous float64 numpy array (it is written in place)")
+        a = np.ascontiguousarray(a, np.float64)
+    if n is not None and a.shape[0] < n:
+        raise ValueError(f"{name} has {a.shape[0]} entries, expected {n}")
+    return a
+
+
+def _ints(a, name):
+    return np.ascontiguousarray(a, np.int32)
+
+
+_DONE = (_native.FEEC_OK, _native.FEEC_BREAKDOWN, _native.FEEC_SMALL_ENERGY, _native.FEEC_MAXITER)
+
+
+def _finish(status, info, where):
+    global _last_info
+    _last_info = info
+    if status not in _DONE:
+        raise _native.FeecError(status, where)
+    return int(info.iterations)
+
+
+def ConjugateGradientSolverCSR(N, x, b, csrrows, csrcolumns, csrvalues, residual, precision, print_modulo=-3):
+    """GPU replacement of ConjugateGradientSolverCSR (solver/sparsesolver.cpp:26-201)."""
+    x = _vec(x, "x", N, True); residual = _vec(residual, "residual", N, True)
+    info = _native.FeecSolveInfo()
+    st = _native.gpu().feec_cg_csr(int(N), x, _vec(b, "b", N), _ints(csrrows, "A"), _ints(csrcolumns, "C"),
+                                   _vec(csrvalues, "V"), residual, float(precision), int(print_modulo), info)
+    return _finish(st, info, "ConjugateGradientSolverCSR")
+
+
+def ConjugateGradientSolverCSR_SSOR(N, x, b, csrrows, csrcolumns, csrvalues, residual, precision, print_modulo,
+                                    diagonal, omega):
+    """GPU replacement of ConjugateGradientSolverCSR_SSOR (solver/sparsesolver.cpp:446-724)."""
+    x = _vec(x, "x", N, True); residual = _vec(residual, "residual", N, True)
+    info = _native.FeecSolveInfo()
+    st = _native.gpu().feec_cg_csr_ssor(int(N), x, _vec(b, "b", N), _ints(csrrows, "A"), _ints(csrcolumns, "C"),
+                                        _vec(csrvalues, "V"), residual, float(precision), int(print_modulo),
+                                        _vec(diagonal, "diagonal", N), float(omega), info)
+    return _finish(st, info, "ConjugateGradientSolverCSR_SSOR")
+
+
+def ConjugateGradientSolverCSR_Rainbow(N, x, b, csrrows, csrcolumns, csrvalues, residual, precision, print_modulo,
+                                       diagonal, omega, num_colors, F, B, R):
+    """GPU replacement of ConjugateGradientSolverCSR_Rainbow (solver/sparsesolver.cpp:1002-1335)."""
+    x = _vec(x, "x", N, True); residual = _vec(residual, "residual", N, True)
+    info = _native.FeecSolveInfo()
+    st = _native.gpu().feec_cg_csr_rainbow(int(N), x, _vec(b, "b", N), _ints(csrrows, "A"), _ints(csrcolumns, "C"),
+                                           _vec(csrvalues, "V"), residual, float(precision), int(print_modulo),
+                                           _vec(diagonal, "diagonal", N), float(omega), int(num_colors),
+                                           _ints(F, "F"), _ints(B, "B"), _ints(R, "R"), info)
+    return _finish(st, info, "ConjugateGradientSolverCSR_Rainbow")

@@ -1,0 +1,98 @@
+"""Device-resident CSR systems (the ``feec_system_*`` part of the C ABI).
+
+A ``System`` uploads a CSR matrix once, optionally prepares the multicolor or
+index-order SSOR layout, and then solves with right-hand sides and iterates that
+stay in device memory. Device buffers are torch tensors (used purely as device
+allocations); every call runs on torch's current CUDA stream.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _native
+
+METHODS = {"cg": _native.METHOD_CG, "ssor": _native.METHOD_SSOR, "rainbow": _native.METHOD_RAINBOW}
+MODES = {"reference": _native.MODE_REFERENCE, "fp64": _native.MODE_FP64, "mixed": _native.MODE_MIXED}
+
+
+def _torch():
+    import torch
+    if not torch.cuda.is_available():
+        raise RuntimeError("simplefem_gb300.System needs a CUDA device")
+    return torch
+
+
+def _ptr(t):
+    return ctypes.c_void_p(t.data_ptr()) if t is not None else None
+
+
+def _stream():
+    torch = _torch()
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+class System:
+    def __init__(self, A, C, V):
+        self._lib = _native.gpu()
+        A = np.ascontiguousarray(A, np.int32)
+        C = np.ascontiguousarray(C, np.int32)
+        V = np.ascontiguousarray(V, np.float64)
+        self.n = int(A.shape[0] - 1)
+        self.nnz = int(C.shape[0])
+        h = ctypes.c_void_p()
+        st = self._lib.feec_system_create(ctypes.byref(h), self.n, A.ctypes.data_as(ctypes.c_void_p),
+                                          C.ctypes.data_as(ctypes.c_void_p), V.ctypes.data_as(ctypes.c_void_p), 1,
+                                          _stream())
+        _native.check(st, "feec_system_create")
+        self._h = h
+        self.prepared = None
+
+    def set_rainbow(self, diagonal, omega, num_colors, F, B, R):
+        d = np.ascontiguousarray(diagonal, np.float64)
+        F = np.ascontiguousarray(F, np.int32); B = np.ascontiguousarray(B, np.int32); R = np.ascontiguousarray(R, np.int32)
+        st = self._lib.feec_system_set_rainbow(self._h, d.ctypes.data_as(ctypes.c_void_p), float(omega), int(num_colors),
+                                               F.ctypes.data_as(ctypes.c_void_p), B.ctypes.data_as(ctypes.c_void_p),
+                                               R.ctypes.data_as(ctypes.c_void_p), 1)
+        _native.check(st, "feec_system_set_rainbow")
+        self.prepared = "rainbow"
+
+    def set_ssor(self, diagonal, omega):
+        d = np.ascontiguousarray(diagonal, np.float64)
+        st = self._lib.feec_system_set_ssor(self._h, d.ctypes.data_as(ctypes.c_void_p), float(omega), 1)
+        _native.check(st, "feec_system_set_ssor")
+        self.prepared = "ssor"
+
+    def solve(self, b, x, method="rainbow", mode="reference", precision=1e-10, max_iter=0, residual=None,
+              raise_on_error=True) -> dict:
+        """Solve A x = b with device tensors b, x (float64, length n); x is the initial guess."""
+        info = _native.FeecSolveInfo()
+        st = self._lib.feec_system_solve(self._h, METHODS[method], MODES[mode], _ptr(x), _ptr(b), _ptr(residual),
+                                         float(precision), int(max_iter), info, _stream())
+        out = info.as_dict()
+        out["status_name"] = _native.STATUS.get(st, str(st))
+        if raise_on_error and st not in (_native.FEEC_OK, _native.FEEC_BREAKDOWN, _native.FEEC_SMALL_ENERGY,
+                                         _native.FEEC_MAXITER):
+            raise _native.FeecError(st, "feec_system_solve")
+        return out
+
+    def apply(self, x, y, scaling=1.0):
+        _native.check(self._lib.feec_system_apply(self._h, _ptr(x), _ptr(y), float(scaling), _stream()),
+                      "feec_system_apply")
+
+    def memory_bytes(self) -> int:
+        b = ctypes.c_size_t(0)
+        _native.check(self._lib.feec_system_memory(self._h, ctypes.byref(b)), "feec_system_memory")
+        return int(b.value)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.feec_system_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,58 @@
+"""Synthetic workloads with the shapes of the benchmark configurations.
+
+``lattice_matrix(dim, r, L, coef_seed)`` assembles the Lagrange P_r stiffness plus
+(coefficient) mass operator on the unit square / cube refined L times — the same
+operator the reference's FEEC route builds (tests/solverfem/csrsolver_stiff.cpp:209-243),
+numbered lexicographically on the degree-of-freedom lattice (see csrc/lattice_fem.cpp).
+``uniform_vector(seed, n)`` draws U[-1, 1) from SplitMix64, reproducible on any host.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _native
+
+
+def lattice_size(dim: int, r: int, L: int):
+    n = ctypes.c_int64(); nnz = ctypes.c_int64()
+    st = _native.workload().feec_lattice_size(dim, r, L, ctypes.byref(n), ctypes.byref(nnz))
+    if st != 0:
+        raise ValueError(f"unsupported lattice dim={dim} r={r} L={L}")
+    return int(n.value), int(nnz.value)
+
+
+def lattice_matrix(dim: int, r: int, L: int, coef_seed: int = 0):
+    """(A, C, V) int32/int32/float64 CSR arrays of the P_r stiffness + mass operator."""
+    n, nnz = lattice_size(dim, r, L)
+    if nnz >= 2**31:
+        raise ValueError("operator too large for int32 CSR")
+    A = np.empty(n + 1, np.int32); C = np.empty(nnz, np.int32); V = np.empty(nnz, np.float64)
+    st = _native.workload().feec_lattice_assemble(dim, r, L, ctypes.c_uint64(coef_seed), A, C, V)
+    if st != 0:
+        raise RuntimeError("lattice assembly failed")
+    return A, C, V
+
+
+def lattice_positions(dim: int, r: int, L: int) -> np.ndarray:
+    n, _ = lattice_size(dim, r, L)
+    pos = np.empty(n * dim, np.float64)
+    _native.workload().feec_lattice_positions(dim, r, L, pos)
+    return pos.reshape(n, dim)
+
+
+def uniform_vector(seed: int, n: int, lo: float = -1.0, hi: float = 1.0) -> np.ndarray:
+    out = np.empty(n, np.float64)
+    _native.workload().feec_uniform_vector(ctypes.c_uint64(seed), n, lo, hi, out)
+    return out
+
+
+# The benchmark configurations (sizes follow the reference's uniform refinement).
+CONFIGS = {
+    "cfg1_2d_p1_l6": dict(dim=2, r=1, L=6),     # plain CG, N = 4,225
+    "cfg2_3d_p2_l5": dict(dim=3, r=2, L=5),     # Rainbow SSOR-PCG, N = 274,625
+    "cfg3_3d_p1_l6": dict(dim=3, r=1, L=6),     # mixed-precision inner sizing, N = 274,625
+    "cfg3_3d_p1_l7": dict(dim=3, r=1, L=7),     # mixed-precision target, N = 2,146,689
+    "cfg4_2d_p2_l7": dict(dim=2, r=2, L=7),     # largest batched system, N = 66,049
+}

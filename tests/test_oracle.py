@@ -1,0 +1,58 @@
+"""Pins the oracle (the C restatement in oracle/feec_oracle.c) to the reference's own
+outputs stored in tests/golden (written by tests/golden/make_golden.py from the
+compiled reference). At one OpenMP thread the restatement must reproduce the
+reference bit for bit: iteration counts, solutions, residual arrays, SpMV,
+diagonal and the Rainbow ordering."""
+import numpy as np
+import pytest
+
+from conftest import golden_names, load_golden
+
+NAMES = golden_names()
+
+
+@pytest.fixture(scope="module")
+def O(built):
+    from oracle import oracle
+    oracle.set_threads(1)
+    return oracle
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_oracle_spmv_diagonal_rainbow_bitexact(O, name):
+    g = load_golden(name)
+    A, C, V, b = g["A"], g["C"], g["V"], g["b"]
+    assert np.array_equal(O.csr_apply(A, C, V, b, 0.7), g["apply_out"])
+    assert np.array_equal(O.csr_diagonal(A, C, V), g["diag"])
+    nc, F, B, R = O.rainbow(A, C)
+    assert nc == int(g["rb_nc"])
+    assert np.array_equal(F, g["rb_F"]) and np.array_equal(B, g["rb_B"]) and np.array_equal(R, g["rb_R"])
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_oracle_solvers_bitexact(O, name):
+    g = load_golden(name)
+    A, C, V, b = g["A"], g["C"], g["V"], g["b"]
+    prec = float(g["precision"])
+    diag = g["diag"]
+    rb = (int(g["rb_nc"]), g["rb_F"], g["rb_B"], g["rb_R"])
+    for key in [k[:-2] for k in g if k.endswith("_K")]:
+        om = float(g[key + "_omega"])
+        if key == "cg":
+            K, x, r = O.cg(A, C, V, b, precision=prec)
+        elif key.startswith("ssor"):
+            K, x, r = O.cg_ssor(A, C, V, b, diag, om, precision=prec)
+        else:
+            K, x, r = O.cg_rainbow(A, C, V, b, diag, rb, om, precision=prec)
+        assert K == int(g[key + "_K"]), key
+        assert np.array_equal(x, g[key + "_x"]), key
+        assert np.array_equal(r, g[key + "_res"]), key
+
+
+def test_oracle_planted_mistake_is_caught(O):
+    """A wrong matrix entry planted in the oracle's input must change its answer."""
+    g = load_golden("fem2d_p1_l6")
+    V = g["V"].copy()
+    V[100] *= 1.0 + 1e-6
+    K, x, _ = O.cg(g["A"], g["C"], V, g["b"], precision=float(g["precision"]))
+    assert not np.array_equal(x, g["cg_x"])
