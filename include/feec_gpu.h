@@ -138,6 +138,11 @@ int feec_system_solve(feec_system* sys, int method, int mode, double* x, const d
 /* y = scaling * A * x with device pointers. */
 int feec_system_apply(feec_system* sys, const double* x, double* y, double scaling, void* stream);
 
+/* Launch-shape override for the persistent solvers (used by the autotuner):
+ * blocks = co-resident grid size, lanes = CSR lanes per row (power of two <= 32);
+ * 0 restores the automatic choice. Sizes beyond the co-resident limit are clamped. */
+int feec_system_set_launch(feec_system* sys, int blocks, int lanes);
+
 /* Bytes of device memory held by the system. */
 int feec_system_memory(const feec_system* sys, size_t* bytes);
 

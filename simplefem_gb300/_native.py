@@ -82,6 +82,7 @@ def gpu():
         L.feec_system_set_ssor.argtypes = [_vp, _vp, _dp, _ip]
         L.feec_system_solve.argtypes = [_vp, _ip, _ip, _vp, _vp, _vp, _dp, _ip, _infop, _vp]
         L.feec_system_apply.argtypes = [_vp, _vp, _vp, _dp, _vp]
+        L.feec_system_set_launch.argtypes = [_vp, _ip, _ip]
         L.feec_system_memory.argtypes = [_vp, ctypes.POINTER(ctypes.c_size_t)]
         L.feec_system_destroy.argtypes = [_vp]
         L.feec_kernel_launches.restype = ctypes.c_ulonglong

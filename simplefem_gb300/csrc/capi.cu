@@ -123,6 +123,7 @@ struct feec_system {
     int* rp = nullptr; int* ci = nullptr; double* val = nullptr; float* val32 = nullptr;
     int* lsplit = nullptr; int* usplit = nullptr;
     double* diag = nullptr; float* diag32 = nullptr;
+    double* wd = nullptr; double* sd = nullptr; float* wd32 = nullptr; float* sd32 = nullptr;
     int nf = 0; int* fptr = nullptr;
     int nbw = 0; int* bptr = nullptr; int* brows = nullptr;
     double omega = 1.0;
@@ -135,6 +136,9 @@ struct feec_system {
     double* scal = nullptr;   // device scalars
     DeviceStatus* st = nullptr;
     int max_blocks = 0;
+    int max_phase_rows = 0;     // largest sweep phase (rows)
+    int user_blocks = 0;        // launch-shape overrides (0 = automatic)
+    int user_lanes = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 };
 
@@ -195,10 +199,11 @@ int true_residual(feec_system* s, const double* bb, const double* xx, double* rr
 }
 
 template <typename T>
-PcgArgs<T> make_pcg_args(feec_system* s, T* x, T* r, T* d, T* z, T* m, T* q, const T* b, const T* val, const T* diag) {
+PcgArgs<T> make_pcg_args(feec_system* s, T* x, T* r, T* d, T* z, T* m, T* q, const T* b, const T* val, const T* wd,
+                         const T* sd) {
     PcgArgs<T> a{};
     a.n = s->n; a.rp = s->rp; a.ci = s->ci; a.val = val; a.lsplit = s->lsplit; a.usplit = s->usplit;
-    a.diag = diag; a.b = b; a.x = x; a.r = r; a.d = d; a.z = z; a.m = m; a.q = q;
+    a.wd = wd; a.sd = sd; a.b = b; a.x = x; a.r = r; a.d = d; a.z = z; a.m = m; a.q = q;
     a.nf = s->nf; a.fptr = s->fptr; a.nbw = s->nbw; a.bptr = s->bptr; a.brows = s->brows;
     a.omega = s->omega; a.partials = s->partials; a.st = s->st;
     return a;
@@ -257,6 +262,13 @@ int solve_core(feec_system* s, int method, int mode, double* xx, const double* b
 
     LaunchShape shape;
     shape.lanes = s->lanes;
+    if (permuted && s->max_phase_rows > 0) {
+        // one pass over the largest sweep phase: enough row groups in the co-resident grid
+        const int maxb = max_coresident_blocks(1, 0, shape.lanes, 512);
+        while (shape.lanes > 1 && (long long)maxb * 512 / shape.lanes < s->max_phase_rows) shape.lanes >>= 1;
+    }
+    if (s->user_lanes > 0) shape.lanes = s->user_lanes;
+    if (s->user_blocks > 0) shape.blocks = s->user_blocks;
     float ms_total = 0.0f;
     int K_total = 0, outer = 0, status = FEEC_OK;
     double final_norm = 0.0;
@@ -286,7 +298,7 @@ int solve_core(feec_system* s, int method, int mode, double* xx, const double* b
                 FEEC_TRY(cudaEventSynchronize(s->ev1));
                 FEEC_TRY(cudaEventElapsedTime(&ms, s->ev0, s->ev1));
             } else {
-                PcgArgs<double> a = make_pcg_args<double>(s, s->x, s->r, s->d, s->z, s->m, s->q, s->b, s->val, s->diag);
+                PcgArgs<double> a = make_pcg_args<double>(s, s->x, s->r, s->d, s->z, s->m, s->q, s->b, s->val, s->wd, s->sd);
                 a.tol2 = tolerance * tolerance;
                 a.use_zr_rule = (mode == FEEC_MODE_REFERENCE) ? 1 : 0;
                 a.rr_stop = (mode == FEEC_MODE_FP64) ? tolerance * tolerance : 0.0;
@@ -350,7 +362,7 @@ int solve_core(feec_system* s, int method, int mode, double* xx, const double* b
                 FEEC_TRY(launch_cg<float>(a, shape, s->stream));
             } else {
                 PcgArgs<float> a = make_pcg_args<float>(s, s->x32, s->r32, s->d32, s->z32, s->m32, s->q32, s->b32,
-                                                        s->val32, s->diag32);
+                                                        s->val32, s->wd32, s->sd32);
                 a.use_zr_rule = 0;
                 a.rr_stop = eta * eta;
                 a.max_iter = max_iter - K_total;
@@ -413,6 +425,7 @@ int build_layout(feec_system* s, int method, const double* diag_dev, double omeg
         FEEC_TRY(M.alloc(s->val, (size_t)s->nnz)); FEEC_TRY(M.alloc(s->val32, (size_t)s->nnz));
         FEEC_TRY(M.alloc(s->lsplit, n)); FEEC_TRY(M.alloc(s->usplit, n));
         FEEC_TRY(M.alloc(s->diag, n)); FEEC_TRY(M.alloc(s->diag32, n));
+        FEEC_TRY(M.alloc(s->wd, n)); FEEC_TRY(M.alloc(s->sd, n)); FEEC_TRY(M.alloc(s->wd32, n)); FEEC_TRY(M.alloc(s->sd32, n));
     }
     // schedules (small, reallocated per preparation)
     FEEC_TRY(M.alloc(s->fptr, fptr.size())); FEEC_TRY(M.alloc(s->bptr, bptr.size())); FEEC_TRY(M.alloc(s->brows, brows.size()));
@@ -432,10 +445,14 @@ int build_layout(feec_system* s, int method, const double* diag_dev, double omeg
                                   s->lsplit, s->usplit, st));
     FEEC_TRY(launch_gather_f64(n, s->perm, diag_dev, s->diag, st));
     FEEC_TRY(launch_cast_f64_f32((size_t)n, s->diag, s->diag32, st));
+    FEEC_TRY(launch_sweep_factors(n, s->diag, omega, s->wd, s->sd, s->wd32, s->sd32, st));
     tmp.release();
     FEEC_TRY(cudaStreamSynchronize(st));
     s->nf = (int)fptr.size() - 1;
     s->nbw = (int)bptr.size() - 1;
+    s->max_phase_rows = 0;
+    for (size_t p = 0; p + 1 < fptr.size(); p++) s->max_phase_rows = std::max(s->max_phase_rows, fptr[p + 1] - fptr[p]);
+    for (size_t p = 0; p + 1 < bptr.size(); p++) s->max_phase_rows = std::max(s->max_phase_rows, bptr[p + 1] - bptr[p]);
     s->omega = omega;
     s->num_levels = num_levels;
     s->prepared = method;
@@ -530,6 +547,13 @@ int feec_system_destroy(feec_system* s) {
     if (s->ev0) cudaEventDestroy(s->ev0);
     if (s->ev1) cudaEventDestroy(s->ev1);
     delete s;
+    return FEEC_OK;
+}
+
+int feec_system_set_launch(feec_system* s, int blocks, int lanes) {
+    if (!s || blocks < 0 || lanes < 0 || lanes > 32 || (lanes & (lanes - 1)) != 0) return FEEC_BADARG;
+    s->user_blocks = blocks;
+    s->user_lanes = lanes;
     return FEEC_OK;
 }
 

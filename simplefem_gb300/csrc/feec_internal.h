@@ -37,7 +37,8 @@ struct PcgArgs {
     int n;
     const int* rp; const int* ci; const T* val;   // rows ordered [L | E | U]
     const int* lsplit; const int* usplit;         // L = [rp, lsplit), E = [lsplit, usplit), U = [usplit, rp+1)
-    const T* diag; const T* b;
+    const T* wd; const T* sd;                     // omega / D (0 where D == 0) and D (2 - omega) / omega
+    const T* b;
     T* x; T* r; T* d; T* z; T* m; T* q;
     int nf; const int* fptr;                      // forward phases: rows [fptr[p], fptr[p+1])
     int nbw; const int* bptr; const int* brows;   // backward phases: rows brows[bptr[p] .. bptr[p+1])
@@ -83,6 +84,8 @@ cudaError_t launch_scatter_f64(int n, const int* perm, const double* src, double
 cudaError_t launch_gather_to_f32(int n, const int* perm, const double* src, float* dst, cudaStream_t s);
 cudaError_t launch_diagonal_f64(int n, const int* A, const int* C, const double* V, double* d, cudaStream_t s);
 cudaError_t launch_cast_f64_f32(size_t n, const double* src, float* dst, cudaStream_t s);
+cudaError_t launch_sweep_factors(int n, const double* diag, double omega, double* wd, double* sd, float* wd32,
+                                 float* sd32, cudaStream_t s);
 // Mixed precision helpers.
 cudaError_t launch_scaled_cast(int n, const double* r, const double* inv_norm_dev, float* r32, cudaStream_t s);
 cudaError_t launch_update_x(int n, const int* perm, const float* c32, const double* norm_dev, double* x, cudaStream_t s);

@@ -100,13 +100,22 @@ __global__ void __launch_bounds__(kThreads) cg_persistent(CgArgs<T> a) {
     grid_sum<1>(p_rr, rr);
     double r_r = rr[0];
 
+    // Scalar control (stop tests, alpha, beta) is evaluated by thread 0 only and
+    // broadcast through shared memory: FP64 issues at 2 lanes/clk/SM on this part,
+    // so redundant per-thread FP64 scalar work would cost more than the sweeps.
+    __shared__ double s_scal[2];
+    __shared__ int s_ctl;
     int K = 0;
     int status = FEEC_MAXITER;
     double d_Ad = 0.0;
     while (K < a.max_iter) {
-        if (a.print_modulo > 0 && K % a.print_modulo == 0 && blockIdx.x == 0 && threadIdx.x == 0)
-            printf("(%d/%d)   INTERIM: Residual norm is %.9le < %.9le\n", K, n, sqrt(r_r), a.print_tol);
-        if (fabs(r_r) < a.tol2) { status = FEEC_OK; break; }                        // :116-119
+        if (threadIdx.x == 0) {
+            if (a.print_modulo > 0 && K % a.print_modulo == 0 && blockIdx.x == 0)
+                printf("(%d/%d)   INTERIM: Residual norm is %.9le < %.9le\n", K, n, sqrt(r_r), a.print_tol);
+            s_ctl = fabs(r_r) < a.tol2 ? 1 : 0;                                          // :116-119
+        }
+        __syncthreads();
+        if (s_ctl) { status = FEEC_OK; break; }
 
         // q = A d, d.q                                                               :126-139
         Acc adq = AT::zero();
@@ -123,11 +132,18 @@ __global__ void __launch_bounds__(kThreads) cg_persistent(CgArgs<T> a) {
         double dq[1];
         grid_sum<1>(p_dq, dq);
         d_Ad = dq[0];
+        if (threadIdx.x == 0) {
+            int ctl = 0;
+            if (!isfinite(r_r) || r_r < 0.0 || !isfinite(d_Ad) || d_Ad < 0.0) ctl = 1;   // :142-151
+            else if (sqrt(fabs(d_Ad)) < kMachineEpsilon) ctl = 2;                         // :153-157
+            s_ctl = ctl;
+            s_scal[0] = r_r / d_Ad;
+        }
+        __syncthreads();
+        if (s_ctl == 1) { status = FEEC_BREAKDOWN; break; }
+        if (s_ctl == 2) { status = FEEC_SMALL_ENERGY; break; }
 
-        if (!isfinite(r_r) || r_r < 0.0 || !isfinite(d_Ad) || d_Ad < 0.0) { status = FEEC_BREAKDOWN; break; }  // :142-151
-        if (sqrt(fabs(d_Ad)) < kMachineEpsilon) { status = FEEC_SMALL_ENERGY; break; }                        // :153-157
-
-        const T alpha = (T)(r_r / d_Ad);
+        const T alpha = (T)s_scal[0];
         Acc arr = AT::zero();
         for (int i = tid; i < n; i += nthr) {                                          // :158-173
             const T di = a.d[i];
@@ -140,7 +156,9 @@ __global__ void __launch_bounds__(kThreads) cg_persistent(CgArgs<T> a) {
         if (!grid_barrier(a.st, epoch, 3)) return;
         grid_sum<1>(p_rr, rr);
         const double r_r_new = rr[0];
-        const T beta = (T)(r_r_new / r_r);                                             // :175-183
+        if (threadIdx.x == 0) s_scal[1] = r_r_new / r_r;                               // :175-183
+        __syncthreads();
+        const T beta = (T)s_scal[1];
         r_r = r_r_new;
         for (int i = tid; i < n; i += nthr) a.d[i] = a.r[i] + beta * a.d[i];
         if (!grid_barrier(a.st, epoch, 4)) return;
@@ -163,15 +181,17 @@ __global__ void __launch_bounds__(kThreads) pcg_persistent(PcgArgs<T> a) {
     const int nthr = gridDim.x * blockDim.x;
     double* p_dq = a.partials;
     double* p_zr = a.partials + gridDim.x;   // (z.r, r.r) pairs
-    const T omega = (T)a.omega;
-    const T two_minus_over = (T)((2.0 - a.omega) / a.omega);
+    // Per-row factors prepared at setup: wd = omega / D (0 where D == 0, the rows the
+    // reference skips), sd = D (2 - omega) / omega. The sweeps then need no division.
+    __shared__ double s_scal[2];
+    __shared__ int s_ctl;
 
     // ---- restart (sparsesolver.cpp:1072-1175 / 506-588) ----
     Acc arr = AT::zero();
     FEEC_FOR_ROW_GROUPS(0, n, i, act) {                      // r = b - A x for rows with D != 0
         const int lo = act ? __ldg(&a.rp[i]) : 0, hi = act ? __ldg(&a.rp[i + 1]) : 0;
         const T s = seg_dot<T, LANES>(a.ci, a.val, a.x, lo, hi, lane);
-        if (act && lane == 0 && __ldg(&a.diag[i]) != T(0)) {
+        if (act && lane == 0 && __ldg(&a.wd[i]) != T(0)) {
             const T ri = __ldg(&a.b[i]) - s;
             a.r[i] = ri;
             arr = AT::add(arr, ri * ri);
@@ -184,8 +204,8 @@ __global__ void __launch_bounds__(kThreads) pcg_persistent(PcgArgs<T> a) {
             const int lo = act ? __ldg(&a.rp[i]) : 0, hi = act ? __ldg(&a.lsplit[i]) : 0;
             const T s = seg_dot<T, LANES>(a.ci, a.val, a.m, lo, hi, lane);
             if (act && lane == 0) {
-                const T D = __ldg(&a.diag[i]);
-                if (D != T(0)) a.m[i] = (a.r[i] - s) * omega / D;
+                const T w = __ldg(&a.wd[i]);
+                if (w != T(0)) a.m[i] = (a.r[i] - s) * w;
             }
         }
         if (!grid_barrier(a.st, epoch, 11)) return;
@@ -198,12 +218,11 @@ __global__ void __launch_bounds__(kThreads) pcg_persistent(PcgArgs<T> a) {
             const int lo = act ? __ldg(&a.usplit[i]) : 0, hi = act ? __ldg(&a.rp[i + 1]) : 0;
             const T s = seg_dot<T, LANES>(a.ci, a.val, a.z, lo, hi, lane);
             if (act && lane == 0) {
-                const T D = __ldg(&a.diag[i]);
-                if (D != T(0)) {
-                    T mi = a.m[i] * D;
-                    mi *= two_minus_over;
+                const T w = __ldg(&a.wd[i]);
+                if (w != T(0)) {
+                    const T mi = a.m[i] * __ldg(&a.sd[i]);
                     a.m[i] = mi;
-                    const T zi = (mi - s) * omega / D;
+                    const T zi = (mi - s) * w;
                     a.z[i] = zi;
                     a.d[i] = zi;
                     azr = AT::add(azr, zi * a.r[i]);
@@ -224,17 +243,23 @@ __global__ void __launch_bounds__(kThreads) pcg_persistent(PcgArgs<T> a) {
     int status = FEEC_MAXITER;
     double d_Ad = 0.0;
     while (K < a.max_iter) {
-        if (a.print_modulo > 0 && K % a.print_modulo == 0 && blockIdx.x == 0 && threadIdx.x == 0)
-            printf("(%d/%d)   INTERIM: Residual norm is %.9le < %.9le\n", K, n, sqrt(z_r), a.print_tol);
-        if (a.use_zr_rule && fabs(z_r) < a.tol2) { status = FEEC_OK; break; }         // :1187-1190
-        if (a.rr_stop > 0.0 && r_r < a.rr_stop) { status = FEEC_OK; break; }
+        if (threadIdx.x == 0) {
+            if (a.print_modulo > 0 && K % a.print_modulo == 0 && blockIdx.x == 0)
+                printf("(%d/%d)   INTERIM: Residual norm is %.9le < %.9le\n", K, n, sqrt(z_r), a.print_tol);
+            int ctl = 0;
+            if (a.use_zr_rule && fabs(z_r) < a.tol2) ctl = 1;                         // :1187-1190
+            if (a.rr_stop > 0.0 && r_r < a.rr_stop) ctl = 1;
+            s_ctl = ctl;
+        }
+        __syncthreads();
+        if (s_ctl) { status = FEEC_OK; break; }
 
         Acc adq = AT::zero();                                                          // :1197-1212
         FEEC_FOR_ROW_GROUPS(0, n, i, act) {
             const int lo = act ? __ldg(&a.rp[i]) : 0, hi = act ? __ldg(&a.rp[i + 1]) : 0;
             const T s = seg_dot<T, LANES>(a.ci, a.val, a.d, lo, hi, lane);
             if (act && lane == 0) {
-                const T qi = (__ldg(&a.diag[i]) != T(0)) ? s : T(0);
+                const T qi = (__ldg(&a.wd[i]) != T(0)) ? s : T(0);
                 a.q[i] = qi;
                 adq = AT::add(adq, a.d[i] * qi);
             }
@@ -244,10 +269,18 @@ __global__ void __launch_bounds__(kThreads) pcg_persistent(PcgArgs<T> a) {
         double dq[1];
         grid_sum<1>(p_dq, dq);
         d_Ad = dq[0];
-        if (!isfinite(z_r) || z_r < 0.0 || !isfinite(d_Ad) || d_Ad < 0.0) { status = FEEC_BREAKDOWN; break; }
-        if (sqrt(fabs(d_Ad)) < kMachineEpsilon) { status = FEEC_SMALL_ENERGY; break; }
+        if (threadIdx.x == 0) {
+            int ctl = 0;
+            if (!isfinite(z_r) || z_r < 0.0 || !isfinite(d_Ad) || d_Ad < 0.0) ctl = 1;
+            else if (sqrt(fabs(d_Ad)) < kMachineEpsilon) ctl = 2;
+            s_ctl = ctl;
+            s_scal[0] = z_r / d_Ad;
+        }
+        __syncthreads();
+        if (s_ctl == 1) { status = FEEC_BREAKDOWN; break; }
+        if (s_ctl == 2) { status = FEEC_SMALL_ENERGY; break; }
 
-        const T alpha = (T)(z_r / d_Ad);
+        const T alpha = (T)s_scal[0];
         arr = AT::zero();
         for (int p = 0; p < a.nf; p++) {                                               // :1230-1261
             const int lo_r = __ldg(&a.fptr[p]), hi_r = __ldg(&a.fptr[p + 1]);
@@ -255,13 +288,13 @@ __global__ void __launch_bounds__(kThreads) pcg_persistent(PcgArgs<T> a) {
                 const int lo = act ? __ldg(&a.rp[i]) : 0, hi = act ? __ldg(&a.lsplit[i]) : 0;
                 const T s = seg_dot<T, LANES>(a.ci, a.val, a.m, lo, hi, lane);
                 if (act && lane == 0) {
-                    const T D = __ldg(&a.diag[i]);
-                    if (D != T(0)) {
+                    const T w = __ldg(&a.wd[i]);
+                    if (w != T(0)) {
                         a.x[i] += alpha * a.d[i];
                         const T ri = a.r[i] - alpha * a.q[i];
                         a.r[i] = ri;
                         arr = AT::add(arr, ri * ri);
-                        a.m[i] = (ri - s) * omega / D;
+                        a.m[i] = (ri - s) * w;
                     }
                 }
             }
@@ -275,12 +308,11 @@ __global__ void __launch_bounds__(kThreads) pcg_persistent(PcgArgs<T> a) {
                 const int lo = act ? __ldg(&a.usplit[i]) : 0, hi = act ? __ldg(&a.rp[i + 1]) : 0;
                 const T s = seg_dot<T, LANES>(a.ci, a.val, a.z, lo, hi, lane);
                 if (act && lane == 0) {
-                    const T D = __ldg(&a.diag[i]);
-                    if (D != T(0)) {
-                        T mi = a.m[i] * D;
-                        mi *= two_minus_over;
+                    const T w = __ldg(&a.wd[i]);
+                    if (w != T(0)) {
+                        const T mi = a.m[i] * __ldg(&a.sd[i]);
                         a.m[i] = mi;
-                        const T zi = (mi - s) * omega / D;
+                        const T zi = (mi - s) * w;
                         a.z[i] = zi;
                         azr = AT::add(azr, zi * a.r[i]);
                     }
@@ -295,10 +327,12 @@ __global__ void __launch_bounds__(kThreads) pcg_persistent(PcgArgs<T> a) {
         grid_sum<2>(p_zr, zr2);
         const double z_r_new = zr2[0];
         r_r = zr2[1];
-        const T beta = (T)(z_r_new / z_r);                                             // :1309-1318
+        if (threadIdx.x == 0) s_scal[1] = z_r_new / z_r;                               // :1309-1318
+        __syncthreads();
+        const T beta = (T)s_scal[1];
         z_r = z_r_new;
         for (int i = tid; i < n; i += nthr) {
-            if (__ldg(&a.diag[i]) != T(0)) a.d[i] = a.z[i] + beta * a.d[i];
+            if (__ldg(&a.wd[i]) != T(0)) a.d[i] = a.z[i] + beta * a.d[i];
         }
         if (!grid_barrier(a.st, epoch, 18)) return;
         K++;

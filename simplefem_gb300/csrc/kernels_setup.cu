@@ -156,6 +156,20 @@ __global__ void cast_kernel(size_t n, const double* __restrict__ src, float* __r
         dst[i] = (float)src[i];
 }
 
+// Sweep factors of the SSOR sweeps: wd = omega / D and sd = D (2 - omega) / omega
+// (wd = 0 marks the rows with D == 0 that the reference skips).
+__global__ void sweep_factors_kernel(int n, const double* __restrict__ diag, double omega, double* __restrict__ wd,
+                                     double* __restrict__ sd, float* __restrict__ wd32, float* __restrict__ sd32) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double D = diag[i];
+    const double w = (D == 0.0) ? 0.0 : omega / D;
+    const double t = D * ((2.0 - omega) / omega);
+    wd[i] = w; sd[i] = t;
+    wd32[i] = (D == 0.0) ? 0.0f : (float)(omega / D);
+    sd32[i] = (float)t;
+}
+
 // r32[i] = r[i] * (*inv_norm)   (scaled residual handed to the FP32 inner solve)
 __global__ void scaled_cast_kernel(int n, const double* __restrict__ r, const double* __restrict__ inv_norm,
                                    float* __restrict__ r32) {
@@ -322,6 +336,11 @@ cudaError_t launch_cast_f64_f32(size_t n, const double* src, float* dst, cudaStr
     int grid = (int)((n + kBlock - 1) / kBlock);
     if (grid > 4096) grid = 4096;
     return launch(cast_kernel, grid, kBlock, s, n, src, dst);
+}
+
+cudaError_t launch_sweep_factors(int n, const double* diag, double omega, double* wd, double* sd, float* wd32,
+                                 float* sd32, cudaStream_t s) {
+    return launch(sweep_factors_kernel, grid_for(n, kBlock), kBlock, s, n, diag, omega, wd, sd, wd32, sd32);
 }
 
 cudaError_t launch_scaled_cast(int n, const double* r, const double* inv_norm_dev, float* r32, cudaStream_t s) {

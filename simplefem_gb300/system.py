@@ -81,6 +81,10 @@ class System:
         _native.check(self._lib.feec_system_apply(self._h, _ptr(x), _ptr(y), float(scaling), _stream()),
                       "feec_system_apply")
 
+    def set_launch(self, blocks=0, lanes=0):
+        """Override the persistent grid size / lanes per row (0 = automatic)."""
+        _native.check(self._lib.feec_system_set_launch(self._h, int(blocks), int(lanes)), "feec_system_set_launch")
+
     def memory_bytes(self) -> int:
         b = ctypes.c_size_t(0)
         _native.check(self._lib.feec_system_memory(self._h, ctypes.byref(b)), "feec_system_memory")
