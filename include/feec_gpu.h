@@ -148,6 +148,19 @@ int feec_system_memory(const feec_system* sys, size_t* bytes);
 
 int feec_system_destroy(feec_system* sys);
 
+/* No counterpart in the reference. Plain CG (reference stopping rule) for callers
+ * that cannot allocate device memory during a solve: every pointer is a device
+ * pointer the caller owns, and the solver's scratch is a fixed 16 MiB file-scope
+ * device array of this library instead of an allocation. At most 1,048,576 rows
+ * (larger N returns FEEC_BADARG). All calls share that array: calls that overlap
+ * on the GPU race and must be serialised by the caller. The first call on a
+ * device looks up the array's address; make it before any stream capture.
+ * max_iter <= 0 means N; `stream` is a cudaStream_t (NULL = legacy default). */
+int feec_cg_csr_noalloc(int N, double* x, const double* b,
+                        const int* A, const int* C, const double* V,
+                        double* residual, double precision, int max_iter,
+                        feec_solve_info* info, void* stream);
+
 /* ---------------------------------------------------------------------------
  * Library information.
  * ------------------------------------------------------------------------- */
