@@ -1,16 +1,16 @@
 """Benchmark: solves/s at 1e-10 relative residual on the 3D P2 Lagrange operator
 refined 5 times (N = 274,625, nnz = 7,678,721), multicolor (Rainbow) SSOR-PCG.
 
-One step = one complete solve of A x = b from x0 = 0 to a true FP64 relative
-residual <= 1e-10, with a fresh seeded U[-1,1] right-hand side. The headline
-`value` is the mixed-precision product path (FP32 inner Rainbow SSOR-PCG with
-compensated dots inside an FP64 defect-correction loop) with b and x resident
-in HBM; `e2e` is the same solve through the public System API with the
-right-hand side copied in from pinned host memory and the solution copied back
-inside the timed region. The plain FP64 GPU CG and the FP64 drop-in Rainbow
-solver (the reference's own stopping rule) on the same matrix are reported beside
-it, together with the oracle (a plain-C restatement of the reference solver)
-timed on the host cores.
+One step = one batch of `--batch` independent solves (seeded U[-1,1] right-hand
+sides, x0 = 0), each to a true FP64 relative residual <= 1e-10, by the batched
+mixed-precision engine (FP32 inner Rainbow SSOR-PCG with compensated dots inside
+FP64 defect correction, one thread block per 4 right-hand sides) with the
+right-hand sides and solutions resident in HBM. `e2e` is the same batch through
+the public System API with the right-hand sides copied in from pinned host memory
+and the solutions copied back inside the timed region. Beside it: one solve on the
+whole GPU (latency p50/p99), the plain FP64 GPU CG and the FP64 drop-in Rainbow
+solver (the reference's own stopping rule) on the same matrix, and the oracle (a
+plain-C restatement of the reference solver) timed on the host cores.
 
 `python bench.py --impl reference` times the reference algorithm on the host
 cores instead (the oracle restatement with OpenMP, the reference's own
@@ -182,16 +182,99 @@ def run_ours(args):
     sysm = System(A, C, V)
     sysm.set_rainbow(diag, 1.0, rb.num_colors, rb.F, rb.B, rb.R)
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)   # 256 MB > L2 (129 MB)
+    stream = torch.cuda.current_stream()
+    B_RHS = args.batch
+    K_TEAM = 4
 
-    def rhs(step):
-        return workloads.uniform_vector(1000 + step + 7919 * rank, n)
+    def rhs_block(step, count):
+        return np.stack([workloads.uniform_vector(1000 + 100003 * rank + 4099 * step + j, n) for j in range(count)])
 
-    def timed_solves(method, mode, steps, warmup, seed_base=0):
-        per = []
-        infos = []
-        stream = torch.cuda.current_stream()
-        for step in range(warmup + steps):
-            b = torch.from_numpy(rhs(seed_base + step)).to(dev)
+    # ---------------- headline: batched mixed-precision Rainbow SSOR-PCG ----------------
+    Bdev = torch.empty((B_RHS, n), dtype=torch.float64, device=dev)
+    Xdev = torch.empty((B_RHS, n), dtype=torch.float64, device=dev)
+    per, infos_all = [], []
+    for step in range(args.warmup):                       # untimed warm-up steps
+        Bdev.copy_(torch.from_numpy(rhs_block(step, B_RHS)))
+        Xdev.zero_()
+        sysm.solve_batch(Bdev, Xdev, method="rainbow", mode="mixed", precision=PRECISION, rhs_per_team=K_TEAM)
+    clocks = ClockSampler(local)
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    launches0 = lib.feec_kernel_launches()
+    clocks.start()
+    for step in range(args.steps):
+        Bdev.copy_(torch.from_numpy(rhs_block(args.warmup + step, B_RHS)))
+        Xdev.zero_()
+        flush.zero_()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        infos = sysm.solve_batch(Bdev, Xdev, method="rainbow", mode="mixed", precision=PRECISION, rhs_per_team=K_TEAM)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        per.append(e0.elapsed_time(e1))
+        infos_all.append(infos)
+    clock_info = clocks.stop()
+    launches = lib.feec_kernel_launches() - launches0
+    total_ms = float(sum(per))
+    if world > 1:
+        t = torch.tensor([total_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+        dist.barrier()
+    value = world * args.steps * B_RHS / (total_ms / 1000.0)
+    flat = [i for infos in infos_all for i in infos]
+    assert all(i["status"] == 0 and 0 <= i["true_relres"] <= PRECISION for i in flat), "batched solve missed 1e-10"
+    inner_iters = [i["iterations"] for i in flat]
+    outer_iters = [i["outer_iterations"] for i in flat]
+
+    # roofline of the batched kernel: algorithmic bytes (matrix once per team iteration,
+    # vectors per right-hand side) over the kernel's event-timed duration
+    teams = (B_RHS + K_TEAM - 1) // K_TEAM
+    mat_b = 8 * (2 * nnz - n) + 12 * (n + 1)
+    vec_b = 17 * 4 * n
+    outer_b = 12 * nnz + 4 * (n + 1) + 24 * n + 20 * n
+    per_step_bytes = 0
+    for infos in infos_all:
+        its = [i["iterations"] for i in infos]
+        outs = [i["outer_iterations"] for i in infos]
+        for t0 in range(teams):
+            cols = range(t0 * K_TEAM, min(B_RHS, (t0 + 1) * K_TEAM))
+            team_it = max(its[j] for j in cols)
+            per_step_bytes += team_it * mat_b + sum(its[j] for j in cols) * vec_b
+            per_step_bytes += (max(outs[j] for j in cols) + 1) * (12 * nnz + 4 * (n + 1)) + \
+                sum(outs[j] + 1 for j in cols) * (outer_b - 12 * nnz - 4 * (n + 1))
+    per_step_bytes /= len(infos_all)
+    peak, peak_kind = measured_peaks()
+    achieved = per_step_bytes / (total_ms / args.steps / 1000.0) / 1e9
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": None, "kernel": "batched_solve_kernel<float,4,rainbow>", "launches_per_step": 1,
+                "bytes_per_launch": per_step_bytes, "ms_per_launch": total_ms / args.steps,
+                "peak_kind": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)"}
+
+    # ---------------- e2e: pinned host B -> device, batched solve, device X -> pinned host ----------------
+    hB = torch.empty((B_RHS, n), dtype=torch.float64).pin_memory()
+    hX = torch.empty((B_RHS, n), dtype=torch.float64).pin_memory()
+    e2e_per = []
+    for step in range(min(2, args.steps)):
+        hB.copy_(torch.from_numpy(rhs_block(500 + step, B_RHS)))
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        Bdev.copy_(hB, non_blocking=True)
+        Xdev.zero_()
+        sysm.solve_batch(Bdev, Xdev, method="rainbow", mode="mixed", precision=PRECISION, rhs_per_team=K_TEAM)
+        hX.copy_(Xdev, non_blocking=True)
+        torch.cuda.synchronize()
+        e2e_per.append(time.perf_counter() - t0)
+    e2e_value = world * B_RHS * len(e2e_per) / sum(e2e_per)
+
+    # ---------------- single-solve latency (whole GPU per solve) and the FP64 baselines ----------------
+    def single(method, mode, count, seed):
+        out, inf = [], []
+        for k in range(count + 1):
+            b = torch.from_numpy(workloads.uniform_vector(seed + k, n)).to(dev)
             x = torch.zeros(n, dtype=torch.float64, device=dev)
             flush.zero_()
             torch.cuda.synchronize()
@@ -200,73 +283,16 @@ def run_ours(args):
             info = sysm.solve(b, x, method=method, mode=mode, precision=PRECISION)
             e1.record(stream)
             torch.cuda.synchronize()
-            if step >= warmup:
-                per.append(e0.elapsed_time(e1))
-                infos.append(info)
-        return per, infos
+            if k > 0:                                   # first call is a warm-up
+                out.append(e0.elapsed_time(e1)); inf.append(info)
+        return out, inf
 
-    # warm-up of the headline path, then the timed region (clocks sampled during it)
-    clocks = ClockSampler(local)
-    if world > 1:
-        dist.barrier()
-    torch.cuda.synchronize()
-    launches0 = lib.feec_kernel_launches()
-    clocks.start()
-    per, infos = timed_solves("rainbow", "mixed", args.steps, args.warmup)
-    clock_info = clocks.stop()
-    launches = lib.feec_kernel_launches() - launches0
-    torch.cuda.synchronize()
-    total_ms = float(sum(per))
-    if world > 1:
-        t = torch.tensor([total_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
-        dist.barrier()
-    value = world * args.steps / (total_ms / 1000.0)
-    assert all(i["status"] == 0 and i["true_relres"] <= PRECISION for i in infos), infos
-    inner_iters = [i["iterations"] for i in infos]
-    outer_iters = [i["outer_iterations"] for i in infos]
-
-    # roofline of the dominant kernel: the FP32 inner persistent PCG launch
-    it_b = rainbow_iteration_bytes(n, nnz, 8, 4)
-    rs_b = rainbow_restart_bytes(n, nnz, 8, 4)
-    inner_bytes = sum(o * rs_b + k * it_b for o, k in zip(outer_iters, inner_iters))
-    inner_ms = sum(i["device_ms"] for i in infos)
-    launches_inner = sum(outer_iters)
-    peak, peak_kind = measured_peaks()
-    achieved = inner_bytes / (inner_ms / 1000.0) / 1e9
-    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": None, "kernel": "pcg_persistent<float>",
-                "bytes_per_launch": inner_bytes / launches_inner, "ms_per_launch": inner_ms / launches_inner,
-                "peak_kind": peak_kind}
-
-    # end to end: pinned host b -> device, solve, device -> pinned host x, all inside the timed region
-    e2e_per = []
-    hb = torch.empty(n, dtype=torch.float64).pin_memory()
-    hx = torch.empty(n, dtype=torch.float64).pin_memory()
-    db = torch.empty(n, dtype=torch.float64, device=dev)
-    for step in range(args.warmup + args.steps):
-        hb.copy_(torch.from_numpy(rhs(500 + step)))
-        flush.zero_()
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        db.copy_(hb, non_blocking=True)
-        x = torch.zeros(n, dtype=torch.float64, device=dev)
-        sysm.solve(db, x, method="rainbow", mode="mixed", precision=PRECISION)
-        hx.copy_(x, non_blocking=True)
-        torch.cuda.synchronize()
-        if step >= args.warmup:
-            e2e_per.append(time.perf_counter() - t0)
-    e2e_value = world * args.steps / sum(e2e_per)
-
-    # plain FP64 GPU CG and the FP64 drop-in Rainbow (reference stopping rule) on the same matrix
-    cg_steps = max(1, min(3, args.steps))
-    cg_per, cg_infos = timed_solves("cg", "fp64", cg_steps, 1, seed_base=2000)
-    rb64_per, rb64_infos = timed_solves("rainbow", "reference", max(1, min(5, args.steps)), 1, seed_base=3000)
-    fp64_rb_per, fp64_rb_infos = timed_solves("rainbow", "fp64", max(1, min(5, args.steps)), 1, seed_base=4000)
+    mixed1, mixed1_i = single("rainbow", "mixed", 5, 7000)
+    cg64, cg64_i = single("cg", "fp64", 3, 8000)
+    rb64, rb64_i = single("rainbow", "reference", 3, 9000)
 
     # drop-in host-pointer call (matrix uploaded inside the call, as the reference signature implies)
-    b0 = rhs(6000)
+    b0 = workloads.uniform_vector(6000, n)
     dropin = []
     for step in range(2):
         xh = np.zeros(n); res = np.zeros(n)
@@ -283,35 +309,44 @@ def run_ours(args):
         oracle.set_threads(threads)
         rbo = (rb.num_colors, rb.F, rb.B, rb.R)
         t0 = time.perf_counter()
-        Ko, _, _ = oracle.cg_rainbow(A, C, V, rhs(0), diag, rbo, 1.0, precision=PRECISION)
+        Ko, _, _ = oracle.cg_rainbow(A, C, V, workloads.uniform_vector(1000, n), diag, rbo, 1.0, precision=PRECISION)
         dt = time.perf_counter() - t0
         cpu = {"value": 1.0 / dt, "unit": "solves/s", "cores": threads, "kind": "port",
                "sample": f"1 full FP64 Rainbow SSOR-PCG solve of the workload ({Ko} iterations, reference "
                          f"stopping rule), oracle restatement with OpenMP"}
+
+    def rate(ms_list):
+        return len(ms_list) / (sum(ms_list) / 1000.0)
 
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD_NAME, "solver": "mixed: FP32 inner Rainbow SSOR-PCG (compensated dots) + "
-                       "FP64 defect correction", "l2": "flushed (256 MB write) before every solve",
-                       "replicas": "independent solves per GPU (replicas only)"},
-            "p50_ms": float(np.percentile(per, 50)), "p99_ms": float(np.percentile(per, 99)),
+            "config": {"workload": WORKLOAD_NAME,
+                       "solver": "batched mixed precision: FP32 inner Rainbow SSOR-PCG (compensated dots) inside "
+                                 "FP64 defect correction, one thread block per 4 right-hand sides",
+                       "batch": B_RHS, "rhs_per_team": K_TEAM,
+                       "l2": "flushed (256 MB write) before every timed step; working set > L2",
+                       "replicas": "independent batches per GPU (replicas only)"},
+            "batch_latency_ms": {"p50": float(np.percentile(per, 50)), "p99": float(np.percentile(per, 99))},
+            "p50_ms": float(np.percentile(mixed1, 50)), "p99_ms": float(np.percentile(mixed1, 99)),
+            "latency_note": "p50/p99 of one solve on the whole GPU (mixed, persistent cooperative kernel); "
+                            "batch_latency_ms is the time to finish a whole batch",
             "inner_iterations": int(np.median(inner_iters)), "outer_iterations": int(np.median(outer_iters)),
-            "true_relres_max": max(i["true_relres"] for i in infos),
-            "fp64_plain_cg": {"solves_per_s": cg_steps / (sum(cg_per) / 1000.0), "ms": float(np.median(cg_per)),
-                              "iterations": int(np.median([i["iterations"] for i in cg_infos]))},
-            "fp64_rainbow_reference_rule": {"solves_per_s": len(rb64_per) / (sum(rb64_per) / 1000.0),
-                                            "ms": float(np.median(rb64_per)),
-                                            "iterations": int(np.median([i["iterations"] for i in rb64_infos]))},
-            "fp64_rainbow_true_residual": {"solves_per_s": len(fp64_rb_per) / (sum(fp64_rb_per) / 1000.0),
-                                           "ms": float(np.median(fp64_rb_per)),
-                                           "iterations": int(np.median([i["iterations"] for i in fp64_rb_infos]))},
+            "true_relres_max": max(i["true_relres"] for i in flat),
+            "single_solve_mixed": {"solves_per_s": rate(mixed1), "ms": float(np.median(mixed1)),
+                                   "iterations": int(np.median([i["iterations"] for i in mixed1_i]))},
+            "fp64_plain_cg": {"solves_per_s": rate(cg64), "ms": float(np.median(cg64)),
+                              "iterations": int(np.median([i["iterations"] for i in cg64_i])),
+                              "note": "plain FP64 CG on the whole GPU, stop at true relres 1e-10"},
+            "fp64_rainbow_reference_rule": {"solves_per_s": rate(rb64), "ms": float(np.median(rb64)),
+                                            "iterations": int(np.median([i["iterations"] for i in rb64_i]))},
             "dropin_host_call_ms": 1000 * float(np.median(dropin)),
             "roofline": roofline,
             "cpu_baseline": cpu,
-            "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": 8 * n, "d2h_bytes_per_step": 8 * n},
+            "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": 8 * n * B_RHS,
+                    "d2h_bytes_per_step": 8 * n * B_RHS},
             "gpu_launches": int(launches),
             "clocks": clock_info,
         }
@@ -324,10 +359,11 @@ def run_ours(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--batch", type=int, default=1216, help="right-hand sides per batched step")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

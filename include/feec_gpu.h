@@ -135,6 +135,25 @@ int feec_system_solve(feec_system* sys, int method, int mode, double* x, const d
                       double* residual, double precision, int max_iter,
                       feec_solve_info* info, void* stream);
 
+/* Batched solves of one system with many right-hand sides (FEEC_MODE_MIXED or
+ * FEEC_MODE_FP64; FEEC_METHOD_CG or FEEC_METHOD_RAINBOW): X and B are device
+ * arrays of nrhs columns of N doubles (column j at X + j*N). One thread block
+ * advances rhs_per_team columns (1, 2 or 4; 0 = automatic) through a complete
+ * solve; blocks take columns from a queue until none are left. infos (host,
+ * nrhs entries, may be NULL) receives each column's result. */
+int feec_system_solve_batch(feec_system* sys, int method, int mode, int nrhs, double* X, const double* B,
+                            double precision, int max_iter, int rhs_per_team,
+                            feec_solve_info* infos, void* stream);
+
+/* Batched solves of many systems, one right-hand side each (device pointers
+ * x[i], b[i] of systems[i]->N doubles; host arrays of pointers). Systems are
+ * processed largest first, one thread block per system. For
+ * FEEC_METHOD_RAINBOW every system must have been prepared with
+ * feec_system_set_rainbow. */
+int feec_solve_many(int nsys, feec_system* const* systems, int method, int mode,
+                    double* const* x, const double* const* b, double precision, int max_iter,
+                    feec_solve_info* infos, void* stream);
+
 /* y = scaling * A * x with device pointers. */
 int feec_system_apply(feec_system* sys, const double* x, double* y, double scaling, void* stream);
 

@@ -82,6 +82,9 @@ def gpu():
         L.feec_system_set_ssor.argtypes = [_vp, _vp, _dp, _ip]
         L.feec_system_solve.argtypes = [_vp, _ip, _ip, _vp, _vp, _vp, _dp, _ip, _infop, _vp]
         L.feec_system_apply.argtypes = [_vp, _vp, _vp, _dp, _vp]
+        L.feec_system_solve_batch.argtypes = [_vp, _ip, _ip, _ip, _vp, _vp, _dp, _ip, _ip, _infop, _vp]
+        L.feec_solve_many.argtypes = [_ip, ctypes.POINTER(_vp), _ip, _ip, ctypes.POINTER(_vp), ctypes.POINTER(_vp),
+                                      _dp, _ip, _infop, _vp]
         L.feec_system_set_launch.argtypes = [_vp, _ip, _ip]
         L.feec_system_memory.argtypes = [_vp, ctypes.POINTER(ctypes.c_size_t)]
         L.feec_system_destroy.argtypes = [_vp]

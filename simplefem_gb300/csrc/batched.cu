@@ -1,0 +1,252 @@
+// Host side of the batched engine: SELL-32 preparation of a system and the two
+// batched entry points of the C ABI (many right-hand sides of one system, or
+// many systems with one right-hand side each).
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+#include <vector>
+
+#include "feec_batched.h"
+#include "feec_device.cuh"
+#include "feec_system.h"
+
+using namespace feec;
+
+namespace {
+
+// Builds (once per system and method) the SELL-32 layout: slices of 32 rows that
+// never cross a color, blocks [L | E | U] per slice.
+int sell_prepare(feec_system* s, int method) {
+    if (s->sell_method == method) return FEEC_OK;
+    if (method == FEEC_METHOD_RAINBOW && s->prepared != FEEC_METHOD_RAINBOW) return FEEC_BADARG;
+    if (method != FEEC_METHOD_RAINBOW && method != FEEC_METHOD_CG) return FEEC_BADARG;
+    s->sell.release();
+    s->sell.stream = s->stream;
+    cudaStream_t st = s->stream;
+    const int n = s->n;
+    // color ranges in the permuted numbering
+    std::vector<int> ranges;
+    if (method == FEEC_METHOD_RAINBOW) {
+        ranges.resize((size_t)s->nf + 1);
+        FEEC_TRY(cudaMemcpyAsync(ranges.data(), s->fptr, sizeof(int) * ranges.size(), cudaMemcpyDeviceToHost, st));
+        FEEC_TRY(cudaStreamSynchronize(st));
+    } else {
+        ranges = {0, n};
+    }
+    const int ncolors = (int)ranges.size() - 1;
+    std::vector<int> row0, nrow, cslice(1, 0);
+    for (int c = 0; c < ncolors; c++) {
+        for (int r = ranges[c]; r < ranges[c + 1]; r += 32) {
+            row0.push_back(r);
+            nrow.push_back(std::min(32, ranges[c + 1] - r));
+        }
+        cslice.push_back((int)row0.size());
+    }
+    const int ns = (int)row0.size();
+    DevArena& M = s->sell;
+    FEEC_TRY(M.alloc(s->slice_row0, ns)); FEEC_TRY(M.alloc(s->slice_nrow, ns)); FEEC_TRY(M.alloc(s->slice_len, ns));
+    FEEC_TRY(M.alloc(s->slice_off, ns)); FEEC_TRY(M.alloc(s->color_slice, cslice.size()));
+    FEEC_TRY(cudaMemcpyAsync(s->slice_row0, row0.data(), sizeof(int) * ns, cudaMemcpyHostToDevice, st));
+    FEEC_TRY(cudaMemcpyAsync(s->slice_nrow, nrow.data(), sizeof(int) * ns, cudaMemcpyHostToDevice, st));
+    FEEC_TRY(cudaMemcpyAsync(s->color_slice, cslice.data(), sizeof(int) * cslice.size(), cudaMemcpyHostToDevice, st));
+    const bool rb = method == FEEC_METHOD_RAINBOW;
+    const int* rp = rb ? s->rp : s->A;
+    const int* cin = rb ? s->ci : s->C;
+    const double* vin = rb ? s->val : s->V;
+    FEEC_TRY(launch_sell_lengths(ns, s->slice_row0, s->slice_nrow, rp, rb ? s->lsplit : nullptr,
+                                 rb ? s->usplit : nullptr, s->slice_len, st));
+    std::vector<int4> len((size_t)ns);
+    FEEC_TRY(cudaMemcpyAsync(len.data(), s->slice_len, sizeof(int4) * ns, cudaMemcpyDeviceToHost, st));
+    FEEC_TRY(cudaStreamSynchronize(st));
+    std::vector<long long> off((size_t)ns);
+    long long total = 0;
+    for (int i = 0; i < ns; i++) {
+        off[i] = total;
+        total += 32ll * (len[i].x + len[i].y + len[i].z);
+    }
+    FEEC_TRY(cudaMemcpyAsync(s->slice_off, off.data(), sizeof(long long) * ns, cudaMemcpyHostToDevice, st));
+    FEEC_TRY(M.alloc(s->sci, (size_t)total)); FEEC_TRY(M.alloc(s->sval32, (size_t)total));
+    FEEC_TRY(M.alloc(s->sval64, (size_t)total));
+    FEEC_TRY(launch_sell_fill(ns, s->slice_row0, s->slice_nrow, s->slice_len, s->slice_off, rp, rb ? s->lsplit : nullptr,
+                              rb ? s->usplit : nullptr, cin, vin, s->sci, s->sval32, s->sval64, st));
+    if (!rb) {
+        std::vector<int> id((size_t)n);
+        std::iota(id.begin(), id.end(), 0);
+        FEEC_TRY(M.alloc(s->ident, n));
+        FEEC_TRY(cudaMemcpyAsync(s->ident, id.data(), sizeof(int) * n, cudaMemcpyHostToDevice, st));
+    }
+    FEEC_TRY(cudaStreamSynchronize(st));
+    s->nslices = ns;
+    s->sell_ncolors = ncolors;
+    s->sell_entries = total;
+    s->sell_method = method;
+    return FEEC_OK;
+}
+
+SellView sell_view(const feec_system* s) {
+    SellView v{};
+    const bool rb = s->sell_method == FEEC_METHOD_RAINBOW;
+    v.n = s->n; v.nslices = s->nslices; v.ncolors = s->sell_ncolors;
+    v.perm = rb ? s->perm : s->ident;
+    v.slice_row0 = s->slice_row0; v.slice_nrow = s->slice_nrow; v.slice_len = s->slice_len; v.slice_off = s->slice_off;
+    v.color_slice = s->color_slice; v.ci = s->sci; v.val32 = s->sval32; v.val64 = s->sval64;
+    v.wd32 = rb ? s->wd32 : nullptr; v.sd32 = rb ? s->sd32 : nullptr;
+    v.wd64 = rb ? s->wd : nullptr; v.sd64 = rb ? s->sd : nullptr;
+    return v;
+}
+
+struct Job {
+    int system;
+    int nrhs;
+    int first;
+    const double* b[kBatchMaxK];
+    double* x[kBatchMaxK];
+};
+
+int run_batch(cudaStream_t st, const std::vector<feec_system*>& systems, std::vector<Job>& jobs, int method, int mode,
+              int K, double precision, int max_iter, int nresults, feec_solve_info* infos, int teams) {
+    const int is_float = mode == FEEC_MODE_MIXED ? 1 : 0;
+    const size_t tsz = is_float ? sizeof(float) : sizeof(double);
+    // largest systems first, so the tail of the batch is short
+    std::stable_sort(jobs.begin(), jobs.end(),
+                     [&](const Job& a, const Job& b) { return systems[a.system]->n > systems[b.system]->n; });
+    DevArena tmp;
+    tmp.stream = st;
+    std::vector<SellView> views;
+    for (auto* s : systems) views.push_back(sell_view(s));
+    SellView* dviews = nullptr;
+    BatchItem* ditems = nullptr;
+    BatchResult* dres = nullptr;
+    int* dnext = nullptr;
+    FEEC_TRY(tmp.alloc(dviews, views.size()));
+    FEEC_TRY(tmp.alloc(ditems, jobs.size()));
+    FEEC_TRY(tmp.alloc(dres, (size_t)nresults));
+    FEEC_TRY(tmp.alloc(dnext, 1));
+    std::vector<BatchItem> items(jobs.size());
+    for (size_t i = 0; i < jobs.size(); i++) {
+        const Job& jb = jobs[i];
+        const size_t len = (size_t)systems[jb.system]->n * K;
+        BatchItem& it = items[i];
+        std::memset(&it, 0, sizeof(it));
+        it.system = jb.system; it.nrhs = jb.nrhs; it.first_result = jb.first;
+        for (int j = 0; j < kBatchMaxK; j++) { it.b[j] = jb.b[j]; it.x[j] = jb.x[j]; }
+        FEEC_TRY(tmp.alloc(it.xp, len)); FEEC_TRY(tmp.alloc(it.bp, len)); FEEC_TRY(tmp.alloc(it.r64, len));
+        char* w = nullptr;
+        FEEC_TRY(tmp.alloc(w, 6 * len * tsz));
+        it.r = w; it.d = w + len * tsz; it.z = w + 2 * len * tsz; it.m = w + 3 * len * tsz; it.q = w + 4 * len * tsz;
+        it.c = w + 5 * len * tsz;
+    }
+    FEEC_TRY(cudaMemcpyAsync(dviews, views.data(), sizeof(SellView) * views.size(), cudaMemcpyHostToDevice, st));
+    FEEC_TRY(cudaMemcpyAsync(ditems, items.data(), sizeof(BatchItem) * items.size(), cudaMemcpyHostToDevice, st));
+    FEEC_TRY(cudaMemsetAsync(dnext, 0, sizeof(int), st));
+    FEEC_TRY(cudaMemsetAsync(dres, 0, sizeof(BatchResult) * nresults, st));
+    BatchArgs a{};
+    a.systems = dviews; a.items = ditems; a.nitems = (int)items.size(); a.next_item = dnext; a.results = dres;
+    a.precision = precision;
+    a.inner_eta = is_float ? 2e-5 : 1e-30;
+    a.inner_margin = is_float ? 0.3 : 1.0;   // FP64 recursion tracks the true residual closely
+    a.max_iter = max_iter;
+    a.max_outer = is_float ? 12 : 4;
+    cudaEvent_t e0, e1;
+    FEEC_TRY(cudaEventCreate(&e0));
+    FEEC_TRY(cudaEventCreate(&e1));
+    FEEC_TRY(cudaEventRecord(e0, st));
+    FEEC_TRY(launch_batched(a, is_float, K, method == FEEC_METHOD_RAINBOW, teams, st));
+    FEEC_TRY(cudaEventRecord(e1, st));
+    std::vector<BatchResult> res((size_t)nresults);
+    FEEC_TRY(cudaMemcpyAsync(res.data(), dres, sizeof(BatchResult) * nresults, cudaMemcpyDeviceToHost, st));
+    FEEC_TRY(cudaStreamSynchronize(st));
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    tmp.release();
+    int worst = FEEC_OK;
+    for (int i = 0; i < nresults; i++) {
+        if (res[i].status != FEEC_OK && worst == FEEC_OK) worst = res[i].status;
+        if (infos) {
+            feec_solve_info& f = infos[i];
+            std::memset(&f, 0, sizeof(f));
+            f.status = res[i].status;
+            f.iterations = res[i].iterations;
+            f.outer_iterations = res[i].outer;
+            f.true_relres = res[i].relres;
+            f.tolerance = precision;
+            f.final_norm = res[i].relres;
+            f.device_ms = ms;
+            f.lanes_per_row = 1;
+            f.grid_blocks = teams;
+        }
+    }
+    FEEC_TRY(cudaStreamSynchronize(st));
+    return worst;
+}
+
+int pick_k(int mode, int rhs_per_team) {
+    const int kmax = batched_max_k(mode == FEEC_MODE_MIXED);
+    int K = rhs_per_team > 0 ? rhs_per_team : kmax;
+    if (K > kmax) K = kmax;
+    if (K != 1 && K != 2 && K != 4) K = K >= 4 ? 4 : (K >= 2 ? 2 : 1);
+    if (K > kmax) K = kmax;
+    return K;
+}
+
+}  // namespace
+
+extern "C" {
+
+int feec_system_solve_batch(feec_system* s, int method, int mode, int nrhs, double* X, const double* Bm,
+                            double precision, int max_iter, int rhs_per_team, feec_solve_info* infos, void* stream) {
+    if (!s || nrhs <= 0 || !X || !Bm || !(precision > 0.0)) return FEEC_BADARG;
+    if (method != FEEC_METHOD_CG && method != FEEC_METHOD_RAINBOW) return FEEC_BADARG;
+    if (mode != FEEC_MODE_MIXED && mode != FEEC_MODE_FP64) return FEEC_BADARG;
+    cudaStream_t keep = s->stream;
+    if (stream) { s->stream = (cudaStream_t)stream; }
+    int st = sell_prepare(s, method);
+    if (st == FEEC_OK) {
+        const int K = pick_k(mode, rhs_per_team);
+        std::vector<feec_system*> systems{s};
+        std::vector<Job> jobs;
+        const size_t n = (size_t)s->n;
+        for (int j0 = 0; j0 < nrhs; j0 += K) {
+            Job jb{};
+            jb.system = 0; jb.first = j0; jb.nrhs = std::min(K, nrhs - j0);
+            for (int j = 0; j < jb.nrhs; j++) { jb.b[j] = Bm + (j0 + j) * n; jb.x[j] = X + (j0 + j) * n; }
+            jobs.push_back(jb);
+        }
+        st = run_batch(s->stream, systems, jobs, method, mode, K, precision, max_iter > 0 ? max_iter : s->n, nrhs,
+                       infos, s->user_blocks);
+    }
+    s->stream = keep;
+    return st;
+}
+
+int feec_solve_many(int nsys, feec_system* const* systems, int method, int mode, double* const* x,
+                    const double* const* b, double precision, int max_iter, feec_solve_info* infos, void* stream) {
+    if (nsys <= 0 || !systems || !x || !b || !(precision > 0.0)) return FEEC_BADARG;
+    if (method != FEEC_METHOD_CG && method != FEEC_METHOD_RAINBOW) return FEEC_BADARG;
+    if (mode != FEEC_MODE_MIXED && mode != FEEC_MODE_FP64) return FEEC_BADARG;
+    cudaStream_t st = stream ? (cudaStream_t)stream : systems[0]->stream;
+    std::vector<feec_system*> sys(systems, systems + nsys);
+    int maxn = 0;
+    for (int i = 0; i < nsys; i++) {
+        if (!sys[i] || !x[i] || !b[i]) return FEEC_BADARG;
+        cudaStream_t keep = sys[i]->stream;
+        sys[i]->stream = st;
+        const int e = sell_prepare(sys[i], method);
+        sys[i]->stream = keep;
+        if (e != FEEC_OK) return e;
+        maxn = std::max(maxn, sys[i]->n);
+    }
+    std::vector<Job> jobs((size_t)nsys);
+    for (int i = 0; i < nsys; i++) {
+        Job& jb = jobs[i];
+        std::memset(&jb, 0, sizeof(jb));
+        jb.system = i; jb.nrhs = 1; jb.first = i; jb.b[0] = b[i]; jb.x[0] = x[i];
+    }
+    return run_batch(st, sys, jobs, method, mode, 1, precision, max_iter > 0 ? max_iter : maxn, nsys, infos, 0);
+}
+
+}  // extern "C"

@@ -17,6 +17,7 @@
 
 #include "feec_device.cuh"
 #include "feec_internal.h"
+#include "feec_system.h"
 
 namespace feec {
 
@@ -39,6 +40,8 @@ struct DeviceCtx {
 std::mutex g_ctx_mutex;
 DeviceCtx g_ctx[64];
 
+}  // namespace
+
 int init_device(int& dev, cudaStream_t& stream) {
     if (cudaGetDevice(&dev) != cudaSuccess) return FEEC_NO_DEVICE;
     if (dev < 0 || dev >= 64) return FEEC_NO_DEVICE;
@@ -58,41 +61,7 @@ int init_device(int& dev, cudaStream_t& stream) {
     return FEEC_OK;
 }
 
-int cuda_status(cudaError_t e) {
-    if (e == cudaSuccess) return FEEC_OK;
-    if (e == cudaErrorMemoryAllocation) return FEEC_OOM;
-    return FEEC_CUDA_ERROR;
-}
-
-// Stream-ordered device allocations owned by one object.
-struct DevArena {
-    std::vector<void*> ptrs;
-    size_t bytes = 0;
-    cudaStream_t stream = nullptr;
-    template <typename T>
-    cudaError_t alloc(T*& p, size_t count) {
-        p = nullptr;
-        if (count == 0) count = 1;
-        void* q = nullptr;
-        cudaError_t e = cudaMallocAsync(&q, count * sizeof(T), stream);
-        if (e != cudaSuccess) return e;
-        ptrs.push_back(q);
-        bytes += count * sizeof(T);
-        p = (T*)q;
-        return cudaSuccess;
-    }
-    void release() {
-        for (void* p : ptrs) cudaFreeAsync(p, stream);
-        ptrs.clear();
-        bytes = 0;
-    }
-};
-
-#define FEEC_TRY(expr)                                   \
-    do {                                                 \
-        cudaError_t _e = (expr);                         \
-        if (_e != cudaSuccess) return cuda_status(_e);   \
-    } while (0)
+namespace {
 
 double host_tolerance(int n, const double* b, double precision) {
     // solver/sparsesolver.cpp:45-48, the same serial loop
@@ -107,40 +76,7 @@ double host_tolerance(int n, const double* b, double precision) {
 
 using namespace feec;
 
-struct feec_system {
-    int dev = 0;
-    int n = 0;
-    int nnz = 0;
-    cudaStream_t stream = nullptr;
-    DevArena mem;      // matrix + layouts
-    DevArena work;     // Krylov workspace
-    int* A = nullptr; int* C = nullptr; double* V = nullptr;   // original CSR
-    float* V32 = nullptr;                                        // FP32 copy for mixed CG
-    int lanes = 4;
-    // preconditioner layout (valid if prepared >= 0)
-    int prepared = -1;
-    int* perm = nullptr; int* iperm = nullptr;
-    int* rp = nullptr; int* ci = nullptr; double* val = nullptr; float* val32 = nullptr;
-    int* lsplit = nullptr; int* usplit = nullptr;
-    double* diag = nullptr; float* diag32 = nullptr;
-    double* wd = nullptr; double* sd = nullptr; float* wd32 = nullptr; float* sd32 = nullptr;
-    int nf = 0; int* fptr = nullptr;
-    int nbw = 0; int* bptr = nullptr; int* brows = nullptr;
-    double omega = 1.0;
-    int num_levels = 0;
-    // workspace (FP64 permuted vectors + FP32 inner vectors)
-    bool work_ready = false;
-    double *x = nullptr, *r = nullptr, *d = nullptr, *z = nullptr, *m = nullptr, *q = nullptr, *b = nullptr;
-    float *x32 = nullptr, *r32 = nullptr, *d32 = nullptr, *z32 = nullptr, *m32 = nullptr, *q32 = nullptr, *b32 = nullptr;
-    double* partials = nullptr;
-    double* scal = nullptr;   // device scalars
-    DeviceStatus* st = nullptr;
-    int max_blocks = 0;
-    int max_phase_rows = 0;     // largest sweep phase (rows)
-    int user_blocks = 0;        // launch-shape overrides (0 = automatic)
-    int user_lanes = 0;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-};
+
 
 namespace {
 
@@ -578,6 +514,16 @@ int feec_system_set_rainbow(feec_system* s, const double* diagonal, double omega
     for (int i = 0; i < n; i++) {
         if (hR[i] < 0 || hR[i] >= n || seen[hR[i]]) return FEEC_BADARG;
         seen[hR[i]] = 1;
+    }
+    // Inside a color the rows are independent, so their order is free: sort them by row
+    // length (stable, longest first) so that 32-row slices hold rows of equal length.
+    {
+        std::vector<int> hA((size_t)n + 1);
+        FEEC_TRY(cudaMemcpyAsync(hA.data(), s->A, sizeof(int) * (n + 1), cudaMemcpyDeviceToHost, s->stream));
+        FEEC_TRY(cudaStreamSynchronize(s->stream));
+        for (int c = 0; c < num_colors; c++)
+            std::stable_sort(hR.begin() + hB[c], hR.begin() + hB[c + 1],
+                             [&](int a, int b) { return hA[a + 1] - hA[a] > hA[b + 1] - hA[b]; });
     }
     // forward phases: colors ascending (rows are renumbered color by color, so ranges are contiguous);
     // backward phases: colors descending

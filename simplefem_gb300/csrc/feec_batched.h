@@ -1,0 +1,68 @@
+// Shared definitions of the batched solver engine (kernels_batched.cu, batched.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "feec_internal.h"
+
+namespace feec {
+
+constexpr int kBatchMaxK = 4;   // right-hand sides advanced together by one team
+
+// Device view of one system in SELL-32 layout over its color-permuted rows.
+struct SellView {
+    int n, nslices, ncolors, pad;
+    const int* perm;            // permuted row -> caller's row
+    const int* slice_row0;      // first permuted row of each slice
+    const int* slice_nrow;      // valid rows in each slice (<= 32)
+    const int4* slice_len;      // (L, E, U, 0) block lengths of each slice
+    const long long* slice_off; // offset of each slice in ci / val
+    const int* color_slice;     // slices of color c: [color_slice[c], color_slice[c+1])
+    const int* ci;              // column-major blocks, padded entries point at a valid row with value 0
+    const float* val32;
+    const double* val64;
+    const float* wd32; const float* sd32;    // omega / D (0 where D == 0) and D (2 - omega) / omega
+    const double* wd64; const double* sd64;
+};
+
+struct BatchItem {
+    int system;        // index into BatchArgs::systems
+    int nrhs;          // columns in use (<= K of the launch)
+    int first_result;  // results[first_result + j] receives column j
+    int pad;
+    const double* b[kBatchMaxK];   // caller right-hand sides (caller numbering)
+    double* x[kBatchMaxK];         // caller solutions (caller numbering; in: initial guess)
+    double* xp; double* bp; double* r64;                 // n*K FP64 workspace
+    void* r; void* d; void* z; void* m; void* q; void* c;  // n*K inner workspace (float or double)
+};
+
+struct BatchResult {
+    int status, iterations, outer, pad;
+    double relres;
+};
+
+struct BatchArgs {
+    const SellView* systems;
+    const BatchItem* items;
+    int nitems;
+    int* next_item;           // work queue head (zeroed before the launch)
+    BatchResult* results;
+    double precision;         // stop when ||b - A x|| <= precision ||b|| (FP64)
+    double inner_eta;         // relative reduction asked of one inner solve
+    double inner_margin;      // the last inner solve aims at margin * (reduction still needed)
+    int max_iter;             // inner iterations per column, summed over outer steps
+    int max_outer;
+};
+
+cudaError_t launch_batched(const BatchArgs& args, int is_float, int K, int rainbow, int teams, cudaStream_t s);
+int batched_max_k(int is_float);
+
+// SELL construction (kernels_setup.cu)
+cudaError_t launch_sell_lengths(int nslices, const int* slice_row0, const int* slice_nrow, const int* rp,
+                                const int* lsplit, const int* usplit, int4* slice_len, cudaStream_t s);
+cudaError_t launch_sell_fill(int nslices, const int* slice_row0, const int* slice_nrow, const int4* slice_len,
+                             const long long* slice_off, const int* rp, const int* lsplit, const int* usplit,
+                             const int* ci_in, const double* val_in, int* ci, float* val32, double* val64,
+                             cudaStream_t s);
+
+}  // namespace feec

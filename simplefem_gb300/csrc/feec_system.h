@@ -1,0 +1,96 @@
+// The device-resident system object and small host helpers shared by the
+// C ABI translation units (capi.cu, batched.cu).
+#pragma once
+
+#include <cstddef>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "feec_batched.h"
+#include "feec_internal.h"
+
+namespace feec {
+
+inline int cuda_status(cudaError_t e) {
+    if (e == cudaSuccess) return FEEC_OK;
+    if (e == cudaErrorMemoryAllocation) return FEEC_OOM;
+    return FEEC_CUDA_ERROR;
+}
+
+// Stream-ordered device allocations owned by one object.
+struct DevArena {
+    std::vector<void*> ptrs;
+    size_t bytes = 0;
+    cudaStream_t stream = nullptr;
+    template <typename T>
+    cudaError_t alloc(T*& p, size_t count) {
+        p = nullptr;
+        if (count == 0) count = 1;
+        void* q = nullptr;
+        cudaError_t e = cudaMallocAsync(&q, count * sizeof(T), stream);
+        if (e != cudaSuccess) return e;
+        ptrs.push_back(q);
+        bytes += count * sizeof(T);
+        p = (T*)q;
+        return cudaSuccess;
+    }
+    void release() {
+        for (void* p : ptrs) cudaFreeAsync(p, stream);
+        ptrs.clear();
+        bytes = 0;
+    }
+};
+
+#define FEEC_TRY(expr)                                        \
+    do {                                                      \
+        cudaError_t _e = (expr);                              \
+        if (_e != cudaSuccess) return ::feec::cuda_status(_e); \
+    } while (0)
+
+int init_device(int& dev, cudaStream_t& stream);
+
+}  // namespace feec
+
+struct feec_system {
+    int dev = 0;
+    int n = 0;
+    int nnz = 0;
+    cudaStream_t stream = nullptr;
+    feec::DevArena mem;      // matrix + layouts
+    feec::DevArena work;     // Krylov workspace
+    int* A = nullptr; int* C = nullptr; double* V = nullptr;   // original CSR
+    float* V32 = nullptr;                                        // FP32 copy for mixed CG
+    int lanes = 4;
+    // preconditioner layout (valid if prepared >= 0)
+    int prepared = -1;
+    int* perm = nullptr; int* iperm = nullptr;
+    int* rp = nullptr; int* ci = nullptr; double* val = nullptr; float* val32 = nullptr;
+    int* lsplit = nullptr; int* usplit = nullptr;
+    double* diag = nullptr; float* diag32 = nullptr;
+    double* wd = nullptr; double* sd = nullptr; float* wd32 = nullptr; float* sd32 = nullptr;
+    int nf = 0; int* fptr = nullptr;
+    int nbw = 0; int* bptr = nullptr; int* brows = nullptr;
+    double omega = 1.0;
+    int num_levels = 0;
+    // workspace (FP64 permuted vectors + FP32 inner vectors)
+    bool work_ready = false;
+    double *x = nullptr, *r = nullptr, *d = nullptr, *z = nullptr, *m = nullptr, *q = nullptr, *b = nullptr;
+    float *x32 = nullptr, *r32 = nullptr, *d32 = nullptr, *z32 = nullptr, *m32 = nullptr, *q32 = nullptr, *b32 = nullptr;
+    double* partials = nullptr;
+    double* scal = nullptr;   // device scalars
+    feec::DeviceStatus* st = nullptr;
+    int max_blocks = 0;
+    int max_phase_rows = 0;     // largest sweep phase (rows)
+    int user_blocks = 0;        // launch-shape overrides (0 = automatic)
+    int user_lanes = 0;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // SELL-32 layout for the batched engine (valid if sell_method >= 0)
+    int sell_method = -1;
+    feec::DevArena sell;
+    int nslices = 0, sell_ncolors = 0;
+    int* slice_row0 = nullptr; int* slice_nrow = nullptr; int4* slice_len = nullptr; long long* slice_off = nullptr;
+    int* color_slice = nullptr; int* sci = nullptr; float* sval32 = nullptr; double* sval64 = nullptr;
+    int* ident = nullptr;
+    long long sell_entries = 0;
+};

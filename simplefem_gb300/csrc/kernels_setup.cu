@@ -4,6 +4,7 @@
 // [L | E | U] split layout that the SSOR / multicolor SSOR sweeps stream.
 #include <cstdint>
 
+#include "feec_batched.h"
 #include "feec_device.cuh"
 #include "feec_internal.h"
 
@@ -184,6 +185,73 @@ __global__ void update_x_kernel(int n, const int* __restrict__ perm, const float
     if (i < n) x[perm ? perm[i] : i] += (*norm) * (double)c32[i];
 }
 
+// SELL-32 block lengths of each slice: the longest L, E and U part over its rows.
+// lsplit == null: the whole row is one block (U), for the unpreconditioned CG.
+__global__ void sell_lengths_kernel(int nslices, const int* __restrict__ row0, const int* __restrict__ nrow,
+                                    const int* __restrict__ rp, const int* __restrict__ lsplit,
+                                    const int* __restrict__ usplit, int4* __restrict__ len) {
+    const int sl = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+    const int lane = threadIdx.x & 31;
+    if (sl >= nslices) return;
+    int l = 0, e = 0, u = 0;
+    if (lane < nrow[sl]) {
+        const int i = row0[sl] + lane;
+        const int a = rp[i], b = rp[i + 1];
+        if (lsplit) { l = lsplit[i] - a; e = usplit[i] - lsplit[i]; u = b - usplit[i]; }
+        else { u = b - a; }
+    }
+    #pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        l = max(l, __shfl_xor_sync(0xffffffffu, l, off));
+        e = max(e, __shfl_xor_sync(0xffffffffu, e, off));
+        u = max(u, __shfl_xor_sync(0xffffffffu, u, off));
+    }
+    if (lane == 0) len[sl] = make_int4(l, e, u, 0);
+}
+
+// Column-major fill of each slice; padding entries get value 0 and the column of
+// the slice's first row, so every gathered index stays valid.
+__global__ void sell_fill_kernel(int nslices, const int* __restrict__ row0, const int* __restrict__ nrow,
+                                 const int4* __restrict__ len, const long long* __restrict__ off,
+                                 const int* __restrict__ rp, const int* __restrict__ lsplit,
+                                 const int* __restrict__ usplit, const int* __restrict__ ci_in,
+                                 const double* __restrict__ val_in, int* __restrict__ ci, float* __restrict__ val32,
+                                 double* __restrict__ val64) {
+    const int sl = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+    const int lane = threadIdx.x & 31;
+    if (sl >= nslices) return;
+    const int4 L = len[sl];
+    const long long base = off[sl];
+    const int r0 = row0[sl];
+    const bool act = lane < nrow[sl];
+    const int i = r0 + lane;
+    int seg_lo[3] = {0, 0, 0}, seg_hi[3] = {0, 0, 0};
+    if (act) {
+        const int a = rp[i], b = rp[i + 1];
+        if (lsplit) {
+            seg_lo[0] = a; seg_hi[0] = lsplit[i];
+            seg_lo[1] = lsplit[i]; seg_hi[1] = usplit[i];
+            seg_lo[2] = usplit[i]; seg_hi[2] = b;
+        } else {
+            seg_lo[2] = a; seg_hi[2] = b;
+        }
+    }
+    const int blen[3] = {L.x, L.y, L.z};
+    long long o = base;
+    for (int blk = 0; blk < 3; blk++) {
+        for (int k = 0; k < blen[blk]; k++) {
+            const int j = seg_lo[blk] + k;
+            const bool real = act && j < seg_hi[blk];
+            const long long dst = o + (long long)k * 32 + lane;
+            ci[dst] = real ? ci_in[j] : r0;
+            const double v = real ? val_in[j] : 0.0;
+            if (val64) val64[dst] = v;
+            if (val32) val32[dst] = (float)v;
+        }
+        o += (long long)blen[blk] * 32;
+    }
+}
+
 // ---- exclusive scan of int32 (three-phase, 4096 elements per block) ----
 constexpr int kScanThreads = 1024;
 constexpr int kScanItems = 4;
@@ -349,6 +417,20 @@ cudaError_t launch_scaled_cast(int n, const double* r, const double* inv_norm_de
 
 cudaError_t launch_update_x(int n, const int* perm, const float* c32, const double* norm_dev, double* x, cudaStream_t s) {
     return launch(update_x_kernel, grid_for(n, kBlock), kBlock, s, n, perm, c32, norm_dev, x);
+}
+
+cudaError_t launch_sell_lengths(int nslices, const int* slice_row0, const int* slice_nrow, const int* rp,
+                                const int* lsplit, const int* usplit, int4* slice_len, cudaStream_t s) {
+    return launch(sell_lengths_kernel, grid_for((long long)nslices * 32, kBlock), kBlock, s, nslices, slice_row0,
+                  slice_nrow, rp, lsplit, usplit, slice_len);
+}
+
+cudaError_t launch_sell_fill(int nslices, const int* slice_row0, const int* slice_nrow, const int4* slice_len,
+                             const long long* slice_off, const int* rp, const int* lsplit, const int* usplit,
+                             const int* ci_in, const double* val_in, int* ci, float* val32, double* val64,
+                             cudaStream_t s) {
+    return launch(sell_fill_kernel, grid_for((long long)nslices * 32, kBlock), kBlock, s, nslices, slice_row0,
+                  slice_nrow, slice_len, slice_off, rp, lsplit, usplit, ci_in, val_in, ci, val32, val64);
 }
 
 size_t scan_scratch_ints(int n) {

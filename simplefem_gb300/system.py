@@ -77,6 +77,18 @@ class System:
             raise _native.FeecError(st, "feec_system_solve")
         return out
 
+    def solve_batch(self, B, X, method="rainbow", mode="mixed", precision=1e-10, max_iter=0, rhs_per_team=0,
+                    raise_on_error=True) -> list:
+        """Solve A X[j] = B[j] for every row j of the (nrhs, n) float64 device tensors B, X
+        (X holds the initial guesses) with the batched engine; one dict per column."""
+        nrhs = int(B.shape[0])
+        infos = (_native.FeecSolveInfo * nrhs)()
+        st = self._lib.feec_system_solve_batch(self._h, METHODS[method], MODES[mode], nrhs, _ptr(X), _ptr(B),
+                                               float(precision), int(max_iter), int(rhs_per_team), infos, _stream())
+        if raise_on_error and st not in (_native.FEEC_OK, _native.FEEC_MAXITER, _native.FEEC_BREAKDOWN):
+            raise _native.FeecError(st, "feec_system_solve_batch")
+        return [i.as_dict() for i in infos]
+
     def apply(self, x, y, scaling=1.0):
         _native.check(self._lib.feec_system_apply(self._h, _ptr(x), _ptr(y), float(scaling), _stream()),
                       "feec_system_apply")
@@ -100,3 +112,19 @@ class System:
             self.close()
         except Exception:
             pass
+
+
+def solve_many(systems, bs, xs, method="rainbow", mode="mixed", precision=1e-10, max_iter=0,
+               raise_on_error=True) -> list:
+    """One batched launch over many systems, one right-hand side each (device tensors)."""
+    lib = _native.gpu()
+    n = len(systems)
+    hs = (ctypes.c_void_p * n)(*[s._h for s in systems])
+    xp = (ctypes.c_void_p * n)(*[x.data_ptr() for x in xs])
+    bp = (ctypes.c_void_p * n)(*[b.data_ptr() for b in bs])
+    infos = (_native.FeecSolveInfo * n)()
+    st = lib.feec_solve_many(n, hs, METHODS[method], MODES[mode], xp, bp, float(precision), int(max_iter), infos,
+                             _stream())
+    if raise_on_error and st not in (_native.FEEC_OK, _native.FEEC_MAXITER, _native.FEEC_BREAKDOWN):
+        raise _native.FeecError(st, "feec_solve_many")
+    return [i.as_dict() for i in infos]
