@@ -158,6 +158,50 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+SPMV_WORKLOAD = dict(dim=3, r=1, L=7)   # 3D P1 refined 7x: N = 2,146,689, nnz = 31,802,497 (> L2)
+
+
+def run_spmv(dev, reps=20):
+    """Resident SpMV (MatrixCSR::apply on the device, SELL-32) on the largest operator of the
+    mixed-precision configuration, FP64 and FP32 values, L2 flushed before every product."""
+    import torch
+    from simplefem_gb300 import workloads
+    from simplefem_gb300.system import System
+    A, C, V = workloads.lattice_matrix(**SPMV_WORKLOAD)
+    n = len(A) - 1
+    nnz = len(C)
+    sysm = System(A, C, V)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)
+    x = torch.from_numpy(workloads.uniform_vector(3, n)).to(dev)
+    y = torch.empty_like(x)
+    x32 = x.float()
+    y32 = torch.empty_like(x32)
+    stream = torch.cuda.current_stream()
+    peak, kind = measured_peaks()
+    out = {"workload": "3D P1 Lagrange stiffness+mass refined 7x: N=2146689, nnz=31802497",
+           "algorithmic_bytes": "S*nnz + 4(N+1) + 2w*N (S=12/8, w=8/4)"}
+    for tag, xx, yy, S_, w in (("fp64", x, y, 12, 8), ("fp32", x32, y32, 8, 4)):
+        sysm.apply(xx, yy)
+        torch.cuda.synchronize()
+        ms = []
+        for _ in range(reps):
+            flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            sysm.apply(xx, yy)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        t = float(np.median(ms))
+        b = S_ * nnz + 4 * (n + 1) + 2 * w * n
+        gbs = b / (t / 1000.0) / 1e9
+        out[tag] = {"us": 1000 * t, "bytes": b, "achieved_gbs": gbs, "frac": gbs / peak, "kernel": f"sell_spmv_kernel<{'double' if tag == 'fp64' else 'float'}>"}
+    out["peak_gbs"] = peak
+    out["peak_kind"] = kind
+    sysm.close()
+    return out
+
+
 def run_ours(args):
     import torch
     import torch.distributed as dist
@@ -173,6 +217,10 @@ def run_ours(args):
     from simplefem_gb300.system import System
 
     lib = _native.gpu()
+    if args.only_spmv:
+        if rank == 0:
+            print(json.dumps({"spmv": run_spmv(dev)}), flush=True)
+        return
     A, C, V = workloads.lattice_matrix(**WORKLOAD)
     n = len(A) - 1
     nnz = len(C)
@@ -301,6 +349,8 @@ def run_ours(args):
                                              rb.num_colors, rb.F, rb.B, rb.R)
         dropin.append(time.perf_counter() - t0)
 
+    spmv = run_spmv(dev)
+
     # CPU baseline: the oracle restatement of the reference Rainbow-PCG on the host cores, one solve
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -343,6 +393,7 @@ def run_ours(args):
             "fp64_rainbow_reference_rule": {"solves_per_s": rate(rb64), "ms": float(np.median(rb64)),
                                             "iterations": int(np.median([i["iterations"] for i in rb64_i]))},
             "dropin_host_call_ms": 1000 * float(np.median(dropin)),
+            "spmv": spmv,
             "roofline": roofline,
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": 8 * n * B_RHS,
@@ -364,6 +415,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--batch", type=int, default=1216, help="right-hand sides per batched step")
+    ap.add_argument("--only-spmv", action="store_true", help="only the resident SpMV measurement")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

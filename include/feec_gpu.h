@@ -116,7 +116,9 @@ int feec_csr_check(int rows, int cols, const int* A, const int* C, const double*
 typedef struct feec_system feec_system;
 
 /* Uploads (host_ptrs != 0) or adopts a copy of (host_ptrs == 0, device pointers)
- * an N x N CSR matrix. `stream` is a cudaStream_t (NULL = the library stream). */
+ * an N x N CSR matrix. `stream` is a cudaStream_t; NULL is CUDA's default stream
+ * (stream 0). It becomes the system's stream; every feec_system_* call below runs on
+ * its own `stream` argument if that is not NULL, else on the system's stream. */
 int feec_system_create(feec_system** sys, int N, const int* A, const int* C, const double* V,
                        int host_ptrs, void* stream);
 
@@ -145,6 +147,14 @@ int feec_system_solve_batch(feec_system* sys, int method, int mode, int nrhs, do
                             double precision, int max_iter, int rhs_per_team,
                             feec_solve_info* infos, void* stream);
 
+/* Autotuner of the batched engine: times short trials of every launch candidate
+ * (right-hand sides per team 1/2/4, team size 128/256/512 threads) on this system
+ * and caches the fastest, which feec_system_solve_batch then uses whenever
+ * rhs_per_team is 0. nrhs_hint caps the trial batch (0 = fill the GPU). Outputs
+ * may be NULL. */
+int feec_system_tune_batch(feec_system* sys, int method, int mode, int nrhs_hint,
+                           int* rhs_per_team, int* team_threads, double* rhs_iters_per_s);
+
 /* Batched solves of many systems, one right-hand side each (device pointers
  * x[i], b[i] of systems[i]->N doubles; host arrays of pointers). Systems are
  * processed largest first, one thread block per system. For
@@ -154,8 +164,12 @@ int feec_solve_many(int nsys, feec_system* const* systems, int method, int mode,
                     double* const* x, const double* const* b, double precision, int max_iter,
                     feec_solve_info* infos, void* stream);
 
-/* y = scaling * A * x with device pointers. */
+/* y = scaling * A * x with device pointers (MatrixCSR::apply on a resident matrix),
+ * over a cached SELL-32 copy of the matrix, one thread per row. */
 int feec_system_apply(feec_system* sys, const double* x, double* y, double scaling, void* stream);
+
+/* The same product on the FP32 copy of the values (x, y float). */
+int feec_system_apply_f32(feec_system* sys, const float* x, float* y, float scaling, void* stream);
 
 /* Launch-shape override for the persistent solvers (used by the autotuner):
  * blocks = co-resident grid size, lanes = CSR lanes per row (power of two <= 32);

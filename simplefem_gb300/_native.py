@@ -82,9 +82,12 @@ def gpu():
         L.feec_system_set_ssor.argtypes = [_vp, _vp, _dp, _ip]
         L.feec_system_solve.argtypes = [_vp, _ip, _ip, _vp, _vp, _vp, _dp, _ip, _infop, _vp]
         L.feec_system_apply.argtypes = [_vp, _vp, _vp, _dp, _vp]
+        L.feec_system_apply_f32.argtypes = [_vp, _vp, _vp, ctypes.c_float, _vp]
         L.feec_system_solve_batch.argtypes = [_vp, _ip, _ip, _ip, _vp, _vp, _dp, _ip, _ip, _infop, _vp]
         L.feec_solve_many.argtypes = [_ip, ctypes.POINTER(_vp), _ip, _ip, ctypes.POINTER(_vp), ctypes.POINTER(_vp),
                                       _dp, _ip, _infop, _vp]
+        L.feec_system_tune_batch.argtypes = [_vp, _ip, _ip, _ip, ctypes.POINTER(ctypes.c_int),
+                                             ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)]
         L.feec_system_set_launch.argtypes = [_vp, _ip, _ip]
         L.feec_system_memory.argtypes = [_vp, ctypes.POINTER(ctypes.c_size_t)]
         L.feec_system_destroy.argtypes = [_vp]

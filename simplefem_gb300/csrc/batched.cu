@@ -14,21 +14,28 @@
 
 using namespace feec;
 
-namespace {
+namespace feec {
+int sell_prepare(feec_system* s, int method);
+SellView sell_view(const feec_system* s, int method);
+}
 
-// Builds (once per system and method) the SELL-32 layout: slices of 32 rows that
-// never cross a color, blocks [L | E | U] per slice.
+namespace feec {
+
+
+// Builds (once per system and ordering) the SELL-32 layout: slices of 32 rows that
+// never cross a color, blocks [L | E | U] per slice (natural order: one block).
 int sell_prepare(feec_system* s, int method) {
-    if (s->sell_method == method) return FEEC_OK;
-    if (method == FEEC_METHOD_RAINBOW && s->prepared != FEEC_METHOD_RAINBOW) return FEEC_BADARG;
     if (method != FEEC_METHOD_RAINBOW && method != FEEC_METHOD_CG) return FEEC_BADARG;
-    s->sell.release();
-    s->sell.stream = s->stream;
+    const bool rb = method == FEEC_METHOD_RAINBOW;
+    SellData& D = s->sell[rb ? 1 : 0];
+    if (D.ready) return FEEC_OK;
+    if (rb && s->prepared != FEEC_METHOD_RAINBOW) return FEEC_BADARG;
+    D.mem.release();
+    D.mem.stream = s->stream;
     cudaStream_t st = s->stream;
     const int n = s->n;
-    // color ranges in the permuted numbering
     std::vector<int> ranges;
-    if (method == FEEC_METHOD_RAINBOW) {
+    if (rb) {
         ranges.resize((size_t)s->nf + 1);
         FEEC_TRY(cudaMemcpyAsync(ranges.data(), s->fptr, sizeof(int) * ranges.size(), cudaMemcpyDeviceToHost, st));
         FEEC_TRY(cudaStreamSynchronize(st));
@@ -45,20 +52,19 @@ int sell_prepare(feec_system* s, int method) {
         cslice.push_back((int)row0.size());
     }
     const int ns = (int)row0.size();
-    DevArena& M = s->sell;
-    FEEC_TRY(M.alloc(s->slice_row0, ns)); FEEC_TRY(M.alloc(s->slice_nrow, ns)); FEEC_TRY(M.alloc(s->slice_len, ns));
-    FEEC_TRY(M.alloc(s->slice_off, ns)); FEEC_TRY(M.alloc(s->color_slice, cslice.size()));
-    FEEC_TRY(cudaMemcpyAsync(s->slice_row0, row0.data(), sizeof(int) * ns, cudaMemcpyHostToDevice, st));
-    FEEC_TRY(cudaMemcpyAsync(s->slice_nrow, nrow.data(), sizeof(int) * ns, cudaMemcpyHostToDevice, st));
-    FEEC_TRY(cudaMemcpyAsync(s->color_slice, cslice.data(), sizeof(int) * cslice.size(), cudaMemcpyHostToDevice, st));
-    const bool rb = method == FEEC_METHOD_RAINBOW;
+    DevArena& M = D.mem;
+    FEEC_TRY(M.alloc(D.slice_row0, ns)); FEEC_TRY(M.alloc(D.slice_nrow, ns)); FEEC_TRY(M.alloc(D.slice_len, ns));
+    FEEC_TRY(M.alloc(D.slice_off, ns)); FEEC_TRY(M.alloc(D.color_slice, cslice.size()));
+    FEEC_TRY(cudaMemcpyAsync(D.slice_row0, row0.data(), sizeof(int) * ns, cudaMemcpyHostToDevice, st));
+    FEEC_TRY(cudaMemcpyAsync(D.slice_nrow, nrow.data(), sizeof(int) * ns, cudaMemcpyHostToDevice, st));
+    FEEC_TRY(cudaMemcpyAsync(D.color_slice, cslice.data(), sizeof(int) * cslice.size(), cudaMemcpyHostToDevice, st));
     const int* rp = rb ? s->rp : s->A;
     const int* cin = rb ? s->ci : s->C;
     const double* vin = rb ? s->val : s->V;
-    FEEC_TRY(launch_sell_lengths(ns, s->slice_row0, s->slice_nrow, rp, rb ? s->lsplit : nullptr,
-                                 rb ? s->usplit : nullptr, s->slice_len, st));
+    FEEC_TRY(launch_sell_lengths(ns, D.slice_row0, D.slice_nrow, rp, rb ? s->lsplit : nullptr,
+                                 rb ? s->usplit : nullptr, D.slice_len, st));
     std::vector<int4> len((size_t)ns);
-    FEEC_TRY(cudaMemcpyAsync(len.data(), s->slice_len, sizeof(int4) * ns, cudaMemcpyDeviceToHost, st));
+    FEEC_TRY(cudaMemcpyAsync(len.data(), D.slice_len, sizeof(int4) * ns, cudaMemcpyDeviceToHost, st));
     FEEC_TRY(cudaStreamSynchronize(st));
     std::vector<long long> off((size_t)ns);
     long long total = 0;
@@ -66,36 +72,41 @@ int sell_prepare(feec_system* s, int method) {
         off[i] = total;
         total += 32ll * (len[i].x + len[i].y + len[i].z);
     }
-    FEEC_TRY(cudaMemcpyAsync(s->slice_off, off.data(), sizeof(long long) * ns, cudaMemcpyHostToDevice, st));
-    FEEC_TRY(M.alloc(s->sci, (size_t)total)); FEEC_TRY(M.alloc(s->sval32, (size_t)total));
-    FEEC_TRY(M.alloc(s->sval64, (size_t)total));
-    FEEC_TRY(launch_sell_fill(ns, s->slice_row0, s->slice_nrow, s->slice_len, s->slice_off, rp, rb ? s->lsplit : nullptr,
-                              rb ? s->usplit : nullptr, cin, vin, s->sci, s->sval32, s->sval64, st));
+    FEEC_TRY(cudaMemcpyAsync(D.slice_off, off.data(), sizeof(long long) * ns, cudaMemcpyHostToDevice, st));
+    FEEC_TRY(M.alloc(D.ci, (size_t)total)); FEEC_TRY(M.alloc(D.val32, (size_t)total));
+    FEEC_TRY(M.alloc(D.val64, (size_t)total));
+    FEEC_TRY(launch_sell_fill(ns, D.slice_row0, D.slice_nrow, D.slice_len, D.slice_off, rp, rb ? s->lsplit : nullptr,
+                              rb ? s->usplit : nullptr, cin, vin, D.ci, D.val32, D.val64, st));
     if (!rb) {
         std::vector<int> id((size_t)n);
         std::iota(id.begin(), id.end(), 0);
-        FEEC_TRY(M.alloc(s->ident, n));
-        FEEC_TRY(cudaMemcpyAsync(s->ident, id.data(), sizeof(int) * n, cudaMemcpyHostToDevice, st));
+        FEEC_TRY(M.alloc(D.ident, n));
+        FEEC_TRY(cudaMemcpyAsync(D.ident, id.data(), sizeof(int) * n, cudaMemcpyHostToDevice, st));
     }
     FEEC_TRY(cudaStreamSynchronize(st));
-    s->nslices = ns;
-    s->sell_ncolors = ncolors;
-    s->sell_entries = total;
-    s->sell_method = method;
+    D.nslices = ns;
+    D.ncolors = ncolors;
+    D.entries = total;
+    D.ready = true;
     return FEEC_OK;
 }
 
-SellView sell_view(const feec_system* s) {
+SellView sell_view(const feec_system* s, int method) {
+    const bool rb = method == FEEC_METHOD_RAINBOW;
+    const SellData& D = s->sell[rb ? 1 : 0];
     SellView v{};
-    const bool rb = s->sell_method == FEEC_METHOD_RAINBOW;
-    v.n = s->n; v.nslices = s->nslices; v.ncolors = s->sell_ncolors;
-    v.perm = rb ? s->perm : s->ident;
-    v.slice_row0 = s->slice_row0; v.slice_nrow = s->slice_nrow; v.slice_len = s->slice_len; v.slice_off = s->slice_off;
-    v.color_slice = s->color_slice; v.ci = s->sci; v.val32 = s->sval32; v.val64 = s->sval64;
+    v.n = s->n; v.nslices = D.nslices; v.ncolors = D.ncolors;
+    v.perm = rb ? s->perm : D.ident;
+    v.slice_row0 = D.slice_row0; v.slice_nrow = D.slice_nrow; v.slice_len = D.slice_len; v.slice_off = D.slice_off;
+    v.color_slice = D.color_slice; v.ci = D.ci; v.val32 = D.val32; v.val64 = D.val64;
     v.wd32 = rb ? s->wd32 : nullptr; v.sd32 = rb ? s->sd32 : nullptr;
     v.wd64 = rb ? s->wd : nullptr; v.sd64 = rb ? s->sd : nullptr;
     return v;
 }
+
+}  // namespace feec
+
+namespace {
 
 struct Job {
     int system;
@@ -106,7 +117,8 @@ struct Job {
 };
 
 int run_batch(cudaStream_t st, const std::vector<feec_system*>& systems, std::vector<Job>& jobs, int method, int mode,
-              int K, double precision, int max_iter, int nresults, feec_solve_info* infos, int teams) {
+              int K, double precision, int max_iter, int nresults, feec_solve_info* infos, int teams, int threads,
+              int max_outer = 0, float* elapsed_ms = nullptr, long long* iter_sum = nullptr) {
     const int is_float = mode == FEEC_MODE_MIXED ? 1 : 0;
     const size_t tsz = is_float ? sizeof(float) : sizeof(double);
     // largest systems first, so the tail of the batch is short
@@ -115,7 +127,7 @@ int run_batch(cudaStream_t st, const std::vector<feec_system*>& systems, std::ve
     DevArena tmp;
     tmp.stream = st;
     std::vector<SellView> views;
-    for (auto* s : systems) views.push_back(sell_view(s));
+    for (auto* s : systems) views.push_back(sell_view(s, method));
     SellView* dviews = nullptr;
     BatchItem* ditems = nullptr;
     BatchResult* dres = nullptr;
@@ -148,12 +160,12 @@ int run_batch(cudaStream_t st, const std::vector<feec_system*>& systems, std::ve
     a.inner_eta = is_float ? 2e-5 : 1e-30;
     a.inner_margin = is_float ? 0.3 : 1.0;   // FP64 recursion tracks the true residual closely
     a.max_iter = max_iter;
-    a.max_outer = is_float ? 12 : 4;
+    a.max_outer = max_outer > 0 ? max_outer : (is_float ? 12 : 4);
     cudaEvent_t e0, e1;
     FEEC_TRY(cudaEventCreate(&e0));
     FEEC_TRY(cudaEventCreate(&e1));
     FEEC_TRY(cudaEventRecord(e0, st));
-    FEEC_TRY(launch_batched(a, is_float, K, method == FEEC_METHOD_RAINBOW, teams, st));
+    FEEC_TRY(launch_batched(a, is_float, K, method == FEEC_METHOD_RAINBOW, threads, teams, st));
     FEEC_TRY(cudaEventRecord(e1, st));
     std::vector<BatchResult> res((size_t)nresults);
     FEEC_TRY(cudaMemcpyAsync(res.data(), dres, sizeof(BatchResult) * nresults, cudaMemcpyDeviceToHost, st));
@@ -163,6 +175,12 @@ int run_batch(cudaStream_t st, const std::vector<feec_system*>& systems, std::ve
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     tmp.release();
+    if (elapsed_ms) *elapsed_ms = ms;
+    if (iter_sum) {
+        long long t = 0;
+        for (int i = 0; i < nresults; i++) t += res[i].iterations;
+        *iter_sum = t;
+    }
     int worst = FEEC_OK;
     for (int i = 0; i < nresults; i++) {
         if (res[i].status != FEEC_OK && worst == FEEC_OK) worst = res[i].status;
@@ -177,11 +195,29 @@ int run_batch(cudaStream_t st, const std::vector<feec_system*>& systems, std::ve
             f.final_norm = res[i].relres;
             f.device_ms = ms;
             f.lanes_per_row = 1;
-            f.grid_blocks = teams;
+            f.grid_blocks = teams > 0 ? teams : batched_resident_teams(is_float, K, method == FEEC_METHOD_RAINBOW, threads);
         }
     }
     FEEC_TRY(cudaStreamSynchronize(st));
     return worst;
+}
+
+struct TunedConfig {
+    bool valid = false;
+    int K = 0, threads = 0;
+    double rhs_iters_per_s = 0.0;
+};
+
+int jobs_for(feec_system* s, int nrhs, int K, double* X, const double* Bm, std::vector<Job>& jobs) {
+    const size_t n = (size_t)s->n;
+    jobs.clear();
+    for (int j0 = 0; j0 < nrhs; j0 += K) {
+        Job jb{};
+        jb.system = 0; jb.first = j0; jb.nrhs = std::min(K, nrhs - j0);
+        for (int j = 0; j < jb.nrhs; j++) { jb.b[j] = Bm + (j0 + j) * n; jb.x[j] = X + (j0 + j) * n; }
+        jobs.push_back(jb);
+    }
+    return FEEC_OK;
 }
 
 int pick_k(int mode, int rhs_per_team) {
@@ -206,21 +242,77 @@ int feec_system_solve_batch(feec_system* s, int method, int mode, int nrhs, doub
     if (stream) { s->stream = (cudaStream_t)stream; }
     int st = sell_prepare(s, method);
     if (st == FEEC_OK) {
-        const int K = pick_k(mode, rhs_per_team);
+        int K = pick_k(mode, rhs_per_team);
+        int threads = 256;
+        if (rhs_per_team == 0 && s->tuned_k[method][mode] > 0) {
+            K = s->tuned_k[method][mode];
+            threads = s->tuned_threads[method][mode];
+        }
         std::vector<feec_system*> systems{s};
         std::vector<Job> jobs;
-        const size_t n = (size_t)s->n;
-        for (int j0 = 0; j0 < nrhs; j0 += K) {
-            Job jb{};
-            jb.system = 0; jb.first = j0; jb.nrhs = std::min(K, nrhs - j0);
-            for (int j = 0; j < jb.nrhs; j++) { jb.b[j] = Bm + (j0 + j) * n; jb.x[j] = X + (j0 + j) * n; }
-            jobs.push_back(jb);
-        }
+        jobs_for(s, nrhs, K, X, Bm, jobs);
         st = run_batch(s->stream, systems, jobs, method, mode, K, precision, max_iter > 0 ? max_iter : s->n, nrhs,
-                       infos, s->user_blocks);
+                       infos, s->user_blocks, threads);
     }
     s->stream = keep;
     return st;
+}
+
+// Autotuner of the batched engine: for every candidate (right-hand sides per team, team
+// size) it runs a short trial on the system itself — enough columns to fill every
+// resident team once, a fixed number of inner iterations — and keeps the candidate with
+// the highest rate of column-iterations per second. The result is cached for this
+// system and used by feec_system_solve_batch when rhs_per_team is 0.
+int feec_system_tune_batch(feec_system* s, int method, int mode, int nrhs_hint, int* rhs_per_team, int* team_threads,
+                           double* rhs_iters_per_s) {
+    if (!s || (method != FEEC_METHOD_CG && method != FEEC_METHOD_RAINBOW) ||
+        (mode != FEEC_MODE_MIXED && mode != FEEC_MODE_FP64))
+        return FEEC_BADARG;
+    int st = sell_prepare(s, method);
+    if (st != FEEC_OK) return st;
+    const int is_float = mode == FEEC_MODE_MIXED;
+    const int Ks[3] = {1, 2, 4};
+    const int Ts[3] = {128, 256, 512};
+    TunedConfig best;
+    const size_t n = (size_t)s->n;
+    for (int ki = 0; ki < 3; ki++) {
+        const int K = Ks[ki];
+        if (K > batched_max_k(is_float)) continue;
+        for (int ti = 0; ti < 3; ti++) {
+            const int T = Ts[ti];
+            if (batched_team_threads(is_float, T) != T) continue;
+            int cols = batched_resident_teams(is_float, K, method == FEEC_METHOD_RAINBOW, T) * K;
+            if (nrhs_hint > 0 && cols > nrhs_hint) cols = std::max(K, (nrhs_hint / K) * K);
+            DevArena tmp; tmp.stream = s->stream;
+            double *B = nullptr, *X = nullptr;
+            FEEC_TRY(tmp.alloc(B, n * cols)); FEEC_TRY(tmp.alloc(X, n * cols));
+            std::vector<double> ones(n, 1.0);
+            for (int c = 0; c < cols; c++)
+                FEEC_TRY(cudaMemcpyAsync(B + c * n, ones.data(), sizeof(double) * n, cudaMemcpyHostToDevice, s->stream));
+            FEEC_TRY(cudaMemsetAsync(X, 0, sizeof(double) * n * cols, s->stream));
+            std::vector<feec_system*> systems{s};
+            std::vector<Job> jobs;
+            jobs_for(s, cols, K, X, B, jobs);
+            float ms = 0.0f;
+            long long its = 0;
+            const int trial_iters = 12;
+            st = run_batch(s->stream, systems, jobs, method, mode, K, 1e-300, trial_iters, cols, nullptr, 0, T, 1, &ms,
+                           &its);
+            tmp.release();
+            cudaStreamSynchronize(s->stream);
+            if (st != FEEC_OK && st != FEEC_MAXITER) return st;
+            const double rate = ms > 0.0f ? (double)its / (ms * 1e-3) : 0.0;
+            if (rate > best.rhs_iters_per_s) { best.valid = true; best.K = K; best.threads = T; best.rhs_iters_per_s = rate; }
+        }
+    }
+    if (!best.valid) return FEEC_CUDA_ERROR;
+    s->tuned_k[method][mode] = best.K;
+    s->tuned_threads[method][mode] = best.threads;
+    s->tuned_rate[method][mode] = best.rhs_iters_per_s;
+    if (rhs_per_team) *rhs_per_team = best.K;
+    if (team_threads) *team_threads = best.threads;
+    if (rhs_iters_per_s) *rhs_iters_per_s = best.rhs_iters_per_s;
+    return FEEC_OK;
 }
 
 int feec_solve_many(int nsys, feec_system* const* systems, int method, int mode, double* const* x,
@@ -246,7 +338,7 @@ int feec_solve_many(int nsys, feec_system* const* systems, int method, int mode,
         std::memset(&jb, 0, sizeof(jb));
         jb.system = i; jb.nrhs = 1; jb.first = i; jb.b[0] = b[i]; jb.x[0] = x[i];
     }
-    return run_batch(st, sys, jobs, method, mode, 1, precision, max_iter > 0 ? max_iter : maxn, nsys, infos, 0);
+    return run_batch(st, sys, jobs, method, mode, 1, precision, max_iter > 0 ? max_iter : maxn, nsys, infos, 0, 256);
 }
 
 }  // extern "C"

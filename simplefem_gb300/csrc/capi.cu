@@ -78,6 +78,11 @@ using namespace feec;
 
 
 
+namespace feec {
+int sell_prepare(feec_system* s, int method);
+SellView sell_view(const feec_system* s, int method);
+}
+
 namespace {
 
 int ensure_work(feec_system* s) {
@@ -198,6 +203,18 @@ int solve_core(feec_system* s, int method, int mode, double* xx, const double* b
 
     LaunchShape shape;
     shape.lanes = s->lanes;
+    // Measured on GB300 (3D P2 operator, 28 entries per row): the FP64 persistent
+    // solvers issue FP64 at 2 lanes/clk/SM, so per-row reductions across lanes and
+    // per-group epilogues cost more than they save; one thread per row is fastest for
+    // plain FP64 CG and 4 lanes per row for the sweeps of the preconditioned solvers.
+    if (method == FEEC_METHOD_CG && mode != FEEC_MODE_MIXED) shape.lanes = 1;
+    else if (shape.lanes > 4) shape.lanes = 4;
+    if (shape.lanes == 1 || shape.lanes == 4) {
+        // two co-resident blocks per SM were fastest in the same measurements
+        int dev_sms = 0;
+        cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, s->dev);
+        shape.blocks = 2 * dev_sms;
+    }
     if (permuted && s->max_phase_rows > 0) {
         // one pass over the largest sweep phase: enough row groups in the co-resident grid
         const int maxb = max_coresident_blocks(1, 0, shape.lanes, 512);
@@ -392,6 +409,7 @@ int build_layout(feec_system* s, int method, const double* diag_dev, double omeg
     s->omega = omega;
     s->num_levels = num_levels;
     s->prepared = method;
+    s->sell[1].ready = false;   // the Rainbow-order SELL copy follows the new ordering
     return FEEC_OK;
 }
 
@@ -435,7 +453,10 @@ int feec_system_create(feec_system** out, int N, const int* A, const int* C, con
     if (!s) return FEEC_OOM;
     s->dev = dev;
     s->n = N;
-    s->stream = stream ? (cudaStream_t)stream : lib_stream;
+    // NULL means CUDA's default stream (stream 0), so the system is ordered with other
+    // work the caller issues there (e.g. a framework's default stream)
+    (void)lib_stream;
+    s->stream = (cudaStream_t)stream;
     s->mem.stream = s->stream;
     s->work.stream = s->stream;
     int nnz = 0;
@@ -478,6 +499,8 @@ int feec_system_create(feec_system** out, int N, const int* A, const int* C, con
 int feec_system_destroy(feec_system* s) {
     if (!s) return FEEC_OK;
     s->work.release();
+    s->sell[0].mem.release();
+    s->sell[1].mem.release();
     s->mem.release();
     cudaStreamSynchronize(s->stream);
     if (s->ev0) cudaEventDestroy(s->ev0);
@@ -598,9 +621,34 @@ int feec_system_solve(feec_system* s, int method, int mode, double* x, const dou
 
 int feec_system_apply(feec_system* s, const double* x, double* y, double scaling, void* stream) {
     if (!s || !x || !y) return FEEC_BADARG;
-    cudaStream_t st = stream ? (cudaStream_t)stream : s->stream;
-    FEEC_TRY(launch_spmv_f64(s->n, s->A, s->C, s->V, x, y, scaling, s->lanes, st));
-    return FEEC_OK;
+    cudaStream_t keep = s->stream;
+    if (stream) s->stream = (cudaStream_t)stream;
+    int e = FEEC_OK;
+    if (s->user_lanes > 0) {
+        // launch-shape override: the CSR kernel with the requested lanes per row
+        e = cuda_status(launch_spmv_f64(s->n, s->A, s->C, s->V, x, y, scaling, s->user_lanes, s->stream));
+    } else {
+        e = sell_prepare(s, FEEC_METHOD_CG);
+        if (e == FEEC_OK) {
+            const SellView v = sell_view(s, FEEC_METHOD_CG);
+            e = cuda_status(launch_sell_spmv(v, 0, x, y, scaling, s->stream));
+        }
+    }
+    s->stream = keep;
+    return e;
+}
+
+int feec_system_apply_f32(feec_system* s, const float* x, float* y, float scaling, void* stream) {
+    if (!s || !x || !y) return FEEC_BADARG;
+    cudaStream_t keep = s->stream;
+    if (stream) s->stream = (cudaStream_t)stream;
+    int e = sell_prepare(s, FEEC_METHOD_CG);
+    if (e == FEEC_OK) {
+        const SellView v = sell_view(s, FEEC_METHOD_CG);
+        e = cuda_status(launch_sell_spmv(v, 1, x, y, (double)scaling, s->stream));
+    }
+    s->stream = keep;
+    return e;
 }
 
 // ---------------------------------------------------------------------------

@@ -54,8 +54,15 @@ struct BatchArgs {
     int max_outer;
 };
 
-cudaError_t launch_batched(const BatchArgs& args, int is_float, int K, int rainbow, int teams, cudaStream_t s);
+cudaError_t launch_batched(const BatchArgs& args, int is_float, int K, int rainbow, int threads, int teams,
+                           cudaStream_t s);
+int batched_resident_teams(int is_float, int K, int rainbow, int threads);
+int batched_team_threads(int is_float, int requested);
 int batched_max_k(int is_float);
+
+// y = scaling * A x over a natural-order SELL-32 layout; is_float selects FP32 data
+// (x, y float) or FP64 (x, y double). One thread per row, coalesced entry loads.
+cudaError_t launch_sell_spmv(const SellView& v, int is_float, const void* x, void* y, double scaling, cudaStream_t s);
 
 // SELL construction (kernels_setup.cu)
 cudaError_t launch_sell_lengths(int nslices, const int* slice_row0, const int* slice_nrow, const int* rp,

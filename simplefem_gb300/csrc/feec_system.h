@@ -50,6 +50,17 @@ struct DevArena {
 
 int init_device(int& dev, cudaStream_t& stream);
 
+// A SELL-32 copy of a system's matrix (see SellView).
+struct SellData {
+    DevArena mem;
+    bool ready = false;
+    int nslices = 0, ncolors = 0;
+    int* slice_row0 = nullptr; int* slice_nrow = nullptr; int4* slice_len = nullptr; long long* slice_off = nullptr;
+    int* color_slice = nullptr; int* ci = nullptr; float* val32 = nullptr; double* val64 = nullptr;
+    int* ident = nullptr;
+    long long entries = 0;
+};
+
 }  // namespace feec
 
 struct feec_system {
@@ -85,12 +96,10 @@ struct feec_system {
     int user_blocks = 0;        // launch-shape overrides (0 = automatic)
     int user_lanes = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-    // SELL-32 layout for the batched engine (valid if sell_method >= 0)
-    int sell_method = -1;
-    feec::DevArena sell;
-    int nslices = 0, sell_ncolors = 0;
-    int* slice_row0 = nullptr; int* slice_nrow = nullptr; int4* slice_len = nullptr; long long* slice_off = nullptr;
-    int* color_slice = nullptr; int* sci = nullptr; float* sval32 = nullptr; double* sval64 = nullptr;
-    int* ident = nullptr;
-    long long sell_entries = 0;
+    // SELL-32 layouts: [0] natural row order (SpMV, batched plain CG), [1] Rainbow order
+    feec::SellData sell[2];
+    // batched-engine launch choice made by the autotuner, per [method][mode] (0 = not tuned)
+    int tuned_k[3][3] = {};
+    int tuned_threads[3][3] = {};
+    double tuned_rate[3][3] = {};
 };

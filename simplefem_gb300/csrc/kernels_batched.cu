@@ -27,7 +27,30 @@ namespace feec {
 
 namespace {
 
-constexpr int kTeamThreads = 256;
+// L2 eviction priorities: every team of a batch streams the same matrix, while each
+// team's vectors are private and touched once per phase. Matrix loads carry an
+// evict_last cache policy so the shared operator stays in L2; row-local vector
+// traffic uses streaming (evict-first) loads and stores.
+__device__ __forceinline__ unsigned long long l2_keep_policy() {
+    unsigned long long p;
+    asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+__device__ __forceinline__ int ld_keep(const int* a, unsigned long long pol) {
+    int v;
+    asm volatile("ld.global.nc.L2::cache_hint.b32 %0, [%1], %2;" : "=r"(v) : "l"(a), "l"(pol));
+    return v;
+}
+__device__ __forceinline__ float ld_keep(const float* a, unsigned long long pol) {
+    float v;
+    asm volatile("ld.global.nc.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(v) : "l"(a), "l"(pol));
+    return v;
+}
+__device__ __forceinline__ double ld_keep(const double* a, unsigned long long pol) {
+    double v;
+    asm volatile("ld.global.nc.L2::cache_hint.f64 %0, [%1], %2;" : "=d"(v) : "l"(a), "l"(pol));
+    return v;
+}
 
 template <typename T, int K> struct Vec;
 template <> struct Vec<float, 1> { using t = float; };
@@ -66,14 +89,15 @@ template <typename T, typename TV, int K>
 __device__ __forceinline__ void block_dot(const int* __restrict__ sci, const TV* __restrict__ sval, long long off,
                                           int len, int lane, const T* X, T (&s)[K]) {
     constexpr int CH = Chunk<T, K>::value;
+    const unsigned long long pol = l2_keep_policy();
     for (int k0 = 0; k0 < len; k0 += CH) {
         int c[CH]; T v[CH];
         #pragma unroll
         for (int u = 0; u < CH; u++) {
             const bool ok = k0 + u < len;
             const long long p = off + (long long)(k0 + u) * 32 + lane;
-            c[u] = ok ? __ldg(&sci[p]) : -1;
-            v[u] = ok ? (T)__ldg(&sval[p]) : T(0);
+            c[u] = ok ? ld_keep(&sci[p], pol) : -1;
+            v[u] = ok ? (T)ld_keep(&sval[p], pol) : T(0);
         }
         T xv[CH][K];
         #pragma unroll
@@ -152,9 +176,28 @@ __device__ __forceinline__ void for_slices(const SellView& S, int s0, int s1, F&
 }
 
 template <typename T, int K>
+__device__ __forceinline__ void load_k_stream(const T* p, T (&v)[K]) {
+    if constexpr (K == 1) {
+        v[0] = __ldcs(p);
+    } else if constexpr (K == 2) {
+        const typename Vec<T, 2>::t u = __ldcs(reinterpret_cast<const typename Vec<T, 2>::t*>(p));
+        v[0] = u.x; v[1] = u.y;
+    } else if constexpr (K == 4 && sizeof(T) == 4) {
+        const float4 u = __ldcs(reinterpret_cast<const float4*>(p));
+        v[0] = u.x; v[1] = u.y; v[2] = u.z; v[3] = u.w;
+    } else {
+        #pragma unroll
+        for (int j = 0; j < K; j += 2) {
+            const double2 u = __ldcs(reinterpret_cast<const double2*>(p + j));
+            v[j] = u.x; v[j + 1] = u.y;
+        }
+    }
+}
+
+template <typename T, int K>
 __device__ __forceinline__ void load_row(const T* v, int row, bool act, T (&out)[K]) {
     if (act) {
-        load_k<T, K>(v + (long long)row * K, out);
+        load_k_stream<T, K>(v + (long long)row * K, out);
     } else {
         #pragma unroll
         for (int j = 0; j < K; j++) out[j] = T(0);
@@ -163,8 +206,18 @@ __device__ __forceinline__ void load_row(const T* v, int row, bool act, T (&out)
 
 template <typename T, int K>
 __device__ __forceinline__ void store_row(T* v, int row, const T (&in)[K]) {
-    #pragma unroll
-    for (int j = 0; j < K; j++) v[(long long)row * K + j] = in[j];
+    T* p = v + (long long)row * K;
+    if constexpr (K == 1) {
+        __stcs(p, in[0]);
+    } else if constexpr (K == 2) {
+        typename Vec<T, 2>::t u; u.x = in[0]; u.y = in[1];
+        __stcs(reinterpret_cast<typename Vec<T, 2>::t*>(p), u);
+    } else if constexpr (K == 4 && sizeof(T) == 4) {
+        __stcs(reinterpret_cast<float4*>(p), make_float4(in[0], in[1], in[2], in[3]));
+    } else {
+        #pragma unroll
+        for (int j = 0; j < K; j += 2) __stcs(reinterpret_cast<double2*>(p + j), make_double2(in[j], in[j + 1]));
+    }
 }
 
 // One team solves work item `it` completely.
@@ -526,8 +579,8 @@ __device__ void team_solve(const BatchArgs& args, const BatchItem& it) {
     }
 }
 
-template <typename T, int K, bool RAINBOW>
-__global__ void __launch_bounds__(kTeamThreads, 2) batched_solve_kernel(BatchArgs args) {
+template <typename T, int K, bool RAINBOW, int THREADS>
+__global__ void __launch_bounds__(THREADS) batched_solve_kernel(BatchArgs args) {
     __shared__ int s_item;
     while (true) {
         if (threadIdx.x == 0) s_item = atomicAdd(args.next_item, 1);
@@ -540,36 +593,52 @@ __global__ void __launch_bounds__(kTeamThreads, 2) batched_solve_kernel(BatchArg
 }
 
 template <typename T, int K, bool RB>
-const void* kfn() { return (const void*)batched_solve_kernel<T, K, RB>; }
-
-const void* pick(int is_float, int K, int rainbow) {
-    if (is_float) {
-        if (rainbow) return K == 1 ? kfn<float, 1, true>() : K == 2 ? kfn<float, 2, true>() : kfn<float, 4, true>();
-        return K == 1 ? kfn<float, 1, false>() : K == 2 ? kfn<float, 2, false>() : kfn<float, 4, false>();
+const void* kfn(int threads) {
+    if constexpr (sizeof(T) == 4) {
+        if (threads == 128) return (const void*)batched_solve_kernel<T, K, RB, 128>;
+        if (threads == 512) return (const void*)batched_solve_kernel<T, K, RB, 512>;
     }
-    if (rainbow) return K == 1 ? kfn<double, 1, true>() : kfn<double, 2, true>();
-    return K == 1 ? kfn<double, 1, false>() : kfn<double, 2, false>();
+    return (const void*)batched_solve_kernel<T, K, RB, 256>;
+}
+
+const void* pick(int is_float, int K, int rainbow, int threads) {
+    if (is_float) {
+        if (rainbow) return K == 1 ? kfn<float, 1, true>(threads) : K == 2 ? kfn<float, 2, true>(threads) : kfn<float, 4, true>(threads);
+        return K == 1 ? kfn<float, 1, false>(threads) : K == 2 ? kfn<float, 2, false>(threads) : kfn<float, 4, false>(threads);
+    }
+    if (rainbow) return K == 1 ? kfn<double, 1, true>(threads) : kfn<double, 2, true>(threads);
+    return K == 1 ? kfn<double, 1, false>(threads) : kfn<double, 2, false>(threads);
 }
 
 }  // namespace
 
 int batched_max_k(int is_float) { return is_float ? 4 : 2; }
 
-cudaError_t launch_batched(const BatchArgs& args, int is_float, int K, int rainbow, int teams, cudaStream_t s) {
-    const void* fn = pick(is_float, K, rainbow);
-    if (teams <= 0) {
-        int dev = 0, sms = 0, per = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, kTeamThreads, 0);
-        teams = sms * (per > 0 ? per : 1);
-    }
+int batched_team_threads(int is_float, int requested) {
+    if (!is_float) return 256;
+    return (requested == 128 || requested == 512) ? requested : 256;
+}
+
+int batched_resident_teams(int is_float, int K, int rainbow, int threads) {
+    threads = batched_team_threads(is_float, threads);
+    const void* fn = pick(is_float, K, rainbow, threads);
+    int dev = 0, sms = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, threads, 0);
+    return sms * (per > 0 ? per : 1);
+}
+
+cudaError_t launch_batched(const BatchArgs& args, int is_float, int K, int rainbow, int threads, int teams, cudaStream_t s) {
+    threads = batched_team_threads(is_float, threads);
+    const void* fn = pick(is_float, K, rainbow, threads);
+    if (teams <= 0) teams = batched_resident_teams(is_float, K, rainbow, threads);
     if (teams > args.nitems) teams = args.nitems;
     if (teams <= 0) return cudaSuccess;
     BatchArgs copy = args;
     void* kargs[] = {&copy};
     note_launch();
-    return cudaLaunchKernel(fn, dim3(teams), dim3(kTeamThreads), kargs, 0, s);
+    return cudaLaunchKernel(fn, dim3(teams), dim3(threads), kargs, 0, s);
 }
 
 }  // namespace feec

@@ -252,6 +252,43 @@ __global__ void sell_fill_kernel(int nslices, const int* __restrict__ row0, cons
     }
 }
 
+// SELL-32 SpMV, one thread per row. The matrix is streamed once (evict-first loads,
+// so it does not push x out of L2); a chunk of column indices and values is loaded
+// before its gathers so every warp keeps several requests in flight.
+template <typename T>
+__global__ void __launch_bounds__(256) sell_spmv_kernel(SellView v, const T* __restrict__ x, T* __restrict__ y, T scaling) {
+    const T* __restrict__ val = sizeof(T) == 4 ? (const T*)v.val32 : (const T*)v.val64;
+    const int lane = threadIdx.x & 31;
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    for (int sl = gw; sl < v.nslices; sl += nw) {
+        const int row0 = __ldg(&v.slice_row0[sl]);
+        const int nrow = __ldg(&v.slice_nrow[sl]);
+        const int4 len = __ldg(&v.slice_len[sl]);
+        const long long off = __ldg(&v.slice_off[sl]);
+        const int L = len.x + len.y + len.z;
+        T s = T(0);
+        constexpr int CH = 8;
+        for (int k0 = 0; k0 < L; k0 += CH) {
+            int c[CH]; T a[CH];
+            #pragma unroll
+            for (int u = 0; u < CH; u++) {
+                const bool ok = k0 + u < L;
+                const long long p = off + (long long)(k0 + u) * 32 + lane;
+                c[u] = ok ? __ldcs(&v.ci[p]) : 0;
+                a[u] = ok ? __ldcs(&val[p]) : T(0);
+            }
+            T xv[CH];
+            #pragma unroll
+            for (int u = 0; u < CH; u++) xv[u] = __ldg(&x[c[u]]);
+            #pragma unroll
+            for (int u = 0; u < CH; u++) s = fma(a[u], xv[u], s);
+        }
+        // FP64 issues at 2 lanes/clk/SM on this part: skip the multiply when scaling == 1
+        if (lane < nrow) y[row0 + lane] = scaling == T(1) ? s : scaling * s;
+    }
+}
+
 // ---- exclusive scan of int32 (three-phase, 4096 elements per block) ----
 constexpr int kScanThreads = 1024;
 constexpr int kScanItems = 4;
@@ -417,6 +454,17 @@ cudaError_t launch_scaled_cast(int n, const double* r, const double* inv_norm_de
 
 cudaError_t launch_update_x(int n, const int* perm, const float* c32, const double* norm_dev, double* x, cudaStream_t s) {
     return launch(update_x_kernel, grid_for(n, kBlock), kBlock, s, n, perm, c32, norm_dev, x);
+}
+
+cudaError_t launch_sell_spmv(const SellView& v, int is_float, const void* x, void* y, double scaling, cudaStream_t s) {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    int grid = grid_for((long long)v.nslices * 32, 256);
+    if (grid > sms * 8) grid = sms * 8;
+    if (is_float)
+        return launch(sell_spmv_kernel<float>, grid, 256, s, v, (const float*)x, (float*)y, (float)scaling);
+    return launch(sell_spmv_kernel<double>, grid, 256, s, v, (const double*)x, (double*)y, scaling);
 }
 
 cudaError_t launch_sell_lengths(int nslices, const int* slice_row0, const int* slice_nrow, const int* rp,

@@ -89,9 +89,22 @@ class System:
             raise _native.FeecError(st, "feec_system_solve_batch")
         return [i.as_dict() for i in infos]
 
+    def tune_batch(self, method="rainbow", mode="mixed", nrhs_hint=0) -> dict:
+        """Run the batched-engine autotuner on this system; the choice is used by solve_batch
+        calls with rhs_per_team=0."""
+        k = ctypes.c_int(0); t = ctypes.c_int(0); rate = ctypes.c_double(0.0)
+        st = self._lib.feec_system_tune_batch(self._h, METHODS[method], MODES[mode], int(nrhs_hint), ctypes.byref(k),
+                                              ctypes.byref(t), ctypes.byref(rate))
+        _native.check(st, "feec_system_tune_batch")
+        return {"rhs_per_team": k.value, "team_threads": t.value, "rhs_iters_per_s": rate.value}
+
     def apply(self, x, y, scaling=1.0):
-        _native.check(self._lib.feec_system_apply(self._h, _ptr(x), _ptr(y), float(scaling), _stream()),
-                      "feec_system_apply")
+        """y = scaling * A x for device tensors (float64, or float32 on the FP32 values)."""
+        if x.dtype.itemsize == 4:
+            st = self._lib.feec_system_apply_f32(self._h, _ptr(x), _ptr(y), float(scaling), _stream())
+        else:
+            st = self._lib.feec_system_apply(self._h, _ptr(x), _ptr(y), float(scaling), _stream())
+        _native.check(st, "feec_system_apply")
 
     def set_launch(self, blocks=0, lanes=0):
         """Override the persistent grid size / lanes per row (0 = automatic)."""

@@ -226,3 +226,26 @@ def test_launch_counter_counts_kernels(cuda):
     n = len(g["A"]) - 1
     S.ConjugateGradientSolverCSR(n, np.zeros(n), g["b"], g["A"], g["C"], g["V"], np.zeros(n), 1e-10, -3)
     assert _native.gpu().feec_kernel_launches() > before
+
+
+@pytest.mark.parametrize("name", ["fem3d_p2_l3", "fem2d_p1_l6", "fem2d_p3_l2_coef", "lap5_n32"])
+def test_system_apply_sell_matches_reference(cuda, name):
+    """Resident SpMV (SELL-32, FP64 and FP32 values) against MatrixCSR::apply's output."""
+    torch = cuda
+    from simplefem_gb300.system import System
+    g = load_golden(name)
+    n = len(g["A"]) - 1
+    sysm = System(g["A"], g["C"], g["V"])
+    x = torch.from_numpy(g["b"]).cuda()
+    y = torch.empty(n, dtype=torch.float64, device="cuda")
+    sysm.apply(x, y, 0.7)
+    ref = g["apply_out"]
+    assert np.max(np.abs(y.cpu().numpy() - ref)) <= 1e-13 * np.max(np.abs(ref))
+    y32 = torch.empty(n, dtype=torch.float32, device="cuda")
+    sysm.apply(x.float(), y32, 0.7)
+    assert np.max(np.abs(y32.double().cpu().numpy() - ref)) <= 2e-6 * np.max(np.abs(ref))
+    for lanes in (1, 4, 8):                      # CSR kernel through the launch-shape override
+        sysm.set_launch(0, lanes)
+        sysm.apply(x, y, 0.7)
+        assert np.max(np.abs(y.cpu().numpy() - ref)) <= 1e-13 * np.max(np.abs(ref))
+    sysm.close()
