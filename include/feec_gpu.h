@@ -195,6 +195,51 @@ int feec_cg_csr_noalloc(int N, double* x, const double* b,
                         feec_solve_info* info, void* stream);
 
 /* ---------------------------------------------------------------------------
+ * Serving loop with continuous batching. A server owns `slots` worker slots; each
+ * submitted request (one SPD solve) waits in a FIFO queue until a slot is free and
+ * the device memory budget has room for its estimated footprint, then is set up
+ * (matrix upload, Rainbow coloring, multicolor SSOR layout) and solved as one
+ * thread-block cluster on the slot's own stream, overlapping with the requests in
+ * the other slots. method: FEEC_METHOD_RAINBOW or FEEC_METHOD_CG; mode:
+ * FEEC_MODE_MIXED or FEEC_MODE_FP64 (true FP64 relative residual <= precision).
+ * ------------------------------------------------------------------------- */
+
+typedef struct feec_server feec_server;
+
+typedef struct feec_request_result {
+    long long id;
+    int n;                   /* unknowns                                            */
+    int status;              /* feec_status of the solve                            */
+    int iterations;          /* inner iterations                                    */
+    int outer_iterations;    /* FP64 defect-correction steps                        */
+    int cluster_blocks;      /* thread blocks of the cluster that solved it         */
+    int pad;
+    double true_relres;      /* ||b - A x|| / ||b|| in FP64 at the end               */
+    double t_submit_ms;      /* host steady-clock times since the server started    */
+    double t_start_ms;       /* solve launched (after admission and set-up)         */
+    double t_end_ms;         /* solution copied back                                */
+} feec_request_result;
+
+int feec_server_create(feec_server** srv, size_t hbm_budget_bytes, int slots, int method, int mode);
+
+/* Queues one request. Host arrays A, C, V (N x N CSR), b and the output x must stay
+ * valid until the request is reported by feec_server_poll. *id identifies it.
+ * FEEC_OOM if its estimated footprint exceeds the whole budget. */
+int feec_server_submit(feec_server* srv, int N, const int* A, const int* C, const double* V,
+                       const double* b, double* x, double precision, long long* id);
+
+/* Moves up to max_out finished requests into out; *nout receives their number. */
+int feec_server_poll(feec_server* srv, feec_request_result* out, int max_out, int* nout);
+
+/* Blocks until every submitted request has finished (FEEC_TIMEOUT after timeout_s). */
+int feec_server_wait(feec_server* srv, double timeout_s);
+
+int feec_server_stats(feec_server* srv, size_t* bytes_in_use, size_t* peak_bytes, int* inflight, long long* queued);
+
+/* Finishes the queued requests, then stops the slots. */
+int feec_server_destroy(feec_server* srv);
+
+/* ---------------------------------------------------------------------------
  * Library information.
  * ------------------------------------------------------------------------- */
 

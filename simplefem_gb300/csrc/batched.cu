@@ -272,15 +272,16 @@ int feec_system_tune_batch(feec_system* s, int method, int mode, int nrhs_hint, 
     if (st != FEEC_OK) return st;
     const int is_float = mode == FEEC_MODE_MIXED;
     const int Ks[3] = {1, 2, 4};
-    const int Ts[3] = {128, 256, 512};
+    const int Ts[4] = {128, 256, 512, 1024};
     TunedConfig best;
     const size_t n = (size_t)s->n;
     for (int ki = 0; ki < 3; ki++) {
         const int K = Ks[ki];
         if (K > batched_max_k(is_float)) continue;
-        for (int ti = 0; ti < 3; ti++) {
+        for (int ti = 0; ti < 4; ti++) {
             const int T = Ts[ti];
             if (batched_team_threads(is_float, T) != T) continue;
+            if (T == 1024 && K > 2) continue;
             int cols = batched_resident_teams(is_float, K, method == FEEC_METHOD_RAINBOW, T) * K;
             if (nrhs_hint > 0 && cols > nrhs_hint) cols = std::max(K, (nrhs_hint / K) * K);
             DevArena tmp; tmp.stream = s->stream;

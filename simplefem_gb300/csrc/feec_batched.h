@@ -57,6 +57,9 @@ struct BatchArgs {
 cudaError_t launch_batched(const BatchArgs& args, int is_float, int K, int rainbow, int threads, int teams,
                            cudaStream_t s);
 int batched_resident_teams(int is_float, int K, int rainbow, int threads);
+// One request per launch on a cluster of `blocks` thread blocks (kernels_cluster.cu).
+cudaError_t launch_cluster(const BatchArgs& args, int item, int is_float, int rainbow, int blocks, cudaStream_t s);
+int cluster_max_blocks(int is_float, int rainbow);
 int batched_team_threads(int is_float, int requested);
 int batched_max_k(int is_float);
 

@@ -1,0 +1,289 @@
+// Serving loop with continuous batching.
+//
+// A feec_server owns `slots` worker threads. Requests (one SPD solve each: a CSR
+// matrix, a right-hand side, a tolerance) wait in a FIFO queue; a free slot takes
+// the next request as soon as the device memory budget has room for it, uploads
+// the matrix, builds the reference's Rainbow coloring and the multicolor SSOR
+// layout, and launches the whole solve as one thread-block cluster on the slot's
+// own stream. Requests that arrive while others run are admitted as slots and
+// memory free up, and their kernels overlap on the GPU; every request's matrix and
+// Krylov vectors stay on the device until it completes. Timing of each request
+// (submission, start of its solve, completion) is recorded for latency reports.
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <mutex>
+#include <new>
+#include <thread>
+#include <vector>
+
+#include "feec_batched.h"
+#include "feec_device.cuh"
+#include "feec_system.h"
+
+using namespace feec;
+
+namespace feec {
+int sell_prepare(feec_system* s, int method);
+SellView sell_view(const feec_system* s, int method);
+}
+
+namespace {
+
+using clock_type = std::chrono::steady_clock;
+
+struct Request {
+    long long id = 0;
+    int n = 0;
+    const int* A = nullptr; const int* C = nullptr; const double* V = nullptr;
+    const double* b = nullptr;
+    double* x = nullptr;
+    double precision = 1e-10;
+    size_t bytes = 0;
+    clock_type::time_point t_submit;
+};
+
+size_t estimate_bytes(int n, long long nnz) {
+    // original CSR + FP32 values, permuted [L|E|U] copy (FP64 + FP32), SELL copy with
+    // padding (int + FP32 + FP64), row arrays, solver vectors
+    return (size_t)(nnz * (12 + 4 + 16 + 16 * 5 / 4)) + (size_t)n * 200 + (32u << 20);
+}
+
+}  // namespace
+
+struct feec_server {
+    int method = FEEC_METHOD_RAINBOW;
+    int mode = FEEC_MODE_MIXED;
+    size_t budget = 0;
+    int device = 0;
+    std::atomic<size_t> in_use{0};
+    std::atomic<size_t> peak{0};
+    std::atomic<int> inflight{0};
+    std::mutex mu;
+    std::condition_variable cv;        // queue / budget / shutdown changes
+    std::deque<Request> queue;
+    std::vector<feec_request_result> done;
+    std::vector<std::thread> workers;
+    bool stop = false;
+    long long next_id = 1;
+    long long submitted = 0, finished = 0;
+    clock_type::time_point t0;
+};
+
+namespace {
+
+double ms_since(const feec_server* srv, clock_type::time_point t) {
+    return std::chrono::duration<double, std::milli>(t - srv->t0).count();
+}
+
+// Sets up and solves one request on `stream`; fills `res`.
+int serve_one(feec_server* srv, const Request& rq, cudaStream_t stream, feec_request_result& res) {
+    feec_system* s = nullptr;
+    int st = feec_system_create(&s, rq.n, rq.A, rq.C, rq.V, 1, stream);
+    if (st != FEEC_OK) return st;
+    struct Guard { feec_system* s; ~Guard() { feec_system_destroy(s); } } guard{s};
+    const bool rainbow = srv->method == FEEC_METHOD_RAINBOW;
+    if (rainbow) {
+        // the reference's Rainbow ordering (sparse/rainbow.cpp:14-130) and the diagonal
+        std::vector<int> F((size_t)rq.n), B((size_t)rq.n + 1), R((size_t)rq.n);
+        int nc = 0;
+        st = feec_rainbow(rq.n, rq.A, rq.C, &nc, F.data(), B.data(), R.data());
+        if (st != FEEC_OK) return st;
+        std::vector<double> diag((size_t)rq.n, 0.0);
+        for (int r = 0; r < rq.n; r++)
+            for (int k = rq.A[r]; k < rq.A[r + 1]; k++)
+                if (rq.C[k] == r) diag[r] += rq.V[k];
+        st = feec_system_set_rainbow(s, diag.data(), 1.0, nc, F.data(), B.data(), R.data(), 1);
+        if (st != FEEC_OK) return st;
+    }
+    st = sell_prepare(s, rainbow ? FEEC_METHOD_RAINBOW : FEEC_METHOD_CG);
+    if (st != FEEC_OK) return st;
+    const int is_float = srv->mode == FEEC_MODE_MIXED;
+    const size_t n = (size_t)rq.n;
+    const size_t tsz = is_float ? sizeof(float) : sizeof(double);
+    DevArena mem;
+    mem.stream = stream;
+    struct MemGuard { DevArena* m; ~MemGuard() { m->release(); } } mguard{&mem};
+    double *b = nullptr, *x = nullptr;
+    char* w = nullptr;
+    SellView* dview = nullptr;
+    BatchItem* ditem = nullptr;
+    BatchResult* dres = nullptr;
+    FEEC_TRY(mem.alloc(b, n)); FEEC_TRY(mem.alloc(x, n));
+    BatchItem it{};
+    FEEC_TRY(mem.alloc(it.xp, n)); FEEC_TRY(mem.alloc(it.bp, n)); FEEC_TRY(mem.alloc(it.r64, n));
+    FEEC_TRY(mem.alloc(w, 6 * n * tsz));
+    FEEC_TRY(mem.alloc(dview, 1)); FEEC_TRY(mem.alloc(ditem, 1)); FEEC_TRY(mem.alloc(dres, 1));
+    it.r = w; it.d = w + n * tsz; it.z = w + 2 * n * tsz; it.m = w + 3 * n * tsz; it.q = w + 4 * n * tsz;
+    it.c = w + 5 * n * tsz;
+    it.system = 0; it.nrhs = 1; it.first_result = 0;
+    it.b[0] = b; it.x[0] = x;
+    const SellView view = sell_view(s, rainbow ? FEEC_METHOD_RAINBOW : FEEC_METHOD_CG);
+    FEEC_TRY(cudaMemcpyAsync(b, rq.b, sizeof(double) * n, cudaMemcpyHostToDevice, stream));
+    FEEC_TRY(cudaMemsetAsync(x, 0, sizeof(double) * n, stream));
+    FEEC_TRY(cudaMemcpyAsync(dview, &view, sizeof(view), cudaMemcpyHostToDevice, stream));
+    FEEC_TRY(cudaMemcpyAsync(ditem, &it, sizeof(it), cudaMemcpyHostToDevice, stream));
+    FEEC_TRY(cudaMemsetAsync(dres, 0, sizeof(BatchResult), stream));
+    BatchArgs a{};
+    a.systems = dview; a.items = ditem; a.nitems = 1; a.next_item = nullptr; a.results = dres;
+    a.precision = rq.precision;
+    a.inner_eta = is_float ? 2e-5 : 1e-30;
+    a.inner_margin = is_float ? 0.3 : 1.0;
+    a.max_iter = rq.n;
+    a.max_outer = is_float ? 12 : 4;
+    // cluster size from the work per iteration: about 0.5 M stored entries per block
+    const long long nnz = view.nslices > 0 ? s->nnz : 0;
+    int blocks = (int)std::min<long long>(16, std::max<long long>(1, nnz / 500000));
+    const int maxb = cluster_max_blocks(is_float, rainbow);
+    if (blocks > maxb) blocks = maxb;
+    // powers of two only
+    int p2 = 1;
+    while (p2 * 2 <= blocks) p2 *= 2;
+    blocks = p2;
+    res.t_start_ms = ms_since(srv, clock_type::now());
+    FEEC_TRY(launch_cluster(a, 0, is_float, rainbow, blocks, stream));
+    BatchResult hr{};
+    FEEC_TRY(cudaMemcpyAsync(&hr, dres, sizeof(hr), cudaMemcpyDeviceToHost, stream));
+    FEEC_TRY(cudaMemcpyAsync(rq.x, x, sizeof(double) * n, cudaMemcpyDeviceToHost, stream));
+    FEEC_TRY(cudaStreamSynchronize(stream));
+    res.status = hr.status;
+    res.iterations = hr.iterations;
+    res.outer_iterations = hr.outer;
+    res.true_relres = hr.relres;
+    res.cluster_blocks = blocks;
+    return hr.status;
+}
+
+void worker_loop(feec_server* srv) {
+    cudaSetDevice(srv->device);
+    cudaStream_t stream = nullptr;
+    if (cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking) != cudaSuccess) return;
+    while (true) {
+        Request rq;
+        {
+            std::unique_lock<std::mutex> lk(srv->mu);
+            // FIFO admission: the head request waits until the budget has room for it
+            srv->cv.wait(lk, [&] {
+                return srv->stop || (!srv->queue.empty() && srv->in_use.load() + srv->queue.front().bytes <= srv->budget);
+            });
+            if (srv->stop && srv->queue.empty()) break;
+            if (srv->queue.empty()) continue;
+            rq = srv->queue.front();
+            srv->queue.pop_front();
+            srv->in_use += rq.bytes;
+            size_t cur = srv->in_use.load();
+            size_t pk = srv->peak.load();
+            while (cur > pk && !srv->peak.compare_exchange_weak(pk, cur)) {}
+            srv->inflight++;
+        }
+        srv->cv.notify_all();
+        feec_request_result res;
+        std::memset(&res, 0, sizeof(res));
+        res.id = rq.id;
+        res.n = rq.n;
+        res.t_submit_ms = ms_since(srv, rq.t_submit);
+        const int st = serve_one(srv, rq, stream, res);
+        if (st != FEEC_OK && res.status == FEEC_OK) res.status = st;
+        res.t_end_ms = ms_since(srv, clock_type::now());
+        {
+            std::lock_guard<std::mutex> lk(srv->mu);
+            srv->in_use -= rq.bytes;
+            srv->inflight--;
+            srv->finished++;
+            srv->done.push_back(res);
+        }
+        srv->cv.notify_all();
+    }
+    cudaStreamSynchronize(stream);
+    cudaStreamDestroy(stream);
+}
+
+}  // namespace
+
+extern "C" {
+
+int feec_server_create(feec_server** out, size_t hbm_budget_bytes, int slots, int method, int mode) {
+    if (!out || hbm_budget_bytes == 0 || slots <= 0 || slots > 256) return FEEC_BADARG;
+    if (method != FEEC_METHOD_RAINBOW && method != FEEC_METHOD_CG) return FEEC_BADARG;
+    if (mode != FEEC_MODE_MIXED && mode != FEEC_MODE_FP64) return FEEC_BADARG;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return FEEC_NO_DEVICE;
+    cudaStream_t lib = nullptr;
+    int st = init_device(dev, lib);
+    if (st != FEEC_OK) return st;
+    feec_server* srv = new (std::nothrow) feec_server();
+    if (!srv) return FEEC_OOM;
+    srv->method = method;
+    srv->mode = mode;
+    srv->budget = hbm_budget_bytes;
+    srv->device = dev;
+    srv->t0 = clock_type::now();
+    for (int i = 0; i < slots; i++) srv->workers.emplace_back(worker_loop, srv);
+    *out = srv;
+    return FEEC_OK;
+}
+
+int feec_server_submit(feec_server* srv, int N, const int* A, const int* C, const double* V, const double* b,
+                       double* x, double precision, long long* id) {
+    if (!srv || N <= 0 || !A || !C || !V || !b || !x || !(precision > 0.0)) return FEEC_BADARG;
+    Request rq;
+    rq.n = N; rq.A = A; rq.C = C; rq.V = V; rq.b = b; rq.x = x; rq.precision = precision;
+    rq.bytes = estimate_bytes(N, A[N]);
+    rq.t_submit = clock_type::now();
+    if (rq.bytes > srv->budget) return FEEC_OOM;
+    {
+        std::lock_guard<std::mutex> lk(srv->mu);
+        if (srv->stop) return FEEC_BADARG;
+        rq.id = srv->next_id++;
+        srv->queue.push_back(rq);
+        srv->submitted++;
+    }
+    srv->cv.notify_all();
+    if (id) *id = rq.id;
+    return FEEC_OK;
+}
+
+int feec_server_poll(feec_server* srv, feec_request_result* out, int max_out, int* nout) {
+    if (!srv || !nout || (max_out > 0 && !out)) return FEEC_BADARG;
+    std::lock_guard<std::mutex> lk(srv->mu);
+    const int k = std::min<int>(max_out, (int)srv->done.size());
+    for (int i = 0; i < k; i++) out[i] = srv->done[i];
+    srv->done.erase(srv->done.begin(), srv->done.begin() + k);
+    *nout = k;
+    return FEEC_OK;
+}
+
+int feec_server_wait(feec_server* srv, double timeout_s) {
+    if (!srv) return FEEC_BADARG;
+    std::unique_lock<std::mutex> lk(srv->mu);
+    const bool ok = srv->cv.wait_for(lk, std::chrono::duration<double>(timeout_s),
+                                     [&] { return srv->finished == srv->submitted; });
+    return ok ? FEEC_OK : FEEC_TIMEOUT;
+}
+
+int feec_server_stats(feec_server* srv, size_t* bytes_in_use, size_t* peak_bytes, int* inflight, long long* queued) {
+    if (!srv) return FEEC_BADARG;
+    std::lock_guard<std::mutex> lk(srv->mu);
+    if (bytes_in_use) *bytes_in_use = srv->in_use.load();
+    if (peak_bytes) *peak_bytes = srv->peak.load();
+    if (inflight) *inflight = srv->inflight.load();
+    if (queued) *queued = (long long)srv->queue.size();
+    return FEEC_OK;
+}
+
+int feec_server_destroy(feec_server* srv) {
+    if (!srv) return FEEC_OK;
+    {
+        std::lock_guard<std::mutex> lk(srv->mu);
+        srv->stop = true;
+    }
+    srv->cv.notify_all();
+    for (auto& t : srv->workers) t.join();
+    delete srv;
+    return FEEC_OK;
+}
+
+}  // extern "C"

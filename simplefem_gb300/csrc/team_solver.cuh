@@ -1,0 +1,674 @@
+// Device solver shared by the batched engine (one block per work item) and the
+// cluster engine (one thread-block cluster per request, used by the serving loop):
+// FP64 defect correction around an FP32 (or FP64) inner PCG with the reference's
+// multicolor SSOR sweeps or no preconditioner, over a SELL-32 layout. The code is
+// written once against a Team policy (BlockTeam / ClusterTeam).
+#pragma once
+#include <cmath>
+#include <cstdio>
+
+#include <cooperative_groups.h>
+
+#include "feec_batched.h"
+#include "feec_device.cuh"
+
+namespace feec {
+namespace team_solver {
+namespace {
+
+// L2 eviction priorities: every team of a batch streams the same matrix, while each
+// team's vectors are private and touched once per phase. Matrix loads carry an
+// evict_last cache policy so the shared operator stays in L2; row-local vector
+// traffic uses streaming (evict-first) loads and stores.
+__device__ __forceinline__ unsigned long long l2_keep_policy() {
+    unsigned long long p;
+    asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+__device__ __forceinline__ int ld_keep(const int* a, unsigned long long pol) {
+    int v;
+    asm volatile("ld.global.nc.L2::cache_hint.b32 %0, [%1], %2;" : "=r"(v) : "l"(a), "l"(pol));
+    return v;
+}
+__device__ __forceinline__ float ld_keep(const float* a, unsigned long long pol) {
+    float v;
+    asm volatile("ld.global.nc.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(v) : "l"(a), "l"(pol));
+    return v;
+}
+__device__ __forceinline__ double ld_keep(const double* a, unsigned long long pol) {
+    double v;
+    asm volatile("ld.global.nc.L2::cache_hint.f64 %0, [%1], %2;" : "=d"(v) : "l"(a), "l"(pol));
+    return v;
+}
+
+template <typename T, int K> struct Vec;
+template <> struct Vec<float, 1> { using t = float; };
+template <> struct Vec<float, 2> { using t = float2; };
+template <> struct Vec<float, 4> { using t = float4; };
+template <> struct Vec<double, 1> { using t = double; };
+template <> struct Vec<double, 2> { using t = double2; };
+
+template <typename T, int K>
+__device__ __forceinline__ void load_k(const T* p, T (&v)[K]) {
+    if constexpr (K == 1) {
+        v[0] = p[0];
+    } else if constexpr (K == 2) {
+        const typename Vec<T, 2>::t u = *reinterpret_cast<const typename Vec<T, 2>::t*>(p);
+        v[0] = u.x; v[1] = u.y;
+    } else if constexpr (K == 4 && sizeof(T) == 4) {
+        const float4 u = *reinterpret_cast<const float4*>(p);
+        v[0] = u.x; v[1] = u.y; v[2] = u.z; v[3] = u.w;
+    } else {
+        #pragma unroll
+        for (int j = 0; j < K; j += 2) {
+            const double2 u = *reinterpret_cast<const double2*>(p + j);
+            v[j] = u.x; v[j + 1] = u.y;
+        }
+    }
+}
+
+// Accumulate sum_k val[k] * X[col[k]] over one column-major block of a slice.
+// Memory-level parallelism: a chunk of CH column indices and values is loaded
+// first (all independent, coalesced across the warp), then the CH gathers are
+// issued together, then the FMAs run; padded slots are predicated off.
+template <typename T, int K>
+struct Chunk { static constexpr int value = (K >= 4) ? 4 : 8; };
+
+template <typename T, typename TV, int K>
+__device__ __forceinline__ void block_dot(const int* __restrict__ sci, const TV* __restrict__ sval, long long off,
+                                          int len, int lane, const T* X, T (&s)[K]) {
+    constexpr int CH = Chunk<T, K>::value;
+    const unsigned long long pol = l2_keep_policy();
+    for (int k0 = 0; k0 < len; k0 += CH) {
+        int c[CH]; T v[CH];
+        #pragma unroll
+        for (int u = 0; u < CH; u++) {
+            const bool ok = k0 + u < len;
+            const long long p = off + (long long)(k0 + u) * 32 + lane;
+            c[u] = ok ? ld_keep(&sci[p], pol) : -1;
+            v[u] = ok ? (T)ld_keep(&sval[p], pol) : T(0);
+        }
+        T xv[CH][K];
+        #pragma unroll
+        for (int u = 0; u < CH; u++) {
+            if (c[u] >= 0) {
+                load_k<T, K>(X + (long long)c[u] * K, xv[u]);
+            } else {
+                #pragma unroll
+                for (int j = 0; j < K; j++) xv[u][j] = T(0);
+            }
+        }
+        #pragma unroll
+        for (int u = 0; u < CH; u++)
+            #pragma unroll
+            for (int j = 0; j < K; j++) s[j] = fma(v[u], xv[u][j], s[j]);
+    }
+}
+
+// Team-wide (block) deterministic sum of NV accumulators, result broadcast to all threads.
+template <typename T, int NV>
+__device__ __forceinline__ void team_sum(typename AccT<T>::type (&v)[NV], double (&out)[NV]) {
+    __shared__ double s_out[NV];
+    block_reduce<T, NV>(v);
+    if (threadIdx.x == 0)
+        #pragma unroll
+        for (int k = 0; k < NV; k++) s_out[k] = AccT<T>::value(v[k]);
+    __syncthreads();
+    #pragma unroll
+    for (int k = 0; k < NV; k++) out[k] = s_out[k];
+    __syncthreads();
+}
+
+template <typename T>
+__device__ __forceinline__ const T* sel_val(const SellView& S);
+template <> __device__ __forceinline__ const float* sel_val<float>(const SellView& S) { return S.val32; }
+template <> __device__ __forceinline__ const double* sel_val<double>(const SellView& S) { return S.val64; }
+template <typename T>
+__device__ __forceinline__ const T* sel_wd(const SellView& S);
+template <> __device__ __forceinline__ const float* sel_wd<float>(const SellView& S) { return S.wd32; }
+template <> __device__ __forceinline__ const double* sel_wd<double>(const SellView& S) { return S.wd64; }
+template <typename T>
+__device__ __forceinline__ const T* sel_sd(const SellView& S);
+template <> __device__ __forceinline__ const float* sel_sd<float>(const SellView& S) { return S.sd32; }
+template <> __device__ __forceinline__ const double* sel_sd<double>(const SellView& S) { return S.sd64; }
+
+// ---------------------------------------------------------------------------
+// Team policies. A team is the set of threads that solves one work item together.
+//   BlockTeam   — one thread block; phase barrier = __syncthreads.
+//   ClusterTeam — a thread-block cluster (co-scheduled by the hardware on one GPC);
+//                 phase barrier = cluster barrier (release/acquire at cluster scope),
+//                 team sums read every block's partial through distributed shared
+//                 memory in a fixed order, so every block obtains the same bits.
+// Neither waits on anything outside its own co-scheduled threads.
+// ---------------------------------------------------------------------------
+struct BlockTeam {
+    __device__ __forceinline__ int rank() const { return 0; }
+    __device__ __forceinline__ int size() const { return 1; }
+    __device__ __forceinline__ int tid() const { return threadIdx.x; }
+    __device__ __forceinline__ int nthreads() const { return blockDim.x; }
+    __device__ __forceinline__ void sync() { __syncthreads(); }
+    template <typename T, int NV>
+    __device__ __forceinline__ void sum(typename AccT<T>::type (&v)[NV], double (&out)[NV]) { team_sum<T, NV>(v, out); }
+};
+
+struct ClusterTeam {
+    int r, sz, buf;
+    __device__ ClusterTeam() : buf(0) {
+        cooperative_groups::cluster_group cl = cooperative_groups::this_cluster();
+        r = (int)cl.block_rank();
+        sz = (int)cl.num_blocks();
+    }
+    __device__ __forceinline__ int rank() const { return r; }
+    __device__ __forceinline__ int size() const { return sz; }
+    __device__ __forceinline__ int tid() const { return r * blockDim.x + threadIdx.x; }
+    __device__ __forceinline__ int nthreads() const { return sz * blockDim.x; }
+    __device__ __forceinline__ void sync() { cooperative_groups::this_cluster().sync(); }
+    template <typename T, int NV>
+    __device__ __forceinline__ void sum(typename AccT<T>::type (&v)[NV], double (&out)[NV]) {
+        __shared__ double s_part[2][NV];
+        __shared__ double s_res[NV];
+        block_reduce<T, NV>(v);
+        if (threadIdx.x == 0)
+            #pragma unroll
+            for (int k = 0; k < NV; k++) s_part[buf][k] = AccT<T>::value(v[k]);
+        cooperative_groups::cluster_group cl = cooperative_groups::this_cluster();
+        cl.sync();
+        if (threadIdx.x == 0) {
+            double acc[NV];
+            #pragma unroll
+            for (int k = 0; k < NV; k++) acc[k] = 0.0;
+            for (int q = 0; q < sz; q++) {
+                const double* rp = cl.map_shared_rank(&s_part[buf][0], q);
+                #pragma unroll
+                for (int k = 0; k < NV; k++) acc[k] += rp[k];
+            }
+            #pragma unroll
+            for (int k = 0; k < NV; k++) s_res[k] = acc[k];
+        }
+        __syncthreads();
+        #pragma unroll
+        for (int k = 0; k < NV; k++) out[k] = s_res[k];
+        __syncthreads();
+        buf ^= 1;   // the next sum writes the other slot; this one is reused two sums later
+    }
+};
+
+struct SliceMeta {
+    int row0, nrow;
+    int4 len;
+    long long off;
+};
+
+__device__ __forceinline__ SliceMeta load_meta(const SellView& S, int sl) {
+    SliceMeta m;
+    m.row0 = __ldg(&S.slice_row0[sl]);
+    m.nrow = __ldg(&S.slice_nrow[sl]);
+    m.len = __ldg(&S.slice_len[sl]);
+    m.off = __ldg(&S.slice_off[sl]);
+    return m;
+}
+
+// Warp-strided loop over slices [s0, s1): the metadata of a warp's next slice is
+// loaded while the current one is processed, so a slice costs two dependent
+// memory round trips (its entries, then the gathers) instead of three.
+template <typename Team, typename F>
+__device__ __forceinline__ void for_slices(const Team& team, const SellView& S, int s0, int s1, F&& body) {
+    const int warp = team.rank() * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const int nwarps = team.size() * (blockDim.x >> 5);
+    int sl = s0 + warp;
+    SliceMeta cur{};
+    if (sl < s1) cur = load_meta(S, sl);
+    for (; sl < s1; sl += nwarps) {
+        SliceMeta nxt{};
+        if (sl + nwarps < s1) nxt = load_meta(S, sl + nwarps);
+        body(cur);
+        cur = nxt;
+    }
+}
+
+template <typename T, int K>
+__device__ __forceinline__ void load_k_stream(const T* p, T (&v)[K]) {
+    if constexpr (K == 1) {
+        v[0] = __ldcs(p);
+    } else if constexpr (K == 2) {
+        const typename Vec<T, 2>::t u = __ldcs(reinterpret_cast<const typename Vec<T, 2>::t*>(p));
+        v[0] = u.x; v[1] = u.y;
+    } else if constexpr (K == 4 && sizeof(T) == 4) {
+        const float4 u = __ldcs(reinterpret_cast<const float4*>(p));
+        v[0] = u.x; v[1] = u.y; v[2] = u.z; v[3] = u.w;
+    } else {
+        #pragma unroll
+        for (int j = 0; j < K; j += 2) {
+            const double2 u = __ldcs(reinterpret_cast<const double2*>(p + j));
+            v[j] = u.x; v[j + 1] = u.y;
+        }
+    }
+}
+
+template <typename T, int K>
+__device__ __forceinline__ void load_row(const T* v, int row, bool act, T (&out)[K]) {
+    if (act) {
+        load_k_stream<T, K>(v + (long long)row * K, out);
+    } else {
+        #pragma unroll
+        for (int j = 0; j < K; j++) out[j] = T(0);
+    }
+}
+
+template <typename T, int K>
+__device__ __forceinline__ void store_row(T* v, int row, const T (&in)[K]) {
+    T* p = v + (long long)row * K;
+    if constexpr (K == 1) {
+        __stcs(p, in[0]);
+    } else if constexpr (K == 2) {
+        typename Vec<T, 2>::t u; u.x = in[0]; u.y = in[1];
+        __stcs(reinterpret_cast<typename Vec<T, 2>::t*>(p), u);
+    } else if constexpr (K == 4 && sizeof(T) == 4) {
+        __stcs(reinterpret_cast<float4*>(p), make_float4(in[0], in[1], in[2], in[3]));
+    } else {
+        #pragma unroll
+        for (int j = 0; j < K; j += 2) __stcs(reinterpret_cast<double2*>(p + j), make_double2(in[j], in[j + 1]));
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Slice streaming: each warp walks its slices of a phase; the metadata of its next
+// slice is loaded while the current one is processed, the slice's own-row values
+// (pre) are requested before its gathers, and the row epilogue (post) runs on all
+// 32 lanes at once. Measured on GB300: staging the column/value stream through
+// shared memory with cp.async was slower than these direct loads — the multicolor
+// gathers, not the matrix stream, bound the sweeps.
+// ---------------------------------------------------------------------------
+inline int team_dynamic_smem(int) { return 0; }
+
+enum { kBlockFull = 0, kBlockL = 1, kBlockU = 2 };
+
+template <int WHICH>
+__device__ __forceinline__ void block_range(const SliceMeta& M, long long& off, int& len) {
+    if (WHICH == kBlockFull) { off = M.off; len = M.len.x + M.len.y + M.len.z; }
+    else if (WHICH == kBlockL) { off = M.off; len = M.len.x; }
+    else { off = M.off + 32ll * (M.len.x + M.len.y); len = M.len.z; }
+}
+
+// Per-row state carried from the prologue (own-row loads) to the epilogue of a slice.
+template <typename U, int K>
+struct RowState {
+    int row;
+    bool act;
+    U w, sdv;
+    U a[K], b[K], c[K], e[K];
+};
+
+template <typename U, typename TV, int K, int WHICH, typename Team, typename Pre, typename Post>
+__device__ __forceinline__ void for_slices_dot(const Team& team, const SellView& S, int s0, int s1, const TV* val,
+                                               const U* X, Pre&& pre, Post&& post) {
+    const int lane = threadIdx.x & 31;
+    for_slices(team, S, s0, s1, [&](const SliceMeta& M) {
+        auto state = pre(M);
+        long long off; int len;
+        block_range<WHICH>(M, off, len);
+        U sum[K];
+        #pragma unroll
+        for (int j = 0; j < K; j++) sum[j] = U(0);
+        block_dot<U, TV, K>(S.ci, val, off, len, lane, X, sum);
+        post(M, state, sum);
+    });
+}
+
+// One team solves work item `it` completely.
+template <typename T, int K, bool RAINBOW, typename Team>
+__device__ void team_solve(Team& team, const BatchArgs& args, const BatchItem& it) {
+    using AT = AccT<T>;
+    using Acc = typename AT::type;
+    const SellView S = args.systems[it.system];
+    const int n = S.n;
+    const int lane = threadIdx.x & 31;
+    const int kk = it.nrhs;                       // active columns (<= K)
+    const T* val = sel_val<T>(S);
+    const T* wd = sel_wd<T>(S);
+    const T* sd = sel_sd<T>(S);
+    double* xp = it.xp; double* bp = it.bp; double* r64 = it.r64;
+    T* r = (T*)it.r; T* d = (T*)it.d; T* z = (T*)it.z; T* m = (T*)it.m; T* q = (T*)it.q; T* c = (T*)it.c;
+    __shared__ double s_scal[4][K];
+    __shared__ int s_flag;
+
+    // gather caller vectors into the permuted, interleaved layout; ||b||^2
+    for (int i = team.tid(); i < n; i += team.nthreads()) {
+        const int o = __ldg(&S.perm[i]);
+        #pragma unroll
+        for (int j = 0; j < K; j++) {
+            bp[(long long)i * K + j] = j < kk ? it.b[j][o] : 0.0;
+            xp[(long long)i * K + j] = j < kk ? it.x[j][o] : 0.0;
+        }
+    }
+    double bnorm2[K];
+    {
+        double a2[K];
+        #pragma unroll
+        for (int j = 0; j < K; j++) a2[j] = 0.0;
+        team.sync();
+        for (int i = team.tid(); i < n; i += team.nthreads())
+            #pragma unroll
+            for (int j = 0; j < K; j++) { const double v = bp[(long long)i * K + j]; a2[j] += v * v; }
+        team.template sum<double, K>(a2, bnorm2);
+    }
+
+    int done[K], iters[K], outer_cnt[K], status[K];
+    double relres[K];
+    #pragma unroll
+    for (int j = 0; j < K; j++) { done[j] = j >= kk; iters[j] = 0; outer_cnt[j] = 0; status[j] = FEEC_MAXITER; relres[j] = -1.0; }
+
+    for (int outer = 0; outer < args.max_outer; outer++) {
+        // ---- FP64 true residual r64 = b - A x and its norm ----
+        team.sync();
+        double rn2[K];
+        {
+            double a2[K];
+            #pragma unroll
+            for (int j = 0; j < K; j++) a2[j] = 0.0;
+            for_slices_dot<double, double, K, kBlockFull>(team, S, 0, S.nslices, S.val64, xp,
+                [&](const SliceMeta& M) {
+                    RowState<double, K> p;
+                    p.row = M.row0 + lane; p.act = lane < M.nrow;
+                    load_row<double, K>(bp, p.row, p.act, p.a);
+                    return p;
+                },
+                [&](const SliceMeta&, const RowState<double, K>& p, const double (&sum)[K]) {
+                    if (p.act) {
+                        double rv[K];
+                        #pragma unroll
+                        for (int j = 0; j < K; j++) { rv[j] = p.a[j] - sum[j]; a2[j] += rv[j] * rv[j]; }
+                        store_row<double, K>(r64, p.row, rv);
+                    }
+                });
+            team.template sum<double, K>(a2, rn2);
+        }
+        // stop tests per column (thread 0 decides, broadcast)
+        if (threadIdx.x == 0) {
+            int all = 1;
+            for (int j = 0; j < K; j++) {
+                if (j < kk) {
+                    const double bn = sqrt(bnorm2[j]);
+                    const double rn = sqrt(rn2[j]);
+                    if (!done[j]) {
+                        if (!(rn == rn)) { done[j] = 1; status[j] = FEEC_BREAKDOWN; }
+                        else if (rn <= args.precision * bn) { done[j] = 1; status[j] = FEEC_OK; }
+                        else if (iters[j] >= args.max_iter) { done[j] = 1; status[j] = FEEC_MAXITER; }
+                    }
+                    relres[j] = bn > 0.0 ? rn / bn : 0.0;
+                    // inner target: the reduction still needed (with margin), never below eta
+                    const double need = args.inner_margin * args.precision * bn / (rn > 0.0 ? rn : 1.0);
+                    s_scal[0][j] = done[j] ? 0.0 : (rn > 0.0 ? 1.0 / rn : 0.0);
+                    s_scal[1][j] = done[j] ? 0.0 : rn;
+                    const double eta = need > args.inner_eta ? need : args.inner_eta;
+                    s_scal[2][j] = eta * eta;
+                } else {
+                    s_scal[0][j] = 0.0; s_scal[1][j] = 0.0; s_scal[2][j] = 0.0;
+                }
+                all = all && done[j];
+            }
+            s_flag = all;
+        }
+        __syncthreads();
+        // thread 0 decided; every other thread reads the decision (s_scal[1] == 0 <=> done)
+        if (threadIdx.x != 0) {
+            #pragma unroll
+            for (int j = 0; j < K; j++) done[j] = s_scal[1][j] == 0.0;
+        }
+        if (s_flag) break;
+        T inv[K];
+        double rnorm[K], eta2d[K];
+        #pragma unroll
+        for (int j = 0; j < K; j++) { inv[j] = (T)s_scal[0][j]; rnorm[j] = s_scal[1][j]; eta2d[j] = s_scal[2][j]; }
+        __syncthreads();
+
+        // ---- inner solve: A c = r64 / ||r64|| in T; restart with c = 0, r = rin ----
+        Acc arr[K], azr[K];
+        #pragma unroll
+        for (int j = 0; j < K; j++) { arr[j] = AT::zero(); azr[j] = AT::zero(); }
+        for (int i = team.tid(); i < n; i += team.nthreads()) {
+            #pragma unroll
+            for (int j = 0; j < K; j++) {
+                const long long p = (long long)i * K + j;
+                const T rv = (T)(r64[p] * (double)inv[j]);
+                r[p] = rv; c[p] = T(0); m[p] = T(0); z[p] = T(0); q[p] = T(0);
+                if constexpr (!RAINBOW) { d[p] = rv; azr[j] = AT::add(azr[j], rv * rv); } else { d[p] = T(0); }
+                arr[j] = AT::add(arr[j], rv * rv);
+            }
+        }
+        team.sync();
+        if constexpr (RAINBOW) {
+            for (int col = 0; col < S.ncolors; col++) {              // forward sweep
+                for_slices_dot<T, T, K, kBlockL>(team, S, __ldg(&S.color_slice[col]), __ldg(&S.color_slice[col + 1]), val, m,
+                    [&](const SliceMeta& M) {
+                        RowState<T, K> p;
+                        p.row = M.row0 + lane; p.act = lane < M.nrow;
+                        p.w = p.act ? __ldg(&wd[p.row]) : T(0);
+                        load_row<T, K>(r, p.row, p.act, p.a);
+                        return p;
+                    },
+                    [&](const SliceMeta&, const RowState<T, K>& p, const T (&sum)[K]) {
+                        if (p.act && p.w != T(0)) {
+                            T mv[K];
+                            #pragma unroll
+                            for (int j = 0; j < K; j++) mv[j] = (p.a[j] - sum[j]) * p.w;
+                            store_row<T, K>(m, p.row, mv);
+                        }
+                    });
+                team.sync();
+            }
+            for (int col = S.ncolors - 1; col >= 0; col--) {         // scale + backward sweep
+                for_slices_dot<T, T, K, kBlockU>(team, S, __ldg(&S.color_slice[col]), __ldg(&S.color_slice[col + 1]), val, z,
+                    [&](const SliceMeta& M) {
+                        RowState<T, K> p;
+                        p.row = M.row0 + lane; p.act = lane < M.nrow;
+                        p.w = p.act ? __ldg(&wd[p.row]) : T(0);
+                        p.sdv = p.act ? __ldg(&sd[p.row]) : T(0);
+                        load_row<T, K>(m, p.row, p.act, p.a);
+                        load_row<T, K>(r, p.row, p.act, p.b);
+                        return p;
+                    },
+                    [&](const SliceMeta&, const RowState<T, K>& p, const T (&sum)[K]) {
+                        if (p.act && p.w != T(0)) {
+                            T mv[K], zv[K];
+                            #pragma unroll
+                            for (int j = 0; j < K; j++) {
+                                mv[j] = p.a[j] * p.sdv;
+                                zv[j] = (mv[j] - sum[j]) * p.w;
+                                azr[j] = AT::add(azr[j], zv[j] * p.b[j]);
+                            }
+                            store_row<T, K>(m, p.row, mv);
+                            store_row<T, K>(z, p.row, zv);
+                            store_row<T, K>(d, p.row, zv);
+                        }
+                    });
+                team.sync();
+            }
+        }
+        double zr[K], rr[K];
+        {
+            Acc both[2 * K];
+            #pragma unroll
+            for (int j = 0; j < K; j++) { both[j] = azr[j]; both[K + j] = arr[j]; }
+            double o[2 * K];
+            team.template sum<T, 2 * K>(both, o);
+            #pragma unroll
+            for (int j = 0; j < K; j++) { zr[j] = o[j]; rr[j] = o[K + j]; }
+        }
+        int active[K];
+        #pragma unroll
+        for (int j = 0; j < K; j++) active[j] = !done[j];
+        while (true) {
+            // per-column stop on the recursive residual of the inner system
+            int any = 0;
+            #pragma unroll
+            for (int j = 0; j < K; j++) {
+                if (active[j] && (rr[j] < eta2d[j] || iters[j] >= args.max_iter)) active[j] = 0;
+                any |= active[j];
+            }
+            if (!any) break;
+            // q = A d (full rows), d.q
+            Acc adq[K];
+            #pragma unroll
+            for (int j = 0; j < K; j++) adq[j] = AT::zero();
+            for_slices_dot<T, T, K, kBlockFull>(team, S, 0, S.nslices, val, d,
+                [&](const SliceMeta& M) {
+                    RowState<T, K> p;
+                    p.row = M.row0 + lane; p.act = lane < M.nrow;
+                    p.w = (RAINBOW && p.act) ? __ldg(&wd[p.row]) : T(1);
+                    load_row<T, K>(d, p.row, p.act, p.a);
+                    return p;
+                },
+                [&](const SliceMeta&, const RowState<T, K>& p, const T (&sum)[K]) {
+                    if (p.act) {
+                        const bool skip = RAINBOW && p.w == T(0);
+                        T qv[K];
+                        #pragma unroll
+                        for (int j = 0; j < K; j++) {
+                            qv[j] = skip ? T(0) : sum[j];
+                            adq[j] = AT::add(adq[j], p.a[j] * qv[j]);
+                        }
+                        store_row<T, K>(q, p.row, qv);
+                    }
+                });
+            double dq[K];
+            team.template sum<T, K>(adq, dq);
+            T alpha[K];
+            #pragma unroll
+            for (int j = 0; j < K; j++) {
+                alpha[j] = T(0);
+                if (active[j]) {
+                    if (!(dq[j] > 0.0) || !(zr[j] >= 0.0) || !isfinite(dq[j]) || !isfinite(zr[j])) active[j] = 0;
+                    else alpha[j] = (T)(zr[j] / dq[j]);
+                }
+            }
+            #pragma unroll
+            for (int j = 0; j < K; j++) { arr[j] = AT::zero(); azr[j] = AT::zero(); }
+            if constexpr (RAINBOW) {
+                for (int col = 0; col < S.ncolors; col++) {
+                    for_slices_dot<T, T, K, kBlockL>(team, S, __ldg(&S.color_slice[col]), __ldg(&S.color_slice[col + 1]), val, m,
+                        [&](const SliceMeta& M) {
+                            RowState<T, K> p;
+                            p.row = M.row0 + lane; p.act = lane < M.nrow;
+                            p.w = p.act ? __ldg(&wd[p.row]) : T(0);
+                            load_row<T, K>(r, p.row, p.act, p.a);
+                            load_row<T, K>(q, p.row, p.act, p.b);
+                            load_row<T, K>(d, p.row, p.act, p.c);
+                            load_row<T, K>(c, p.row, p.act, p.e);
+                            return p;
+                        },
+                        [&](const SliceMeta&, const RowState<T, K>& p, const T (&sum)[K]) {
+                            if (p.act && p.w != T(0)) {
+                                T mv[K], rv[K], cv[K];
+                                #pragma unroll
+                                for (int j = 0; j < K; j++) {
+                                    cv[j] = p.e[j] + alpha[j] * p.c[j];
+                                    rv[j] = p.a[j] - alpha[j] * p.b[j];
+                                    arr[j] = AT::add(arr[j], rv[j] * rv[j]);
+                                    mv[j] = (rv[j] - sum[j]) * p.w;
+                                }
+                                store_row<T, K>(c, p.row, cv);
+                                store_row<T, K>(r, p.row, rv);
+                                store_row<T, K>(m, p.row, mv);
+                            }
+                        });
+                    team.sync();
+                }
+                for (int col = S.ncolors - 1; col >= 0; col--) {
+                    for_slices_dot<T, T, K, kBlockU>(team, S, __ldg(&S.color_slice[col]), __ldg(&S.color_slice[col + 1]), val, z,
+                        [&](const SliceMeta& M) {
+                            RowState<T, K> p;
+                            p.row = M.row0 + lane; p.act = lane < M.nrow;
+                            p.w = p.act ? __ldg(&wd[p.row]) : T(0);
+                            p.sdv = p.act ? __ldg(&sd[p.row]) : T(0);
+                            load_row<T, K>(m, p.row, p.act, p.a);
+                            load_row<T, K>(r, p.row, p.act, p.b);
+                            return p;
+                        },
+                        [&](const SliceMeta&, const RowState<T, K>& p, const T (&sum)[K]) {
+                            if (p.act && p.w != T(0)) {
+                                T mv[K], zv[K];
+                                #pragma unroll
+                                for (int j = 0; j < K; j++) {
+                                    mv[j] = p.a[j] * p.sdv;
+                                    zv[j] = (mv[j] - sum[j]) * p.w;
+                                    azr[j] = AT::add(azr[j], zv[j] * p.b[j]);
+                                }
+                                store_row<T, K>(m, p.row, mv);
+                                store_row<T, K>(z, p.row, zv);
+                            }
+                        });
+                    team.sync();
+                }
+            } else {
+                for (int i = team.tid(); i < n; i += team.nthreads())
+                    #pragma unroll
+                    for (int j = 0; j < K; j++) {
+                        const long long p = (long long)i * K + j;
+                        c[p] += alpha[j] * d[p];
+                        const T rv = r[p] - alpha[j] * q[p];
+                        r[p] = rv;
+                        arr[j] = AT::add(arr[j], rv * rv);
+                        azr[j] = AT::add(azr[j], rv * rv);
+                    }
+            }
+            double zr_new[K];
+            {
+                Acc both[2 * K];
+                #pragma unroll
+                for (int j = 0; j < K; j++) { both[j] = azr[j]; both[K + j] = arr[j]; }
+                double o[2 * K];
+                team.template sum<T, 2 * K>(both, o);
+                #pragma unroll
+                for (int j = 0; j < K; j++) { zr_new[j] = o[j]; rr[j] = active[j] ? o[K + j] : rr[j]; }
+            }
+            T beta[K];
+            #pragma unroll
+            for (int j = 0; j < K; j++) {
+                beta[j] = active[j] ? (T)(zr_new[j] / zr[j]) : T(0);
+                if (active[j]) { zr[j] = zr_new[j]; iters[j]++; }
+            }
+            // d = z + beta d for the active columns (CG: z = r)
+            for (int i = team.tid(); i < n; i += team.nthreads()) {
+                if (RAINBOW && __ldg(&wd[i]) == T(0)) continue;
+                #pragma unroll
+                for (int j = 0; j < K; j++) {
+                    if (!active[j]) continue;
+                    const long long p = (long long)i * K + j;
+                    d[p] = (RAINBOW ? z[p] : r[p]) + beta[j] * d[p];
+                }
+            }
+            team.sync();
+        }
+        // x += ||r|| c in FP64
+        for (int i = team.tid(); i < n; i += team.nthreads())
+            #pragma unroll
+            for (int j = 0; j < K; j++) {
+                const long long p = (long long)i * K + j;
+                if (!done[j]) xp[p] += rnorm[j] * (double)c[p];
+            }
+        #pragma unroll
+        for (int j = 0; j < K; j++) if (!done[j]) outer_cnt[j]++;
+    }
+    // scatter x back to the caller's numbering and report
+    team.sync();
+    for (int i = team.tid(); i < n; i += team.nthreads()) {
+        const int o = __ldg(&S.perm[i]);
+        #pragma unroll
+        for (int j = 0; j < K; j++)
+            if (j < kk) it.x[j][o] = xp[(long long)i * K + j];
+    }
+    if (team.rank() == 0 && threadIdx.x == 0) {
+        for (int j = 0; j < kk; j++) {
+            const int slot = it.first_result + j;
+            args.results[slot].status = done[j] ? status[j] : FEEC_MAXITER;
+            args.results[slot].iterations = iters[j];
+            args.results[slot].outer = outer_cnt[j];
+            args.results[slot].relres = relres[j];
+        }
+    }
+}
+
+}  // namespace
+}  // namespace team_solver
+}  // namespace feec
