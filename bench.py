@@ -202,6 +202,82 @@ def run_spmv(dev, reps=20):
     return out
 
 
+def run_batched_uneven(dev, count=512, reps=3):
+    """512 independent uneven systems (2D P1/P2, refinements 3-7, coefficient mass) in one
+    graph-captured batched launch, mixed precision and FP64, each column to 1e-10."""
+    import torch
+    import simplefem_gb300 as S
+    from simplefem_gb300 import workloads
+    from simplefem_gb300.system import Batch, System
+    specs = workloads.batched_uneven_systems(count, 4242)
+    systems = []
+    for sp in specs:
+        A, C, V = workloads.lattice_matrix(**sp)
+        n = len(A) - 1
+        mat = S.MatrixCSR(n, n, A, C, V)
+        rb = S.Rainbow(mat)
+        sysm = System(A, C, V)
+        sysm.set_rainbow(mat.getDiagonal().raw(), 1.0, rb.num_colors, rb.F, rb.B, rb.R)
+        systems.append(sysm)
+    out = {"systems": count, "n_min": min(s.n for s in systems), "n_max": max(s.n for s in systems),
+           "unknowns_total": sum(s.n for s in systems)}
+    for mode, method in (("mixed", "rainbow"), ("fp64", "rainbow"), ("fp64", "cg")):
+        bs = [torch.empty(s.n, dtype=torch.float64, device=dev) for s in systems]
+        xs = [torch.zeros(s.n, dtype=torch.float64, device=dev) for s in systems]
+        batch = Batch(systems, bs, xs, method=method, mode=mode, precision=PRECISION)
+        times = []
+        for rep in range(reps + 1):
+            for i, sysm in enumerate(systems):
+                bs[i].copy_(torch.from_numpy(workloads.uniform_vector(77 * rep + i, sysm.n)))
+                xs[i].zero_()
+            torch.cuda.synchronize()
+            infos, ms = batch.run()
+            assert all(i["status"] == 0 and i["true_relres"] <= PRECISION for i in infos), f"{mode}/{method} failed"
+            if rep > 0:
+                times.append(ms)
+        batch.close()
+        t = float(np.median(times))
+        out[f"{mode}_{method}"] = {"ms_per_batch": t, "solves_per_s": count / (t / 1000.0),
+                                   "iterations_median": int(np.median([i["iterations"] for i in infos]))}
+    for s in systems:
+        s.close()
+    return out
+
+
+def run_serving(mode, method, count=200, rate=200.0, slots=24, budget=120 * 10**9):
+    """Poisson-arrival request stream through the continuous-batching server."""
+    from simplefem_gb300 import workloads
+    from simplefem_gb300.serving import Server
+    reqs = workloads.serving_requests(count, 2026, rate_per_s=rate)
+    pool = {}
+    for rq in reqs:
+        key = (rq["dim"], rq["r"], rq["L"], rq["coef_seed"])
+        if key not in pool:
+            pool[key] = workloads.lattice_matrix(*key)
+    rhs = [workloads.uniform_vector(rq["rhs_seed"], rq["n"]) for rq in reqs]
+    srv = Server(hbm_budget_bytes=budget, slots=slots, method=method, mode=mode)
+    t0 = time.perf_counter()
+    for rq, b in zip(reqs, rhs):
+        dt = rq["t"] - (time.perf_counter() - t0)
+        if dt > 0:
+            time.sleep(dt)
+        A, C, V = pool[(rq["dim"], rq["r"], rq["L"], rq["coef_seed"])]
+        srv.submit(A, C, V, b, rq["tol"])
+    ok = srv.wait(1800)
+    makespan = time.perf_counter() - t0
+    res = srv.poll(4096)
+    stats = srv.stats()
+    srv.close()
+    lat = np.array([r["latency_ms"] for r in res])
+    bad = [r for r in res if r["status"] != 0 or r["true_relres"] > [q for q in reqs][r["id"] - 1]["tol"]]
+    return {"mode": mode, "method": method, "requests": count, "arrival_rate_per_s": rate, "slots": slots,
+            "hbm_budget_gb": budget / 1e9, "completed": len(res), "failed": len(bad), "all_done": bool(ok),
+            "solves_per_s": len(res) / makespan, "makespan_s": makespan,
+            "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+            "peak_bytes": stats["peak_bytes"],
+            "unknowns_range": [min(r["n"] for r in reqs), max(r["n"] for r in reqs)]}
+
+
 def run_ours(args):
     import torch
     import torch.distributed as dist
@@ -220,6 +296,17 @@ def run_ours(args):
     if args.only_spmv:
         if rank == 0:
             print(json.dumps({"spmv": run_spmv(dev)}), flush=True)
+        return
+    if args.only_uneven:
+        if rank == 0:
+            print(json.dumps({"batched_uneven": run_batched_uneven(dev)}), flush=True)
+        return
+    if args.only_serving:
+        if rank == 0:
+            print(json.dumps({"serving": [run_serving("mixed", "rainbow", args.requests),
+                                          run_serving("fp64", "cg", args.requests),
+                                          run_serving("mixed", "rainbow", 100, rate=5.0),
+                                          run_serving("fp64", "cg", 100, rate=5.0)]}), flush=True)
         return
     A, C, V = workloads.lattice_matrix(**WORKLOAD)
     n = len(A) - 1
@@ -350,6 +437,13 @@ def run_ours(args):
         dropin.append(time.perf_counter() - t0)
 
     spmv = run_spmv(dev)
+    uneven = run_batched_uneven(dev) if not args.skip_extras else None
+    serving = None
+    if not args.skip_extras:
+        serving = {"mixed_rainbow": run_serving("mixed", "rainbow", args.requests),
+                   "fp64_cg": run_serving("fp64", "cg", args.requests),
+                   "mixed_rainbow_at_5_per_s": run_serving("mixed", "rainbow", 100, rate=5.0),
+                   "fp64_cg_at_5_per_s": run_serving("fp64", "cg", 100, rate=5.0)}
 
     # CPU baseline: the oracle restatement of the reference Rainbow-PCG on the host cores, one solve
     cpu = None
@@ -394,6 +488,8 @@ def run_ours(args):
                                             "iterations": int(np.median([i["iterations"] for i in rb64_i]))},
             "dropin_host_call_ms": 1000 * float(np.median(dropin)),
             "spmv": spmv,
+            "batched_uneven": uneven,
+            "serving": serving,
             "roofline": roofline,
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": 8 * n * B_RHS,
@@ -416,6 +512,10 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--batch", type=int, default=1216, help="right-hand sides per batched step")
     ap.add_argument("--only-spmv", action="store_true", help="only the resident SpMV measurement")
+    ap.add_argument("--only-uneven", action="store_true", help="only the 512 uneven systems batch")
+    ap.add_argument("--only-serving", action="store_true", help="only the serving stream")
+    ap.add_argument("--requests", type=int, default=200, help="requests in the serving stream")
+    ap.add_argument("--skip-extras", action="store_true", help="skip the uneven-batch and serving legs")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

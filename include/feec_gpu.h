@@ -164,6 +164,18 @@ int feec_solve_many(int nsys, feec_system* const* systems, int method, int mode,
                     double* const* x, const double* const* b, double precision, int max_iter,
                     feec_solve_info* infos, void* stream);
 
+/* A reusable batch over many systems (one right-hand side each, device pointers
+ * x[i], b[i] that stay valid for the batch's lifetime; x holds the initial guess
+ * on every run). Everything is set up once and the launch sequence is captured in
+ * a CUDA graph; feec_batch_run replays it and fills infos[i] (host, nsys entries,
+ * may be NULL) and *device_ms. team_threads 0 = 256. */
+typedef struct feec_batch feec_batch;
+int feec_batch_create(feec_batch** batch, int nsys, feec_system* const* systems, int method, int mode,
+                      double* const* x, const double* const* b, double precision, int max_iter,
+                      int team_threads, void* stream);
+int feec_batch_run(feec_batch* batch, feec_solve_info* infos, double* device_ms);
+int feec_batch_destroy(feec_batch* batch);
+
 /* y = scaling * A * x with device pointers (MatrixCSR::apply on a resident matrix),
  * over a cached SELL-32 copy of the matrix, one thread per row. */
 int feec_system_apply(feec_system* sys, const double* x, double* y, double scaling, void* stream);

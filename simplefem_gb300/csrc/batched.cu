@@ -30,6 +30,7 @@ int sell_prepare(feec_system* s, int method) {
     SellData& D = s->sell[rb ? 1 : 0];
     if (D.ready) return FEEC_OK;
     if (rb && s->prepared != FEEC_METHOD_RAINBOW) return FEEC_BADARG;
+    HomeStreamScope home(s);
     D.mem.release();
     D.mem.stream = s->stream;
     cudaStream_t st = s->stream;
@@ -340,6 +341,172 @@ int feec_solve_many(int nsys, feec_system* const* systems, int method, int mode,
         jb.system = i; jb.nrhs = 1; jb.first = i; jb.b[0] = b[i]; jb.x[0] = x[i];
     }
     return run_batch(st, sys, jobs, method, mode, 1, precision, max_iter > 0 ? max_iter : maxn, nsys, infos, 0, 256);
+}
+
+// ---------------------------------------------------------------------------
+// Reusable batch: the systems, their right-hand-side / solution buffers, the work
+// table and all workspace are set up once; the launch sequence (queue reset,
+// result reset, batched kernel) is captured in a CUDA graph and replayed by
+// feec_batch_run, so a repeated batch costs one graph launch.
+// ---------------------------------------------------------------------------
+struct feec_batch {
+    cudaStream_t stream = nullptr;        // own stream: the graph is captured on and replayed on it
+    cudaStream_t user_stream = nullptr;   // the caller's stream (may be the legacy default stream)
+    cudaEvent_t ev_in = nullptr;
+    bool own_stream = false;
+    DevArena mem;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    BatchResult* dres = nullptr;
+    int nresults = 0;
+    double precision = 0.0;
+    int teams = 0;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+};
+
+int feec_batch_create(feec_batch** out, int nsys, feec_system* const* systems, int method, int mode, double* const* x,
+                      const double* const* b, double precision, int max_iter, int team_threads, void* stream) {
+    if (!out || nsys <= 0 || !systems || !x || !b || !(precision > 0.0)) return FEEC_BADARG;
+    if (method != FEEC_METHOD_CG && method != FEEC_METHOD_RAINBOW) return FEEC_BADARG;
+    if (mode != FEEC_MODE_MIXED && mode != FEEC_MODE_FP64) return FEEC_BADARG;
+    *out = nullptr;
+    feec_batch* bt = new (std::nothrow) feec_batch();
+    if (!bt) return FEEC_OOM;
+    struct Cleanup {
+        feec_batch*& p;
+        bool keep = false;
+        ~Cleanup() {
+            if (!keep && p) {
+                p->mem.release();
+                cudaStreamSynchronize(p->stream);
+                if (p->own_stream) cudaStreamDestroy(p->stream);
+                if (p->ev_in) cudaEventDestroy(p->ev_in);
+                delete p;
+                p = nullptr;
+            }
+        }
+    } cleanup{bt};
+    // The legacy default stream cannot be captured: the batch owns a non-blocking
+    // stream and orders it after the caller's stream with an event on every run.
+    bt->user_stream = (cudaStream_t)stream;
+    FEEC_TRY(cudaStreamSynchronize(bt->user_stream));
+    FEEC_TRY(cudaStreamCreateWithFlags(&bt->stream, cudaStreamNonBlocking));
+    bt->own_stream = true;
+    FEEC_TRY(cudaEventCreateWithFlags(&bt->ev_in, cudaEventDisableTiming));
+    bt->mem.stream = bt->stream;
+    bt->precision = precision;
+    int maxn = 0;
+    std::vector<feec_system*> sys(systems, systems + nsys);
+    for (int i = 0; i < nsys; i++) {
+        if (!sys[i] || !x[i] || !b[i]) return FEEC_BADARG;
+        cudaStream_t keep = sys[i]->stream;
+        sys[i]->stream = bt->stream;
+        const int e = sell_prepare(sys[i], method);
+        sys[i]->stream = keep;
+        if (e != FEEC_OK) return e;
+        maxn = std::max(maxn, sys[i]->n);
+    }
+    const int is_float = mode == FEEC_MODE_MIXED;
+    const size_t tsz = is_float ? sizeof(float) : sizeof(double);
+    // largest systems first
+    std::vector<int> order((size_t)nsys);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int a, int c) { return sys[a]->n > sys[c]->n; });
+    std::vector<SellView> views;
+    for (auto* sp : sys) views.push_back(sell_view(sp, method));
+    SellView* dviews = nullptr;
+    BatchItem* ditems = nullptr;
+    int* dnext = nullptr;
+    DevArena& M = bt->mem;
+    FEEC_TRY(M.alloc(dviews, views.size()));
+    FEEC_TRY(M.alloc(ditems, (size_t)nsys));
+    FEEC_TRY(M.alloc(bt->dres, (size_t)nsys));
+    FEEC_TRY(M.alloc(dnext, 1));
+    std::vector<BatchItem> items((size_t)nsys);
+    for (int k = 0; k < nsys; k++) {
+        const int i = order[k];
+        const size_t len = (size_t)sys[i]->n;
+        BatchItem& it = items[k];
+        std::memset(&it, 0, sizeof(it));
+        it.system = i; it.nrhs = 1; it.first_result = i;
+        it.b[0] = b[i]; it.x[0] = x[i];
+        FEEC_TRY(M.alloc(it.xp, len)); FEEC_TRY(M.alloc(it.bp, len)); FEEC_TRY(M.alloc(it.r64, len));
+        char* w = nullptr;
+        FEEC_TRY(M.alloc(w, 6 * len * tsz));
+        it.r = w; it.d = w + len * tsz; it.z = w + 2 * len * tsz; it.m = w + 3 * len * tsz; it.q = w + 4 * len * tsz;
+        it.c = w + 5 * len * tsz;
+    }
+    FEEC_TRY(cudaMemcpyAsync(dviews, views.data(), sizeof(SellView) * views.size(), cudaMemcpyHostToDevice, bt->stream));
+    FEEC_TRY(cudaMemcpyAsync(ditems, items.data(), sizeof(BatchItem) * items.size(), cudaMemcpyHostToDevice, bt->stream));
+    FEEC_TRY(cudaStreamSynchronize(bt->stream));
+    BatchArgs a{};
+    a.systems = dviews; a.items = ditems; a.nitems = nsys; a.next_item = dnext; a.results = bt->dres;
+    a.precision = precision;
+    a.inner_eta = is_float ? 2e-5 : 1e-30;
+    a.inner_margin = is_float ? 0.3 : 1.0;
+    a.max_iter = max_iter > 0 ? max_iter : maxn;
+    a.max_outer = is_float ? 12 : 4;
+    const int threads = team_threads > 0 ? team_threads : 256;
+    bt->teams = std::min(nsys, batched_resident_teams(is_float, 1, method == FEEC_METHOD_RAINBOW, threads));
+    // capture the launch sequence once (batched_resident_teams above already set the
+    // kernel's attributes, so nothing but stream work happens while capturing)
+    FEEC_TRY(cudaStreamBeginCapture(bt->stream, cudaStreamCaptureModeRelaxed));
+    cudaMemsetAsync(dnext, 0, sizeof(int), bt->stream);
+    cudaMemsetAsync(bt->dres, 0, sizeof(BatchResult) * nsys, bt->stream);
+    const cudaError_t le = launch_batched(a, is_float, 1, method == FEEC_METHOD_RAINBOW, threads, bt->teams, bt->stream);
+    const cudaError_t ce = cudaStreamEndCapture(bt->stream, &bt->graph);
+    if (le != cudaSuccess) return cuda_status(le);
+    if (ce != cudaSuccess) return cuda_status(ce);
+    FEEC_TRY(cudaGraphInstantiate(&bt->exec, bt->graph, 0));
+    FEEC_TRY(cudaEventCreate(&bt->e0));
+    FEEC_TRY(cudaEventCreate(&bt->e1));
+    bt->nresults = nsys;
+    cleanup.keep = true;
+    *out = bt;
+    return FEEC_OK;
+}
+
+int feec_batch_run(feec_batch* bt, feec_solve_info* infos, double* device_ms) {
+    if (!bt) return FEEC_BADARG;
+    FEEC_TRY(cudaEventRecord(bt->ev_in, bt->user_stream));     // inputs written on the caller's stream
+    FEEC_TRY(cudaStreamWaitEvent(bt->stream, bt->ev_in, 0));
+    FEEC_TRY(cudaEventRecord(bt->e0, bt->stream));
+    FEEC_TRY(cudaGraphLaunch(bt->exec, bt->stream));
+    note_launch();
+    FEEC_TRY(cudaEventRecord(bt->e1, bt->stream));
+    std::vector<BatchResult> res((size_t)bt->nresults);
+    FEEC_TRY(cudaMemcpyAsync(res.data(), bt->dres, sizeof(BatchResult) * bt->nresults, cudaMemcpyDeviceToHost, bt->stream));
+    FEEC_TRY(cudaStreamSynchronize(bt->stream));
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, bt->e0, bt->e1);
+    if (device_ms) *device_ms = ms;
+    int worst = FEEC_OK;
+    for (int i = 0; i < bt->nresults; i++) {
+        if (res[i].status != FEEC_OK && worst == FEEC_OK) worst = res[i].status;
+        if (infos) {
+            feec_solve_info& f = infos[i];
+            std::memset(&f, 0, sizeof(f));
+            f.status = res[i].status; f.iterations = res[i].iterations; f.outer_iterations = res[i].outer;
+            f.true_relres = res[i].relres; f.tolerance = bt->precision; f.final_norm = res[i].relres;
+            f.device_ms = ms; f.grid_blocks = bt->teams; f.lanes_per_row = 1;
+        }
+    }
+    return worst;
+}
+
+int feec_batch_destroy(feec_batch* bt) {
+    if (!bt) return FEEC_OK;
+    cudaStreamSynchronize(bt->stream);
+    if (bt->exec) cudaGraphExecDestroy(bt->exec);
+    if (bt->graph) cudaGraphDestroy(bt->graph);
+    if (bt->e0) cudaEventDestroy(bt->e0);
+    if (bt->e1) cudaEventDestroy(bt->e1);
+    bt->mem.release();
+    cudaStreamSynchronize(bt->stream);
+    if (bt->ev_in) cudaEventDestroy(bt->ev_in);
+    if (bt->own_stream) cudaStreamDestroy(bt->stream);
+    delete bt;
+    return FEEC_OK;
 }
 
 }  // extern "C"

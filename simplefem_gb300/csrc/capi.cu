@@ -87,6 +87,7 @@ namespace {
 
 int ensure_work(feec_system* s) {
     if (s->work_ready) return FEEC_OK;
+    HomeStreamScope home(s);
     s->work.stream = s->stream;
     const size_t n = (size_t)s->n;
     FEEC_TRY(s->work.alloc(s->x, n)); FEEC_TRY(s->work.alloc(s->r, n)); FEEC_TRY(s->work.alloc(s->d, n));
@@ -457,6 +458,7 @@ int feec_system_create(feec_system** out, int N, const int* A, const int* C, con
     // work the caller issues there (e.g. a framework's default stream)
     (void)lib_stream;
     s->stream = (cudaStream_t)stream;
+    s->home_stream = s->stream;
     s->mem.stream = s->stream;
     s->work.stream = s->stream;
     int nnz = 0;
@@ -611,11 +613,11 @@ int feec_system_solve(feec_system* s, int method, int mode, double* x, const dou
     if (method < FEEC_METHOD_CG || method > FEEC_METHOD_RAINBOW || mode < FEEC_MODE_REFERENCE || mode > FEEC_MODE_MIXED)
         return FEEC_BADARG;
     cudaStream_t keep = s->stream;
-    if (stream) { s->stream = (cudaStream_t)stream; s->work.stream = s->stream; }
+    if (stream) s->stream = (cudaStream_t)stream;
     const auto t0 = std::chrono::steady_clock::now();
     int st = solve_core(s, method, mode, x, b, residual, precision, max_iter, 0.0, -3, info);
     if (info) info->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
-    s->stream = keep; s->work.stream = keep;
+    s->stream = keep;
     return st;
 }
 

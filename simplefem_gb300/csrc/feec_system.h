@@ -50,6 +50,11 @@ struct DevArena {
 
 int init_device(int& dev, cudaStream_t& stream);
 
+// While alive, routes a system's work to its creation ("home") stream, after the
+// stream of the current call has drained; used for one-time set-up whose
+// allocations outlive the call (their frees are ordered on the home stream).
+struct HomeStreamScope;
+
 // A SELL-32 copy of a system's matrix (see SellView).
 struct SellData {
     DevArena mem;
@@ -67,7 +72,8 @@ struct feec_system {
     int dev = 0;
     int n = 0;
     int nnz = 0;
-    cudaStream_t stream = nullptr;
+    cudaStream_t stream = nullptr;         // stream of the current call
+    cudaStream_t home_stream = nullptr;    // stream given at creation: owns every persistent allocation
     feec::DevArena mem;      // matrix + layouts
     feec::DevArena work;     // Krylov workspace
     int* A = nullptr; int* C = nullptr; double* V = nullptr;   // original CSR
@@ -103,3 +109,22 @@ struct feec_system {
     int tuned_threads[3][3] = {};
     double tuned_rate[3][3] = {};
 };
+
+namespace feec {
+struct HomeStreamScope {
+    feec_system* s;
+    cudaStream_t saved;
+    explicit HomeStreamScope(feec_system* sys) : s(sys), saved(sys->stream) {
+        if (saved != s->home_stream) {
+            cudaStreamSynchronize(saved);
+            s->stream = s->home_stream;
+        }
+    }
+    ~HomeStreamScope() {
+        if (saved != s->home_stream) {
+            cudaStreamSynchronize(s->home_stream);
+            s->stream = saved;
+        }
+    }
+};
+}  // namespace feec

@@ -1,5 +1,8 @@
 // Serving loop with continuous batching.
 //
+// Requests above `big_nnz` stored entries take the whole GPU through the persistent
+// cooperative solver, one at a time (the "big lane"); all others run as clusters.
+//
 // A feec_server owns `slots` worker threads. Requests (one SPD solve each: a CSR
 // matrix, a right-hand side, a tolerance) wait in a FIFO queue; a free slot takes
 // the next request as soon as the device memory budget has room for it, uploads
@@ -56,6 +59,8 @@ size_t estimate_bytes(int n, long long nnz) {
 
 struct feec_server {
     int method = FEEC_METHOD_RAINBOW;
+    long long big_nnz = 4000000;       // requests with more stored entries use the whole-GPU solver
+    std::mutex big_lane;               // ... one at a time
     int mode = FEEC_MODE_MIXED;
     size_t budget = 0;
     int device = 0;
@@ -99,9 +104,37 @@ int serve_one(feec_server* srv, const Request& rq, cudaStream_t stream, feec_req
         st = feec_system_set_rainbow(s, diag.data(), 1.0, nc, F.data(), B.data(), R.data(), 1);
         if (st != FEEC_OK) return st;
     }
+    const int is_float = srv->mode == FEEC_MODE_MIXED;
+    cudaEvent_t done_ev = nullptr;
+    FEEC_TRY(cudaEventCreateWithFlags(&done_ev, cudaEventBlockingSync | cudaEventDisableTiming));
+    struct EvGuard { cudaEvent_t e; ~EvGuard() { cudaEventDestroy(e); } } evguard{done_ev};
+    if ((long long)s->nnz >= srv->big_nnz) {
+        // Large request: the whole GPU for one solve (persistent cooperative kernel). One at a
+        // time, so two grid-wide solves never compete for co-residency.
+        DevArena io;
+        io.stream = stream;
+        struct IoGuard { DevArena* m; ~IoGuard() { m->release(); } } ioguard{&io};
+        double *b = nullptr, *x = nullptr;
+        FEEC_TRY(io.alloc(b, (size_t)rq.n)); FEEC_TRY(io.alloc(x, (size_t)rq.n));
+        FEEC_TRY(cudaMemcpyAsync(b, rq.b, sizeof(double) * rq.n, cudaMemcpyHostToDevice, stream));
+        FEEC_TRY(cudaMemsetAsync(x, 0, sizeof(double) * rq.n, stream));
+        feec_solve_info info;
+        std::lock_guard<std::mutex> lane(srv->big_lane);
+        res.t_start_ms = ms_since(srv, clock_type::now());
+        st = feec_system_solve(s, rainbow ? FEEC_METHOD_RAINBOW : FEEC_METHOD_CG, srv->mode, x, b, nullptr,
+                               rq.precision, 0, &info, stream);
+        FEEC_TRY(cudaMemcpyAsync(rq.x, x, sizeof(double) * rq.n, cudaMemcpyDeviceToHost, stream));
+        FEEC_TRY(cudaEventRecord(done_ev, stream));
+        FEEC_TRY(cudaEventSynchronize(done_ev));
+        res.status = info.status;
+        res.iterations = info.iterations;
+        res.outer_iterations = info.outer_iterations;
+        res.true_relres = info.true_relres;
+        res.cluster_blocks = -info.grid_blocks;   // negative: whole-GPU persistent grid
+        return st;
+    }
     st = sell_prepare(s, rainbow ? FEEC_METHOD_RAINBOW : FEEC_METHOD_CG);
     if (st != FEEC_OK) return st;
-    const int is_float = srv->mode == FEEC_MODE_MIXED;
     const size_t n = (size_t)rq.n;
     const size_t tsz = is_float ? sizeof(float) : sizeof(double);
     DevArena mem;
@@ -134,9 +167,9 @@ int serve_one(feec_server* srv, const Request& rq, cudaStream_t stream, feec_req
     a.inner_margin = is_float ? 0.3 : 1.0;
     a.max_iter = rq.n;
     a.max_outer = is_float ? 12 : 4;
-    // cluster size from the work per iteration: about 0.5 M stored entries per block
+    // cluster size from the work per iteration: about 0.25 M stored entries per block
     const long long nnz = view.nslices > 0 ? s->nnz : 0;
-    int blocks = (int)std::min<long long>(16, std::max<long long>(1, nnz / 500000));
+    int blocks = (int)std::min<long long>(16, std::max<long long>(1, nnz / 250000));
     const int maxb = cluster_max_blocks(is_float, rainbow);
     if (blocks > maxb) blocks = maxb;
     // powers of two only
@@ -148,7 +181,8 @@ int serve_one(feec_server* srv, const Request& rq, cudaStream_t stream, feec_req
     BatchResult hr{};
     FEEC_TRY(cudaMemcpyAsync(&hr, dres, sizeof(hr), cudaMemcpyDeviceToHost, stream));
     FEEC_TRY(cudaMemcpyAsync(rq.x, x, sizeof(double) * n, cudaMemcpyDeviceToHost, stream));
-    FEEC_TRY(cudaStreamSynchronize(stream));
+    FEEC_TRY(cudaEventRecord(done_ev, stream));
+    FEEC_TRY(cudaEventSynchronize(done_ev));    // blocking wait: slots do not spin on the host
     res.status = hr.status;
     res.iterations = hr.iterations;
     res.outer_iterations = hr.outer;

@@ -141,3 +141,44 @@ def solve_many(systems, bs, xs, method="rainbow", mode="mixed", precision=1e-10,
     if raise_on_error and st not in (_native.FEEC_OK, _native.FEEC_MAXITER, _native.FEEC_BREAKDOWN):
         raise _native.FeecError(st, "feec_solve_many")
     return [i.as_dict() for i in infos]
+
+
+class Batch:
+    """Many systems, one right-hand side each, solved by one graph-captured batched launch.
+
+    ``bs`` and ``xs`` are device tensors that stay bound to the batch: write new
+    right-hand sides into ``bs`` and initial guesses into ``xs`` before each ``run``."""
+
+    def __init__(self, systems, bs, xs, method="rainbow", mode="mixed", precision=1e-10, max_iter=0,
+                 team_threads=0):
+        self._lib = _native.gpu()
+        n = len(systems)
+        self.systems, self.bs, self.xs = systems, bs, xs
+        hs = (ctypes.c_void_p * n)(*[s._h for s in systems])
+        xp = (ctypes.c_void_p * n)(*[x.data_ptr() for x in xs])
+        bp = (ctypes.c_void_p * n)(*[b.data_ptr() for b in bs])
+        h = ctypes.c_void_p()
+        st = self._lib.feec_batch_create(ctypes.byref(h), n, hs, METHODS[method], MODES[mode], xp, bp,
+                                         float(precision), int(max_iter), int(team_threads), _stream())
+        _native.check(st, "feec_batch_create")
+        self._h = h
+        self.n = n
+
+    def run(self, raise_on_error=True) -> tuple:
+        infos = (_native.FeecSolveInfo * self.n)()
+        ms = ctypes.c_double(0.0)
+        st = self._lib.feec_batch_run(self._h, infos, ctypes.byref(ms))
+        if raise_on_error and st not in (_native.FEEC_OK, _native.FEEC_MAXITER, _native.FEEC_BREAKDOWN):
+            raise _native.FeecError(st, "feec_batch_run")
+        return [i.as_dict() for i in infos], ms.value
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.feec_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -56,3 +56,43 @@ CONFIGS = {
     "cfg3_3d_p1_l7": dict(dim=3, r=1, L=7),     # mixed-precision target, N = 2,146,689
     "cfg4_2d_p2_l7": dict(dim=2, r=2, L=7),     # largest batched system, N = 66,049
 }
+
+
+def lattice_choices(n_min=1000, n_max=2_000_000, dims=(2, 3), degrees=(1, 2, 3)):
+    """All (dim, r, L) whose unknown count (r 2^L + 1)^d lies in [n_min, n_max]."""
+    out = []
+    for d in dims:
+        for r in degrees:
+            for L in range(0, 13):
+                n = (r * 2 ** L + 1) ** d
+                if n > n_max:
+                    break
+                if n >= n_min:
+                    out.append((n, d, r, L))
+    return sorted(out)
+
+
+def serving_requests(count, seed, rate_per_s=200.0, n_min=1000, n_max=2_000_000, tolerances=(1e-8, 1e-10, 1e-12)):
+    """A seeded Poisson-arrival request stream: 2D or 3D (50/50), P1-P3, the refinement whose
+    unknown count is nearest (in log) to a log-uniform draw in [n_min, n_max], a per-request
+    coefficient seed, and a tolerance drawn from `tolerances`."""
+    rng = np.random.default_rng(seed)
+    t = 0.0
+    reqs = []
+    choices = {d: [c for c in lattice_choices(n_min, n_max, dims=(d,))] for d in (2, 3)}
+    for i in range(count):
+        t += rng.exponential(1.0 / rate_per_s)
+        d = 2 if rng.random() < 0.5 else 3
+        target = np.exp(rng.uniform(np.log(n_min), np.log(n_max)))
+        cands = choices[d]
+        n, dd, r, L = min(cands, key=lambda c: abs(np.log(c[0]) - np.log(target)))
+        reqs.append(dict(t=t, dim=dd, r=r, L=L, n=n, coef_seed=1 + int(rng.integers(0, 2)),
+                         rhs_seed=int(rng.integers(1, 2**62)), tol=float(rng.choice(tolerances))))
+    return reqs
+
+
+def batched_uneven_systems(count, seed):
+    """The uneven batch: 2D P1 or P2 (50/50), refinement uniform in 3..7, a per-system
+    coefficient seed (log-uniform [0.1, 10] cell coefficients on the mass term)."""
+    rng = np.random.default_rng(seed)
+    return [dict(dim=2, r=int(rng.integers(1, 3)), L=int(rng.integers(3, 8)), coef_seed=1 + i) for i in range(count)]
