@@ -41,6 +41,58 @@ __device__ __forceinline__ T seg_dot(const int* __restrict__ ci, const T* __rest
     return s;
 }
 
+// Pipelined row loops of the preconditioned solver. A group (LANES lanes) walks its
+// row slots of a phase; the bounds of its next row are loaded while the current row
+// is processed, and the first row of the next phase is loaded before the grid
+// barrier that separates the phases (the matrix structure is read-only, so only
+// the gathered vector values have to wait for the barrier).
+struct RowRef {
+    int i, a, e;   // row (-1: no row for this group), segment [a, e) of ci / val
+};
+
+enum { kRowsL = 0, kRowsBackwardU = 1, kRowsFull = 2 };
+
+template <int KIND, typename T>
+__device__ __forceinline__ RowRef row_ref(const PcgArgs<T>& a, int k, int hi) {
+    RowRef r{-1, 0, 0};
+    if (k < hi) {
+        if (KIND == kRowsBackwardU) {
+            r.i = __ldg(&a.brows[k]);
+            r.a = __ldg(&a.usplit[r.i]);
+            r.e = __ldg(&a.rp[r.i + 1]);
+        } else {
+            r.i = k;
+            r.a = __ldg(&a.rp[k]);
+            r.e = (KIND == kRowsL) ? __ldg(&a.lsplit[k]) : __ldg(&a.rp[k + 1]);
+        }
+    }
+    return r;
+}
+
+template <int LANES>
+__device__ __forceinline__ int group_base(int lo) {
+    return lo + (int)((blockIdx.x * blockDim.x + threadIdx.x) / 32) * (32 / LANES);
+}
+template <int LANES>
+__device__ __forceinline__ int group_first(int lo) {
+    return group_base<LANES>(lo) + (int)((threadIdx.x & 31) / LANES);
+}
+template <int LANES>
+__device__ __forceinline__ int group_stride() {
+    return (int)(gridDim.x * blockDim.x / 32) * (32 / LANES);
+}
+
+template <int LANES, int KIND, typename T, typename F>
+__device__ __forceinline__ void rows_pipelined(const PcgArgs<T>& a, int lo, int hi, RowRef cur, F&& body) {
+    const int stride = group_stride<LANES>();
+    int k = group_first<LANES>(lo);
+    for (int base = group_base<LANES>(lo); base < hi; base += stride, k += stride) {
+        const RowRef nxt = row_ref<KIND>(a, k + stride, hi);
+        body(cur);
+        cur = nxt;
+    }
+}
+
 template <typename T>
 __device__ __forceinline__ void write_partials(double* dst, typename AccT<T>::type v0) {
     typename AccT<T>::type v[1] = {v0};
@@ -242,6 +294,7 @@ __global__ void __launch_bounds__(kThreads) pcg_persistent(PcgArgs<T> a) {
     int K = 0;
     int status = FEEC_MAXITER;
     double d_Ad = 0.0;
+    RowRef pf = row_ref<kRowsFull>(a, group_first<LANES>(0), n);
     while (K < a.max_iter) {
         if (threadIdx.x == 0) {
             if (a.print_modulo > 0 && K % a.print_modulo == 0 && blockIdx.x == 0)
@@ -255,16 +308,18 @@ __global__ void __launch_bounds__(kThreads) pcg_persistent(PcgArgs<T> a) {
         if (s_ctl) { status = FEEC_OK; break; }
 
         Acc adq = AT::zero();                                                          // :1197-1212
-        FEEC_FOR_ROW_GROUPS(0, n, i, act) {
-            const int lo = act ? __ldg(&a.rp[i]) : 0, hi = act ? __ldg(&a.rp[i + 1]) : 0;
-            const T s = seg_dot<T, LANES>(a.ci, a.val, a.d, lo, hi, lane);
+        rows_pipelined<LANES, kRowsFull>(a, 0, n, pf, [&](const RowRef& R) {
+            const bool act = R.i >= 0;
+            const T s = seg_dot<T, LANES>(a.ci, a.val, a.d, R.a, R.e, lane);
             if (act && lane == 0) {
-                const T qi = (__ldg(&a.wd[i]) != T(0)) ? s : T(0);
-                a.q[i] = qi;
-                adq = AT::add(adq, a.d[i] * qi);
+                const T qi = (__ldg(&a.wd[R.i]) != T(0)) ? s : T(0);
+                a.q[R.i] = qi;
+                adq = AT::add(adq, a.d[R.i] * qi);
             }
-        }
+        });
         write_partials<T>(p_dq, adq);
+        int flo = __ldg(&a.fptr[0]), fhi = __ldg(&a.fptr[1]);
+        pf = row_ref<kRowsL>(a, group_first<LANES>(flo), fhi);
         if (!grid_barrier(a.st, epoch, 14)) return;
         double dq[1];
         grid_sum<1>(p_dq, dq);
@@ -283,45 +338,52 @@ __global__ void __launch_bounds__(kThreads) pcg_persistent(PcgArgs<T> a) {
         const T alpha = (T)s_scal[0];
         arr = AT::zero();
         for (int p = 0; p < a.nf; p++) {                                               // :1230-1261
-            const int lo_r = __ldg(&a.fptr[p]), hi_r = __ldg(&a.fptr[p + 1]);
-            FEEC_FOR_ROW_GROUPS(lo_r, hi_r, i, act) {
-                const int lo = act ? __ldg(&a.rp[i]) : 0, hi = act ? __ldg(&a.lsplit[i]) : 0;
-                const T s = seg_dot<T, LANES>(a.ci, a.val, a.m, lo, hi, lane);
+            rows_pipelined<LANES, kRowsL>(a, flo, fhi, pf, [&](const RowRef& R) {
+                const bool act = R.i >= 0;
+                const T s = seg_dot<T, LANES>(a.ci, a.val, a.m, R.a, R.e, lane);
                 if (act && lane == 0) {
-                    const T w = __ldg(&a.wd[i]);
+                    const T w = __ldg(&a.wd[R.i]);
                     if (w != T(0)) {
-                        a.x[i] += alpha * a.d[i];
-                        const T ri = a.r[i] - alpha * a.q[i];
-                        a.r[i] = ri;
+                        a.x[R.i] += alpha * a.d[R.i];
+                        const T ri = a.r[R.i] - alpha * a.q[R.i];
+                        a.r[R.i] = ri;
                         arr = AT::add(arr, ri * ri);
-                        a.m[i] = (ri - s) * w;
+                        a.m[R.i] = (ri - s) * w;
                     }
                 }
+            });
+            if (p + 1 < a.nf) {
+                flo = fhi;
+                fhi = __ldg(&a.fptr[p + 2]);
+                pf = row_ref<kRowsL>(a, group_first<LANES>(flo), fhi);
+            } else {
+                pf = row_ref<kRowsBackwardU>(a, group_first<LANES>(__ldg(&a.bptr[0])), __ldg(&a.bptr[1]));
             }
             if (!grid_barrier(a.st, epoch, 15)) return;
         }
         azr = AT::zero();
         for (int p = 0; p < a.nbw; p++) {                                              // :1263-1307
             const int lo_r = __ldg(&a.bptr[p]), hi_r = __ldg(&a.bptr[p + 1]);
-            FEEC_FOR_ROW_GROUPS(lo_r, hi_r, k, act) {
-                const int i = act ? __ldg(&a.brows[k]) : 0;
-                const int lo = act ? __ldg(&a.usplit[i]) : 0, hi = act ? __ldg(&a.rp[i + 1]) : 0;
-                const T s = seg_dot<T, LANES>(a.ci, a.val, a.z, lo, hi, lane);
+            rows_pipelined<LANES, kRowsBackwardU>(a, lo_r, hi_r, pf, [&](const RowRef& R) {
+                const bool act = R.i >= 0;
+                const T s = seg_dot<T, LANES>(a.ci, a.val, a.z, R.a, R.e, lane);
                 if (act && lane == 0) {
-                    const T w = __ldg(&a.wd[i]);
+                    const T w = __ldg(&a.wd[R.i]);
                     if (w != T(0)) {
-                        const T mi = a.m[i] * __ldg(&a.sd[i]);
-                        a.m[i] = mi;
+                        const T mi = a.m[R.i] * __ldg(&a.sd[R.i]);
+                        a.m[R.i] = mi;
                         const T zi = (mi - s) * w;
-                        a.z[i] = zi;
-                        azr = AT::add(azr, zi * a.r[i]);
+                        a.z[R.i] = zi;
+                        azr = AT::add(azr, zi * a.r[R.i]);
                     }
                 }
-            }
+            });
             if (p + 1 < a.nbw) {
+                pf = row_ref<kRowsBackwardU>(a, group_first<LANES>(hi_r), __ldg(&a.bptr[p + 2]));
                 if (!grid_barrier(a.st, epoch, 16)) return;
             }
         }
+        pf = row_ref<kRowsFull>(a, group_first<LANES>(0), n);
         write_partials2<T>(p_zr, azr, arr);
         if (!grid_barrier(a.st, epoch, 17)) return;
         grid_sum<2>(p_zr, zr2);
