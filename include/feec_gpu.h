@@ -64,6 +64,9 @@ typedef struct feec_solve_info {
     double total_ms;         /* wall time of the call including copies                     */
     int grid_blocks;         /* persistent grid size used                                  */
     int lanes_per_row;       /* CSR lanes per row used by the SpMV and sweeps              */
+    int fp64_fallback;       /* MIXED: 1 if FP32 inner solves stagnated (operator too       */
+                             /* ill-conditioned for FP32) and the solve finished in FP64    */
+    int reserved;
 } feec_solve_info;
 
 /* ---------------------------------------------------------------------------
@@ -132,7 +135,12 @@ int feec_system_set_rainbow(feec_system* sys, const double* diagonal, double ome
 int feec_system_set_ssor(feec_system* sys, const double* diagonal, double omega, int host_ptrs);
 
 /* Solves A x = b on the device. x (in/out, initial guess), b and residual are
- * device pointers of N doubles (residual may be NULL). max_iter <= 0 means N. */
+ * device pointers of N doubles (residual may be NULL). max_iter <= 0 means N.
+ * FEEC_MODE_MIXED (here and in the batched and serving entry points below): when an
+ * FP32 inner solve gains less than half the digits it was asked for (condition
+ * number times FP32 roundoff near 1e-2 or above), the solve continues in FP64 from
+ * its current iterate with a fresh budget of max_iter iterations, and
+ * info->fp64_fallback is 1. */
 int feec_system_solve(feec_system* sys, int method, int mode, double* x, const double* b,
                       double* residual, double precision, int max_iter,
                       feec_solve_info* info, void* stream);
@@ -225,7 +233,7 @@ typedef struct feec_request_result {
     int iterations;          /* inner iterations                                    */
     int outer_iterations;    /* FP64 defect-correction steps                        */
     int cluster_blocks;      /* thread blocks of the cluster that solved it         */
-    int pad;
+    int fp64_fallback;       /* 1 if mixed precision stagnated and FP64 finished it */
     double true_relres;      /* ||b - A x|| / ||b|| in FP64 at the end               */
     double t_submit_ms;      /* host steady-clock times since the server started    */
     double t_start_ms;       /* solve launched (after admission and set-up)         */

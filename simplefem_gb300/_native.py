@@ -29,6 +29,8 @@ class FeecSolveInfo(ctypes.Structure):
         ("total_ms", ctypes.c_double),
         ("grid_blocks", ctypes.c_int),
         ("lanes_per_row", ctypes.c_int),
+        ("fp64_fallback", ctypes.c_int),
+        ("reserved", ctypes.c_int),
     ]
 
     def as_dict(self):

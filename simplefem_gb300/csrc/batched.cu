@@ -117,9 +117,10 @@ struct Job {
     double* x[kBatchMaxK];
 };
 
-int run_batch(cudaStream_t st, const std::vector<feec_system*>& systems, std::vector<Job>& jobs, int method, int mode,
-              int K, double precision, int max_iter, int nresults, feec_solve_info* infos, int teams, int threads,
-              int max_outer = 0, float* elapsed_ms = nullptr, long long* iter_sum = nullptr) {
+// One launch of the batched kernel over `jobs`; the per-column results come back in `res`.
+int run_batch_results(cudaStream_t st, const std::vector<feec_system*>& systems, std::vector<Job>& jobs, int method,
+                      int mode, int K, double precision, int max_iter, int nresults, int teams, int threads,
+                      int max_outer, bool stall_check, std::vector<BatchResult>& res, float* elapsed_ms) {
     const int is_float = mode == FEEC_MODE_MIXED ? 1 : 0;
     const size_t tsz = is_float ? sizeof(float) : sizeof(double);
     // largest systems first, so the tail of the batch is short
@@ -162,13 +163,14 @@ int run_batch(cudaStream_t st, const std::vector<feec_system*>& systems, std::ve
     a.inner_margin = is_float ? 0.3 : 1.0;   // FP64 recursion tracks the true residual closely
     a.max_iter = max_iter;
     a.max_outer = max_outer > 0 ? max_outer : (is_float ? 12 : 4);
+    a.stall_check = (is_float && stall_check) ? 1 : 0;
     cudaEvent_t e0, e1;
     FEEC_TRY(cudaEventCreate(&e0));
     FEEC_TRY(cudaEventCreate(&e1));
     FEEC_TRY(cudaEventRecord(e0, st));
     FEEC_TRY(launch_batched(a, is_float, K, method == FEEC_METHOD_RAINBOW, threads, teams, st));
     FEEC_TRY(cudaEventRecord(e1, st));
-    std::vector<BatchResult> res((size_t)nresults);
+    res.assign((size_t)nresults, BatchResult{});
     FEEC_TRY(cudaMemcpyAsync(res.data(), dres, sizeof(BatchResult) * nresults, cudaMemcpyDeviceToHost, st));
     FEEC_TRY(cudaStreamSynchronize(st));
     float ms = 0.0f;
@@ -176,14 +178,51 @@ int run_batch(cudaStream_t st, const std::vector<feec_system*>& systems, std::ve
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     tmp.release();
+    FEEC_TRY(cudaStreamSynchronize(st));
     if (elapsed_ms) *elapsed_ms = ms;
-    if (iter_sum) {
-        long long t = 0;
-        for (int i = 0; i < nresults; i++) t += res[i].iterations;
-        *iter_sum = t;
+    return FEEC_OK;
+}
+
+// Columns that the stall check stopped (an operator too ill-conditioned for FP32 inner
+// solves) continue from their current iterate — already written back to the caller's
+// x — in the FP64 batched solver, one column per team, with a fresh budget of max_iter
+// iterations; their results are merged.
+int rescue_stagnated(cudaStream_t st, const std::vector<feec_system*>& systems, const std::vector<Job>& jobs,
+                     int method, double precision, int max_iter, std::vector<BatchResult>& res, float* extra_ms) {
+    std::vector<Job> again;
+    std::vector<int> slot;
+    for (const Job& jb : jobs)
+        for (int j = 0; j < jb.nrhs; j++) {
+            const int r = jb.first + j;
+            if (res[r].status != kStatusStagnated) continue;
+            Job nj{};
+            nj.system = jb.system; nj.nrhs = 1; nj.first = (int)again.size();
+            nj.b[0] = jb.b[j]; nj.x[0] = jb.x[j];
+            again.push_back(nj);
+            slot.push_back(r);
+        }
+    if (again.empty()) return FEEC_OK;
+    std::vector<BatchResult> r2;
+    float ms = 0.0f;
+    const int st2 = run_batch_results(st, systems, again, method, FEEC_MODE_FP64, 1, precision, max_iter,
+                                      (int)again.size(), 0, 256, 0, false, r2, &ms);
+    if (st2 != FEEC_OK) return st2;
+    for (size_t k = 0; k < slot.size(); k++) {
+        BatchResult& d = res[slot[k]];
+        d.status = r2[k].status;
+        d.iterations += r2[k].iterations;
+        d.outer += r2[k].outer;
+        d.relres = r2[k].relres;
+        d.fp64_fallback = 1;
     }
-    int worst = FEEC_OK;
-    for (int i = 0; i < nresults; i++) {
+    if (extra_ms) *extra_ms += ms;
+    return FEEC_OK;
+}
+
+void fill_infos(const std::vector<BatchResult>& res, double precision, float ms, int grid, feec_solve_info* infos,
+                int& worst) {
+    worst = FEEC_OK;
+    for (size_t i = 0; i < res.size(); i++) {
         if (res[i].status != FEEC_OK && worst == FEEC_OK) worst = res[i].status;
         if (infos) {
             feec_solve_info& f = infos[i];
@@ -196,10 +235,35 @@ int run_batch(cudaStream_t st, const std::vector<feec_system*>& systems, std::ve
             f.final_norm = res[i].relres;
             f.device_ms = ms;
             f.lanes_per_row = 1;
-            f.grid_blocks = teams > 0 ? teams : batched_resident_teams(is_float, K, method == FEEC_METHOD_RAINBOW, threads);
+            f.grid_blocks = grid;
+            f.fp64_fallback = res[i].fp64_fallback;
         }
     }
-    FEEC_TRY(cudaStreamSynchronize(st));
+}
+
+int run_batch(cudaStream_t st, const std::vector<feec_system*>& systems, std::vector<Job>& jobs, int method, int mode,
+              int K, double precision, int max_iter, int nresults, feec_solve_info* infos, int teams, int threads,
+              int max_outer = 0, float* elapsed_ms = nullptr, long long* iter_sum = nullptr) {
+    const int is_float = mode == FEEC_MODE_MIXED ? 1 : 0;
+    std::vector<BatchResult> res;
+    float ms = 0.0f;
+    const bool rescue = is_float && max_outer == 0;   // the autotuner's trials run a fixed iteration count
+    int st2 = run_batch_results(st, systems, jobs, method, mode, K, precision, max_iter, nresults, teams, threads,
+                                max_outer, rescue, res, &ms);
+    if (st2 != FEEC_OK) return st2;
+    if (rescue) {
+        st2 = rescue_stagnated(st, systems, jobs, method, precision, max_iter, res, &ms);
+        if (st2 != FEEC_OK) return st2;
+    }
+    if (elapsed_ms) *elapsed_ms = ms;
+    if (iter_sum) {
+        long long t = 0;
+        for (int i = 0; i < nresults; i++) t += res[i].iterations;
+        *iter_sum = t;
+    }
+    int worst = FEEC_OK;
+    fill_infos(res, precision, ms, teams > 0 ? teams : batched_resident_teams(is_float, K, method == FEEC_METHOD_RAINBOW, threads),
+               infos, worst);
     return worst;
 }
 
@@ -362,6 +426,10 @@ struct feec_batch {
     double precision = 0.0;
     int teams = 0;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
+    // for the FP64 finish of stagnated systems (mixed precision only)
+    int method = 0, mode = 0, max_iter = 0;
+    std::vector<feec_system*> systems;
+    std::vector<Job> jobs;
 };
 
 int feec_batch_create(feec_batch** out, int nsys, feec_system* const* systems, int method, int mode, double* const* x,
@@ -446,6 +514,14 @@ int feec_batch_create(feec_batch** out, int nsys, feec_system* const* systems, i
     a.inner_margin = is_float ? 0.3 : 1.0;
     a.max_iter = max_iter > 0 ? max_iter : maxn;
     a.max_outer = is_float ? 12 : 4;
+    a.stall_check = is_float;
+    bt->method = method; bt->mode = mode; bt->max_iter = a.max_iter;
+    bt->systems = sys;
+    for (int i = 0; i < nsys; i++) {
+        Job jb{};
+        jb.system = i; jb.nrhs = 1; jb.first = i; jb.b[0] = b[i]; jb.x[0] = x[i];
+        bt->jobs.push_back(jb);
+    }
     const int threads = team_threads > 0 ? team_threads : 256;
     bt->teams = std::min(nsys, batched_resident_teams(is_float, 1, method == FEEC_METHOD_RAINBOW, threads));
     // capture the launch sequence once (batched_resident_teams above already set the
@@ -479,18 +555,14 @@ int feec_batch_run(feec_batch* bt, feec_solve_info* infos, double* device_ms) {
     FEEC_TRY(cudaStreamSynchronize(bt->stream));
     float ms = 0.0f;
     cudaEventElapsedTime(&ms, bt->e0, bt->e1);
+    if (bt->mode == FEEC_MODE_MIXED) {
+        const int st = rescue_stagnated(bt->stream, bt->systems, bt->jobs, bt->method, bt->precision, bt->max_iter,
+                                        res, &ms);
+        if (st != FEEC_OK) return st;
+    }
     if (device_ms) *device_ms = ms;
     int worst = FEEC_OK;
-    for (int i = 0; i < bt->nresults; i++) {
-        if (res[i].status != FEEC_OK && worst == FEEC_OK) worst = res[i].status;
-        if (infos) {
-            feec_solve_info& f = infos[i];
-            std::memset(&f, 0, sizeof(f));
-            f.status = res[i].status; f.iterations = res[i].iterations; f.outer_iterations = res[i].outer;
-            f.true_relres = res[i].relres; f.tolerance = bt->precision; f.final_norm = res[i].relres;
-            f.device_ms = ms; f.grid_blocks = bt->teams; f.lanes_per_row = 1;
-        }
-    }
+    fill_infos(res, bt->precision, ms, bt->teams, infos, worst);
     return worst;
 }
 

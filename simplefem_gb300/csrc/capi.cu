@@ -207,10 +207,14 @@ int solve_core(feec_system* s, int method, int mode, double* xx, const double* b
     // Measured on GB300 (3D P2 operator, 28 entries per row): the FP64 persistent
     // solvers issue FP64 at 2 lanes/clk/SM, so per-row reductions across lanes and
     // per-group epilogues cost more than they save; one thread per row is fastest for
-    // plain FP64 CG and 4 lanes per row for the sweeps of the preconditioned solvers.
+    // plain FP64 CG and 4 lanes per row for the sweeps of the preconditioned solvers
+    // (8 for their FP32 inner solves).
     if (method == FEEC_METHOD_CG && mode != FEEC_MODE_MIXED) shape.lanes = 1;
-    else if (shape.lanes > 4) shape.lanes = 4;
-    if (shape.lanes == 1 || shape.lanes == 4) {
+    else {
+        const int cap = (mode == FEEC_MODE_MIXED && method != FEEC_METHOD_CG) ? 8 : 4;
+        if (shape.lanes > cap) shape.lanes = cap;
+    }
+    if (shape.lanes == 1 || shape.lanes == 4 || shape.lanes == 8) {
         // two co-resident blocks per SM were fastest in the same measurements
         int dev_sms = 0;
         cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, s->dev);
@@ -226,12 +230,15 @@ int solve_core(feec_system* s, int method, int mode, double* xx, const double* b
     float ms_total = 0.0f;
     int K_total = 0, outer = 0, status = FEEC_OK;
     double final_norm = 0.0;
+    int fell_back = 0;
     DeviceStatus hs{};
 
-    if (mode == FEEC_MODE_REFERENCE || mode == FEEC_MODE_FP64) {
-        // FP64 mode: run with the recursive-residual rule, then confirm on the true residual and
-        // restart from the current iterate if the recursion drifted (at most a few times).
-        const int max_restarts = (mode == FEEC_MODE_FP64) ? 4 : 1;
+    // FP64 solve from the current iterate s->x: run with the recursive-residual rule, then
+    // confirm on the true residual and restart from the current iterate if the recursion
+    // drifted (at most a few times). REFERENCE mode runs once with the reference's rule.
+    auto run_fp64 = [&](int run_mode) -> int {
+        const int max_restarts = (run_mode == FEEC_MODE_FP64) ? 4 : 1;
+        const int k0 = K_total;   // iterations before this FP64 run do not count against its budget
         for (int attempt = 0; attempt < max_restarts; attempt++) {
             FEEC_TRY(cudaMemsetAsync(s->d, 0, sizeof(double) * n, s->stream));
             FEEC_TRY(cudaMemsetAsync(s->z, 0, sizeof(double) * n, s->stream));
@@ -242,7 +249,7 @@ int solve_core(feec_system* s, int method, int mode, double* xx, const double* b
                 CgArgs<double> a{};
                 a.n = n; a.rp = s->A; a.ci = s->C; a.val = s->V; a.b = s->b; a.x = s->x; a.r = s->r; a.d = s->d; a.q = s->q;
                 a.tol2 = tolerance * tolerance;
-                a.max_iter = max_iter - K_total;
+                a.max_iter = max_iter - (K_total - k0);
                 a.print_modulo = print_modulo; a.print_tol = tolerance;
                 a.partials = s->partials; a.st = s->st;
                 FEEC_TRY(reset_status(s));
@@ -254,9 +261,9 @@ int solve_core(feec_system* s, int method, int mode, double* xx, const double* b
             } else {
                 PcgArgs<double> a = make_pcg_args<double>(s, s->x, s->r, s->d, s->z, s->m, s->q, s->b, s->val, s->wd, s->sd);
                 a.tol2 = tolerance * tolerance;
-                a.use_zr_rule = (mode == FEEC_MODE_REFERENCE) ? 1 : 0;
-                a.rr_stop = (mode == FEEC_MODE_FP64) ? tolerance * tolerance : 0.0;
-                a.max_iter = max_iter - K_total;
+                a.use_zr_rule = (run_mode == FEEC_MODE_REFERENCE) ? 1 : 0;
+                a.rr_stop = (run_mode == FEEC_MODE_FP64) ? tolerance * tolerance : 0.0;
+                a.max_iter = max_iter - (K_total - k0);
                 a.print_modulo = print_modulo; a.print_tol = tolerance;
                 st = timed_launch_pcg64(s, a, shape, ms);
                 if (st != FEEC_OK) return st;
@@ -268,13 +275,19 @@ int solve_core(feec_system* s, int method, int mode, double* xx, const double* b
             status = hs.status;
             final_norm = std::sqrt(std::fabs(hs.final_value));
             outer++;
-            if (mode == FEEC_MODE_REFERENCE || status != FEEC_OK) break;
+            if (run_mode == FEEC_MODE_REFERENCE || status != FEEC_OK) break;
             double rn2 = 0.0;
             st = true_residual(s, s->b, s->x, s->d, rn2, permuted);
             if (st != FEEC_OK) return st;
             if (std::sqrt(rn2) <= tolerance) break;
-            if (K_total >= max_iter) { status = FEEC_MAXITER; break; }
+            if (K_total - k0 >= max_iter) { status = FEEC_MAXITER; break; }
         }
+        return FEEC_OK;
+    };
+
+    if (mode == FEEC_MODE_REFERENCE || mode == FEEC_MODE_FP64) {
+        st = run_fp64(mode);
+        if (st != FEEC_OK) return st;
     } else {
         // MIXED: FP64 defect correction around an FP32 inner solve (compensated FP32 dots).
         if (method == FEEC_METHOD_CG && !s->V32) return FEEC_BADARG;
@@ -282,6 +295,8 @@ int solve_core(feec_system* s, int method, int mode, double* xx, const double* b
         const double inner_eta = 2e-5;   // relative reduction asked of one inner solve
         const int max_outer = 12;
         double rn2 = 0.0;
+        double stall_limit = 0.0;        // residual norm above which the last outer step stagnated
+        bool stagnated = false;
         for (outer = 0; outer < max_outer; outer++) {
             st = true_residual(s, s->b, s->x, s->r, rn2, permuted);
             if (st != FEEC_OK) return st;
@@ -289,6 +304,11 @@ int solve_core(feec_system* s, int method, int mode, double* xx, const double* b
             final_norm = rn;
             if (!(rn == rn)) { status = FEEC_BREAKDOWN; break; }
             if (rn <= tolerance) { status = FEEC_OK; break; }
+            // An inner solve that gained less than half the digits it was asked for means the
+            // operator is too ill-conditioned for FP32 arithmetic (condition number times the
+            // FP32 unit roundoff near 1e-2 or above): finish in FP64 from the current iterate,
+            // with a fresh budget of max_iter iterations.
+            if (outer > 0 && rn > stall_limit) { stagnated = true; break; }
             if (K_total >= max_iter) { status = FEEC_MAXITER; break; }
             const double inv = 1.0 / rn;
             const double scal_h[2] = {inv, rn};
@@ -303,6 +323,7 @@ int solve_core(feec_system* s, int method, int mode, double* xx, const double* b
             // do not over-solve the last step: ask only for the reduction still needed (with margin)
             const double need = 0.3 * tolerance / rn;
             const double eta = std::max(inner_eta, need);
+            stall_limit = rn * std::sqrt(eta);
             float ms = 0.0f;
             FEEC_TRY(reset_status(s));
             FEEC_TRY(cudaEventRecord(s->ev0, s->stream));
@@ -334,6 +355,11 @@ int solve_core(feec_system* s, int method, int mode, double* xx, const double* b
             if (hs.status == FEEC_BREAKDOWN && hs.iterations == 0) { status = FEEC_BREAKDOWN; break; }
         }
         if (outer == max_outer) status = FEEC_MAXITER;
+        if (stagnated) {
+            st = run_fp64(FEEC_MODE_FP64);
+            if (st != FEEC_OK) return st;
+            fell_back = 1;
+        }
         // leave the FP64 recursive residual array holding the true residual
         double rn2b = 0.0;
         st = true_residual(s, s->b, s->x, s->r, rn2b, permuted);
@@ -351,6 +377,7 @@ int solve_core(feec_system* s, int method, int mode, double* xx, const double* b
         info->iterations = K_total;
         info->outer_iterations = outer;
         info->num_colors = method == FEEC_METHOD_CG ? 0 : s->num_levels;
+        info->fp64_fallback = fell_back;
         info->tolerance = (mode == FEEC_MODE_REFERENCE) ? tolerance : precision;
         info->final_norm = final_norm;
         info->device_ms = ms_total;

@@ -37,7 +37,8 @@ struct BatchItem {
 };
 
 struct BatchResult {
-    int status, iterations, outer, pad;
+    int status, iterations, outer;
+    int fp64_fallback;        // set on the host when a stagnated column was finished in FP64
     double relres;
 };
 
@@ -52,7 +53,12 @@ struct BatchArgs {
     double inner_margin;      // the last inner solve aims at margin * (reduction still needed)
     int max_iter;             // inner iterations per column, summed over outer steps
     int max_outer;
+    int stall_check;          // 1: stop a column whose last inner solve gained less than half
+                              // the digits asked (status kStatusStagnated; the host finishes it in FP64)
 };
+
+// Internal result status of a column stopped by the stall check; never returned to callers.
+constexpr int kStatusStagnated = 100;
 
 cudaError_t launch_batched(const BatchArgs& args, int is_float, int K, int rainbow, int threads, int teams,
                            cudaStream_t s);

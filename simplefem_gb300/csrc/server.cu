@@ -131,6 +131,7 @@ int serve_one(feec_server* srv, const Request& rq, cudaStream_t stream, feec_req
         res.outer_iterations = info.outer_iterations;
         res.true_relres = info.true_relres;
         res.cluster_blocks = -info.grid_blocks;   // negative: whole-GPU persistent grid
+        res.fp64_fallback = info.fp64_fallback;
         return st;
     }
     st = sell_prepare(s, rainbow ? FEEC_METHOD_RAINBOW : FEEC_METHOD_CG);
@@ -167,6 +168,7 @@ int serve_one(feec_server* srv, const Request& rq, cudaStream_t stream, feec_req
     a.inner_margin = is_float ? 0.3 : 1.0;
     a.max_iter = rq.n;
     a.max_outer = is_float ? 12 : 4;
+    a.stall_check = is_float;
     // cluster size from the work per iteration: about 0.25 M stored entries per block
     const long long nnz = view.nslices > 0 ? s->nnz : 0;
     int blocks = (int)std::min<long long>(16, std::max<long long>(1, nnz / 250000));
@@ -180,14 +182,45 @@ int serve_one(feec_server* srv, const Request& rq, cudaStream_t stream, feec_req
     FEEC_TRY(launch_cluster(a, 0, is_float, rainbow, blocks, stream));
     BatchResult hr{};
     FEEC_TRY(cudaMemcpyAsync(&hr, dres, sizeof(hr), cudaMemcpyDeviceToHost, stream));
-    FEEC_TRY(cudaMemcpyAsync(rq.x, x, sizeof(double) * n, cudaMemcpyDeviceToHost, stream));
     FEEC_TRY(cudaEventRecord(done_ev, stream));
     FEEC_TRY(cudaEventSynchronize(done_ev));    // blocking wait: slots do not spin on the host
+    if (hr.status == kStatusStagnated) {
+        // FP32 inner solves stopped gaining digits (an operator too ill-conditioned for FP32):
+        // finish in FP64 from the current iterate on the device; the workspace grows to FP64
+        // within the bytes the admission estimate counted for this request.
+        char* w64 = nullptr;
+        FEEC_TRY(mem.alloc(w64, 6 * n * sizeof(double)));
+        const size_t d = n * sizeof(double);
+        it.r = w64; it.d = w64 + d; it.z = w64 + 2 * d; it.m = w64 + 3 * d; it.q = w64 + 4 * d; it.c = w64 + 5 * d;
+        FEEC_TRY(cudaMemcpyAsync(ditem, &it, sizeof(it), cudaMemcpyHostToDevice, stream));
+        FEEC_TRY(cudaMemsetAsync(dres, 0, sizeof(BatchResult), stream));
+        a.inner_eta = 1e-30;
+        a.inner_margin = 1.0;
+        a.max_iter = rq.n;
+        a.max_outer = 4;
+        a.stall_check = 0;
+        int b64 = std::min(blocks, cluster_max_blocks(0, rainbow));
+        int q2 = 1;
+        while (q2 * 2 <= b64) q2 *= 2;
+        FEEC_TRY(launch_cluster(a, 0, 0, rainbow, q2, stream));
+        BatchResult h2{};
+        FEEC_TRY(cudaMemcpyAsync(&h2, dres, sizeof(h2), cudaMemcpyDeviceToHost, stream));
+        FEEC_TRY(cudaEventRecord(done_ev, stream));
+        FEEC_TRY(cudaEventSynchronize(done_ev));
+        h2.iterations += hr.iterations;
+        h2.outer += hr.outer;
+        h2.fp64_fallback = 1;
+        hr = h2;
+    }
+    FEEC_TRY(cudaMemcpyAsync(rq.x, x, sizeof(double) * n, cudaMemcpyDeviceToHost, stream));
+    FEEC_TRY(cudaEventRecord(done_ev, stream));
+    FEEC_TRY(cudaEventSynchronize(done_ev));
     res.status = hr.status;
     res.iterations = hr.iterations;
     res.outer_iterations = hr.outer;
     res.true_relres = hr.relres;
     res.cluster_blocks = blocks;
+    res.fp64_fallback = hr.fp64_fallback;
     return hr.status;
 }
 

@@ -354,9 +354,12 @@ __device__ void team_solve(Team& team, const BatchArgs& args, const BatchItem& i
     }
 
     int done[K], iters[K], outer_cnt[K], status[K];
-    double relres[K];
+    double relres[K], stall_limit[K];
     #pragma unroll
-    for (int j = 0; j < K; j++) { done[j] = j >= kk; iters[j] = 0; outer_cnt[j] = 0; status[j] = FEEC_MAXITER; relres[j] = -1.0; }
+    for (int j = 0; j < K; j++) {
+        done[j] = j >= kk; iters[j] = 0; outer_cnt[j] = 0; status[j] = FEEC_MAXITER; relres[j] = -1.0;
+        stall_limit[j] = 0.0;
+    }
 
     for (int outer = 0; outer < args.max_outer; outer++) {
         // ---- FP64 true residual r64 = b - A x and its norm ----
@@ -393,6 +396,9 @@ __device__ void team_solve(Team& team, const BatchArgs& args, const BatchItem& i
                     if (!done[j]) {
                         if (!(rn == rn)) { done[j] = 1; status[j] = FEEC_BREAKDOWN; }
                         else if (rn <= args.precision * bn) { done[j] = 1; status[j] = FEEC_OK; }
+                        else if (args.stall_check && outer_cnt[j] > 0 && rn > stall_limit[j]) {
+                            done[j] = 1; status[j] = kStatusStagnated;
+                        }
                         else if (iters[j] >= args.max_iter) { done[j] = 1; status[j] = FEEC_MAXITER; }
                     }
                     relres[j] = bn > 0.0 ? rn / bn : 0.0;
@@ -402,6 +408,7 @@ __device__ void team_solve(Team& team, const BatchArgs& args, const BatchItem& i
                     s_scal[1][j] = done[j] ? 0.0 : rn;
                     const double eta = need > args.inner_eta ? need : args.inner_eta;
                     s_scal[2][j] = eta * eta;
+                    stall_limit[j] = rn * sqrt(eta);   // the next residual must gain half the digits asked
                 } else {
                     s_scal[0][j] = 0.0; s_scal[1][j] = 0.0; s_scal[2][j] = 0.0;
                 }

@@ -23,7 +23,7 @@ MODES = {"fp64": _native.MODE_FP64, "mixed": _native.MODE_MIXED}
 class RequestResult(ctypes.Structure):
     _fields_ = [
         ("id", ctypes.c_longlong), ("n", ctypes.c_int), ("status", ctypes.c_int), ("iterations", ctypes.c_int),
-        ("outer_iterations", ctypes.c_int), ("cluster_blocks", ctypes.c_int), ("pad", ctypes.c_int),
+        ("outer_iterations", ctypes.c_int), ("cluster_blocks", ctypes.c_int), ("fp64_fallback", ctypes.c_int),
         ("true_relres", ctypes.c_double), ("t_submit_ms", ctypes.c_double), ("t_start_ms", ctypes.c_double),
         ("t_end_ms", ctypes.c_double),
     ]
@@ -77,7 +77,7 @@ class Server:
         with self._lock:
             for i in range(n.value):
                 r = buf[i]
-                d = {name: getattr(r, name) for name, _ in RequestResult._fields_ if name != "pad"}
+                d = {name: getattr(r, name) for name, _ in RequestResult._fields_}
                 arrays = self._live.pop(r.id)
                 d["x"] = arrays[4]
                 d["latency_ms"] = r.t_end_ms - r.t_submit_ms
