@@ -4,9 +4,9 @@ refined 5 times (N = 274,625, nnz = 7,678,721), multicolor (Rainbow) SSOR-PCG.
 One step = one batch of `--batch` independent solves (seeded U[-1,1] right-hand
 sides, x0 = 0), each to a true FP64 relative residual <= 1e-10, by the batched
 mixed-precision engine (FP32 inner Rainbow SSOR-PCG with compensated dots inside
-FP64 defect correction, one thread block per 4 right-hand sides) with the
-right-hand sides and solutions resident in HBM. `e2e` is the same batch through
-the public System API with the right-hand sides copied in from pinned host memory
+FP64 defect correction; right-hand sides per team and team size chosen by the
+engine's autotuner for the batch, untimed) with the right-hand sides and
+solutions resident in HBM. `e2e` is the same batch through the public System API with the right-hand sides copied in from pinned host memory
 and the solutions copied back inside the timed region. Beside it: one solve on the
 whole GPU (latency p50/p99), the plain FP64 GPU CG and the FP64 drop-in Rainbow
 solver (the reference's own stopping rule) on the same matrix, and the oracle (a
@@ -244,6 +244,113 @@ def run_batched_uneven(dev, count=512, reps=3):
     return out
 
 
+def _rainbow_system(A, C, V):
+    import simplefem_gb300 as S
+    from simplefem_gb300.system import System
+    n = len(A) - 1
+    mat = S.MatrixCSR(n, n, A, C, V)
+    rb = S.Rainbow(mat)
+    sysm = System(A, C, V)
+    sysm.set_rainbow(mat.getDiagonal().raw(), 1.0, rb.num_colors, rb.F, rb.B, rb.R)
+    return sysm, rb.num_colors
+
+
+def run_block_rhs(dev, nrhs=64, reps=3):
+    """64 right-hand sides of the 2D P2 L7 coefficient-mass system (N = 66,049) solved as
+    one blocked batch (K right-hand sides per team share every matrix load), the launch
+    configuration chosen by the autotuner for this batch size; plain CG and Rainbow
+    SSOR-PCG, FP64 and mixed precision, each column to 1e-10. Beside it, single FP64
+    CG solves on the whole GPU."""
+    import torch
+    from simplefem_gb300 import workloads
+    A, C, V = workloads.lattice_matrix(2, 2, 7, 1)
+    n = len(A) - 1
+    sysm, ncol = _rainbow_system(A, C, V)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream()
+    B = torch.from_numpy(np.stack([workloads.uniform_vector(4000 + j, n) for j in range(nrhs)])).to(dev)
+    X = torch.zeros_like(B)
+    out = {"workload": f"2D P2 Lagrange stiffness + coefficient mass (log-uniform [0.1, 10]) refined 7x: N={n}, "
+                       f"nnz={len(C)}, {ncol} colors; {nrhs} right-hand sides", "nrhs": nrhs}
+    for method, mode in (("cg", "fp64"), ("cg", "mixed"), ("rainbow", "fp64"), ("rainbow", "mixed")):
+        cfg = sysm.tune_batch(method, mode, nrhs_hint=nrhs)
+        ms, infos = [], None
+        for rep in range(reps + 1):
+            X.zero_()
+            flush.zero_()
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            infos = sysm.solve_batch(B, X, method=method, mode=mode, precision=PRECISION)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            if rep > 0:
+                ms.append(e0.elapsed_time(e1))
+        assert all(i["status"] == 0 and i["true_relres"] <= PRECISION for i in infos), f"block {method}/{mode}"
+        t = float(np.median(ms))
+        out[f"{method}_{mode}"] = {"ms_per_batch": t, "solves_per_s": nrhs / (t / 1000.0), "config": cfg,
+                                   "iterations_median": int(np.median([i["iterations"] for i in infos])),
+                                   "outer_median": int(np.median([i["outer_iterations"] for i in infos])),
+                                   "fp64_fallbacks": int(sum(i["fp64_fallback"] for i in infos))}
+    single = []
+    for j in range(4):
+        x = torch.zeros(n, dtype=torch.float64, device=dev)
+        flush.zero_()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        sysm.solve(B[j], x, method="cg", mode="fp64", precision=PRECISION)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        if j > 0:
+            single.append(e0.elapsed_time(e1))
+    out["fp64_cg_single_on_whole_gpu"] = {"ms": float(np.median(single)),
+                                          "solves_per_s": 1000.0 / float(np.median(single))}
+    sysm.close()
+    return out
+
+
+def run_mixed_large(dev, reps=3):
+    """The mixed-precision target operator (3D P1 L7, N = 2,146,689): one solve on the whole
+    GPU to 1e-10 in mixed precision and in FP64, each solution's error against an FP64 CG
+    solve at 1e-13 true relative residual."""
+    import torch
+    from simplefem_gb300 import workloads
+    A, C, V = workloads.lattice_matrix(3, 1, 7)
+    n = len(A) - 1
+    sysm, ncol = _rainbow_system(A, C, V)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream()
+    b = torch.from_numpy(workloads.uniform_vector(77, n)).to(dev)
+    xr = torch.zeros(n, dtype=torch.float64, device=dev)
+    ref = sysm.solve(b, xr, method="cg", mode="fp64", precision=1e-13)
+    out = {"workload": f"3D P1 Lagrange stiffness+mass refined 7x: N={n}, nnz={len(C)}, {ncol} colors",
+           "error_reference": {"solver": "FP64 CG to 1e-13 true relative residual", "iterations": ref["iterations"],
+                               "true_relres": ref["true_relres"]}}
+    for method, mode in (("rainbow", "mixed"), ("rainbow", "fp64"), ("cg", "mixed"), ("cg", "fp64")):
+        ms, info, x = [], None, None
+        for rep in range(reps + 1):
+            x = torch.zeros(n, dtype=torch.float64, device=dev)
+            flush.zero_()
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            info = sysm.solve(b, x, method=method, mode=mode, precision=PRECISION)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            if rep > 0:
+                ms.append(e0.elapsed_time(e1))
+        assert info["status"] == 0 and info["true_relres"] <= PRECISION, (method, mode, info)
+        err = float((x - xr).norm() / xr.norm())
+        t = float(np.median(ms))
+        out[f"{method}_{mode}"] = {"ms": t, "solves_per_s": 1000.0 / t, "iterations": info["iterations"],
+                                   "outer_iterations": info["outer_iterations"], "true_relres": info["true_relres"],
+                                   "rel_error_vs_fp64_1e-13": err, "fp64_fallback": info["fp64_fallback"],
+                                   "lanes_per_row": info["lanes_per_row"], "grid_blocks": info["grid_blocks"]}
+    sysm.close()
+    return out
+
+
 def run_serving(mode, method, count=200, rate=200.0, slots=24, budget=120 * 10**9):
     """Poisson-arrival request stream through the continuous-batching server."""
     from simplefem_gb300 import workloads
@@ -301,6 +408,14 @@ def run_ours(args):
         if rank == 0:
             print(json.dumps({"batched_uneven": run_batched_uneven(dev)}), flush=True)
         return
+    if args.only_block_rhs:
+        if rank == 0:
+            print(json.dumps({"block_rhs_64": run_block_rhs(dev)}), flush=True)
+        return
+    if args.only_mixed_large:
+        if rank == 0:
+            print(json.dumps({"mixed_large": run_mixed_large(dev)}), flush=True)
+        return
     if args.only_serving:
         if rank == 0:
             print(json.dumps({"serving": [run_serving("mixed", "rainbow", args.requests),
@@ -308,7 +423,7 @@ def run_ours(args):
                                           run_serving("mixed", "rainbow", 100, rate=5.0),
                                           run_serving("fp64", "cg", 100, rate=5.0)]}), flush=True)
         return
-    A, C, V = workloads.lattice_matrix(**WORKLOAD)
+    A, C, V = workloads.lattice_matrix(**dict(WORKLOAD, L=args.level))
     n = len(A) - 1
     nnz = len(C)
     mat = S.MatrixCSR(n, n, A, C, V)
@@ -319,7 +434,17 @@ def run_ours(args):
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)   # 256 MB > L2 (129 MB)
     stream = torch.cuda.current_stream()
     B_RHS = args.batch
-    K_TEAM = 4
+    if args.rhs_per_team > 0:
+        # a fixed launch configuration (profiling captures: the kernel launches are then exactly
+        # the warm-up and timed steps)
+        sysm.set_batch_config("rainbow", "mixed", rhs_per_team=args.rhs_per_team, team_threads=args.team_threads,
+                              team_blocks=args.team_blocks)
+        tuned = {"rhs_per_team": args.rhs_per_team, "team_threads": args.team_threads,
+                 "team_blocks": args.team_blocks, "fixed": True}
+    else:
+        # launch configuration of the batched engine from the autotuner, for this batch size (untimed)
+        tuned = sysm.tune_batch("rainbow", "mixed", nrhs_hint=B_RHS)
+    K_TEAM = tuned["rhs_per_team"]
 
     def rhs_block(step, count):
         return np.stack([workloads.uniform_vector(1000 + 100003 * rank + 4099 * step + j, n) for j in range(count)])
@@ -331,7 +456,7 @@ def run_ours(args):
     for step in range(args.warmup):                       # untimed warm-up steps
         Bdev.copy_(torch.from_numpy(rhs_block(step, B_RHS)))
         Xdev.zero_()
-        sysm.solve_batch(Bdev, Xdev, method="rainbow", mode="mixed", precision=PRECISION, rhs_per_team=K_TEAM)
+        sysm.solve_batch(Bdev, Xdev, method="rainbow", mode="mixed", precision=PRECISION)
     clocks = ClockSampler(local)
     if world > 1:
         dist.barrier()
@@ -345,7 +470,7 @@ def run_ours(args):
         torch.cuda.synchronize()
         e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        infos = sysm.solve_batch(Bdev, Xdev, method="rainbow", mode="mixed", precision=PRECISION, rhs_per_team=K_TEAM)
+        infos = sysm.solve_batch(Bdev, Xdev, method="rainbow", mode="mixed", precision=PRECISION)
         e1.record(stream)
         torch.cuda.synchronize()
         per.append(e0.elapsed_time(e1))
@@ -383,8 +508,12 @@ def run_ours(args):
     per_step_bytes /= len(infos_all)
     peak, peak_kind = measured_peaks()
     achieved = per_step_bytes / (total_ms / args.steps / 1000.0) / 1e9
+    if tuned["team_blocks"] > 1:
+        kernel_name = f"cluster_batched_kernel<float,{K_TEAM},true> ({tuned['team_blocks']}-block clusters)"
+    else:
+        kernel_name = f"batched_solve_kernel<float,{K_TEAM},true,{tuned['team_threads']}>"
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": None, "kernel": "batched_solve_kernel<float,4,rainbow>", "launches_per_step": 1,
+                "traffic": None, "kernel": kernel_name, "launches_per_step": 1,
                 "bytes_per_launch": per_step_bytes, "ms_per_launch": total_ms / args.steps,
                 "peak_kind": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)"}
 
@@ -399,11 +528,26 @@ def run_ours(args):
         t0 = time.perf_counter()
         Bdev.copy_(hB, non_blocking=True)
         Xdev.zero_()
-        sysm.solve_batch(Bdev, Xdev, method="rainbow", mode="mixed", precision=PRECISION, rhs_per_team=K_TEAM)
+        sysm.solve_batch(Bdev, Xdev, method="rainbow", mode="mixed", precision=PRECISION)
         hX.copy_(Xdev, non_blocking=True)
         torch.cuda.synchronize()
         e2e_per.append(time.perf_counter() - t0)
     e2e_value = world * B_RHS * len(e2e_per) / sum(e2e_per)
+
+    if args.only_batched:
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world,
+                              "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+                              "config": {"workload": f"3D P2 refined {args.level}x, N={n}, nnz={nnz}",
+                                         "batch": B_RHS, "rhs_per_team": K_TEAM, "autotuner": tuned},
+                              "inner_iterations": int(np.median(inner_iters)), "roofline": roofline,
+                              "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": 8 * n * B_RHS,
+                                      "d2h_bytes_per_step": 8 * n * B_RHS},
+                              "gpu_launches": int(launches), "clocks": clock_info}), flush=True)
+        sysm.close()
+        if world > 1:
+            dist.destroy_process_group()
+        return
 
     # ---------------- single-solve latency (whole GPU per solve) and the FP64 baselines ----------------
     def single(method, mode, count, seed):
@@ -438,6 +582,8 @@ def run_ours(args):
 
     spmv = run_spmv(dev)
     uneven = run_batched_uneven(dev) if not args.skip_extras else None
+    block_rhs = run_block_rhs(dev) if not args.skip_extras else None
+    mixed_large = run_mixed_large(dev) if not args.skip_extras else None
     serving = None
     if not args.skip_extras:
         serving = {"mixed_rainbow": run_serving("mixed", "rainbow", args.requests),
@@ -467,10 +613,11 @@ def run_ours(args):
             "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD_NAME,
+            "config": {"workload": WORKLOAD_NAME if args.level == 5 else
+                       f"PROFILING CASE ONLY: 3D P2 refined {args.level}x, N={n}, nnz={nnz}",
                        "solver": "batched mixed precision: FP32 inner Rainbow SSOR-PCG (compensated dots) inside "
-                                 "FP64 defect correction, one thread block per 4 right-hand sides",
-                       "batch": B_RHS, "rhs_per_team": K_TEAM,
+                                 "FP64 defect correction, K right-hand sides per team (autotuned)",
+                       "batch": B_RHS, "rhs_per_team": K_TEAM, "autotuner": tuned,
                        "l2": "flushed (256 MB write) before every timed step; working set > L2",
                        "replicas": "independent batches per GPU (replicas only)"},
             "batch_latency_ms": {"p50": float(np.percentile(per, 50)), "p99": float(np.percentile(per, 99))},
@@ -489,6 +636,8 @@ def run_ours(args):
             "dropin_host_call_ms": 1000 * float(np.median(dropin)),
             "spmv": spmv,
             "batched_uneven": uneven,
+            "block_rhs_64": block_rhs,
+            "mixed_large": mixed_large,
             "serving": serving,
             "roofline": roofline,
             "cpu_baseline": cpu,
@@ -514,6 +663,17 @@ def main():
     ap.add_argument("--only-spmv", action="store_true", help="only the resident SpMV measurement")
     ap.add_argument("--only-uneven", action="store_true", help="only the 512 uneven systems batch")
     ap.add_argument("--only-serving", action="store_true", help="only the serving stream")
+    ap.add_argument("--only-block-rhs", action="store_true", help="only the 64 right-hand-side blocked batch")
+    ap.add_argument("--only-mixed-large", action="store_true", help="only the 3D P1 L7 mixed-precision solves")
+    ap.add_argument("--only-batched", action="store_true",
+                    help="only the batched headline step (no single-solve, SpMV, CPU or extra legs)")
+    ap.add_argument("--rhs-per-team", type=int, default=0,
+                    help="fixed right-hand sides per team instead of the autotuner's choice (profiling)")
+    ap.add_argument("--team-threads", type=int, default=512, help="with --rhs-per-team: threads per team block")
+    ap.add_argument("--team-blocks", type=int, default=1, help="with --rhs-per-team: blocks per team (cluster)")
+    ap.add_argument("--level", type=int, default=5,
+                    help="refinement level of the 3D P2 headline operator (5 = the benchmark; smaller only for "
+                         "profiling captures)")
     ap.add_argument("--requests", type=int, default=200, help="requests in the serving stream")
     ap.add_argument("--skip-extras", action="store_true", help="skip the uneven-batch and serving legs")
     args = ap.parse_args()

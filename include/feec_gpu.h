@@ -156,12 +156,22 @@ int feec_system_solve_batch(feec_system* sys, int method, int mode, int nrhs, do
                             feec_solve_info* infos, void* stream);
 
 /* Autotuner of the batched engine: times short trials of every launch candidate
- * (right-hand sides per team 1/2/4, team size 128/256/512 threads) on this system
- * and caches the fastest, which feec_system_solve_batch then uses whenever
- * rhs_per_team is 0. nrhs_hint caps the trial batch (0 = fill the GPU). Outputs
- * may be NULL. */
+ * (right-hand sides per team 1/2/4; a one-block team of 128..1024 threads, or —
+ * when nrhs_hint leaves fewer work items than the GPU holds one-block teams — a
+ * cluster team of 2/4/8/16 blocks) on this system and caches the fastest, which
+ * feec_system_solve_batch then uses whenever rhs_per_team is 0. nrhs_hint is the
+ * batch size to tune for (0 = fill the GPU). Outputs may be NULL; *team_blocks is
+ * 1 for a one-block team. */
 int feec_system_tune_batch(feec_system* sys, int method, int mode, int nrhs_hint,
-                           int* rhs_per_team, int* team_threads, double* rhs_iters_per_s);
+                           int* rhs_per_team, int* team_threads, int* team_blocks,
+                           double* rhs_iters_per_s);
+
+/* Sets the batched launch configuration used when rhs_per_team is 0, as the
+ * autotuner would (rhs_per_team 0 clears it). team_blocks 1: one-block teams of
+ * team_threads (128/256/512/1024) threads; 2..16 (power of two): cluster teams
+ * of that many 512-thread blocks (team_threads ignored). */
+int feec_system_set_batch_config(feec_system* sys, int method, int mode, int rhs_per_team,
+                                 int team_threads, int team_blocks);
 
 /* Batched solves of many systems, one right-hand side each (device pointers
  * x[i], b[i] of systems[i]->N doubles; host arrays of pointers). Systems are

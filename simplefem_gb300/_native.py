@@ -89,7 +89,9 @@ def gpu():
         L.feec_solve_many.argtypes = [_ip, ctypes.POINTER(_vp), _ip, _ip, ctypes.POINTER(_vp), ctypes.POINTER(_vp),
                                       _dp, _ip, _infop, _vp]
         L.feec_system_tune_batch.argtypes = [_vp, _ip, _ip, _ip, ctypes.POINTER(ctypes.c_int),
-                                             ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)]
+                                             ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
+                                             ctypes.POINTER(ctypes.c_double)]
+        L.feec_system_set_batch_config.argtypes = [_vp, _ip, _ip, _ip, _ip, _ip]
         L.feec_batch_create.argtypes = [ctypes.POINTER(_vp), _ip, ctypes.POINTER(_vp), _ip, _ip, ctypes.POINTER(_vp),
                                          ctypes.POINTER(_vp), _dp, _ip, _ip, _vp]
         L.feec_batch_run.argtypes = [_vp, _infop, ctypes.POINTER(ctypes.c_double)]

@@ -118,9 +118,12 @@ struct Job {
 };
 
 // One launch of the batched kernel over `jobs`; the per-column results come back in `res`.
+// team_blocks >= 2: clusters of that many blocks are the teams (threads is then the cluster
+// kernel's fixed block size); teams = 0 fills the GPU with resident teams.
 int run_batch_results(cudaStream_t st, const std::vector<feec_system*>& systems, std::vector<Job>& jobs, int method,
                       int mode, int K, double precision, int max_iter, int nresults, int teams, int threads,
-                      int max_outer, bool stall_check, std::vector<BatchResult>& res, float* elapsed_ms) {
+                      int team_blocks, int max_outer, bool stall_check, std::vector<BatchResult>& res,
+                      float* elapsed_ms) {
     const int is_float = mode == FEEC_MODE_MIXED ? 1 : 0;
     const size_t tsz = is_float ? sizeof(float) : sizeof(double);
     // largest systems first, so the tail of the batch is short
@@ -168,7 +171,10 @@ int run_batch_results(cudaStream_t st, const std::vector<feec_system*>& systems,
     FEEC_TRY(cudaEventCreate(&e0));
     FEEC_TRY(cudaEventCreate(&e1));
     FEEC_TRY(cudaEventRecord(e0, st));
-    FEEC_TRY(launch_batched(a, is_float, K, method == FEEC_METHOD_RAINBOW, threads, teams, st));
+    if (team_blocks >= 2)
+        FEEC_TRY(launch_batched_clusters(a, is_float, K, method == FEEC_METHOD_RAINBOW, team_blocks, teams, st));
+    else
+        FEEC_TRY(launch_batched(a, is_float, K, method == FEEC_METHOD_RAINBOW, threads, teams, st));
     FEEC_TRY(cudaEventRecord(e1, st));
     res.assign((size_t)nresults, BatchResult{});
     FEEC_TRY(cudaMemcpyAsync(res.data(), dres, sizeof(BatchResult) * nresults, cudaMemcpyDeviceToHost, st));
@@ -205,7 +211,7 @@ int rescue_stagnated(cudaStream_t st, const std::vector<feec_system*>& systems, 
     std::vector<BatchResult> r2;
     float ms = 0.0f;
     const int st2 = run_batch_results(st, systems, again, method, FEEC_MODE_FP64, 1, precision, max_iter,
-                                      (int)again.size(), 0, 256, 0, false, r2, &ms);
+                                      (int)again.size(), 0, 256, 1, 0, false, r2, &ms);
     if (st2 != FEEC_OK) return st2;
     for (size_t k = 0; k < slot.size(); k++) {
         BatchResult& d = res[slot[k]];
@@ -243,13 +249,13 @@ void fill_infos(const std::vector<BatchResult>& res, double precision, float ms,
 
 int run_batch(cudaStream_t st, const std::vector<feec_system*>& systems, std::vector<Job>& jobs, int method, int mode,
               int K, double precision, int max_iter, int nresults, feec_solve_info* infos, int teams, int threads,
-              int max_outer = 0, float* elapsed_ms = nullptr, long long* iter_sum = nullptr) {
+              int team_blocks = 1, int max_outer = 0, float* elapsed_ms = nullptr, long long* iter_sum = nullptr) {
     const int is_float = mode == FEEC_MODE_MIXED ? 1 : 0;
     std::vector<BatchResult> res;
     float ms = 0.0f;
     const bool rescue = is_float && max_outer == 0;   // the autotuner's trials run a fixed iteration count
     int st2 = run_batch_results(st, systems, jobs, method, mode, K, precision, max_iter, nresults, teams, threads,
-                                max_outer, rescue, res, &ms);
+                                team_blocks, max_outer, rescue, res, &ms);
     if (st2 != FEEC_OK) return st2;
     if (rescue) {
         st2 = rescue_stagnated(st, systems, jobs, method, precision, max_iter, res, &ms);
@@ -261,9 +267,16 @@ int run_batch(cudaStream_t st, const std::vector<feec_system*>& systems, std::ve
         for (int i = 0; i < nresults; i++) t += res[i].iterations;
         *iter_sum = t;
     }
+    const int rb = method == FEEC_METHOD_RAINBOW;
+    int grid = 0;
+    if (team_blocks >= 2) {
+        const int nc = teams > 0 ? teams : cluster_batched_resident(is_float, K, rb, team_blocks);
+        grid = std::min<int>(nc, (int)jobs.size()) * team_blocks;
+    } else {
+        grid = teams > 0 ? teams : std::min<int>(batched_resident_teams(is_float, K, rb, threads), (int)jobs.size());
+    }
     int worst = FEEC_OK;
-    fill_infos(res, precision, ms, teams > 0 ? teams : batched_resident_teams(is_float, K, method == FEEC_METHOD_RAINBOW, threads),
-               infos, worst);
+    fill_infos(res, precision, ms, grid, infos, worst);
     return worst;
 }
 
@@ -308,75 +321,127 @@ int feec_system_solve_batch(feec_system* s, int method, int mode, int nrhs, doub
     int st = sell_prepare(s, method);
     if (st == FEEC_OK) {
         int K = pick_k(mode, rhs_per_team);
-        int threads = 256;
+        int threads = 256, blocks = 1;
         if (rhs_per_team == 0 && s->tuned_k[method][mode] > 0) {
             K = s->tuned_k[method][mode];
             threads = s->tuned_threads[method][mode];
+            blocks = std::max(1, s->tuned_blocks[method][mode]);
         }
         std::vector<feec_system*> systems{s};
         std::vector<Job> jobs;
         jobs_for(s, nrhs, K, X, Bm, jobs);
         st = run_batch(s->stream, systems, jobs, method, mode, K, precision, max_iter > 0 ? max_iter : s->n, nrhs,
-                       infos, s->user_blocks, threads);
+                       infos, blocks >= 2 ? 0 : s->user_blocks, threads, blocks);
     }
     s->stream = keep;
     return st;
 }
 
-// Autotuner of the batched engine: for every candidate (right-hand sides per team, team
-// size) it runs a short trial on the system itself — enough columns to fill every
-// resident team once, a fixed number of inner iterations — and keeps the candidate with
-// the highest rate of column-iterations per second. The result is cached for this
-// system and used by feec_system_solve_batch when rhs_per_team is 0.
+int feec_system_set_batch_config(feec_system* s, int method, int mode, int rhs_per_team, int team_threads,
+                                 int team_blocks) {
+    if (!s || (method != FEEC_METHOD_CG && method != FEEC_METHOD_RAINBOW) ||
+        (mode != FEEC_MODE_MIXED && mode != FEEC_MODE_FP64))
+        return FEEC_BADARG;
+    const int is_float = mode == FEEC_MODE_MIXED;
+    if (rhs_per_team == 0) {   // forget the configuration: automatic choice again
+        s->tuned_k[method][mode] = 0; s->tuned_threads[method][mode] = 0; s->tuned_blocks[method][mode] = 0;
+        s->tuned_rate[method][mode] = 0.0;
+        return FEEC_OK;
+    }
+    if (pick_k(mode, rhs_per_team) != rhs_per_team) return FEEC_BADARG;
+    if (team_blocks < 1 || team_blocks > 16 || (team_blocks & (team_blocks - 1)) != 0) return FEEC_BADARG;
+    if (team_blocks == 1 && batched_team_threads(is_float, team_threads) != team_threads) return FEEC_BADARG;
+    if (team_blocks == 1 && team_threads == 1024 && rhs_per_team > 2) return FEEC_BADARG;
+    if (team_blocks >= 2) {
+        if (cluster_batched_resident(is_float, rhs_per_team, method == FEEC_METHOD_RAINBOW, team_blocks) <= 0)
+            return FEEC_BADARG;
+        team_threads = cluster_batched_threads();
+    }
+    s->tuned_k[method][mode] = rhs_per_team;
+    s->tuned_threads[method][mode] = team_threads;
+    s->tuned_blocks[method][mode] = team_blocks;
+    s->tuned_rate[method][mode] = 0.0;
+    return FEEC_OK;
+}
+
+// Autotuner of the batched engine: for every candidate (right-hand sides per team; team
+// size 128..1024 threads for a one-block team, or 2..16 blocks for a cluster team when
+// the batch has fewer work items than the GPU holds block teams) it runs a short trial
+// on the system itself — the batch's columns (at most what the resident teams hold at
+// once), a fixed number of inner iterations — and keeps the candidate with the highest
+// rate of column-iterations per second. The result is cached for this system and used
+// by feec_system_solve_batch when rhs_per_team is 0.
 int feec_system_tune_batch(feec_system* s, int method, int mode, int nrhs_hint, int* rhs_per_team, int* team_threads,
-                           double* rhs_iters_per_s) {
+                           int* team_blocks, double* rhs_iters_per_s) {
     if (!s || (method != FEEC_METHOD_CG && method != FEEC_METHOD_RAINBOW) ||
         (mode != FEEC_MODE_MIXED && mode != FEEC_MODE_FP64))
         return FEEC_BADARG;
     int st = sell_prepare(s, method);
     if (st != FEEC_OK) return st;
     const int is_float = mode == FEEC_MODE_MIXED;
+    const int rb = method == FEEC_METHOD_RAINBOW;
+    struct Candidate { int K, threads, blocks, resident; };
+    std::vector<Candidate> cands;
     const int Ks[3] = {1, 2, 4};
     const int Ts[4] = {128, 256, 512, 1024};
-    TunedConfig best;
-    const size_t n = (size_t)s->n;
-    for (int ki = 0; ki < 3; ki++) {
-        const int K = Ks[ki];
+    const int Cs[4] = {2, 4, 8, 16};
+    for (int K : Ks) {
         if (K > batched_max_k(is_float)) continue;
-        for (int ti = 0; ti < 4; ti++) {
-            const int T = Ts[ti];
+        for (int T : Ts) {
             if (batched_team_threads(is_float, T) != T) continue;
             if (T == 1024 && K > 2) continue;
-            int cols = batched_resident_teams(is_float, K, method == FEEC_METHOD_RAINBOW, T) * K;
-            if (nrhs_hint > 0 && cols > nrhs_hint) cols = std::max(K, (nrhs_hint / K) * K);
-            DevArena tmp; tmp.stream = s->stream;
-            double *B = nullptr, *X = nullptr;
-            FEEC_TRY(tmp.alloc(B, n * cols)); FEEC_TRY(tmp.alloc(X, n * cols));
-            std::vector<double> ones(n, 1.0);
-            for (int c = 0; c < cols; c++)
-                FEEC_TRY(cudaMemcpyAsync(B + c * n, ones.data(), sizeof(double) * n, cudaMemcpyHostToDevice, s->stream));
-            FEEC_TRY(cudaMemsetAsync(X, 0, sizeof(double) * n * cols, s->stream));
-            std::vector<feec_system*> systems{s};
-            std::vector<Job> jobs;
-            jobs_for(s, cols, K, X, B, jobs);
-            float ms = 0.0f;
-            long long its = 0;
-            const int trial_iters = 12;
-            st = run_batch(s->stream, systems, jobs, method, mode, K, 1e-300, trial_iters, cols, nullptr, 0, T, 1, &ms,
-                           &its);
-            tmp.release();
-            cudaStreamSynchronize(s->stream);
-            if (st != FEEC_OK && st != FEEC_MAXITER) return st;
-            const double rate = ms > 0.0f ? (double)its / (ms * 1e-3) : 0.0;
-            if (rate > best.rhs_iters_per_s) { best.valid = true; best.K = K; best.threads = T; best.rhs_iters_per_s = rate; }
+            cands.push_back({K, T, 1, batched_resident_teams(is_float, K, rb, T)});
+        }
+        const int items = nrhs_hint > 0 ? (nrhs_hint + K - 1) / K : 0;
+        if (items > 0 && items < batched_resident_teams(is_float, K, rb, cluster_batched_threads()))
+            for (int C : Cs) {
+                const int res = cluster_batched_resident(is_float, K, rb, C);
+                if (res > 0) cands.push_back({K, cluster_batched_threads(), C, res});
+            }
+    }
+    TunedConfig best;
+    int best_blocks = 1;
+    const size_t n = (size_t)s->n;
+    for (const Candidate& c : cands) {
+        const int K = c.K;
+        int cols = c.resident * K;
+        if (nrhs_hint > 0 && cols > nrhs_hint) cols = std::max(K, ((nrhs_hint + K - 1) / K) * K);
+        DevArena tmp; tmp.stream = s->stream;
+        double *B = nullptr, *X = nullptr;
+        FEEC_TRY(tmp.alloc(B, n * cols)); FEEC_TRY(tmp.alloc(X, n * cols));
+        std::vector<double> ones(n, 1.0);
+        FEEC_TRY(cudaMemcpyAsync(B, ones.data(), sizeof(double) * n, cudaMemcpyHostToDevice, s->stream));
+        for (int done = 1; done < cols;) {   // replicate on the device, doubling the filled columns
+            const int c = std::min(done, cols - done);
+            FEEC_TRY(cudaMemcpyAsync(B + done * n, B, sizeof(double) * n * c, cudaMemcpyDeviceToDevice, s->stream));
+            done += c;
+        }
+        FEEC_TRY(cudaMemsetAsync(X, 0, sizeof(double) * n * cols, s->stream));
+        std::vector<feec_system*> systems{s};
+        std::vector<Job> jobs;
+        jobs_for(s, cols, K, X, B, jobs);
+        float ms = 0.0f;
+        long long its = 0;
+        const int trial_iters = 12;
+        st = run_batch(s->stream, systems, jobs, method, mode, K, 1e-300, trial_iters, cols, nullptr, 0, c.threads,
+                       c.blocks, 1, &ms, &its);
+        tmp.release();
+        cudaStreamSynchronize(s->stream);
+        if (st != FEEC_OK && st != FEEC_MAXITER) return st;
+        const double rate = ms > 0.0f ? (double)its / (ms * 1e-3) : 0.0;
+        if (rate > best.rhs_iters_per_s) {
+            best.valid = true; best.K = K; best.threads = c.threads; best.rhs_iters_per_s = rate;
+            best_blocks = c.blocks;
         }
     }
     if (!best.valid) return FEEC_CUDA_ERROR;
     s->tuned_k[method][mode] = best.K;
     s->tuned_threads[method][mode] = best.threads;
+    s->tuned_blocks[method][mode] = best_blocks;
     s->tuned_rate[method][mode] = best.rhs_iters_per_s;
     if (rhs_per_team) *rhs_per_team = best.K;
     if (team_threads) *team_threads = best.threads;
+    if (team_blocks) *team_blocks = best_blocks;
     if (rhs_iters_per_s) *rhs_iters_per_s = best.rhs_iters_per_s;
     return FEEC_OK;
 }

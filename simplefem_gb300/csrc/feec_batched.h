@@ -68,6 +68,11 @@ cudaError_t launch_cluster(const BatchArgs& args, int item, int is_float, int ra
 int cluster_max_blocks(int is_float, int rainbow);
 int batched_team_threads(int is_float, int requested);
 int batched_max_k(int is_float);
+// Batched engine with clusters of `blocks` (2..16) thread blocks as teams (kernels_cluster_batched.cu).
+cudaError_t launch_batched_clusters(const BatchArgs& args, int is_float, int K, int rainbow, int blocks, int clusters,
+                                    cudaStream_t s);
+int cluster_batched_resident(int is_float, int K, int rainbow, int blocks);
+int cluster_batched_threads();
 
 // y = scaling * A x over a natural-order SELL-32 layout; is_float selects FP32 data
 // (x, y float) or FP64 (x, y double). One thread per row, coalesced entry loads.

@@ -107,6 +107,7 @@ struct feec_system {
     // batched-engine launch choice made by the autotuner, per [method][mode] (0 = not tuned)
     int tuned_k[3][3] = {};
     int tuned_threads[3][3] = {};
+    int tuned_blocks[3][3] = {};       // blocks per team: 1 = block team, 2..16 = cluster team
     double tuned_rate[3][3] = {};
 };
 

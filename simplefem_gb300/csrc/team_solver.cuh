@@ -74,20 +74,31 @@ __device__ __forceinline__ void load_k(const T* p, T (&v)[K]) {
 template <typename T, int K>
 struct Chunk { static constexpr int value = (K >= 4) ? 4 : 8; };
 
+template <typename T, typename TV, int CH>
+__device__ __forceinline__ void load_entries(const int* __restrict__ sci, const TV* __restrict__ sval, long long off,
+                                             int k0, int len, int lane, unsigned long long pol, int (&c)[CH],
+                                             T (&v)[CH]) {
+    #pragma unroll
+    for (int u = 0; u < CH; u++) {
+        const bool ok = k0 + u < len;
+        const long long p = off + (long long)(k0 + u) * 32 + lane;
+        c[u] = ok ? ld_keep(&sci[p], pol) : -1;
+        v[u] = ok ? (T)ld_keep(&sval[p], pol) : T(0);
+    }
+}
+
+// Software-pipelined over chunks of CH entries: the column indices and values of the
+// next chunk are requested together with the gathers of the current one, so a chunk
+// costs one memory round trip instead of two.
 template <typename T, typename TV, int K>
 __device__ __forceinline__ void block_dot(const int* __restrict__ sci, const TV* __restrict__ sval, long long off,
                                           int len, int lane, const T* X, T (&s)[K]) {
     constexpr int CH = Chunk<T, K>::value;
     const unsigned long long pol = l2_keep_policy();
+    if (len <= 0) return;
+    int c[CH]; T v[CH];
+    load_entries<T, TV, CH>(sci, sval, off, 0, len, lane, pol, c, v);
     for (int k0 = 0; k0 < len; k0 += CH) {
-        int c[CH]; T v[CH];
-        #pragma unroll
-        for (int u = 0; u < CH; u++) {
-            const bool ok = k0 + u < len;
-            const long long p = off + (long long)(k0 + u) * 32 + lane;
-            c[u] = ok ? ld_keep(&sci[p], pol) : -1;
-            v[u] = ok ? (T)ld_keep(&sval[p], pol) : T(0);
-        }
         T xv[CH][K];
         #pragma unroll
         for (int u = 0; u < CH; u++) {
@@ -98,10 +109,14 @@ __device__ __forceinline__ void block_dot(const int* __restrict__ sci, const TV*
                 for (int j = 0; j < K; j++) xv[u][j] = T(0);
             }
         }
+        int cn[CH]; T vn[CH];
+        load_entries<T, TV, CH>(sci, sval, off, k0 + CH, len, lane, pol, cn, vn);
         #pragma unroll
         for (int u = 0; u < CH; u++)
             #pragma unroll
             for (int j = 0; j < K; j++) s[j] = fma(v[u], xv[u][j], s[j]);
+        #pragma unroll
+        for (int u = 0; u < CH; u++) { c[u] = cn[u]; v[u] = vn[u]; }
     }
 }
 
@@ -315,6 +330,20 @@ __device__ __forceinline__ void for_slices_dot(const Team& team, const SellView&
     });
 }
 
+// Per-column control state of a team, in shared memory: thread 0 of every block
+// updates it from the team sums (all blocks of a cluster team compute the same values
+// from the same sums) and the other threads read the few scalars a phase needs. Keeping
+// the bookkeeping out of registers leaves them to the slice loops.
+template <typename T, int K>
+struct TeamControl {
+    double bnorm2[K], relres[K], stall[K], rnorm[K], eta2[K], zr[K], rr[K];
+    int iters[K], outer[K], status[K];
+    T alpha[K], beta[K], inv[K];
+    int done;        // bit j: column j finished (converged, failed or absent)
+    int active;      // bit j: column j still iterating in the current inner solve
+    int all_done;
+};
+
 // One team solves work item `it` completely.
 template <typename T, int K, bool RAINBOW, typename Team>
 __device__ void team_solve(Team& team, const BatchArgs& args, const BatchItem& it) {
@@ -329,8 +358,8 @@ __device__ void team_solve(Team& team, const BatchArgs& args, const BatchItem& i
     const T* sd = sel_sd<T>(S);
     double* xp = it.xp; double* bp = it.bp; double* r64 = it.r64;
     T* r = (T*)it.r; T* d = (T*)it.d; T* z = (T*)it.z; T* m = (T*)it.m; T* q = (T*)it.q; T* c = (T*)it.c;
-    __shared__ double s_scal[4][K];
-    __shared__ int s_flag;
+    __shared__ TeamControl<T, K> ctl;
+    const bool leader = threadIdx.x == 0;
 
     // gather caller vectors into the permuted, interleaved layout; ||b||^2
     for (int i = team.tid(); i < n; i += team.nthreads()) {
@@ -341,32 +370,31 @@ __device__ void team_solve(Team& team, const BatchArgs& args, const BatchItem& i
             xp[(long long)i * K + j] = j < kk ? it.x[j][o] : 0.0;
         }
     }
-    double bnorm2[K];
     {
-        double a2[K];
+        double a2[K], o[K];
         #pragma unroll
         for (int j = 0; j < K; j++) a2[j] = 0.0;
         team.sync();
         for (int i = team.tid(); i < n; i += team.nthreads())
             #pragma unroll
             for (int j = 0; j < K; j++) { const double v = bp[(long long)i * K + j]; a2[j] += v * v; }
-        team.template sum<double, K>(a2, bnorm2);
-    }
-
-    int done[K], iters[K], outer_cnt[K], status[K];
-    double relres[K], stall_limit[K];
-    #pragma unroll
-    for (int j = 0; j < K; j++) {
-        done[j] = j >= kk; iters[j] = 0; outer_cnt[j] = 0; status[j] = FEEC_MAXITER; relres[j] = -1.0;
-        stall_limit[j] = 0.0;
+        team.template sum<double, K>(a2, o);
+        if (leader) {
+            ctl.done = 0;
+            for (int j = 0; j < K; j++) {
+                ctl.bnorm2[j] = o[j];
+                ctl.iters[j] = 0; ctl.outer[j] = 0; ctl.status[j] = FEEC_MAXITER; ctl.relres[j] = -1.0;
+                ctl.stall[j] = 0.0;
+                if (j >= kk) ctl.done |= 1 << j;
+            }
+        }
     }
 
     for (int outer = 0; outer < args.max_outer; outer++) {
         // ---- FP64 true residual r64 = b - A x and its norm ----
         team.sync();
-        double rn2[K];
         {
-            double a2[K];
+            double a2[K], rn2[K];
             #pragma unroll
             for (int j = 0; j < K; j++) a2[j] = 0.0;
             for_slices_dot<double, double, K, kBlockFull>(team, S, 0, S.nslices, S.val64, xp,
@@ -385,62 +413,55 @@ __device__ void team_solve(Team& team, const BatchArgs& args, const BatchItem& i
                     }
                 });
             team.template sum<double, K>(a2, rn2);
-        }
-        // stop tests per column (thread 0 decides, broadcast)
-        if (threadIdx.x == 0) {
-            int all = 1;
-            for (int j = 0; j < K; j++) {
-                if (j < kk) {
-                    const double bn = sqrt(bnorm2[j]);
+            // stop tests and the next inner target per column
+            if (leader) {
+                int done = ctl.done;
+                for (int j = 0; j < kk; j++) {
+                    const double bn = sqrt(ctl.bnorm2[j]);
                     const double rn = sqrt(rn2[j]);
-                    if (!done[j]) {
-                        if (!(rn == rn)) { done[j] = 1; status[j] = FEEC_BREAKDOWN; }
-                        else if (rn <= args.precision * bn) { done[j] = 1; status[j] = FEEC_OK; }
-                        else if (args.stall_check && outer_cnt[j] > 0 && rn > stall_limit[j]) {
-                            done[j] = 1; status[j] = kStatusStagnated;
-                        }
-                        else if (iters[j] >= args.max_iter) { done[j] = 1; status[j] = FEEC_MAXITER; }
+                    if (!(done >> j & 1)) {
+                        int st = -1;
+                        if (!(rn == rn)) st = FEEC_BREAKDOWN;
+                        else if (rn <= args.precision * bn) st = FEEC_OK;
+                        else if (args.stall_check && ctl.outer[j] > 0 && rn > ctl.stall[j]) st = kStatusStagnated;
+                        else if (ctl.iters[j] >= args.max_iter) st = FEEC_MAXITER;
+                        if (st >= 0) { done |= 1 << j; ctl.status[j] = st; }
                     }
-                    relres[j] = bn > 0.0 ? rn / bn : 0.0;
+                    ctl.relres[j] = bn > 0.0 ? rn / bn : 0.0;
                     // inner target: the reduction still needed (with margin), never below eta
                     const double need = args.inner_margin * args.precision * bn / (rn > 0.0 ? rn : 1.0);
-                    s_scal[0][j] = done[j] ? 0.0 : (rn > 0.0 ? 1.0 / rn : 0.0);
-                    s_scal[1][j] = done[j] ? 0.0 : rn;
                     const double eta = need > args.inner_eta ? need : args.inner_eta;
-                    s_scal[2][j] = eta * eta;
-                    stall_limit[j] = rn * sqrt(eta);   // the next residual must gain half the digits asked
-                } else {
-                    s_scal[0][j] = 0.0; s_scal[1][j] = 0.0; s_scal[2][j] = 0.0;
+                    const bool live = !(done >> j & 1);
+                    ctl.inv[j] = live && rn > 0.0 ? (T)(1.0 / rn) : T(0);
+                    ctl.rnorm[j] = live ? rn : 0.0;
+                    ctl.eta2[j] = eta * eta;
+                    ctl.stall[j] = rn * sqrt(eta);   // the next residual must gain half the digits asked
                 }
-                all = all && done[j];
+                for (int j = kk; j < K; j++) { ctl.inv[j] = T(0); ctl.rnorm[j] = 0.0; ctl.eta2[j] = 0.0; }
+                ctl.done = done;
+                ctl.all_done = done == (1 << K) - 1;
             }
-            s_flag = all;
         }
         __syncthreads();
-        // thread 0 decided; every other thread reads the decision (s_scal[1] == 0 <=> done)
-        if (threadIdx.x != 0) {
-            #pragma unroll
-            for (int j = 0; j < K; j++) done[j] = s_scal[1][j] == 0.0;
-        }
-        if (s_flag) break;
-        T inv[K];
-        double rnorm[K], eta2d[K];
-        #pragma unroll
-        for (int j = 0; j < K; j++) { inv[j] = (T)s_scal[0][j]; rnorm[j] = s_scal[1][j]; eta2d[j] = s_scal[2][j]; }
-        __syncthreads();
+        if (ctl.all_done) break;
 
         // ---- inner solve: A c = r64 / ||r64|| in T; restart with c = 0, r = rin ----
         Acc arr[K], azr[K];
         #pragma unroll
         for (int j = 0; j < K; j++) { arr[j] = AT::zero(); azr[j] = AT::zero(); }
-        for (int i = team.tid(); i < n; i += team.nthreads()) {
+        {
+            T inv[K];
             #pragma unroll
-            for (int j = 0; j < K; j++) {
-                const long long p = (long long)i * K + j;
-                const T rv = (T)(r64[p] * (double)inv[j]);
-                r[p] = rv; c[p] = T(0); m[p] = T(0); z[p] = T(0); q[p] = T(0);
-                if constexpr (!RAINBOW) { d[p] = rv; azr[j] = AT::add(azr[j], rv * rv); } else { d[p] = T(0); }
-                arr[j] = AT::add(arr[j], rv * rv);
+            for (int j = 0; j < K; j++) inv[j] = ctl.inv[j];
+            for (int i = team.tid(); i < n; i += team.nthreads()) {
+                #pragma unroll
+                for (int j = 0; j < K; j++) {
+                    const long long p = (long long)i * K + j;
+                    const T rv = (T)(r64[p] * (double)inv[j]);
+                    r[p] = rv; c[p] = T(0); m[p] = T(0); z[p] = T(0); q[p] = T(0);
+                    if constexpr (!RAINBOW) { d[p] = rv; azr[j] = AT::add(azr[j], rv * rv); } else { d[p] = T(0); }
+                    arr[j] = AT::add(arr[j], rv * rv);
+                }
             }
         }
         team.sync();
@@ -492,28 +513,23 @@ __device__ void team_solve(Team& team, const BatchArgs& args, const BatchItem& i
                 team.sync();
             }
         }
-        double zr[K], rr[K];
         {
             Acc both[2 * K];
             #pragma unroll
             for (int j = 0; j < K; j++) { both[j] = azr[j]; both[K + j] = arr[j]; }
             double o[2 * K];
             team.template sum<T, 2 * K>(both, o);
-            #pragma unroll
-            for (int j = 0; j < K; j++) { zr[j] = o[j]; rr[j] = o[K + j]; }
-        }
-        int active[K];
-        #pragma unroll
-        for (int j = 0; j < K; j++) active[j] = !done[j];
-        while (true) {
-            // per-column stop on the recursive residual of the inner system
-            int any = 0;
-            #pragma unroll
-            for (int j = 0; j < K; j++) {
-                if (active[j] && (rr[j] < eta2d[j] || iters[j] >= args.max_iter)) active[j] = 0;
-                any |= active[j];
+            if (leader) {
+                int act = 0;
+                for (int j = 0; j < K; j++) {
+                    ctl.zr[j] = o[j]; ctl.rr[j] = o[K + j];
+                    if (!(ctl.done >> j & 1) && !(ctl.rr[j] < ctl.eta2[j]) && ctl.iters[j] < args.max_iter) act |= 1 << j;
+                }
+                ctl.active = act;
             }
-            if (!any) break;
+        }
+        __syncthreads();
+        while (ctl.active) {
             // q = A d (full rows), d.q
             Acc adq[K];
             #pragma unroll
@@ -538,17 +554,27 @@ __device__ void team_solve(Team& team, const BatchArgs& args, const BatchItem& i
                         store_row<T, K>(q, p.row, qv);
                     }
                 });
-            double dq[K];
-            team.template sum<T, K>(adq, dq);
-            T alpha[K];
-            #pragma unroll
-            for (int j = 0; j < K; j++) {
-                alpha[j] = T(0);
-                if (active[j]) {
-                    if (!(dq[j] > 0.0) || !(zr[j] >= 0.0) || !isfinite(dq[j]) || !isfinite(zr[j])) active[j] = 0;
-                    else alpha[j] = (T)(zr[j] / dq[j]);
+            {
+                double dq[K];
+                team.template sum<T, K>(adq, dq);
+                if (leader) {
+                    int act = ctl.active;
+                    for (int j = 0; j < K; j++) {
+                        T a = T(0);
+                        if (act >> j & 1) {
+                            const double zr = ctl.zr[j];
+                            if (!(dq[j] > 0.0) || !(zr >= 0.0) || !isfinite(dq[j]) || !isfinite(zr)) act &= ~(1 << j);
+                            else a = (T)(zr / dq[j]);
+                        }
+                        ctl.alpha[j] = a;
+                    }
+                    ctl.active = act;
                 }
             }
+            __syncthreads();
+            T alpha[K];
+            #pragma unroll
+            for (int j = 0; j < K; j++) alpha[j] = ctl.alpha[j];
             #pragma unroll
             for (int j = 0; j < K; j++) { arr[j] = AT::zero(); azr[j] = AT::zero(); }
             if constexpr (RAINBOW) {
@@ -619,43 +645,63 @@ __device__ void team_solve(Team& team, const BatchArgs& args, const BatchItem& i
                         azr[j] = AT::add(azr[j], rv * rv);
                     }
             }
-            double zr_new[K];
             {
                 Acc both[2 * K];
                 #pragma unroll
                 for (int j = 0; j < K; j++) { both[j] = azr[j]; both[K + j] = arr[j]; }
                 double o[2 * K];
                 team.template sum<T, 2 * K>(both, o);
-                #pragma unroll
-                for (int j = 0; j < K; j++) { zr_new[j] = o[j]; rr[j] = active[j] ? o[K + j] : rr[j]; }
+                if (leader) {
+                    const int was = ctl.active;
+                    int act = was;
+                    for (int j = 0; j < K; j++) {
+                        T b = T(0);
+                        if (was >> j & 1) {
+                            b = (T)(o[j] / ctl.zr[j]);
+                            ctl.zr[j] = o[j];
+                            ctl.rr[j] = o[K + j];
+                            ctl.iters[j]++;
+                            if (ctl.rr[j] < ctl.eta2[j] || ctl.iters[j] >= args.max_iter) act &= ~(1 << j);
+                        }
+                        ctl.beta[j] = b;
+                    }
+                    ctl.active = act;
+                }
             }
-            T beta[K];
-            #pragma unroll
-            for (int j = 0; j < K; j++) {
-                beta[j] = active[j] ? (T)(zr_new[j] / zr[j]) : T(0);
-                if (active[j]) { zr[j] = zr_new[j]; iters[j]++; }
-            }
-            // d = z + beta d for the active columns (CG: z = r)
-            for (int i = team.tid(); i < n; i += team.nthreads()) {
-                if (RAINBOW && __ldg(&wd[i]) == T(0)) continue;
+            __syncthreads();
+            // d = z + beta d (CG: z = r); columns that stopped have beta = 0 and are not read again
+            {
+                T beta[K];
                 #pragma unroll
-                for (int j = 0; j < K; j++) {
-                    if (!active[j]) continue;
-                    const long long p = (long long)i * K + j;
-                    d[p] = (RAINBOW ? z[p] : r[p]) + beta[j] * d[p];
+                for (int j = 0; j < K; j++) beta[j] = ctl.beta[j];
+                const T* zsrc = RAINBOW ? z : r;
+                for (int i = team.tid(); i < n; i += team.nthreads()) {
+                    if (RAINBOW && __ldg(&wd[i]) == T(0)) continue;
+                    T zv[K], dv[K];
+                    load_k_stream<T, K>(zsrc + (long long)i * K, zv);
+                    load_k_stream<T, K>(d + (long long)i * K, dv);
+                    #pragma unroll
+                    for (int j = 0; j < K; j++) dv[j] = zv[j] + beta[j] * dv[j];
+                    store_row<T, K>(d, i, dv);
                 }
             }
             team.sync();
         }
-        // x += ||r|| c in FP64
-        for (int i = team.tid(); i < n; i += team.nthreads())
+        // x += ||r|| c in FP64 (rnorm is 0 for finished columns)
+        {
+            double rnorm[K];
             #pragma unroll
-            for (int j = 0; j < K; j++) {
-                const long long p = (long long)i * K + j;
-                if (!done[j]) xp[p] += rnorm[j] * (double)c[p];
-            }
-        #pragma unroll
-        for (int j = 0; j < K; j++) if (!done[j]) outer_cnt[j]++;
+            for (int j = 0; j < K; j++) rnorm[j] = ctl.rnorm[j];
+            const int done = ctl.done;
+            for (int i = team.tid(); i < n; i += team.nthreads())
+                #pragma unroll
+                for (int j = 0; j < K; j++) {
+                    const long long p = (long long)i * K + j;
+                    if (!(done >> j & 1)) xp[p] += rnorm[j] * (double)c[p];
+                }
+        }
+        if (leader)
+            for (int j = 0; j < K; j++) if (!(ctl.done >> j & 1)) ctl.outer[j]++;
     }
     // scatter x back to the caller's numbering and report
     team.sync();
@@ -665,13 +711,13 @@ __device__ void team_solve(Team& team, const BatchArgs& args, const BatchItem& i
         for (int j = 0; j < K; j++)
             if (j < kk) it.x[j][o] = xp[(long long)i * K + j];
     }
-    if (team.rank() == 0 && threadIdx.x == 0) {
+    if (team.rank() == 0 && leader) {
         for (int j = 0; j < kk; j++) {
             const int slot = it.first_result + j;
-            args.results[slot].status = done[j] ? status[j] : FEEC_MAXITER;
-            args.results[slot].iterations = iters[j];
-            args.results[slot].outer = outer_cnt[j];
-            args.results[slot].relres = relres[j];
+            args.results[slot].status = (ctl.done >> j & 1) ? ctl.status[j] : FEEC_MAXITER;
+            args.results[slot].iterations = ctl.iters[j];
+            args.results[slot].outer = ctl.outer[j];
+            args.results[slot].relres = ctl.relres[j];
         }
     }
 }

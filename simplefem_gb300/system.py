@@ -92,11 +92,19 @@ class System:
     def tune_batch(self, method="rainbow", mode="mixed", nrhs_hint=0) -> dict:
         """Run the batched-engine autotuner on this system; the choice is used by solve_batch
         calls with rhs_per_team=0."""
-        k = ctypes.c_int(0); t = ctypes.c_int(0); rate = ctypes.c_double(0.0)
+        k = ctypes.c_int(0); t = ctypes.c_int(0); c = ctypes.c_int(0); rate = ctypes.c_double(0.0)
         st = self._lib.feec_system_tune_batch(self._h, METHODS[method], MODES[mode], int(nrhs_hint), ctypes.byref(k),
-                                              ctypes.byref(t), ctypes.byref(rate))
+                                              ctypes.byref(t), ctypes.byref(c), ctypes.byref(rate))
         _native.check(st, "feec_system_tune_batch")
-        return {"rhs_per_team": k.value, "team_threads": t.value, "rhs_iters_per_s": rate.value}
+        return {"rhs_per_team": k.value, "team_threads": t.value, "team_blocks": c.value, "rhs_iters_per_s": rate.value}
+
+    def set_batch_config(self, method="rainbow", mode="mixed", rhs_per_team=0, team_threads=256, team_blocks=1):
+        """Fix the batched launch configuration used by solve_batch(rhs_per_team=0): K right-hand
+        sides per team, and either one-block teams of team_threads threads (team_blocks=1) or
+        cluster teams of team_blocks blocks. rhs_per_team=0 returns to the automatic choice."""
+        st = self._lib.feec_system_set_batch_config(self._h, METHODS[method], MODES[mode], int(rhs_per_team),
+                                                    int(team_threads), int(team_blocks))
+        _native.check(st, "feec_system_set_batch_config")
 
     def apply(self, x, y, scaling=1.0):
         """y = scaling * A x for device tensors (float64, or float32 on the FP32 values)."""

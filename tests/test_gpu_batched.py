@@ -147,3 +147,72 @@ def test_graph_captured_batch_replays(cuda):
     batch.close()
     for s in systems:
         s.close()
+
+
+@pytest.mark.parametrize("mode,k,blocks", [("mixed", 4, 4), ("mixed", 2, 8), ("mixed", 1, 2), ("fp64", 2, 4),
+                                           ("fp64", 1, 16)])
+def test_cluster_teams_reach_tolerance(cuda, mode, k, blocks):
+    """Cluster teams (2-16 blocks per work item, sums over distributed shared memory):
+    every column reaches 1e-10 and agrees with an exact solve to 1e-9; FP64 iteration
+    counts equal those of one-block teams within 2% (only the summation order differs)."""
+    torch = cuda
+    from simplefem_gb300 import workloads
+    sysm, M = _prepared(2, 2, 5, seed=4)
+    n = sysm.n
+    nrhs = 6
+    Bh = np.stack([workloads.uniform_vector(900 + j, n) for j in range(nrhs)])
+    X = torch.zeros((nrhs, n), dtype=torch.float64, device="cuda")
+    sysm.set_batch_config("rainbow", mode, rhs_per_team=k, team_blocks=blocks)
+    infos = sysm.solve_batch(torch.from_numpy(Bh).cuda(), X, method="rainbow", mode=mode, precision=1e-10)
+    assert all(i["grid_blocks"] % blocks == 0 for i in infos)
+    sysm.set_batch_config("rainbow", mode, rhs_per_team=0)
+    X1 = torch.zeros((nrhs, n), dtype=torch.float64, device="cuda")
+    ref = sysm.solve_batch(torch.from_numpy(Bh).cuda(), X1, method="rainbow", mode=mode, precision=1e-10,
+                           rhs_per_team=k)
+    Xh = X.cpu().numpy()
+    lu = sla.splu(M.tocsc())
+    for j in range(nrhs):
+        assert infos[j]["status"] == 0, (j, infos[j])
+        assert np.linalg.norm(Bh[j] - M @ Xh[j]) / np.linalg.norm(Bh[j]) <= 1e-10
+        xs = lu.solve(Bh[j])
+        assert np.linalg.norm(Xh[j] - xs) / np.linalg.norm(xs) < 1e-9
+        if mode == "fp64":
+            a, b = infos[j]["iterations"], ref[j]["iterations"]
+            assert abs(a - b) <= max(1, int(np.ceil(0.02 * b))), (a, b)
+    sysm.close()
+
+
+def test_autotuner_choice_is_used_and_correct(cuda):
+    """The autotuner returns a valid configuration (cluster teams allowed when the batch
+    has few work items), and solve_batch with rhs_per_team=0 runs it to 1e-10."""
+    torch = cuda
+    from simplefem_gb300 import workloads
+    sysm, M = _prepared(2, 2, 6, seed=5)
+    n = sysm.n
+    for hint in (8, 0):
+        cfg = sysm.tune_batch("rainbow", "mixed", nrhs_hint=hint)
+        assert cfg["rhs_per_team"] in (1, 2, 4) and cfg["team_blocks"] in (1, 2, 4, 8, 16), cfg
+        assert cfg["rhs_iters_per_s"] > 0
+        if cfg["team_blocks"] == 1:
+            assert cfg["team_threads"] in (128, 256, 512, 1024)
+        nrhs = 8
+        Bh = np.stack([workloads.uniform_vector(950 + j, n) for j in range(nrhs)])
+        X = torch.zeros((nrhs, n), dtype=torch.float64, device="cuda")
+        infos = sysm.solve_batch(torch.from_numpy(Bh).cuda(), X, method="rainbow", mode="mixed", precision=1e-10)
+        Xh = X.cpu().numpy()
+        for j in range(nrhs):
+            assert infos[j]["status"] == 0
+            assert np.linalg.norm(Bh[j] - M @ Xh[j]) / np.linalg.norm(Bh[j]) <= 1e-10
+    sysm.close()
+
+
+def test_batch_config_rejects_invalid(cuda):
+    from simplefem_gb300 import FeecError
+    sysm, _ = _prepared(2, 1, 3)
+    for kw in (dict(rhs_per_team=3), dict(rhs_per_team=4, team_blocks=3), dict(rhs_per_team=4, team_blocks=32),
+               dict(rhs_per_team=4, team_threads=100)):
+        with pytest.raises(FeecError):
+            sysm.set_batch_config("rainbow", "mixed", **kw)
+    with pytest.raises(FeecError):
+        sysm.set_batch_config("rainbow", "fp64", rhs_per_team=4)
+    sysm.close()
