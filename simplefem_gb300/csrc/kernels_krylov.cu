@@ -42,19 +42,30 @@ __device__ __forceinline__ T seg_dot(const int* __restrict__ ci, const T* __rest
 }
 
 // Pipelined row loops of the preconditioned solver. A group (LANES lanes) walks its
-// row slots of a phase; the bounds of its next row are loaded while the current row
-// is processed, and the first row of the next phase is loaded before the grid
-// barrier that separates the phases (the matrix structure is read-only, so only
-// the gathered vector values have to wait for the barrier).
+// row slots of a phase; the bounds of its next row and the first entries of that
+// row's segment (column indices and values, PF per lane) are loaded while the
+// current row is processed, and the first row of the next phase is loaded the same
+// way before the grid barrier that separates the phases: the matrix is read-only,
+// so only the gathered vector values have to wait for the barrier.
+template <typename T, int LANES>
+struct Prefetch {   // entries per lane, within the 64 registers of a thread
+    static constexpr int value = sizeof(T) == 8 ? ((LANES >= 8) ? 1 : 2) : ((LANES >= 16) ? 1 : (LANES >= 8 ? 2 : 4));
+};
+
+template <typename T, int LANES>
 struct RowRef {
-    int i, a, e;   // row (-1: no row for this group), segment [a, e) of ci / val
+    static constexpr int PF = Prefetch<T, LANES>::value;
+    int i, a, e;        // row (-1: no row for this group), segment [a, e) of ci / val
+    int c[PF];          // this lane's first PF entries: j = a + lane + t * LANES
+    T v[PF];
 };
 
 enum { kRowsL = 0, kRowsBackwardU = 1, kRowsFull = 2 };
 
-template <int KIND, typename T>
-__device__ __forceinline__ RowRef row_ref(const PcgArgs<T>& a, int k, int hi) {
-    RowRef r{-1, 0, 0};
+template <int KIND, int LANES, typename T>
+__device__ __forceinline__ RowRef<T, LANES> row_ref(const PcgArgs<T>& a, int k, int hi) {
+    RowRef<T, LANES> r;
+    r.i = -1; r.a = 0; r.e = 0;
     if (k < hi) {
         if (KIND == kRowsBackwardU) {
             r.i = __ldg(&a.brows[k]);
@@ -66,7 +77,30 @@ __device__ __forceinline__ RowRef row_ref(const PcgArgs<T>& a, int k, int hi) {
             r.e = (KIND == kRowsL) ? __ldg(&a.lsplit[k]) : __ldg(&a.rp[k + 1]);
         }
     }
+    const int lane = threadIdx.x & (LANES - 1);
+    #pragma unroll
+    for (int t = 0; t < RowRef<T, LANES>::PF; t++) {
+        const int j = r.a + lane + t * LANES;
+        const bool ok = j < r.e;
+        r.c[t] = ok ? __ldg(&a.ci[j]) : 0;
+        r.v[t] = ok ? __ldg(&a.val[j]) : T(0);
+    }
     return r;
+}
+
+// seg_dot over a prefetched row: the same terms in the same order as seg_dot.
+template <typename T, int LANES>
+__device__ __forceinline__ T seg_dot_pre(const RowRef<T, LANES>& R, const int* __restrict__ ci,
+                                         const T* __restrict__ v, const T* x, int lane) {
+    constexpr int PF = RowRef<T, LANES>::PF;
+    T s = T(0);
+    #pragma unroll
+    for (int t = 0; t < PF; t++)
+        if (R.a + lane + t * LANES < R.e) s = fma(R.v[t], x[R.c[t]], s);
+    for (int j = R.a + lane + PF * LANES; j < R.e; j += LANES) s = fma(__ldg(&v[j]), x[__ldg(&ci[j])], s);
+    #pragma unroll
+    for (int off = LANES / 2; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off, LANES);
+    return s;
 }
 
 template <int LANES>
@@ -83,11 +117,11 @@ __device__ __forceinline__ int group_stride() {
 }
 
 template <int LANES, int KIND, typename T, typename F>
-__device__ __forceinline__ void rows_pipelined(const PcgArgs<T>& a, int lo, int hi, RowRef cur, F&& body) {
+__device__ __forceinline__ void rows_pipelined(const PcgArgs<T>& a, int lo, int hi, RowRef<T, LANES> cur, F&& body) {
     const int stride = group_stride<LANES>();
     int k = group_first<LANES>(lo);
     for (int base = group_base<LANES>(lo); base < hi; base += stride, k += stride) {
-        const RowRef nxt = row_ref<KIND>(a, k + stride, hi);
+        const RowRef<T, LANES> nxt = row_ref<KIND, LANES>(a, k + stride, hi);
         body(cur);
         cur = nxt;
     }
@@ -222,8 +256,10 @@ __global__ void __launch_bounds__(kThreads) cg_persistent(CgArgs<T> a) {
 // ---------------------------------------------------------------------------
 // SSOR / multicolor SSOR preconditioned CG
 // ---------------------------------------------------------------------------
+// Two co-resident 512-thread blocks per SM (64 registers per thread): the phases are
+// latency-bound, so warps in flight matter more than registers.
 template <typename T, int LANES>
-__global__ void __launch_bounds__(kThreads) pcg_persistent(PcgArgs<T> a) {
+__global__ void __launch_bounds__(kThreads, 2) pcg_persistent(PcgArgs<T> a) {
     using AT = AccT<T>;
     using Acc = typename AT::type;
     unsigned long long epoch = 0;
@@ -294,7 +330,7 @@ __global__ void __launch_bounds__(kThreads) pcg_persistent(PcgArgs<T> a) {
     int K = 0;
     int status = FEEC_MAXITER;
     double d_Ad = 0.0;
-    RowRef pf = row_ref<kRowsFull>(a, group_first<LANES>(0), n);
+    RowRef<T, LANES> pf = row_ref<kRowsFull, LANES>(a, group_first<LANES>(0), n);
     while (K < a.max_iter) {
         if (threadIdx.x == 0) {
             if (a.print_modulo > 0 && K % a.print_modulo == 0 && blockIdx.x == 0)
@@ -308,9 +344,9 @@ __global__ void __launch_bounds__(kThreads) pcg_persistent(PcgArgs<T> a) {
         if (s_ctl) { status = FEEC_OK; break; }
 
         Acc adq = AT::zero();                                                          // :1197-1212
-        rows_pipelined<LANES, kRowsFull>(a, 0, n, pf, [&](const RowRef& R) {
+        rows_pipelined<LANES, kRowsFull>(a, 0, n, pf, [&](const RowRef<T, LANES>& R) {
             const bool act = R.i >= 0;
-            const T s = seg_dot<T, LANES>(a.ci, a.val, a.d, R.a, R.e, lane);
+            const T s = seg_dot_pre<T, LANES>(R, a.ci, a.val, a.d, lane);
             if (act && lane == 0) {
                 const T qi = (__ldg(&a.wd[R.i]) != T(0)) ? s : T(0);
                 a.q[R.i] = qi;
@@ -319,7 +355,7 @@ __global__ void __launch_bounds__(kThreads) pcg_persistent(PcgArgs<T> a) {
         });
         write_partials<T>(p_dq, adq);
         int flo = __ldg(&a.fptr[0]), fhi = __ldg(&a.fptr[1]);
-        pf = row_ref<kRowsL>(a, group_first<LANES>(flo), fhi);
+        pf = row_ref<kRowsL, LANES>(a, group_first<LANES>(flo), fhi);
         if (!grid_barrier(a.st, epoch, 14)) return;
         double dq[1];
         grid_sum<1>(p_dq, dq);
@@ -338,9 +374,9 @@ __global__ void __launch_bounds__(kThreads) pcg_persistent(PcgArgs<T> a) {
         const T alpha = (T)s_scal[0];
         arr = AT::zero();
         for (int p = 0; p < a.nf; p++) {                                               // :1230-1261
-            rows_pipelined<LANES, kRowsL>(a, flo, fhi, pf, [&](const RowRef& R) {
+            rows_pipelined<LANES, kRowsL>(a, flo, fhi, pf, [&](const RowRef<T, LANES>& R) {
                 const bool act = R.i >= 0;
-                const T s = seg_dot<T, LANES>(a.ci, a.val, a.m, R.a, R.e, lane);
+                const T s = seg_dot_pre<T, LANES>(R, a.ci, a.val, a.m, lane);
                 if (act && lane == 0) {
                     const T w = __ldg(&a.wd[R.i]);
                     if (w != T(0)) {
@@ -355,18 +391,18 @@ __global__ void __launch_bounds__(kThreads) pcg_persistent(PcgArgs<T> a) {
             if (p + 1 < a.nf) {
                 flo = fhi;
                 fhi = __ldg(&a.fptr[p + 2]);
-                pf = row_ref<kRowsL>(a, group_first<LANES>(flo), fhi);
+                pf = row_ref<kRowsL, LANES>(a, group_first<LANES>(flo), fhi);
             } else {
-                pf = row_ref<kRowsBackwardU>(a, group_first<LANES>(__ldg(&a.bptr[0])), __ldg(&a.bptr[1]));
+                pf = row_ref<kRowsBackwardU, LANES>(a, group_first<LANES>(__ldg(&a.bptr[0])), __ldg(&a.bptr[1]));
             }
             if (!grid_barrier(a.st, epoch, 15)) return;
         }
         azr = AT::zero();
         for (int p = 0; p < a.nbw; p++) {                                              // :1263-1307
             const int lo_r = __ldg(&a.bptr[p]), hi_r = __ldg(&a.bptr[p + 1]);
-            rows_pipelined<LANES, kRowsBackwardU>(a, lo_r, hi_r, pf, [&](const RowRef& R) {
+            rows_pipelined<LANES, kRowsBackwardU>(a, lo_r, hi_r, pf, [&](const RowRef<T, LANES>& R) {
                 const bool act = R.i >= 0;
-                const T s = seg_dot<T, LANES>(a.ci, a.val, a.z, R.a, R.e, lane);
+                const T s = seg_dot_pre<T, LANES>(R, a.ci, a.val, a.z, lane);
                 if (act && lane == 0) {
                     const T w = __ldg(&a.wd[R.i]);
                     if (w != T(0)) {
@@ -379,11 +415,11 @@ __global__ void __launch_bounds__(kThreads) pcg_persistent(PcgArgs<T> a) {
                 }
             });
             if (p + 1 < a.nbw) {
-                pf = row_ref<kRowsBackwardU>(a, group_first<LANES>(hi_r), __ldg(&a.bptr[p + 2]));
+                pf = row_ref<kRowsBackwardU, LANES>(a, group_first<LANES>(hi_r), __ldg(&a.bptr[p + 2]));
                 if (!grid_barrier(a.st, epoch, 16)) return;
             }
         }
-        pf = row_ref<kRowsFull>(a, group_first<LANES>(0), n);
+        pf = row_ref<kRowsFull, LANES>(a, group_first<LANES>(0), n);
         write_partials2<T>(p_zr, azr, arr);
         if (!grid_barrier(a.st, epoch, 17)) return;
         grid_sum<2>(p_zr, zr2);
