@@ -367,10 +367,12 @@ int feec_system_set_batch_config(feec_system* s, int method, int mode, int rhs_p
 // Autotuner of the batched engine: for every candidate (right-hand sides per team; team
 // size 128..1024 threads for a one-block team, or 2..16 blocks for a cluster team when
 // the batch has fewer work items than the GPU holds block teams) it runs a short trial
-// on the system itself — the batch's columns (at most what the resident teams hold at
-// once), a fixed number of inner iterations — and keeps the candidate with the highest
-// rate of column-iterations per second. The result is cached for this system and used
-// by feec_system_solve_batch when rhs_per_team is 0.
+// on the system itself — the batch's columns (without a size hint, one work item per
+// resident team), a fixed number of inner iterations — and rates it in
+// column-iterations per second. The three best are trialled again at two lengths, and
+// the difference rates the iterations alone (a solve's set-up favours wide teams in a
+// short trial). The winner is cached for this system and used by
+// feec_system_solve_batch when rhs_per_team is 0.
 int feec_system_tune_batch(feec_system* s, int method, int mode, int nrhs_hint, int* rhs_per_team, int* team_threads,
                            int* team_blocks, double* rhs_iters_per_s) {
     if (!s || (method != FEEC_METHOD_CG && method != FEEC_METHOD_RAINBOW) ||
@@ -399,38 +401,66 @@ int feec_system_tune_batch(feec_system* s, int method, int mode, int nrhs_hint, 
                 if (res > 0) cands.push_back({K, cluster_batched_threads(), C, res});
             }
     }
-    TunedConfig best;
-    int best_blocks = 1;
     const size_t n = (size_t)s->n;
-    for (const Candidate& c : cands) {
+    // A rough right-hand side (U[-1, 1) from a fixed-seed LCG): a smooth one such as all
+    // ones converges within a few iterations and would time set-up instead of iterations.
+    std::vector<double> rhs(n);
+    {
+        unsigned long long g = 0x9E3779B97F4A7C15ull;
+        for (size_t i = 0; i < n; i++) {
+            g = g * 6364136223846793005ull + 1442695040888963407ull;
+            rhs[i] = (double)(g >> 11) * (2.0 / 9007199254740992.0) - 1.0;
+        }
+    }
+    // One trial: `iters` inner iterations of every column; time and column-iterations done.
+    auto trial = [&](const Candidate& c, int iters, float& ms, long long& its) -> int {
         const int K = c.K;
-        int cols = c.resident * K;
-        if (nrhs_hint > 0 && cols > nrhs_hint) cols = std::max(K, ((nrhs_hint + K - 1) / K) * K);
+        // the whole batch when its size is known (a batch with more work items than resident
+        // teams runs in waves, and the trial must see them), else one item per resident team
+        const int cols = nrhs_hint > 0 ? ((nrhs_hint + K - 1) / K) * K : c.resident * K;
         DevArena tmp; tmp.stream = s->stream;
         double *B = nullptr, *X = nullptr;
         FEEC_TRY(tmp.alloc(B, n * cols)); FEEC_TRY(tmp.alloc(X, n * cols));
-        std::vector<double> ones(n, 1.0);
-        FEEC_TRY(cudaMemcpyAsync(B, ones.data(), sizeof(double) * n, cudaMemcpyHostToDevice, s->stream));
+        FEEC_TRY(cudaMemcpyAsync(B, rhs.data(), sizeof(double) * n, cudaMemcpyHostToDevice, s->stream));
         for (int done = 1; done < cols;) {   // replicate on the device, doubling the filled columns
-            const int c = std::min(done, cols - done);
-            FEEC_TRY(cudaMemcpyAsync(B + done * n, B, sizeof(double) * n * c, cudaMemcpyDeviceToDevice, s->stream));
-            done += c;
+            const int m = std::min(done, cols - done);
+            FEEC_TRY(cudaMemcpyAsync(B + done * n, B, sizeof(double) * n * m, cudaMemcpyDeviceToDevice, s->stream));
+            done += m;
         }
         FEEC_TRY(cudaMemsetAsync(X, 0, sizeof(double) * n * cols, s->stream));
         std::vector<feec_system*> systems{s};
         std::vector<Job> jobs;
         jobs_for(s, cols, K, X, B, jobs);
-        float ms = 0.0f;
-        long long its = 0;
-        const int trial_iters = 12;
-        st = run_batch(s->stream, systems, jobs, method, mode, K, 1e-300, trial_iters, cols, nullptr, 0, c.threads,
-                       c.blocks, 1, &ms, &its);
+        ms = 0.0f; its = 0;
+        const int e = run_batch(s->stream, systems, jobs, method, mode, K, 1e-300, iters, cols, nullptr, 0, c.threads,
+                                c.blocks, 1, &ms, &its);
         tmp.release();
         cudaStreamSynchronize(s->stream);
-        if (st != FEEC_OK && st != FEEC_MAXITER) return st;
-        const double rate = ms > 0.0f ? (double)its / (ms * 1e-3) : 0.0;
+        return (e == FEEC_OK || e == FEEC_MAXITER) ? FEEC_OK : e;
+    };
+    // Screening: a short trial per candidate (its rate includes the set-up of a solve).
+    std::vector<std::pair<double, size_t>> screened;
+    for (size_t ci = 0; ci < cands.size(); ci++) {
+        float ms; long long its;
+        st = trial(cands[ci], 12, ms, its);
+        if (st != FEEC_OK) return st;
+        screened.push_back({ms > 0.0f ? (double)its / (ms * 1e-3) : 0.0, ci});
+    }
+    std::sort(screened.begin(), screened.end(), [](const auto& a, const auto& b) { return a.first > b.first; });
+    // Final: the best three by screening, rated on the difference of a long and a short trial,
+    // so the rate is that of the iterations alone, without the set-up of a solve.
+    TunedConfig best;
+    int best_blocks = 1;
+    for (size_t r = 0; r < screened.size() && r < 3; r++) {
+        const Candidate& c = cands[screened[r].second];
+        float ms1, ms2; long long its1, its2;
+        st = trial(c, 6, ms1, its1);
+        if (st != FEEC_OK) return st;
+        st = trial(c, 30, ms2, its2);
+        if (st != FEEC_OK) return st;
+        const double rate = (ms2 > ms1 && its2 > its1) ? (double)(its2 - its1) / ((ms2 - ms1) * 1e-3) : screened[r].first;
         if (rate > best.rhs_iters_per_s) {
-            best.valid = true; best.K = K; best.threads = c.threads; best.rhs_iters_per_s = rate;
+            best.valid = true; best.K = c.K; best.threads = c.threads; best.rhs_iters_per_s = rate;
             best_blocks = c.blocks;
         }
     }

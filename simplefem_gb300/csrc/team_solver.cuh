@@ -72,7 +72,7 @@ __device__ __forceinline__ void load_k(const T* p, T (&v)[K]) {
 // first (all independent, coalesced across the warp), then the CH gathers are
 // issued together, then the FMAs run; padded slots are predicated off.
 template <typename T, int K>
-struct Chunk { static constexpr int value = (K >= 4) ? 4 : 8; };
+struct Chunk { static constexpr int value = sizeof(T) == 8 ? ((K >= 2) ? 2 : 4) : ((K >= 4) ? 4 : 8); };
 
 template <typename T, typename TV, int CH>
 __device__ __forceinline__ void load_entries(const int* __restrict__ sci, const TV* __restrict__ sval, long long off,
@@ -336,7 +336,7 @@ __device__ __forceinline__ void for_slices_dot(const Team& team, const SellView&
 // the bookkeeping out of registers leaves them to the slice loops.
 template <typename T, int K>
 struct TeamControl {
-    double bnorm2[K], relres[K], stall[K], rnorm[K], eta2[K], zr[K], rr[K];
+    double bnorm2[K], relres[K], stall[K], rnorm[K], eta2[K], zr[K], rr[K], rr_next[K];
     int iters[K], outer[K], status[K];
     T alpha[K], beta[K], inv[K];
     int done;        // bit j: column j finished (converged, failed or absent)
@@ -586,26 +586,28 @@ __device__ void team_solve(Team& team, const BatchArgs& args, const BatchItem& i
                             p.w = p.act ? __ldg(&wd[p.row]) : T(0);
                             load_row<T, K>(r, p.row, p.act, p.a);
                             load_row<T, K>(q, p.row, p.act, p.b);
-                            load_row<T, K>(d, p.row, p.act, p.c);
-                            load_row<T, K>(c, p.row, p.act, p.e);
                             return p;
                         },
                         [&](const SliceMeta&, const RowState<T, K>& p, const T (&sum)[K]) {
                             if (p.act && p.w != T(0)) {
-                                T mv[K], rv[K], cv[K];
+                                T mv[K], rv[K];
                                 #pragma unroll
                                 for (int j = 0; j < K; j++) {
-                                    cv[j] = p.e[j] + alpha[j] * p.c[j];
                                     rv[j] = p.a[j] - alpha[j] * p.b[j];
                                     arr[j] = AT::add(arr[j], rv[j] * rv[j]);
                                     mv[j] = (rv[j] - sum[j]) * p.w;
                                 }
-                                store_row<T, K>(c, p.row, cv);
                                 store_row<T, K>(r, p.row, rv);
                                 store_row<T, K>(m, p.row, mv);
                             }
                         });
                     team.sync();
+                }
+                {   // r.r now, so its accumulators are not carried through the backward sweep
+                    double o[K];
+                    team.template sum<T, K>(arr, o);
+                    if (leader)
+                        for (int j = 0; j < K; j++) ctl.rr_next[j] = o[j];
                 }
                 for (int col = S.ncolors - 1; col >= 0; col--) {
                     for_slices_dot<T, T, K, kBlockU>(team, S, __ldg(&S.color_slice[col]), __ldg(&S.color_slice[col + 1]), val, z,
@@ -646,11 +648,18 @@ __device__ void team_solve(Team& team, const BatchArgs& args, const BatchItem& i
                     }
             }
             {
-                Acc both[2 * K];
-                #pragma unroll
-                for (int j = 0; j < K; j++) { both[j] = azr[j]; both[K + j] = arr[j]; }
                 double o[2 * K];
-                team.template sum<T, 2 * K>(both, o);
+                if constexpr (RAINBOW) {
+                    double oz[K];
+                    team.template sum<T, K>(azr, oz);
+                    #pragma unroll
+                    for (int j = 0; j < K; j++) { o[j] = oz[j]; o[K + j] = ctl.rr_next[j]; }
+                } else {
+                    Acc both[2 * K];
+                    #pragma unroll
+                    for (int j = 0; j < K; j++) { both[j] = azr[j]; both[K + j] = arr[j]; }
+                    team.template sum<T, 2 * K>(both, o);
+                }
                 if (leader) {
                     const int was = ctl.active;
                     int act = was;
@@ -669,7 +678,9 @@ __device__ void team_solve(Team& team, const BatchArgs& args, const BatchItem& i
                 }
             }
             __syncthreads();
-            // d = z + beta d (CG: z = r); columns that stopped have beta = 0 and are not read again
+            // Rainbow: c += alpha d (the solution update of the reference's forward sweep,
+            // moved here where d is loaded anyway); then d = z + beta d (CG: z = r). Columns
+            // that stopped have alpha = beta = 0 and their d is not read again.
             {
                 T beta[K];
                 #pragma unroll
@@ -680,6 +691,13 @@ __device__ void team_solve(Team& team, const BatchArgs& args, const BatchItem& i
                     T zv[K], dv[K];
                     load_k_stream<T, K>(zsrc + (long long)i * K, zv);
                     load_k_stream<T, K>(d + (long long)i * K, dv);
+                    if constexpr (RAINBOW) {
+                        T cv[K];
+                        load_k_stream<T, K>(c + (long long)i * K, cv);
+                        #pragma unroll
+                        for (int j = 0; j < K; j++) cv[j] = cv[j] + alpha[j] * dv[j];
+                        store_row<T, K>(c, i, cv);
+                    }
                     #pragma unroll
                     for (int j = 0; j < K; j++) dv[j] = zv[j] + beta[j] * dv[j];
                     store_row<T, K>(d, i, dv);
