@@ -39,6 +39,23 @@ PRECISION = 1e-10
 DRAM_OVER_ALGORITHMIC_K4_T512 = 1.030
 
 
+def max_over_ranks(x, device=None):
+    """Largest value of x over the ranks of the default process group (x itself when
+    there is none): the timed region of the slowest replica bounds the whole job."""
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(x)
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(units_per_rank, world, seconds):
+    """Whole-job throughput of `world` replicas that each processed `units_per_rank`."""
+    return world * units_per_rank / seconds
+
+
 def rank_info():
     return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
 
@@ -478,13 +495,10 @@ def run_ours(args):
         infos_all.append(infos)
     clock_info = clocks.stop()
     launches = lib.feec_kernel_launches() - launches0
-    total_ms = float(sum(per))
+    total_ms = max_over_ranks(float(sum(per)), dev)
     if world > 1:
-        t = torch.tensor([total_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
         dist.barrier()
-    value = world * args.steps * B_RHS / (total_ms / 1000.0)
+    value = whole_job_rate(args.steps * B_RHS, world, total_ms / 1000.0)
     flat = [i for infos in infos_all for i in infos]
     assert all(i["status"] == 0 and 0 <= i["true_relres"] <= PRECISION for i in flat), "batched solve missed 1e-10"
     inner_iters = [i["iterations"] for i in flat]
@@ -542,7 +556,7 @@ def run_ours(args):
         hX.copy_(Xdev, non_blocking=True)
         torch.cuda.synchronize()
         e2e_per.append(time.perf_counter() - t0)
-    e2e_value = world * B_RHS * len(e2e_per) / sum(e2e_per)
+    e2e_value = whole_job_rate(B_RHS * len(e2e_per), world, max_over_ranks(sum(e2e_per), dev))
 
     if args.only_batched:
         if rank == 0:
