@@ -119,6 +119,13 @@ int serve_one(feec_server* srv, const Request& rq, cudaStream_t stream, feec_req
         FEEC_TRY(cudaMemcpyAsync(b, rq.b, sizeof(double) * rq.n, cudaMemcpyHostToDevice, stream));
         FEEC_TRY(cudaMemsetAsync(x, 0, sizeof(double) * rq.n, stream));
         feec_solve_info info;
+        // One persistent block per SM (not two): every SM keeps room for a cluster block, so
+        // the requests being solved as clusters keep running beside the large solve instead
+        // of queueing behind it, and the large solve's cooperative launch finds its blocks a
+        // place even while clusters are resident.
+        int sms = 0;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, srv->device);
+        feec_system_set_launch(s, sms, 0);
         std::lock_guard<std::mutex> lane(srv->big_lane);
         res.t_start_ms = ms_since(srv, clock_type::now());
         st = feec_system_solve(s, rainbow ? FEEC_METHOD_RAINBOW : FEEC_METHOD_CG, srv->mode, x, b, nullptr,
