@@ -374,6 +374,226 @@ int oracle_cg_rainbow(int N, double* x, const double* b, const int* A, const int
     return K;
 }
 
+/* Shared by both Eisenstat variants: work vectors start as NaN, as in the reference
+ * (std::fill_n(..., notanumber)), so rows the sweeps skip stay NaN. */
+static double* nan_vector(int N)
+{
+    double* v = (double*)malloc((size_t)(N > 0 ? N : 1) * sizeof(double));
+    if (v) for (int i = 0; i < N; i++) v[i] = NAN;
+    return v;
+}
+
+/* solver/sparsesolver.cpp:726-995, SSOR-PCG with Eisenstat's trick (index order); returns K.
+ * The iteration works on the L-solved residual: `residual` holds it on return. */
+int oracle_cg_ssor_eisenstat(int N, double* x, const double* b, const int* A, const int* C, const double* V,
+                             double* residual, double precision, int print_modulo,
+                             const double* diagonal, double omega)
+{
+    (void)print_modulo;
+    double tolerance = 0.0;                                   /* :750-753 */
+    for (int i = 0; i < N; i++) tolerance += b[i] * b[i];
+    tolerance = precision * sqrt(tolerance);
+    tolerance = dmax(tolerance, ORACLE_DESIRED_PRECISION);
+
+    double* direction = nan_vector(N);                        /* :766-773 */
+    double* zirconium = nan_vector(N);
+    double* technical = nan_vector(N);
+    double* auxiliary = nan_vector(N);
+    if (!direction || !zirconium || !technical || !auxiliary) {
+        free(direction); free(zirconium); free(technical); free(auxiliary); return -1;
+    }
+    double z_r = NAN;
+    int K = 0;
+    while (K < N) {
+        if (K == 0) {                                         /* :786-842 */
+            #pragma omp parallel for
+            for (int c = 0; c < N; c++) {
+                if (diagonal[c] == 0.0) continue;
+                double aux = b[c];
+                for (int d = A[c]; d < A[c + 1]; d++)
+                    if (diagonal[C[d]] != 0.0) aux -= V[d] * x[C[d]];
+                auxiliary[c] = aux;
+            }
+            for (int c = 0; c < N; c++) {
+                if (diagonal[c] == 0.0) continue;
+                double aux = auxiliary[c];
+                for (int d = A[c]; d < A[c + 1]; d++)
+                    if (C[d] < c && diagonal[C[d]] != 0.0) aux -= V[d] * residual[C[d]];
+                residual[c] = aux * omega / diagonal[c];
+            }
+            z_r = 0.0;
+            #pragma omp parallel for reduction(+:z_r)
+            for (int c = 0; c < N; c++) {
+                if (diagonal[c] == 0.0) continue;
+                zirconium[c] = residual[c] * diagonal[c] * (2.0 - omega) / omega;
+                direction[c] = zirconium[c];
+                z_r += zirconium[c] * residual[c];
+            }
+        }
+        if (fabs(z_r) < tolerance * tolerance) break;        /* :859-862 */
+
+        double d_Ad = 0.0;                                    /* :870-914 */
+        for (int c = N - 1; c >= 0; c--) {
+            if (diagonal[c] == 0.0) continue;
+            double aux = direction[c];
+            for (int d = A[c]; d < A[c + 1]; d++)
+                if (C[d] > c && diagonal[C[d]] != 0.0) aux -= V[d] * technical[C[d]];
+            technical[c] = aux * omega / diagonal[c];
+        }
+        for (int c = 0; c < N; c++) {
+            if (diagonal[c] == 0.0) continue;
+            double aux = direction[c] - (2.0 / omega - 1.0) * diagonal[c] * technical[c];
+            for (int d = A[c]; d < A[c + 1]; d++)
+                if (C[d] < c && diagonal[C[d]] != 0.0) aux -= V[d] * auxiliary[C[d]];
+            auxiliary[c] = aux * omega / diagonal[c];
+        }
+        #pragma omp parallel for reduction(+:d_Ad)
+        for (int c = 0; c < N; c++) {
+            if (diagonal[c] == 0.0) continue;
+            auxiliary[c] += technical[c];
+            d_Ad += auxiliary[c] * direction[c];
+        }
+        int numerator_bad = !isfinite(z_r) || z_r < 0.0;      /* :918-933 */
+        int denominator_bad = !isfinite(d_Ad) || d_Ad < 0.0;
+        int denominator_small = sqrt(fabs(d_Ad)) < ORACLE_MACHINE_EPSILON;
+        if (numerator_bad || denominator_bad) break;
+        if (denominator_small) break;
+
+        const double alpha = z_r / d_Ad;                      /* :936-975 */
+        double z_r_new = 0.0;
+        #pragma omp parallel for reduction(+:z_r_new)
+        for (int c = 0; c < N; c++) {
+            if (diagonal[c] == 0.0) continue;
+            x[c] += alpha * technical[c];
+            residual[c] -= alpha * auxiliary[c];
+            zirconium[c] = residual[c] * (diagonal[c] * (2.0 - omega) / omega);
+            z_r_new += zirconium[c] * residual[c];
+        }
+        const double beta = z_r_new / z_r;
+        z_r = z_r_new;
+        #pragma omp parallel for
+        for (int c = 0; c < N; c++) {
+            if (diagonal[c] == 0.0) continue;
+            direction[c] = zirconium[c] + beta * direction[c];
+        }
+        K++;
+    }
+    free(direction); free(zirconium); free(technical); free(auxiliary);
+    return K;
+}
+
+/* solver/sparsesolver.cpp:1338-1645, multicolor SSOR-PCG with Eisenstat's trick; returns K.
+ * As in the reference, the column guard diagonal[col] != 0 applies in the restart only. */
+int oracle_cg_eisenstat_rainbow(int N, double* x, const double* b, const int* A, const int* C, const double* V,
+                                double* residual, double precision, int print_modulo,
+                                const double* diagonal, double omega,
+                                int num_colors, const int* F, const int* B, const int* R)
+{
+    (void)print_modulo;
+    double tolerance = 0.0;                                   /* :1367-1370 */
+    for (int i = 0; i < N; i++) tolerance += b[i] * b[i];
+    tolerance = precision * sqrt(tolerance);
+    tolerance = dmax(tolerance, ORACLE_DESIRED_PRECISION);
+
+    double* direction = nan_vector(N);                        /* :1383-1394 */
+    double* zirconium = nan_vector(N);
+    double* technical = nan_vector(N);
+    double* auxiliary = nan_vector(N);
+    if (!direction || !zirconium || !technical || !auxiliary) {
+        free(direction); free(zirconium); free(technical); free(auxiliary); return -1;
+    }
+    double z_r = NAN;
+    int K = 0;
+    while (K < N) {
+        if (K == 0) {                                         /* :1409-1478 */
+            #pragma omp parallel for
+            for (int c = 0; c < N; c++) {
+                if (diagonal[c] == 0.0) continue;
+                double aux = b[c];
+                for (int d = A[c]; d < A[c + 1]; d++)
+                    if (diagonal[C[d]] != 0.0) aux -= V[d] * x[C[d]];
+                auxiliary[c] = aux;
+            }
+            for (int color = 0; color < num_colors; color++) {
+                #pragma omp parallel for
+                for (int i = B[color]; i < B[color + 1]; i++) {
+                    const int c = R[i];
+                    if (diagonal[c] == 0.0) continue;
+                    double aux = auxiliary[c];
+                    for (int d = A[c]; d < A[c + 1]; d++)
+                        if (F[C[d]] < F[c] && diagonal[C[d]] != 0.0) aux -= V[d] * residual[C[d]];
+                    residual[c] = aux * omega / diagonal[c];
+                }
+            }
+            z_r = 0.0;
+            #pragma omp parallel for reduction(+:z_r)
+            for (int c = 0; c < N; c++) {
+                if (diagonal[c] == 0.0) continue;
+                zirconium[c] = residual[c] * diagonal[c] * (2.0 - omega) / omega;
+                direction[c] = zirconium[c];
+                z_r += zirconium[c] * residual[c];
+            }
+        }
+        if (fabs(z_r) < tolerance * tolerance) break;        /* :1495-1498 */
+
+        double d_Ad = 0.0;                                    /* :1506-1574 */
+        for (int color = num_colors - 1; color >= 0; color--) {
+            #pragma omp parallel for
+            for (int i = B[color]; i < B[color + 1]; i++) {
+                const int c = R[i];
+                if (diagonal[c] == 0.0) continue;
+                double aux = direction[c];
+                for (int d = A[c]; d < A[c + 1]; d++)
+                    if (F[C[d]] > F[c]) aux -= V[d] * technical[C[d]];
+                technical[c] = aux * omega / diagonal[c];
+            }
+        }
+        for (int color = 0; color < num_colors; color++) {
+            #pragma omp parallel for
+            for (int i = B[color]; i < B[color + 1]; i++) {
+                const int c = R[i];
+                if (diagonal[c] == 0.0) continue;
+                double aux = direction[c] - (2.0 / omega - 1.0) * diagonal[c] * technical[c];
+                for (int d = A[c]; d < A[c + 1]; d++)
+                    if (F[C[d]] < F[c]) aux -= V[d] * auxiliary[C[d]];
+                auxiliary[c] = aux * omega / diagonal[c];
+            }
+        }
+        #pragma omp parallel for reduction(+:d_Ad)
+        for (int c = 0; c < N; c++) {
+            if (diagonal[c] == 0.0) continue;
+            auxiliary[c] += technical[c];
+            d_Ad += auxiliary[c] * direction[c];
+        }
+        int numerator_bad = !isfinite(z_r) || z_r < 0.0;      /* :1578-1593 */
+        int denominator_bad = !isfinite(d_Ad) || d_Ad < 0.0;
+        int denominator_small = sqrt(fabs(d_Ad)) < ORACLE_MACHINE_EPSILON;
+        if (numerator_bad || denominator_bad) break;
+        if (denominator_small) break;
+
+        const double alpha = z_r / d_Ad;                      /* :1596-1629 */
+        double z_r_new = 0.0;
+        #pragma omp parallel for reduction(+:z_r_new)
+        for (int c = 0; c < N; c++) {
+            if (diagonal[c] == 0.0) continue;
+            x[c] += alpha * technical[c];
+            residual[c] -= alpha * auxiliary[c];
+            zirconium[c] = residual[c] * (diagonal[c] * (2.0 - omega) / omega);
+            z_r_new += zirconium[c] * residual[c];
+        }
+        const double beta = z_r_new / z_r;
+        z_r = z_r_new;
+        #pragma omp parallel for
+        for (int c = 0; c < N; c++) {
+            if (diagonal[c] == 0.0) continue;
+            direction[c] = zirconium[c] + beta * direction[c];
+        }
+        K++;
+    }
+    free(direction); free(zirconium); free(technical); free(auxiliary);
+    return K;
+}
+
 /* Number of OpenMP threads the oracle would use (1 without OpenMP). */
 int oracle_max_threads(void)
 {

@@ -44,6 +44,8 @@ def lib():
         L.oracle_cg.argtypes = [ctypes.c_int, _f64p, _f64p, _i32p, _i32p, _f64p, _f64p, ctypes.c_double, ctypes.c_int]
         L.oracle_cg_ssor.argtypes = L.oracle_cg.argtypes + [_f64p, ctypes.c_double]
         L.oracle_cg_rainbow.argtypes = L.oracle_cg_ssor.argtypes + [ctypes.c_int, _i32p, _i32p, _i32p]
+        L.oracle_cg_ssor_eisenstat.argtypes = L.oracle_cg_ssor.argtypes
+        L.oracle_cg_eisenstat_rainbow.argtypes = L.oracle_cg_rainbow.argtypes
         L.oracle_max_threads.restype = ctypes.c_int
         L.oracle_set_threads.argtypes = [ctypes.c_int]
         _lib = L
@@ -105,4 +107,25 @@ def cg_rainbow(A, C, V, b, diag, rb, omega=1.0, x0=None, precision=1e-10):
                                 np.ascontiguousarray(diag, np.float64), float(omega), int(nc),
                                 np.ascontiguousarray(F, np.int32), np.ascontiguousarray(B, np.int32),
                                 np.ascontiguousarray(R, np.int32))
+    return K, x, res
+
+
+def cg_ssor_eisenstat(A, C, V, b, diag, omega=1.0, x0=None, precision=1e-10):
+    n = len(A) - 1
+    x = np.zeros(n) if x0 is None else np.array(x0, np.float64)
+    res = np.array(b, np.float64)
+    K = lib().oracle_cg_ssor_eisenstat(n, x, np.ascontiguousarray(b, np.float64), A, C, V, res, float(precision),
+                                       -3, np.ascontiguousarray(diag, np.float64), float(omega))
+    return K, x, res
+
+
+def cg_eisenstat_rainbow(A, C, V, b, diag, rb, omega=1.0, x0=None, precision=1e-10):
+    n = len(A) - 1
+    nc, F, B, R = rb
+    x = np.zeros(n) if x0 is None else np.array(x0, np.float64)
+    res = np.array(b, np.float64)
+    K = lib().oracle_cg_eisenstat_rainbow(n, x, np.ascontiguousarray(b, np.float64), A, C, V, res, float(precision),
+                                          -3, np.ascontiguousarray(diag, np.float64), float(omega), int(nc),
+                                          np.ascontiguousarray(F, np.int32), np.ascontiguousarray(B, np.int32),
+                                          np.ascontiguousarray(R, np.int32))
     return K, x, res

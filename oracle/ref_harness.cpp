@@ -14,8 +14,8 @@
 //       the broken scalar mass cell by cell with a log-uniform [0.1,10] factor
 //       hashed from the cell position (cell_coefficient below).
 //       Writes the CSR plus the position of every global degree of freedom.
-//   solve <cg|ssor|rainbow> <in.csr> <in.vec b> <in.vec x0> <precision> <omega> <out.sol>
-//       Calls ConjugateGradientSolverCSR{,_SSOR,_Rainbow} (solver/sparsesolver.hpp)
+//   solve <cg|ssor|rainbow|eisenstat|eisenstat_rainbow> <in.csr> <in.vec b> <in.vec x0> <precision> <omega> <out.sol>
+//       Calls ConjugateGradientSolverCSR{,_SSOR,_Rainbow,_SSOR_Eisenstat,_Eisenstat_Rainbow} (solver/sparsesolver.hpp)
 //       with print_modulo = -3; writes K, x, residual, solve seconds.
 //   rainbow <in.csr> <out.rb>        Rainbow(A) (sparse/rainbow.cpp:14-130)
 //   apply <in.csr> <in.vec> <scaling> <out.vec>   MatrixCSR::apply (sparse/matcsr.cpp:216-244)
@@ -209,6 +209,18 @@ int main(int argc, char** argv) {
             auto t0 = std::chrono::steady_clock::now();
             K = ConjugateGradientSolverCSR_Rainbow((int)m.n, x.data(), b.data(), mat.getA(), mat.getC(), mat.getV(), res.data(), precision, -3, diag.raw(), omega,
                                                    rb.num_colors, rb.F.data(), rb.B.data(), rb.R.data());
+            secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        } else if (kind == "eisenstat") {
+            FloatVector diag = mat.getDiagonal();
+            auto t0 = std::chrono::steady_clock::now();
+            K = ConjugateGradientSolverCSR_SSOR_Eisenstat((int)m.n, x.data(), b.data(), mat.getA(), mat.getC(), mat.getV(), res.data(), precision, -3, diag.raw(), omega);
+            secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        } else if (kind == "eisenstat_rainbow") {
+            FloatVector diag = mat.getDiagonal();
+            Rainbow rb(mat);
+            auto t0 = std::chrono::steady_clock::now();
+            K = ConjugateGradientSolverCSR_Eisenstat_Rainbow((int)m.n, x.data(), b.data(), mat.getA(), mat.getC(), mat.getV(), res.data(), precision, -3, diag.raw(), omega,
+                                                             rb.num_colors, rb.F.data(), rb.B.data(), rb.R.data());
             secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
         } else die("unknown solver kind");
         FILE* f = std::fopen(argv[8], "wb"); if (!f) die("cannot write sol");

@@ -11,7 +11,8 @@ compressed ``.npz`` holding:
 * ``MatrixCSR::getDiagonal`` (``diag``) and ``MatrixCSR::apply`` of ``b`` with scaling
   0.7 (``apply_out``);
 * ``Rainbow(A)``: ``rb_nc``, ``rb_F``, ``rb_B``, ``rb_R``;
-* for each solver ``cg``, ``ssor``, ``rainbow`` (and ``ssor13``/``rainbow13`` at
+* for each solver ``cg``, ``ssor``, ``rainbow``, ``eis`` (SSOR-Eisenstat), ``eisrb``
+  (Eisenstat-Rainbow) (and ``ssor13``/``rainbow13``/``eis13``/``eisrb13`` at
   omega = 1.3 where listed): the returned iteration count ``<s>_K``, the solution
   ``<s>_x`` and the residual array ``<s>_res`` written by the reference, at one
   OpenMP thread (the plain CG is only correct there).
@@ -107,10 +108,12 @@ def main():
             run("rainbow", t("m.csr"), t("rb.rb"))
             nc, F, B, R = csrio.read_rainbow(t("rb.rb"))
             out.update(rb_nc=np.int64(nc), rb_F=F, rb_B=B, rb_R=R)
-            solves = [("cg", "cg", 1.0), ("ssor", "ssor", 1.0), ("rainbow", "rainbow", 1.0)]
+            solves = [("cg", "cg", 1.0), ("ssor", "ssor", 1.0), ("rainbow", "rainbow", 1.0),
+                      ("eis", "eisenstat", 1.0), ("eisrb", "eisenstat_rainbow", 1.0)]
             for om in omegas:
                 tag = str(om).replace(".", "")
-                solves += [(f"ssor{tag}", "ssor", om), (f"rainbow{tag}", "rainbow", om)]
+                solves += [(f"ssor{tag}", "ssor", om), (f"rainbow{tag}", "rainbow", om),
+                           (f"eis{tag}", "eisenstat", om), (f"eisrb{tag}", "eisenstat_rainbow", om)]
             for key, kind, om in solves:
                 run("solve", kind, t("m.csr"), t("b.vec"), t("x0.vec"), repr(PRECISION), repr(om), t("s.sol"))
                 K, x, res, _ = csrio.read_sol(t("s.sol"))
@@ -118,8 +121,8 @@ def main():
                 out[f"{key}_omega"] = np.float64(om)
             out["precision"] = np.float64(PRECISION)
             np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **out)
-            print(f"{name}: N={m.n} nnz={m.nnz} colors={nc} K(cg/ssor/rainbow)="
-                  f"{out['cg_K']}/{out['ssor_K']}/{out['rainbow_K']}")
+            print(f"{name}: N={m.n} nnz={m.nnz} colors={nc} K(cg/ssor/rainbow/eis/eisrb)="
+                  f"{out['cg_K']}/{out['ssor_K']}/{out['rainbow_K']}/{out['eis_K']}/{out['eisrb_K']}")
 
 
 if __name__ == "__main__":

@@ -69,7 +69,7 @@ def _run_dropin(g, key):
 def test_dropin_solvers_match_reference(cuda, name):
     g = load_golden(name)
     xs, M = exact_solution(g)
-    keys = [k[:-2] for k in g if k.endswith("_K")]
+    keys = [k[:-2] for k in g if k.endswith("_K") and not k.startswith("eis")]
     for key in keys:
         K, x, res, info = _run_dropin(g, key)
         K_ref = int(g[key + "_K"])

@@ -2,7 +2,8 @@
 outputs stored in tests/golden (written by tests/golden/make_golden.py from the
 compiled reference). At one OpenMP thread the restatement must reproduce the
 reference bit for bit: iteration counts, solutions, residual arrays, SpMV,
-diagonal and the Rainbow ordering."""
+diagonal and the Rainbow ordering, for all five CG drivers (plain, SSOR, Rainbow,
+SSOR-Eisenstat, Eisenstat-Rainbow)."""
 import numpy as np
 import pytest
 
@@ -42,6 +43,10 @@ def test_oracle_solvers_bitexact(O, name):
             K, x, r = O.cg(A, C, V, b, precision=prec)
         elif key.startswith("ssor"):
             K, x, r = O.cg_ssor(A, C, V, b, diag, om, precision=prec)
+        elif key.startswith("eisrb"):
+            K, x, r = O.cg_eisenstat_rainbow(A, C, V, b, diag, rb, om, precision=prec)
+        elif key.startswith("eis"):
+            K, x, r = O.cg_ssor_eisenstat(A, C, V, b, diag, om, precision=prec)
         else:
             K, x, r = O.cg_rainbow(A, C, V, b, diag, rb, om, precision=prec)
         assert K == int(g[key + "_K"]), key
