@@ -38,7 +38,11 @@ typedef enum feec_status {
 enum {
     FEEC_METHOD_CG = 0,        /* ConjugateGradientSolverCSR          (sparsesolver.cpp:26-201)   */
     FEEC_METHOD_SSOR = 1,      /* ConjugateGradientSolverCSR_SSOR     (sparsesolver.cpp:446-724)  */
-    FEEC_METHOD_RAINBOW = 2    /* ConjugateGradientSolverCSR_Rainbow  (sparsesolver.cpp:1002-1335) */
+    FEEC_METHOD_RAINBOW = 2,   /* ConjugateGradientSolverCSR_Rainbow  (sparsesolver.cpp:1002-1335) */
+    FEEC_METHOD_SSOR_EISENSTAT = 3,    /* ConjugateGradientSolverCSR_SSOR_Eisenstat (sparsesolver.cpp:726-995);
+                                          needs feec_system_set_ssor; FEEC_MODE_REFERENCE only     */
+    FEEC_METHOD_RAINBOW_EISENSTAT = 4  /* ConjugateGradientSolverCSR_Eisenstat_Rainbow (sparsesolver.cpp:1338-1645);
+                                          needs feec_system_set_rainbow; FEEC_MODE_REFERENCE only  */
 };
 
 /* Arithmetic / stopping modes for feec_system_solve. */
@@ -94,6 +98,24 @@ int feec_cg_csr_rainbow(int N, double* x, const double* b,
                         const double* diagonal, double omega,
                         int num_colors, const int* F, const int* B, const int* R,
                         feec_solve_info* info);
+
+/* Replaces ConjugateGradientSolverCSR_SSOR_Eisenstat, solver/sparsesolver.hpp:46-56
+ * (sparsesolver.cpp:726-995). As in the reference, `residual` receives the residual of
+ * the L-solved system the iteration works on. */
+int feec_cg_csr_ssor_eisenstat(int N, double* x, const double* b,
+                               const int* A, const int* C, const double* V,
+                               double* residual, double precision, int print_modulo,
+                               const double* diagonal, double omega,
+                               feec_solve_info* info);
+
+/* Replaces ConjugateGradientSolverCSR_Eisenstat_Rainbow, solver/sparsesolver.hpp:73-84
+ * (sparsesolver.cpp:1338-1645). */
+int feec_cg_csr_eisenstat_rainbow(int N, double* x, const double* b,
+                                  const int* A, const int* C, const double* V,
+                                  double* residual, double precision, int print_modulo,
+                                  const double* diagonal, double omega,
+                                  int num_colors, const int* F, const int* B, const int* R,
+                                  feec_solve_info* info);
 
 /* Replaces MatrixCSR::apply(dest, src, scaling), sparse/matcsr.cpp:216-244:
  * dest = scaling * A * src (rows x cols matrix, host pointers). */

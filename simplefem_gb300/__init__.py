@@ -1,13 +1,14 @@
 """GB300-native sparse-CSR Krylov path of FEEC++ (martinlicht/simplefem).
 
 CSR SpMV, the ConjugateGradientSolverCSR drivers (plain, SSOR, multicolor
-"Rainbow" SSOR) and the Rainbow coloring, as hand-written sm_103a kernels behind
+"Rainbow" SSOR, and both with Eisenstat's trick) and the Rainbow coloring, as hand-written sm_103a kernels behind
 the C ABI of ``include/feec_gpu.h``. This package is the Python host side of that
 ABI; it mirrors the reference's MatrixCSR / Rainbow / raw-pointer solver surface.
 """
 from ._native import FeecError, FeecSolveInfo  # noqa: F401
-from .solver import (ConjugateGradientSolverCSR, ConjugateGradientSolverCSR_Rainbow,  # noqa: F401
-                     ConjugateGradientSolverCSR_SSOR, last_info)
+from .solver import (ConjugateGradientSolverCSR, ConjugateGradientSolverCSR_Eisenstat_Rainbow,  # noqa: F401
+                     ConjugateGradientSolverCSR_Rainbow, ConjugateGradientSolverCSR_SSOR,
+                     ConjugateGradientSolverCSR_SSOR_Eisenstat, last_info)
 from .sparse import FloatVector, MatrixCSR, Rainbow  # noqa: F401
 
 # Constants of base/base.hpp:121-131 (Float = double)
@@ -15,4 +16,5 @@ machine_epsilon = 2.220446049250313080847263336181640625e-16
 desired_precision = 1.490116119384765625e-08
 
 __all__ = ["MatrixCSR", "Rainbow", "FloatVector", "ConjugateGradientSolverCSR", "ConjugateGradientSolverCSR_SSOR",
-           "ConjugateGradientSolverCSR_Rainbow", "last_info", "FeecError", "machine_epsilon", "desired_precision"]
+           "ConjugateGradientSolverCSR_Rainbow", "ConjugateGradientSolverCSR_SSOR_Eisenstat",
+           "ConjugateGradientSolverCSR_Eisenstat_Rainbow", "last_info", "FeecError", "machine_epsilon", "desired_precision"]

@@ -172,6 +172,8 @@ const char* method_title(int method) {
     switch (method) {
         case FEEC_METHOD_SSOR: return "Conjugate Gradient CSR (SSOR)";
         case FEEC_METHOD_RAINBOW: return "Conjugate Gradient CSR (SSOR-Rainbow)";
+        case FEEC_METHOD_SSOR_EISENSTAT: return "Conjugate Gradient CSR (SSOR-Eisenstat)";
+        case FEEC_METHOD_RAINBOW_EISENSTAT: return "Conjugate Gradient CSR (SSOR-Rainbow-Eisenstat)";
         default: return "Conjugate Gradient CSR";
     }
 }
@@ -182,7 +184,12 @@ const char* method_title(int method) {
 int solve_core(feec_system* s, int method, int mode, double* xx, const double* bb, double* res, double precision,
                int max_iter, double tol_override, int print_modulo, feec_solve_info* info) {
     const int n = s->n;
-    if (method != FEEC_METHOD_CG && s->prepared != method) return FEEC_BADARG;
+    const bool eisenstat = method == FEEC_METHOD_SSOR_EISENSTAT || method == FEEC_METHOD_RAINBOW_EISENSTAT;
+    // the layout a method sweeps over: the Eisenstat variants use the SSOR / Rainbow ones
+    const int layout = method == FEEC_METHOD_SSOR_EISENSTAT ? FEEC_METHOD_SSOR
+                     : method == FEEC_METHOD_RAINBOW_EISENSTAT ? FEEC_METHOD_RAINBOW : method;
+    if (method != FEEC_METHOD_CG && s->prepared != layout) return FEEC_BADARG;
+    if (eisenstat && mode != FEEC_MODE_REFERENCE) return FEEC_BADARG;
     int st = ensure_work(s);
     if (st != FEEC_OK) return st;
     if (max_iter <= 0) max_iter = n;
@@ -255,6 +262,29 @@ int solve_core(feec_system* s, int method, int mode, double* xx, const double* b
                 FEEC_TRY(reset_status(s));
                 FEEC_TRY(cudaEventRecord(s->ev0, s->stream));
                 FEEC_TRY(launch_cg<double>(a, shape, s->stream));
+                FEEC_TRY(cudaEventRecord(s->ev1, s->stream));
+                FEEC_TRY(cudaEventSynchronize(s->ev1));
+                FEEC_TRY(cudaEventElapsedTime(&ms, s->ev0, s->ev1));
+            } else if (eisenstat) {
+                if (!s->w) {
+                    HomeStreamScope home(s);
+                    FEEC_TRY(s->work.alloc(s->w, (size_t)n));
+                }
+                // the reference starts its work vectors as NaN (sparsesolver.cpp:766-773,
+                // 1383-1394); rows the sweeps skip (D == 0) keep that value
+                for (double* v : {s->d, s->z, s->m, s->q, s->w})
+                    FEEC_TRY(cudaMemsetAsync(v, 0xFF, sizeof(double) * n, s->stream));
+                PcgArgs<double> a = make_pcg_args<double>(s, s->x, s->r, s->d, s->z, s->m, s->q, s->b, s->val, s->wd, s->sd);
+                a.dg = s->diag; a.w = s->w;
+                a.guard_restart = s->zero_diag_rows > 0;
+                a.guard_iter = method == FEEC_METHOD_SSOR_EISENSTAT && s->zero_diag_rows > 0;
+                a.tol2 = tolerance * tolerance;
+                a.use_zr_rule = 1;
+                a.max_iter = max_iter - (K_total - k0);
+                a.print_modulo = print_modulo; a.print_tol = tolerance;
+                FEEC_TRY(reset_status(s));
+                FEEC_TRY(cudaEventRecord(s->ev0, s->stream));
+                FEEC_TRY(launch_eisenstat(a, shape, s->stream));
                 FEEC_TRY(cudaEventRecord(s->ev1, s->stream));
                 FEEC_TRY(cudaEventSynchronize(s->ev1));
                 FEEC_TRY(cudaEventElapsedTime(&ms, s->ev0, s->ev1));
@@ -428,6 +458,12 @@ int build_layout(feec_system* s, int method, const double* diag_dev, double omeg
     FEEC_TRY(launch_cast_f64_f32((size_t)n, s->diag, s->diag32, st));
     FEEC_TRY(launch_sweep_factors(n, s->diag, omega, s->wd, s->sd, s->wd32, s->sd32, st));
     tmp.release();
+    {
+        std::vector<double> dh((size_t)n);
+        FEEC_TRY(cudaMemcpyAsync(dh.data(), s->diag, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+        FEEC_TRY(cudaStreamSynchronize(st));
+        s->zero_diag_rows = (int)std::count(dh.begin(), dh.end(), 0.0);
+    }
     FEEC_TRY(cudaStreamSynchronize(st));
     s->nf = (int)fptr.size() - 1;
     s->nbw = (int)bptr.size() - 1;
@@ -637,7 +673,7 @@ int feec_system_solve(feec_system* s, int method, int mode, double* x, const dou
                       double precision, int max_iter, feec_solve_info* info, void* stream) {
     zero_info(info);
     if (!s || !x || !b || !(precision > 0.0)) return FEEC_BADARG;
-    if (method < FEEC_METHOD_CG || method > FEEC_METHOD_RAINBOW || mode < FEEC_MODE_REFERENCE || mode > FEEC_MODE_MIXED)
+    if (method < FEEC_METHOD_CG || method > FEEC_METHOD_RAINBOW_EISENSTAT || mode < FEEC_MODE_REFERENCE || mode > FEEC_MODE_MIXED)
         return FEEC_BADARG;
     cudaStream_t keep = s->stream;
     if (stream) s->stream = (cudaStream_t)stream;
@@ -690,8 +726,9 @@ static int dropin_solve(int method, int N, double* x, const double* b, const int
     zero_info(info);
     // the reference asserts these (sparsesolver.cpp:32-43, 1013-1027)
     if (N <= 0 || !x || !b || !A || !C || !V || !residual || !(precision > 0.0)) return FEEC_BADARG;
+    const bool rb = method == FEEC_METHOD_RAINBOW || method == FEEC_METHOD_RAINBOW_EISENSTAT;
     if (method != FEEC_METHOD_CG && !diagonal) return FEEC_BADARG;
-    if (method == FEEC_METHOD_RAINBOW && (num_colors < 0 || !F || !B || !R)) return FEEC_BADARG;
+    if (rb && (num_colors < 0 || !F || !B || !R)) return FEEC_BADARG;
     const auto t0 = std::chrono::steady_clock::now();
     const double tolerance = host_tolerance(N, b, precision);
     if (print_modulo >= -1) std::printf("(%d/%d)     BEGIN: %s\n", 0, N, method_title(method));
@@ -699,8 +736,8 @@ static int dropin_solve(int method, int N, double* x, const double* b, const int
     feec_system* s = nullptr;
     int st = feec_system_create(&s, N, A, C, V, 1, nullptr);
     if (st != FEEC_OK) return st;
-    if (method == FEEC_METHOD_RAINBOW) st = feec_system_set_rainbow(s, diagonal, omega, num_colors, F, B, R, 1);
-    else if (method == FEEC_METHOD_SSOR) st = feec_system_set_ssor(s, diagonal, omega, 1);
+    if (rb) st = feec_system_set_rainbow(s, diagonal, omega, num_colors, F, B, R, 1);
+    else if (method != FEEC_METHOD_CG) st = feec_system_set_ssor(s, diagonal, omega, 1);
     double *dx = nullptr, *db = nullptr, *dr = nullptr;
     DevArena io; io.stream = s->stream;
     if (st == FEEC_OK) {
@@ -755,6 +792,21 @@ int feec_cg_csr_rainbow(int N, double* x, const double* b, const int* A, const i
                         int num_colors, const int* F, const int* B, const int* R, feec_solve_info* info) {
     return dropin_solve(FEEC_METHOD_RAINBOW, N, x, b, A, C, V, residual, precision, print_modulo, diagonal, omega,
                         num_colors, F, B, R, info);
+}
+
+int feec_cg_csr_ssor_eisenstat(int N, double* x, const double* b, const int* A, const int* C, const double* V,
+                               double* residual, double precision, int print_modulo, const double* diagonal,
+                               double omega, feec_solve_info* info) {
+    return dropin_solve(FEEC_METHOD_SSOR_EISENSTAT, N, x, b, A, C, V, residual, precision, print_modulo, diagonal,
+                        omega, 0, nullptr, nullptr, nullptr, info);
+}
+
+int feec_cg_csr_eisenstat_rainbow(int N, double* x, const double* b, const int* A, const int* C, const double* V,
+                                  double* residual, double precision, int print_modulo, const double* diagonal,
+                                  double omega, int num_colors, const int* F, const int* B, const int* R,
+                                  feec_solve_info* info) {
+    return dropin_solve(FEEC_METHOD_RAINBOW_EISENSTAT, N, x, b, A, C, V, residual, precision, print_modulo, diagonal,
+                        omega, num_colors, F, B, R, info);
 }
 
 int feec_csr_apply(int rows, int cols, const int* A, const int* C, const double* V, const double* src, double* dest,

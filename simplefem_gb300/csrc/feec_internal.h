@@ -51,6 +51,11 @@ struct PcgArgs {
     double print_tol;
     double* partials;    // >= 3 * gridDim.x doubles
     DeviceStatus* st;
+    // Eisenstat variants only
+    const T* dg;         // the diagonal D, permuted like the rows
+    T* w;                // the sweeps' combined vector (auxiliary + technical)
+    int guard_restart;   // skip entries whose column has D == 0 in the restart sweeps
+    int guard_iter;      // ... and in the iteration sweeps (index-order variant)
 };
 
 struct LaunchShape {
@@ -62,6 +67,8 @@ struct LaunchShape {
 // Kernel launchers (kernels_krylov.cu). Return the CUDA error of the launch.
 template <typename T> cudaError_t launch_cg(const CgArgs<T>& a, LaunchShape& shape, cudaStream_t s);
 template <typename T> cudaError_t launch_pcg(const PcgArgs<T>& a, LaunchShape& shape, cudaStream_t s);
+// SSOR-PCG with Eisenstat's trick over the same phase schedules (kernels_eisenstat.cu).
+cudaError_t launch_eisenstat(const PcgArgs<double>& a, LaunchShape& shape, cudaStream_t s);
 // Largest co-resident grid for the given kernel family and lane count.
 int max_coresident_blocks(int family, int is_float, int lanes, int threads);
 int pick_lanes(double avg_nnz_per_row);

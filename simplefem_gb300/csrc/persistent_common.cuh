@@ -1,0 +1,57 @@
+// Building blocks shared by the persistent (one cooperative launch per solve) Krylov
+// kernels: row-group iteration, lane-split segment dot products, per-block partial
+// sums and the status epilogue.
+#pragma once
+#include "feec_device.cuh"
+#include "feec_internal.h"
+
+namespace feec {
+
+constexpr int kThreads = 512;
+constexpr double kMachineEpsilon = 2.220446049250313080847263336181640625e-16;  // base/base.hpp:123
+
+// Iterate rows [lo, hi) with LANES lanes per row; the loop trip count is
+// uniform across each warp so the shuffles inside `body` see all 32 lanes.
+#define FEEC_FOR_ROW_GROUPS(lo, hi, row, active)                                                   \
+    for (int _base = (lo) + (int)((blockIdx.x * blockDim.x + threadIdx.x) / 32) * (32 / LANES);    \
+         _base < (hi); _base += (int)(gridDim.x * blockDim.x / 32) * (32 / LANES))                  \
+        for (int row = _base + (int)((threadIdx.x & 31) / LANES), _once = 1; _once; _once = 0)      \
+            for (bool active = row < (hi); _once; _once = 0)
+
+template <typename T, int LANES>
+__device__ __forceinline__ T seg_dot(const int* __restrict__ ci, const T* __restrict__ v, const T* x, int lo, int hi,
+                                     int lane) {
+    T s = T(0);
+    for (int j = lo + lane; j < hi; j += LANES) s = fma(__ldg(&v[j]), x[__ldg(&ci[j])], s);
+    #pragma unroll
+    for (int off = LANES / 2; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off, LANES);
+    return s;
+}
+
+template <typename T>
+__device__ __forceinline__ void write_partials(double* dst, typename AccT<T>::type v0) {
+    typename AccT<T>::type v[1] = {v0};
+    block_reduce<T, 1>(v);
+    if (threadIdx.x == 0) dst[blockIdx.x] = AccT<T>::value(v[0]);
+}
+
+template <typename T>
+__device__ __forceinline__ void write_partials2(double* dst, typename AccT<T>::type v0, typename AccT<T>::type v1) {
+    typename AccT<T>::type v[2] = {v0, v1};
+    block_reduce<T, 2>(v);
+    if (threadIdx.x == 0) {
+        dst[2 * blockIdx.x + 0] = AccT<T>::value(v[0]);
+        dst[2 * blockIdx.x + 1] = AccT<T>::value(v[1]);
+    }
+}
+
+__device__ __forceinline__ void finish(DeviceStatus* st, int status, int K, double fv, double av) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        atomicCAS(&st->status, FEEC_OK, status);
+        st->iterations = K;
+        st->final_value = fv;
+        st->aux_value = av;
+    }
+}
+
+}  // namespace feec

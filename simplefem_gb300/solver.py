@@ -78,3 +78,29 @@ def ConjugateGradientSolverCSR_Rainbow(N, x, b, csrrows, csrcolumns, csrvalues, 
                                            _vec(diagonal, "diagonal", N), float(omega), int(num_colors),
                                            _ints(F, "F"), _ints(B, "B"), _ints(R, "R"), info)
     return _finish(st, info, "ConjugateGradientSolverCSR_Rainbow")
+
+
+def ConjugateGradientSolverCSR_SSOR_Eisenstat(N, x, b, csrrows, csrcolumns, csrvalues, residual, precision,
+                                              print_modulo, diagonal, omega):
+    """GPU replacement of ConjugateGradientSolverCSR_SSOR_Eisenstat (solver/sparsesolver.cpp:726-995);
+    `residual` receives the residual of the L-solved system, as in the reference."""
+    x = _vec(x, "x", N, True); residual = _vec(residual, "residual", N, True)
+    info = _native.FeecSolveInfo()
+    st = _native.gpu().feec_cg_csr_ssor_eisenstat(int(N), x, _vec(b, "b", N), _ints(csrrows, "A"),
+                                                  _ints(csrcolumns, "C"), _vec(csrvalues, "V"), residual,
+                                                  float(precision), int(print_modulo), _vec(diagonal, "diagonal", N),
+                                                  float(omega), info)
+    return _finish(st, info, "ConjugateGradientSolverCSR_SSOR_Eisenstat")
+
+
+def ConjugateGradientSolverCSR_Eisenstat_Rainbow(N, x, b, csrrows, csrcolumns, csrvalues, residual, precision,
+                                                 print_modulo, diagonal, omega, num_colors, F, B, R):
+    """GPU replacement of ConjugateGradientSolverCSR_Eisenstat_Rainbow (solver/sparsesolver.cpp:1338-1645)."""
+    x = _vec(x, "x", N, True); residual = _vec(residual, "residual", N, True)
+    info = _native.FeecSolveInfo()
+    st = _native.gpu().feec_cg_csr_eisenstat_rainbow(int(N), x, _vec(b, "b", N), _ints(csrrows, "A"),
+                                                     _ints(csrcolumns, "C"), _vec(csrvalues, "V"), residual,
+                                                     float(precision), int(print_modulo),
+                                                     _vec(diagonal, "diagonal", N), float(omega), int(num_colors),
+                                                     _ints(F, "F"), _ints(B, "B"), _ints(R, "R"), info)
+    return _finish(st, info, "ConjugateGradientSolverCSR_Eisenstat_Rainbow")

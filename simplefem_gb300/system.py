@@ -13,7 +13,8 @@ import numpy as np
 
 from . import _native
 
-METHODS = {"cg": _native.METHOD_CG, "ssor": _native.METHOD_SSOR, "rainbow": _native.METHOD_RAINBOW}
+METHODS = {"cg": _native.METHOD_CG, "ssor": _native.METHOD_SSOR, "rainbow": _native.METHOD_RAINBOW,
+           "ssor_eisenstat": _native.METHOD_SSOR_EISENSTAT, "rainbow_eisenstat": _native.METHOD_RAINBOW_EISENSTAT}
 MODES = {"reference": _native.MODE_REFERENCE, "fp64": _native.MODE_FP64, "mixed": _native.MODE_MIXED}
 
 

@@ -43,7 +43,9 @@ def test_dropin_exports_reference_mangled_names(built):
     # C++ names of solver/sparsesolver.hpp:11-19, 33-43, 59-70 with Float = double
     for mangled in ["_Z26ConjugateGradientSolverCSRiPdPKdPKiS3_S1_S_di",
                     "_Z31ConjugateGradientSolverCSR_SSORiPdPKdPKiS3_S1_S_diS1_d",
-                    "_Z34ConjugateGradientSolverCSR_RainbowiPdPKdPKiS3_S1_S_diS1_diS3_S3_S3_"]:
+                    "_Z34ConjugateGradientSolverCSR_RainbowiPdPKdPKiS3_S1_S_diS1_diS3_S3_S3_",
+                    "_Z41ConjugateGradientSolverCSR_SSOR_EisenstatiPdPKdPKiS3_S1_S_diS1_d",
+                    "_Z44ConjugateGradientSolverCSR_Eisenstat_RainbowiPdPKdPKiS3_S1_S_diS1_diS3_S3_S3_"]:
         assert mangled in out, mangled
 
 
