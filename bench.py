@@ -593,6 +593,7 @@ def run_ours(args):
     mixed1, mixed1_i = single("rainbow", "mixed", 5, 7000)
     cg64, cg64_i = single("cg", "fp64", 3, 8000)
     rb64, rb64_i = single("rainbow", "reference", 3, 9000)
+    eis64, eis64_i = single("rainbow_eisenstat", "reference", 3, 9500)
 
     # drop-in host-pointer call (matrix uploaded inside the call, as the reference signature implies)
     b0 = workloads.uniform_vector(6000, n)
@@ -657,6 +658,8 @@ def run_ours(args):
                               "note": "plain FP64 CG on the whole GPU, stop at true relres 1e-10"},
             "fp64_rainbow_reference_rule": {"solves_per_s": rate(rb64), "ms": float(np.median(rb64)),
                                             "iterations": int(np.median([i["iterations"] for i in rb64_i]))},
+            "fp64_eisenstat_rainbow_reference_rule": {"solves_per_s": rate(eis64), "ms": float(np.median(eis64)),
+                                                      "iterations": int(np.median([i["iterations"] for i in eis64_i]))},
             "dropin_host_call_ms": 1000 * float(np.median(dropin)),
             "spmv": spmv,
             "batched_uneven": uneven,

@@ -336,13 +336,338 @@ __device__ __forceinline__ void for_slices_dot(const Team& team, const SellView&
 // the bookkeeping out of registers leaves them to the slice loops.
 template <typename T, int K>
 struct TeamControl {
-    double bnorm2[K], relres[K], stall[K], rnorm[K], eta2[K], zr[K], rr[K], rr_next[K];
+    double bnorm2[K], relres[K], stall[K], rnorm[K], eta2[K], zr[K], rr[K], rr0[K];
     int iters[K], outer[K], status[K];
     T alpha[K], beta[K], inv[K];
     int done;        // bit j: column j finished (converged, failed or absent)
     int active;      // bit j: column j still iterating in the current inner solve
     int all_done;
 };
+
+// Leader's stop test of the inner solve for the columns in `mask`: the monitored
+// quantity has fallen below eta^2 times its start value, or the iteration budget is used.
+template <typename T, int K>
+__device__ __forceinline__ int inner_active(const TeamControl<T, K>& ctl, int mask, int max_iter) {
+    int act = 0;
+    for (int j = 0; j < K; j++)
+        if ((mask >> j & 1) && !(ctl.rr[j] < ctl.eta2[j] * ctl.rr0[j]) && ctl.iters[j] < max_iter) act |= 1 << j;
+    return act;
+}
+
+// Plain CG inner solve (ConjugateGradientSolverCSR, solver/sparsesolver.cpp:26-201), K columns
+// in lockstep: q = A d, then x/r updates, then d = r + beta d. Stops on the recursive r.r.
+template <typename T, int K, typename Team>
+__device__ void inner_cg(Team& team, const SellView& S, const BatchArgs& args, TeamControl<T, K>& ctl, const T* val,
+                         const double* r64, T* r, T* d, T* q, T* c) {
+    using AT = AccT<T>;
+    using Acc = typename AT::type;
+    const int n = S.n;
+    const int lane = threadIdx.x & 31;
+    const bool leader = threadIdx.x == 0;
+    Acc arr[K];
+    #pragma unroll
+    for (int j = 0; j < K; j++) arr[j] = AT::zero();
+    {
+        T inv[K];
+        #pragma unroll
+        for (int j = 0; j < K; j++) inv[j] = ctl.inv[j];
+        for (int i = team.tid(); i < n; i += team.nthreads()) {
+            #pragma unroll
+            for (int j = 0; j < K; j++) {
+                const long long p = (long long)i * K + j;
+                const T rv = (T)(r64[p] * (double)inv[j]);
+                r[p] = rv; c[p] = T(0); d[p] = rv;
+                arr[j] = AT::add(arr[j], rv * rv);
+            }
+        }
+    }
+    {
+        double o[K];
+        team.template sum<T, K>(arr, o);
+        if (leader) {
+            for (int j = 0; j < K; j++) { ctl.zr[j] = o[j]; ctl.rr[j] = o[j]; ctl.rr0[j] = 1.0; }
+            ctl.active = inner_active<T, K>(ctl, ~ctl.done, args.max_iter);
+        }
+    }
+    __syncthreads();
+    while (ctl.active) {
+        Acc adq[K];
+        #pragma unroll
+        for (int j = 0; j < K; j++) adq[j] = AT::zero();
+        for_slices_dot<T, T, K, kBlockFull>(team, S, 0, S.nslices, val, d,
+            [&](const SliceMeta& M) {
+                RowState<T, K> p;
+                p.row = M.row0 + lane; p.act = lane < M.nrow;
+                load_row<T, K>(d, p.row, p.act, p.a);
+                return p;
+            },
+            [&](const SliceMeta&, const RowState<T, K>& p, const T (&sum)[K]) {
+                if (p.act) {
+                    #pragma unroll
+                    for (int j = 0; j < K; j++) adq[j] = AT::add(adq[j], p.a[j] * sum[j]);
+                    store_row<T, K>(q, p.row, sum);
+                }
+            });
+        {
+            double dq[K];
+            team.template sum<T, K>(adq, dq);
+            if (leader) {
+                int act = ctl.active;
+                for (int j = 0; j < K; j++) {
+                    T a = T(0);
+                    if (act >> j & 1) {
+                        const double zr = ctl.zr[j];
+                        if (!(dq[j] > 0.0) || !(zr >= 0.0) || !isfinite(dq[j]) || !isfinite(zr)) act &= ~(1 << j);
+                        else a = (T)(zr / dq[j]);
+                    }
+                    ctl.alpha[j] = a;
+                }
+                ctl.active = act;
+            }
+        }
+        __syncthreads();
+        T alpha[K];
+        #pragma unroll
+        for (int j = 0; j < K; j++) { alpha[j] = ctl.alpha[j]; arr[j] = AT::zero(); }
+        for (int i = team.tid(); i < n; i += team.nthreads())
+            #pragma unroll
+            for (int j = 0; j < K; j++) {
+                const long long p = (long long)i * K + j;
+                c[p] += alpha[j] * d[p];
+                const T rv = r[p] - alpha[j] * q[p];
+                r[p] = rv;
+                arr[j] = AT::add(arr[j], rv * rv);
+            }
+        {
+            double o[K];
+            team.template sum<T, K>(arr, o);
+            if (leader) {
+                const int was = ctl.active;
+                for (int j = 0; j < K; j++) {
+                    T b = T(0);
+                    if (was >> j & 1) {
+                        b = (T)(o[j] / ctl.zr[j]);
+                        ctl.zr[j] = o[j]; ctl.rr[j] = o[j];
+                        ctl.iters[j]++;
+                    }
+                    ctl.beta[j] = b;
+                }
+                ctl.active = inner_active<T, K>(ctl, was, args.max_iter);
+            }
+        }
+        __syncthreads();
+        {
+            T beta[K];
+            #pragma unroll
+            for (int j = 0; j < K; j++) beta[j] = ctl.beta[j];
+            for (int i = team.tid(); i < n; i += team.nthreads()) {
+                T rv[K], dv[K];
+                load_k_stream<T, K>(r + (long long)i * K, rv);
+                load_k_stream<T, K>(d + (long long)i * K, dv);
+                #pragma unroll
+                for (int j = 0; j < K; j++) dv[j] = rv[j] + beta[j] * dv[j];
+                store_row<T, K>(d, i, dv);
+            }
+        }
+        team.sync();
+    }
+}
+
+// Multicolor SSOR-PCG inner solve in Eisenstat's formulation
+// (ConjugateGradientSolverCSR_Eisenstat_Rainbow, solver/sparsesolver.cpp:1338-1645): the
+// same preconditioned iterates as the Rainbow solver (:1002-1335) in exact arithmetic, but
+// an iteration is one backward and one forward sweep over the strict parts — no SpMV
+// over full rows — so each stored entry is read and gathered once per iteration instead
+// of twice. Vectors (interleaved [row][K]): r = L-solved residual, d = direction,
+// z = S r, m = technical (backward sweep), q = auxiliary (forward sweep), c = solution.
+// With sd = D (2 - w) / w, the reference's (2/w - 1) D equals sd. The previous
+// iteration's d = z + beta d runs inside the backward sweep (a row's d is read only by
+// the row itself). Stops on z.r relative to its start value.
+template <typename T, int K, typename Team>
+__device__ void inner_eisenstat(Team& team, const SellView& S, const BatchArgs& args, TeamControl<T, K>& ctl,
+                                const T* val, const T* wd, const T* sd, const double* r64, T* r, T* d, T* z, T* m,
+                                T* q, T* c) {
+    using AT = AccT<T>;
+    using Acc = typename AT::type;
+    const int n = S.n;
+    const int lane = threadIdx.x & 31;
+    const bool leader = threadIdx.x == 0;
+    {   // restart from c = 0: auxiliary = r64 / ||r64||
+        T inv[K];
+        #pragma unroll
+        for (int j = 0; j < K; j++) inv[j] = ctl.inv[j];
+        for (int i = team.tid(); i < n; i += team.nthreads()) {
+            #pragma unroll
+            for (int j = 0; j < K; j++) {
+                const long long p = (long long)i * K + j;
+                q[p] = (T)(r64[p] * (double)inv[j]);
+                r[p] = T(0); c[p] = T(0); d[p] = T(0); z[p] = T(0); m[p] = T(0);
+            }
+        }
+    }
+    team.sync();
+    Acc azr[K];
+    #pragma unroll
+    for (int j = 0; j < K; j++) azr[j] = AT::zero();
+    for (int col = 0; col < S.ncolors; col++) {                  // L-solve of the residual, z = S r, d = z
+        for_slices_dot<T, T, K, kBlockL>(team, S, __ldg(&S.color_slice[col]), __ldg(&S.color_slice[col + 1]), val, r,
+            [&](const SliceMeta& M) {
+                RowState<T, K> p;
+                p.row = M.row0 + lane; p.act = lane < M.nrow;
+                p.w = p.act ? __ldg(&wd[p.row]) : T(0);
+                p.sdv = p.act ? __ldg(&sd[p.row]) : T(0);
+                load_row<T, K>(q, p.row, p.act, p.a);
+                return p;
+            },
+            [&](const SliceMeta&, const RowState<T, K>& p, const T (&sum)[K]) {
+                if (p.act && p.w != T(0)) {
+                    T rv[K], zv[K];
+                    #pragma unroll
+                    for (int j = 0; j < K; j++) {
+                        rv[j] = (p.a[j] - sum[j]) * p.w;
+                        zv[j] = rv[j] * p.sdv;
+                        azr[j] = AT::add(azr[j], zv[j] * rv[j]);
+                    }
+                    store_row<T, K>(r, p.row, rv);
+                    store_row<T, K>(z, p.row, zv);
+                    store_row<T, K>(d, p.row, zv);
+                }
+            });
+        team.sync();
+    }
+    {
+        double o[K];
+        team.template sum<T, K>(azr, o);
+        if (leader) {
+            for (int j = 0; j < K; j++) { ctl.zr[j] = o[j]; ctl.rr[j] = o[j]; ctl.rr0[j] = o[j] > 0.0 ? o[j] : 1.0; }
+            ctl.active = inner_active<T, K>(ctl, ~ctl.done, args.max_iter);
+        }
+    }
+    __syncthreads();
+    bool first = true;
+    while (ctl.active) {
+        {   // backward sweep: technical = (d - U technical) w / D, with d = z + beta d first
+            T beta[K];
+            #pragma unroll
+            for (int j = 0; j < K; j++) beta[j] = ctl.beta[j];
+            for (int col = S.ncolors - 1; col >= 0; col--) {
+                for_slices_dot<T, T, K, kBlockU>(team, S, __ldg(&S.color_slice[col]), __ldg(&S.color_slice[col + 1]),
+                                                 val, m,
+                    [&](const SliceMeta& M) {
+                        RowState<T, K> p;
+                        p.row = M.row0 + lane; p.act = lane < M.nrow;
+                        p.w = p.act ? __ldg(&wd[p.row]) : T(0);
+                        load_row<T, K>(d, p.row, p.act, p.a);
+                        if (!first) load_row<T, K>(z, p.row, p.act, p.b);
+                        return p;
+                    },
+                    [&](const SliceMeta&, const RowState<T, K>& p, const T (&sum)[K]) {
+                        if (p.act && p.w != T(0)) {
+                            T dv[K], mv[K];
+                            #pragma unroll
+                            for (int j = 0; j < K; j++) {
+                                dv[j] = first ? p.a[j] : p.b[j] + beta[j] * p.a[j];
+                                mv[j] = (dv[j] - sum[j]) * p.w;
+                            }
+                            if (!first) store_row<T, K>(d, p.row, dv);
+                            store_row<T, K>(m, p.row, mv);
+                        }
+                    });
+                team.sync();
+            }
+        }
+        Acc dad[K];
+        #pragma unroll
+        for (int j = 0; j < K; j++) dad[j] = AT::zero();
+        for (int col = 0; col < S.ncolors; col++) {              // forward sweep: auxiliary, d.(aux + tech)
+            for_slices_dot<T, T, K, kBlockL>(team, S, __ldg(&S.color_slice[col]), __ldg(&S.color_slice[col + 1]), val, q,
+                [&](const SliceMeta& M) {
+                    RowState<T, K> p;
+                    p.row = M.row0 + lane; p.act = lane < M.nrow;
+                    p.w = p.act ? __ldg(&wd[p.row]) : T(0);
+                    p.sdv = p.act ? __ldg(&sd[p.row]) : T(0);
+                    load_row<T, K>(d, p.row, p.act, p.a);
+                    load_row<T, K>(m, p.row, p.act, p.b);
+                    return p;
+                },
+                [&](const SliceMeta&, const RowState<T, K>& p, const T (&sum)[K]) {
+                    if (p.act && p.w != T(0)) {
+                        T av[K];
+                        #pragma unroll
+                        for (int j = 0; j < K; j++) {
+                            av[j] = (p.a[j] - p.sdv * p.b[j] - sum[j]) * p.w;
+                            dad[j] = AT::add(dad[j], (av[j] + p.b[j]) * p.a[j]);
+                        }
+                        store_row<T, K>(q, p.row, av);
+                    }
+                });
+            team.sync();
+        }
+        {
+            double dq[K];
+            team.template sum<T, K>(dad, dq);
+            if (leader) {
+                int act = ctl.active;
+                for (int j = 0; j < K; j++) {
+                    T a = T(0);
+                    if (act >> j & 1) {
+                        const double zr = ctl.zr[j];
+                        if (!(dq[j] > 0.0) || !(zr >= 0.0) || !isfinite(dq[j]) || !isfinite(zr)) act &= ~(1 << j);
+                        else a = (T)(zr / dq[j]);
+                    }
+                    ctl.alpha[j] = a;
+                }
+                ctl.active = act;
+            }
+        }
+        __syncthreads();
+        {   // update: c += alpha technical, r -= alpha (auxiliary + technical), z = S r, z.r
+            T alpha[K];
+            #pragma unroll
+            for (int j = 0; j < K; j++) { alpha[j] = ctl.alpha[j]; azr[j] = AT::zero(); }
+            for (int i = team.tid(); i < n; i += team.nthreads()) {
+                const T w = __ldg(&wd[i]);
+                if (w == T(0)) continue;
+                const T sdv = __ldg(&sd[i]);
+                T cv[K], mv[K], qv[K], rv[K], zv[K];
+                load_k_stream<T, K>(c + (long long)i * K, cv);
+                load_k_stream<T, K>(m + (long long)i * K, mv);
+                load_k_stream<T, K>(q + (long long)i * K, qv);
+                load_k_stream<T, K>(r + (long long)i * K, rv);
+                #pragma unroll
+                for (int j = 0; j < K; j++) {
+                    cv[j] += alpha[j] * mv[j];
+                    rv[j] -= alpha[j] * (qv[j] + mv[j]);
+                    zv[j] = rv[j] * sdv;
+                    azr[j] = AT::add(azr[j], zv[j] * rv[j]);
+                }
+                store_row<T, K>(c, i, cv);
+                store_row<T, K>(r, i, rv);
+                store_row<T, K>(z, i, zv);
+            }
+        }
+        {
+            double o[K];
+            team.template sum<T, K>(azr, o);
+            if (leader) {
+                const int was = ctl.active;
+                for (int j = 0; j < K; j++) {
+                    T b = T(0);
+                    if (was >> j & 1) {
+                        b = (T)(o[j] / ctl.zr[j]);
+                        ctl.zr[j] = o[j]; ctl.rr[j] = o[j];
+                        ctl.iters[j]++;
+                    }
+                    ctl.beta[j] = b;
+                }
+                ctl.active = inner_active<T, K>(ctl, was, args.max_iter);
+            }
+        }
+        __syncthreads();
+        first = false;
+        team.sync();
+    }
+}
 
 // One team solves work item `it` completely.
 template <typename T, int K, bool RAINBOW, typename Team>
@@ -445,266 +770,11 @@ __device__ void team_solve(Team& team, const BatchArgs& args, const BatchItem& i
         __syncthreads();
         if (ctl.all_done) break;
 
-        // ---- inner solve: A c = r64 / ||r64|| in T; restart with c = 0, r = rin ----
-        Acc arr[K], azr[K];
-        #pragma unroll
-        for (int j = 0; j < K; j++) { arr[j] = AT::zero(); azr[j] = AT::zero(); }
-        {
-            T inv[K];
-            #pragma unroll
-            for (int j = 0; j < K; j++) inv[j] = ctl.inv[j];
-            for (int i = team.tid(); i < n; i += team.nthreads()) {
-                #pragma unroll
-                for (int j = 0; j < K; j++) {
-                    const long long p = (long long)i * K + j;
-                    const T rv = (T)(r64[p] * (double)inv[j]);
-                    r[p] = rv; c[p] = T(0); m[p] = T(0); z[p] = T(0); q[p] = T(0);
-                    if constexpr (!RAINBOW) { d[p] = rv; azr[j] = AT::add(azr[j], rv * rv); } else { d[p] = T(0); }
-                    arr[j] = AT::add(arr[j], rv * rv);
-                }
-            }
-        }
-        team.sync();
-        if constexpr (RAINBOW) {
-            for (int col = 0; col < S.ncolors; col++) {              // forward sweep
-                for_slices_dot<T, T, K, kBlockL>(team, S, __ldg(&S.color_slice[col]), __ldg(&S.color_slice[col + 1]), val, m,
-                    [&](const SliceMeta& M) {
-                        RowState<T, K> p;
-                        p.row = M.row0 + lane; p.act = lane < M.nrow;
-                        p.w = p.act ? __ldg(&wd[p.row]) : T(0);
-                        load_row<T, K>(r, p.row, p.act, p.a);
-                        return p;
-                    },
-                    [&](const SliceMeta&, const RowState<T, K>& p, const T (&sum)[K]) {
-                        if (p.act && p.w != T(0)) {
-                            T mv[K];
-                            #pragma unroll
-                            for (int j = 0; j < K; j++) mv[j] = (p.a[j] - sum[j]) * p.w;
-                            store_row<T, K>(m, p.row, mv);
-                        }
-                    });
-                team.sync();
-            }
-            for (int col = S.ncolors - 1; col >= 0; col--) {         // scale + backward sweep
-                for_slices_dot<T, T, K, kBlockU>(team, S, __ldg(&S.color_slice[col]), __ldg(&S.color_slice[col + 1]), val, z,
-                    [&](const SliceMeta& M) {
-                        RowState<T, K> p;
-                        p.row = M.row0 + lane; p.act = lane < M.nrow;
-                        p.w = p.act ? __ldg(&wd[p.row]) : T(0);
-                        p.sdv = p.act ? __ldg(&sd[p.row]) : T(0);
-                        load_row<T, K>(m, p.row, p.act, p.a);
-                        load_row<T, K>(r, p.row, p.act, p.b);
-                        return p;
-                    },
-                    [&](const SliceMeta&, const RowState<T, K>& p, const T (&sum)[K]) {
-                        if (p.act && p.w != T(0)) {
-                            T mv[K], zv[K];
-                            #pragma unroll
-                            for (int j = 0; j < K; j++) {
-                                mv[j] = p.a[j] * p.sdv;
-                                zv[j] = (mv[j] - sum[j]) * p.w;
-                                azr[j] = AT::add(azr[j], zv[j] * p.b[j]);
-                            }
-                            store_row<T, K>(m, p.row, mv);
-                            store_row<T, K>(z, p.row, zv);
-                            store_row<T, K>(d, p.row, zv);
-                        }
-                    });
-                team.sync();
-            }
-        }
-        {
-            Acc both[2 * K];
-            #pragma unroll
-            for (int j = 0; j < K; j++) { both[j] = azr[j]; both[K + j] = arr[j]; }
-            double o[2 * K];
-            team.template sum<T, 2 * K>(both, o);
-            if (leader) {
-                int act = 0;
-                for (int j = 0; j < K; j++) {
-                    ctl.zr[j] = o[j]; ctl.rr[j] = o[K + j];
-                    if (!(ctl.done >> j & 1) && !(ctl.rr[j] < ctl.eta2[j]) && ctl.iters[j] < args.max_iter) act |= 1 << j;
-                }
-                ctl.active = act;
-            }
-        }
-        __syncthreads();
-        while (ctl.active) {
-            // q = A d (full rows), d.q
-            Acc adq[K];
-            #pragma unroll
-            for (int j = 0; j < K; j++) adq[j] = AT::zero();
-            for_slices_dot<T, T, K, kBlockFull>(team, S, 0, S.nslices, val, d,
-                [&](const SliceMeta& M) {
-                    RowState<T, K> p;
-                    p.row = M.row0 + lane; p.act = lane < M.nrow;
-                    p.w = (RAINBOW && p.act) ? __ldg(&wd[p.row]) : T(1);
-                    load_row<T, K>(d, p.row, p.act, p.a);
-                    return p;
-                },
-                [&](const SliceMeta&, const RowState<T, K>& p, const T (&sum)[K]) {
-                    if (p.act) {
-                        const bool skip = RAINBOW && p.w == T(0);
-                        T qv[K];
-                        #pragma unroll
-                        for (int j = 0; j < K; j++) {
-                            qv[j] = skip ? T(0) : sum[j];
-                            adq[j] = AT::add(adq[j], p.a[j] * qv[j]);
-                        }
-                        store_row<T, K>(q, p.row, qv);
-                    }
-                });
-            {
-                double dq[K];
-                team.template sum<T, K>(adq, dq);
-                if (leader) {
-                    int act = ctl.active;
-                    for (int j = 0; j < K; j++) {
-                        T a = T(0);
-                        if (act >> j & 1) {
-                            const double zr = ctl.zr[j];
-                            if (!(dq[j] > 0.0) || !(zr >= 0.0) || !isfinite(dq[j]) || !isfinite(zr)) act &= ~(1 << j);
-                            else a = (T)(zr / dq[j]);
-                        }
-                        ctl.alpha[j] = a;
-                    }
-                    ctl.active = act;
-                }
-            }
-            __syncthreads();
-            T alpha[K];
-            #pragma unroll
-            for (int j = 0; j < K; j++) alpha[j] = ctl.alpha[j];
-            #pragma unroll
-            for (int j = 0; j < K; j++) { arr[j] = AT::zero(); azr[j] = AT::zero(); }
-            if constexpr (RAINBOW) {
-                for (int col = 0; col < S.ncolors; col++) {
-                    for_slices_dot<T, T, K, kBlockL>(team, S, __ldg(&S.color_slice[col]), __ldg(&S.color_slice[col + 1]), val, m,
-                        [&](const SliceMeta& M) {
-                            RowState<T, K> p;
-                            p.row = M.row0 + lane; p.act = lane < M.nrow;
-                            p.w = p.act ? __ldg(&wd[p.row]) : T(0);
-                            load_row<T, K>(r, p.row, p.act, p.a);
-                            load_row<T, K>(q, p.row, p.act, p.b);
-                            return p;
-                        },
-                        [&](const SliceMeta&, const RowState<T, K>& p, const T (&sum)[K]) {
-                            if (p.act && p.w != T(0)) {
-                                T mv[K], rv[K];
-                                #pragma unroll
-                                for (int j = 0; j < K; j++) {
-                                    rv[j] = p.a[j] - alpha[j] * p.b[j];
-                                    arr[j] = AT::add(arr[j], rv[j] * rv[j]);
-                                    mv[j] = (rv[j] - sum[j]) * p.w;
-                                }
-                                store_row<T, K>(r, p.row, rv);
-                                store_row<T, K>(m, p.row, mv);
-                            }
-                        });
-                    team.sync();
-                }
-                {   // r.r now, so its accumulators are not carried through the backward sweep
-                    double o[K];
-                    team.template sum<T, K>(arr, o);
-                    if (leader)
-                        for (int j = 0; j < K; j++) ctl.rr_next[j] = o[j];
-                }
-                for (int col = S.ncolors - 1; col >= 0; col--) {
-                    for_slices_dot<T, T, K, kBlockU>(team, S, __ldg(&S.color_slice[col]), __ldg(&S.color_slice[col + 1]), val, z,
-                        [&](const SliceMeta& M) {
-                            RowState<T, K> p;
-                            p.row = M.row0 + lane; p.act = lane < M.nrow;
-                            p.w = p.act ? __ldg(&wd[p.row]) : T(0);
-                            p.sdv = p.act ? __ldg(&sd[p.row]) : T(0);
-                            load_row<T, K>(m, p.row, p.act, p.a);
-                            load_row<T, K>(r, p.row, p.act, p.b);
-                            return p;
-                        },
-                        [&](const SliceMeta&, const RowState<T, K>& p, const T (&sum)[K]) {
-                            if (p.act && p.w != T(0)) {
-                                T mv[K], zv[K];
-                                #pragma unroll
-                                for (int j = 0; j < K; j++) {
-                                    mv[j] = p.a[j] * p.sdv;
-                                    zv[j] = (mv[j] - sum[j]) * p.w;
-                                    azr[j] = AT::add(azr[j], zv[j] * p.b[j]);
-                                }
-                                store_row<T, K>(m, p.row, mv);
-                                store_row<T, K>(z, p.row, zv);
-                            }
-                        });
-                    team.sync();
-                }
-            } else {
-                for (int i = team.tid(); i < n; i += team.nthreads())
-                    #pragma unroll
-                    for (int j = 0; j < K; j++) {
-                        const long long p = (long long)i * K + j;
-                        c[p] += alpha[j] * d[p];
-                        const T rv = r[p] - alpha[j] * q[p];
-                        r[p] = rv;
-                        arr[j] = AT::add(arr[j], rv * rv);
-                        azr[j] = AT::add(azr[j], rv * rv);
-                    }
-            }
-            {
-                double o[2 * K];
-                if constexpr (RAINBOW) {
-                    double oz[K];
-                    team.template sum<T, K>(azr, oz);
-                    #pragma unroll
-                    for (int j = 0; j < K; j++) { o[j] = oz[j]; o[K + j] = ctl.rr_next[j]; }
-                } else {
-                    Acc both[2 * K];
-                    #pragma unroll
-                    for (int j = 0; j < K; j++) { both[j] = azr[j]; both[K + j] = arr[j]; }
-                    team.template sum<T, 2 * K>(both, o);
-                }
-                if (leader) {
-                    const int was = ctl.active;
-                    int act = was;
-                    for (int j = 0; j < K; j++) {
-                        T b = T(0);
-                        if (was >> j & 1) {
-                            b = (T)(o[j] / ctl.zr[j]);
-                            ctl.zr[j] = o[j];
-                            ctl.rr[j] = o[K + j];
-                            ctl.iters[j]++;
-                            if (ctl.rr[j] < ctl.eta2[j] || ctl.iters[j] >= args.max_iter) act &= ~(1 << j);
-                        }
-                        ctl.beta[j] = b;
-                    }
-                    ctl.active = act;
-                }
-            }
-            __syncthreads();
-            // Rainbow: c += alpha d (the solution update of the reference's forward sweep,
-            // moved here where d is loaded anyway); then d = z + beta d (CG: z = r). Columns
-            // that stopped have alpha = beta = 0 and their d is not read again.
-            {
-                T beta[K];
-                #pragma unroll
-                for (int j = 0; j < K; j++) beta[j] = ctl.beta[j];
-                const T* zsrc = RAINBOW ? z : r;
-                for (int i = team.tid(); i < n; i += team.nthreads()) {
-                    if (RAINBOW && __ldg(&wd[i]) == T(0)) continue;
-                    T zv[K], dv[K];
-                    load_k_stream<T, K>(zsrc + (long long)i * K, zv);
-                    load_k_stream<T, K>(d + (long long)i * K, dv);
-                    if constexpr (RAINBOW) {
-                        T cv[K];
-                        load_k_stream<T, K>(c + (long long)i * K, cv);
-                        #pragma unroll
-                        for (int j = 0; j < K; j++) cv[j] = cv[j] + alpha[j] * dv[j];
-                        store_row<T, K>(c, i, cv);
-                    }
-                    #pragma unroll
-                    for (int j = 0; j < K; j++) dv[j] = zv[j] + beta[j] * dv[j];
-                    store_row<T, K>(d, i, dv);
-                }
-            }
-            team.sync();
-        }
+        // ---- inner solve: A c = r64 / ||r64|| in T, from c = 0 ----
+        if constexpr (RAINBOW)
+            inner_eisenstat<T, K>(team, S, args, ctl, val, wd, sd, r64, r, d, z, m, q, c);
+        else
+            inner_cg<T, K>(team, S, args, ctl, val, r64, r, d, q, c);
         // x += ||r|| c in FP64 (rnorm is 0 for finished columns)
         {
             double rnorm[K];
