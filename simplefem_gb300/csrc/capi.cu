@@ -284,7 +284,32 @@ int solve_core(feec_system* s, int method, int mode, double* xx, const double* b
                 a.print_modulo = print_modulo; a.print_tol = tolerance;
                 FEEC_TRY(reset_status(s));
                 FEEC_TRY(cudaEventRecord(s->ev0, s->stream));
-                FEEC_TRY(launch_eisenstat(a, shape, s->stream));
+                FEEC_TRY(launch_eisenstat<double>(a, shape, s->stream));
+                FEEC_TRY(cudaEventRecord(s->ev1, s->stream));
+                FEEC_TRY(cudaEventSynchronize(s->ev1));
+                FEEC_TRY(cudaEventElapsedTime(&ms, s->ev0, s->ev1));
+            } else if (run_mode == FEEC_MODE_FP64) {
+                // FP64 product mode of the preconditioned solvers: Eisenstat's formulation (the
+                // same preconditioned iterates, no SpMV over full rows per iteration). It stops
+                // when z.r has fallen by (tolerance / ||b - A x||)^2; the check below confirms
+                // on the true residual and restarts from the current iterate if needed.
+                double rn2 = 0.0;
+                st = true_residual(s, s->b, s->x, s->q, rn2, permuted);
+                if (st != FEEC_OK) return st;
+                if (std::sqrt(rn2) <= tolerance) { status = FEEC_OK; final_norm = std::sqrt(rn2); break; }
+                if (!s->w) {
+                    HomeStreamScope home(s);
+                    FEEC_TRY(s->work.alloc(s->w, (size_t)n));
+                }
+                PcgArgs<double> a = make_pcg_args<double>(s, s->x, s->r, s->d, s->z, s->m, s->q, s->b, s->val, s->wd, s->sd);
+                a.dg = s->diag; a.w = s->w;
+                a.guard_restart = a.guard_iter = s->zero_diag_rows > 0;
+                a.use_zr_rule = 0;
+                a.rr_stop = tolerance * tolerance / rn2;
+                a.max_iter = max_iter - (K_total - k0);
+                FEEC_TRY(reset_status(s));
+                FEEC_TRY(cudaEventRecord(s->ev0, s->stream));
+                FEEC_TRY(launch_eisenstat<double>(a, shape, s->stream));
                 FEEC_TRY(cudaEventRecord(s->ev1, s->stream));
                 FEEC_TRY(cudaEventSynchronize(s->ev1));
                 FEEC_TRY(cudaEventElapsedTime(&ms, s->ev0, s->ev1));
@@ -309,7 +334,8 @@ int solve_core(feec_system* s, int method, int mode, double* xx, const double* b
             double rn2 = 0.0;
             st = true_residual(s, s->b, s->x, s->d, rn2, permuted);
             if (st != FEEC_OK) return st;
-            if (std::sqrt(rn2) <= tolerance) break;
+            final_norm = std::sqrt(rn2);
+            if (final_norm <= tolerance) break;
             if (K_total - k0 >= max_iter) { status = FEEC_MAXITER; break; }
         }
         return FEEC_OK;
@@ -366,12 +392,22 @@ int solve_core(feec_system* s, int method, int mode, double* xx, const double* b
                 a.partials = s->partials; a.st = s->st;
                 FEEC_TRY(launch_cg<float>(a, shape, s->stream));
             } else {
+                // The inner multicolor / index-order SSOR-PCG runs in Eisenstat's formulation:
+                // the same preconditioned iterates, but an iteration is one backward and one
+                // forward sweep over the strict parts, with no SpMV over full rows. It stops
+                // when z.r has fallen by eta^2; the FP64 outer loop checks the true residual.
+                if (!s->w32) {
+                    HomeStreamScope home(s);
+                    FEEC_TRY(s->work.alloc(s->w32, (size_t)n));
+                }
                 PcgArgs<float> a = make_pcg_args<float>(s, s->x32, s->r32, s->d32, s->z32, s->m32, s->q32, s->b32,
                                                         s->val32, s->wd32, s->sd32);
+                a.dg = s->diag32; a.w = s->w32;
+                a.guard_restart = a.guard_iter = s->zero_diag_rows > 0;
                 a.use_zr_rule = 0;
                 a.rr_stop = eta * eta;
                 a.max_iter = max_iter - K_total;
-                FEEC_TRY(launch_pcg<float>(a, shape, s->stream));
+                FEEC_TRY(launch_eisenstat<float>(a, shape, s->stream));
             }
             FEEC_TRY(cudaEventRecord(s->ev1, s->stream));
             FEEC_TRY(launch_update_x(n, nullptr, s->x32, s->scal + 3, s->x, s->stream));

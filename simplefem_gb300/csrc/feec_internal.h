@@ -44,7 +44,7 @@ struct PcgArgs {
     int nbw; const int* bptr; const int* brows;   // backward phases: rows brows[bptr[p] .. bptr[p+1])
     double omega;
     double tol2;         // reference rule: stop when |z.r| < tol2 (if use_zr_rule)
-    double rr_stop;      // stop when the recursive r.r < rr_stop (if > 0)
+    double rr_stop;      // stop when the recursive r.r < rr_stop (if > 0); Eisenstat: when z.r < rr_stop * (z.r at the start)
     int use_zr_rule;
     int max_iter;
     int print_modulo;
@@ -68,7 +68,7 @@ struct LaunchShape {
 template <typename T> cudaError_t launch_cg(const CgArgs<T>& a, LaunchShape& shape, cudaStream_t s);
 template <typename T> cudaError_t launch_pcg(const PcgArgs<T>& a, LaunchShape& shape, cudaStream_t s);
 // SSOR-PCG with Eisenstat's trick over the same phase schedules (kernels_eisenstat.cu).
-cudaError_t launch_eisenstat(const PcgArgs<double>& a, LaunchShape& shape, cudaStream_t s);
+template <typename T> cudaError_t launch_eisenstat(const PcgArgs<T>& a, LaunchShape& shape, cudaStream_t s);
 // Largest co-resident grid for the given kernel family and lane count.
 int max_coresident_blocks(int family, int is_float, int lanes, int threads);
 int pick_lanes(double avg_nnz_per_row);

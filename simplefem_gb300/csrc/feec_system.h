@@ -94,6 +94,7 @@ struct feec_system {
     bool work_ready = false;
     double *x = nullptr, *r = nullptr, *d = nullptr, *z = nullptr, *m = nullptr, *q = nullptr, *b = nullptr;
     double* w = nullptr;               // Eisenstat solvers only: auxiliary + technical
+    float* w32 = nullptr;              // ... FP32 copy for the mixed-precision inner solves
     int zero_diag_rows = 0;            // rows with D == 0 in the prepared layout (the sweeps skip them)
     float *x32 = nullptr, *r32 = nullptr, *d32 = nullptr, *z32 = nullptr, *m32 = nullptr, *q32 = nullptr, *b32 = nullptr;
     double* partials = nullptr;

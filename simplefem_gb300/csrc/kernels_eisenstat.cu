@@ -15,7 +15,9 @@
 // direction is only ever read by its own row), and auxiliary + technical and the
 // direction . (auxiliary + technical) sum run in the forward sweep, into a separate
 // vector because later colors still gather the pure auxiliary. An iteration has
-// 2 * phases + 2 grid barriers. Only FP64, like the reference's drop-in.
+// 2 * phases + 2 grid barriers. T = double is the drop-in (the reference's stopping rule);
+// T = float is the inner solve of the mixed-precision mode (stops when z.r has fallen by
+// a given factor, compensated FP32 sums).
 #include <cmath>
 #include <cstdio>
 
@@ -28,15 +30,14 @@ namespace {
 
 // seg_dot that can skip entries whose column has D == 0 (the reference's
 // `diagonal[csrcolumns[d]] != 0.` guard; wd = omega / D is 0 exactly there).
-template <int LANES>
-__device__ __forceinline__ double seg_dot_guarded(const int* __restrict__ ci, const double* __restrict__ v,
-                                                  const double* x, const double* __restrict__ wd, int lo, int hi,
-                                                  int lane, bool guard) {
-    double s = 0.0;
+template <typename T, int LANES>
+__device__ __forceinline__ T seg_dot_guarded(const int* __restrict__ ci, const T* __restrict__ v, const T* x,
+                                             const T* __restrict__ wd, int lo, int hi, int lane, bool guard) {
+    T s = T(0);
     if (guard) {
         for (int j = lo + lane; j < hi; j += LANES) {
             const int c = __ldg(&ci[j]);
-            if (__ldg(&wd[c]) != 0.0) s = fma(__ldg(&v[j]), x[c], s);
+            if (__ldg(&wd[c]) != T(0)) s = fma(__ldg(&v[j]), x[c], s);
         }
     } else {
         for (int j = lo + lane; j < hi; j += LANES) s = fma(__ldg(&v[j]), x[__ldg(&ci[j])], s);
@@ -48,9 +49,9 @@ __device__ __forceinline__ double seg_dot_guarded(const int* __restrict__ ci, co
 
 // Vectors: r = residual (of the L-solved system, as the reference keeps it),
 // d = direction, z = zirconium, m = technical, q = auxiliary, w = auxiliary + technical.
-template <int LANES>
-__global__ void __launch_bounds__(kThreads, 2) eisenstat_persistent(PcgArgs<double> a) {
-    using AT = AccT<double>;
+template <typename T, int LANES>
+__global__ void __launch_bounds__(kThreads, 2) eisenstat_persistent(PcgArgs<T> a) {
+    using AT = AccT<T>;
     using Acc = typename AT::type;
     unsigned long long epoch = 0;
     const int n = a.n;
@@ -58,7 +59,7 @@ __global__ void __launch_bounds__(kThreads, 2) eisenstat_persistent(PcgArgs<doub
     const int tid = blockIdx.x * blockDim.x + threadIdx.x;
     const int nthr = gridDim.x * blockDim.x;
     const bool g_restart = a.guard_restart != 0, g_iter = a.guard_iter != 0;
-    const double c2 = 2.0 / a.omega - 1.0;
+    const T c2 = (T)(2.0 / a.omega - 1.0);
     // two partial-sum arrays, used alternately: a block writes one only after a grid
     // barrier has passed since every block last read it
     double* p_dad = a.partials;
@@ -69,45 +70,48 @@ __global__ void __launch_bounds__(kThreads, 2) eisenstat_persistent(PcgArgs<doub
     // ---- restart (:786-842 / :1409-1478): auxiliary = b - A x, forward solve into r ----
     FEEC_FOR_ROW_GROUPS(0, n, i, act) {
         const int lo = act ? __ldg(&a.rp[i]) : 0, hi = act ? __ldg(&a.rp[i + 1]) : 0;
-        const double s = seg_dot_guarded<LANES>(a.ci, a.val, a.x, a.wd, lo, hi, lane, g_restart);
-        if (act && lane == 0 && __ldg(&a.wd[i]) != 0.0) a.q[i] = __ldg(&a.b[i]) - s;
+        const T s = seg_dot_guarded<T, LANES>(a.ci, a.val, a.x, a.wd, lo, hi, lane, g_restart);
+        if (act && lane == 0 && __ldg(&a.wd[i]) != T(0)) a.q[i] = __ldg(&a.b[i]) - s;
     }
     if (!grid_barrier(a.st, epoch, 30)) return;
     for (int p = 0; p < a.nf; p++) {
         const int lo_r = __ldg(&a.fptr[p]), hi_r = __ldg(&a.fptr[p + 1]);
         FEEC_FOR_ROW_GROUPS(lo_r, hi_r, i, act) {
             const int lo = act ? __ldg(&a.rp[i]) : 0, hi = act ? __ldg(&a.lsplit[i]) : 0;
-            const double s = seg_dot_guarded<LANES>(a.ci, a.val, a.r, a.wd, lo, hi, lane, g_restart);
+            const T s = seg_dot_guarded<T, LANES>(a.ci, a.val, a.r, a.wd, lo, hi, lane, g_restart);
             if (act && lane == 0) {
-                const double w = __ldg(&a.wd[i]);
-                if (w != 0.0) a.r[i] = (a.q[i] - s) * w;
+                const T w = __ldg(&a.wd[i]);
+                if (w != T(0)) a.r[i] = (a.q[i] - s) * w;
             }
         }
         if (!grid_barrier(a.st, epoch, 31)) return;
     }
     Acc azr = AT::zero();
     for (int i = tid; i < n; i += nthr) {
-        if (__ldg(&a.wd[i]) == 0.0) continue;
-        const double ri = a.r[i];
-        const double zi = ri * __ldg(&a.sd[i]);
+        if (__ldg(&a.wd[i]) == T(0)) continue;
+        const T ri = a.r[i];
+        const T zi = ri * __ldg(&a.sd[i]);
         a.z[i] = zi;
         a.d[i] = zi;
         azr = AT::add(azr, zi * ri);
     }
-    write_partials<double>(p_zr, azr);
+    write_partials<T>(p_zr, azr);
     if (!grid_barrier(a.st, epoch, 32)) return;
     double one[1];
     grid_sum<1>(p_zr, one);
     double z_r = one[0];
+    const double z_r0 = z_r;
 
     int K = 0;
     int status = FEEC_MAXITER;
-    double beta = 0.0;
+    T beta = T(0);
     while (K < a.max_iter) {
         if (threadIdx.x == 0) {
             if (a.print_modulo > 0 && K % a.print_modulo == 0 && blockIdx.x == 0)
                 printf("(%d/%d)   INTERIM: Residual norm is %.9le < %.9le\n", K, n, sqrt(z_r), a.print_tol);
-            s_ctl = (a.use_zr_rule && fabs(z_r) < a.tol2) ? 1 : 0;                       // :859-862
+            int ctl = (a.use_zr_rule && fabs(z_r) < a.tol2) ? 1 : 0;                     // :859-862
+            if (a.rr_stop > 0.0 && z_r < a.rr_stop * z_r0) ctl = 1;                       // relative (inner solves)
+            s_ctl = ctl;
         }
         __syncthreads();
         if (s_ctl) { status = FEEC_OK; break; }
@@ -118,11 +122,11 @@ __global__ void __launch_bounds__(kThreads, 2) eisenstat_persistent(PcgArgs<doub
             FEEC_FOR_ROW_GROUPS(lo_r, hi_r, k, act) {
                 const int i = act ? __ldg(&a.brows[k]) : 0;
                 const int lo = act ? __ldg(&a.usplit[i]) : 0, hi = act ? __ldg(&a.rp[i + 1]) : 0;
-                const double s = seg_dot_guarded<LANES>(a.ci, a.val, a.m, a.wd, lo, hi, lane, g_iter);
+                const T s = seg_dot_guarded<T, LANES>(a.ci, a.val, a.m, a.wd, lo, hi, lane, g_iter);
                 if (act && lane == 0) {
-                    const double w = __ldg(&a.wd[i]);
-                    if (w != 0.0) {
-                        double dv = a.d[i];
+                    const T w = __ldg(&a.wd[i]);
+                    if (w != T(0)) {
+                        T dv = a.d[i];
                         if (K > 0) { dv = a.z[i] + beta * dv; a.d[i] = dv; }                // :990-997
                         a.m[i] = (dv - s) * w;
                     }
@@ -136,14 +140,14 @@ __global__ void __launch_bounds__(kThreads, 2) eisenstat_persistent(PcgArgs<doub
             const int lo_r = __ldg(&a.fptr[p]), hi_r = __ldg(&a.fptr[p + 1]);
             FEEC_FOR_ROW_GROUPS(lo_r, hi_r, i, act) {
                 const int lo = act ? __ldg(&a.rp[i]) : 0, hi = act ? __ldg(&a.lsplit[i]) : 0;
-                const double s = seg_dot_guarded<LANES>(a.ci, a.val, a.q, a.wd, lo, hi, lane, g_iter);
+                const T s = seg_dot_guarded<T, LANES>(a.ci, a.val, a.q, a.wd, lo, hi, lane, g_iter);
                 if (act && lane == 0) {
-                    const double w = __ldg(&a.wd[i]);
-                    if (w != 0.0) {
-                        const double dv = a.d[i], tv = a.m[i];
-                        const double av = (dv - c2 * __ldg(&a.dg[i]) * tv - s) * w;
+                    const T w = __ldg(&a.wd[i]);
+                    if (w != T(0)) {
+                        const T dv = a.d[i], tv = a.m[i];
+                        const T av = (dv - c2 * __ldg(&a.dg[i]) * tv - s) * w;
                         a.q[i] = av;
-                        const double cv = av + tv;
+                        const T cv = av + tv;
                         a.w[i] = cv;
                         dad = AT::add(dad, cv * dv);
                     }
@@ -151,7 +155,7 @@ __global__ void __launch_bounds__(kThreads, 2) eisenstat_persistent(PcgArgs<doub
             }
             if (p + 1 < a.nf && !grid_barrier(a.st, epoch, 34)) return;
         }
-        write_partials<double>(p_dad, dad);
+        write_partials<T>(p_dad, dad);
         if (!grid_barrier(a.st, epoch, 35)) return;
         grid_sum<1>(p_dad, one);
         const double d_Ad = one[0];
@@ -165,48 +169,50 @@ __global__ void __launch_bounds__(kThreads, 2) eisenstat_persistent(PcgArgs<doub
         __syncthreads();
         if (s_ctl == 1) { status = FEEC_BREAKDOWN; break; }
         if (s_ctl == 2) { status = FEEC_SMALL_ENERGY; break; }
-        const double alpha = s_scal[0];
+        const T alpha = (T)s_scal[0];
 
         // update (:936-975): x += alpha technical, r -= alpha (auxiliary + technical), z, z.r
         Acc zrn = AT::zero();
         for (int i = tid; i < n; i += nthr) {
-            if (__ldg(&a.wd[i]) == 0.0) continue;
+            if (__ldg(&a.wd[i]) == T(0)) continue;
             a.x[i] += alpha * a.m[i];
-            const double ri = a.r[i] - alpha * a.w[i];
+            const T ri = a.r[i] - alpha * a.w[i];
             a.r[i] = ri;
-            const double zi = ri * __ldg(&a.sd[i]);
+            const T zi = ri * __ldg(&a.sd[i]);
             a.z[i] = zi;
             zrn = AT::add(zrn, zi * ri);
         }
-        write_partials<double>(p_zr, zrn);
+        write_partials<T>(p_zr, zrn);
         if (!grid_barrier(a.st, epoch, 36)) return;
         grid_sum<1>(p_zr, one);
         if (threadIdx.x == 0) s_scal[1] = one[0] / z_r;
         __syncthreads();
-        beta = s_scal[1];
+        beta = (T)s_scal[1];
         z_r = one[0];
         K++;
     }
     finish(a.st, status, K, z_r, 0.0);
 }
 
+template <typename T>
 const void* eisenstat_fn(int lanes) {
     switch (lanes) {
-        case 1: return (const void*)eisenstat_persistent<1>;
-        case 2: return (const void*)eisenstat_persistent<2>;
-        case 4: return (const void*)eisenstat_persistent<4>;
-        case 8: return (const void*)eisenstat_persistent<8>;
-        case 16: return (const void*)eisenstat_persistent<16>;
-        default: return (const void*)eisenstat_persistent<32>;
+        case 1: return (const void*)eisenstat_persistent<T, 1>;
+        case 2: return (const void*)eisenstat_persistent<T, 2>;
+        case 4: return (const void*)eisenstat_persistent<T, 4>;
+        case 8: return (const void*)eisenstat_persistent<T, 8>;
+        case 16: return (const void*)eisenstat_persistent<T, 16>;
+        default: return (const void*)eisenstat_persistent<T, 32>;
     }
 }
 
 }  // namespace
 
-cudaError_t launch_eisenstat(const PcgArgs<double>& a, LaunchShape& shape, cudaStream_t s) {
+template <typename T>
+cudaError_t launch_eisenstat(const PcgArgs<T>& a, LaunchShape& shape, cudaStream_t s) {
     if (shape.threads <= 0) shape.threads = kThreads;
     if (shape.lanes <= 0) shape.lanes = 1;
-    const void* fn = eisenstat_fn(shape.lanes);
+    const void* fn = eisenstat_fn<T>(shape.lanes);
     int dev = 0, sms = 0, per_sm = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
@@ -219,10 +225,13 @@ cudaError_t launch_eisenstat(const PcgArgs<double>& a, LaunchShape& shape, cudaS
     if (b > maxb) b = maxb;
     if (b < 1) b = 1;
     shape.blocks = b;
-    PcgArgs<double> copy = a;
+    PcgArgs<T> copy = a;
     void* args[] = {&copy};
     note_launch();
     return cudaLaunchCooperativeKernel(fn, dim3(shape.blocks), dim3(shape.threads), args, 0, s);
 }
+
+template cudaError_t launch_eisenstat<double>(const PcgArgs<double>&, LaunchShape&, cudaStream_t);
+template cudaError_t launch_eisenstat<float>(const PcgArgs<float>&, LaunchShape&, cudaStream_t);
 
 }  // namespace feec
