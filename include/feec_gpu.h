@@ -170,7 +170,8 @@ int feec_system_solve(feec_system* sys, int method, int mode, double* x, const d
 /* Batched solves of one system with many right-hand sides (FEEC_MODE_MIXED or
  * FEEC_MODE_FP64; FEEC_METHOD_CG or FEEC_METHOD_RAINBOW): X and B are device
  * arrays of nrhs columns of N doubles (column j at X + j*N). One thread block
- * advances rhs_per_team columns (1, 2 or 4; 0 = automatic) through a complete
+ * advances rhs_per_team columns (1, 2, 4 or 8 in FP32 / MIXED; 1 or 2 in FP64;
+ * 0 = automatic) through a complete
  * solve; blocks take columns from a queue until none are left. infos (host,
  * nrhs entries, may be NULL) receives each column's result. */
 int feec_system_solve_batch(feec_system* sys, int method, int mode, int nrhs, double* X, const double* B,
@@ -178,7 +179,7 @@ int feec_system_solve_batch(feec_system* sys, int method, int mode, int nrhs, do
                             feec_solve_info* infos, void* stream);
 
 /* Autotuner of the batched engine: times short trials of every launch candidate
- * (right-hand sides per team 1/2/4; a one-block team of 128..1024 threads, or —
+ * (right-hand sides per team 1/2/4/8; a one-block team of 128..1024 threads, or —
  * when nrhs_hint leaves fewer work items than the GPU holds one-block teams — a
  * cluster team of 2/4/8/16 blocks) on this system and caches the fastest, which
  * feec_system_solve_batch then uses whenever rhs_per_team is 0. nrhs_hint is the

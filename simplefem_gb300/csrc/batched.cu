@@ -302,7 +302,7 @@ int pick_k(int mode, int rhs_per_team) {
     const int kmax = batched_max_k(mode == FEEC_MODE_MIXED);
     int K = rhs_per_team > 0 ? rhs_per_team : kmax;
     if (K > kmax) K = kmax;
-    if (K != 1 && K != 2 && K != 4) K = K >= 4 ? 4 : (K >= 2 ? 2 : 1);
+    if (K != 1 && K != 2 && K != 4 && K != 8) K = K >= 8 ? 8 : (K >= 4 ? 4 : (K >= 2 ? 2 : 1));
     if (K > kmax) K = kmax;
     return K;
 }
@@ -352,6 +352,7 @@ int feec_system_set_batch_config(feec_system* s, int method, int mode, int rhs_p
     if (team_blocks < 1 || team_blocks > 16 || (team_blocks & (team_blocks - 1)) != 0) return FEEC_BADARG;
     if (team_blocks == 1 && batched_team_threads(is_float, team_threads) != team_threads) return FEEC_BADARG;
     if (team_blocks == 1 && team_threads == 1024 && rhs_per_team > 2) return FEEC_BADARG;
+    if (team_blocks == 1 && rhs_per_team == 8 && team_threads != 256 && team_threads != 512) return FEEC_BADARG;
     if (team_blocks >= 2) {
         if (cluster_batched_resident(is_float, rhs_per_team, method == FEEC_METHOD_RAINBOW, team_blocks) <= 0)
             return FEEC_BADARG;
@@ -384,7 +385,7 @@ int feec_system_tune_batch(feec_system* s, int method, int mode, int nrhs_hint, 
     const int rb = method == FEEC_METHOD_RAINBOW;
     struct Candidate { int K, threads, blocks, resident; };
     std::vector<Candidate> cands;
-    const int Ks[3] = {1, 2, 4};
+    const int Ks[4] = {1, 2, 4, 8};
     const int Ts[4] = {128, 256, 512, 1024};
     const int Cs[4] = {2, 4, 8, 16};
     for (int K : Ks) {
@@ -392,6 +393,7 @@ int feec_system_tune_batch(feec_system* s, int method, int mode, int nrhs_hint, 
         for (int T : Ts) {
             if (batched_team_threads(is_float, T) != T) continue;
             if (T == 1024 && K > 2) continue;
+            if (K == 8 && T != 256 && T != 512) continue;
             cands.push_back({K, T, 1, batched_resident_teams(is_float, K, rb, T)});
         }
         const int items = nrhs_hint > 0 ? (nrhs_hint + K - 1) / K : 0;

@@ -7,7 +7,7 @@
 
 namespace feec {
 
-constexpr int kBatchMaxK = 4;   // right-hand sides advanced together by one team
+constexpr int kBatchMaxK = 8;   // right-hand sides advanced together by one team
 
 // Device view of one system in SELL-32 layout over its color-permuted rows.
 struct SellView {

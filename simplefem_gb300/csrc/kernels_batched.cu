@@ -42,7 +42,11 @@ __global__ void __launch_bounds__(THREADS, (1024 / THREADS) > 0 ? (1024 / THREAD
 
 template <typename T, int K, bool RB>
 const void* kfn(int threads) {
-    if constexpr (sizeof(T) == 4) {
+    if constexpr (sizeof(T) == 4 && K == 8) {
+        if (threads == 512) return (const void*)batched_solve_kernel<T, K, RB, 512>;
+        return (const void*)batched_solve_kernel<T, K, RB, 256>;
+    }
+    if constexpr (sizeof(T) == 4 && K < 8) {
         if (threads == 128) return (const void*)batched_solve_kernel<T, K, RB, 128>;
         if (threads == 512) return (const void*)batched_solve_kernel<T, K, RB, 512>;
         if constexpr (K <= 2) {
@@ -52,27 +56,44 @@ const void* kfn(int threads) {
     return (const void*)batched_solve_kernel<T, K, RB, 256>;
 }
 
+// nullptr for a (precision, K) without a compiled kernel: a work item's vectors are laid out
+// for its K, so a kernel of another K must never run it.
 const void* pick(int is_float, int K, int rainbow, int threads) {
     if (is_float) {
-        if (rainbow) return K == 1 ? kfn<float, 1, true>(threads) : K == 2 ? kfn<float, 2, true>(threads) : kfn<float, 4, true>(threads);
-        return K == 1 ? kfn<float, 1, false>(threads) : K == 2 ? kfn<float, 2, false>(threads) : kfn<float, 4, false>(threads);
+        switch (K) {
+            case 1: return rainbow ? kfn<float, 1, true>(threads) : kfn<float, 1, false>(threads);
+            case 2: return rainbow ? kfn<float, 2, true>(threads) : kfn<float, 2, false>(threads);
+            case 4: return rainbow ? kfn<float, 4, true>(threads) : kfn<float, 4, false>(threads);
+            case 8: return rainbow ? kfn<float, 8, true>(threads) : kfn<float, 8, false>(threads);
+            default: return nullptr;
+        }
     }
-    if (rainbow) return K == 1 ? kfn<double, 1, true>(threads) : kfn<double, 2, true>(threads);
-    return K == 1 ? kfn<double, 1, false>(threads) : kfn<double, 2, false>(threads);
+    switch (K) {
+        case 1: return rainbow ? kfn<double, 1, true>(threads) : kfn<double, 1, false>(threads);
+        case 2: return rainbow ? kfn<double, 2, true>(threads) : kfn<double, 2, false>(threads);
+        default: return nullptr;
+    }
 }
 
 }  // namespace
 
-int batched_max_k(int is_float) { return is_float ? 4 : 2; }
+int batched_max_k(int is_float) { return is_float ? 8 : 2; }
 
 int batched_team_threads(int is_float, int requested) {
     if (!is_float) return 256;
     return (requested == 128 || requested == 512 || requested == 1024) ? requested : 256;
 }
 
+// The block size of the kernel that runs (K = 8 exists for 256 and 512 threads only).
+int team_threads_for(int is_float, int K, int requested) {
+    const int t = batched_team_threads(is_float, requested);
+    return (K == 8 && t != 512) ? 256 : t;
+}
+
 int batched_resident_teams(int is_float, int K, int rainbow, int threads) {
-    threads = batched_team_threads(is_float, threads);
+    threads = team_threads_for(is_float, K, threads);
     const void* fn = pick(is_float, K, rainbow, threads);
+    if (!fn) return 0;
     const int smem = team_dynamic_smem(threads);
     cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     int dev = 0, sms = 0, per = 0;
@@ -83,8 +104,9 @@ int batched_resident_teams(int is_float, int K, int rainbow, int threads) {
 }
 
 cudaError_t launch_batched(const BatchArgs& args, int is_float, int K, int rainbow, int threads, int teams, cudaStream_t s) {
-    threads = batched_team_threads(is_float, threads);
+    threads = team_threads_for(is_float, K, threads);
     const void* fn = pick(is_float, K, rainbow, threads);
+    if (!fn) return cudaErrorInvalidValue;
     const int smem = team_dynamic_smem(threads);
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) return e;

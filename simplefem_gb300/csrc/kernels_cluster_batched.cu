@@ -33,13 +33,16 @@ __global__ void __launch_bounds__(kTeamThreads, 1024 / kTeamThreads) cluster_bat
     }
 }
 
+// nullptr for a K without a compiled kernel (a work item's vectors are laid out for its K).
 template <typename T, bool RB>
 const void* kfn(int K) {
     if constexpr (sizeof(T) == 4) {
+        if (K == 8) return (const void*)cluster_batched_kernel<T, 8, RB>;
         if (K == 4) return (const void*)cluster_batched_kernel<T, 4, RB>;
     }
     if (K == 2) return (const void*)cluster_batched_kernel<T, 2, RB>;
-    return (const void*)cluster_batched_kernel<T, 1, RB>;
+    if (K == 1) return (const void*)cluster_batched_kernel<T, 1, RB>;
+    return nullptr;
 }
 
 const void* pick(int is_float, int K, int rainbow) {
@@ -75,7 +78,7 @@ int cluster_batched_threads() { return kTeamThreads; }
 int cluster_batched_resident(int is_float, int K, int rainbow, int blocks) {
     if (blocks < 2 || blocks > 16) return 0;
     const void* fn = pick(is_float, K, rainbow);
-    if (prepare(fn, blocks) != cudaSuccess) return 0;
+    if (!fn || prepare(fn, blocks) != cudaSuccess) return 0;
     cudaLaunchAttribute attr;
     cudaLaunchConfig_t cfg = cluster_config(blocks, 1, attr, nullptr);
     int n = 0;
@@ -86,6 +89,7 @@ int cluster_batched_resident(int is_float, int K, int rainbow, int blocks) {
 cudaError_t launch_batched_clusters(const BatchArgs& args, int is_float, int K, int rainbow, int blocks, int clusters,
                                     cudaStream_t s) {
     const void* fn = pick(is_float, K, rainbow);
+    if (!fn) return cudaErrorInvalidValue;
     cudaError_t e = prepare(fn, blocks);
     if (e != cudaSuccess) return e;
     if (clusters <= 0) clusters = cluster_batched_resident(is_float, K, rainbow, blocks);

@@ -55,9 +55,12 @@ __device__ __forceinline__ void load_k(const T* p, T (&v)[K]) {
     } else if constexpr (K == 2) {
         const typename Vec<T, 2>::t u = *reinterpret_cast<const typename Vec<T, 2>::t*>(p);
         v[0] = u.x; v[1] = u.y;
-    } else if constexpr (K == 4 && sizeof(T) == 4) {
-        const float4 u = *reinterpret_cast<const float4*>(p);
-        v[0] = u.x; v[1] = u.y; v[2] = u.z; v[3] = u.w;
+    } else if constexpr (K % 4 == 0 && sizeof(T) == 4) {
+        #pragma unroll
+        for (int j = 0; j < K; j += 4) {
+            const float4 u = *reinterpret_cast<const float4*>(p + j);
+            v[j] = u.x; v[j + 1] = u.y; v[j + 2] = u.z; v[j + 3] = u.w;
+        }
     } else {
         #pragma unroll
         for (int j = 0; j < K; j += 2) {
@@ -72,7 +75,7 @@ __device__ __forceinline__ void load_k(const T* p, T (&v)[K]) {
 // first (all independent, coalesced across the warp), then the CH gathers are
 // issued together, then the FMAs run; padded slots are predicated off.
 template <typename T, int K>
-struct Chunk { static constexpr int value = sizeof(T) == 8 ? ((K >= 2) ? 2 : 4) : ((K >= 4) ? 4 : 8); };
+struct Chunk { static constexpr int value = sizeof(T) == 8 ? ((K >= 2) ? 2 : 4) : (K >= 8 ? 2 : ((K >= 4) ? 4 : 8)); };
 
 template <typename T, typename TV, int CH>
 __device__ __forceinline__ void load_entries(const int* __restrict__ sci, const TV* __restrict__ sval, long long off,
@@ -248,9 +251,12 @@ __device__ __forceinline__ void load_k_stream(const T* p, T (&v)[K]) {
     } else if constexpr (K == 2) {
         const typename Vec<T, 2>::t u = __ldcs(reinterpret_cast<const typename Vec<T, 2>::t*>(p));
         v[0] = u.x; v[1] = u.y;
-    } else if constexpr (K == 4 && sizeof(T) == 4) {
-        const float4 u = __ldcs(reinterpret_cast<const float4*>(p));
-        v[0] = u.x; v[1] = u.y; v[2] = u.z; v[3] = u.w;
+    } else if constexpr (K % 4 == 0 && sizeof(T) == 4) {
+        #pragma unroll
+        for (int j = 0; j < K; j += 4) {
+            const float4 u = __ldcs(reinterpret_cast<const float4*>(p + j));
+            v[j] = u.x; v[j + 1] = u.y; v[j + 2] = u.z; v[j + 3] = u.w;
+        }
     } else {
         #pragma unroll
         for (int j = 0; j < K; j += 2) {
@@ -278,8 +284,10 @@ __device__ __forceinline__ void store_row(T* v, int row, const T (&in)[K]) {
     } else if constexpr (K == 2) {
         typename Vec<T, 2>::t u; u.x = in[0]; u.y = in[1];
         __stcs(reinterpret_cast<typename Vec<T, 2>::t*>(p), u);
-    } else if constexpr (K == 4 && sizeof(T) == 4) {
-        __stcs(reinterpret_cast<float4*>(p), make_float4(in[0], in[1], in[2], in[3]));
+    } else if constexpr (K % 4 == 0 && sizeof(T) == 4) {
+        #pragma unroll
+        for (int j = 0; j < K; j += 4)
+            __stcs(reinterpret_cast<float4*>(p + j), make_float4(in[j], in[j + 1], in[j + 2], in[j + 3]));
     } else {
         #pragma unroll
         for (int j = 0; j < K; j += 2) __stcs(reinterpret_cast<double2*>(p + j), make_double2(in[j], in[j + 1]));

@@ -26,7 +26,8 @@ def _prepared(dim, r, L, seed=0, method="rainbow"):
 
 
 @pytest.mark.parametrize("method,mode,k", [("rainbow", "mixed", 4), ("rainbow", "mixed", 1), ("rainbow", "fp64", 2),
-                                           ("cg", "mixed", 4), ("cg", "fp64", 1), ("rainbow", "mixed", 2)])
+                                           ("cg", "mixed", 4), ("cg", "fp64", 1), ("rainbow", "mixed", 2),
+                                           ("rainbow", "mixed", 8), ("cg", "mixed", 8)])
 def test_batch_of_rhs_reaches_tolerance(cuda, method, mode, k):
     torch = cuda
     from simplefem_gb300 import workloads
@@ -150,7 +151,7 @@ def test_graph_captured_batch_replays(cuda):
 
 
 @pytest.mark.parametrize("mode,k,blocks", [("mixed", 4, 4), ("mixed", 2, 8), ("mixed", 1, 2), ("fp64", 2, 4),
-                                           ("fp64", 1, 16)])
+                                           ("fp64", 1, 16), ("mixed", 8, 4)])
 def test_cluster_teams_reach_tolerance(cuda, mode, k, blocks):
     """Cluster teams (2-16 blocks per work item, sums over distributed shared memory):
     every column reaches 1e-10 and agrees with an exact solve to 1e-9; FP64 iteration
@@ -210,7 +211,8 @@ def test_batch_config_rejects_invalid(cuda):
     from simplefem_gb300 import FeecError
     sysm, _ = _prepared(2, 1, 3)
     for kw in (dict(rhs_per_team=3), dict(rhs_per_team=4, team_blocks=3), dict(rhs_per_team=4, team_blocks=32),
-               dict(rhs_per_team=4, team_threads=100)):
+               dict(rhs_per_team=4, team_threads=100), dict(rhs_per_team=8, team_threads=1024),
+               dict(rhs_per_team=16)):
         with pytest.raises(FeecError):
             sysm.set_batch_config("rainbow", "mixed", **kw)
     with pytest.raises(FeecError):
