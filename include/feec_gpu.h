@@ -302,6 +302,13 @@ unsigned long long feec_kernel_launches(void);
 /* Human-readable name of a status code. */
 const char* feec_status_string(int status);
 
+/* Self-test of the bounded device waits (no counterpart in the reference): runs a
+ * kernel whose single wait is never satisfied, with a limit of limit_s seconds (at
+ * most 10). The wait gives up as a solver's grid barrier does; *status receives the
+ * status the kernel recorded (FEEC_TIMEOUT), *site the wait site, *elapsed_ms the host
+ * time of the call. Returns FEEC_OK when the GPU answered normally afterwards. */
+int feec_selftest_wait_timeout(double limit_s, int* status, int* site, double* elapsed_ms);
+
 #ifdef __cplusplus
 }
 #endif

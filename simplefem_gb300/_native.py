@@ -102,6 +102,8 @@ def gpu():
         L.feec_system_memory.argtypes = [_vp, ctypes.POINTER(ctypes.c_size_t)]
         L.feec_system_destroy.argtypes = [_vp]
         L.feec_kernel_launches.restype = ctypes.c_ulonglong
+        L.feec_selftest_wait_timeout.argtypes = [_dp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
+                                                 ctypes.POINTER(ctypes.c_double)]
         L.feec_status_string.restype = ctypes.c_char_p
         L.feec_status_string.argtypes = [_ip]
         _gpu = L

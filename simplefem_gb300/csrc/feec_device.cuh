@@ -46,6 +46,30 @@ __device__ __forceinline__ unsigned long long globaltimer_ns() {
     return t;
 }
 
+// One thread waits until the counter st->barrier reaches `target`. Gives up after
+// `limit_ns` (or kSpinLimit polls), or when another block has given up: it then sets
+// the abort flag, FEEC_TIMEOUT and the site, and returns false.
+__device__ __forceinline__ bool wait_counter(DeviceStatus* st, unsigned long long target, int site,
+                                             unsigned long long limit_ns) {
+    unsigned long long spins = 0, t0 = 0;
+    while (ld_acquire_u64(&st->barrier) < target) {
+        ++spins;
+        if ((spins & 255ull) == 0) {
+            if (ld_volatile_i32(&st->abort)) return false;
+            const unsigned long long t = globaltimer_ns();
+            if (t0 == 0) t0 = t;
+            if (spins > kSpinLimit || t - t0 > limit_ns) {
+                atomicExch(&st->abort, 1);
+                atomicCAS(&st->status, FEEC_OK, FEEC_TIMEOUT);
+                atomicExch(&st->timeout_site, site);
+                return false;
+            }
+        }
+        if (spins > 32) __nanosleep(32);
+    }
+    return true;
+}
+
 // Grid-wide barrier for a cooperatively launched grid. `epoch` is the number of
 // barriers this block has passed (identical in every block). Returns false if
 // the wait gave up (time or poll limit) or another block gave up; the caller
@@ -58,24 +82,7 @@ __device__ __forceinline__ bool grid_barrier(DeviceStatus* st, unsigned long lon
         const unsigned long long target = epoch * (unsigned long long)(gridDim.x * gridDim.y);
         __threadfence();
         atomicAdd(&st->barrier, 1ull);
-        int ok = 1;
-        unsigned long long spins = 0, t0 = 0;
-        while (ld_acquire_u64(&st->barrier) < target) {
-            ++spins;
-            if ((spins & 255ull) == 0) {
-                if (ld_volatile_i32(&st->abort)) { ok = 0; break; }
-                const unsigned long long t = globaltimer_ns();
-                if (t0 == 0) t0 = t;
-                if (spins > kSpinLimit || t - t0 > kWaitNanos) {
-                    atomicExch(&st->abort, 1);
-                    atomicCAS(&st->status, FEEC_OK, FEEC_TIMEOUT);
-                    atomicExch(&st->timeout_site, site);
-                    ok = 0;
-                    break;
-                }
-            }
-            if (spins > 32) __nanosleep(32);
-        }
+        const int ok = wait_counter(st, target, site, kWaitNanos) ? 1 : 0;
         __threadfence();
         s_ok = ok;
     }
