@@ -269,20 +269,32 @@ __global__ void __launch_bounds__(256) sell_spmv_kernel(SellView v, const T* __r
         const int L = len.x + len.y + len.z;
         T s = T(0);
         constexpr int CH = 8;
+        // software-pipelined: the next chunk's indices and values are requested together
+        // with the current chunk's gathers, so a chunk costs one memory round trip
+        int c[CH]; T a[CH];
+        #pragma unroll
+        for (int u = 0; u < CH; u++) {
+            const bool ok = u < L;
+            const long long p = off + (long long)u * 32 + lane;
+            c[u] = ok ? __ldcs(&v.ci[p]) : 0;
+            a[u] = ok ? __ldcs(&val[p]) : T(0);
+        }
         for (int k0 = 0; k0 < L; k0 += CH) {
-            int c[CH]; T a[CH];
-            #pragma unroll
-            for (int u = 0; u < CH; u++) {
-                const bool ok = k0 + u < L;
-                const long long p = off + (long long)(k0 + u) * 32 + lane;
-                c[u] = ok ? __ldcs(&v.ci[p]) : 0;
-                a[u] = ok ? __ldcs(&val[p]) : T(0);
-            }
             T xv[CH];
             #pragma unroll
             for (int u = 0; u < CH; u++) xv[u] = __ldg(&x[c[u]]);
+            int cn[CH]; T an[CH];
+            #pragma unroll
+            for (int u = 0; u < CH; u++) {
+                const bool ok = k0 + CH + u < L;
+                const long long p = off + (long long)(k0 + CH + u) * 32 + lane;
+                cn[u] = ok ? __ldcs(&v.ci[p]) : 0;
+                an[u] = ok ? __ldcs(&val[p]) : T(0);
+            }
             #pragma unroll
             for (int u = 0; u < CH; u++) s = fma(a[u], xv[u], s);
+            #pragma unroll
+            for (int u = 0; u < CH; u++) { c[u] = cn[u]; a[u] = an[u]; }
         }
         // FP64 issues at 2 lanes/clk/SM on this part: skip the multiply when scaling == 1
         if (lane < nrow) y[row0 + lane] = scaling == T(1) ? s : scaling * s;
