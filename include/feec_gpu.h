@@ -41,8 +41,10 @@ enum {
     FEEC_METHOD_RAINBOW = 2,   /* ConjugateGradientSolverCSR_Rainbow  (sparsesolver.cpp:1002-1335) */
     FEEC_METHOD_SSOR_EISENSTAT = 3,    /* ConjugateGradientSolverCSR_SSOR_Eisenstat (sparsesolver.cpp:726-995);
                                           needs feec_system_set_ssor; FEEC_MODE_REFERENCE only     */
-    FEEC_METHOD_RAINBOW_EISENSTAT = 4  /* ConjugateGradientSolverCSR_Eisenstat_Rainbow (sparsesolver.cpp:1338-1645);
+    FEEC_METHOD_RAINBOW_EISENSTAT = 4, /* ConjugateGradientSolverCSR_Eisenstat_Rainbow (sparsesolver.cpp:1338-1645);
                                           needs feec_system_set_rainbow; FEEC_MODE_REFERENCE only  */
+    FEEC_METHOD_DIAGONAL = 5           /* ConjugateGradientSolverCSR_DiagonalPreconditioner (sparsesolver.cpp:221-416);
+                                          needs feec_system_set_diagonal_precon; REFERENCE only    */
 };
 
 /* Arithmetic / stopping modes for feec_system_solve. */
@@ -83,6 +85,14 @@ int feec_cg_csr(int N, double* x, const double* b,
                 const int* A, const int* C, const double* V,
                 double* residual, double precision, int print_modulo,
                 feec_solve_info* info);
+
+/* Replaces ConjugateGradientSolverCSR_DiagonalPreconditioner, solver/sparsesolver.hpp:21-31
+ * (sparsesolver.cpp:221-416): CG preconditioned by z = precon * r (rows with precon == 0 are
+ * skipped, as in the reference). */
+int feec_cg_csr_diagonal_precon(int N, double* x, const double* b,
+                                const int* A, const int* C, const double* V,
+                                double* residual, double precision, int print_modulo,
+                                const double* precon, feec_solve_info* info);
 
 /* Replaces ConjugateGradientSolverCSR_SSOR, solver/sparsesolver.hpp:33-43 (sparsesolver.cpp:446-724). */
 int feec_cg_csr_ssor(int N, double* x, const double* b,
@@ -152,6 +162,10 @@ int feec_system_create(feec_system** sys, int N, const int* A, const int* C, con
  * host_ptrs != 0, else device pointers. */
 int feec_system_set_rainbow(feec_system* sys, const double* diagonal, double omega,
                             int num_colors, const int* F, const int* B, const int* R, int host_ptrs);
+
+/* Sets the diagonal preconditioner of FEEC_METHOD_DIAGONAL (N values; host pointer if
+ * host_ptrs != 0, else device pointer). */
+int feec_system_set_diagonal_precon(feec_system* sys, const double* precon, int host_ptrs);
 
 /* Prepares the lexicographic SSOR layout (level-scheduled triangular sweeps). */
 int feec_system_set_ssor(feec_system* sys, const double* diagonal, double omega, int host_ptrs);

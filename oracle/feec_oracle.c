@@ -143,6 +143,79 @@ int oracle_cg(int N, double* x, const double* b, const int* A, const int* C, con
     return K;
 }
 
+static double* nan_vector(int N);
+
+/* solver/sparsesolver.cpp:221-416, CG with a diagonal preconditioner z = precon * r;
+ * returns K. The direction update (:386-395) is `omp parallel` without `for` in the
+ * reference (a race with more than one thread); it runs serially here. */
+int oracle_cg_diag(int N, double* x, const double* b, const int* A, const int* C, const double* V,
+                   double* residual, double precision, int print_modulo, const double* precon)
+{
+    (void)print_modulo;
+    double tolerance = 0.0;                                   /* :243-246 */
+    for (int i = 0; i < N; i++) tolerance += b[i] * b[i];
+    tolerance = precision * sqrt(tolerance);
+    tolerance = dmax(tolerance, ORACLE_DESIRED_PRECISION);
+
+    double* direction = nan_vector(N);                        /* :259-264 */
+    double* zirconium = nan_vector(N);
+    double* auxiliary = nan_vector(N);
+    if (!direction || !zirconium || !auxiliary) {
+        free(direction); free(zirconium); free(auxiliary); return -1;
+    }
+    double z_r = NAN;
+    int K = 0;
+    while (K < N) {
+        if (K == 0) {                                         /* :283-302 */
+            z_r = 0.0;
+            #pragma omp parallel for reduction(+:z_r)
+            for (int c = 0; c < N; c++) {
+                if (precon[c] == 0.0) continue;
+                residual[c] = b[c];
+                for (int d = A[c]; d < A[c + 1]; d++) residual[c] -= V[d] * x[C[d]];
+                zirconium[c] = precon[c] * residual[c];
+                direction[c] = zirconium[c];
+                z_r += zirconium[c] * residual[c];
+            }
+        }
+        if (fabs(z_r) < tolerance * tolerance) break;        /* :318-321 */
+
+        double d_Ad = 0.0;                                    /* :330-345 */
+        #pragma omp parallel for reduction(+:d_Ad)
+        for (int c = 0; c < N; c++) {
+            if (precon[c] == 0.0) continue;
+            auxiliary[c] = 0.0;
+            for (int d = A[c]; d < A[c + 1]; d++) auxiliary[c] += V[d] * direction[C[d]];
+            d_Ad += direction[c] * auxiliary[c];
+        }
+        int numerator_bad = !isfinite(z_r) || z_r < 0.0;      /* :348-363 */
+        int denominator_bad = !isfinite(d_Ad) || d_Ad < 0.0;
+        int denominator_small = sqrt(fabs(d_Ad)) < ORACLE_MACHINE_EPSILON;
+        if (numerator_bad || denominator_bad) break;
+        if (denominator_small) break;
+
+        const double alpha = z_r / d_Ad;                      /* :366-384 */
+        double z_r_new = 0.0;
+        #pragma omp parallel for reduction(+:z_r_new)
+        for (int c = 0; c < N; c++) {
+            if (precon[c] == 0.0) continue;
+            x[c] += alpha * direction[c];
+            residual[c] -= alpha * auxiliary[c];
+            zirconium[c] = precon[c] * residual[c];
+            z_r_new += zirconium[c] * residual[c];
+        }
+        const double beta = z_r_new / z_r;                    /* :386-397 */
+        z_r = z_r_new;
+        for (int c = 0; c < N; c++) {
+            if (precon[c] == 0.0) continue;
+            direction[c] = zirconium[c] + beta * direction[c];
+        }
+        K++;
+    }
+    free(direction); free(zirconium); free(auxiliary);
+    return K;
+}
+
 /* solver/sparsesolver.cpp:446-724, SSOR-preconditioned CG in index order; returns K */
 int oracle_cg_ssor(int N, double* x, const double* b, const int* A, const int* C, const double* V,
                    double* residual, double precision, int print_modulo,

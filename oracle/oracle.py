@@ -45,6 +45,7 @@ def lib():
         L.oracle_cg_ssor.argtypes = L.oracle_cg.argtypes + [_f64p, ctypes.c_double]
         L.oracle_cg_rainbow.argtypes = L.oracle_cg_ssor.argtypes + [ctypes.c_int, _i32p, _i32p, _i32p]
         L.oracle_cg_ssor_eisenstat.argtypes = L.oracle_cg_ssor.argtypes
+        L.oracle_cg_diag.argtypes = L.oracle_cg.argtypes + [_f64p]
         L.oracle_cg_eisenstat_rainbow.argtypes = L.oracle_cg_rainbow.argtypes
         L.oracle_max_threads.restype = ctypes.c_int
         L.oracle_set_threads.argtypes = [ctypes.c_int]
@@ -128,4 +129,13 @@ def cg_eisenstat_rainbow(A, C, V, b, diag, rb, omega=1.0, x0=None, precision=1e-
                                           -3, np.ascontiguousarray(diag, np.float64), float(omega), int(nc),
                                           np.ascontiguousarray(F, np.int32), np.ascontiguousarray(B, np.int32),
                                           np.ascontiguousarray(R, np.int32))
+    return K, x, res
+
+
+def cg_diag(A, C, V, b, precon, x0=None, precision=1e-10):
+    n = len(A) - 1
+    x = np.zeros(n) if x0 is None else np.array(x0, np.float64)
+    res = np.array(b, np.float64)
+    K = lib().oracle_cg_diag(n, x, np.ascontiguousarray(b, np.float64), A, C, V, res, float(precision), -3,
+                             np.ascontiguousarray(precon, np.float64))
     return K, x, res

@@ -14,8 +14,9 @@
 //       the broken scalar mass cell by cell with a log-uniform [0.1,10] factor
 //       hashed from the cell position (cell_coefficient below).
 //       Writes the CSR plus the position of every global degree of freedom.
-//   solve <cg|ssor|rainbow|eisenstat|eisenstat_rainbow> <in.csr> <in.vec b> <in.vec x0> <precision> <omega> <out.sol>
-//       Calls ConjugateGradientSolverCSR{,_SSOR,_Rainbow,_SSOR_Eisenstat,_Eisenstat_Rainbow} (solver/sparsesolver.hpp)
+//   solve <cg|diag|ssor|rainbow|eisenstat|eisenstat_rainbow> <in.csr> <in.vec b> <in.vec x0> <precision> <omega> <out.sol>
+//       Calls ConjugateGradientSolverCSR{,_DiagonalPreconditioner (precon = 1/diagonal),_SSOR,_Rainbow,
+//       _SSOR_Eisenstat,_Eisenstat_Rainbow} (solver/sparsesolver.hpp)
 //       with print_modulo = -3; writes K, x, residual, solve seconds.
 //   rainbow <in.csr> <out.rb>        Rainbow(A) (sparse/rainbow.cpp:14-130)
 //   apply <in.csr> <in.vec> <scaling> <out.vec>   MatrixCSR::apply (sparse/matcsr.cpp:216-244)
@@ -209,6 +210,14 @@ int main(int argc, char** argv) {
             auto t0 = std::chrono::steady_clock::now();
             K = ConjugateGradientSolverCSR_Rainbow((int)m.n, x.data(), b.data(), mat.getA(), mat.getC(), mat.getV(), res.data(), precision, -3, diag.raw(), omega,
                                                    rb.num_colors, rb.F.data(), rb.B.data(), rb.R.data());
+            secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        } else if (kind == "diag") {
+            // the preconditioner the reference's callers pass: the inverse diagonal
+            FloatVector diag = mat.getDiagonal();
+            std::vector<double> precon(m.n);
+            for (int64_t i = 0; i < m.n; i++) precon[i] = diag[i] != 0.0 ? 1.0 / diag[i] : 0.0;
+            auto t0 = std::chrono::steady_clock::now();
+            K = ConjugateGradientSolverCSR_DiagonalPreconditioner((int)m.n, x.data(), b.data(), mat.getA(), mat.getC(), mat.getV(), res.data(), precision, -3, precon.data());
             secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
         } else if (kind == "eisenstat") {
             FloatVector diag = mat.getDiagonal();

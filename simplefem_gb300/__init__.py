@@ -6,8 +6,8 @@ the C ABI of ``include/feec_gpu.h``. This package is the Python host side of tha
 ABI; it mirrors the reference's MatrixCSR / Rainbow / raw-pointer solver surface.
 """
 from ._native import FeecError, FeecSolveInfo  # noqa: F401
-from .solver import (ConjugateGradientSolverCSR, ConjugateGradientSolverCSR_Eisenstat_Rainbow,  # noqa: F401
-                     ConjugateGradientSolverCSR_Rainbow, ConjugateGradientSolverCSR_SSOR,
+from .solver import (ConjugateGradientSolverCSR, ConjugateGradientSolverCSR_DiagonalPreconditioner,  # noqa: F401
+                     ConjugateGradientSolverCSR_Eisenstat_Rainbow, ConjugateGradientSolverCSR_Rainbow, ConjugateGradientSolverCSR_SSOR,
                      ConjugateGradientSolverCSR_SSOR_Eisenstat, last_info)
 from .sparse import FloatVector, MatrixCSR, Rainbow  # noqa: F401
 
@@ -15,6 +15,7 @@ from .sparse import FloatVector, MatrixCSR, Rainbow  # noqa: F401
 machine_epsilon = 2.220446049250313080847263336181640625e-16
 desired_precision = 1.490116119384765625e-08
 
-__all__ = ["MatrixCSR", "Rainbow", "FloatVector", "ConjugateGradientSolverCSR", "ConjugateGradientSolverCSR_SSOR",
+__all__ = ["MatrixCSR", "Rainbow", "FloatVector", "ConjugateGradientSolverCSR",
+           "ConjugateGradientSolverCSR_DiagonalPreconditioner", "ConjugateGradientSolverCSR_SSOR",
            "ConjugateGradientSolverCSR_Rainbow", "ConjugateGradientSolverCSR_SSOR_Eisenstat",
            "ConjugateGradientSolverCSR_Eisenstat_Rainbow", "last_info", "FeecError", "machine_epsilon", "desired_precision"]

@@ -41,7 +41,7 @@ STATUS = {0: "ok", 1: "breakdown", 2: "small_energy", 3: "maxiter", 4: "timeout"
           7: "cuda_error", 8: "no_device"}
 FEEC_OK, FEEC_BREAKDOWN, FEEC_SMALL_ENERGY, FEEC_MAXITER, FEEC_TIMEOUT, FEEC_OOM, FEEC_BADARG, FEEC_CUDA_ERROR, \
     FEEC_NO_DEVICE = range(9)
-METHOD_CG, METHOD_SSOR, METHOD_RAINBOW, METHOD_SSOR_EISENSTAT, METHOD_RAINBOW_EISENSTAT = 0, 1, 2, 3, 4
+METHOD_CG, METHOD_SSOR, METHOD_RAINBOW, METHOD_SSOR_EISENSTAT, METHOD_RAINBOW_EISENSTAT, METHOD_DIAGONAL = 0, 1, 2, 3, 4, 5
 MODE_REFERENCE, MODE_FP64, MODE_MIXED = 0, 1, 2
 
 
@@ -76,6 +76,8 @@ def gpu():
         L.feec_cg_csr_ssor.argtypes = host + [_f64p, _dp, _infop]
         L.feec_cg_csr_rainbow.argtypes = host + [_f64p, _dp, _ip, _i32p, _i32p, _i32p, _infop]
         L.feec_cg_csr_ssor_eisenstat.argtypes = L.feec_cg_csr_ssor.argtypes
+        L.feec_cg_csr_diagonal_precon.argtypes = host + [_f64p, _infop]
+        L.feec_system_set_diagonal_precon.argtypes = [_vp, _vp, _ip]
         L.feec_cg_csr_eisenstat_rainbow.argtypes = L.feec_cg_csr_rainbow.argtypes
         L.feec_csr_apply.argtypes = [_ip, _ip, _i32p, _i32p, _f64p, _f64p, _f64p, _dp]
         L.feec_csr_diagonal.argtypes = [_ip, _i32p, _i32p, _f64p, _f64p]

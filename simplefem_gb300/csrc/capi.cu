@@ -174,6 +174,7 @@ const char* method_title(int method) {
         case FEEC_METHOD_RAINBOW: return "Conjugate Gradient CSR (SSOR-Rainbow)";
         case FEEC_METHOD_SSOR_EISENSTAT: return "Conjugate Gradient CSR (SSOR-Eisenstat)";
         case FEEC_METHOD_RAINBOW_EISENSTAT: return "Conjugate Gradient CSR (SSOR-Rainbow-Eisenstat)";
+        case FEEC_METHOD_DIAGONAL: return "Conjugate Gradient CSR (Diag)";
         default: return "Conjugate Gradient CSR";
     }
 }
@@ -188,12 +189,16 @@ int solve_core(feec_system* s, int method, int mode, double* xx, const double* b
     // the layout a method sweeps over: the Eisenstat variants use the SSOR / Rainbow ones
     const int layout = method == FEEC_METHOD_SSOR_EISENSTAT ? FEEC_METHOD_SSOR
                      : method == FEEC_METHOD_RAINBOW_EISENSTAT ? FEEC_METHOD_RAINBOW : method;
-    if (method != FEEC_METHOD_CG && s->prepared != layout) return FEEC_BADARG;
-    if (eisenstat && mode != FEEC_MODE_REFERENCE) return FEEC_BADARG;
+    const bool diagonal = method == FEEC_METHOD_DIAGONAL;
+    // plain CG and the diagonally preconditioned CG run on the caller's CSR in its own numbering
+    const bool cg_family = method == FEEC_METHOD_CG || diagonal;
+    if (!cg_family && s->prepared != layout) return FEEC_BADARG;
+    if (diagonal && !s->precon) return FEEC_BADARG;
+    if ((eisenstat || diagonal) && mode != FEEC_MODE_REFERENCE) return FEEC_BADARG;
     int st = ensure_work(s);
     if (st != FEEC_OK) return st;
     if (max_iter <= 0) max_iter = n;
-    const bool permuted = method != FEEC_METHOD_CG;
+    const bool permuted = !cg_family;
     const int* perm = permuted ? s->perm : nullptr;
 
     // bring b, x (and the caller's residual for rows the sweeps skip) into solver order
@@ -216,7 +221,7 @@ int solve_core(feec_system* s, int method, int mode, double* xx, const double* b
     // per-group epilogues cost more than they save; one thread per row is fastest for
     // plain FP64 CG and 4 lanes per row for the sweeps of the preconditioned solvers
     // (8 for their FP32 inner solves).
-    if (method == FEEC_METHOD_CG && mode != FEEC_MODE_MIXED) shape.lanes = 1;
+    if (cg_family && mode != FEEC_MODE_MIXED) shape.lanes = 1;
     else {
         const int cap = (mode == FEEC_MODE_MIXED && method != FEEC_METHOD_CG) ? 8 : 4;
         if (shape.lanes > cap) shape.lanes = cap;
@@ -252,9 +257,16 @@ int solve_core(feec_system* s, int method, int mode, double* xx, const double* b
             FEEC_TRY(cudaMemsetAsync(s->m, 0, sizeof(double) * n, s->stream));
             FEEC_TRY(cudaMemsetAsync(s->q, 0, sizeof(double) * n, s->stream));
             float ms = 0.0f;
-            if (method == FEEC_METHOD_CG) {
+            if (cg_family) {
                 CgArgs<double> a{};
                 a.n = n; a.rp = s->A; a.ci = s->C; a.val = s->V; a.b = s->b; a.x = s->x; a.r = s->r; a.d = s->d; a.q = s->q;
+                if (diagonal) {
+                    a.precon = s->precon; a.z = s->z;
+                    // the reference starts its work vectors as NaN (sparsesolver.cpp:259-264);
+                    // rows it skips (precon == 0) keep that value
+                    for (double* v : {s->d, s->z, s->q})
+                        FEEC_TRY(cudaMemsetAsync(v, 0xFF, sizeof(double) * n, s->stream));
+                }
                 a.tol2 = tolerance * tolerance;
                 a.max_iter = max_iter - (K_total - k0);
                 a.print_modulo = print_modulo; a.print_tol = tolerance;
@@ -442,7 +454,7 @@ int solve_core(feec_system* s, int method, int mode, double* xx, const double* b
         info->status = status;
         info->iterations = K_total;
         info->outer_iterations = outer;
-        info->num_colors = method == FEEC_METHOD_CG ? 0 : s->num_levels;
+        info->num_colors = cg_family ? 0 : s->num_levels;
         info->fp64_fallback = fell_back;
         info->tolerance = (mode == FEEC_MODE_REFERENCE) ? tolerance : precision;
         info->final_norm = final_norm;
@@ -670,6 +682,18 @@ int feec_system_set_rainbow(feec_system* s, const double* diagonal, double omega
     return st;
 }
 
+int feec_system_set_diagonal_precon(feec_system* s, const double* precon, int host_ptrs) {
+    if (!s || !precon) return FEEC_BADARG;
+    if (!s->precon) {
+        HomeStreamScope home(s);
+        FEEC_TRY(s->mem.alloc(s->precon, (size_t)s->n));
+    }
+    FEEC_TRY(cudaMemcpyAsync(s->precon, precon, sizeof(double) * s->n,
+                             host_ptrs ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, s->stream));
+    FEEC_TRY(cudaStreamSynchronize(s->stream));
+    return FEEC_OK;
+}
+
 int feec_system_set_ssor(feec_system* s, const double* diagonal, double omega, int host_ptrs) {
     if (!s || !diagonal || !(omega > 0.0) || !(omega < 2.0)) return FEEC_BADARG;
     const int n = s->n;
@@ -709,7 +733,7 @@ int feec_system_solve(feec_system* s, int method, int mode, double* x, const dou
                       double precision, int max_iter, feec_solve_info* info, void* stream) {
     zero_info(info);
     if (!s || !x || !b || !(precision > 0.0)) return FEEC_BADARG;
-    if (method < FEEC_METHOD_CG || method > FEEC_METHOD_RAINBOW_EISENSTAT || mode < FEEC_MODE_REFERENCE || mode > FEEC_MODE_MIXED)
+    if (method < FEEC_METHOD_CG || method > FEEC_METHOD_DIAGONAL || mode < FEEC_MODE_REFERENCE || mode > FEEC_MODE_MIXED)
         return FEEC_BADARG;
     cudaStream_t keep = s->stream;
     if (stream) s->stream = (cudaStream_t)stream;
@@ -773,6 +797,7 @@ static int dropin_solve(int method, int N, double* x, const double* b, const int
     int st = feec_system_create(&s, N, A, C, V, 1, nullptr);
     if (st != FEEC_OK) return st;
     if (rb) st = feec_system_set_rainbow(s, diagonal, omega, num_colors, F, B, R, 1);
+    else if (method == FEEC_METHOD_DIAGONAL) st = feec_system_set_diagonal_precon(s, diagonal, 1);
     else if (method != FEEC_METHOD_CG) st = feec_system_set_ssor(s, diagonal, omega, 1);
     double *dx = nullptr, *db = nullptr, *dr = nullptr;
     DevArena io; io.stream = s->stream;
@@ -828,6 +853,13 @@ int feec_cg_csr_rainbow(int N, double* x, const double* b, const int* A, const i
                         int num_colors, const int* F, const int* B, const int* R, feec_solve_info* info) {
     return dropin_solve(FEEC_METHOD_RAINBOW, N, x, b, A, C, V, residual, precision, print_modulo, diagonal, omega,
                         num_colors, F, B, R, info);
+}
+
+int feec_cg_csr_diagonal_precon(int N, double* x, const double* b, const int* A, const int* C, const double* V,
+                                double* residual, double precision, int print_modulo, const double* precon,
+                                feec_solve_info* info) {
+    return dropin_solve(FEEC_METHOD_DIAGONAL, N, x, b, A, C, V, residual, precision, print_modulo, precon, 1.0, 0,
+                        nullptr, nullptr, nullptr, info);
 }
 
 int feec_cg_csr_ssor_eisenstat(int N, double* x, const double* b, const int* A, const int* C, const double* V,

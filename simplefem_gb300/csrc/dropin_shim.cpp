@@ -1,5 +1,5 @@
 // libfeec_dropin.so: exports the reference's own C++ entry points of the CSR
-// Krylov path (solver/sparsesolver.hpp:11-19, 33-43, 46-56, 59-70, 73-84, with Float =
+// Krylov path (solver/sparsesolver.hpp:11-19, 21-31, 33-43, 46-56, 59-70, 73-84, with Float =
 // double, the reference's default build) so that an application linked
 // against FEEC++'s solver module can link this library instead and run the
 // solves on the GPU unchanged. Each function forwards to the C ABI and returns
@@ -76,4 +76,14 @@ int ConjugateGradientSolverCSR_Eisenstat_Rainbow(const int N, double* x, const d
     const int st = feec_cg_csr_eisenstat_rainbow(N, x, b, csrrows, csrcolumns, csrvalues, residual, precision,
                                                  print_modulo, diagonal, omega, num_colors, F, B, R, &info);
     return checked(st, info, "ConjugateGradientSolverCSR_Eisenstat_Rainbow");
+}
+
+int ConjugateGradientSolverCSR_DiagonalPreconditioner(const int N, double* x, const double* b, const int* csrrows,
+                                                      const int* csrcolumns, const double* csrvalues,
+                                                      double* residual, double precision, int print_modulo,
+                                                      const double* precon) {
+    feec_solve_info info;
+    const int st = feec_cg_csr_diagonal_precon(N, x, b, csrrows, csrcolumns, csrvalues, residual, precision,
+                                               print_modulo, precon, &info);
+    return checked(st, info, "ConjugateGradientSolverCSR_DiagonalPreconditioner");
 }

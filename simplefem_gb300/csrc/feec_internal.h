@@ -30,6 +30,10 @@ struct CgArgs {
     double print_tol;   // tolerance printed in interim lines
     double* partials;   // >= 3 * gridDim.x doubles
     DeviceStatus* st;
+    // diagonal preconditioner (ConjugateGradientSolverCSR_DiagonalPreconditioner) when not
+    // null: z = precon * r, rows with precon == 0 are skipped, the stop test is on z.r
+    const T* precon;
+    T* z;
 };
 
 template <typename T>

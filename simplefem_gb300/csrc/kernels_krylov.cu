@@ -122,16 +122,31 @@ __global__ void __launch_bounds__(kThreads) cg_persistent(CgArgs<T> a) {
     double* p_dq = a.partials;
     double* p_rr = a.partials + gridDim.x;
 
-    // restart (sparsesolver.cpp:76-104): r = b - A x, d = r, r.r
+    // With a diagonal preconditioner (sparsesolver.cpp:221-416) z = precon r replaces r in
+    // the direction and the scalar products, and rows with precon == 0 are skipped.
+    const T* pc = a.precon;
+    // restart (sparsesolver.cpp:76-104 / :283-302): r = b - A x, d = r (or z), r.r (or z.r)
     Acc acc = AT::zero();
     FEEC_FOR_ROW_GROUPS(0, n, i, act) {
         const int lo = act ? __ldg(&a.rp[i]) : 0, hi = act ? __ldg(&a.rp[i + 1]) : 0;
         const T s = seg_dot<T, LANES>(a.ci, a.val, a.x, lo, hi, lane);
         if (act && lane == 0) {
-            const T ri = __ldg(&a.b[i]) - s;
-            a.r[i] = ri;
-            a.d[i] = ri;
-            acc = AT::add(acc, ri * ri);
+            if (pc) {
+                const T p = __ldg(&pc[i]);
+                if (p != T(0)) {
+                    const T ri = __ldg(&a.b[i]) - s;
+                    a.r[i] = ri;
+                    const T zi = p * ri;
+                    a.z[i] = zi;
+                    a.d[i] = zi;
+                    acc = AT::add(acc, zi * ri);
+                }
+            } else {
+                const T ri = __ldg(&a.b[i]) - s;
+                a.r[i] = ri;
+                a.d[i] = ri;
+                acc = AT::add(acc, ri * ri);
+            }
         }
     }
     write_partials<T>(p_rr, acc);
@@ -160,9 +175,10 @@ __global__ void __launch_bounds__(kThreads) cg_persistent(CgArgs<T> a) {
         // q = A d, d.q                                                               :126-139
         Acc adq = AT::zero();
         FEEC_FOR_ROW_GROUPS(0, n, i, act) {
-            const int lo = act ? __ldg(&a.rp[i]) : 0, hi = act ? __ldg(&a.rp[i + 1]) : 0;
+            const bool live = act && (!pc || __ldg(&pc[i]) != T(0));
+            const int lo = live ? __ldg(&a.rp[i]) : 0, hi = live ? __ldg(&a.rp[i + 1]) : 0;
             const T s = seg_dot<T, LANES>(a.ci, a.val, a.d, lo, hi, lane);
-            if (act && lane == 0) {
+            if (live && lane == 0) {
                 a.q[i] = s;
                 adq = AT::add(adq, a.d[i] * s);
             }
@@ -185,12 +201,20 @@ __global__ void __launch_bounds__(kThreads) cg_persistent(CgArgs<T> a) {
 
         const T alpha = (T)s_scal[0];
         Acc arr = AT::zero();
-        for (int i = tid; i < n; i += nthr) {                                          // :158-173
+        for (int i = tid; i < n; i += nthr) {                                          // :158-173 / :361-378
+            T p = T(1);
+            if (pc) { p = __ldg(&pc[i]); if (p == T(0)) continue; }
             const T di = a.d[i];
             a.x[i] += alpha * di;
             const T ri = a.r[i] - alpha * a.q[i];
             a.r[i] = ri;
-            arr = AT::add(arr, ri * ri);
+            if (pc) {
+                const T zi = p * ri;
+                a.z[i] = zi;
+                arr = AT::add(arr, zi * ri);
+            } else {
+                arr = AT::add(arr, ri * ri);
+            }
         }
         write_partials<T>(p_rr, arr);
         if (!grid_barrier(a.st, epoch, 3)) return;
@@ -200,7 +224,12 @@ __global__ void __launch_bounds__(kThreads) cg_persistent(CgArgs<T> a) {
         __syncthreads();
         const T beta = (T)s_scal[1];
         r_r = r_r_new;
-        for (int i = tid; i < n; i += nthr) a.d[i] = a.r[i] + beta * a.d[i];
+        if (pc) {
+            for (int i = tid; i < n; i += nthr)
+                if (__ldg(&pc[i]) != T(0)) a.d[i] = a.z[i] + beta * a.d[i];            // :386-395
+        } else {
+            for (int i = tid; i < n; i += nthr) a.d[i] = a.r[i] + beta * a.d[i];
+        }
         if (!grid_barrier(a.st, epoch, 4)) return;
         K++;
     }

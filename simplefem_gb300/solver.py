@@ -104,3 +104,15 @@ def ConjugateGradientSolverCSR_Eisenstat_Rainbow(N, x, b, csrrows, csrcolumns, c
                                                      _vec(diagonal, "diagonal", N), float(omega), int(num_colors),
                                                      _ints(F, "F"), _ints(B, "B"), _ints(R, "R"), info)
     return _finish(st, info, "ConjugateGradientSolverCSR_Eisenstat_Rainbow")
+
+
+def ConjugateGradientSolverCSR_DiagonalPreconditioner(N, x, b, csrrows, csrcolumns, csrvalues, residual, precision,
+                                                      print_modulo, precon):
+    """GPU replacement of ConjugateGradientSolverCSR_DiagonalPreconditioner (solver/sparsesolver.cpp:221-416)."""
+    x = _vec(x, "x", N, True); residual = _vec(residual, "residual", N, True)
+    info = _native.FeecSolveInfo()
+    st = _native.gpu().feec_cg_csr_diagonal_precon(int(N), x, _vec(b, "b", N), _ints(csrrows, "A"),
+                                                   _ints(csrcolumns, "C"), _vec(csrvalues, "V"), residual,
+                                                   float(precision), int(print_modulo), _vec(precon, "precon", N),
+                                                   info)
+    return _finish(st, info, "ConjugateGradientSolverCSR_DiagonalPreconditioner")

@@ -14,7 +14,8 @@ import numpy as np
 from . import _native
 
 METHODS = {"cg": _native.METHOD_CG, "ssor": _native.METHOD_SSOR, "rainbow": _native.METHOD_RAINBOW,
-           "ssor_eisenstat": _native.METHOD_SSOR_EISENSTAT, "rainbow_eisenstat": _native.METHOD_RAINBOW_EISENSTAT}
+           "ssor_eisenstat": _native.METHOD_SSOR_EISENSTAT, "rainbow_eisenstat": _native.METHOD_RAINBOW_EISENSTAT,
+           "diagonal": _native.METHOD_DIAGONAL}
 MODES = {"reference": _native.MODE_REFERENCE, "fp64": _native.MODE_FP64, "mixed": _native.MODE_MIXED}
 
 
@@ -58,6 +59,12 @@ class System:
                                                R.ctypes.data_as(ctypes.c_void_p), 1)
         _native.check(st, "feec_system_set_rainbow")
         self.prepared = "rainbow"
+
+    def set_diagonal_precon(self, precon):
+        """The diagonal preconditioner (z = precon * r) of method="diagonal"."""
+        p = np.ascontiguousarray(precon, np.float64)
+        st = self._lib.feec_system_set_diagonal_precon(self._h, p.ctypes.data_as(ctypes.c_void_p), 1)
+        _native.check(st, "feec_system_set_diagonal_precon")
 
     def set_ssor(self, diagonal, omega):
         d = np.ascontiguousarray(diagonal, np.float64)

@@ -11,7 +11,8 @@ compressed ``.npz`` holding:
 * ``MatrixCSR::getDiagonal`` (``diag``) and ``MatrixCSR::apply`` of ``b`` with scaling
   0.7 (``apply_out``);
 * ``Rainbow(A)``: ``rb_nc``, ``rb_F``, ``rb_B``, ``rb_R``;
-* for each solver ``cg``, ``ssor``, ``rainbow``, ``eis`` (SSOR-Eisenstat), ``eisrb``
+* for each solver ``cg``, ``jac`` (diagonal preconditioner 1/diagonal), ``ssor``, ``rainbow``,
+  ``eis`` (SSOR-Eisenstat), ``eisrb``
   (Eisenstat-Rainbow) (and ``ssor13``/``rainbow13``/``eis13``/``eisrb13`` at
   omega = 1.3 where listed): the returned iteration count ``<s>_K``, the solution
   ``<s>_x`` and the residual array ``<s>_res`` written by the reference, at one
@@ -108,7 +109,7 @@ def main():
             run("rainbow", t("m.csr"), t("rb.rb"))
             nc, F, B, R = csrio.read_rainbow(t("rb.rb"))
             out.update(rb_nc=np.int64(nc), rb_F=F, rb_B=B, rb_R=R)
-            solves = [("cg", "cg", 1.0), ("ssor", "ssor", 1.0), ("rainbow", "rainbow", 1.0),
+            solves = [("cg", "cg", 1.0), ("jac", "diag", 1.0), ("ssor", "ssor", 1.0), ("rainbow", "rainbow", 1.0),
                       ("eis", "eisenstat", 1.0), ("eisrb", "eisenstat_rainbow", 1.0)]
             for om in omegas:
                 tag = str(om).replace(".", "")

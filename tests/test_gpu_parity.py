@@ -57,6 +57,11 @@ def _run_dropin(g, key):
     om = float(g[key + "_omega"])
     if key == "cg":
         K = S.ConjugateGradientSolverCSR(n, x, g["b"], g["A"], g["C"], g["V"], res, prec, -3)
+    elif key == "jac":
+        d = g["diag"]
+        precon = np.where(d != 0, 1.0 / np.where(d != 0, d, 1.0), 0.0)
+        K = S.ConjugateGradientSolverCSR_DiagonalPreconditioner(n, x, g["b"], g["A"], g["C"], g["V"], res, prec, -3,
+                                                               precon)
     elif key.startswith("ssor"):
         K = S.ConjugateGradientSolverCSR_SSOR(n, x, g["b"], g["A"], g["C"], g["V"], res, prec, -3, g["diag"], om)
     elif key.startswith("eisrb"):

@@ -45,6 +45,7 @@ def test_dropin_exports_reference_mangled_names(built):
                     "_Z31ConjugateGradientSolverCSR_SSORiPdPKdPKiS3_S1_S_diS1_d",
                     "_Z34ConjugateGradientSolverCSR_RainbowiPdPKdPKiS3_S1_S_diS1_diS3_S3_S3_",
                     "_Z41ConjugateGradientSolverCSR_SSOR_EisenstatiPdPKdPKiS3_S1_S_diS1_d",
+                    "_Z49ConjugateGradientSolverCSR_DiagonalPreconditioneriPdPKdPKiS3_S1_S_diS1_",
                     "_Z44ConjugateGradientSolverCSR_Eisenstat_RainbowiPdPKdPKiS3_S1_S_diS1_diS3_S3_S3_"]:
         assert mangled in out, mangled
 

@@ -2,8 +2,8 @@
 outputs stored in tests/golden (written by tests/golden/make_golden.py from the
 compiled reference). At one OpenMP thread the restatement must reproduce the
 reference bit for bit: iteration counts, solutions, residual arrays, SpMV,
-diagonal and the Rainbow ordering, for all five CG drivers (plain, SSOR, Rainbow,
-SSOR-Eisenstat, Eisenstat-Rainbow)."""
+diagonal and the Rainbow ordering, for all six CG drivers (plain, diagonal
+preconditioner, SSOR, Rainbow, SSOR-Eisenstat, Eisenstat-Rainbow)."""
 import numpy as np
 import pytest
 
@@ -41,6 +41,9 @@ def test_oracle_solvers_bitexact(O, name):
         om = float(g[key + "_omega"])
         if key == "cg":
             K, x, r = O.cg(A, C, V, b, precision=prec)
+        elif key == "jac":
+            K, x, r = O.cg_diag(A, C, V, b, np.where(diag != 0, 1.0 / np.where(diag != 0, diag, 1.0), 0.0),
+                                precision=prec)
         elif key.startswith("ssor"):
             K, x, r = O.cg_ssor(A, C, V, b, diag, om, precision=prec)
         elif key.startswith("eisrb"):
