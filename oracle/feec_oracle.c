@@ -667,6 +667,158 @@ int oracle_cg_eisenstat_rainbow(int N, double* x, const double* b, const int* A,
     return K;
 }
 
+/* ---------------------------------------------------------------------------
+ * CSR algebra (the step before the solver path)
+ * ------------------------------------------------------------------------- */
+
+/* sparse/matcsr.cpp:585-688 (sort_and_compress_csrdata_reduced), in place: per row, an
+ * exchange sort by column that merges equal columns into the first (the later one set
+ * to 0), a bubble pass that moves zeros to the end, the row keeps its entries before the
+ * first zero; then the rows are compacted and A rebuilt. Returns the new entry count. */
+int oracle_csr_compress(int rows, int* A, int* C, double* V)
+{
+    int* nnz = (int*)malloc((size_t)(rows > 0 ? rows : 1) * sizeof(int));
+    if (!nnz) return -1;
+    #pragma omp parallel for
+    for (int r = 0; r < rows; r++) {
+        for (int i = A[r]; i < A[r + 1]; i++)
+            for (int j = i + 1; j < A[r + 1]; j++) {
+                if (C[i] == C[j]) { V[i] += V[j]; V[j] = 0.0; continue; }
+                if (C[i] > C[j]) {
+                    const int tc = C[i]; C[i] = C[j]; C[j] = tc;
+                    const double tv = V[i]; V[i] = V[j]; V[j] = tv;
+                }
+            }
+        for (int i = A[r]; i < A[r + 1]; i++)
+            for (int j = A[r] + 1; j < A[r + 1]; j++)
+                if (V[j - 1] == 0.0 && V[j] != 0.0) {
+                    const int tc = C[j - 1]; C[j - 1] = C[j]; C[j] = tc;
+                    const double tv = V[j - 1]; V[j - 1] = V[j]; V[j] = tv;
+                }
+        int first_zero = A[r];
+        while (first_zero < A[r + 1] && V[first_zero] != 0.0) first_zero++;
+        nnz[r] = first_zero - A[r];
+    }
+    int target = 0;
+    for (int r = 0; r < rows; r++)
+        for (int i = A[r]; i < A[r] + nnz[r]; i++) { C[target] = C[i]; V[target] = V[i]; target++; }
+    for (int r = 0; r < rows; r++) A[r + 1] = nnz[r];
+    A[0] = 0;
+    for (int r = 1; r <= rows; r++) A[r] += A[r - 1];
+    free(nnz);
+    return A[rows];
+}
+
+/* sparse/matcsr.cpp:707-765, MatrixCSRAddition: s1 * mat1 + s2 * mat2 (same shape). The
+ * outputs hold A1[rows] + A2[rows] entries before compression; returns the final count. */
+int oracle_csr_add(int rows, const int* A1, const int* C1, const double* V1, const int* A2, const int* C2,
+                   const double* V2, double s1, double s2, int* A, int* C, double* V)
+{
+    A[0] = 0;
+    for (int r = 1; r <= rows; r++) A[r] = A[r - 1] + (A1[r] - A1[r - 1]) + (A2[r] - A2[r - 1]);
+    for (int r = 0; r < rows; r++) {
+        int i = 0;
+        for (int c1 = A1[r]; c1 < A1[r + 1]; c1++) C[A[r] + (i++)] = C1[c1];
+        for (int c2 = A2[r]; c2 < A2[r + 1]; c2++) C[A[r] + (i++)] = C2[c2];
+    }
+    for (int r = 0; r < rows; r++) {
+        int i = 0;
+        for (int v1 = A1[r]; v1 < A1[r + 1]; v1++) V[A[r] + (i++)] = s1 * V1[v1];
+        for (int v2 = A2[r]; v2 < A2[r + 1]; v2++) V[A[r] + (i++)] = s2 * V2[v2];
+    }
+    return oracle_csr_compress(rows, A, C, V);
+}
+
+/* sparse/matcsr.cpp:767-796: entries of mat1 * mat2 before compression (the capacity the
+ * outputs of oracle_csr_multiply need). */
+long long oracle_csr_multiply_size(int rows, const int* A1, const int* C1, const int* A2)
+{
+    long long total = 0;
+    for (int r = 0; r < rows; r++)
+        for (int c1 = A1[r]; c1 < A1[r + 1]; c1++) total += A2[C1[c1] + 1] - A2[C1[c1]];
+    return total;
+}
+
+/* sparse/matcsr.cpp:767-849, MatrixCSRMultiplication: all products in row order, then
+ * the compression above. Returns the final entry count. */
+int oracle_csr_multiply(int rows, const int* A1, const int* C1, const double* V1, const int* A2, const int* C2,
+                        const double* V2, int* A, int* C, double* V)
+{
+    A[0] = 0;
+    for (int r = 0; r < rows; r++) {
+        int cnt = 0;
+        for (int c1 = A1[r]; c1 < A1[r + 1]; c1++) cnt += A2[C1[c1] + 1] - A2[C1[c1]];
+        A[r + 1] = A[r] + cnt;
+    }
+    #pragma omp parallel for
+    for (int r = 0; r < rows; r++) {
+        int cur = A[r];
+        for (int c1 = A1[r]; c1 < A1[r + 1]; c1++)
+            for (int c2 = A2[C1[c1]]; c2 < A2[C1[c1] + 1]; c2++) {
+                C[cur] = C2[c2];
+                V[cur] = V1[c1] * V2[c2];
+                cur++;
+            }
+    }
+    return oracle_csr_compress(rows, A, C, V);
+}
+
+/* sparse/matcsr.cpp:291-350, MatrixCSR::getTranspose: entries bucketed by column, each
+ * column filled from its end in row order, then the compression above. Returns the count. */
+int oracle_csr_transpose(int rows, int cols, const int* A, const int* C, const double* V, int* B, int* D, double* W)
+{
+    const int nnz = A[rows];
+    int* Z = (int*)calloc((size_t)(cols > 0 ? cols : 1), sizeof(int));
+    if (!Z) return -1;
+    for (int i = 0; i < nnz; i++) Z[C[i]]++;
+    B[0] = 0;
+    for (int c = 1; c <= cols; c++) B[c] = B[c - 1] + Z[c - 1];
+    for (int r = 0; r < rows; r++)
+        for (int i = A[r]; i < A[r + 1]; i++) {
+            const int c = C[i];
+            const int index = --Z[c];
+            D[B[c] + index] = r;
+            W[B[c] + index] = V[i];
+        }
+    free(Z);
+    return oracle_csr_compress(cols, B, D, W);
+}
+
+/* sparse/matcsr.cpp:43-89 with sparse/sparsematrix.cpp:405-458: MatrixCSR(SparseMatrix).
+ * Entries with value 0 are dropped, the rest sorted by (row, column) and equal positions
+ * summed in sorted order (the reference's std::sort leaves equal keys in an unspecified
+ * order; this sort is stable, so equal keys are summed in input order), then laid out as
+ * CSR. Returns the entry count (A, C, V need `count` entries of room). */
+typedef struct { int r, c; double v; long long i; } OracleEntry;
+static int entry_cmp(const void* pa, const void* pb)
+{
+    const OracleEntry* a = (const OracleEntry*)pa; const OracleEntry* b = (const OracleEntry*)pb;
+    if (a->r != b->r) return a->r < b->r ? -1 : 1;
+    if (a->c != b->c) return a->c < b->c ? -1 : 1;
+    return a->i < b->i ? -1 : (a->i > b->i);
+}
+int oracle_coo_to_csr(int rows, long long count, const int* r, const int* c, const double* v, int* A, int* C,
+                      double* V)
+{
+    OracleEntry* e = (OracleEntry*)malloc((size_t)(count > 0 ? count : 1) * sizeof(OracleEntry));
+    if (!e) return -1;
+    long long m = 0;
+    for (long long i = 0; i < count; i++)
+        if (v[i] != 0.0) { e[m].r = r[i]; e[m].c = c[i]; e[m].v = v[i]; e[m].i = i; m++; }
+    qsort(e, (size_t)m, sizeof(OracleEntry), entry_cmp);
+    long long dest = 0;
+    for (long long src = 1; src < m; src++) {
+        if (e[src].r == e[dest].r && e[src].c == e[dest].c) e[dest].v += e[src].v;
+        else e[++dest] = e[src];
+    }
+    const long long n = m > 0 ? dest + 1 : 0;
+    for (int k = 0; k <= rows; k++) A[k] = 0;
+    for (long long i = 0; i < n; i++) { A[e[i].r + 1] += 1; C[i] = e[i].c; V[i] = e[i].v; }
+    for (int k = 1; k <= rows; k++) A[k] += A[k - 1];
+    free(e);
+    return (int)n;
+}
+
 /* Number of OpenMP threads the oracle would use (1 without OpenMP). */
 int oracle_max_threads(void)
 {

@@ -47,6 +47,14 @@ def lib():
         L.oracle_cg_ssor_eisenstat.argtypes = L.oracle_cg_ssor.argtypes
         L.oracle_cg_diag.argtypes = L.oracle_cg.argtypes + [_f64p]
         L.oracle_cg_eisenstat_rainbow.argtypes = L.oracle_cg_rainbow.argtypes
+        L.oracle_csr_compress.argtypes = [ctypes.c_int, _i32p, _i32p, _f64p]
+        L.oracle_csr_add.argtypes = [ctypes.c_int, _i32p, _i32p, _f64p, _i32p, _i32p, _f64p, ctypes.c_double,
+                                     ctypes.c_double, _i32p, _i32p, _f64p]
+        L.oracle_csr_multiply_size.argtypes = [ctypes.c_int, _i32p, _i32p, _i32p]
+        L.oracle_csr_multiply_size.restype = ctypes.c_longlong
+        L.oracle_csr_multiply.argtypes = [ctypes.c_int, _i32p, _i32p, _f64p, _i32p, _i32p, _f64p, _i32p, _i32p, _f64p]
+        L.oracle_csr_transpose.argtypes = [ctypes.c_int, ctypes.c_int, _i32p, _i32p, _f64p, _i32p, _i32p, _f64p]
+        L.oracle_coo_to_csr.argtypes = [ctypes.c_int, ctypes.c_longlong, _i32p, _i32p, _f64p, _i32p, _i32p, _f64p]
         L.oracle_max_threads.restype = ctypes.c_int
         L.oracle_set_threads.argtypes = [ctypes.c_int]
         _lib = L
@@ -139,3 +147,43 @@ def cg_diag(A, C, V, b, precon, x0=None, precision=1e-10):
     K = lib().oracle_cg_diag(n, x, np.ascontiguousarray(b, np.float64), A, C, V, res, float(precision), -3,
                              np.ascontiguousarray(precon, np.float64))
     return K, x, res
+
+
+def _i32(a):
+    return np.ascontiguousarray(a, np.int32)
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, np.float64)
+
+
+def csr_add(A1, C1, V1, A2, C2, V2, s1, s2):
+    rows = len(A1) - 1
+    cap = int(A1[-1]) + int(A2[-1])
+    A = np.empty(rows + 1, np.int32); C = np.empty(max(cap, 1), np.int32); V = np.empty(max(cap, 1))
+    n = lib().oracle_csr_add(rows, _i32(A1), _i32(C1), _f64(V1), _i32(A2), _i32(C2), _f64(V2), float(s1), float(s2),
+                             A, C, V)
+    return A, C[:n].copy(), V[:n].copy()
+
+
+def csr_multiply(A1, C1, V1, A2, C2, V2):
+    rows = len(A1) - 1
+    cap = int(lib().oracle_csr_multiply_size(rows, _i32(A1), _i32(C1), _i32(A2)))
+    A = np.empty(rows + 1, np.int32); C = np.empty(max(cap, 1), np.int32); V = np.empty(max(cap, 1))
+    n = lib().oracle_csr_multiply(rows, _i32(A1), _i32(C1), _f64(V1), _i32(A2), _i32(C2), _f64(V2), A, C, V)
+    return A, C[:n].copy(), V[:n].copy()
+
+
+def csr_transpose(A, C, V, cols):
+    rows = len(A) - 1
+    nnz = int(A[-1])
+    B = np.empty(cols + 1, np.int32); D = np.empty(max(nnz, 1), np.int32); W = np.empty(max(nnz, 1))
+    n = lib().oracle_csr_transpose(rows, int(cols), _i32(A), _i32(C), _f64(V), B, D, W)
+    return B, D[:n].copy(), W[:n].copy()
+
+
+def coo_to_csr(rows, r, c, v):
+    count = len(r)
+    A = np.empty(rows + 1, np.int32); C = np.empty(max(count, 1), np.int32); V = np.empty(max(count, 1))
+    n = lib().oracle_coo_to_csr(int(rows), count, _i32(r), _i32(c), _f64(v), A, C, V)
+    return A, C[:n].copy(), V[:n].copy()

@@ -21,6 +21,10 @@
 //   rainbow <in.csr> <out.rb>        Rainbow(A) (sparse/rainbow.cpp:14-130)
 //   apply <in.csr> <in.vec> <scaling> <out.vec>   MatrixCSR::apply (sparse/matcsr.cpp:216-244)
 //   diag <in.csr> <out.vec>          MatrixCSR::getDiagonal (sparse/matcsr.cpp:266-286)
+//   csradd <a.csr> <b.csr> <s1> <s2> <out.csr>   MatrixCSRAddition (sparse/matcsr.cpp:707-765)
+//   csrmul <a.csr> <b.csr> <out.csr>             MatrixCSRMultiplication (sparse/matcsr.cpp:767-849)
+//   csrtrans <a.csr> <out.csr>                   MatrixCSR::getTranspose (sparse/matcsr.cpp:291-350)
+//   coo2csr <in.coo> <out.csr>                   MatrixCSR(SparseMatrix) (sparse/matcsr.cpp:43-89)
 
 #include <chrono>
 #include <cmath>
@@ -273,6 +277,38 @@ int main(int argc, char** argv) {
         FloatVector d = mat.getDiagonal();
         FILE* f = std::fopen(argv[3], "wb"); if (!f) die("cannot write vec");
         write_raw(f, d.raw(), 8 * m.n); std::fclose(f);
+        return 0;
+    }
+    if (cmd == "csradd") {
+        if (argc != 7) die("csradd <a.csr> <b.csr> <s1> <s2> <out.csr>");
+        MatrixCSR a = to_matrix(read_csr(argv[2])), b = to_matrix(read_csr(argv[3]));
+        write_csr(argv[6], from_matrix(MatrixCSRAddition(a, b, std::atof(argv[4]), std::atof(argv[5]))));
+        return 0;
+    }
+    if (cmd == "csrmul") {
+        if (argc != 5) die("csrmul <a.csr> <b.csr> <out.csr>");
+        MatrixCSR a = to_matrix(read_csr(argv[2])), b = to_matrix(read_csr(argv[3]));
+        write_csr(argv[4], from_matrix(MatrixCSRMultiplication(a, b)));
+        return 0;
+    }
+    if (cmd == "csrtrans") {
+        if (argc != 4) die("csrtrans <a.csr> <out.csr>");
+        write_csr(argv[3], from_matrix(to_matrix(read_csr(argv[2])).getTranspose()));
+        return 0;
+    }
+    if (cmd == "coo2csr") {
+        if (argc != 4) die("coo2csr <in.coo> <out.csr>");
+        FILE* f = std::fopen(argv[2], "rb"); if (!f) die("cannot read coo");
+        char magic[8]; if (std::fread(magic, 1, 8, f) != 8 || std::memcmp(magic, "FEECCOO1", 8)) die("bad coo magic");
+        int64_t hdr[3]; if (std::fread(hdr, 8, 3, f) != 3) die("short coo");
+        std::vector<int> r(hdr[2]), c(hdr[2]); std::vector<double> v(hdr[2]);
+        if (std::fread(r.data(), 4, hdr[2], f) != (size_t)hdr[2] || std::fread(c.data(), 4, hdr[2], f) != (size_t)hdr[2] ||
+            std::fread(v.data(), 8, hdr[2], f) != (size_t)hdr[2]) die("short coo data");
+        std::fclose(f);
+        std::vector<SparseMatrix::MatrixEntry> e(hdr[2]);
+        for (int64_t i = 0; i < hdr[2]; i++) e[i] = SparseMatrix::MatrixEntry{r[i], c[i], v[i]};
+        SparseMatrix sm((int)hdr[0], (int)hdr[1], e);
+        write_csr(argv[3], from_matrix(MatrixCSR(sm)));
         return 0;
     }
     die("unknown command");

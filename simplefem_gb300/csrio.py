@@ -5,6 +5,8 @@
 ``.vec``  : raw float64 array.
 ``.sol``  : int64 [N, K], float64 seconds, float64 x[N], float64 residual[N].
 ``.rb``   : int64 [N, num_colors], int32 F[N], int32 B[num_colors+1], int32 R[N].
+``.coo``  : b"FEECCOO1", int64 [rows, cols, count], int32 row[count], int32 col[count],
+            float64 value[count] (``SparseMatrix`` entries, sparse/sparsematrix.hpp:31-38).
 
 The CSR arrays are exactly ``MatrixCSR``'s ``A``/``C``/``V`` (sparse/matcsr.hpp:117-119).
 """
@@ -115,3 +117,11 @@ def write_rainbow(path, nc, F, B, R) -> None:
 
 def exists(path) -> bool:
     return os.path.exists(path)
+
+
+def write_coo(path, rows: int, cols: int, r, c, v) -> None:
+    r = np.ascontiguousarray(r, np.int32); c = np.ascontiguousarray(c, np.int32); v = np.ascontiguousarray(v, np.float64)
+    with _open(path, "wb") as f:
+        f.write(b"FEECCOO1")
+        f.write(np.array([rows, cols, len(r)], np.int64).tobytes())
+        f.write(r.tobytes()); f.write(c.tobytes()); f.write(v.tobytes())

@@ -64,3 +64,21 @@ def test_oracle_planted_mistake_is_caught(O):
     V[100] *= 1.0 + 1e-6
     K, x, _ = O.cg(g["A"], g["C"], V, g["b"], precision=float(g["precision"]))
     assert not np.array_equal(x, g["cg_x"])
+
+
+def test_oracle_csr_algebra_bitexact(O):
+    """MatrixCSRAddition, MatrixCSRMultiplication (square and rectangular),
+    MatrixCSR::getTranspose and MatrixCSR(SparseMatrix) exactly as the reference wrote them."""
+    g = load_golden("csr_algebra")
+    X = (g["X_A"], g["X_C"], g["X_V"]); Y = (g["Y_A"], g["Y_C"], g["Y_V"]); Xr = (g["Xr_A"], g["Xr_C"], g["Xr_V"])
+    cases = {
+        "add": O.csr_add(*X, *Y, 0.7, -1.3),
+        "mul": O.csr_multiply(*X, *Y),
+        "mulr": O.csr_multiply(*Xr, *Y),
+        "tr": O.csr_transpose(*Xr, int(g["Xr_ncols"])),
+        "coo": O.coo_to_csr(len(g["X_A"]) - 1, g["coo_in_r"], g["coo_in_c"], g["coo_in_v"]),
+    }
+    for case, (A, C, V) in cases.items():
+        assert np.array_equal(A, g[case + "_A"]), case
+        assert np.array_equal(C, g[case + "_C"]), case
+        assert np.array_equal(V, g[case + "_V"]), case
