@@ -888,13 +888,19 @@ int feec_csr_apply(int rows, int cols, const int* A, const int* C, const double*
     int st = init_device(dev, s);
     if (st != FEEC_OK) return st;
     DevArena m; m.stream = s;
-    int *dA = nullptr, *dC = nullptr; double *dV = nullptr, *dx = nullptr, *dy = nullptr;
+    int *dA = nullptr, *dC = nullptr, *bad = nullptr; double *dV = nullptr, *dx = nullptr, *dy = nullptr;
+    int bad_h = 0;
     cudaError_t e;
+    // the matrix is checked on the device before the SpMV indexes through it
     if ((e = m.alloc(dA, (size_t)rows + 1)) == cudaSuccess && (e = m.alloc(dC, (size_t)nnz)) == cudaSuccess &&
         (e = m.alloc(dV, (size_t)nnz)) == cudaSuccess && (e = m.alloc(dx, (size_t)cols)) == cudaSuccess &&
-        (e = m.alloc(dy, (size_t)rows)) == cudaSuccess &&
+        (e = m.alloc(dy, (size_t)rows)) == cudaSuccess && (e = m.alloc(bad, 1)) == cudaSuccess &&
+        (e = cudaMemsetAsync(bad, 0, sizeof(int), s)) == cudaSuccess &&
         (e = cudaMemcpyAsync(dA, A, sizeof(int) * ((size_t)rows + 1), cudaMemcpyHostToDevice, s)) == cudaSuccess &&
         (nnz == 0 || (e = cudaMemcpyAsync(dC, C, sizeof(int) * (size_t)nnz, cudaMemcpyHostToDevice, s)) == cudaSuccess) &&
+        (e = launch_validate_csr_cols(rows, cols, nnz, dA, dC, bad, s)) == cudaSuccess &&
+        (e = cudaMemcpyAsync(&bad_h, bad, sizeof(int), cudaMemcpyDeviceToHost, s)) == cudaSuccess &&
+        (e = cudaStreamSynchronize(s)) == cudaSuccess && !bad_h &&
         (nnz == 0 || (e = cudaMemcpyAsync(dV, V, sizeof(double) * (size_t)nnz, cudaMemcpyHostToDevice, s)) == cudaSuccess) &&
         (cols == 0 || (e = cudaMemcpyAsync(dx, src, sizeof(double) * (size_t)cols, cudaMemcpyHostToDevice, s)) == cudaSuccess) &&
         (e = launch_spmv_f64(rows, dA, dC, dV, dx, dy, scaling, pick_lanes((double)nnz / rows), s)) == cudaSuccess &&
@@ -903,6 +909,7 @@ int feec_csr_apply(int rows, int cols, const int* A, const int* C, const double*
     }
     m.release();
     cudaStreamSynchronize(s);
+    if (e == cudaSuccess && bad_h) return FEEC_BADARG;
     return cuda_status(e);
 }
 

@@ -87,6 +87,8 @@ cudaError_t launch_permute_split(int n, const int* A, const int* C, const double
                                  const int* iperm, const int* key, const int* new_rp, int* out_ci,
                                  double* out_v, float* out_v32, int* lsplit, int* usplit, cudaStream_t s);
 cudaError_t launch_validate_csr(int n, int nnz, const int* A, const int* C, int* bad, cudaStream_t s);
+// rows x ncols: row pointers monotone from 0 to nnz, columns in [0, ncols); sets *bad on a violation
+cudaError_t launch_validate_csr_cols(int n, int ncols, int nnz, const int* A, const int* C, int* bad, cudaStream_t s);
 cudaError_t launch_row_lengths(int n, const int* A, const int* perm, int* len, cudaStream_t s);
 cudaError_t launch_exclusive_scan(int n, const int* in, int* out, int* scratch, cudaStream_t s);
 cudaError_t launch_inverse_perm(int n, const int* perm, int* iperm, cudaStream_t s);

@@ -80,7 +80,8 @@ __global__ void diagonal_kernel(int n, const int* __restrict__ A, const int* __r
 
 // Structural check of a square CSR matrix: A[0] == 0, A non-decreasing, A[n] == nnz,
 // 0 <= C < n. Any violation sets *bad (nothing is indexed through unchecked values).
-__global__ void validate_csr_kernel(int n, int nnz, const int* __restrict__ A, const int* __restrict__ C, int* bad) {
+__global__ void validate_csr_kernel(int n, int ncols, int nnz, const int* __restrict__ A, const int* __restrict__ C,
+                                    int* bad) {
     const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     const long long stride = (long long)gridDim.x * blockDim.x;
     for (long long i = tid; i < n; i += stride) {
@@ -90,7 +91,7 @@ __global__ void validate_csr_kernel(int n, int nnz, const int* __restrict__ A, c
     if (tid == 0 && (A[0] != 0 || A[n] != nnz)) atomicExch(bad, 1);
     for (long long j = tid; j < nnz; j += stride) {
         const int c = C[j];
-        if (c < 0 || c >= n) atomicExch(bad, 1);
+        if (c < 0 || c >= ncols) atomicExch(bad, 1);
     }
 }
 
@@ -414,12 +415,16 @@ cudaError_t launch_diagonal_f64(int n, const int* A, const int* C, const double*
     return launch(diagonal_kernel, grid_for(n, kBlock), kBlock, s, n, A, C, V, d);
 }
 
-cudaError_t launch_validate_csr(int n, int nnz, const int* A, const int* C, int* bad, cudaStream_t s) {
+cudaError_t launch_validate_csr_cols(int n, int ncols, int nnz, const int* A, const int* C, int* bad, cudaStream_t s) {
     long long work = (long long)n > (long long)nnz ? n : nnz;
     int grid = grid_for(work, kBlock);
     if (grid > 8192) grid = 8192;
     if (grid < 1) grid = 1;
-    return launch(validate_csr_kernel, grid, kBlock, s, n, nnz, A, C, bad);
+    return launch(validate_csr_kernel, grid, kBlock, s, n, ncols, nnz, A, C, bad);
+}
+
+cudaError_t launch_validate_csr(int n, int nnz, const int* A, const int* C, int* bad, cudaStream_t s) {
+    return launch_validate_csr_cols(n, n, nnz, A, C, bad, s);
 }
 
 cudaError_t launch_row_lengths(int n, const int* A, const int* perm, int* len, cudaStream_t s) {
