@@ -135,6 +135,44 @@ int feec_csr_apply(int rows, int cols, const int* A, const int* C, const double*
 /* Replaces MatrixCSR::getDiagonal, sparse/matcsr.cpp:266-286 (host pointers). */
 int feec_csr_diagonal(int N, const int* A, const int* C, const double* V, double* diagonal);
 
+/* CSR algebra on the GPU (host pointers; inputs checked on the host first, FEEC_BADARG on
+ * row pointers that are not monotone from 0 or columns out of range). Results are the
+ * reference's bit for bit: entries laid out in the reference's order, rows compressed
+ * by the reference's exchange sort (sparse/matcsr.cpp:585-688, sort_and_compress_csrdata_reduced),
+ * entries that sum to zero dropped. *nnz receives the final entry count.
+ *
+ * Replaces MatrixCSRAddition(mat1, mat2, s1, s2), sparse/matcsr.cpp:707-765:
+ * s1 * (A1,C1,V1) + s2 * (A2,C2,V2), both rows x cols. A has rows+1 entries; C and V
+ * need A1[rows] + A2[rows] entries of room. */
+int feec_csr_add(int rows, int cols, const int* A1, const int* C1, const double* V1,
+                 const int* A2, const int* C2, const double* V2, double s1, double s2,
+                 int* A, int* C, double* V, int* nnz);
+
+/* Entries of (rows x inner) * (inner x cols) before compression, sparse/matcsr.cpp:776-796:
+ * the room C and V need for feec_csr_multiply. */
+int feec_csr_multiply_size(int rows, int inner, const int* A1, const int* C1, const int* A2,
+                           long long* size);
+
+/* Replaces MatrixCSRMultiplication(mat1, mat2), sparse/matcsr.cpp:767-849. FEEC_BADARG when
+ * the uncompressed product exceeds INT_MAX entries (the reference's int offsets). */
+int feec_csr_multiply(int rows, int inner, int cols, const int* A1, const int* C1, const double* V1,
+                      const int* A2, const int* C2, const double* V2,
+                      int* A, int* C, double* V, int* nnz);
+
+/* Replaces MatrixCSR::getTranspose, sparse/matcsr.cpp:291-350: (A,C,V) rows x cols to
+ * (B,D,W) cols x rows. B has cols+1 entries; D and W need A[rows] entries of room. */
+int feec_csr_transpose(int rows, int cols, const int* A, const int* C, const double* V,
+                       int* B, int* D, double* W, int* nnz);
+
+/* Replaces MatrixCSR(const SparseMatrix&), sparse/matcsr.cpp:43-89 with
+ * SparseMatrix::sortandcompressentries, sparse/sparsematrix.cpp:405-458: `count` COO
+ * entries (row r[i], column c[i], value v[i]) to CSR; zero values dropped, entries at the
+ * same position summed in input order (the reference's std::sort leaves that order
+ * unspecified, so sums of duplicates can differ from it in the last bit). A has rows+1
+ * entries; C and V need `count` entries of room. */
+int feec_coo_to_csr(int rows, int cols, long long count, const int* r, const int* c, const double* v,
+                    int* A, int* C, double* V, int* nnz);
+
 /* Replaces Rainbow::Rainbow(mat, do_shuffle = false), sparse/rainbow.cpp:14-130.
  * F[N], B[N+1] (num_colors+1 entries used), R[N], host pointers; bit-identical
  * to the reference's greedy coloring. */

@@ -81,6 +81,12 @@ def gpu():
         L.feec_cg_csr_eisenstat_rainbow.argtypes = L.feec_cg_csr_rainbow.argtypes
         L.feec_csr_apply.argtypes = [_ip, _ip, _i32p, _i32p, _f64p, _f64p, _f64p, _dp]
         L.feec_csr_diagonal.argtypes = [_ip, _i32p, _i32p, _f64p, _f64p]
+        _cp = ctypes.POINTER(ctypes.c_int)
+        L.feec_csr_add.argtypes = [_ip, _ip, _i32p, _i32p, _f64p, _i32p, _i32p, _f64p, _dp, _dp, _i32p, _i32p, _f64p, _cp]
+        L.feec_csr_multiply_size.argtypes = [_ip, _ip, _i32p, _i32p, _i32p, ctypes.POINTER(ctypes.c_longlong)]
+        L.feec_csr_multiply.argtypes = [_ip, _ip, _ip, _i32p, _i32p, _f64p, _i32p, _i32p, _f64p, _i32p, _i32p, _f64p, _cp]
+        L.feec_csr_transpose.argtypes = [_ip, _ip, _i32p, _i32p, _f64p, _i32p, _i32p, _f64p, _cp]
+        L.feec_coo_to_csr.argtypes = [_ip, _ip, ctypes.c_longlong, _i32p, _i32p, _f64p, _i32p, _i32p, _f64p, _cp]
         L.feec_rainbow.argtypes = [_ip, _i32p, _i32p, ctypes.POINTER(ctypes.c_int), _i32p, _i32p, _i32p]
         L.feec_csr_check.argtypes = [_ip, _ip, _i32p, _i32p, _f64p]
         L.feec_system_create.argtypes = [ctypes.POINTER(_vp), _ip, _vp, _vp, _vp, _ip, _vp]

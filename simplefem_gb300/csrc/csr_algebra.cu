@@ -1,0 +1,435 @@
+// CSR algebra on the device — the step before the solver path in FEEC++ (assembly of
+// stiffness and mass matrices as products and sums of FEEC operators):
+//
+//   feec_csr_add        MatrixCSRAddition            (sparse/matcsr.cpp:707-765)
+//   feec_csr_multiply   MatrixCSRMultiplication      (sparse/matcsr.cpp:767-849)
+//   feec_csr_transpose  MatrixCSR::getTranspose      (sparse/matcsr.cpp:291-350)
+//   feec_coo_to_csr     MatrixCSR(const SparseMatrix&) (sparse/matcsr.cpp:43-89,
+//                       with SparseMatrix::sortandcompressentries, sparsematrix.cpp:405-458)
+//
+// The reference builds every result by laying the entries of each row out in a fixed
+// order and then compressing rows with sort_and_compress_csrdata_reduced
+// (sparse/matcsr.cpp:585-688): an exchange sort that merges equal columns into the
+// first (zeroing the later one), then the nonzeros kept in order. Which entries meet in
+// which order decides the rounding of merged sums, so the device lays entries out in
+// the same order and runs the same per-row exchange sort, one thread per row; its
+// results are bit-identical to the reference's. (The reference's final zero bubble pass
+// is a stable partition of nonzeros before zeros; the device does that partition
+// directly.) The expansions, counts and prefix sums around it are parallel.
+//
+// COO -> CSR: the reference sorts entries with std::sort, which leaves entries of equal
+// (row, column) in an unspecified order; here equal positions are summed in input
+// order (an ordering the device makes deterministic), so sums of duplicates may differ
+// from the reference's in rounding while the structure is identical.
+//
+// Entry points take host pointers, like feec_csr_apply; inputs are checked on the host
+// (row pointers monotone from 0, columns in range) before any kernel indexes through them.
+#include <algorithm>
+#include <climits>
+#include <vector>
+
+#include "feec_device.cuh"
+#include "feec_internal.h"
+#include "feec_system.h"
+
+namespace feec {
+namespace {
+
+constexpr int kAlgBlock = 256;
+
+int grid_of(long long n) { return (int)std::max<long long>(1, (n + kAlgBlock - 1) / kAlgBlock); }
+
+// The reference's per-row compression (sparse/matcsr.cpp:600-657) on C[lo, hi), V[lo, hi):
+// returns the number of entries kept (the nonzeros, moved to the front in order).
+__device__ int compress_row(int* C, double* V, int lo, int hi) {
+    for (int i = lo; i < hi; i++) {
+        int ci = C[i];
+        double vi = V[i];
+        for (int j = i + 1; j < hi; j++) {
+            const int cj = C[j];
+            if (ci == cj) { vi += V[j]; V[j] = 0.0; continue; }
+            if (ci > cj) { const double vj = V[j]; C[j] = ci; V[j] = vi; ci = cj; vi = vj; }
+        }
+        C[i] = ci; V[i] = vi;
+    }
+    int k = lo;
+    for (int i = lo; i < hi; i++)
+        if (V[i] != 0.0) { C[k] = C[i]; V[k] = V[i]; k++; }
+    return k - lo;
+}
+
+__global__ void compress_rows_kernel(int rows, const int* __restrict__ A, int* C, double* V, int* __restrict__ cnt) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r < rows) cnt[r] = compress_row(C, V, A[r], A[r + 1]);
+}
+
+// Compaction: the first cnt[r] entries of row r move to the exclusive prefix offset.
+__global__ void compact_rows_kernel(int rows, const int* __restrict__ A, const int* __restrict__ cnt,
+                                    const int* __restrict__ off, const int* __restrict__ C, const double* __restrict__ V,
+                                    int* __restrict__ Co, double* __restrict__ Vo, int* __restrict__ Ao) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= rows) return;
+    const int src = A[r], dst = off[r], k = cnt[r];
+    for (int i = 0; i < k; i++) { Co[dst + i] = C[src + i]; Vo[dst + i] = V[src + i]; }
+    Ao[r] = dst;
+    if (r == rows - 1) Ao[rows] = dst + k;
+}
+
+__global__ void add_layout_kernel(int rows, const int* __restrict__ A1, const int* __restrict__ C1,
+                                  const double* __restrict__ V1, const int* __restrict__ A2, const int* __restrict__ C2,
+                                  const double* __restrict__ V2, double s1, double s2, const int* __restrict__ A,
+                                  int* __restrict__ C, double* __restrict__ V) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= rows) return;
+    int k = A[r];
+    for (int c1 = A1[r]; c1 < A1[r + 1]; c1++) { C[k] = C1[c1]; V[k] = s1 * V1[c1]; k++; }
+    for (int c2 = A2[r]; c2 < A2[r + 1]; c2++) { C[k] = C2[c2]; V[k] = s2 * V2[c2]; k++; }
+}
+
+__global__ void add_lengths_kernel(int rows, const int* __restrict__ A1, const int* __restrict__ A2, int* __restrict__ len) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r < rows) len[r] = (A1[r + 1] - A1[r]) + (A2[r + 1] - A2[r]);
+}
+
+__global__ void mul_lengths_kernel(int rows, const int* __restrict__ A1, const int* __restrict__ C1,
+                                   const int* __restrict__ A2, long long* __restrict__ len) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= rows) return;
+    long long n = 0;
+    for (int c1 = A1[r]; c1 < A1[r + 1]; c1++) n += A2[C1[c1] + 1] - A2[C1[c1]];
+    len[r] = n;
+}
+
+// Products of row r in the reference's order (:819-832).
+__global__ void mul_layout_kernel(int rows, const int* __restrict__ A1, const int* __restrict__ C1,
+                                  const double* __restrict__ V1, const int* __restrict__ A2, const int* __restrict__ C2,
+                                  const double* __restrict__ V2, const int* __restrict__ A, int* __restrict__ C,
+                                  double* __restrict__ V) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= rows) return;
+    int k = A[r];
+    for (int c1 = A1[r]; c1 < A1[r + 1]; c1++) {
+        const int m = C1[c1];
+        const double v1 = V1[c1];
+        for (int c2 = A2[m]; c2 < A2[m + 1]; c2++) { C[k] = C2[c2]; V[k] = v1 * V2[c2]; k++; }
+    }
+}
+
+__global__ void count_keys_kernel(long long n, const int* __restrict__ key, const unsigned char* __restrict__ keep,
+                                  int* __restrict__ cnt) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i < n && (!keep || keep[i])) atomicAdd(&cnt[key[i]], 1);
+}
+
+// Scatter of entry indices into buckets (order inside a bucket is arbitrary; the bucket
+// is sorted by entry index afterwards, which makes the result deterministic).
+__global__ void bucket_kernel(long long n, const int* __restrict__ key, const unsigned char* __restrict__ keep,
+                              const int* __restrict__ start, int* __restrict__ fill, long long* __restrict__ idx) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= n || (keep && !keep[i])) return;
+    const int b = key[i];
+    const int pos = atomicAdd(&fill[b], 1);
+    idx[start[b] + pos] = i;
+}
+
+// Sort the entry indices of each bucket: ascending (COO rows: input order), or descending
+// (transpose columns: the reference fills a column from its end in row order, :319-338).
+__global__ void sort_bucket_kernel(int nb, const int* __restrict__ start, long long* idx, int descending) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nb) return;
+    const int lo = start[b], hi = start[b + 1];
+    for (int i = lo + 1; i < hi; i++) {
+        const long long v = idx[i];
+        int j = i - 1;
+        while (j >= lo && (descending ? idx[j] < v : idx[j] > v)) { idx[j + 1] = idx[j]; j--; }
+        idx[j + 1] = v;
+    }
+}
+
+// Transpose: entry i of the CSR (row row_of[i]) goes to its column's bucket position.
+__global__ void transpose_fill_kernel(int ncols, const int* __restrict__ B, const long long* __restrict__ idx,
+                                      const int* __restrict__ row_of, const double* __restrict__ V, int* __restrict__ D,
+                                      double* __restrict__ W) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= ncols) return;
+    for (int k = B[c]; k < B[c + 1]; k++) { const long long i = idx[k]; D[k] = row_of[i]; W[k] = V[i]; }
+}
+
+__global__ void row_of_kernel(int rows, const int* __restrict__ A, int* __restrict__ row_of) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= rows) return;
+    for (int i = A[r]; i < A[r + 1]; i++) row_of[i] = r;
+}
+
+__global__ void nonzero_kernel(long long n, const double* __restrict__ v, unsigned char* __restrict__ keep) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i < n) keep[i] = v[i] != 0.0;
+}
+
+// COO row: entries (in input order) sorted by column (stable), equal columns summed in
+// that order (sparsematrix.cpp:430-452), written to C/V from the bucket start.
+__global__ void coo_row_kernel(int rows, const int* __restrict__ start, long long* idx, const int* __restrict__ col,
+                               const double* __restrict__ val, int* __restrict__ C, double* __restrict__ V,
+                               int* __restrict__ cnt) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= rows) return;
+    const int lo = start[r], hi = start[r + 1];
+    for (int i = lo + 1; i < hi; i++) {           // stable insertion sort by column
+        const long long v = idx[i];
+        const int cv = col[v];
+        int j = i - 1;
+        while (j >= lo && col[idx[j]] > cv) { idx[j + 1] = idx[j]; j--; }
+        idx[j + 1] = v;
+    }
+    int k = lo;
+    for (int i = lo; i < hi; i++) {
+        const long long e = idx[i];
+        if (k > lo && C[k - 1] == col[e]) V[k - 1] += val[e];
+        else { C[k] = col[e]; V[k] = val[e]; k++; }
+    }
+    cnt[r] = k - lo;
+}
+
+__global__ void ll_to_int_kernel(int n, const long long* __restrict__ in, int* __restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = (int)in[i];
+}
+
+// Host-side checks of a CSR given by host pointers.
+bool csr_ok(int rows, int cols, const int* A, const int* C) {
+    if (rows < 0 || cols < 0 || !A || A[0] != 0) return false;
+    for (int r = 0; r < rows; r++) if (A[r + 1] < A[r]) return false;
+    const int nnz = A[rows];
+    if (nnz > 0 && !C) return false;
+    for (int i = 0; i < nnz; i++) if (C[i] < 0 || C[i] >= cols) return false;
+    return true;
+}
+
+// Compress the rows laid out at (dA, dC, dV), compact them into (oA, oC, oV) on the device.
+int compress_and_compact(DevArena& m, cudaStream_t s, int rows, int* dA, int* dC, double* dV, int*& oA, int*& oC,
+                         double*& oV, int& nnz_out) {
+    int *cnt = nullptr, *off = nullptr, *scr = nullptr;
+    FEEC_TRY(m.alloc(cnt, (size_t)rows + 1)); FEEC_TRY(m.alloc(off, (size_t)rows + 1));
+    FEEC_TRY(m.alloc(scr, scan_scratch_ints(rows + 1)));
+    FEEC_TRY(cudaMemsetAsync(cnt + rows, 0, sizeof(int), s));
+    note_launch();
+    compress_rows_kernel<<<grid_of(rows), kAlgBlock, 0, s>>>(rows, dA, dC, dV, cnt);
+    FEEC_TRY(cudaGetLastError());
+    FEEC_TRY(launch_exclusive_scan(rows + 1, cnt, off, scr, s));
+    FEEC_TRY(cudaMemcpyAsync(&nnz_out, off + rows, sizeof(int), cudaMemcpyDeviceToHost, s));
+    FEEC_TRY(cudaStreamSynchronize(s));
+    FEEC_TRY(m.alloc(oA, (size_t)rows + 1)); FEEC_TRY(m.alloc(oC, (size_t)std::max(nnz_out, 1)));
+    FEEC_TRY(m.alloc(oV, (size_t)std::max(nnz_out, 1)));
+    if (rows == 0) FEEC_TRY(cudaMemsetAsync(oA, 0, sizeof(int), s));
+    note_launch();
+    compact_rows_kernel<<<grid_of(rows), kAlgBlock, 0, s>>>(rows, dA, cnt, off, dC, dV, oC, oV, oA);
+    FEEC_TRY(cudaGetLastError());
+    return FEEC_OK;
+}
+
+int download(cudaStream_t s, int rows, int nnz, const int* oA, const int* oC, const double* oV, int* A, int* C,
+             double* V) {
+    FEEC_TRY(cudaMemcpyAsync(A, oA, sizeof(int) * ((size_t)rows + 1), cudaMemcpyDeviceToHost, s));
+    if (nnz > 0) {
+        FEEC_TRY(cudaMemcpyAsync(C, oC, sizeof(int) * (size_t)nnz, cudaMemcpyDeviceToHost, s));
+        FEEC_TRY(cudaMemcpyAsync(V, oV, sizeof(double) * (size_t)nnz, cudaMemcpyDeviceToHost, s));
+    }
+    FEEC_TRY(cudaStreamSynchronize(s));
+    return FEEC_OK;
+}
+
+template <typename T>
+int upload(DevArena& m, cudaStream_t s, T*& d, const T* h, size_t n) {
+    FEEC_TRY(m.alloc(d, std::max<size_t>(n, 1)));
+    if (n) FEEC_TRY(cudaMemcpyAsync(d, h, sizeof(T) * n, cudaMemcpyHostToDevice, s));
+    return FEEC_OK;
+}
+
+struct Scope {   // device arena released and the stream drained on every return path
+    DevArena m;
+    cudaStream_t s;
+    ~Scope() { m.release(); cudaStreamSynchronize(s); }
+};
+
+}  // namespace
+}  // namespace feec
+
+using namespace feec;
+
+extern "C" {
+
+int feec_csr_add(int rows, int cols, const int* A1, const int* C1, const double* V1, const int* A2, const int* C2,
+                 const double* V2, double s1, double s2, int* A, int* C, double* V, int* nnz) {
+    if (!csr_ok(rows, cols, A1, C1) || !csr_ok(rows, cols, A2, C2) || !A || !nnz) return FEEC_BADARG;
+    const long long cap = (long long)A1[rows] + A2[rows];
+    if (cap > INT_MAX || (cap > 0 && (!C || !V || (A1[rows] > 0 && !V1) || (A2[rows] > 0 && !V2)))) return FEEC_BADARG;
+    int dev = 0; cudaStream_t s = nullptr;
+    int st = init_device(dev, s);
+    if (st != FEEC_OK) return st;
+    Scope sc{DevArena{}, s}; sc.m.stream = s;
+    int *dA1, *dC1, *dA2, *dC2; double *dV1, *dV2;
+    if ((st = upload(sc.m, s, dA1, A1, (size_t)rows + 1)) || (st = upload(sc.m, s, dC1, C1, (size_t)A1[rows])) ||
+        (st = upload(sc.m, s, dV1, V1, (size_t)A1[rows])) || (st = upload(sc.m, s, dA2, A2, (size_t)rows + 1)) ||
+        (st = upload(sc.m, s, dC2, C2, (size_t)A2[rows])) || (st = upload(sc.m, s, dV2, V2, (size_t)A2[rows])))
+        return st;
+    int *len, *dA, *dC, *scr; double* dV;
+    FEEC_TRY(sc.m.alloc(len, (size_t)rows + 1)); FEEC_TRY(sc.m.alloc(dA, (size_t)rows + 1));
+    FEEC_TRY(sc.m.alloc(scr, scan_scratch_ints(rows + 1)));
+    FEEC_TRY(sc.m.alloc(dC, (size_t)std::max<long long>(cap, 1))); FEEC_TRY(sc.m.alloc(dV, (size_t)std::max<long long>(cap, 1)));
+    FEEC_TRY(cudaMemsetAsync(len + rows, 0, sizeof(int), s));
+    note_launch();
+    add_lengths_kernel<<<grid_of(rows), kAlgBlock, 0, s>>>(rows, dA1, dA2, len);
+    FEEC_TRY(cudaGetLastError());
+    FEEC_TRY(launch_exclusive_scan(rows + 1, len, dA, scr, s));
+    note_launch();
+    add_layout_kernel<<<grid_of(rows), kAlgBlock, 0, s>>>(rows, dA1, dC1, dV1, dA2, dC2, dV2, s1, s2, dA, dC, dV);
+    FEEC_TRY(cudaGetLastError());
+    int *oA, *oC; double* oV; int n = 0;
+    if ((st = compress_and_compact(sc.m, s, rows, dA, dC, dV, oA, oC, oV, n)) != FEEC_OK) return st;
+    if ((st = download(s, rows, n, oA, oC, oV, A, C, V)) != FEEC_OK) return st;
+    *nnz = n;
+    return FEEC_OK;
+}
+
+int feec_csr_multiply_size(int rows, int inner, const int* A1, const int* C1, const int* A2, long long* size) {
+    if (!csr_ok(rows, inner, A1, C1) || !A2 || !size) return FEEC_BADARG;
+    for (int r = 0; r < inner; r++) if (A2[r + 1] < A2[r] || A2[0] != 0) return FEEC_BADARG;
+    long long total = 0;
+    for (int r = 0; r < rows; r++)
+        for (int c1 = A1[r]; c1 < A1[r + 1]; c1++) total += A2[C1[c1] + 1] - A2[C1[c1]];
+    *size = total;
+    return FEEC_OK;
+}
+
+int feec_csr_multiply(int rows, int inner, int cols, const int* A1, const int* C1, const double* V1, const int* A2,
+                      const int* C2, const double* V2, int* A, int* C, double* V, int* nnz) {
+    if (!csr_ok(rows, inner, A1, C1) || !csr_ok(inner, cols, A2, C2) || !A || !nnz) return FEEC_BADARG;
+    if ((A1[rows] > 0 && !V1) || (A2[inner] > 0 && !V2)) return FEEC_BADARG;
+    long long cap = 0;
+    int st = feec_csr_multiply_size(rows, inner, A1, C1, A2, &cap);
+    if (st != FEEC_OK) return st;
+    if (cap > INT_MAX || (cap > 0 && (!C || !V))) return FEEC_BADARG;
+    int dev = 0; cudaStream_t s = nullptr;
+    if ((st = init_device(dev, s)) != FEEC_OK) return st;
+    Scope sc{DevArena{}, s}; sc.m.stream = s;
+    int *dA1, *dC1, *dA2, *dC2; double *dV1, *dV2;
+    if ((st = upload(sc.m, s, dA1, A1, (size_t)rows + 1)) || (st = upload(sc.m, s, dC1, C1, (size_t)A1[rows])) ||
+        (st = upload(sc.m, s, dV1, V1, (size_t)A1[rows])) || (st = upload(sc.m, s, dA2, A2, (size_t)inner + 1)) ||
+        (st = upload(sc.m, s, dC2, C2, (size_t)A2[inner])) || (st = upload(sc.m, s, dV2, V2, (size_t)A2[inner])))
+        return st;
+    long long* len64; int *len, *dA, *dC, *scr; double* dV;
+    FEEC_TRY(sc.m.alloc(len64, (size_t)rows + 1)); FEEC_TRY(sc.m.alloc(len, (size_t)rows + 1));
+    FEEC_TRY(sc.m.alloc(dA, (size_t)rows + 1)); FEEC_TRY(sc.m.alloc(scr, scan_scratch_ints(rows + 1)));
+    FEEC_TRY(sc.m.alloc(dC, (size_t)std::max<long long>(cap, 1))); FEEC_TRY(sc.m.alloc(dV, (size_t)std::max<long long>(cap, 1)));
+    FEEC_TRY(cudaMemsetAsync(len + rows, 0, sizeof(int), s));
+    note_launch();
+    mul_lengths_kernel<<<grid_of(rows), kAlgBlock, 0, s>>>(rows, dA1, dC1, dA2, len64);
+    note_launch();
+    ll_to_int_kernel<<<grid_of(rows), kAlgBlock, 0, s>>>(rows, len64, len);   // cap <= INT_MAX: every row fits
+    FEEC_TRY(cudaGetLastError());
+    FEEC_TRY(launch_exclusive_scan(rows + 1, len, dA, scr, s));
+    note_launch();
+    mul_layout_kernel<<<grid_of(rows), kAlgBlock, 0, s>>>(rows, dA1, dC1, dV1, dA2, dC2, dV2, dA, dC, dV);
+    FEEC_TRY(cudaGetLastError());
+    int *oA, *oC; double* oV; int n = 0;
+    if ((st = compress_and_compact(sc.m, s, rows, dA, dC, dV, oA, oC, oV, n)) != FEEC_OK) return st;
+    if ((st = download(s, rows, n, oA, oC, oV, A, C, V)) != FEEC_OK) return st;
+    *nnz = n;
+    return FEEC_OK;
+}
+
+int feec_csr_transpose(int rows, int cols, const int* A, const int* C, const double* V, int* B, int* D, double* W,
+                       int* nnz) {
+    if (!csr_ok(rows, cols, A, C) || !B || !nnz) return FEEC_BADARG;
+    const int m = A[rows];
+    if (m > 0 && (!V || !D || !W)) return FEEC_BADARG;
+    int dev = 0; cudaStream_t s = nullptr;
+    int st = init_device(dev, s);
+    if (st != FEEC_OK) return st;
+    Scope sc{DevArena{}, s}; sc.m.stream = s;
+    int *dA, *dC; double* dV;
+    if ((st = upload(sc.m, s, dA, A, (size_t)rows + 1)) || (st = upload(sc.m, s, dC, C, (size_t)m)) ||
+        (st = upload(sc.m, s, dV, V, (size_t)m)))
+        return st;
+    int *cnt, *dB, *fill, *row_of, *scr, *dD; long long* idx; double* dW;
+    FEEC_TRY(sc.m.alloc(cnt, (size_t)cols + 1)); FEEC_TRY(sc.m.alloc(dB, (size_t)cols + 1));
+    FEEC_TRY(sc.m.alloc(fill, (size_t)cols + 1)); FEEC_TRY(sc.m.alloc(scr, scan_scratch_ints(cols + 1)));
+    FEEC_TRY(sc.m.alloc(row_of, (size_t)std::max(m, 1))); FEEC_TRY(sc.m.alloc(idx, (size_t)std::max(m, 1)));
+    FEEC_TRY(sc.m.alloc(dD, (size_t)std::max(m, 1))); FEEC_TRY(sc.m.alloc(dW, (size_t)std::max(m, 1)));
+    FEEC_TRY(cudaMemsetAsync(cnt, 0, sizeof(int) * ((size_t)cols + 1), s));
+    FEEC_TRY(cudaMemsetAsync(fill, 0, sizeof(int) * ((size_t)cols + 1), s));
+    note_launch();
+    count_keys_kernel<<<grid_of(m), kAlgBlock, 0, s>>>(m, dC, nullptr, cnt);
+    FEEC_TRY(cudaGetLastError());
+    FEEC_TRY(launch_exclusive_scan(cols + 1, cnt, dB, scr, s));
+    note_launch();
+    row_of_kernel<<<grid_of(rows), kAlgBlock, 0, s>>>(rows, dA, row_of);
+    note_launch();
+    bucket_kernel<<<grid_of(m), kAlgBlock, 0, s>>>(m, dC, nullptr, dB, fill, idx);
+    note_launch();
+    sort_bucket_kernel<<<grid_of(cols), kAlgBlock, 0, s>>>(cols, dB, idx, 1);
+    note_launch();
+    transpose_fill_kernel<<<grid_of(cols), kAlgBlock, 0, s>>>(cols, dB, idx, row_of, dV, dD, dW);
+    FEEC_TRY(cudaGetLastError());
+    int *oA, *oC; double* oV; int n = 0;
+    if ((st = compress_and_compact(sc.m, s, cols, dB, dD, dW, oA, oC, oV, n)) != FEEC_OK) return st;
+    if ((st = download(s, cols, n, oA, oC, oV, B, D, W)) != FEEC_OK) return st;
+    *nnz = n;
+    return FEEC_OK;
+}
+
+int feec_coo_to_csr(int rows, int cols, long long count, const int* r, const int* c, const double* v, int* A, int* C,
+                    double* V, int* nnz) {
+    if (rows < 0 || cols < 0 || count < 0 || count > INT_MAX || !A || !nnz) return FEEC_BADARG;
+    if (count > 0 && (!r || !c || !v || !C || !V)) return FEEC_BADARG;
+    for (long long i = 0; i < count; i++)
+        if (r[i] < 0 || r[i] >= rows || c[i] < 0 || c[i] >= cols) return FEEC_BADARG;
+    int dev = 0; cudaStream_t s = nullptr;
+    int st = init_device(dev, s);
+    if (st != FEEC_OK) return st;
+    Scope sc{DevArena{}, s}; sc.m.stream = s;
+    int *dr, *dc; double* dv;
+    if ((st = upload(sc.m, s, dr, r, (size_t)count)) || (st = upload(sc.m, s, dc, c, (size_t)count)) ||
+        (st = upload(sc.m, s, dv, v, (size_t)count)))
+        return st;
+    unsigned char* keep; int *cnt, *start, *fill, *scr, *dC, *rc; long long* idx; double* dV;
+    FEEC_TRY(sc.m.alloc(keep, (size_t)std::max<long long>(count, 1)));
+    FEEC_TRY(sc.m.alloc(cnt, (size_t)rows + 1)); FEEC_TRY(sc.m.alloc(start, (size_t)rows + 1));
+    FEEC_TRY(sc.m.alloc(fill, (size_t)rows + 1)); FEEC_TRY(sc.m.alloc(scr, scan_scratch_ints(rows + 1)));
+    FEEC_TRY(sc.m.alloc(idx, (size_t)std::max<long long>(count, 1)));
+    FEEC_TRY(sc.m.alloc(dC, (size_t)std::max<long long>(count, 1))); FEEC_TRY(sc.m.alloc(dV, (size_t)std::max<long long>(count, 1)));
+    FEEC_TRY(sc.m.alloc(rc, (size_t)rows + 1));
+    FEEC_TRY(cudaMemsetAsync(cnt, 0, sizeof(int) * ((size_t)rows + 1), s));
+    FEEC_TRY(cudaMemsetAsync(fill, 0, sizeof(int) * ((size_t)rows + 1), s));
+    FEEC_TRY(cudaMemsetAsync(rc, 0, sizeof(int) * ((size_t)rows + 1), s));
+    note_launch();
+    nonzero_kernel<<<grid_of(count), kAlgBlock, 0, s>>>(count, dv, keep);          // zeros dropped (:411-420)
+    note_launch();
+    count_keys_kernel<<<grid_of(count), kAlgBlock, 0, s>>>(count, dr, keep, cnt);
+    FEEC_TRY(cudaGetLastError());
+    FEEC_TRY(launch_exclusive_scan(rows + 1, cnt, start, scr, s));
+    note_launch();
+    bucket_kernel<<<grid_of(count), kAlgBlock, 0, s>>>(count, dr, keep, start, fill, idx);
+    note_launch();
+    sort_bucket_kernel<<<grid_of(rows), kAlgBlock, 0, s>>>(rows, start, idx, 0);
+    note_launch();
+    coo_row_kernel<<<grid_of(rows), kAlgBlock, 0, s>>>(rows, start, idx, dc, dv, dC, dV, rc);
+    FEEC_TRY(cudaGetLastError());
+    // rows now hold their merged entries from start[r]; compact them
+    int *off, *oA, *oC; double* oV; int n = 0;
+    FEEC_TRY(sc.m.alloc(off, (size_t)rows + 1));
+    FEEC_TRY(launch_exclusive_scan(rows + 1, rc, off, scr, s));
+    FEEC_TRY(cudaMemcpyAsync(&n, off + rows, sizeof(int), cudaMemcpyDeviceToHost, s));
+    FEEC_TRY(cudaStreamSynchronize(s));
+    FEEC_TRY(sc.m.alloc(oA, (size_t)rows + 1)); FEEC_TRY(sc.m.alloc(oC, (size_t)std::max(n, 1)));
+    FEEC_TRY(sc.m.alloc(oV, (size_t)std::max(n, 1)));
+    if (rows == 0) FEEC_TRY(cudaMemsetAsync(oA, 0, sizeof(int), s));
+    note_launch();
+    compact_rows_kernel<<<grid_of(rows), kAlgBlock, 0, s>>>(rows, start, rc, off, dC, dV, oC, oV, oA);
+    FEEC_TRY(cudaGetLastError());
+    if ((st = download(s, rows, n, oA, oC, oV, A, C, V)) != FEEC_OK) return st;
+    *nnz = n;
+    return FEEC_OK;
+}
+
+}  // extern "C"

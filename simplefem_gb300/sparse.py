@@ -102,6 +102,69 @@ class MatrixCSR:
         _native.check(_native.gpu().feec_csr_diagonal(self.rows, self.A, self.C, self.V, d), "getDiagonal")
         return FloatVector(d)
 
+    def getTranspose(self) -> "MatrixCSR":
+        """Transpose on the GPU (MatrixCSR::getTranspose, sparse/matcsr.cpp:291-350), bit-identical."""
+        B = np.empty(self.columns + 1, np.int32)
+        D = np.empty(max(self.getnumberofentries(), 1), np.int32)
+        W = np.empty(max(self.getnumberofentries(), 1), np.float64)
+        nnz = ctypes.c_int(0)
+        st = _native.gpu().feec_csr_transpose(self.rows, self.columns, self.A, self.C, self.V, B, D, W,
+                                              ctypes.byref(nnz))
+        _native.check(st, "MatrixCSR::getTranspose")
+        return MatrixCSR(self.columns, self.rows, B, D[:nnz.value], W[:nnz.value])
+
+    @classmethod
+    def from_coo(cls, rows, columns, r, c, v) -> "MatrixCSR":
+        """CSR from coordinate entries (MatrixCSR(const SparseMatrix&), sparse/matcsr.cpp:43-89 with
+        SparseMatrix::sortandcompressentries, sparse/sparsematrix.cpp:405-458) on the GPU: zero
+        values dropped, entries at one position summed in input order."""
+        r = np.ascontiguousarray(r, np.int32)
+        c = np.ascontiguousarray(c, np.int32)
+        v = np.ascontiguousarray(v, np.float64)
+        if not (r.shape == c.shape == v.shape) or r.ndim != 1:
+            raise ValueError("from_coo: r, c and v must be 1-D arrays of one length")
+        A = np.empty(int(rows) + 1, np.int32)
+        C = np.empty(max(r.shape[0], 1), np.int32)
+        V = np.empty(max(r.shape[0], 1), np.float64)
+        nnz = ctypes.c_int(0)
+        st = _native.gpu().feec_coo_to_csr(int(rows), int(columns), r.shape[0], r, c, v, A, C, V, ctypes.byref(nnz))
+        _native.check(st, "MatrixCSR(SparseMatrix)")
+        return cls(rows, columns, A, C[:nnz.value], V[:nnz.value])
+
+
+def MatrixCSRAddition(mat1: MatrixCSR, mat2: MatrixCSR, s1: float = 1.0, s2: float = 1.0) -> MatrixCSR:
+    """s1 * mat1 + s2 * mat2 on the GPU (sparse/matcsr.cpp:707-765), bit-identical to the reference."""
+    if mat1.rows != mat2.rows or mat1.columns != mat2.columns:
+        raise ValueError("MatrixCSRAddition: dimension mismatch")
+    cap = max(mat1.getnumberofentries() + mat2.getnumberofentries(), 1)
+    A = np.empty(mat1.rows + 1, np.int32)
+    C = np.empty(cap, np.int32)
+    V = np.empty(cap, np.float64)
+    nnz = ctypes.c_int(0)
+    st = _native.gpu().feec_csr_add(mat1.rows, mat1.columns, mat1.A, mat1.C, mat1.V, mat2.A, mat2.C, mat2.V,
+                                    float(s1), float(s2), A, C, V, ctypes.byref(nnz))
+    _native.check(st, "MatrixCSRAddition")
+    return MatrixCSR(mat1.rows, mat1.columns, A, C[:nnz.value], V[:nnz.value])
+
+
+def MatrixCSRMultiplication(mat1: MatrixCSR, mat2: MatrixCSR) -> MatrixCSR:
+    """mat1 * mat2 on the GPU (sparse/matcsr.cpp:767-849), bit-identical to the reference."""
+    if mat1.columns != mat2.rows:
+        raise ValueError("MatrixCSRMultiplication: dimension mismatch")
+    L = _native.gpu()
+    size = ctypes.c_longlong(0)
+    _native.check(L.feec_csr_multiply_size(mat1.rows, mat1.columns, mat1.A, mat1.C, mat2.A, ctypes.byref(size)),
+                  "MatrixCSRMultiplication")
+    cap = max(int(size.value), 1)
+    A = np.empty(mat1.rows + 1, np.int32)
+    C = np.empty(cap, np.int32)
+    V = np.empty(cap, np.float64)
+    nnz = ctypes.c_int(0)
+    st = L.feec_csr_multiply(mat1.rows, mat1.columns, mat2.columns, mat1.A, mat1.C, mat1.V, mat2.A, mat2.C, mat2.V,
+                             A, C, V, ctypes.byref(nnz))
+    _native.check(st, "MatrixCSRMultiplication")
+    return MatrixCSR(mat1.rows, mat2.columns, A, C[:nnz.value], V[:nnz.value])
+
 
 class Rainbow:
     """Greedy multicolor ordering of a CSR graph (sparse/rainbow.hpp:13-31, rainbow.cpp:14-130).
