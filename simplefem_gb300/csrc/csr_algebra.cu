@@ -12,8 +12,8 @@
 // (sparse/matcsr.cpp:585-688): an exchange sort that merges equal columns into the
 // first (zeroing the later one), then the nonzeros kept in order. Which entries meet in
 // which order decides the rounding of merged sums, so the device lays entries out in
-// the same order and runs the same per-row exchange sort, one thread per row; its
-// results are bit-identical to the reference's. (The reference's final zero bubble pass
+// the same order and runs the same per-row exchange sort (one warp per row, its passes
+// pipelined across the lanes); its results are bit-identical to the reference's. (The reference's final zero bubble pass
 // is a stable partition of nonzeros before zeros; the device does that partition
 // directly.) The expansions, counts and prefix sums around it are parallel.
 //
@@ -39,51 +39,123 @@ constexpr int kAlgBlock = 256;
 
 int grid_of(long long n) { return (int)std::max<long long>(1, (n + kAlgBlock - 1) / kAlgBlock); }
 
-// The reference's per-row compression (sparse/matcsr.cpp:600-657) on C[lo, hi), V[lo, hi):
-// returns the number of entries kept (the nonzeros, moved to the front in order).
-__device__ int compress_row(int* C, double* V, int lo, int hi) {
-    for (int i = lo; i < hi; i++) {
-        int ci = C[i];
-        double vi = V[i];
-        for (int j = i + 1; j < hi; j++) {
-            const int cj = C[j];
-            if (ci == cj) { vi += V[j]; V[j] = 0.0; continue; }
-            if (ci > cj) { const double vj = V[j]; C[j] = ci; V[j] = vi; ci = cj; vi = vj; }
+constexpr unsigned kFull = 0xffffffffu;
+constexpr int kWarpsPerBlock = 4;
+constexpr int kWarpBlock = kWarpsPerBlock * 32;
+constexpr int kRowCap = 1024;   // entries of one row staged in shared memory per warp (12 KB)
+
+int warp_grid(long long rows) { return (int)std::max<long long>(1, (rows + kWarpsPerBlock - 1) / kWarpsPerBlock); }
+
+// The reference's per-row exchange sort (sparse/matcsr.cpp:601-622) on c[0, L), v[0, L),
+// run by one warp as a systolic pipeline. Pass p of the reference keeps a running
+// minimum (column, value) in a register, scans positions p+1.., merges equal columns
+// into it (zeroing the merged entry) and swaps smaller ones in; at its end the register
+// is stored at position p. Lane k runs pass i+k of a sweep of 32 passes, one step behind
+// lane k-1: it receives each element after lane k-1 has processed it and hands it on.
+// Every pass therefore sees every position in exactly the state the serial sort gives
+// it, and every sum is formed in the serial order: the result is bit-identical, at about
+// L*L/64 warp steps instead of L*L/2 serial ones. Lane 0 reads the stream (one element
+// ahead), lane 31 stores what leaves the pipeline; columns are >= 0, -1 marks no element.
+__device__ void warp_exchange_sort(int* c, double* v, int L, int lane) {
+    for (int i = 0; i < L; i += 32) {
+        int rc = 0; double rv = 0.0;          // register of pass i + lane
+        int pc = -1; double pv = 0.0;         // element this lane hands on (-1: none)
+        int nc = -1; double nv = 0.0;         // lane 0: next element of the stream
+        if (lane == 0) { nc = c[i]; nv = v[i]; }
+        const int steps = (L - i) + 31;
+        for (int s = 0; s < steps; s++) {
+            int xc = __shfl_up_sync(kFull, pc, 1);
+            double xv = __shfl_up_sync(kFull, pv, 1);
+            if (lane == 0) {
+                xc = nc; xv = nv;
+                const int q1 = i + s + 1;
+                if (q1 < L) { nc = c[q1]; nv = v[q1]; } else nc = -1;
+            }
+            pc = -1;
+            if (xc >= 0) {
+                if (s == 2 * lane) { rc = xc; rv = xv; }          // position i + lane: the register
+                else {
+                    if (xc == rc) { rv += xv; xv = 0.0; }
+                    else if (xc < rc) { const int tc = xc; const double tv = xv; xc = rc; xv = rv; rc = tc; rv = tv; }
+                    pc = xc; pv = xv;
+                }
+            }
+            if (lane == 31 && pc >= 0) { const int q = i + s - 31; c[q] = pc; v[q] = pv; pc = -1; }
         }
-        C[i] = ci; V[i] = vi;
+        if (i + lane < L) { c[i + lane] = rc; v[i + lane] = rv; }
+        __syncwarp();
     }
-    int k = lo;
-    for (int i = lo; i < hi; i++)
-        if (V[i] != 0.0) { C[k] = C[i]; V[k] = V[i]; k++; }
-    return k - lo;
 }
 
-__global__ void compress_rows_kernel(int rows, const int* __restrict__ A, int* C, double* V, int* __restrict__ cnt) {
-    const int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r < rows) cnt[r] = compress_row(C, V, A[r], A[r + 1]);
+// The nonzeros of (c, v)[0, L) in order, written to (dc, dv) (which may be c, v
+// themselves: a write never passes the read position); returns their count. This is
+// the reference's zero bubble pass (:624-649), a stable partition of the nonzeros.
+__device__ int warp_keep_nonzeros(const int* c, const double* v, int L, int* dc, double* dv, int lane) {
+    int k = 0;
+    for (int base = 0; base < L; base += 32) {
+        const int q = base + lane;
+        int cq = 0; double vq = 0.0;
+        if (q < L) { cq = c[q]; vq = v[q]; }
+        const bool keep = q < L && vq != 0.0;
+        const unsigned m = __ballot_sync(kFull, keep);
+        __syncwarp();
+        if (keep) { const int d = k + __popc(m & ((1u << lane) - 1u)); dc[d] = cq; dv[d] = vq; }
+        k += __popc(m);
+        __syncwarp();
+    }
+    return k;
 }
 
-// Compaction: the first cnt[r] entries of row r move to the exclusive prefix offset.
+// One warp per row: sort and merge (in shared memory when the row fits), keep the
+// nonzeros at the row's start; cnt[r] = their count.
+__global__ void __launch_bounds__(kWarpBlock)
+compress_rows_kernel(int rows, const int* __restrict__ A, int* C, double* V, int* __restrict__ cnt) {
+    __shared__ int sc[kWarpsPerBlock][kRowCap];
+    __shared__ double sv[kWarpsPerBlock][kRowCap];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int r = blockIdx.x * kWarpsPerBlock + w;
+    if (r >= rows) return;
+    const int lo = A[r], L = A[r + 1] - lo;
+    int k;
+    if (L <= kRowCap) {
+        for (int q = lane; q < L; q += 32) { sc[w][q] = C[lo + q]; sv[w][q] = V[lo + q]; }
+        __syncwarp();
+        warp_exchange_sort(sc[w], sv[w], L, lane);
+        k = warp_keep_nonzeros(sc[w], sv[w], L, C + lo, V + lo, lane);
+    } else {
+        warp_exchange_sort(C + lo, V + lo, L, lane);
+        k = warp_keep_nonzeros(C + lo, V + lo, L, C + lo, V + lo, lane);
+    }
+    if (lane == 0) cnt[r] = k;
+}
+
+// Compaction, one warp per row: the first cnt[r] entries of row r move to the
+// exclusive prefix offset off[r].
 __global__ void compact_rows_kernel(int rows, const int* __restrict__ A, const int* __restrict__ cnt,
                                     const int* __restrict__ off, const int* __restrict__ C, const double* __restrict__ V,
                                     int* __restrict__ Co, double* __restrict__ Vo, int* __restrict__ Ao) {
-    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    const int r = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
     if (r >= rows) return;
     const int src = A[r], dst = off[r], k = cnt[r];
-    for (int i = 0; i < k; i++) { Co[dst + i] = C[src + i]; Vo[dst + i] = V[src + i]; }
-    Ao[r] = dst;
-    if (r == rows - 1) Ao[rows] = dst + k;
+    for (int t = lane; t < k; t += 32) { Co[dst + t] = C[src + t]; Vo[dst + t] = V[src + t]; }
+    if (lane == 0) {
+        Ao[r] = dst;
+        if (r == rows - 1) Ao[rows] = dst + k;
+    }
 }
 
+// s1 * row r of the first matrix, then s2 * row r of the second (:736-752), one warp per row.
 __global__ void add_layout_kernel(int rows, const int* __restrict__ A1, const int* __restrict__ C1,
                                   const double* __restrict__ V1, const int* __restrict__ A2, const int* __restrict__ C2,
                                   const double* __restrict__ V2, double s1, double s2, const int* __restrict__ A,
                                   int* __restrict__ C, double* __restrict__ V) {
-    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    const int r = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
     if (r >= rows) return;
-    int k = A[r];
-    for (int c1 = A1[r]; c1 < A1[r + 1]; c1++) { C[k] = C1[c1]; V[k] = s1 * V1[c1]; k++; }
-    for (int c2 = A2[r]; c2 < A2[r + 1]; c2++) { C[k] = C2[c2]; V[k] = s2 * V2[c2]; k++; }
+    const int k = A[r], lo1 = A1[r], n1 = A1[r + 1] - lo1, lo2 = A2[r], n2 = A2[r + 1] - lo2;
+    for (int t = lane; t < n1; t += 32) { C[k + t] = C1[lo1 + t]; V[k + t] = s1 * V1[lo1 + t]; }
+    for (int t = lane; t < n2; t += 32) { C[k + n1 + t] = C2[lo2 + t]; V[k + n1 + t] = s2 * V2[lo2 + t]; }
 }
 
 __global__ void add_lengths_kernel(int rows, const int* __restrict__ A1, const int* __restrict__ A2, int* __restrict__ len) {
@@ -100,18 +172,22 @@ __global__ void mul_lengths_kernel(int rows, const int* __restrict__ A1, const i
     len[r] = n;
 }
 
-// Products of row r in the reference's order (:819-832).
+// Products of row r in the reference's order (:819-832), one warp per row: the row of
+// the second matrix that each entry of row r selects is copied scaled, lanes in parallel.
 __global__ void mul_layout_kernel(int rows, const int* __restrict__ A1, const int* __restrict__ C1,
                                   const double* __restrict__ V1, const int* __restrict__ A2, const int* __restrict__ C2,
                                   const double* __restrict__ V2, const int* __restrict__ A, int* __restrict__ C,
                                   double* __restrict__ V) {
-    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    const int r = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
     if (r >= rows) return;
     int k = A[r];
     for (int c1 = A1[r]; c1 < A1[r + 1]; c1++) {
         const int m = C1[c1];
         const double v1 = V1[c1];
-        for (int c2 = A2[m]; c2 < A2[m + 1]; c2++) { C[k] = C2[c2]; V[k] = v1 * V2[c2]; k++; }
+        const int lo2 = A2[m], n2 = A2[m + 1] - lo2;
+        for (int t = lane; t < n2; t += 32) { C[k + t] = C2[lo2 + t]; V[k + t] = v1 * V2[lo2 + t]; }
+        k += n2;
     }
 }
 
@@ -146,13 +222,15 @@ __global__ void sort_bucket_kernel(int nb, const int* __restrict__ start, long l
     }
 }
 
-// Transpose: entry i of the CSR (row row_of[i]) goes to its column's bucket position.
+// Transpose, one warp per column: entry i of the CSR (row row_of[i]) goes to its
+// column's bucket position.
 __global__ void transpose_fill_kernel(int ncols, const int* __restrict__ B, const long long* __restrict__ idx,
                                       const int* __restrict__ row_of, const double* __restrict__ V, int* __restrict__ D,
                                       double* __restrict__ W) {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    const int c = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
     if (c >= ncols) return;
-    for (int k = B[c]; k < B[c + 1]; k++) { const long long i = idx[k]; D[k] = row_of[i]; W[k] = V[i]; }
+    for (int k = B[c] + lane; k < B[c + 1]; k += 32) { const long long i = idx[k]; D[k] = row_of[i]; W[k] = V[i]; }
 }
 
 __global__ void row_of_kernel(int rows, const int* __restrict__ A, int* __restrict__ row_of) {
@@ -213,7 +291,7 @@ int compress_and_compact(DevArena& m, cudaStream_t s, int rows, int* dA, int* dC
     FEEC_TRY(m.alloc(scr, scan_scratch_ints(rows + 1)));
     FEEC_TRY(cudaMemsetAsync(cnt + rows, 0, sizeof(int), s));
     note_launch();
-    compress_rows_kernel<<<grid_of(rows), kAlgBlock, 0, s>>>(rows, dA, dC, dV, cnt);
+    compress_rows_kernel<<<warp_grid(rows), kWarpBlock, 0, s>>>(rows, dA, dC, dV, cnt);
     FEEC_TRY(cudaGetLastError());
     FEEC_TRY(launch_exclusive_scan(rows + 1, cnt, off, scr, s));
     FEEC_TRY(cudaMemcpyAsync(&nnz_out, off + rows, sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -222,7 +300,7 @@ int compress_and_compact(DevArena& m, cudaStream_t s, int rows, int* dA, int* dC
     FEEC_TRY(m.alloc(oV, (size_t)std::max(nnz_out, 1)));
     if (rows == 0) FEEC_TRY(cudaMemsetAsync(oA, 0, sizeof(int), s));
     note_launch();
-    compact_rows_kernel<<<grid_of(rows), kAlgBlock, 0, s>>>(rows, dA, cnt, off, dC, dV, oC, oV, oA);
+    compact_rows_kernel<<<warp_grid(rows), kWarpBlock, 0, s>>>(rows, dA, cnt, off, dC, dV, oC, oV, oA);
     FEEC_TRY(cudaGetLastError());
     return FEEC_OK;
 }
@@ -282,7 +360,7 @@ int feec_csr_add(int rows, int cols, const int* A1, const int* C1, const double*
     FEEC_TRY(cudaGetLastError());
     FEEC_TRY(launch_exclusive_scan(rows + 1, len, dA, scr, s));
     note_launch();
-    add_layout_kernel<<<grid_of(rows), kAlgBlock, 0, s>>>(rows, dA1, dC1, dV1, dA2, dC2, dV2, s1, s2, dA, dC, dV);
+    add_layout_kernel<<<warp_grid(rows), kWarpBlock, 0, s>>>(rows, dA1, dC1, dV1, dA2, dC2, dV2, s1, s2, dA, dC, dV);
     FEEC_TRY(cudaGetLastError());
     int *oA, *oC; double* oV; int n = 0;
     if ((st = compress_and_compact(sc.m, s, rows, dA, dC, dV, oA, oC, oV, n)) != FEEC_OK) return st;
@@ -329,7 +407,7 @@ int feec_csr_multiply(int rows, int inner, int cols, const int* A1, const int* C
     FEEC_TRY(cudaGetLastError());
     FEEC_TRY(launch_exclusive_scan(rows + 1, len, dA, scr, s));
     note_launch();
-    mul_layout_kernel<<<grid_of(rows), kAlgBlock, 0, s>>>(rows, dA1, dC1, dV1, dA2, dC2, dV2, dA, dC, dV);
+    mul_layout_kernel<<<warp_grid(rows), kWarpBlock, 0, s>>>(rows, dA1, dC1, dV1, dA2, dC2, dV2, dA, dC, dV);
     FEEC_TRY(cudaGetLastError());
     int *oA, *oC; double* oV; int n = 0;
     if ((st = compress_and_compact(sc.m, s, rows, dA, dC, dV, oA, oC, oV, n)) != FEEC_OK) return st;
@@ -369,7 +447,7 @@ int feec_csr_transpose(int rows, int cols, const int* A, const int* C, const dou
     note_launch();
     sort_bucket_kernel<<<grid_of(cols), kAlgBlock, 0, s>>>(cols, dB, idx, 1);
     note_launch();
-    transpose_fill_kernel<<<grid_of(cols), kAlgBlock, 0, s>>>(cols, dB, idx, row_of, dV, dD, dW);
+    transpose_fill_kernel<<<warp_grid(cols), kWarpBlock, 0, s>>>(cols, dB, idx, row_of, dV, dD, dW);
     FEEC_TRY(cudaGetLastError());
     int *oA, *oC; double* oV; int n = 0;
     if ((st = compress_and_compact(sc.m, s, cols, dB, dD, dW, oA, oC, oV, n)) != FEEC_OK) return st;
@@ -425,7 +503,7 @@ int feec_coo_to_csr(int rows, int cols, long long count, const int* r, const int
     FEEC_TRY(sc.m.alloc(oV, (size_t)std::max(n, 1)));
     if (rows == 0) FEEC_TRY(cudaMemsetAsync(oA, 0, sizeof(int), s));
     note_launch();
-    compact_rows_kernel<<<grid_of(rows), kAlgBlock, 0, s>>>(rows, start, rc, off, dC, dV, oC, oV, oA);
+    compact_rows_kernel<<<warp_grid(rows), kWarpBlock, 0, s>>>(rows, start, rc, off, dC, dV, oC, oV, oA);
     FEEC_TRY(cudaGetLastError());
     if ((st = download(s, rows, n, oA, oC, oV, A, C, V)) != FEEC_OK) return st;
     *nnz = n;

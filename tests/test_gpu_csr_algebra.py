@@ -145,3 +145,17 @@ def test_transpose_full_size_symmetric_operator(cuda):
     n = len(A) - 1
     X = S.MatrixCSR(n, n, A, C, V)
     _same(X.getTranspose(), A, C, V, "symmetric transpose")
+
+
+def test_multiply_long_rows_match_oracle(cuda):
+    """Product rows longer than one warp's shared-memory stage (1600 entries before
+    compression, many equal columns) take the in-place path; still bit-identical."""
+    import simplefem_gb300 as S
+    from oracle import oracle
+    rng = np.random.default_rng(5)
+    n, per_row = 200, 40
+    C = np.concatenate([np.sort(rng.choice(n, per_row, replace=False)) for _ in range(n)]).astype(np.int32)
+    A = np.arange(0, n * per_row + 1, per_row, dtype=np.int32)
+    V = rng.standard_normal(n * per_row)
+    X = S.MatrixCSR(n, n, A, C, V)
+    _same(S.MatrixCSRMultiplication(X, X), *oracle.csr_multiply(A, C, V, A, C, V), "long rows")
