@@ -369,6 +369,57 @@ def run_mixed_large(dev, reps=3):
     return out
 
 
+def run_csr_algebra(with_cpu, reps=3):
+    """CSR algebra through the C ABI with host arrays (upload, kernels, download inside the
+    timed call): the operator product X*X of lattice operators and, at solver size, the
+    transpose and a sum. Every GPU result is compared bit for bit with the oracle's (the
+    oracle's OpenMP restatement of the reference's algorithm is the CPU time beside it)."""
+    import simplefem_gb300 as S
+    from simplefem_gb300 import workloads
+    oracle = None
+    if with_cpu:
+        from oracle import oracle
+        oracle.set_threads(os.cpu_count() or 1)
+
+    def timed(fn, count):
+        fn()
+        t = []
+        for _ in range(count):
+            t0 = time.perf_counter(); r = fn(); t.append(time.perf_counter() - t0)
+        return 1000.0 * float(np.median(t)), r
+
+    def same(M, ref):
+        return bool(np.array_equal(M.A, ref[0]) and np.array_equal(M.C, ref[1]) and
+                    np.array_equal(M.V.view(np.int64), ref[2].view(np.int64)))
+
+    out = {"note": "host arrays in and out (C ABI call incl. H2D/D2H and host-side index checks); "
+                   "cpu = oracle restatement with OpenMP on the host cores; results compared bit for bit"}
+    for (d, r, L) in ((3, 1, 5), (3, 2, 4)):
+        A, C, V = workloads.lattice_matrix(d, r, L, 0)
+        n = len(A) - 1
+        X = S.MatrixCSR(n, n, A, C, V)
+        ms, M = timed(lambda: S.MatrixCSRMultiplication(X, X), reps)
+        leg = {"workload": f"{d}D P{r} refined {L}x: X*X, N={n}, nnz={len(C)} -> {M.getnumberofentries()}",
+               "gpu_ms": ms}
+        if oracle is not None:
+            cms, ref = timed(lambda: oracle.csr_multiply(A, C, V, A, C, V), 1)
+            leg.update({"cpu_ms": cms, "cpu_cores": os.cpu_count() or 1, "bit_identical": same(M, ref)})
+        out[f"multiply_{d}d_p{r}_l{L}"] = leg
+    A, C, V = workloads.lattice_matrix(3, 2, 6, 0)
+    n = len(A) - 1
+    X = S.MatrixCSR(n, n, A, C, V)
+    for name, fn, cfn in (("transpose", lambda: X.getTranspose(), lambda: oracle.csr_transpose(A, C, V, n)),
+                          ("add", lambda: S.MatrixCSRAddition(X, X, 1.0, 0.5),
+                           lambda: oracle.csr_add(A, C, V, A, C, V, 1.0, 0.5))):
+        ms, M = timed(fn, reps)
+        leg = {"workload": f"3D P2 refined 6x: {name}, N={n}, nnz={len(C)}", "gpu_ms": ms}
+        if oracle is not None:
+            cms, ref = timed(cfn, 1)
+            leg.update({"cpu_ms": cms, "cpu_cores": os.cpu_count() or 1, "bit_identical": same(M, ref)})
+        out[f"{name}_3d_p2_l6"] = leg
+    return out
+
+
 def run_serving(mode, method, count=200, rate=200.0, slots=24, budget=120 * 10**9):
     """Poisson-arrival request stream through the continuous-batching server."""
     from simplefem_gb300 import workloads
@@ -433,6 +484,10 @@ def run_ours(args):
     if args.only_mixed_large:
         if rank == 0:
             print(json.dumps({"mixed_large": run_mixed_large(dev)}), flush=True)
+        return
+    if args.only_csr_algebra:
+        if rank == 0:
+            print(json.dumps({"csr_algebra": run_csr_algebra(not args.no_cpu)}), flush=True)
         return
     if args.only_serving:
         if rank == 0:
@@ -616,6 +671,7 @@ def run_ours(args):
     uneven = run_batched_uneven(dev) if not args.skip_extras else None
     block_rhs = run_block_rhs(dev) if not args.skip_extras else None
     mixed_large = run_mixed_large(dev) if not args.skip_extras else None
+    csr_algebra = run_csr_algebra(rank == 0 and not args.no_cpu) if not args.skip_extras else None
     serving = None
     if not args.skip_extras:
         serving = {"mixed_rainbow": run_serving("mixed", "rainbow", args.requests),
@@ -672,6 +728,7 @@ def run_ours(args):
             "batched_uneven": uneven,
             "block_rhs_64": block_rhs,
             "mixed_large": mixed_large,
+            "csr_algebra": csr_algebra,
             "serving": serving,
             "roofline": roofline,
             "cpu_baseline": cpu,
@@ -699,6 +756,7 @@ def main():
     ap.add_argument("--only-serving", action="store_true", help="only the serving stream")
     ap.add_argument("--only-block-rhs", action="store_true", help="only the 64 right-hand-side blocked batch")
     ap.add_argument("--only-mixed-large", action="store_true", help="only the 3D P1 L7 mixed-precision solves")
+    ap.add_argument("--only-csr-algebra", action="store_true", help="only the CSR algebra leg (product, transpose, sum)")
     ap.add_argument("--only-batched", action="store_true",
                     help="only the batched headline step (no single-solve, SpMV, CPU or extra legs)")
     ap.add_argument("--rhs-per-team", type=int, default=0,

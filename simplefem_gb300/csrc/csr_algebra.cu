@@ -46,6 +46,20 @@ constexpr int kRowCap = 1024;   // entries of one row staged in shared memory pe
 
 int warp_grid(long long rows) { return (int)std::max<long long>(1, (rows + kWarpsPerBlock - 1) / kWarpsPerBlock); }
 
+// Values travel through the sort as the two 32-bit halves of their bit patterns: every
+// move, select and shuffle stays on the 32-bit integer pipes (64-bit operations share
+// the GPU's narrow FP64 pipe), and a value is a zero exactly when its bits other than
+// the sign are all zero.
+__device__ __forceinline__ bool nonzero_halves(unsigned hi, unsigned lo) { return ((hi << 1) | lo) != 0u; }
+
+// r + x in FP64 where `add` is set, else r. Kept out of line: compiled inline, the add is
+// if-converted and then occupies the FP64 pipe on every step of the sort.
+__device__ __noinline__ uint2 merge_add(bool add, uint2 r, uint2 x) {
+    if (!add) return r;
+    const double t = __hiloint2double((int)r.y, (int)r.x) + __hiloint2double((int)x.y, (int)x.x);
+    return make_uint2((unsigned)__double2loint(t), (unsigned)__double2hiint(t));
+}
+
 // The reference's per-row exchange sort (sparse/matcsr.cpp:601-622) on c[0, L), v[0, L),
 // run by one warp as a systolic pipeline. Pass p of the reference keeps a running
 // minimum (column, value) in a register, scans positions p+1.., merges equal columns
@@ -53,36 +67,50 @@ int warp_grid(long long rows) { return (int)std::max<long long>(1, (rows + kWarp
 // is stored at position p. Lane k runs pass i+k of a sweep of 32 passes, one step behind
 // lane k-1: it receives each element after lane k-1 has processed it and hands it on.
 // Every pass therefore sees every position in exactly the state the serial sort gives
-// it, and every sum is formed in the serial order: the result is bit-identical, at about
-// L*L/64 warp steps instead of L*L/2 serial ones. Lane 0 reads the stream (one element
-// ahead), lane 31 stores what leaves the pipeline; columns are >= 0, -1 marks no element.
-__device__ void warp_exchange_sort(int* c, double* v, int L, int lane) {
+// it, and every sum is formed in the serial order, at about L*L/64 warp steps instead
+// of L*L/2 serial ones. The stream enters at lane 0 (a broadcast load one element
+// ahead) and leaves at lane 31; columns are >= 0, -1 marks no element.
+//
+// A merge where either value is zero is a select: x + 0 and 0 + x are x, up to the sign
+// of a zero sum, and zeros are dropped afterwards, so the kept entries are bit-identical.
+// Only merges of two nonzeros (a few percent of the steps) issue a warp-wide FP64 add.
+__device__ void warp_exchange_sort(int* c, uint2* v, int L, int lane) {
     for (int i = 0; i < L; i += 32) {
-        int rc = 0; double rv = 0.0;          // register of pass i + lane
-        int pc = -1; double pv = 0.0;         // element this lane hands on (-1: none)
-        int nc = -1; double nv = 0.0;         // lane 0: next element of the stream
-        if (lane == 0) { nc = c[i]; nv = v[i]; }
+        int rc = 0; unsigned rh = 0, rl = 0;          // register of pass i + lane
+        int pc = -1; unsigned ph = 0, pl = 0;         // element this lane hands on (-1: none)
+        int nc = c[i]; uint2 nv = v[i];               // next element of the stream (all lanes)
         const int steps = (L - i) + 31;
         for (int s = 0; s < steps; s++) {
             int xc = __shfl_up_sync(kFull, pc, 1);
-            double xv = __shfl_up_sync(kFull, pv, 1);
-            if (lane == 0) {
-                xc = nc; xv = nv;
-                const int q1 = i + s + 1;
-                if (q1 < L) { nc = c[q1]; nv = v[q1]; } else nc = -1;
+            unsigned xh = __shfl_up_sync(kFull, ph, 1);
+            unsigned xl = __shfl_up_sync(kFull, pl, 1);
+            if (lane == 0) { xc = nc; xl = nv.x; xh = nv.y; }
+            const int q1 = i + s + 1;
+            if (q1 < L) { nc = c[q1]; nv = v[q1]; } else { nc = -1; }
+            const bool valid = xc >= 0;
+            const bool reg = valid && s == 2 * lane;          // position i + lane: the register
+            const bool proc = valid && !reg;
+            const bool eq = proc && xc == rc;
+            const bool lt = proc && xc < rc;
+            const bool rnz = nonzero_halves(rh, rl), xnz = nonzero_halves(xh, xl);
+            const bool add = eq && rnz && xnz;
+            if (__any_sync(kFull, add)) {          // rare: a real call, so the add is not speculated
+                const uint2 t = merge_add(add, make_uint2(rl, rh), make_uint2(xl, xh));
+                rl = t.x; rh = t.y;
             }
-            pc = -1;
-            if (xc >= 0) {
-                if (s == 2 * lane) { rc = xc; rv = xv; }          // position i + lane: the register
-                else {
-                    if (xc == rc) { rv += xv; xv = 0.0; }
-                    else if (xc < rc) { const int tc = xc; const double tv = xv; xc = rc; xv = rv; rc = tc; rv = tv; }
-                    pc = xc; pv = xv;
-                }
+            if (eq && !rnz) { rh = xh; rl = xl; }
+            if (eq) { xh = 0u; xl = 0u; }
+            const int oc = lt ? rc : xc;
+            const unsigned oh = lt ? rh : xh, ol = lt ? rl : xl;
+            if (lt || reg) { rc = xc; rh = xh; rl = xl; }
+            pc = proc ? oc : -1;
+            ph = oh; pl = ol;
+            if (lane == 31) {
+                if (pc >= 0) { const int q = i + s - 31; c[q] = pc; v[q] = make_uint2(pl, ph); }
+                pc = -1;
             }
-            if (lane == 31 && pc >= 0) { const int q = i + s - 31; c[q] = pc; v[q] = pv; pc = -1; }
         }
-        if (i + lane < L) { c[i + lane] = rc; v[i + lane] = rv; }
+        if (i + lane < L) { c[i + lane] = rc; v[i + lane] = make_uint2(rl, rh); }
         __syncwarp();
     }
 }
@@ -90,13 +118,13 @@ __device__ void warp_exchange_sort(int* c, double* v, int L, int lane) {
 // The nonzeros of (c, v)[0, L) in order, written to (dc, dv) (which may be c, v
 // themselves: a write never passes the read position); returns their count. This is
 // the reference's zero bubble pass (:624-649), a stable partition of the nonzeros.
-__device__ int warp_keep_nonzeros(const int* c, const double* v, int L, int* dc, double* dv, int lane) {
+__device__ int warp_keep_nonzeros(const int* c, const uint2* v, int L, int* dc, uint2* dv, int lane) {
     int k = 0;
     for (int base = 0; base < L; base += 32) {
         const int q = base + lane;
-        int cq = 0; double vq = 0.0;
+        int cq = 0; uint2 vq = make_uint2(0u, 0u);
         if (q < L) { cq = c[q]; vq = v[q]; }
-        const bool keep = q < L && vq != 0.0;
+        const bool keep = q < L && nonzero_halves(vq.y, vq.x);
         const unsigned m = __ballot_sync(kFull, keep);
         __syncwarp();
         if (keep) { const int d = k + __popc(m & ((1u << lane) - 1u)); dc[d] = cq; dv[d] = vq; }
@@ -107,11 +135,12 @@ __device__ int warp_keep_nonzeros(const int* c, const double* v, int L, int* dc,
 }
 
 // One warp per row: sort and merge (in shared memory when the row fits), keep the
-// nonzeros at the row's start; cnt[r] = their count.
+// nonzeros at the row's start; cnt[r] = their count. Values are handled as bit patterns.
 __global__ void __launch_bounds__(kWarpBlock)
-compress_rows_kernel(int rows, const int* __restrict__ A, int* C, double* V, int* __restrict__ cnt) {
+compress_rows_kernel(int rows, const int* __restrict__ A, int* C, double* Vd, int* __restrict__ cnt) {
     __shared__ int sc[kWarpsPerBlock][kRowCap];
-    __shared__ double sv[kWarpsPerBlock][kRowCap];
+    __shared__ uint2 sv[kWarpsPerBlock][kRowCap];
+    uint2* V = reinterpret_cast<uint2*>(Vd);
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int r = blockIdx.x * kWarpsPerBlock + w;
     if (r >= rows) return;
