@@ -819,6 +819,100 @@ int oracle_coo_to_csr(int rows, long long count, const int* r, const int* c, con
     return (int)n;
 }
 
+/* sparse/sparsematrix.cpp:609-722, SparseMatrixMultiplication(left, right), with
+ * SparseMatrix::sortandcompressentries (:405-458) for the operands and the result.
+ * Operands: zeros dropped, sorted (left by column then row, right by row then column),
+ * equal positions summed in sorted order. Every product L(i,k) R(k,j) is emitted in the
+ * order k, then i, then j; the result drops zero products, is sorted by row then column
+ * and sums equal positions in sorted order. The reference's std::sort leaves the order of
+ * equal positions unspecified; these sorts are stable (input order, then emission order:
+ * k ascending). Entries are returned row-wise sorted. */
+static long long compress_entries(long long count, const int* r, const int* c, const double* v, int colwise,
+                                  OracleEntry* e)
+{
+    long long m = 0;
+    for (long long i = 0; i < count; i++)
+        if (v[i] != 0.0) {
+            e[m].r = colwise ? c[i] : r[i]; e[m].c = colwise ? r[i] : c[i];
+            e[m].v = v[i]; e[m].i = i; m++;
+        }
+    qsort(e, (size_t)m, sizeof(OracleEntry), entry_cmp);
+    if (m == 0) return 0;
+    long long dest = 0;
+    for (long long src = 1; src < m; src++) {
+        if (e[src].r == e[dest].r && e[src].c == e[dest].c) e[dest].v += e[src].v;
+        else e[++dest] = e[src];
+    }
+    return dest + 1;
+}
+
+/* Upper bound on the products emitted (before any compression): for every k, the left
+ * entries in column k times the right entries in row k. */
+long long oracle_coo_multiply_size(int inner, long long ln, const int* lc, long long rn, const int* rr)
+{
+    long long* a = (long long*)calloc((size_t)(inner > 0 ? inner : 1), sizeof(long long));
+    long long* b = (long long*)calloc((size_t)(inner > 0 ? inner : 1), sizeof(long long));
+    long long total = 0;
+    if (!a || !b) { free(a); free(b); return -1; }
+    for (long long i = 0; i < ln; i++) a[lc[i]]++;
+    for (long long i = 0; i < rn; i++) b[rr[i]]++;
+    for (int k = 0; k < inner; k++) total += a[k] * b[k];
+    free(a); free(b);
+    return total;
+}
+
+long long oracle_coo_multiply(long long ln, const int* lr, const int* lc, const double* lv,
+                              long long rn, const int* rr, const int* rc, const double* rv,
+                              int* out_r, int* out_c, double* out_v)
+{
+    OracleEntry* le = (OracleEntry*)malloc((size_t)(ln > 0 ? ln : 1) * sizeof(OracleEntry));
+    OracleEntry* re = (OracleEntry*)malloc((size_t)(rn > 0 ? rn : 1) * sizeof(OracleEntry));
+    if (!le || !re) { free(le); free(re); return -1; }
+    const long long lnum = compress_entries(ln, lr, lc, lv, 1, le);   /* (column k, row i) */
+    const long long rnum = compress_entries(rn, rr, rc, rv, 0, re);   /* (row k, column j) */
+    long long cap = 0;
+    for (long long lb = 0, rb = 0; lb < lnum && rb < rnum;) {
+        if (le[lb].r == re[rb].r) {
+            const int k = le[lb].r;
+            long long ln2 = lb, rn2 = rb;
+            while (ln2 < lnum && le[ln2].r == k) ln2++;
+            while (rn2 < rnum && re[rn2].r == k) rn2++;
+            cap += (ln2 - lb) * (rn2 - rb);
+            lb = ln2; rb = rn2;
+        } else if (le[lb].r < re[rb].r) lb++; else rb++;
+    }
+    OracleEntry* pe = (OracleEntry*)malloc((size_t)(cap > 0 ? cap : 1) * sizeof(OracleEntry));
+    if (!pe) { free(le); free(re); return -1; }
+    long long m = 0;
+    for (long long lb = 0, rb = 0; lb < lnum && rb < rnum;) {
+        if (le[lb].r == re[rb].r) {
+            const int k = le[lb].r;
+            long long ln2 = lb, rn2 = rb;
+            while (ln2 < lnum && le[ln2].r == k) ln2++;
+            while (rn2 < rnum && re[rn2].r == k) rn2++;
+            for (long long a = lb; a < ln2; a++)
+                for (long long b = rb; b < rn2; b++) {
+                    const double prod = le[a].v * re[b].v;
+                    if (prod != 0.0) { pe[m].r = le[a].c; pe[m].c = re[b].c; pe[m].v = prod; pe[m].i = m; m++; }
+                }
+            lb = ln2; rb = rn2;
+        } else if (le[lb].r < re[rb].r) lb++; else rb++;
+    }
+    qsort(pe, (size_t)m, sizeof(OracleEntry), entry_cmp);
+    long long n = 0;
+    if (m > 0) {
+        long long dest = 0;
+        for (long long src = 1; src < m; src++) {
+            if (pe[src].r == pe[dest].r && pe[src].c == pe[dest].c) pe[dest].v += pe[src].v;
+            else pe[++dest] = pe[src];
+        }
+        n = dest + 1;
+    }
+    for (long long i = 0; i < n; i++) { out_r[i] = pe[i].r; out_c[i] = pe[i].c; out_v[i] = pe[i].v; }
+    free(le); free(re); free(pe);
+    return n;
+}
+
 /* Number of OpenMP threads the oracle would use (1 without OpenMP). */
 int oracle_max_threads(void)
 {

@@ -55,6 +55,11 @@ def lib():
         L.oracle_csr_multiply.argtypes = [ctypes.c_int, _i32p, _i32p, _f64p, _i32p, _i32p, _f64p, _i32p, _i32p, _f64p]
         L.oracle_csr_transpose.argtypes = [ctypes.c_int, ctypes.c_int, _i32p, _i32p, _f64p, _i32p, _i32p, _f64p]
         L.oracle_coo_to_csr.argtypes = [ctypes.c_int, ctypes.c_longlong, _i32p, _i32p, _f64p, _i32p, _i32p, _f64p]
+        L.oracle_coo_multiply_size.argtypes = [ctypes.c_int, ctypes.c_longlong, _i32p, ctypes.c_longlong, _i32p]
+        L.oracle_coo_multiply_size.restype = ctypes.c_longlong
+        L.oracle_coo_multiply.argtypes = [ctypes.c_longlong, _i32p, _i32p, _f64p, ctypes.c_longlong, _i32p, _i32p,
+                                          _f64p, _i32p, _i32p, _f64p]
+        L.oracle_coo_multiply.restype = ctypes.c_longlong
         L.oracle_max_threads.restype = ctypes.c_int
         L.oracle_set_threads.argtypes = [ctypes.c_int]
         _lib = L
@@ -187,3 +192,14 @@ def coo_to_csr(rows, r, c, v):
     A = np.empty(rows + 1, np.int32); C = np.empty(max(count, 1), np.int32); V = np.empty(max(count, 1))
     n = lib().oracle_coo_to_csr(int(rows), count, _i32(r), _i32(c), _f64(v), A, C, V)
     return A, C[:n].copy(), V[:n].copy()
+
+
+def coo_multiply(inner, left, right):
+    """SparseMatrixMultiplication of two COO operands given as (r, c, v): the product's
+    entries (r, c, v), sorted by row then column."""
+    lr, lc, lv = (_i32(left[0]), _i32(left[1]), _f64(left[2]))
+    rr, rc, rv = (_i32(right[0]), _i32(right[1]), _f64(right[2]))
+    cap = int(lib().oracle_coo_multiply_size(int(inner), len(lr), lc, len(rr), rr))
+    r = np.empty(max(cap, 1), np.int32); c = np.empty(max(cap, 1), np.int32); v = np.empty(max(cap, 1))
+    n = int(lib().oracle_coo_multiply(len(lr), lr, lc, lv, len(rr), rr, rc, rv, r, c, v))
+    return r[:n].copy(), c[:n].copy(), v[:n].copy()

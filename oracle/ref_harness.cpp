@@ -25,6 +25,7 @@
 //   csrmul <a.csr> <b.csr> <out.csr>             MatrixCSRMultiplication (sparse/matcsr.cpp:767-849)
 //   csrtrans <a.csr> <out.csr>                   MatrixCSR::getTranspose (sparse/matcsr.cpp:291-350)
 //   coo2csr <in.coo> <out.csr>                   MatrixCSR(SparseMatrix) (sparse/matcsr.cpp:43-89)
+//   coomul <a.coo> <b.coo> <out.coo>             SparseMatrixMultiplication (sparse/sparsematrix.cpp:609-722)
 
 #include <chrono>
 #include <cmath>
@@ -89,6 +90,30 @@ static std::vector<double> read_vec(const char* path, int64_t n) {
 }
 
 static void write_raw(FILE* f, const void* p, size_t bytes) { if (bytes && std::fwrite(p, 1, bytes, f) != bytes) die("write"); }
+
+static SparseMatrix read_coo(const char* path) {
+    FILE* f = std::fopen(path, "rb"); if (!f) die("cannot read coo");
+    char magic[8]; if (std::fread(magic, 1, 8, f) != 8 || std::memcmp(magic, "FEECCOO1", 8)) die("bad coo magic");
+    int64_t hdr[3]; if (std::fread(hdr, 8, 3, f) != 3) die("short coo");
+    std::vector<int> r(hdr[2]), c(hdr[2]); std::vector<double> v(hdr[2]);
+    if (std::fread(r.data(), 4, hdr[2], f) != (size_t)hdr[2] || std::fread(c.data(), 4, hdr[2], f) != (size_t)hdr[2] ||
+        std::fread(v.data(), 8, hdr[2], f) != (size_t)hdr[2]) die("short coo data");
+    std::fclose(f);
+    std::vector<SparseMatrix::MatrixEntry> e(hdr[2]);
+    for (int64_t i = 0; i < hdr[2]; i++) e[i] = SparseMatrix::MatrixEntry{r[i], c[i], v[i]};
+    return SparseMatrix((int)hdr[0], (int)hdr[1], e);
+}
+
+static void write_coo(const char* path, const SparseMatrix& m) {
+    FILE* f = std::fopen(path, "wb"); if (!f) die("cannot write coo");
+    const auto& e = m.getentries();
+    const int64_t hdr[3] = {m.getdimout(), m.getdimin(), (int64_t)e.size()};
+    std::vector<int> r(e.size()), c(e.size()); std::vector<double> v(e.size());
+    for (size_t i = 0; i < e.size(); i++) { r[i] = e[i].row; c[i] = e[i].column; v[i] = e[i].value; }
+    write_raw(f, "FEECCOO1", 8); write_raw(f, hdr, sizeof(hdr));
+    write_raw(f, r.data(), 4 * r.size()); write_raw(f, c.data(), 4 * c.size()); write_raw(f, v.data(), 8 * v.size());
+    std::fclose(f);
+}
 
 static MatrixCSR to_matrix(const Csr& m) {
     std::vector<int> A(m.A), C(m.C); std::vector<Float> V(m.V.begin(), m.V.end());
@@ -298,17 +323,13 @@ int main(int argc, char** argv) {
     }
     if (cmd == "coo2csr") {
         if (argc != 4) die("coo2csr <in.coo> <out.csr>");
-        FILE* f = std::fopen(argv[2], "rb"); if (!f) die("cannot read coo");
-        char magic[8]; if (std::fread(magic, 1, 8, f) != 8 || std::memcmp(magic, "FEECCOO1", 8)) die("bad coo magic");
-        int64_t hdr[3]; if (std::fread(hdr, 8, 3, f) != 3) die("short coo");
-        std::vector<int> r(hdr[2]), c(hdr[2]); std::vector<double> v(hdr[2]);
-        if (std::fread(r.data(), 4, hdr[2], f) != (size_t)hdr[2] || std::fread(c.data(), 4, hdr[2], f) != (size_t)hdr[2] ||
-            std::fread(v.data(), 8, hdr[2], f) != (size_t)hdr[2]) die("short coo data");
-        std::fclose(f);
-        std::vector<SparseMatrix::MatrixEntry> e(hdr[2]);
-        for (int64_t i = 0; i < hdr[2]; i++) e[i] = SparseMatrix::MatrixEntry{r[i], c[i], v[i]};
-        SparseMatrix sm((int)hdr[0], (int)hdr[1], e);
-        write_csr(argv[3], from_matrix(MatrixCSR(sm)));
+        write_csr(argv[3], from_matrix(MatrixCSR(read_coo(argv[2]))));
+        return 0;
+    }
+    if (cmd == "coomul") {
+        if (argc != 5) die("coomul <a.coo> <b.coo> <out.coo>");
+        const SparseMatrix a = read_coo(argv[2]), b = read_coo(argv[3]);
+        write_coo(argv[4], SparseMatrixMultiplication(a, b));
         return 0;
     }
     die("unknown command");

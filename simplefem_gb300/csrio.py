@@ -125,3 +125,17 @@ def write_coo(path, rows: int, cols: int, r, c, v) -> None:
         f.write(b"FEECCOO1")
         f.write(np.array([rows, cols, len(r)], np.int64).tobytes())
         f.write(r.tobytes()); f.write(c.tobytes()); f.write(v.tobytes())
+
+
+def read_coo(path):
+    """(r, c, v, rows, cols) of a FEECCOO1 file."""
+    with _open(path, "rb") as f:
+        buf = f.read()
+    if buf[:8] != b"FEECCOO1":
+        raise ValueError(f"{path}: not a FEECCOO1 file")
+    rows, cols, count = (int(x) for x in np.frombuffer(buf, np.int64, 3, 8))
+    off = 32
+    r = np.frombuffer(buf, np.int32, count, off).copy(); off += 4 * count
+    c = np.frombuffer(buf, np.int32, count, off).copy(); off += 4 * count
+    v = np.frombuffer(buf, np.float64, count, off).copy()
+    return r, c, v, rows, cols

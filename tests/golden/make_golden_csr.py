@@ -13,6 +13,9 @@ Stored (prefix per case): inputs ``<case>_in*`` and the reference's output CSR
 * ``coo``  : COO -> CSR of X's entries, shuffled, a third of them split into two equal
   halves (the two halves sum to the entry exactly in either order) and 500 explicit
   zeros (the reference drops them).
+* ``coomul``: SparseMatrixMultiplication (sparse/sparsematrix.cpp:609-722) of X[:700] and
+  Y, both given as shuffled COO with split halves and explicit zeros; inputs
+  ``coomul_l_{r,c,v}``, ``coomul_r_{r,c,v}``, output ``coomul_out_{r,c,v}`` (row-wise).
 
 Usage: python tests/golden/make_golden_csr.py   (needs the reference sources; run once).
 """
@@ -86,6 +89,31 @@ def main():
         out["coo_in_r"] = r; out["coo_in_c"] = c; out["coo_in_v"] = v
         csrio.write_coo(t("m.coo"), X.n, X.n, r, c, v)
         run("coo2csr", t("m.coo"), t("o.csr")); store("coo", t("o.csr"))
+
+        rng2 = np.random.default_rng(2027)
+
+        def scrambled(m, zeros):
+            rows_m = np.repeat(np.arange(m.n, dtype=np.int32), np.diff(m.A))
+            rr, cc, vv = list(rows_m), list(m.C), list(m.V)
+            for i in np.nonzero(rng2.random(len(vv)) < 0.25)[0]:
+                h = vv[i] * 0.5
+                vv[i] = h
+                rr.append(rows_m[i]); cc.append(m.C[i]); vv.append(h)
+            rr += list(rng2.integers(0, m.n, zeros)); cc += list(rng2.integers(0, m.ncols, zeros)); vv += [0.0] * zeros
+            perm = rng2.permutation(len(rr))
+            return np.array(rr, np.int32)[perm], np.array(cc, np.int32)[perm], np.array(vv)[perm]
+
+        L_ = scrambled(Xr, 200)
+        R_ = scrambled(Y, 300)
+        csrio.write_coo(t("l.coo"), Xr.n, Xr.ncols, *L_)
+        csrio.write_coo(t("r.coo"), Y.n, Y.ncols, *R_)
+        for key, arrs in (("coomul_l", L_), ("coomul_r", R_)):
+            out[key + "_r"], out[key + "_c"], out[key + "_v"] = arrs
+        run("coomul", t("l.coo"), t("r.coo"), t("p.coo"))
+        pr, pc, pv, prow, pcol = csrio.read_coo(t("p.coo"))
+        out["coomul_out_r"] = pr; out["coomul_out_c"] = pc; out["coomul_out_v"] = pv
+        out["coomul_shape"] = np.array([prow, pcol], np.int64)
+        print(f"coomul: {prow} x {pcol}, {len(pr)} entries")
     np.savez_compressed(os.path.join(HERE, "csr_algebra.npz"), **out)
 
 

@@ -82,3 +82,29 @@ def test_oracle_csr_algebra_bitexact(O):
         assert np.array_equal(A, g[case + "_A"]), case
         assert np.array_equal(C, g[case + "_C"]), case
         assert np.array_equal(V, g[case + "_V"]), case
+
+
+def test_oracle_coo_multiply_against_reference(O):
+    """SparseMatrixMultiplication (sparse/sparsematrix.cpp:609-722) against the reference's
+    own output: the structure bit for bit, entries with one product bit for bit, and sums
+    of several products within 16 eps of the sum of their magnitudes (the reference's
+    std::sort leaves the order of equal positions, hence the summation order, unspecified;
+    the oracle sums in emission order)."""
+    g = load_golden("csr_algebra")
+    inner = int(len(g["Y_A"]) - 1)
+    L = (g["coomul_l_r"], g["coomul_l_c"], g["coomul_l_v"])
+    R = (g["coomul_r_r"], g["coomul_r_c"], g["coomul_r_v"])
+    r, c, v = O.coo_multiply(inner, L, R)
+    assert np.array_equal(r, g["coomul_out_r"]) and np.array_equal(c, g["coomul_out_c"])
+    _, _, mag = O.coo_multiply(inner, (L[0], L[1], np.abs(L[2])), (R[0], R[1], np.abs(R[2])))
+    ref = g["coomul_out_v"]
+    assert np.all(np.abs(v - ref) <= 16 * np.finfo(float).eps * mag)
+    # products per entry: the product of the compressed operands' patterns
+    rows = int(g["coomul_shape"][0])
+    Al, Cl, _ = O.coo_to_csr(rows, *L)
+    Ar, Cr, _ = O.coo_to_csr(inner, *R)
+    Ap, Cp, count = O.csr_multiply(Al, Cl, np.ones(len(Cl)), Ar, Cr, np.ones(len(Cr)))
+    assert np.array_equal(Cp, c) and np.array_equal(np.repeat(np.arange(rows), np.diff(Ap)), r)
+    single = count == 1.0
+    assert 0 < single.sum() < len(v)
+    assert np.array_equal(v[single], ref[single])
