@@ -173,6 +173,24 @@ int feec_csr_transpose(int rows, int cols, const int* A, const int* C, const dou
 int feec_coo_to_csr(int rows, int cols, long long count, const int* r, const int* c, const double* v,
                     int* A, int* C, double* V, int* nnz);
 
+/* Upper bound on the entries of a COO product (left lrows x inner with ln entries, right
+ * inner x rcols with rn entries): for every k, left entries in column k times right entries
+ * in row k (sparse/sparsematrix.cpp:622-660 counts the same after compressing). */
+int feec_coo_multiply_size(int inner, long long ln, const int* lc, long long rn, const int* rr,
+                           long long* size);
+
+/* Replaces SparseMatrixMultiplication(left, right), sparse/sparsematrix.cpp:609-722: both
+ * operands compressed (zeros dropped, equal positions summed in input order), every product
+ * L(i,k) R(k,j), zero products dropped, equal positions summed in k order; the result
+ * row-wise sorted in out_r/out_c/out_v (room: feec_coo_multiply_size), *count entries. The
+ * reference's std::sort leaves the summation order of equal positions unspecified, so
+ * entries with several products can differ from it in rounding (the structure and entries
+ * with one product are identical). */
+int feec_coo_multiply(int lrows, int inner, int rcols,
+                      long long ln, const int* lr, const int* lc, const double* lv,
+                      long long rn, const int* rr, const int* rc, const double* rv,
+                      int* out_r, int* out_c, double* out_v, long long* count);
+
 /* Replaces Rainbow::Rainbow(mat, do_shuffle = false), sparse/rainbow.cpp:14-130.
  * F[N], B[N+1] (num_colors+1 entries used), R[N], host pointers; bit-identical
  * to the reference's greedy coloring. */

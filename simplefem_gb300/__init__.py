@@ -9,13 +9,14 @@ from ._native import FeecError, FeecSolveInfo  # noqa: F401
 from .solver import (ConjugateGradientSolverCSR, ConjugateGradientSolverCSR_DiagonalPreconditioner,  # noqa: F401
                      ConjugateGradientSolverCSR_Eisenstat_Rainbow, ConjugateGradientSolverCSR_Rainbow, ConjugateGradientSolverCSR_SSOR,
                      ConjugateGradientSolverCSR_SSOR_Eisenstat, last_info)
-from .sparse import FloatVector, MatrixCSR, MatrixCSRAddition, MatrixCSRMultiplication, Rainbow  # noqa: F401
+from .sparse import (FloatVector, MatrixCSR, MatrixCSRAddition, MatrixCSRMultiplication, Rainbow,  # noqa: F401
+                     SparseMatrix, SparseMatrixMultiplication)
 
 # Constants of base/base.hpp:121-131 (Float = double)
 machine_epsilon = 2.220446049250313080847263336181640625e-16
 desired_precision = 1.490116119384765625e-08
 
-__all__ = ["MatrixCSR", "MatrixCSRAddition", "MatrixCSRMultiplication", "Rainbow", "FloatVector", "ConjugateGradientSolverCSR",
+__all__ = ["MatrixCSR", "MatrixCSRAddition", "MatrixCSRMultiplication", "SparseMatrix", "SparseMatrixMultiplication", "Rainbow", "FloatVector", "ConjugateGradientSolverCSR",
            "ConjugateGradientSolverCSR_DiagonalPreconditioner", "ConjugateGradientSolverCSR_SSOR",
            "ConjugateGradientSolverCSR_Rainbow", "ConjugateGradientSolverCSR_SSOR_Eisenstat",
            "ConjugateGradientSolverCSR_Eisenstat_Rainbow", "last_info", "FeecError", "machine_epsilon", "desired_precision"]

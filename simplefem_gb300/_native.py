@@ -87,6 +87,10 @@ def gpu():
         L.feec_csr_multiply.argtypes = [_ip, _ip, _ip, _i32p, _i32p, _f64p, _i32p, _i32p, _f64p, _i32p, _i32p, _f64p, _cp]
         L.feec_csr_transpose.argtypes = [_ip, _ip, _i32p, _i32p, _f64p, _i32p, _i32p, _f64p, _cp]
         L.feec_coo_to_csr.argtypes = [_ip, _ip, ctypes.c_longlong, _i32p, _i32p, _f64p, _i32p, _i32p, _f64p, _cp]
+        _llp = ctypes.POINTER(ctypes.c_longlong)
+        L.feec_coo_multiply_size.argtypes = [_ip, ctypes.c_longlong, _i32p, ctypes.c_longlong, _i32p, _llp]
+        L.feec_coo_multiply.argtypes = [_ip, _ip, _ip, ctypes.c_longlong, _i32p, _i32p, _f64p, ctypes.c_longlong,
+                                        _i32p, _i32p, _f64p, _i32p, _i32p, _f64p, _llp]
         L.feec_rainbow.argtypes = [_ip, _i32p, _i32p, ctypes.POINTER(ctypes.c_int), _i32p, _i32p, _i32p]
         L.feec_csr_check.argtypes = [_ip, _ip, _i32p, _i32p, _f64p]
         L.feec_system_create.argtypes = [ctypes.POINTER(_vp), _ip, _vp, _vp, _vp, _ip, _vp]

@@ -302,6 +302,165 @@ __global__ void ll_to_int_kernel(int n, const long long* __restrict__ in, int* _
     if (i < n) out[i] = (int)in[i];
 }
 
+// ---- SparseMatrixMultiplication (sparse/sparsematrix.cpp:609-722) ----------------------
+// Per left row i, the products L(i,k) R(k,j) for k ascending (the left CSR row is sorted
+// by k) are accumulated into a hash table keyed by j: within one k the columns j are
+// distinct, so the lanes of a warp add one right row in parallel without meeting, and
+// every entry receives its products in k order, the order in which the reference's
+// stable emission (k, then i, then j) lists them. Zero products are skipped (the
+// reference drops them before merging); the first product of an entry is stored, the
+// later ones added, as the reference's compression does.
+
+constexpr int kHashWarps = 2;
+constexpr int kHashSlots = 2048;                 // shared table per warp: 24 KB
+constexpr int kHashMaxKeys = kHashSlots * 3 / 4;
+
+__device__ __forceinline__ unsigned col_hash(int j) { return (unsigned)j * 2654435761u; }
+
+__device__ __forceinline__ int next_pow2_at_least(long long x, int lo) {
+    int h = lo;
+    while (h < x && h < (1 << 30)) h <<= 1;
+    return h;
+}
+
+// Accumulates row i into (keys, vals)[0, H) (keys preset to -1). Returns the number of
+// distinct columns, or -1 once more than max_keys would be held (the caller retries the
+// row with a larger table).
+__device__ int product_row_accumulate(int i, const int* __restrict__ LA, const int* __restrict__ LC,
+                                      const double* __restrict__ LV, const int* __restrict__ RA,
+                                      const int* __restrict__ RC, const double* __restrict__ RV, int* keys,
+                                      double* vals, int H, int max_keys, int lane) {
+    int distinct = 0;
+    for (int a = LA[i]; a < LA[i + 1]; a++) {
+        const int k = LC[a];
+        const double lv = LV[a];
+        const int lo = RA[k], len = RA[k + 1] - lo;
+        for (int base = 0; base < len; base += 32) {
+            const int t = base + lane;
+            bool created = false, placed = true;
+            if (t < len) {
+                const int j = RC[lo + t];
+                const double prod = lv * RV[lo + t];
+                if (prod != 0.0) {
+                    unsigned h = col_hash(j) & (unsigned)(H - 1);
+                    placed = false;
+                    for (int probe = 0; probe < H; probe++) {
+                        const int cur = *((volatile int*)&keys[h]);
+                        if (cur == j) { placed = true; break; }
+                        if (cur == -1) {
+                            const int prev = atomicCAS(&keys[h], -1, j);
+                            if (prev == -1) { created = true; placed = true; break; }
+                            if (prev == j) { placed = true; break; }
+                        }
+                        h = (h + 1) & (unsigned)(H - 1);
+                    }
+                    if (created) vals[h] = prod;
+                    else if (placed) vals[h] = vals[h] + prod;
+                }
+            }
+            distinct += __popc(__ballot_sync(kFull, created));
+            const bool lost = __any_sync(kFull, !placed);
+            __syncwarp();
+            if (lost || distinct > max_keys) return -1;
+        }
+    }
+    return distinct;
+}
+
+// The table's d entries moved to its front (in place), then written to (oc, ov) sorted
+// by column (rank = number of smaller columns).
+__device__ void table_to_sorted_row(int* keys, double* vals, int H, int* __restrict__ oc, double* __restrict__ ov,
+                                    int lane) {
+    int d = 0;
+    for (int base = 0; base < H; base += 32) {
+        const int key = keys[base + lane];
+        const double val = vals[base + lane];
+        const bool occ = key >= 0;
+        const unsigned m = __ballot_sync(kFull, occ);
+        __syncwarp();
+        if (occ) { const int at = d + __popc(m & ((1u << lane) - 1u)); keys[at] = key; vals[at] = val; }
+        d += __popc(m);
+        __syncwarp();
+    }
+    for (int base = 0; base < d; base += 32) {
+        const int e = base + lane;
+        const int ke = e < d ? keys[e] : 0;
+        int rank = 0;
+        for (int f = 0; f < d; f++) rank += keys[f] < ke;
+        if (e < d) { oc[rank] = ke; ov[rank] = vals[e]; }
+    }
+    __syncwarp();
+}
+
+// E[i] = min(products of row i, columns): room for row i's distinct columns.
+__global__ void product_room_kernel(int rows, int cols, const long long* __restrict__ P, int* __restrict__ E,
+                                    unsigned long long* __restrict__ total) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= rows) return;
+    const int e = (int)(P[i] < cols ? P[i] : cols);
+    E[i] = e;
+    atomicAdd(total, (unsigned long long)e);
+}
+
+// One warp per left row, table in shared memory; rows that overflow it are flagged.
+__global__ void __launch_bounds__(kHashWarps * 32)
+coo_product_rows_kernel(int rows, const int* __restrict__ LA, const int* __restrict__ LC, const double* __restrict__ LV,
+                        const int* __restrict__ RA, const int* __restrict__ RC, const double* __restrict__ RV,
+                        const int* __restrict__ E, const int* __restrict__ SD, int* __restrict__ RCo,
+                        double* __restrict__ RVo, int* __restrict__ cnt, int* __restrict__ big) {
+    __shared__ int skeys[kHashWarps][kHashSlots];
+    __shared__ double svals[kHashWarps][kHashSlots];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int i = blockIdx.x * kHashWarps + w;
+    if (i >= rows) return;
+    const int H = next_pow2_at_least(2LL * E[i], 32) < kHashSlots ? next_pow2_at_least(2LL * E[i], 32) : kHashSlots;
+    for (int q = lane; q < H; q += 32) skeys[w][q] = -1;
+    __syncwarp();
+    const int d = product_row_accumulate(i, LA, LC, LV, RA, RC, RV, skeys[w], svals[w], H,
+                                         H == kHashSlots ? kHashMaxKeys : H, lane);
+    if (d < 0) {
+        if (lane == 0) { big[i] = 1; cnt[i] = 0; }
+        return;
+    }
+    table_to_sorted_row(skeys[w], svals[w], H, RCo + SD[i], RVo + SD[i], lane);
+    if (lane == 0) { big[i] = 0; cnt[i] = d; }
+}
+
+// Table sizes in global memory for the flagged rows (0 for the others).
+__global__ void big_table_size_kernel(int rows, const int* __restrict__ E, const int* __restrict__ big,
+                                      int* __restrict__ G, unsigned long long* __restrict__ total) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= rows) return;
+    const int g = big[i] ? next_pow2_at_least(2LL * E[i], 32) : 0;
+    G[i] = g;
+    if (g) atomicAdd(total, (unsigned long long)g);
+}
+
+// The flagged rows again, each with a global table of at least twice its room.
+__global__ void coo_product_big_rows_kernel(int rows, const int* __restrict__ LA, const int* __restrict__ LC,
+                                            const double* __restrict__ LV, const int* __restrict__ RA,
+                                            const int* __restrict__ RC, const double* __restrict__ RV,
+                                            const int* __restrict__ big, const int* __restrict__ GO,
+                                            int* __restrict__ gkeys, double* __restrict__ gvals,
+                                            const int* __restrict__ SD, int* __restrict__ RCo,
+                                            double* __restrict__ RVo, int* __restrict__ cnt, int* __restrict__ err) {
+    const int lane = threadIdx.x & 31;
+    const int i = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
+    if (i >= rows || !big[i]) return;
+    const int H = GO[i + 1] - GO[i];
+    int* keys = gkeys + GO[i];
+    double* vals = gvals + GO[i];
+    for (int q = lane; q < H; q += 32) keys[q] = -1;
+    __syncwarp();
+    const int d = product_row_accumulate(i, LA, LC, LV, RA, RC, RV, keys, vals, H, H, lane);
+    if (d < 0) {                     // cannot happen: H >= 2 * (room of the row)
+        if (lane == 0) { atomicExch(err, 1); cnt[i] = 0; }
+        return;
+    }
+    table_to_sorted_row(keys, vals, H, RCo + SD[i], RVo + SD[i], lane);
+    if (lane == 0) cnt[i] = d;
+}
+
 // Host-side checks of a CSR given by host pointers.
 bool csr_ok(int rows, int cols, const int* A, const int* C) {
     if (rows < 0 || cols < 0 || !A || A[0] != 0) return false;
@@ -349,6 +508,48 @@ template <typename T>
 int upload(DevArena& m, cudaStream_t s, T*& d, const T* h, size_t n) {
     FEEC_TRY(m.alloc(d, std::max<size_t>(n, 1)));
     if (n) FEEC_TRY(cudaMemcpyAsync(d, h, sizeof(T) * n, cudaMemcpyHostToDevice, s));
+    return FEEC_OK;
+}
+
+// COO entries on the device (indices already checked) to a row-sorted CSR with equal
+// positions summed in input order and zero values dropped first.
+int coo_to_csr_dev(DevArena& m, cudaStream_t s, int rows, long long count, const int* dr, const int* dc,
+                   const double* dv, int*& oA, int*& oC, double*& oV, int& n) {
+    unsigned char* keep; int *cnt, *start, *fill, *scr, *dC, *rc; long long* idx; double* dV;
+    FEEC_TRY(m.alloc(keep, (size_t)std::max<long long>(count, 1)));
+    FEEC_TRY(m.alloc(cnt, (size_t)rows + 1)); FEEC_TRY(m.alloc(start, (size_t)rows + 1));
+    FEEC_TRY(m.alloc(fill, (size_t)rows + 1)); FEEC_TRY(m.alloc(scr, scan_scratch_ints(rows + 1)));
+    FEEC_TRY(m.alloc(idx, (size_t)std::max<long long>(count, 1)));
+    FEEC_TRY(m.alloc(dC, (size_t)std::max<long long>(count, 1))); FEEC_TRY(m.alloc(dV, (size_t)std::max<long long>(count, 1)));
+    FEEC_TRY(m.alloc(rc, (size_t)rows + 1));
+    FEEC_TRY(cudaMemsetAsync(cnt, 0, sizeof(int) * ((size_t)rows + 1), s));
+    FEEC_TRY(cudaMemsetAsync(fill, 0, sizeof(int) * ((size_t)rows + 1), s));
+    FEEC_TRY(cudaMemsetAsync(rc, 0, sizeof(int) * ((size_t)rows + 1), s));
+    note_launch();
+    nonzero_kernel<<<grid_of(count), kAlgBlock, 0, s>>>(count, dv, keep);          // zeros dropped (:411-420)
+    note_launch();
+    count_keys_kernel<<<grid_of(count), kAlgBlock, 0, s>>>(count, dr, keep, cnt);
+    FEEC_TRY(cudaGetLastError());
+    FEEC_TRY(launch_exclusive_scan(rows + 1, cnt, start, scr, s));
+    note_launch();
+    bucket_kernel<<<grid_of(count), kAlgBlock, 0, s>>>(count, dr, keep, start, fill, idx);
+    note_launch();
+    sort_bucket_kernel<<<grid_of(rows), kAlgBlock, 0, s>>>(rows, start, idx, 0);
+    note_launch();
+    coo_row_kernel<<<grid_of(rows), kAlgBlock, 0, s>>>(rows, start, idx, dc, dv, dC, dV, rc);
+    FEEC_TRY(cudaGetLastError());
+    // rows now hold their merged entries from start[r]; compact them
+    int* off;
+    FEEC_TRY(m.alloc(off, (size_t)rows + 1));
+    FEEC_TRY(launch_exclusive_scan(rows + 1, rc, off, scr, s));
+    FEEC_TRY(cudaMemcpyAsync(&n, off + rows, sizeof(int), cudaMemcpyDeviceToHost, s));
+    FEEC_TRY(cudaStreamSynchronize(s));
+    FEEC_TRY(m.alloc(oA, (size_t)rows + 1)); FEEC_TRY(m.alloc(oC, (size_t)std::max(n, 1)));
+    FEEC_TRY(m.alloc(oV, (size_t)std::max(n, 1)));
+    if (rows == 0) FEEC_TRY(cudaMemsetAsync(oA, 0, sizeof(int), s));
+    note_launch();
+    compact_rows_kernel<<<warp_grid(rows), kWarpBlock, 0, s>>>(rows, start, rc, off, dC, dV, oC, oV, oA);
+    FEEC_TRY(cudaGetLastError());
     return FEEC_OK;
 }
 
@@ -499,43 +700,121 @@ int feec_coo_to_csr(int rows, int cols, long long count, const int* r, const int
     if ((st = upload(sc.m, s, dr, r, (size_t)count)) || (st = upload(sc.m, s, dc, c, (size_t)count)) ||
         (st = upload(sc.m, s, dv, v, (size_t)count)))
         return st;
-    unsigned char* keep; int *cnt, *start, *fill, *scr, *dC, *rc; long long* idx; double* dV;
-    FEEC_TRY(sc.m.alloc(keep, (size_t)std::max<long long>(count, 1)));
-    FEEC_TRY(sc.m.alloc(cnt, (size_t)rows + 1)); FEEC_TRY(sc.m.alloc(start, (size_t)rows + 1));
-    FEEC_TRY(sc.m.alloc(fill, (size_t)rows + 1)); FEEC_TRY(sc.m.alloc(scr, scan_scratch_ints(rows + 1)));
-    FEEC_TRY(sc.m.alloc(idx, (size_t)std::max<long long>(count, 1)));
-    FEEC_TRY(sc.m.alloc(dC, (size_t)std::max<long long>(count, 1))); FEEC_TRY(sc.m.alloc(dV, (size_t)std::max<long long>(count, 1)));
-    FEEC_TRY(sc.m.alloc(rc, (size_t)rows + 1));
-    FEEC_TRY(cudaMemsetAsync(cnt, 0, sizeof(int) * ((size_t)rows + 1), s));
-    FEEC_TRY(cudaMemsetAsync(fill, 0, sizeof(int) * ((size_t)rows + 1), s));
-    FEEC_TRY(cudaMemsetAsync(rc, 0, sizeof(int) * ((size_t)rows + 1), s));
-    note_launch();
-    nonzero_kernel<<<grid_of(count), kAlgBlock, 0, s>>>(count, dv, keep);          // zeros dropped (:411-420)
-    note_launch();
-    count_keys_kernel<<<grid_of(count), kAlgBlock, 0, s>>>(count, dr, keep, cnt);
-    FEEC_TRY(cudaGetLastError());
-    FEEC_TRY(launch_exclusive_scan(rows + 1, cnt, start, scr, s));
-    note_launch();
-    bucket_kernel<<<grid_of(count), kAlgBlock, 0, s>>>(count, dr, keep, start, fill, idx);
-    note_launch();
-    sort_bucket_kernel<<<grid_of(rows), kAlgBlock, 0, s>>>(rows, start, idx, 0);
-    note_launch();
-    coo_row_kernel<<<grid_of(rows), kAlgBlock, 0, s>>>(rows, start, idx, dc, dv, dC, dV, rc);
-    FEEC_TRY(cudaGetLastError());
-    // rows now hold their merged entries from start[r]; compact them
-    int *off, *oA, *oC; double* oV; int n = 0;
-    FEEC_TRY(sc.m.alloc(off, (size_t)rows + 1));
-    FEEC_TRY(launch_exclusive_scan(rows + 1, rc, off, scr, s));
-    FEEC_TRY(cudaMemcpyAsync(&n, off + rows, sizeof(int), cudaMemcpyDeviceToHost, s));
-    FEEC_TRY(cudaStreamSynchronize(s));
-    FEEC_TRY(sc.m.alloc(oA, (size_t)rows + 1)); FEEC_TRY(sc.m.alloc(oC, (size_t)std::max(n, 1)));
-    FEEC_TRY(sc.m.alloc(oV, (size_t)std::max(n, 1)));
-    if (rows == 0) FEEC_TRY(cudaMemsetAsync(oA, 0, sizeof(int), s));
-    note_launch();
-    compact_rows_kernel<<<warp_grid(rows), kWarpBlock, 0, s>>>(rows, start, rc, off, dC, dV, oC, oV, oA);
-    FEEC_TRY(cudaGetLastError());
+    int *oA, *oC; double* oV; int n = 0;
+    if ((st = coo_to_csr_dev(sc.m, s, rows, count, dr, dc, dv, oA, oC, oV, n)) != FEEC_OK) return st;
     if ((st = download(s, rows, n, oA, oC, oV, A, C, V)) != FEEC_OK) return st;
     *nnz = n;
+    return FEEC_OK;
+}
+
+int feec_coo_multiply_size(int inner, long long ln, const int* lc, long long rn, const int* rr, long long* size) {
+    if (inner < 0 || ln < 0 || rn < 0 || !size || (ln > 0 && !lc) || (rn > 0 && !rr)) return FEEC_BADARG;
+    std::vector<long long> a((size_t)inner + 1, 0), b((size_t)inner + 1, 0);
+    for (long long i = 0; i < ln; i++) { if (lc[i] < 0 || lc[i] >= inner) return FEEC_BADARG; a[lc[i]]++; }
+    for (long long i = 0; i < rn; i++) { if (rr[i] < 0 || rr[i] >= inner) return FEEC_BADARG; b[rr[i]]++; }
+    long long total = 0;
+    for (int k = 0; k < inner; k++) total += a[k] * b[k];
+    *size = total;
+    return FEEC_OK;
+}
+
+int feec_coo_multiply(int lrows, int inner, int rcols, long long ln, const int* lr, const int* lc, const double* lv,
+                      long long rn, const int* rr, const int* rc, const double* rv, int* out_r, int* out_c,
+                      double* out_v, long long* count) {
+    if (lrows < 0 || inner < 0 || rcols < 0 || ln < 0 || rn < 0 || ln > INT_MAX || rn > INT_MAX || !count)
+        return FEEC_BADARG;
+    if ((ln > 0 && (!lr || !lc || !lv)) || (rn > 0 && (!rr || !rc || !rv))) return FEEC_BADARG;
+    for (long long i = 0; i < ln; i++)
+        if (lr[i] < 0 || lr[i] >= lrows || lc[i] < 0 || lc[i] >= inner) return FEEC_BADARG;
+    for (long long i = 0; i < rn; i++)
+        if (rr[i] < 0 || rr[i] >= inner || rc[i] < 0 || rc[i] >= rcols) return FEEC_BADARG;
+    int dev = 0; cudaStream_t s = nullptr;
+    int st = init_device(dev, s);
+    if (st != FEEC_OK) return st;
+    Scope sc{DevArena{}, s}; sc.m.stream = s;
+    int *dlr, *dlc, *drr, *drc; double *dlv, *drv;
+    if ((st = upload(sc.m, s, dlr, lr, (size_t)ln)) || (st = upload(sc.m, s, dlc, lc, (size_t)ln)) ||
+        (st = upload(sc.m, s, dlv, lv, (size_t)ln)) || (st = upload(sc.m, s, drr, rr, (size_t)rn)) ||
+        (st = upload(sc.m, s, drc, rc, (size_t)rn)) || (st = upload(sc.m, s, drv, rv, (size_t)rn)))
+        return st;
+    // both operands compressed (zeros dropped, equal positions summed in input order), as CSR
+    int *LA, *LC, *RA, *RC; double *LV, *RV; int lnnz = 0, rnnz = 0;
+    if ((st = coo_to_csr_dev(sc.m, s, lrows, ln, dlr, dlc, dlv, LA, LC, LV, lnnz)) != FEEC_OK) return st;
+    if ((st = coo_to_csr_dev(sc.m, s, inner, rn, drr, drc, drv, RA, RC, RV, rnnz)) != FEEC_OK) return st;
+    // room per row and the offsets of the rows' sorted entries
+    long long* P; int *E, *SD, *scr, *cnt, *big; unsigned long long* tot;
+    FEEC_TRY(sc.m.alloc(P, (size_t)lrows + 1)); FEEC_TRY(sc.m.alloc(E, (size_t)lrows + 1));
+    FEEC_TRY(sc.m.alloc(SD, (size_t)lrows + 1)); FEEC_TRY(sc.m.alloc(scr, scan_scratch_ints(lrows + 1)));
+    FEEC_TRY(sc.m.alloc(cnt, (size_t)lrows + 1)); FEEC_TRY(sc.m.alloc(big, (size_t)lrows + 1));
+    FEEC_TRY(sc.m.alloc(tot, 2));
+    FEEC_TRY(cudaMemsetAsync(tot, 0, 2 * sizeof(unsigned long long), s));
+    FEEC_TRY(cudaMemsetAsync(E + lrows, 0, sizeof(int), s));
+    FEEC_TRY(cudaMemsetAsync(cnt + lrows, 0, sizeof(int), s));
+    FEEC_TRY(cudaMemsetAsync(big + lrows, 0, sizeof(int), s));
+    note_launch();
+    mul_lengths_kernel<<<grid_of(lrows), kAlgBlock, 0, s>>>(lrows, LA, LC, RA, P);
+    note_launch();
+    product_room_kernel<<<grid_of(lrows), kAlgBlock, 0, s>>>(lrows, rcols, P, E, tot);
+    FEEC_TRY(cudaGetLastError());
+    unsigned long long room = 0;
+    FEEC_TRY(cudaMemcpyAsync(&room, tot, sizeof(room), cudaMemcpyDeviceToHost, s));
+    FEEC_TRY(cudaStreamSynchronize(s));
+    if (room > (unsigned long long)INT_MAX) return FEEC_BADARG;      // int offsets, as MatrixCSR's
+    FEEC_TRY(launch_exclusive_scan(lrows + 1, E, SD, scr, s));
+    int* RCo; double* RVo;
+    FEEC_TRY(sc.m.alloc(RCo, (size_t)std::max<unsigned long long>(room, 1)));
+    FEEC_TRY(sc.m.alloc(RVo, (size_t)std::max<unsigned long long>(room, 1)));
+    note_launch();
+    coo_product_rows_kernel<<<(int)std::max<long long>(1, (lrows + kHashWarps - 1) / kHashWarps), kHashWarps * 32, 0, s>>>(
+        lrows, LA, LC, LV, RA, RC, RV, E, SD, RCo, RVo, cnt, big);
+    FEEC_TRY(cudaGetLastError());
+    // rows whose distinct columns overflow the shared table: again, with global tables
+    int *G, *GO, *err;
+    FEEC_TRY(sc.m.alloc(G, (size_t)lrows + 1)); FEEC_TRY(sc.m.alloc(GO, (size_t)lrows + 1)); FEEC_TRY(sc.m.alloc(err, 1));
+    FEEC_TRY(cudaMemsetAsync(G + lrows, 0, sizeof(int), s));
+    FEEC_TRY(cudaMemsetAsync(err, 0, sizeof(int), s));
+    note_launch();
+    big_table_size_kernel<<<grid_of(lrows), kAlgBlock, 0, s>>>(lrows, E, big, G, tot + 1);
+    FEEC_TRY(cudaGetLastError());
+    unsigned long long gsize = 0;
+    FEEC_TRY(cudaMemcpyAsync(&gsize, tot + 1, sizeof(gsize), cudaMemcpyDeviceToHost, s));
+    FEEC_TRY(cudaStreamSynchronize(s));
+    if (gsize > 0) {
+        if (gsize > (unsigned long long)INT_MAX) return FEEC_OOM;
+        FEEC_TRY(launch_exclusive_scan(lrows + 1, G, GO, scr, s));
+        int* gkeys; double* gvals;
+        FEEC_TRY(sc.m.alloc(gkeys, (size_t)gsize)); FEEC_TRY(sc.m.alloc(gvals, (size_t)gsize));
+        note_launch();
+        coo_product_big_rows_kernel<<<warp_grid(lrows), kWarpBlock, 0, s>>>(lrows, LA, LC, LV, RA, RC, RV, big, GO,
+                                                                          gkeys, gvals, SD, RCo, RVo, cnt, err);
+        FEEC_TRY(cudaGetLastError());
+        int herr = 0;
+        FEEC_TRY(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, s));
+        FEEC_TRY(cudaStreamSynchronize(s));
+        if (herr) return FEEC_CUDA_ERROR;
+    }
+    // compaction to the final row-sorted entries, then their rows
+    int *off, *oA, *oC, *orow; double* oV; int n = 0;
+    FEEC_TRY(sc.m.alloc(off, (size_t)lrows + 1));
+    FEEC_TRY(launch_exclusive_scan(lrows + 1, cnt, off, scr, s));
+    FEEC_TRY(cudaMemcpyAsync(&n, off + lrows, sizeof(int), cudaMemcpyDeviceToHost, s));
+    FEEC_TRY(cudaStreamSynchronize(s));
+    if (n > 0 && (!out_r || !out_c || !out_v)) return FEEC_BADARG;
+    FEEC_TRY(sc.m.alloc(oA, (size_t)lrows + 1)); FEEC_TRY(sc.m.alloc(oC, (size_t)std::max(n, 1)));
+    FEEC_TRY(sc.m.alloc(oV, (size_t)std::max(n, 1))); FEEC_TRY(sc.m.alloc(orow, (size_t)std::max(n, 1)));
+    if (lrows == 0) FEEC_TRY(cudaMemsetAsync(oA, 0, sizeof(int), s));
+    note_launch();
+    compact_rows_kernel<<<warp_grid(lrows), kWarpBlock, 0, s>>>(lrows, SD, cnt, off, RCo, RVo, oC, oV, oA);
+    note_launch();
+    row_of_kernel<<<grid_of(lrows), kAlgBlock, 0, s>>>(lrows, oA, orow);
+    FEEC_TRY(cudaGetLastError());
+    if (n > 0) {
+        FEEC_TRY(cudaMemcpyAsync(out_r, orow, sizeof(int) * (size_t)n, cudaMemcpyDeviceToHost, s));
+        FEEC_TRY(cudaMemcpyAsync(out_c, oC, sizeof(int) * (size_t)n, cudaMemcpyDeviceToHost, s));
+        FEEC_TRY(cudaMemcpyAsync(out_v, oV, sizeof(double) * (size_t)n, cudaMemcpyDeviceToHost, s));
+    }
+    FEEC_TRY(cudaStreamSynchronize(s));
+    *count = n;
     return FEEC_OK;
 }
 

@@ -201,3 +201,44 @@ class Rainbow:
 
     def text(self) -> str:
         return f"num_colors: {self.num_colors}"
+
+
+class SparseMatrix:
+    """Coordinate-format matrix (sparse/sparsematrix.hpp): ``rows x columns`` with entries
+    ``(r[i], c[i], v[i])`` in any order, duplicates allowed."""
+
+    def __init__(self, rows, columns, r, c, v):
+        self.rows = int(rows)
+        self.columns = int(columns)
+        self.r = np.ascontiguousarray(r, np.int32)
+        self.c = np.ascontiguousarray(c, np.int32)
+        self.v = np.ascontiguousarray(v, np.float64)
+        if not (self.r.shape == self.c.shape == self.v.shape) or self.r.ndim != 1:
+            raise ValueError("SparseMatrix: r, c and v must be 1-D arrays of one length")
+
+    def getdimout(self): return self.rows
+    def getdimin(self): return self.columns
+    def getnumberofentries(self): return int(self.r.shape[0])
+
+    def to_csr(self) -> MatrixCSR:
+        """MatrixCSR(const SparseMatrix&) (sparse/matcsr.cpp:43-89) on the GPU."""
+        return MatrixCSR.from_coo(self.rows, self.columns, self.r, self.c, self.v)
+
+
+def SparseMatrixMultiplication(left: SparseMatrix, right: SparseMatrix) -> SparseMatrix:
+    """left * right on the GPU (sparse/sparsematrix.cpp:609-722); entries row-wise sorted."""
+    if left.columns != right.rows:
+        raise ValueError("SparseMatrixMultiplication: dimension mismatch")
+    L = _native.gpu()
+    size = ctypes.c_longlong(0)
+    _native.check(L.feec_coo_multiply_size(left.columns, left.getnumberofentries(), left.c,
+                                           right.getnumberofentries(), right.r, ctypes.byref(size)),
+                  "SparseMatrixMultiplication")
+    cap = max(int(size.value), 1)
+    r = np.empty(cap, np.int32); c = np.empty(cap, np.int32); v = np.empty(cap, np.float64)
+    count = ctypes.c_longlong(0)
+    st = L.feec_coo_multiply(left.rows, left.columns, right.columns, left.getnumberofentries(), left.r, left.c, left.v,
+                             right.getnumberofentries(), right.r, right.c, right.v, r, c, v, ctypes.byref(count))
+    _native.check(st, "SparseMatrixMultiplication")
+    n = int(count.value)
+    return SparseMatrix(left.rows, right.columns, r[:n].copy(), c[:n].copy(), v[:n].copy())

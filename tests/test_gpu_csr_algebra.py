@@ -159,3 +159,87 @@ def test_multiply_long_rows_match_oracle(cuda):
     V = rng.standard_normal(n * per_row)
     X = S.MatrixCSR(n, n, A, C, V)
     _same(S.MatrixCSRMultiplication(X, X), *oracle.csr_multiply(A, C, V, A, C, V), "long rows")
+
+
+def _coo_of(A, C, V, rng, split=0.25, zeros=0, cols=None):
+    """COO entries of a CSR, shuffled, some split into two exact halves, explicit zeros."""
+    n = len(A) - 1
+    r = np.repeat(np.arange(n, dtype=np.int32), np.diff(A)); c = C.copy(); v = V.copy()
+    s = rng.random(len(v)) < split
+    v[s] *= 0.5
+    r = np.concatenate([r, r[s], rng.integers(0, n, zeros).astype(np.int32)])
+    c = np.concatenate([c, c[s], rng.integers(0, cols or n, zeros).astype(np.int32)])
+    v = np.concatenate([v, v[s], np.zeros(zeros)])
+    p = rng.permutation(len(r))
+    return r[p], c[p], v[p]
+
+
+def test_coo_multiply_matches_reference_fixture_and_oracle(cuda):
+    """SparseMatrixMultiplication: bit-identical to the oracle; against the reference's
+    own output the structure and single-product entries bit for bit, sums of several
+    products within 16 eps of the sum of magnitudes (unspecified std::sort order)."""
+    import simplefem_gb300 as S
+    from oracle import oracle
+    g = load_golden("csr_algebra")
+    rows, cols = (int(x) for x in g["coomul_shape"])
+    inner = len(g["Y_A"]) - 1
+    L = S.SparseMatrix(rows, inner, g["coomul_l_r"], g["coomul_l_c"], g["coomul_l_v"])
+    R = S.SparseMatrix(inner, cols, g["coomul_r_r"], g["coomul_r_c"], g["coomul_r_v"])
+    P = S.SparseMatrixMultiplication(L, R)
+    r_o, c_o, v_o = oracle.coo_multiply(inner, (L.r, L.c, L.v), (R.r, R.c, R.v))
+    assert np.array_equal(P.r, r_o) and np.array_equal(P.c, c_o)
+    assert np.array_equal(P.v.view(np.int64), v_o.view(np.int64))
+    assert np.array_equal(P.r, g["coomul_out_r"]) and np.array_equal(P.c, g["coomul_out_c"])
+    _, _, mag = oracle.coo_multiply(inner, (L.r, L.c, np.abs(L.v)), (R.r, R.c, np.abs(R.v)))
+    assert np.all(np.abs(P.v - g["coomul_out_v"]) <= 16 * np.finfo(float).eps * mag)
+
+
+@pytest.mark.parametrize("dim,r,L", [(2, 2, 5), (3, 1, 4), (2, 3, 3)])
+def test_coo_multiply_matches_oracle_on_lattice(cuda, dim, r, L):
+    import simplefem_gb300 as S
+    from oracle import oracle
+    rng = np.random.default_rng(100 + dim * 10 + r)
+    A1, C1, V1 = _lattice(dim, r, L, 1)
+    A2, C2, V2 = _lattice(dim, r, L, 2)
+    n = len(A1) - 1
+    l = _coo_of(A1, C1, V1, rng, zeros=50)
+    rr = _coo_of(A2, C2, V2, rng, zeros=50)
+    P = S.SparseMatrixMultiplication(S.SparseMatrix(n, n, *l), S.SparseMatrix(n, n, *rr))
+    r_o, c_o, v_o = oracle.coo_multiply(n, l, rr)
+    assert np.array_equal(P.r, r_o) and np.array_equal(P.c, c_o)
+    assert np.array_equal(P.v.view(np.int64), v_o.view(np.int64))
+
+
+def test_coo_multiply_wide_rows_and_edge_cases(cuda):
+    """Product rows with more distinct columns than the shared-memory table holds take
+    the global-table pass; zero products are dropped before merging; empty operands."""
+    import simplefem_gb300 as S
+    from oracle import oracle
+    rng = np.random.default_rng(9)
+    inner, cols = 2000, 3000
+    # left: row 0 touches 300 columns k, rows 1..9 a few; right: 20 random columns per row
+    lr = np.concatenate([np.zeros(300, np.int32), rng.integers(1, 10, 60).astype(np.int32)])
+    lc = np.concatenate([rng.choice(inner, 300, replace=False), rng.integers(0, inner, 60)]).astype(np.int32)
+    lv = rng.standard_normal(len(lr))
+    rr = np.repeat(np.arange(inner, dtype=np.int32), 20)
+    rc = np.concatenate([rng.choice(cols, 20, replace=False) for _ in range(inner)]).astype(np.int32)
+    rv = rng.standard_normal(len(rr))
+    # two products that underflow to zero: entry (9, rc[0..]) gets only those
+    lr = np.concatenate([lr, [9]]).astype(np.int32); lc = np.concatenate([lc, [0]]).astype(np.int32)
+    lv = np.concatenate([lv, [1e-200]]); rv[:20] = np.where(np.arange(20) < 2, 1e-200, rv[:20])
+    left, right = S.SparseMatrix(10, inner, lr, lc, lv), S.SparseMatrix(inner, cols, rr, rc, rv)
+    P = S.SparseMatrixMultiplication(left, right)
+    assert np.sum(P.r == 0) > 1536            # row 0 overflowed the shared table
+    r_o, c_o, v_o = oracle.coo_multiply(inner, (lr, lc, lv), (rr, rc, rv))
+    assert np.array_equal(P.r, r_o) and np.array_equal(P.c, c_o)
+    assert np.array_equal(P.v.view(np.int64), v_o.view(np.int64))
+    E = S.SparseMatrixMultiplication(S.SparseMatrix(4, 5, [], [], []), S.SparseMatrix(5, 6, [1], [2], [3.0]))
+    assert E.getnumberofentries() == 0
+    from simplefem_gb300 import _native
+    cnt = ctypes.c_longlong(0)
+    bad = np.array([7], np.int32)
+    out_i = np.empty(4, np.int32); out_v = np.empty(4)
+    st = _native.gpu().feec_coo_multiply(4, 5, 6, 1, np.array([0], np.int32), bad, np.ones(1), 1,
+                                         np.array([1], np.int32), np.array([2], np.int32), np.ones(1),
+                                         out_i, out_i.copy(), out_v, ctypes.byref(cnt))
+    assert st == _native.FEEC_BADARG
