@@ -819,6 +819,193 @@ int oracle_coo_to_csr(int rows, long long count, const int* r, const int* c, con
     return (int)n;
 }
 
+/* solver/sparsesolver.cpp:1687-1915, ConjugateResidualSolverCSR (and the arithmetically
+ * identical _textbook variant, :1918-2156); returns K. */
+int oracle_cr(int N, double* x, const double* b, const int* A, const int* C, const double* V,
+              double* res, double precision, int print_modulo)
+{
+    (void)print_modulo;
+    double tolerance = 0.0;                                   /* :1709-1712 */
+    for (int i = 0; i < N; i++) tolerance += b[i] * b[i];
+    tolerance = precision * sqrt(tolerance);
+    tolerance = dmax(tolerance, ORACLE_DESIRED_PRECISION);
+    double* dir = nan_vector(N); double* Adir = nan_vector(N); double* Ares = nan_vector(N);
+    double* vil = nan_vector(N);
+    if (!dir || !Adir || !Ares || !vil) { free(dir); free(Adir); free(Ares); free(vil); return -1; }
+    double Ad_r = NAN, Ad_Ad = NAN;
+    int K = 0;
+    while (K < N) {
+        if (K == 0) {                                         /* :1749-1790 */
+            for (int c = 0; c < N; c++) {
+                res[c] = b[c];
+                for (int d = A[c]; d < A[c + 1]; d++) res[c] -= V[d] * x[C[d]];
+                dir[c] = res[c];
+            }
+            Ad_r = 0.0; Ad_Ad = 0.0;
+            for (int c = 0; c < N; c++) {
+                Adir[c] = 0.0;
+                for (int e = A[c]; e < A[c + 1]; e++) Adir[c] += V[e] * dir[C[e]];
+                Ares[c] = Adir[c];
+                Ad_r += Adir[c] * res[c];
+                Ad_Ad += Adir[c] * Adir[c];
+            }
+        }
+        if (!isfinite(Ad_r) || Ad_r < 0.0) break;             /* :1804-1815 */
+        if (fabs(Ad_r) < tolerance * tolerance) break;
+        if (!isfinite(Ad_Ad) || Ad_Ad < 0.0) break;           /* :1819-1833 */
+        if (sqrt(fabs(Ad_Ad)) < ORACLE_MACHINE_EPSILON) break;
+        const double alpha = Ad_r / Ad_Ad;                    /* :1840-1865 */
+        double new_Ar_r = 0.0;
+        for (int c = 0; c < N; c++) {
+            vil[c] = 0.0;
+            for (int d = A[c]; d < A[c + 1]; d++) vil[c] += V[d] * Adir[C[d]];
+            x[c] = x[c] + alpha * dir[c];
+            res[c] = res[c] - alpha * Adir[c];
+            Ares[c] = Ares[c] - alpha * vil[c];
+            new_Ar_r += Ares[c] * res[c];
+        }
+        const double beta = new_Ar_r / Ad_r;                  /* :1867-1882 */
+        Ad_Ad = 0.0;
+        for (int c = 0; c < N; c++) {
+            dir[c] = res[c] + beta * dir[c];
+            Adir[c] = Ares[c] + beta * Adir[c];
+            Ad_Ad += Adir[c] * Adir[c];
+        }
+        Ad_r = new_Ar_r;
+        K++;
+    }
+    free(dir); free(Adir); free(Ares); free(vil);
+    return K;
+}
+
+/* solver/sparsesolver.cpp:2159-2425, MINRESCSR; returns K (res = b - A x at the end). */
+int oracle_minres(int N, double* x, const double* b, const int* A, const int* C, const double* V,
+                  double* res, double precision, int print_modulo)
+{
+    (void)print_modulo;
+    double tolerance = 0.0;                                   /* :2181-2184 */
+    for (int i = 0; i < N; i++) tolerance += b[i] * b[i];
+    tolerance = precision * sqrt(tolerance);
+    tolerance = dmax(tolerance, ORACLE_DESIRED_PRECISION);
+    double* v0 = nan_vector(N); double* v1 = nan_vector(N); double* w0 = nan_vector(N); double* w1 = nan_vector(N);
+    double* vn = nan_vector(N); double* wn = nan_vector(N); double* p = nan_vector(N);
+    if (!v0 || !v1 || !w0 || !w1 || !vn || !wn || !p) {
+        free(v0); free(v1); free(w0); free(w1); free(vn); free(wn); free(p); return -1;
+    }
+    double gamma = NAN, eta = NAN, s0 = NAN, s1 = NAN, c0 = NAN, c1 = NAN;
+    int K = 0;
+    while (K < N) {
+        if (K == 0) {                                         /* :2233-2283 */
+            double gamma_sq = 0.0;
+            for (int c = 0; c < N; c++) {
+                v0[c] = 0.0; w0[c] = 0.0; v1[c] = b[c]; w1[c] = 0.0;
+                for (int d = A[c]; d < A[c + 1]; d++) v1[c] -= V[d] * x[C[d]];
+                gamma_sq += v1[c] * v1[c];
+            }
+            gamma = sqrt(gamma_sq);
+            for (int c = 0; c < N; c++) v1[c] /= gamma;
+            s0 = s1 = 0.0;
+            c0 = c1 = 1.0;
+            eta = gamma;
+        }
+        if (fabs(eta) < tolerance) break;                     /* :2290-2293 */
+        double delta = 0.0;                                   /* :2297-2313 */
+        for (int c = 0; c < N; c++) {
+            p[c] = 0.0;
+            for (int d = A[c]; d < A[c + 1]; d++) p[c] += V[d] * v1[C[d]];
+            delta += p[c] * v1[c];
+        }
+        double gamma_n_sq = 0.0;                              /* :2317-2330 */
+        for (int c = 0; c < N; c++) {
+            vn[c] = p[c] - delta * v1[c] - gamma * v0[c];
+            gamma_n_sq += vn[c] * vn[c];
+        }
+        const double gamma_n = sqrt(gamma_n_sq);
+        for (int c = 0; c < N; c++) vn[c] /= gamma_n;
+        const double alpha_0 = c1 * delta - c0 * s1 * gamma; /* :2338-2349 */
+        const double alpha_1 = sqrt(alpha_0 * alpha_0 + gamma_n * gamma_n);
+        const double alpha_2 = s1 * delta + c0 * c1 * gamma;
+        const double alpha_3 = s0 * gamma;
+        const double cn = alpha_0 / alpha_1;
+        const double sn = gamma_n / alpha_1;
+        for (int c = 0; c < N; c++) {                         /* :2353-2360 */
+            wn[c] = (v1[c] - alpha_2 * w1[c] - alpha_3 * w0[c]) / alpha_1;
+            x[c] = x[c] + cn * eta * wn[c];
+        }
+        eta = -sn * eta;                                      /* :2362-2378 */
+        double* t;
+        t = v0; v0 = v1; v1 = t;
+        t = w0; w0 = w1; w1 = t;
+        t = v1; v1 = vn; vn = t;
+        t = w1; w1 = wn; wn = t;
+        gamma = gamma_n;
+        c0 = c1; s0 = s1; c1 = cn; s1 = sn;
+        K++;
+    }
+    for (int c = 0; c < N; c++) {                             /* :2397-2403 */
+        res[c] = b[c];
+        for (int d = A[c]; d < A[c + 1]; d++) res[c] -= V[d] * x[C[d]];
+    }
+    free(v0); free(v1); free(w0); free(w1); free(vn); free(wn); free(p);
+    return K;
+}
+
+/* solver/sparsesolver.cpp:2428-2590, ChebyshevIteration_DiagonalPreconditioner; returns K.
+ * As in the reference, x receives x_next after the last rotation of the three iterates. */
+int oracle_chebyshev(int N, double* x, const double* b, const int* A, const int* C, const double* V,
+                     double* residual, double precision, int print_modulo, const double* precon,
+                     double lower, double upper)
+{
+    (void)print_modulo;
+    double tolerance = 0.0;                                   /* :2452-2455 */
+    for (int i = 0; i < N; i++) tolerance += b[i] * b[i];
+    tolerance = precision * sqrt(tolerance);
+    tolerance = dmax(tolerance, ORACLE_DESIRED_PRECISION);
+    double* z = (double*)malloc(sizeof(double) * (size_t)(N > 0 ? N : 1));
+    double* x_prev = nan_vector(N); double* x_curr = nan_vector(N); double* x_next = nan_vector(N);
+    if (!z || !x_prev || !x_curr || !x_next) { free(z); free(x_prev); free(x_curr); free(x_next); return -1; }
+    for (int c = 0; c < N; c++) x_prev[c] = x_curr[c] = x_next[c] = x[c];
+    const double alpha = 2. / (upper + lower);                /* :2486-2487 */
+    const double mu = (upper + lower) / (upper - lower);
+    double gamma_prev = NAN, gamma_curr = NAN, r_r = NAN;
+    int K = 0;
+    while (K < N) {
+        if (K == 0) {                                         /* :2499-2531 */
+            gamma_prev = 1.;
+            gamma_curr = mu;
+            r_r = 0.;
+            for (int c = 0; c < N; c++) x_prev[c] = x[c];
+            for (int c = 0; c < N; c++) {
+                residual[c] = b[c];
+                for (int d = A[c]; d < A[c + 1]; d++) residual[c] -= V[d] * x_prev[C[d]];
+                z[c] = precon[c] * residual[c];
+                x_curr[c] = x_prev[c] + alpha * z[c];
+                r_r += residual[c] * residual[c];
+            }
+        }
+        if (sqrt(r_r) < tolerance) break;                     /* :2535-2538 */
+        const double gamma_next = 2. * mu * gamma_curr - gamma_prev;   /* :2542-2563 */
+        const double omega = 2. * mu * gamma_curr / gamma_next;
+        r_r = 0.;
+        for (int c = 0; c < N; c++) {
+            residual[c] = b[c];
+            for (int d = A[c]; d < A[c + 1]; d++) residual[c] -= V[d] * x_curr[C[d]];
+            z[c] = precon[c] * residual[c];
+            x_next[c] = x_prev[c] + omega * (alpha * z[c] + x_curr[c] - x_prev[c]);
+            r_r += residual[c] * residual[c];
+        }
+        gamma_prev = gamma_curr;
+        gamma_curr = gamma_next;
+        double* t;
+        t = x_curr; x_curr = x_prev; x_prev = t;
+        t = x_next; x_next = x_curr; x_curr = t;
+        K++;
+    }
+    for (int c = 0; c < N; c++) x[c] = x_next[c];              /* :2578-2582 */
+    free(z); free(x_prev); free(x_curr); free(x_next);
+    return K;
+}
+
 /* sparse/sparsematrix.cpp:609-722, SparseMatrixMultiplication(left, right), with
  * SparseMatrix::sortandcompressentries (:405-458) for the operands and the result.
  * Operands: zeros dropped, sorted (left by column then row, right by row then column),

@@ -60,6 +60,9 @@ def lib():
         L.oracle_coo_multiply.argtypes = [ctypes.c_longlong, _i32p, _i32p, _f64p, ctypes.c_longlong, _i32p, _i32p,
                                           _f64p, _i32p, _i32p, _f64p]
         L.oracle_coo_multiply.restype = ctypes.c_longlong
+        L.oracle_cr.argtypes = L.oracle_cg.argtypes
+        L.oracle_minres.argtypes = L.oracle_cg.argtypes
+        L.oracle_chebyshev.argtypes = L.oracle_cg.argtypes + [_f64p, ctypes.c_double, ctypes.c_double]
         L.oracle_max_threads.restype = ctypes.c_int
         L.oracle_set_threads.argtypes = [ctypes.c_int]
         _lib = L
@@ -100,6 +103,34 @@ def cg(A, C, V, b, x0=None, precision=1e-10):
     x = np.zeros(n) if x0 is None else np.array(x0, np.float64)
     res = np.array(b, np.float64)
     K = lib().oracle_cg(n, x, np.ascontiguousarray(b, np.float64), A, C, V, res, float(precision), -3)
+    return K, x, res
+
+
+def cr(A, C, V, b, x0=None, precision=1e-10):
+    """ConjugateResidualSolverCSR (and _textbook, the same arithmetic): (K, x, residual)."""
+    n = len(A) - 1
+    x = np.zeros(n) if x0 is None else np.array(x0, np.float64)
+    res = np.array(b, np.float64)
+    K = lib().oracle_cr(n, x, np.ascontiguousarray(b, np.float64), A, C, V, res, float(precision), -3)
+    return K, x, res
+
+
+def minres(A, C, V, b, x0=None, precision=1e-10):
+    """MINRESCSR: (K, x, b - A x)."""
+    n = len(A) - 1
+    x = np.zeros(n) if x0 is None else np.array(x0, np.float64)
+    res = np.array(b, np.float64)
+    K = lib().oracle_minres(n, x, np.ascontiguousarray(b, np.float64), A, C, V, res, float(precision), -3)
+    return K, x, res
+
+
+def chebyshev(A, C, V, b, precon, lower, upper, x0=None, precision=1e-10):
+    """ChebyshevIteration_DiagonalPreconditioner: (K, x, residual)."""
+    n = len(A) - 1
+    x = np.zeros(n) if x0 is None else np.array(x0, np.float64)
+    res = np.array(b, np.float64)
+    K = lib().oracle_chebyshev(n, x, np.ascontiguousarray(b, np.float64), A, C, V, res, float(precision), -3,
+                               np.ascontiguousarray(precon, np.float64), float(lower), float(upper))
     return K, x, res
 
 

@@ -14,9 +14,12 @@
 //       the broken scalar mass cell by cell with a log-uniform [0.1,10] factor
 //       hashed from the cell position (cell_coefficient below).
 //       Writes the CSR plus the position of every global degree of freedom.
-//   solve <cg|diag|ssor|rainbow|eisenstat|eisenstat_rainbow> <in.csr> <in.vec b> <in.vec x0> <precision> <omega> <out.sol>
+//   solve <cg|diag|ssor|rainbow|eisenstat|eisenstat_rainbow|cr|cr_textbook|minres|chebyshev>
+//         <in.csr> <in.vec b> <in.vec x0> <precision> <omega> <out.sol>
 //       Calls ConjugateGradientSolverCSR{,_DiagonalPreconditioner (precon = 1/diagonal),_SSOR,_Rainbow,
-//       _SSOR_Eisenstat,_Eisenstat_Rainbow} (solver/sparsesolver.hpp)
+//       _SSOR_Eisenstat,_Eisenstat_Rainbow}, ConjugateResidualSolverCSR{,_textbook}, MINRESCSR or
+//       ChebyshevIteration_DiagonalPreconditioner (precon = 1/diagonal, omega = "lower:upper")
+//       (solver/sparsesolver.hpp)
 //       with print_modulo = -3; writes K, x, residual, solve seconds.
 //   rainbow <in.csr> <out.rb>        Rainbow(A) (sparse/rainbow.cpp:14-130)
 //   apply <in.csr> <in.vec> <scaling> <out.vec>   MatrixCSR::apply (sparse/matcsr.cpp:216-244)
@@ -259,6 +262,26 @@ int main(int argc, char** argv) {
             auto t0 = std::chrono::steady_clock::now();
             K = ConjugateGradientSolverCSR_Eisenstat_Rainbow((int)m.n, x.data(), b.data(), mat.getA(), mat.getC(), mat.getV(), res.data(), precision, -3, diag.raw(), omega,
                                                              rb.num_colors, rb.F.data(), rb.B.data(), rb.R.data());
+            secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        } else if (kind == "cr" || kind == "cr_textbook" || kind == "minres") {
+            auto t0 = std::chrono::steady_clock::now();
+            if (kind == "cr")
+                K = ConjugateResidualSolverCSR((int)m.n, x.data(), b.data(), mat.getA(), mat.getC(), mat.getV(), res.data(), precision, -3);
+            else if (kind == "cr_textbook")
+                K = ConjugateResidualSolverCSR_textbook((int)m.n, x.data(), b.data(), mat.getA(), mat.getC(), mat.getV(), res.data(), precision, -3);
+            else
+                K = MINRESCSR((int)m.n, x.data(), b.data(), mat.getA(), mat.getC(), mat.getV(), res.data(), precision, -3);
+            secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        } else if (kind == "chebyshev") {
+            // the omega argument carries the spectral bounds as "lower:upper"; precon = 1/diagonal
+            double lower = 0.0, upper = 0.0;
+            if (std::sscanf(argv[7], "%lf:%lf", &lower, &upper) != 2) die("chebyshev wants <lower:upper> as omega");
+            FloatVector diag = mat.getDiagonal();
+            std::vector<double> precon(m.n);
+            for (int64_t i = 0; i < m.n; i++) precon[i] = diag[i] != 0.0 ? 1.0 / diag[i] : 0.0;
+            auto t0 = std::chrono::steady_clock::now();
+            K = ChebyshevIteration_DiagonalPreconditioner((int)m.n, x.data(), b.data(), mat.getA(), mat.getC(), mat.getV(), res.data(), precision, -3,
+                                                          precon.data(), lower, upper);
             secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
         } else die("unknown solver kind");
         FILE* f = std::fopen(argv[8], "wb"); if (!f) die("cannot write sol");

@@ -12,8 +12,11 @@ compressed ``.npz`` holding:
   0.7 (``apply_out``);
 * ``Rainbow(A)``: ``rb_nc``, ``rb_F``, ``rb_B``, ``rb_R``;
 * for each solver ``cg``, ``jac`` (diagonal preconditioner 1/diagonal), ``ssor``, ``rainbow``,
-  ``eis`` (SSOR-Eisenstat), ``eisrb``
-  (Eisenstat-Rainbow) (and ``ssor13``/``rainbow13``/``eis13``/``eisrb13`` at
+  ``eis`` (SSOR-Eisenstat), ``eisrb`` (Eisenstat-Rainbow), ``cr`` / ``crt``
+  (ConjugateResidualSolverCSR and its _textbook twin), ``minres`` (MINRESCSR) and
+  ``cheb`` (ChebyshevIteration_DiagonalPreconditioner with precon = 1/diagonal and the
+  spectral bounds ``cheb_lower`` / ``cheb_upper`` of D^-1 A widened by 1 %, from a dense
+  eigensolve) (and ``ssor13``/``rainbow13``/``eis13``/``eisrb13`` at
   omega = 1.3 where listed): the returned iteration count ``<s>_K``, the solution
   ``<s>_x`` and the residual array ``<s>_res`` written by the reference, at one
   OpenMP thread (the plain CG is only correct there).
@@ -77,6 +80,17 @@ def lap5(n):
     return csrio.CsrData(np.array(A, np.int32), np.array(C, np.int32), np.array(V), n * n)
 
 
+def spectral_bounds(m):
+    """[0.99 lambda_min, 1.01 lambda_max] of D^-1 A (dense symmetric eigensolve of
+    D^-1/2 A D^-1/2; every fixture has positive diagonal)."""
+    M = np.zeros((m.n, m.n))
+    rows = np.repeat(np.arange(m.n), np.diff(m.A))
+    np.add.at(M, (rows, m.C), m.V)
+    d = 1.0 / np.sqrt(np.diag(M))
+    ev = np.linalg.eigvalsh(d[:, None] * M * d[None, :])
+    return 0.99 * float(ev[0]), 1.01 * float(ev[-1])
+
+
 def main():
     if not os.path.exists(HARNESS):
         sys.exit("build the reference harness first: make -C oracle -f Makefile.ref")
@@ -115,11 +129,16 @@ def main():
                 tag = str(om).replace(".", "")
                 solves += [(f"ssor{tag}", "ssor", om), (f"rainbow{tag}", "rainbow", om),
                            (f"eis{tag}", "eisenstat", om), (f"eisrb{tag}", "eisenstat_rainbow", om)]
+            solves += [("cr", "cr", 1.0), ("crt", "cr_textbook", 1.0), ("minres", "minres", 1.0)]
+            lo, hi = spectral_bounds(m)
+            out["cheb_lower"] = np.float64(lo); out["cheb_upper"] = np.float64(hi)
+            solves += [("cheb", "chebyshev", f"{lo!r}:{hi!r}")]
             for key, kind, om in solves:
-                run("solve", kind, t("m.csr"), t("b.vec"), t("x0.vec"), repr(PRECISION), repr(om), t("s.sol"))
+                run("solve", kind, t("m.csr"), t("b.vec"), t("x0.vec"), repr(PRECISION),
+                    om if isinstance(om, str) else repr(om), t("s.sol"))
                 K, x, res, _ = csrio.read_sol(t("s.sol"))
                 out[f"{key}_K"] = np.int64(K); out[f"{key}_x"] = x; out[f"{key}_res"] = res
-                out[f"{key}_omega"] = np.float64(om)
+                out[f"{key}_omega"] = np.float64(1.0 if isinstance(om, str) else om)
             out["precision"] = np.float64(PRECISION)
             np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **out)
             print(f"{name}: N={m.n} nnz={m.nnz} colors={nc} K(cg/ssor/rainbow/eis/eisrb)="

@@ -44,6 +44,13 @@ def test_oracle_solvers_bitexact(O, name):
         elif key == "jac":
             K, x, r = O.cg_diag(A, C, V, b, np.where(diag != 0, 1.0 / np.where(diag != 0, diag, 1.0), 0.0),
                                 precision=prec)
+        elif key in ("cr", "crt"):
+            K, x, r = O.cr(A, C, V, b, precision=prec)
+        elif key == "minres":
+            K, x, r = O.minres(A, C, V, b, precision=prec)
+        elif key == "cheb":
+            K, x, r = O.chebyshev(A, C, V, b, np.where(diag != 0, 1.0 / np.where(diag != 0, diag, 1.0), 0.0),
+                                  float(g["cheb_lower"]), float(g["cheb_upper"]), precision=prec)
         elif key.startswith("ssor"):
             K, x, r = O.cg_ssor(A, C, V, b, diag, om, precision=prec)
         elif key.startswith("eisrb"):
