@@ -405,6 +405,22 @@ def run_csr_algebra(with_cpu, reps=3):
             cms, ref = timed(lambda: oracle.csr_multiply(A, C, V, A, C, V), 1)
             leg.update({"cpu_ms": cms, "cpu_cores": os.cpu_count() or 1, "bit_identical": same(M, ref)})
         out[f"multiply_{d}d_p{r}_l{L}"] = leg
+    # SparseMatrixMultiplication of two COO operands (3D P1 refined 5x, entries shuffled)
+    A, C, V = workloads.lattice_matrix(3, 1, 5, 0)
+    n = len(A) - 1
+    rng = np.random.default_rng(4)
+    perm = rng.permutation(len(C))
+    rows = np.repeat(np.arange(n, dtype=np.int32), np.diff(A))[perm]
+    Lc = S.SparseMatrix(n, n, rows, C[perm], V[perm])
+    ms, P = timed(lambda: S.SparseMatrixMultiplication(Lc, Lc), reps)
+    leg = {"workload": f"3D P1 refined 5x: COO X*X, N={n}, {len(C)} entries -> {P.getnumberofentries()}",
+           "gpu_ms": ms}
+    if oracle is not None:
+        cms, ref = timed(lambda: oracle.coo_multiply(n, (Lc.r, Lc.c, Lc.v), (Lc.r, Lc.c, Lc.v)), 1)
+        leg.update({"cpu_ms": cms, "cpu_cores": 1, "bit_identical": bool(
+            np.array_equal(P.r, ref[0]) and np.array_equal(P.c, ref[1]) and
+            np.array_equal(P.v.view(np.int64), ref[2].view(np.int64)))})
+    out["coo_multiply_3d_p1_l5"] = leg
     A, C, V = workloads.lattice_matrix(3, 2, 6, 0)
     n = len(A) - 1
     X = S.MatrixCSR(n, n, A, C, V)

@@ -127,6 +127,38 @@ int feec_cg_csr_eisenstat_rainbow(int N, double* x, const double* b,
                                   int num_colors, const int* F, const int* B, const int* R,
                                   feec_solve_info* info);
 
+/* Replaces ConjugateResidualSolverCSR, solver/sparsesolver.hpp:89-97 (sparsesolver.cpp:1687-1915):
+ * stops when |r.A r| < tolerance^2, the reference's rule; `residual` receives the recursive
+ * residual. */
+int feec_cr_csr(int N, double* x, const double* b,
+                const int* A, const int* C, const double* V,
+                double* residual, double precision, int print_modulo,
+                feec_solve_info* info);
+
+/* Replaces ConjugateResidualSolverCSR_textbook, solver/sparsesolver.hpp:99-107
+ * (sparsesolver.cpp:1918-2156); the same arithmetic as ConjugateResidualSolverCSR. */
+int feec_cr_csr_textbook(int N, double* x, const double* b,
+                         const int* A, const int* C, const double* V,
+                         double* residual, double precision, int print_modulo,
+                         feec_solve_info* info);
+
+/* Replaces MINRESCSR, solver/sparsesolver.hpp:112-120 (sparsesolver.cpp:2159-2425): stops
+ * when |eta| < tolerance; `residual` receives b - A x. */
+int feec_minres_csr(int N, double* x, const double* b,
+                    const int* A, const int* C, const double* V,
+                    double* residual, double precision, int print_modulo,
+                    feec_solve_info* info);
+
+/* Replaces ChebyshevIteration_DiagonalPreconditioner, solver/sparsesolver.hpp:127-139
+ * (sparsesolver.cpp:2428-2590): z = precon * r, spectral bounds [lower, upper] of the
+ * preconditioned operator; stops when ||r|| < tolerance. As in the reference, x receives
+ * the iterate before the last one computed. */
+int feec_chebyshev_diag(int N, double* x, const double* b,
+                        const int* A, const int* C, const double* V,
+                        double* residual, double precision, int print_modulo,
+                        const double* precon, double lower, double upper,
+                        feec_solve_info* info);
+
 /* Replaces MatrixCSR::apply(dest, src, scaling), sparse/matcsr.cpp:216-244:
  * dest = scaling * A * src (rows x cols matrix, host pointers). */
 int feec_csr_apply(int rows, int cols, const int* A, const int* C, const double* V,

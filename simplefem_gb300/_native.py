@@ -79,6 +79,10 @@ def gpu():
         L.feec_cg_csr_diagonal_precon.argtypes = host + [_f64p, _infop]
         L.feec_system_set_diagonal_precon.argtypes = [_vp, _vp, _ip]
         L.feec_cg_csr_eisenstat_rainbow.argtypes = L.feec_cg_csr_rainbow.argtypes
+        L.feec_cr_csr.argtypes = host + [_infop]
+        L.feec_cr_csr_textbook.argtypes = host + [_infop]
+        L.feec_minres_csr.argtypes = host + [_infop]
+        L.feec_chebyshev_diag.argtypes = host + [_f64p, _dp, _dp, _infop]
         L.feec_csr_apply.argtypes = [_ip, _ip, _i32p, _i32p, _f64p, _f64p, _f64p, _dp]
         L.feec_csr_diagonal.argtypes = [_ip, _i32p, _i32p, _f64p, _f64p]
         _cp = ctypes.POINTER(ctypes.c_int)

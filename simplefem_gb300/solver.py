@@ -116,3 +116,41 @@ def ConjugateGradientSolverCSR_DiagonalPreconditioner(N, x, b, csrrows, csrcolum
                                                    float(precision), int(print_modulo), _vec(precon, "precon", N),
                                                    info)
     return _finish(st, info, "ConjugateGradientSolverCSR_DiagonalPreconditioner")
+
+
+def _plain(fn, where, N, x, b, csrrows, csrcolumns, csrvalues, residual, precision, print_modulo):
+    x = _vec(x, "x", N, True); residual = _vec(residual, "residual", N, True)
+    info = _native.FeecSolveInfo()
+    st = fn(int(N), x, _vec(b, "b", N), _ints(csrrows, "A"), _ints(csrcolumns, "C"), _vec(csrvalues, "V"), residual,
+            float(precision), int(print_modulo), info)
+    return _finish(st, info, where)
+
+
+def ConjugateResidualSolverCSR(N, x, b, csrrows, csrcolumns, csrvalues, residual, precision, print_modulo=-3):
+    """GPU replacement of ConjugateResidualSolverCSR (solver/sparsesolver.cpp:1687-1915)."""
+    return _plain(_native.gpu().feec_cr_csr, "ConjugateResidualSolverCSR", N, x, b, csrrows, csrcolumns, csrvalues,
+                  residual, precision, print_modulo)
+
+
+def ConjugateResidualSolverCSR_textbook(N, x, b, csrrows, csrcolumns, csrvalues, residual, precision,
+                                        print_modulo=-3):
+    """GPU replacement of ConjugateResidualSolverCSR_textbook (solver/sparsesolver.cpp:1918-2156)."""
+    return _plain(_native.gpu().feec_cr_csr_textbook, "ConjugateResidualSolverCSR_textbook", N, x, b, csrrows,
+                  csrcolumns, csrvalues, residual, precision, print_modulo)
+
+
+def MINRESCSR(N, x, b, csrrows, csrcolumns, csrvalues, res, precision, print_modulo=-3):
+    """GPU replacement of MINRESCSR (solver/sparsesolver.cpp:2159-2425)."""
+    return _plain(_native.gpu().feec_minres_csr, "MINRESCSR", N, x, b, csrrows, csrcolumns, csrvalues, res,
+                  precision, print_modulo)
+
+
+def ChebyshevIteration_DiagonalPreconditioner(N, x, b, csrrows, csrcolumns, csrvalues, residual, precision,
+                                              print_modulo, precon, lower, upper):
+    """GPU replacement of ChebyshevIteration_DiagonalPreconditioner (solver/sparsesolver.cpp:2428-2590)."""
+    x = _vec(x, "x", N, True); residual = _vec(residual, "residual", N, True)
+    info = _native.FeecSolveInfo()
+    st = _native.gpu().feec_chebyshev_diag(int(N), x, _vec(b, "b", N), _ints(csrrows, "A"), _ints(csrcolumns, "C"),
+                                           _vec(csrvalues, "V"), residual, float(precision), int(print_modulo),
+                                           _vec(precon, "precon", N), float(lower), float(upper), info)
+    return _finish(st, info, "ChebyshevIteration_DiagonalPreconditioner")

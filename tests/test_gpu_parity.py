@@ -57,6 +57,17 @@ def _run_dropin(g, key):
     om = float(g[key + "_omega"])
     if key == "cg":
         K = S.ConjugateGradientSolverCSR(n, x, g["b"], g["A"], g["C"], g["V"], res, prec, -3)
+    elif key == "cr":
+        K = S.ConjugateResidualSolverCSR(n, x, g["b"], g["A"], g["C"], g["V"], res, prec, -3)
+    elif key == "crt":
+        K = S.ConjugateResidualSolverCSR_textbook(n, x, g["b"], g["A"], g["C"], g["V"], res, prec, -3)
+    elif key == "minres":
+        K = S.MINRESCSR(n, x, g["b"], g["A"], g["C"], g["V"], res, prec, -3)
+    elif key == "cheb":
+        d = g["diag"]
+        precon = np.where(d != 0, 1.0 / np.where(d != 0, d, 1.0), 0.0)
+        K = S.ChebyshevIteration_DiagonalPreconditioner(n, x, g["b"], g["A"], g["C"], g["V"], res, prec, -3, precon,
+                                                        float(g["cheb_lower"]), float(g["cheb_upper"]))
     elif key == "jac":
         d = g["diag"]
         precon = np.where(d != 0, 1.0 / np.where(d != 0, d, 1.0), 0.0)
@@ -81,12 +92,19 @@ def _run_dropin(g, key):
 def test_dropin_solvers_match_reference(cuda, name):
     g = load_golden(name)
     xs, M = exact_solution(g)
-    keys = [k[:-2] for k in g if k.endswith("_K") and k[:-2] not in ("cr", "crt", "minres", "cheb")]
+    keys = [k[:-2] for k in g if k.endswith("_K")]
     tol = max(float(g["precision"]) * np.linalg.norm(g["b"]), 2.0 ** -26)
     for key in keys:
         K, x, res, info = _run_dropin(g, key)
         K_ref = int(g[key + "_K"])
-        assert info["status"] == 0, (key, info)
+        n = len(g["A"]) - 1
+        # the reference stops at K = N without converging on the smallest Laplacians (Chebyshev);
+        # conjugate residuals test "energy negative" before "energy small" (:1804-1812), so a
+        # round-off negative energy at convergence ends the solve through the breakdown branch
+        if key in ("cr", "crt") and info["status"] == 1:
+            assert info["final_norm"] < tol, (key, info)
+        else:
+            assert info["status"] == (3 if K_ref == n else 0), (key, info)
         assert abs(K - K_ref) <= max(1, int(np.ceil(0.02 * K_ref))), (key, K, K_ref)
         x_ref = g[key + "_x"]
         own_err = np.linalg.norm(x_ref - xs) / np.linalg.norm(xs)
@@ -98,6 +116,9 @@ def test_dropin_solvers_match_reference(cuda, name):
             om = float(g[key + "_omega"])
             zr = float(np.sum(res * res * g["diag"] * (2.0 - om) / om))
             assert abs(zr) < tol * tol * 1.0001, (key, zr, tol)
+        elif key == "cheb":
+            # as in the reference, x is the iterate before the one the residual belongs to
+            assert np.linalg.norm(res - g[key + "_res"]) <= 1e-6 * np.linalg.norm(g["b"]) + 1e-12, key
         else:
             # the residual array is the recursive residual; it must describe x
             true_r = g["b"] - M @ x
