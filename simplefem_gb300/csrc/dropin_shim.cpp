@@ -1,5 +1,5 @@
 // libfeec_dropin.so: exports the reference's own C++ entry points of the CSR
-// Krylov path (solver/sparsesolver.hpp:11-19, 21-31, 33-43, 46-56, 59-70, 73-84, with Float =
+// Krylov path (solver/sparsesolver.hpp:11-19, 21-31, 33-43, 46-56, 59-70, 73-84, 89-139, with Float =
 // double, the reference's default build) so that an application linked
 // against FEEC++'s solver module can link this library instead and run the
 // solves on the GPU unchanged. Each function forwards to the C ABI and returns
@@ -86,4 +86,39 @@ int ConjugateGradientSolverCSR_DiagonalPreconditioner(const int N, double* x, co
     const int st = feec_cg_csr_diagonal_precon(N, x, b, csrrows, csrcolumns, csrvalues, residual, precision,
                                                print_modulo, precon, &info);
     return checked(st, info, "ConjugateGradientSolverCSR_DiagonalPreconditioner");
+}
+
+// solver/sparsesolver.hpp:89-139: conjugate residuals, MINRES and the diagonally
+// preconditioned Chebyshev iteration.
+int ConjugateResidualSolverCSR(const int N, double* x, const double* b, const int* csrrows, const int* csrcolumns,
+                               const double* csrvalues, double* residual, double precision, int print_modulo) {
+    feec_solve_info info;
+    const int st = feec_cr_csr(N, x, b, csrrows, csrcolumns, csrvalues, residual, precision, print_modulo, &info);
+    return checked(st, info, "ConjugateResidualSolverCSR");
+}
+
+int ConjugateResidualSolverCSR_textbook(const int N, double* x, const double* b, const int* csrrows,
+                                        const int* csrcolumns, const double* csrvalues, double* residual,
+                                        double precision, int print_modulo) {
+    feec_solve_info info;
+    const int st = feec_cr_csr_textbook(N, x, b, csrrows, csrcolumns, csrvalues, residual, precision, print_modulo,
+                                        &info);
+    return checked(st, info, "ConjugateResidualSolverCSR_textbook");
+}
+
+int MINRESCSR(const int N, double* x, const double* b, const int* csrrows, const int* csrcolumns,
+              const double* csrvalues, double* res, const double precision, int print_modulo) {
+    feec_solve_info info;
+    const int st = feec_minres_csr(N, x, b, csrrows, csrcolumns, csrvalues, res, precision, print_modulo, &info);
+    return checked(st, info, "MINRESCSR");
+}
+
+int ChebyshevIteration_DiagonalPreconditioner(const int N, double* x, const double* b, const int* csrrows,
+                                              const int* csrcolumns, const double* csrvalues, double* residual,
+                                              const double precision, int print_modulo, const double* precon,
+                                              const double lower, const double upper) {
+    feec_solve_info info;
+    const int st = feec_chebyshev_diag(N, x, b, csrrows, csrcolumns, csrvalues, residual, precision, print_modulo,
+                                       precon, lower, upper, &info);
+    return checked(st, info, "ChebyshevIteration_DiagonalPreconditioner");
 }

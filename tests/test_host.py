@@ -46,7 +46,11 @@ def test_dropin_exports_reference_mangled_names(built):
                     "_Z34ConjugateGradientSolverCSR_RainbowiPdPKdPKiS3_S1_S_diS1_diS3_S3_S3_",
                     "_Z41ConjugateGradientSolverCSR_SSOR_EisenstatiPdPKdPKiS3_S1_S_diS1_d",
                     "_Z49ConjugateGradientSolverCSR_DiagonalPreconditioneriPdPKdPKiS3_S1_S_diS1_",
-                    "_Z44ConjugateGradientSolverCSR_Eisenstat_RainbowiPdPKdPKiS3_S1_S_diS1_diS3_S3_S3_"]:
+                    "_Z44ConjugateGradientSolverCSR_Eisenstat_RainbowiPdPKdPKiS3_S1_S_diS1_diS3_S3_S3_",
+                    "_Z26ConjugateResidualSolverCSRiPdPKdPKiS3_S1_S_di",
+                    "_Z35ConjugateResidualSolverCSR_textbookiPdPKdPKiS3_S1_S_di",
+                    "_Z9MINRESCSRiPdPKdPKiS3_S1_S_di",
+                    "_Z41ChebyshevIteration_DiagonalPreconditioneriPdPKdPKiS3_S1_S_diS1_dd"]:
         assert mangled in out, mangled
 
 
