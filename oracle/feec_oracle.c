@@ -1006,6 +1006,112 @@ int oracle_chebyshev(int N, double* x, const double* b, const int* A, const int*
     return K;
 }
 
+/* solver/systemsparsesolver.cpp:52-1120, the Hodge conjugate residual solvers: conjugate
+ * residuals on M = B A^-1 Bt + C (N x N; A is L x L, B N x L, Bt L x N), A^-1 applied by an
+ * inner CG to inner_precision: variant 0 diagonally preconditioned (precon = 1 / the
+ * diagonal, :76-91; HodgeConjugateResidualSolverCSR_diagonal), 1 SSOR with omega = 1
+ * (:500-516; _SSOR and HodgeConjugateResidualSolverCSR), 2 plain CG (_textbook). The inner
+ * solve of each restart starts from zero, those of the iterations from the previous inner
+ * solution (:253-277). Returns K. */
+int oracle_hodge_cr(int variant, int N, int L, double* x, const double* b,
+                    const int* Ar, const int* Ac, const double* Av, const int* Br, const int* Bc, const double* Bv,
+                    const int* Btr, const int* Btc, const double* Btv, const int* Cr, const int* Cc, const double* Cv,
+                    double* res, double precision, double inner_precision)
+{
+    const double sign_A = 1.;                                 /* systemsparsesolver.hpp:8 */
+    double tolerance = 0.0;
+    for (int i = 0; i < N; i++) tolerance += b[i] * b[i];
+    tolerance = precision * sqrt(tolerance);
+    tolerance = dmax(tolerance, ORACLE_DESIRED_PRECISION);
+    double* dir = (double*)malloc(sizeof(double) * (size_t)N);
+    double* Mdir = (double*)malloc(sizeof(double) * (size_t)N);
+    double* Mres = (double*)malloc(sizeof(double) * (size_t)N);
+    double* vil = (double*)malloc(sizeof(double) * (size_t)N);
+    double* aux1 = (double*)malloc(sizeof(double) * (size_t)L);
+    double* aux2 = (double*)malloc(sizeof(double) * (size_t)L);
+    double* auxR = (double*)malloc(sizeof(double) * (size_t)L);
+    double* diag = (double*)malloc(sizeof(double) * (size_t)L);
+    if (!dir || !Mdir || !Mres || !vil || !aux1 || !aux2 || !auxR || !diag) {
+        free(dir); free(Mdir); free(Mres); free(vil); free(aux1); free(aux2); free(auxR); free(diag); return -1;
+    }
+    for (int c = 0; c < L; c++) {                             /* :76-91 / :500-516 */
+        diag[c] = 0.;
+        for (int d = Ar[c]; d < Ar[c + 1]; d++) if (Ac[d] == c) diag[c] += Av[d];
+        if (variant == 0) diag[c] = 1. / diag[c];
+    }
+#define HODGE_INNER(xx, bb)                                                                          \
+    do {                                                                                            \
+        if (variant == 0) oracle_cg_diag(L, xx, bb, Ar, Ac, Av, auxR, inner_precision, -3, diag);   \
+        else if (variant == 1) oracle_cg_ssor(L, xx, bb, Ar, Ac, Av, auxR, inner_precision, -3, diag, 1.); \
+        else oracle_cg(L, xx, bb, Ar, Ac, Av, auxR, inner_precision, -3);                           \
+    } while (0)
+    double Md_r = NAN, Md_Md = NAN;
+    int K = 0;
+    while (K < N) {
+        if (K == 0) {                                         /* :107-200 */
+            for (int c = 0; c < L; c++) {
+                aux1[c] = 0.;
+                for (int d = Btr[c]; d < Btr[c + 1]; d++) aux1[c] += Btv[d] * x[Btc[d]];
+            }
+            for (int c = 0; c < L; c++) aux2[c] = 0.;
+            HODGE_INNER(aux2, aux1);
+            for (int c = 0; c < N; c++) {
+                res[c] = b[c];
+                for (int d = Br[c]; d < Br[c + 1]; d++) res[c] -= sign_A * Bv[d] * aux2[Bc[d]];
+                for (int d = Cr[c]; d < Cr[c + 1]; d++) res[c] -= Cv[d] * x[Cc[d]];
+                dir[c] = res[c];
+            }
+            Md_r = 0.; Md_Md = 0.;
+            for (int c = 0; c < L; c++) {
+                aux1[c] = 0;
+                for (int d = Btr[c]; d < Btr[c + 1]; d++) aux1[c] += Btv[d] * dir[Btc[d]];
+            }
+            for (int c = 0; c < L; c++) aux2[c] = 0.;
+            HODGE_INNER(aux2, aux1);
+            for (int c = 0; c < N; c++) {
+                Mdir[c] = 0.;
+                for (int d = Br[c]; d < Br[c + 1]; d++) Mdir[c] += sign_A * Bv[d] * aux2[Bc[d]];
+                for (int d = Cr[c]; d < Cr[c + 1]; d++) Mdir[c] += Cv[d] * dir[Cc[d]];
+                Mres[c] = Mdir[c];
+                Md_r += Mdir[c] * res[c];
+                Md_Md += Mdir[c] * Mdir[c];
+            }
+        }
+        if (!isfinite(Md_r) || Md_r < 0.) break;             /* :212-222 */
+        if (fabs(Md_r) < tolerance * tolerance) break;
+        if (!isfinite(Md_Md) || Md_Md < 0.) break;           /* :224-238 */
+        if (sqrt(fabs(Md_Md)) < ORACLE_MACHINE_EPSILON) break;
+        const double alpha = Md_r / Md_Md;                    /* :242-300 */
+        double new_Mr_r = 0.;
+        for (int c = 0; c < L; c++) {
+            aux1[c] = 0.;
+            for (int d = Btr[c]; d < Btr[c + 1]; d++) aux1[c] += Btv[d] * Mdir[Btc[d]];
+        }
+        HODGE_INNER(aux2, aux1);
+        for (int c = 0; c < N; c++) {
+            vil[c] = 0.;
+            for (int d = Br[c]; d < Br[c + 1]; d++) vil[c] += sign_A * Bv[d] * aux2[Bc[d]];
+            for (int d = Cr[c]; d < Cr[c + 1]; d++) vil[c] += Cv[d] * Mdir[Cc[d]];
+            x[c] = x[c] + alpha * dir[c];
+            res[c] = res[c] - alpha * Mdir[c];
+            Mres[c] = Mres[c] - alpha * vil[c];
+            new_Mr_r += Mres[c] * res[c];
+        }
+        const double beta = new_Mr_r / Md_r;                  /* :302-318 */
+        Md_Md = 0.;
+        for (int c = 0; c < N; c++) {
+            dir[c] = res[c] + beta * dir[c];
+            Mdir[c] = Mres[c] + beta * Mdir[c];
+            Md_Md += Mdir[c] * Mdir[c];
+        }
+        Md_r = new_Mr_r;
+        K++;
+    }
+#undef HODGE_INNER
+    free(dir); free(Mdir); free(Mres); free(vil); free(aux1); free(aux2); free(auxR); free(diag);
+    return K;
+}
+
 /* sparse/sparsematrix.cpp:609-722, SparseMatrixMultiplication(left, right), with
  * SparseMatrix::sortandcompressentries (:405-458) for the operands and the result.
  * Operands: zeros dropped, sorted (left by column then row, right by row then column),

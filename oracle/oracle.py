@@ -63,6 +63,8 @@ def lib():
         L.oracle_cr.argtypes = L.oracle_cg.argtypes
         L.oracle_minres.argtypes = L.oracle_cg.argtypes
         L.oracle_chebyshev.argtypes = L.oracle_cg.argtypes + [_f64p, ctypes.c_double, ctypes.c_double]
+        L.oracle_hodge_cr.argtypes = ([ctypes.c_int, ctypes.c_int, ctypes.c_int, _f64p, _f64p] + [_i32p, _i32p, _f64p] * 4
+                                      + [_f64p, ctypes.c_double, ctypes.c_double])
         L.oracle_max_threads.restype = ctypes.c_int
         L.oracle_set_threads.argtypes = [ctypes.c_int]
         _lib = L
@@ -234,3 +236,17 @@ def coo_multiply(inner, left, right):
     r = np.empty(max(cap, 1), np.int32); c = np.empty(max(cap, 1), np.int32); v = np.empty(max(cap, 1))
     n = int(lib().oracle_coo_multiply(len(lr), lr, lc, lv, len(rr), rr, rc, rv, r, c, v))
     return r[:n].copy(), c[:n].copy(), v[:n].copy()
+
+
+def hodge_cr(variant, Amat, Bmat, Btmat, Cmat, b, x0=None, precision=1e-10, inner_precision=1e-12):
+    """Hodge conjugate residuals (variant 0 diagonal, 1 SSOR, 2 plain inner CG); matrices
+    are (A, C, V) triples: A L x L, B N x L, Bt L x N, C N x N. Returns (K, x, residual)."""
+    N = len(Cmat[0]) - 1
+    L = len(Amat[0]) - 1
+    x = np.zeros(N) if x0 is None else np.array(x0, np.float64)
+    res = np.zeros(N)
+    mats = []
+    for M in (Amat, Bmat, Btmat, Cmat):
+        mats += [_i32(M[0]), _i32(M[1]), _f64(M[2])]
+    K = lib().oracle_hodge_cr(int(variant), N, L, x, _f64(b), *mats, res, float(precision), float(inner_precision))
+    return K, x, res

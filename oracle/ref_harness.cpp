@@ -29,6 +29,9 @@
 //   csrtrans <a.csr> <out.csr>                   MatrixCSR::getTranspose (sparse/matcsr.cpp:291-350)
 //   coo2csr <in.coo> <out.csr>                   MatrixCSR(SparseMatrix) (sparse/matcsr.cpp:43-89)
 //   coomul <a.coo> <b.coo> <out.coo>             SparseMatrixMultiplication (sparse/sparsematrix.cpp:609-722)
+//   hodge <diagonal|ssor|textbook|plain> <A.csr> <B.csr> <Bt.csr> <C.csr> <b.vec> <precision> <inner_precision> <out.sol>
+//       HodgeConjugateResidualSolverCSR{_diagonal,_SSOR,_textbook,} (solver/systemsparsesolver.hpp:10-72)
+//       from x0 = 0 with print_modulo = -3 and inner print_modulo = -3
 
 #include <chrono>
 #include <cmath>
@@ -49,6 +52,7 @@
 #include "mesh/examples2D.hpp"
 #include "mesh/examples3D.hpp"
 #include "solver/sparsesolver.hpp"
+#include "solver/systemsparsesolver.hpp"
 #include "fem/global.inclsullivan.hpp"
 #include "fem/global.massmatrix.hpp"
 #include "fem/global.diffmatrix.hpp"
@@ -347,6 +351,34 @@ int main(int argc, char** argv) {
     if (cmd == "coo2csr") {
         if (argc != 4) die("coo2csr <in.coo> <out.csr>");
         write_csr(argv[3], from_matrix(MatrixCSR(read_coo(argv[2]))));
+        return 0;
+    }
+    if (cmd == "hodge") {
+        if (argc != 11) die("hodge <variant> <A.csr> <B.csr> <Bt.csr> <C.csr> <b.vec> <precision> <inner_precision> <out.sol>");
+        const std::string kind = argv[2];
+        Csr A = read_csr(argv[3]), B = read_csr(argv[4]), Bt = read_csr(argv[5]), C = read_csr(argv[6]);
+        const int N = (int)C.n, L = (int)A.n;
+        std::vector<double> b = read_vec(argv[7], N), x(N, 0.0), res(N, 0.0);
+        const double precision = std::atof(argv[8]), inner = std::atof(argv[9]);
+        int K = -1;
+        auto t0 = std::chrono::steady_clock::now();
+        auto call = [&](auto fn) {
+            return fn(N, L, x.data(), b.data(), A.A.data(), A.C.data(), A.V.data(), B.A.data(), B.C.data(), B.V.data(),
+                      Bt.A.data(), Bt.C.data(), Bt.V.data(), C.A.data(), C.C.data(), C.V.data(), res.data(), precision, -3,
+                      inner, -3);
+        };
+        if (kind == "diagonal") K = call(HodgeConjugateResidualSolverCSR_diagonal);
+        else if (kind == "ssor") K = call(HodgeConjugateResidualSolverCSR_SSOR);
+        else if (kind == "textbook") K = call(HodgeConjugateResidualSolverCSR_textbook);
+        else if (kind == "plain") K = call(HodgeConjugateResidualSolverCSR);
+        else die("unknown hodge variant");
+        const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        FILE* f = std::fopen(argv[10], "wb"); if (!f) die("cannot write sol");
+        int64_t hdr[2] = {N, K};
+        write_raw(f, hdr, 16); write_raw(f, &secs, 8);
+        write_raw(f, x.data(), 8 * (size_t)N); write_raw(f, res.data(), 8 * (size_t)N);
+        std::fclose(f);
+        std::printf("K=%d secs=%.6f\n", K, secs);
         return 0;
     }
     if (cmd == "coomul") {

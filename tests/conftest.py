@@ -17,9 +17,10 @@ def pytest_configure(config):
 
 
 def golden_names():
-    """The solver fixtures (one operator each); csr_algebra.npz holds the CSR algebra cases."""
+    """The solver fixtures (one operator each); csr_algebra.npz holds the CSR algebra cases
+    and hodge.npz the block system of the Hodge solvers."""
     return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz"))
-                  if not p.endswith("csr_algebra.npz"))
+                  if not (p.endswith("csr_algebra.npz") or p.endswith("hodge.npz")))
 
 
 def load_golden(name):

@@ -115,3 +115,16 @@ def test_oracle_coo_multiply_against_reference(O):
     single = count == 1.0
     assert 0 < single.sum() < len(v)
     assert np.array_equal(v[single], ref[single])
+
+
+def test_oracle_hodge_cr_bitexact(O):
+    """The Hodge conjugate residual solvers (solver/systemsparsesolver.cpp:18-1120) exactly
+    as the reference's own code computed them: K, x and the residual."""
+    g = load_golden("hodge")
+    M = lambda k: (g[k + "_A"], g[k + "_C"], g[k + "_V"])  # noqa: E731
+    for key, variant in (("diagonal", 0), ("ssor", 1), ("textbook", 2), ("plain", 1)):
+        K, x, r = O.hodge_cr(variant, M("A"), M("B"), M("Bt"), M("C"), g["b"], precision=float(g["precision"]),
+                             inner_precision=float(g["inner_precision"]))
+        assert K == int(g[key + "_K"]), key
+        assert np.array_equal(x, g[key + "_x"]), key
+        assert np.array_equal(r, g[key + "_res"]), key
