@@ -159,6 +159,28 @@ int feec_chebyshev_diag(int N, double* x, const double* b,
                         const double* precon, double lower, double upper,
                         feec_solve_info* info);
 
+/* Hodge conjugate residual solvers, solver/systemsparsesolver.hpp:10-72
+ * (systemsparsesolver.cpp:18-1120): conjugate residuals on M = B A^-1 Bt + C with
+ * A (L x L), B (N x L), Bt (L x N), C (N x N), x, b, residual of N entries; A^-1 applied by
+ * an inner CG on A to inner_precision (feec_hodge_cr_csr_diagonal: CG with precon
+ * 1/diag(A); feec_hodge_cr_csr_ssor and feec_hodge_cr_csr: SSOR-PCG with omega = 1;
+ * feec_hodge_cr_csr_textbook: plain CG). The outer stopping rule is the reference's
+ * (|Mr.r| < tolerance^2). info->iterations is the outer K; info->outer_iterations holds the
+ * total count of inner iterations. inner_print_modulo is accepted and not used (inner
+ * solves are silent). */
+#define FEEC_HODGE_PARAMS                                                                              \
+    int N, int L, double* x, const double* b,                                                          \
+    const int* Arows, const int* Acolumns, const double* Avalues,                                      \
+    const int* Brows, const int* Bcolumns, const double* Bvalues,                                      \
+    const int* Btrows, const int* Btcolumns, const double* Btvalues,                                   \
+    const int* Crows, const int* Ccolumns, const double* Cvalues,                                      \
+    double* residual, double precision, int print_modulo,                                              \
+    double inner_precision, int inner_print_modulo, feec_solve_info* info
+int feec_hodge_cr_csr(FEEC_HODGE_PARAMS);            /* HodgeConjugateResidualSolverCSR          (:18-50)    */
+int feec_hodge_cr_csr_diagonal(FEEC_HODGE_PARAMS);   /* HodgeConjugateResidualSolverCSR_diagonal (:52-424)   */
+int feec_hodge_cr_csr_ssor(FEEC_HODGE_PARAMS);       /* HodgeConjugateResidualSolverCSR_SSOR     (:426-796)  */
+int feec_hodge_cr_csr_textbook(FEEC_HODGE_PARAMS);   /* HodgeConjugateResidualSolverCSR_textbook (:798-1120) */
+
 /* Replaces MatrixCSR::apply(dest, src, scaling), sparse/matcsr.cpp:216-244:
  * dest = scaling * A * src (rows x cols matrix, host pointers). */
 int feec_csr_apply(int rows, int cols, const int* A, const int* C, const double* V,

@@ -12,7 +12,8 @@ from .solver import (ConjugateGradientSolverCSR, ConjugateGradientSolverCSR_Diag
                      ConjugateGradientSolverCSR_Eisenstat_Rainbow, ConjugateGradientSolverCSR_Rainbow, ConjugateGradientSolverCSR_SSOR,
                      ConjugateGradientSolverCSR_SSOR_Eisenstat, ConjugateResidualSolverCSR,
                      ConjugateResidualSolverCSR_textbook, MINRESCSR, ChebyshevIteration_DiagonalPreconditioner,
-                     last_info)
+                     HodgeConjugateResidualSolverCSR, HodgeConjugateResidualSolverCSR_diagonal,
+                     HodgeConjugateResidualSolverCSR_SSOR, HodgeConjugateResidualSolverCSR_textbook, last_info)
 from .sparse import (FloatVector, MatrixCSR, MatrixCSRAddition, MatrixCSRMultiplication, Rainbow,  # noqa: F401
                      SparseMatrix, SparseMatrixMultiplication)
 
@@ -24,4 +25,6 @@ __all__ = ["MatrixCSR", "MatrixCSRAddition", "MatrixCSRMultiplication", "SparseM
            "ConjugateGradientSolverCSR_DiagonalPreconditioner", "ConjugateGradientSolverCSR_SSOR",
            "ConjugateGradientSolverCSR_Rainbow", "ConjugateGradientSolverCSR_SSOR_Eisenstat",
            "ConjugateGradientSolverCSR_Eisenstat_Rainbow", "ConjugateResidualSolverCSR",
-           "ConjugateResidualSolverCSR_textbook", "MINRESCSR", "ChebyshevIteration_DiagonalPreconditioner", "last_info", "FeecError", "machine_epsilon", "desired_precision"]
+           "ConjugateResidualSolverCSR_textbook", "MINRESCSR", "ChebyshevIteration_DiagonalPreconditioner",
+           "HodgeConjugateResidualSolverCSR", "HodgeConjugateResidualSolverCSR_diagonal",
+           "HodgeConjugateResidualSolverCSR_SSOR", "HodgeConjugateResidualSolverCSR_textbook", "last_info", "FeecError", "machine_epsilon", "desired_precision"]

@@ -83,6 +83,10 @@ def gpu():
         L.feec_cr_csr_textbook.argtypes = host + [_infop]
         L.feec_minres_csr.argtypes = host + [_infop]
         L.feec_chebyshev_diag.argtypes = host + [_f64p, _dp, _dp, _infop]
+        hodge = [_ip, _ip, _f64p, _f64p] + [_i32p, _i32p, _f64p] * 4 + [_f64p, _dp, _ip, _dp, _ip, _infop]
+        for name in ("feec_hodge_cr_csr", "feec_hodge_cr_csr_diagonal", "feec_hodge_cr_csr_ssor",
+                     "feec_hodge_cr_csr_textbook"):
+            getattr(L, name).argtypes = hodge
         L.feec_csr_apply.argtypes = [_ip, _ip, _i32p, _i32p, _f64p, _f64p, _f64p, _dp]
         L.feec_csr_diagonal.argtypes = [_ip, _i32p, _i32p, _f64p, _f64p]
         _cp = ctypes.POINTER(ctypes.c_int)

@@ -1,5 +1,6 @@
 // libfeec_dropin.so: exports the reference's own C++ entry points of the CSR
-// Krylov path (solver/sparsesolver.hpp:11-19, 21-31, 33-43, 46-56, 59-70, 73-84, 89-139, with Float =
+// Krylov path (solver/sparsesolver.hpp:11-19, 21-31, 33-43, 46-56, 59-70, 73-84, 89-139, and
+// solver/systemsparsesolver.hpp:10-72, with Float =
 // double, the reference's default build) so that an application linked
 // against FEEC++'s solver module can link this library instead and run the
 // solves on the GPU unchanged. Each function forwards to the C ABI and returns
@@ -122,3 +123,21 @@ int ChebyshevIteration_DiagonalPreconditioner(const int N, double* x, const doub
                                        precon, lower, upper, &info);
     return checked(st, info, "ChebyshevIteration_DiagonalPreconditioner");
 }
+
+// solver/systemsparsesolver.hpp:10-72: the Hodge conjugate residual solvers.
+#define FEEC_SHIM_HODGE(name, entry)                                                                          \
+    int name(const int N, const int L, double* x, const double* b, const int* Arows, const int* Acolumns,       \
+             const double* Avalues, const int* Brows, const int* Bcolumns, const double* Bvalues,               \
+             const int* Btrows, const int* Btcolumns, const double* Btvalues, const int* Crows,                 \
+             const int* Ccolumns, const double* Cvalues, double* residual, double precision, int print_modulo,  \
+             double inneriteration_precision, int inneriteration_print_modulo) {                                \
+        feec_solve_info info;                                                                                   \
+        const int st = entry(N, L, x, b, Arows, Acolumns, Avalues, Brows, Bcolumns, Bvalues, Btrows, Btcolumns, \
+                             Btvalues, Crows, Ccolumns, Cvalues, residual, precision, print_modulo,              \
+                             inneriteration_precision, inneriteration_print_modulo, &info);                     \
+        return checked(st, info, #name);                                                                        \
+    }
+FEEC_SHIM_HODGE(HodgeConjugateResidualSolverCSR, feec_hodge_cr_csr)
+FEEC_SHIM_HODGE(HodgeConjugateResidualSolverCSR_diagonal, feec_hodge_cr_csr_diagonal)
+FEEC_SHIM_HODGE(HodgeConjugateResidualSolverCSR_SSOR, feec_hodge_cr_csr_ssor)
+FEEC_SHIM_HODGE(HodgeConjugateResidualSolverCSR_textbook, feec_hodge_cr_csr_textbook)

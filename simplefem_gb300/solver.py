@@ -154,3 +154,44 @@ def ChebyshevIteration_DiagonalPreconditioner(N, x, b, csrrows, csrcolumns, csrv
                                            _vec(csrvalues, "V"), residual, float(precision), int(print_modulo),
                                            _vec(precon, "precon", N), float(lower), float(upper), info)
     return _finish(st, info, "ChebyshevIteration_DiagonalPreconditioner")
+
+
+def _hodge(entry, where, N, L, x, b, A, B, Bt, C, residual, precision, print_modulo, inner_precision,
+           inner_print_modulo):
+    x = _vec(x, "x", N, True); residual = _vec(residual, "residual", N, True)
+    mats = []
+    for name, M in (("A", A), ("B", B), ("Bt", Bt), ("C", C)):
+        mats += [_ints(M[0], name + "rows"), _ints(M[1], name + "columns"), _vec(M[2], name + "values")]
+    info = _native.FeecSolveInfo()
+    st = getattr(_native.gpu(), entry)(int(N), int(L), x, _vec(b, "b", N), *mats, residual, float(precision),
+                                       int(print_modulo), float(inner_precision), int(inner_print_modulo), info)
+    return _finish(st, info, where)
+
+
+def HodgeConjugateResidualSolverCSR(N, L, x, b, A, B, Bt, C, residual, precision, print_modulo,
+                                    inneriteration_precision, inneriteration_print_modulo=-3):
+    """GPU replacement of HodgeConjugateResidualSolverCSR (solver/systemsparsesolver.cpp:18-50):
+    conjugate residuals on B A^-1 Bt + C, inner SSOR-PCG. A, B, Bt, C are (rows, columns, values)."""
+    return _hodge("feec_hodge_cr_csr", "HodgeConjugateResidualSolverCSR", N, L, x, b, A, B, Bt, C, residual,
+                  precision, print_modulo, inneriteration_precision, inneriteration_print_modulo)
+
+
+def HodgeConjugateResidualSolverCSR_diagonal(N, L, x, b, A, B, Bt, C, residual, precision, print_modulo,
+                                             inneriteration_precision, inneriteration_print_modulo=-3):
+    """GPU replacement of HodgeConjugateResidualSolverCSR_diagonal (systemsparsesolver.cpp:52-424)."""
+    return _hodge("feec_hodge_cr_csr_diagonal", "HodgeConjugateResidualSolverCSR_diagonal", N, L, x, b, A, B, Bt, C,
+                  residual, precision, print_modulo, inneriteration_precision, inneriteration_print_modulo)
+
+
+def HodgeConjugateResidualSolverCSR_SSOR(N, L, x, b, A, B, Bt, C, residual, precision, print_modulo,
+                                         inneriteration_precision, inneriteration_print_modulo=-3):
+    """GPU replacement of HodgeConjugateResidualSolverCSR_SSOR (systemsparsesolver.cpp:426-796)."""
+    return _hodge("feec_hodge_cr_csr_ssor", "HodgeConjugateResidualSolverCSR_SSOR", N, L, x, b, A, B, Bt, C,
+                  residual, precision, print_modulo, inneriteration_precision, inneriteration_print_modulo)
+
+
+def HodgeConjugateResidualSolverCSR_textbook(N, L, x, b, A, B, Bt, C, residual, precision, print_modulo,
+                                             inneriteration_precision, inneriteration_print_modulo=-3):
+    """GPU replacement of HodgeConjugateResidualSolverCSR_textbook (systemsparsesolver.cpp:798-1120)."""
+    return _hodge("feec_hodge_cr_csr_textbook", "HodgeConjugateResidualSolverCSR_textbook", N, L, x, b, A, B, Bt, C,
+                  residual, precision, print_modulo, inneriteration_precision, inneriteration_print_modulo)

@@ -50,7 +50,11 @@ def test_dropin_exports_reference_mangled_names(built):
                     "_Z26ConjugateResidualSolverCSRiPdPKdPKiS3_S1_S_di",
                     "_Z35ConjugateResidualSolverCSR_textbookiPdPKdPKiS3_S1_S_di",
                     "_Z9MINRESCSRiPdPKdPKiS3_S1_S_di",
-                    "_Z41ChebyshevIteration_DiagonalPreconditioneriPdPKdPKiS3_S1_S_diS1_dd"]:
+                    "_Z41ChebyshevIteration_DiagonalPreconditioneriPdPKdPKiS3_S1_S_diS1_dd",
+                    "_Z31HodgeConjugateResidualSolverCSRiiPdPKdPKiS3_S1_S3_S3_S1_S3_S3_S1_S3_S3_S1_S_didi",
+                    "_Z40HodgeConjugateResidualSolverCSR_diagonaliiPdPKdPKiS3_S1_S3_S3_S1_S3_S3_S1_S3_S3_S1_S_didi",
+                    "_Z36HodgeConjugateResidualSolverCSR_SSORiiPdPKdPKiS3_S1_S3_S3_S1_S3_S3_S1_S3_S3_S1_S_didi",
+                    "_Z40HodgeConjugateResidualSolverCSR_textbookiiPdPKdPKiS3_S1_S3_S3_S1_S3_S3_S1_S3_S3_S1_S_didi"]:
         assert mangled in out, mangled
 
 
