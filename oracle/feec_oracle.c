@@ -1112,6 +1112,141 @@ int oracle_hodge_cr(int variant, int N, int L, double* x, const double* b,
     return K;
 }
 
+/* solver/systemsparsesolver.cpp:1122-1575, HodgeHerzogSoodhalterMethod: preconditioned
+ * MINRES on [[-A, Bt], [B, C]] [x_A; x_C] = [b_A; b_C] with the block preconditioner
+ * diag(PA, PC) applied by inner CG solves (each block skipped when its matrix is absent:
+ * PAr == NULL / PCr == NULL). Returns the iteration count. */
+static double odot(int n, const double* a, const double* b)
+{
+    double s = 0.;
+    for (int i = 0; i < n; i++) s += a[i] * b[i];
+    return s;
+}
+
+int oracle_hodge_hs(int dA, int dC, double* x_A, double* x_C, const double* b_A, const double* b_C,
+                    const int* Ar, const int* Ac, const double* Av, const int* Br, const int* Bc, const double* Bv,
+                    const int* Btr, const int* Btc, const double* Btv, const int* Cr, const int* Cc, const double* Cv,
+                    double precision, const int* PAr, const int* PAc, const double* PAv,
+                    const int* PCr, const int* PCc, const double* PCv, double inner_precision)
+{
+    const double sign_A = 1.;
+    double tolerance = 0.;                                    /* :1167-1171 */
+    for (int i = 0; i < dA; i++) tolerance += b_A[i] * b_A[i];
+    for (int i = 0; i < dC; i++) tolerance += b_C[i] * b_C[i];
+    tolerance = precision * sqrt(tolerance);
+    tolerance = dmax(tolerance, ORACLE_DESIRED_PRECISION);
+    double *v0_A = nan_vector(dA), *v1_A = nan_vector(dA), *w0_A = nan_vector(dA), *w1_A = nan_vector(dA);
+    double *z_A = nan_vector(dA), *vn_A = nan_vector(dA), *wn_A = nan_vector(dA), *zn_A = nan_vector(dA);
+    double *m_A = nan_vector(dA), *p_A = nan_vector(dA);
+    double *v0_C = nan_vector(dC), *v1_C = nan_vector(dC), *w0_C = nan_vector(dC), *w1_C = nan_vector(dC);
+    double *z_C = nan_vector(dC), *vn_C = nan_vector(dC), *wn_C = nan_vector(dC), *zn_C = nan_vector(dC);
+    double *m_C = nan_vector(dC), *p_C = nan_vector(dC);
+    double* all[] = {v0_A, v1_A, w0_A, w1_A, z_A, vn_A, wn_A, zn_A, m_A, p_A,
+                     v0_C, v1_C, w0_C, w1_C, z_C, vn_C, wn_C, zn_C, m_C, p_C};
+    for (int k = 0; k < 20; k++) if (!all[k]) { for (int j = 0; j < 20; j++) free(all[j]); return -1; }
+    double mu_A = NAN, mu_C = NAN, gamma = NAN, eta = NAN, eta_A = NAN, eta_C = NAN;
+    double s0 = NAN, s1 = NAN, c0 = NAN, c1 = NAN;
+    const int max_iteration_count = dA + dC;
+    int count = 0;
+    const int pa = PAr && PAc && PAv, pc = PCr && PCc && PCv;
+    (void)mu_A; (void)mu_C; (void)eta_A; (void)eta_C;
+    while (count < max_iteration_count) {
+        if (count == 0) {                                     /* :1240-1330 */
+            for (int a = 0; a < dA; a++) v0_A[a] = w0_A[a] = w1_A[a] = 0.;
+            for (int c = 0; c < dC; c++) v0_C[c] = w0_C[c] = w1_C[c] = 0.;
+            for (int r = 0; r < dA; r++) {
+                v1_A[r] = b_A[r];
+                for (int d = Ar[r]; d < Ar[r + 1]; d++) v1_A[r] += sign_A * Av[d] * x_A[Ac[d]];
+                for (int d = Btr[r]; d < Btr[r + 1]; d++) v1_A[r] -= Btv[d] * x_C[Btc[d]];
+            }
+            for (int r = 0; r < dC; r++) {
+                v1_C[r] = b_C[r];
+                for (int d = Br[r]; d < Br[r + 1]; d++) v1_C[r] -= Bv[d] * x_A[Bc[d]];
+                for (int d = Cr[r]; d < Cr[r + 1]; d++) v1_C[r] -= Cv[d] * x_C[Cc[d]];
+            }
+            for (int r = 0; r < dA; r++) z_A[r] = v1_A[r];
+            for (int r = 0; r < dC; r++) z_C[r] = v1_C[r];
+            if (pa) oracle_cg(dA, z_A, v1_A, PAr, PAc, PAv, wn_A, inner_precision, -3);
+            if (pc) oracle_cg(dC, z_C, v1_C, PCr, PCc, PCv, wn_C, inner_precision, -3);
+            const double v1_z_A = odot(dA, v1_A, z_A);
+            const double v1_z_C = odot(dC, v1_C, z_C);
+            gamma = sqrt(v1_z_A + v1_z_C);
+            for (int a = 0; a < dA; a++) { v1_A[a] /= gamma; z_A[a] /= gamma; m_A[a] = v1_A[a]; }
+            for (int c = 0; c < dC; c++) { v1_C[c] /= gamma; z_C[c] /= gamma; m_C[c] = v1_C[c]; }
+            const double psi_A = v1_z_A / (gamma * gamma);
+            const double psi_C = v1_z_C / (gamma * gamma);
+            mu_A = psi_A; mu_C = psi_C;
+            eta = gamma;
+            eta_A = gamma * sqrt(psi_A); eta_C = gamma * sqrt(psi_C);
+            s0 = s1 = 0.;
+            c0 = c1 = 1.;
+        }
+        if (fabs(eta) < tolerance) break;                     /* :1336-1339 */
+        double z_p_A = 0., z_p_C = 0.;                        /* :1345-1371 */
+        for (int r = 0; r < dA; r++) {
+            p_A[r] = 0.;
+            for (int d = Ar[r]; d < Ar[r + 1]; d++) p_A[r] -= sign_A * Av[d] * z_A[Ac[d]];
+            for (int d = Btr[r]; d < Btr[r + 1]; d++) p_A[r] += Btv[d] * z_C[Btc[d]];
+            z_p_A += p_A[r] * z_A[r];
+        }
+        for (int r = 0; r < dC; r++) {
+            p_C[r] = 0.;
+            for (int d = Br[r]; d < Br[r + 1]; d++) p_C[r] += Bv[d] * z_A[Bc[d]];
+            for (int d = Cr[r]; d < Cr[r + 1]; d++) p_C[r] += Cv[d] * z_C[Cc[d]];
+            z_p_C += p_C[r] * z_C[r];
+        }
+        const double delta = z_p_A + z_p_C;
+        for (int a = 0; a < dA; a++) vn_A[a] = p_A[a] - delta * v1_A[a] - gamma * v0_A[a];
+        for (int c = 0; c < dC; c++) vn_C[c] = p_C[c] - delta * v1_C[c] - gamma * v0_C[c];
+        double zn_vn_A = 0., zn_vn_C = 0.;
+        for (int a = 0; a < dA; a++) { zn_A[a] = vn_A[a]; zn_vn_A += zn_A[a] * vn_A[a]; }
+        for (int c = 0; c < dC; c++) { zn_C[c] = vn_C[c]; zn_vn_C += zn_C[c] * vn_C[c]; }
+        if (pa) { oracle_cg(dA, zn_A, vn_A, PAr, PAc, PAv, wn_A, inner_precision, -3); zn_vn_A = odot(dA, zn_A, vn_A); }
+        if (pc) { oracle_cg(dC, zn_C, vn_C, PCr, PCc, PCv, wn_C, inner_precision, -3); zn_vn_C = odot(dC, zn_C, vn_C); }
+        const double gamma_n = sqrt(zn_vn_A + zn_vn_C);
+        for (int a = 0; a < dA; a++) { vn_A[a] /= gamma_n; zn_A[a] /= gamma_n; }
+        for (int c = 0; c < dC; c++) { vn_C[c] /= gamma_n; zn_C[c] /= gamma_n; }
+        const double alpha_0 = c1 * delta - c0 * s1 * gamma;
+        const double alpha_1 = sqrt(alpha_0 * alpha_0 + gamma_n * gamma_n);
+        const double alpha_2 = s1 * delta + c0 * c1 * gamma;
+        const double alpha_3 = s0 * gamma;
+        const double cn = alpha_0 / alpha_1;
+        const double sn = gamma_n / alpha_1;
+        double theta_A = 0., theta_C = 0., psi_A = 0., psi_C = 0.;
+        for (int a = 0; a < dA; a++) { theta_A += m_A[a] * zn_A[a]; psi_A += zn_A[a] * vn_A[a]; }
+        for (int c = 0; c < dC; c++) { theta_C += m_C[c] * zn_C[c]; psi_C += zn_C[c] * vn_C[c]; }
+        for (int a = 0; a < dA; a++) {
+            m_A[a] = -sn * m_A[a] + cn * vn_A[a];
+            wn_A[a] = (z_A[a] - alpha_3 * w0_A[a] - alpha_2 * w1_A[a]) / alpha_1;
+            x_A[a] = x_A[a] + cn * eta * wn_A[a];
+        }
+        for (int c = 0; c < dC; c++) {
+            m_C[c] = -sn * m_C[c] + cn * vn_C[c];
+            wn_C[c] = (z_C[c] - alpha_3 * w0_C[c] - alpha_2 * w1_C[c]) / alpha_1;
+            x_C[c] = x_C[c] + cn * eta * wn_C[c];
+        }
+        mu_A = sn * sn * mu_A - 2 * sn * cn * theta_A + cn * cn * psi_A;
+        mu_C = sn * sn * mu_C - 2 * sn * cn * theta_C + cn * cn * psi_C;
+        eta = -sn * eta;
+        eta_A = eta * sqrt(psi_A); eta_C = eta * sqrt(psi_C);
+        double* t;                                            /* :1494-1503 */
+        t = v0_A; v0_A = v1_A; v1_A = t; t = v1_A; v1_A = vn_A; vn_A = t;
+        t = v0_C; v0_C = v1_C; v1_C = t; t = v1_C; v1_C = vn_C; vn_C = t;
+        t = w0_A; w0_A = w1_A; w1_A = t; t = w1_A; w1_A = wn_A; wn_A = t;
+        t = w0_C; w0_C = w1_C; w1_C = t; t = w1_C; w1_C = wn_C; wn_C = t;
+        t = z_A; z_A = zn_A; zn_A = t;
+        t = z_C; z_C = zn_C; zn_C = t;
+        gamma = gamma_n;
+        c0 = c1; c1 = cn;
+        s0 = s1; s1 = sn;
+        count++;
+    }
+    double* fin[] = {v0_A, v1_A, w0_A, w1_A, z_A, vn_A, wn_A, zn_A, m_A, p_A,
+                     v0_C, v1_C, w0_C, w1_C, z_C, vn_C, wn_C, zn_C, m_C, p_C};
+    for (int j = 0; j < 20; j++) free(fin[j]);
+    return count;
+}
+
 /* sparse/sparsematrix.cpp:609-722, SparseMatrixMultiplication(left, right), with
  * SparseMatrix::sortandcompressentries (:405-458) for the operands and the result.
  * Operands: zeros dropped, sorted (left by column then row, right by row then column),

@@ -65,6 +65,10 @@ def lib():
         L.oracle_chebyshev.argtypes = L.oracle_cg.argtypes + [_f64p, ctypes.c_double, ctypes.c_double]
         L.oracle_hodge_cr.argtypes = ([ctypes.c_int, ctypes.c_int, ctypes.c_int, _f64p, _f64p] + [_i32p, _i32p, _f64p] * 4
                                       + [_f64p, ctypes.c_double, ctypes.c_double])
+        _ip32 = ctypes.POINTER(ctypes.c_int); _dp64 = ctypes.POINTER(ctypes.c_double)
+        L.oracle_hodge_hs.argtypes = ([ctypes.c_int, ctypes.c_int, _f64p, _f64p, _f64p, _f64p]
+                                      + [_i32p, _i32p, _f64p] * 4 + [ctypes.c_double]
+                                      + [_ip32, _ip32, _dp64] * 2 + [ctypes.c_double])
         L.oracle_max_threads.restype = ctypes.c_int
         L.oracle_set_threads.argtypes = [ctypes.c_int]
         _lib = L
@@ -250,3 +254,25 @@ def hodge_cr(variant, Amat, Bmat, Btmat, Cmat, b, x0=None, precision=1e-10, inne
         mats += [_i32(M[0]), _i32(M[1]), _f64(M[2])]
     K = lib().oracle_hodge_cr(int(variant), N, L, x, _f64(b), *mats, res, float(precision), float(inner_precision))
     return K, x, res
+
+
+def hodge_hs(Amat, Bmat, Btmat, Cmat, b_A, b_C, PA=None, PC=None, precision=1e-10, inner_precision=1e-12):
+    """HodgeHerzogSoodhalterMethod from x = 0: (K, x_A, x_C). PA / PC are (rows, columns,
+    values) triples or None."""
+    dA, dC = len(Amat[0]) - 1, len(Cmat[0]) - 1
+    xA, xC = np.zeros(dA), np.zeros(dC)
+    mats = []
+    for M in (Amat, Bmat, Btmat, Cmat):
+        mats += [_i32(M[0]), _i32(M[1]), _f64(M[2])]
+    keep = []
+
+    def opt(P):
+        if P is None:
+            return [None, None, None]
+        a, c, v = _i32(P[0]), _i32(P[1]), _f64(P[2])
+        keep.extend([a, c, v])
+        return [a.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), c.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                v.ctypes.data_as(ctypes.POINTER(ctypes.c_double))]
+    K = lib().oracle_hodge_hs(dA, dC, xA, xC, _f64(b_A), _f64(b_C), *mats, float(precision), *opt(PA), *opt(PC),
+                              float(inner_precision))
+    return K, xA, xC

@@ -29,6 +29,9 @@
 //   csrtrans <a.csr> <out.csr>                   MatrixCSR::getTranspose (sparse/matcsr.cpp:291-350)
 //   coo2csr <in.coo> <out.csr>                   MatrixCSR(SparseMatrix) (sparse/matcsr.cpp:43-89)
 //   coomul <a.coo> <b.coo> <out.coo>             SparseMatrixMultiplication (sparse/sparsematrix.cpp:609-722)
+//   hhs <A.csr> <B.csr> <Bt.csr> <C.csr> <PA.csr|-> <PC.csr|-> <bA.vec> <bC.vec> <precision> <inner_precision> <out>
+//       HodgeHerzogSoodhalterMethod (solver/systemsparsesolver.hpp:74-95) from x = 0, print_modulo -3;
+//       writes int64 {dim_A, dim_C, K} then x_A and x_C
 //   hodge <diagonal|ssor|textbook|plain> <A.csr> <B.csr> <Bt.csr> <C.csr> <b.vec> <precision> <inner_precision> <out.sol>
 //       HodgeConjugateResidualSolverCSR{_diagonal,_SSOR,_textbook,} (solver/systemsparsesolver.hpp:10-72)
 //       from x0 = 0 with print_modulo = -3 and inner print_modulo = -3
@@ -379,6 +382,25 @@ int main(int argc, char** argv) {
         write_raw(f, x.data(), 8 * (size_t)N); write_raw(f, res.data(), 8 * (size_t)N);
         std::fclose(f);
         std::printf("K=%d secs=%.6f\n", K, secs);
+        return 0;
+    }
+    if (cmd == "hhs") {
+        if (argc != 13) die("hhs <A> <B> <Bt> <C> <PA|-> <PC|-> <bA> <bC> <precision> <inner_precision> <out>");
+        Csr A = read_csr(argv[2]), B = read_csr(argv[3]), Bt = read_csr(argv[4]), C = read_csr(argv[5]);
+        const bool pa = std::string(argv[6]) != "-", pc = std::string(argv[7]) != "-";
+        Csr PA = pa ? read_csr(argv[6]) : Csr(), PC = pc ? read_csr(argv[7]) : Csr();
+        const int dA = (int)A.n, dC = (int)C.n;
+        std::vector<double> bA = read_vec(argv[8], dA), bC = read_vec(argv[9], dC), xA(dA, 0.0), xC(dC, 0.0);
+        const int K = HodgeHerzogSoodhalterMethod(
+            dA, dC, xA.data(), xC.data(), bA.data(), bC.data(), A.A.data(), A.C.data(), A.V.data(), B.A.data(),
+            B.C.data(), B.V.data(), Bt.A.data(), Bt.C.data(), Bt.V.data(), C.A.data(), C.C.data(), C.V.data(),
+            std::atof(argv[10]), -3, pa ? PA.A.data() : nullptr, pa ? PA.C.data() : nullptr, pa ? PA.V.data() : nullptr,
+            pc ? PC.A.data() : nullptr, pc ? PC.C.data() : nullptr, pc ? PC.V.data() : nullptr, std::atof(argv[11]), -3);
+        FILE* f = std::fopen(argv[12], "wb"); if (!f) die("cannot write hhs");
+        int64_t hdr[3] = {dA, dC, K};
+        write_raw(f, hdr, 24); write_raw(f, xA.data(), 8 * (size_t)dA); write_raw(f, xC.data(), 8 * (size_t)dC);
+        std::fclose(f);
+        std::printf("K=%d\n", K);
         return 0;
     }
     if (cmd == "coomul") {

@@ -13,6 +13,11 @@ Stored per variant ``diagonal``, ``ssor``, ``textbook`` and ``plain``
 (HodgeConjugateResidualSolverCSR): ``<v>_K``, ``<v>_x``, ``<v>_res``, at precision 1e-10
 with inner precision 1e-12, from x0 = 0, one OpenMP thread.
 
+HodgeHerzogSoodhalterMethod (systemsparsesolver.cpp:1122-1575) on [[-A, Bt], [B, C]] with
+right-hand sides ``hhs_bA`` (L), ``hhs_bC`` (N) (seeded U[-1, 1]), for the preconditioner
+cases ``hhs_pp`` (PA = A, PC = C), ``hhs_pn`` (PA = A only) and ``hhs_nn`` (none):
+``<case>_K``, ``<case>_xA``, ``<case>_xC`` (precision 1e-10, inner precision 1e-12).
+
 Usage: python tests/golden/make_golden_hodge.py   (needs the reference sources; run once).
 """
 from __future__ import annotations
@@ -69,6 +74,20 @@ def main():
             K, x, res, _ = csrio.read_sol(t("s.sol"))
             out[f"{variant}_K"] = np.int64(K); out[f"{variant}_x"] = x; out[f"{variant}_res"] = res
             print(f"{variant}: N={N} L={L} K={K}")
+        rng2 = np.random.default_rng(4343)
+        bA = rng2.uniform(-1.0, 1.0, L); bC = rng2.uniform(-1.0, 1.0, N)
+        csrio.write_vec(t("ba.vec"), bA); csrio.write_vec(t("bc.vec"), bC)
+        out["hhs_bA"] = bA; out["hhs_bC"] = bC
+        for case, pa, pc in (("hhs_pp", t("a.csr"), t("c.csr")), ("hhs_pn", t("a.csr"), "-"), ("hhs_nn", "-", "-")):
+            run("hhs", t("a.csr"), t("b.csr"), t("bt.csr"), t("c.csr"), pa, pc, t("ba.vec"), t("bc.vec"),
+                repr(PRECISION), repr(INNER), t("h.out"))
+            with open(t("h.out"), "rb") as f:
+                buf = f.read()
+            dA, dC, K = (int(v) for v in np.frombuffer(buf, np.int64, 3, 0))
+            out[case + "_K"] = np.int64(K)
+            out[case + "_xA"] = np.frombuffer(buf, np.float64, dA, 24).copy()
+            out[case + "_xC"] = np.frombuffer(buf, np.float64, dC, 24 + 8 * dA).copy()
+            print(f"{case}: K={K}")
     np.savez_compressed(os.path.join(HERE, "hodge.npz"), **out)
 
 

@@ -128,3 +128,15 @@ def test_oracle_hodge_cr_bitexact(O):
         assert K == int(g[key + "_K"]), key
         assert np.array_equal(x, g[key + "_x"]), key
         assert np.array_equal(r, g[key + "_res"]), key
+
+
+def test_oracle_hodge_herzog_soodhalter_bitexact(O):
+    """HodgeHerzogSoodhalterMethod (solver/systemsparsesolver.cpp:1122-1575) exactly as the
+    reference computed it, with both block preconditioners, with PA only and with none."""
+    g = load_golden("hodge")
+    M = lambda k: (g[k + "_A"], g[k + "_C"], g[k + "_V"])  # noqa: E731
+    for case, PA, PC in (("hhs_pp", M("A"), M("C")), ("hhs_pn", M("A"), None), ("hhs_nn", None, None)):
+        K, xA, xC = O.hodge_hs(M("A"), M("B"), M("Bt"), M("C"), g["hhs_bA"], g["hhs_bC"], PA, PC,
+                               float(g["precision"]), float(g["inner_precision"]))
+        assert K == int(g[case + "_K"]), case
+        assert np.array_equal(xA, g[case + "_xA"]) and np.array_equal(xC, g[case + "_xC"]), case
