@@ -181,6 +181,24 @@ int feec_hodge_cr_csr_diagonal(FEEC_HODGE_PARAMS);   /* HodgeConjugateResidualSo
 int feec_hodge_cr_csr_ssor(FEEC_HODGE_PARAMS);       /* HodgeConjugateResidualSolverCSR_SSOR     (:426-796)  */
 int feec_hodge_cr_csr_textbook(FEEC_HODGE_PARAMS);   /* HodgeConjugateResidualSolverCSR_textbook (:798-1120) */
 
+/* Replaces HodgeHerzogSoodhalterMethod, solver/systemsparsesolver.hpp:74-95
+ * (systemsparsesolver.cpp:1122-1575): preconditioned MINRES on [[-A, Bt], [B, C]] [x_A; x_C] =
+ * [b_A; b_C] (A: dim_A x dim_A, Bt: dim_A x dim_C, B: dim_C x dim_A, C: dim_C x dim_C) with the
+ * block preconditioner diag(PA, PC) applied by inner CG solves to inner_precision; a block
+ * whose three arrays are not all given is skipped, as in the reference. Returns the
+ * reference's status through info; info->iterations is its iteration count and
+ * info->outer_iterations the total of inner iterations. */
+int feec_hodge_herzog_soodhalter(int dimension_A, int dimension_C, double* x_A, double* x_C,
+                                 const double* b_A, const double* b_C,
+                                 const int* Arows, const int* Acolumns, const double* Avalues,
+                                 const int* Brows, const int* Bcolumns, const double* Bvalues,
+                                 const int* Btrows, const int* Btcolumns, const double* Btvalues,
+                                 const int* Crows, const int* Ccolumns, const double* Cvalues,
+                                 double precision, int print_modulo,
+                                 const int* PArows, const int* PAcolumns, const double* PAvalues,
+                                 const int* PCrows, const int* PCcolumns, const double* PCvalues,
+                                 double inner_precision, int inner_print_modulo, feec_solve_info* info);
+
 /* Replaces MatrixCSR::apply(dest, src, scaling), sparse/matcsr.cpp:216-244:
  * dest = scaling * A * src (rows x cols matrix, host pointers). */
 int feec_csr_apply(int rows, int cols, const int* A, const int* C, const double* V,

@@ -13,7 +13,8 @@ from .solver import (ConjugateGradientSolverCSR, ConjugateGradientSolverCSR_Diag
                      ConjugateGradientSolverCSR_SSOR_Eisenstat, ConjugateResidualSolverCSR,
                      ConjugateResidualSolverCSR_textbook, MINRESCSR, ChebyshevIteration_DiagonalPreconditioner,
                      HodgeConjugateResidualSolverCSR, HodgeConjugateResidualSolverCSR_diagonal,
-                     HodgeConjugateResidualSolverCSR_SSOR, HodgeConjugateResidualSolverCSR_textbook, last_info)
+                     HodgeConjugateResidualSolverCSR_SSOR, HodgeConjugateResidualSolverCSR_textbook,
+                     HodgeHerzogSoodhalterMethod, last_info)
 from .sparse import (FloatVector, MatrixCSR, MatrixCSRAddition, MatrixCSRMultiplication, Rainbow,  # noqa: F401
                      SparseMatrix, SparseMatrixMultiplication)
 
@@ -27,4 +28,5 @@ __all__ = ["MatrixCSR", "MatrixCSRAddition", "MatrixCSRMultiplication", "SparseM
            "ConjugateGradientSolverCSR_Eisenstat_Rainbow", "ConjugateResidualSolverCSR",
            "ConjugateResidualSolverCSR_textbook", "MINRESCSR", "ChebyshevIteration_DiagonalPreconditioner",
            "HodgeConjugateResidualSolverCSR", "HodgeConjugateResidualSolverCSR_diagonal",
-           "HodgeConjugateResidualSolverCSR_SSOR", "HodgeConjugateResidualSolverCSR_textbook", "last_info", "FeecError", "machine_epsilon", "desired_precision"]
+           "HodgeConjugateResidualSolverCSR_SSOR", "HodgeConjugateResidualSolverCSR_textbook",
+           "HodgeHerzogSoodhalterMethod", "last_info", "FeecError", "machine_epsilon", "desired_precision"]

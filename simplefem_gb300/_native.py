@@ -87,6 +87,9 @@ def gpu():
         for name in ("feec_hodge_cr_csr", "feec_hodge_cr_csr_diagonal", "feec_hodge_cr_csr_ssor",
                      "feec_hodge_cr_csr_textbook"):
             getattr(L, name).argtypes = hodge
+        _ip32 = ctypes.POINTER(ctypes.c_int); _dp64 = ctypes.POINTER(ctypes.c_double)
+        L.feec_hodge_herzog_soodhalter.argtypes = ([_ip, _ip, _f64p, _f64p, _f64p, _f64p] + [_i32p, _i32p, _f64p] * 4
+                                                   + [_dp, _ip] + [_ip32, _ip32, _dp64] * 2 + [_dp, _ip, _infop])
         L.feec_csr_apply.argtypes = [_ip, _ip, _i32p, _i32p, _f64p, _f64p, _f64p, _dp]
         L.feec_csr_diagonal.argtypes = [_ip, _i32p, _i32p, _f64p, _f64p]
         _cp = ctypes.POINTER(ctypes.c_int)

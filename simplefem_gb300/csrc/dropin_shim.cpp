@@ -141,3 +141,20 @@ FEEC_SHIM_HODGE(HodgeConjugateResidualSolverCSR, feec_hodge_cr_csr)
 FEEC_SHIM_HODGE(HodgeConjugateResidualSolverCSR_diagonal, feec_hodge_cr_csr_diagonal)
 FEEC_SHIM_HODGE(HodgeConjugateResidualSolverCSR_SSOR, feec_hodge_cr_csr_ssor)
 FEEC_SHIM_HODGE(HodgeConjugateResidualSolverCSR_textbook, feec_hodge_cr_csr_textbook)
+
+int HodgeHerzogSoodhalterMethod(const int dimension_A, const int dimension_C, double* x_A, double* x_C,
+                                const double* b_A, const double* b_C, const int* Arows, const int* Acolumns,
+                                const double* Avalues, const int* Brows, const int* Bcolumns, const double* Bvalues,
+                                const int* Btrows, const int* Btcolumns, const double* Btvalues, const int* Crows,
+                                const int* Ccolumns, const double* Cvalues, double precision, int print_modulo,
+                                const int* PArows, const int* PAcolumns, const double* PAvalues, const int* PCrows,
+                                const int* PCcolumns, const double* PCvalues, double inneriteration_precision,
+                                int inneriteration_print_modulo) {
+    feec_solve_info info;
+    const int st = feec_hodge_herzog_soodhalter(dimension_A, dimension_C, x_A, x_C, b_A, b_C, Arows, Acolumns, Avalues,
+                                                Brows, Bcolumns, Bvalues, Btrows, Btcolumns, Btvalues, Crows, Ccolumns,
+                                                Cvalues, precision, print_modulo, PArows, PAcolumns, PAvalues, PCrows,
+                                                PCcolumns, PCvalues, inneriteration_precision,
+                                                inneriteration_print_modulo, &info);
+    return checked(st, info, "HodgeHerzogSoodhalterMethod");
+}

@@ -195,3 +195,31 @@ def HodgeConjugateResidualSolverCSR_textbook(N, L, x, b, A, B, Bt, C, residual, 
     """GPU replacement of HodgeConjugateResidualSolverCSR_textbook (systemsparsesolver.cpp:798-1120)."""
     return _hodge("feec_hodge_cr_csr_textbook", "HodgeConjugateResidualSolverCSR_textbook", N, L, x, b, A, B, Bt, C,
                   residual, precision, print_modulo, inneriteration_precision, inneriteration_print_modulo)
+
+
+def HodgeHerzogSoodhalterMethod(dimension_A, dimension_C, x_A, x_C, b_A, b_C, A, B, Bt, C, precision, print_modulo,
+                                PA, PC, inneriteration_precision, inneriteration_print_modulo=-3):
+    """GPU replacement of HodgeHerzogSoodhalterMethod (solver/systemsparsesolver.cpp:1122-1575):
+    block-preconditioned MINRES on [[-A, Bt], [B, C]]. A, B, Bt, C (and PA, PC, or None) are
+    (rows, columns, values) triples."""
+    import ctypes
+    dA, dC = int(dimension_A), int(dimension_C)
+    x_A = _vec(x_A, "x_A", dA, True); x_C = _vec(x_C, "x_C", dC, True)
+    mats = []
+    for name, M in (("A", A), ("B", B), ("Bt", Bt), ("C", C)):
+        mats += [_ints(M[0], name + "rows"), _ints(M[1], name + "columns"), _vec(M[2], name + "values")]
+    keep = []
+
+    def opt(P, name):
+        if P is None:
+            return [None, None, None]
+        r, c, v = _ints(P[0], name + "rows"), _ints(P[1], name + "columns"), _vec(P[2], name + "values")
+        keep.extend([r, c, v])
+        return [r.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), c.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                v.ctypes.data_as(ctypes.POINTER(ctypes.c_double))]
+    info = _native.FeecSolveInfo()
+    st = _native.gpu().feec_hodge_herzog_soodhalter(dA, dC, x_A, x_C, _vec(b_A, "b_A", dA), _vec(b_C, "b_C", dC),
+                                                    *mats, float(precision), int(print_modulo), *opt(PA, "PA"),
+                                                    *opt(PC, "PC"), float(inneriteration_precision),
+                                                    int(inneriteration_print_modulo), info)
+    return _finish(st, info, "HodgeHerzogSoodhalterMethod")

@@ -112,3 +112,36 @@ def test_hodge_rejects_out_of_range_columns(cuda):
                                                   g["C_A"], g["C_C"], g["C_V"], np.zeros(N), 1e-10, -3, 1e-12, -3,
                                                   ctypes.byref(info))
     assert st == _native.FEEC_BADARG
+
+
+def test_herzog_soodhalter_matches_reference_fixture(cuda):
+    """HodgeHerzogSoodhalterMethod with both, one and no block preconditioners: solution
+    within max(1e-9, 2 x the reference's own error against a dense solve of the saddle-point
+    system); iteration count within the oracle's one-ulp band plus one."""
+    import simplefem_gb300 as S
+    from oracle import oracle
+    g = load_golden("hodge")
+    M = lambda k: (g[k + "_A"], g[k + "_C"], g[k + "_V"])  # noqa: E731
+    dC, dA = len(g["C_A"]) - 1, len(g["A_A"]) - 1
+    K_full = np.block([[-_dense(M("A"), dA, dA), _dense(M("Bt"), dA, dC)],
+                       [_dense(M("B"), dC, dA), _dense(M("C"), dC, dC)]])
+    xs = np.linalg.solve(K_full, np.concatenate([g["hhs_bA"], g["hhs_bC"]]))
+    prec, inner = float(g["precision"]), float(g["inner_precision"])
+    oracle.set_threads(1)
+    for case, PA, PC in (("hhs_pp", M("A"), M("C")), ("hhs_pn", M("A"), None), ("hhs_nn", None, None)):
+        xA = np.zeros(dA); xC = np.zeros(dC)
+        K = S.HodgeHerzogSoodhalterMethod(dA, dC, xA, xC, g["hhs_bA"], g["hhs_bC"], M("A"), M("B"), M("Bt"), M("C"),
+                                          prec, -3, PA, PC, inner, -3)
+        info = S.last_info()
+        K_ref = int(g[case + "_K"])
+        assert info["status"] == (0 if K_ref < dA + dC else 3), (case, info)
+        band = 0
+        for sc in (1 + 1e-15, 1 - 1e-15):
+            K_p, _, _ = oracle.hodge_hs(M("A"), M("B"), M("Bt"), M("C"), g["hhs_bA"] * sc, g["hhs_bC"] * sc, PA, PC,
+                                        prec, inner)
+            band = max(band, abs(K_p - K_ref))
+        assert _close_K(K, K_ref) or abs(K - K_ref) <= band + 1, (case, K, K_ref, band)
+        x_ref = np.concatenate([g[case + "_xA"], g[case + "_xC"]])
+        own = np.linalg.norm(x_ref - xs) / np.linalg.norm(xs)
+        diff = np.linalg.norm(np.concatenate([xA, xC]) - x_ref) / np.linalg.norm(x_ref)
+        assert diff <= max(1e-9, 2.0 * own), (case, diff, own)

@@ -54,7 +54,8 @@ def test_dropin_exports_reference_mangled_names(built):
                     "_Z31HodgeConjugateResidualSolverCSRiiPdPKdPKiS3_S1_S3_S3_S1_S3_S3_S1_S3_S3_S1_S_didi",
                     "_Z40HodgeConjugateResidualSolverCSR_diagonaliiPdPKdPKiS3_S1_S3_S3_S1_S3_S3_S1_S3_S3_S1_S_didi",
                     "_Z36HodgeConjugateResidualSolverCSR_SSORiiPdPKdPKiS3_S1_S3_S3_S1_S3_S3_S1_S3_S3_S1_S_didi",
-                    "_Z40HodgeConjugateResidualSolverCSR_textbookiiPdPKdPKiS3_S1_S3_S3_S1_S3_S3_S1_S3_S3_S1_S_didi"]:
+                    "_Z40HodgeConjugateResidualSolverCSR_textbookiiPdPKdPKiS3_S1_S3_S3_S1_S3_S3_S1_S3_S3_S1_S_didi",
+                    "_Z27HodgeHerzogSoodhalterMethodiiPdS_PKdS1_PKiS3_S1_S3_S3_S1_S3_S3_S1_S3_S3_S1_diS3_S3_S1_S3_S3_S1_di"]:
         assert mangled in out, mangled
 
 
