@@ -436,6 +436,67 @@ def run_csr_algebra(with_cpu, reps=3):
     return out
 
 
+def run_krylov_more(with_cpu):
+    """The further drop-in drivers through their host-pointer entry points (upload inside the
+    call): conjugate residuals and MINRES beside plain CG on the 3D P1 operator refined 6x,
+    and the Hodge conjugate residual solver (inner SSOR-PCG) on a block system. The CPU
+    column is the oracle restatement (serial, as the reference's loops run per thread)."""
+    import simplefem_gb300 as S
+    from simplefem_gb300 import workloads
+    oracle = None
+    if with_cpu:
+        from oracle import oracle
+        oracle.set_threads(1)
+    A, C, V = workloads.lattice_matrix(3, 1, 6, 0)
+    n = len(A) - 1
+    b = workloads.uniform_vector(17, n)
+    out = {"workload": f"3D P1 refined 6x, N={n}, nnz={len(C)}, precision 1e-10, host arrays in and out"}
+    for name, fn, ofn in (("cg", S.ConjugateGradientSolverCSR, None),
+                          ("cr", S.ConjugateResidualSolverCSR, None if oracle is None else oracle.cr),
+                          ("minres", S.MINRESCSR, None if oracle is None else oracle.minres)):
+        x = np.zeros(n); res = np.zeros(n)
+        fn(n, x, b, A, C, V, res, 1e-10, -3)                     # warm-up
+        x = np.zeros(n); res = np.zeros(n)
+        t0 = time.perf_counter()
+        K = fn(n, x, b, A, C, V, res, 1e-10, -3)
+        wall = 1000.0 * (time.perf_counter() - t0)
+        info = S.last_info()
+        leg = {"iterations": K, "status": info["status"], "call_ms": wall, "device_ms": info["device_ms"]}
+        if ofn is not None:
+            t0 = time.perf_counter()
+            K_o, _, _ = ofn(A, C, V, b, precision=1e-10)
+            leg.update({"cpu_ms": 1000.0 * (time.perf_counter() - t0), "cpu_iterations": K_o, "cpu_cores": 1})
+        out[name] = leg
+    # Hodge: A = 3D P1 refined 5x (L = 35,937), C = 2D P1 refined 7x (N = 16,641), B 6 entries per row
+    rng = np.random.default_rng(12)
+    Am = workloads.lattice_matrix(3, 1, 5, 0)
+    Cm = workloads.lattice_matrix(2, 1, 7, 3)
+    L, N = len(Am[0]) - 1, len(Cm[0]) - 1
+    cols = np.concatenate([np.sort(rng.choice(L, 6, replace=False)) for _ in range(N)]).astype(np.int32)
+    Bm = (np.arange(0, 6 * N + 1, 6, dtype=np.int32), cols, rng.uniform(-1, 1, 6 * N))
+    Btm = S.MatrixCSR(N, L, *Bm).getTranspose()
+    Btm = (Btm.A, Btm.C, Btm.V)
+    bh = rng.uniform(-1, 1, N)
+    for key, fn, variant, inner_name in (("hodge_cr_ssor", S.HodgeConjugateResidualSolverCSR, 1, "SSOR-PCG"),
+                                         ("hodge_cr_diagonal", S.HodgeConjugateResidualSolverCSR_diagonal, 0,
+                                          "diagonal PCG")):
+        x = np.zeros(N); res = np.zeros(N)
+        t0 = time.perf_counter()
+        K = fn(N, L, x, bh, Am, Bm, Btm, Cm, res, 1e-8, -3, 1e-10)
+        wall = 1000.0 * (time.perf_counter() - t0)
+        info = S.last_info()
+        leg = {"workload": f"CR on B A^-1 Bt + C: A 3D P1 L5 (L={L}), C 2D P1 L7 (N={N}), B 6/row; "
+                           f"precision 1e-8, inner {inner_name} to 1e-10",
+               "outer_iterations": K, "inner_iterations": info["outer_iterations"], "status": info["status"],
+               "call_ms": wall}
+        if oracle is not None:
+            t0 = time.perf_counter()
+            K_o, _, _ = oracle.hodge_cr(variant, Am, Bm, Btm, Cm, bh, precision=1e-8, inner_precision=1e-10)
+            leg.update({"cpu_ms": 1000.0 * (time.perf_counter() - t0), "cpu_outer_iterations": K_o, "cpu_cores": 1})
+        out[key] = leg
+    return out
+
+
 def run_serving(mode, method, count=200, rate=200.0, slots=24, budget=120 * 10**9):
     """Poisson-arrival request stream through the continuous-batching server."""
     from simplefem_gb300 import workloads
@@ -500,6 +561,10 @@ def run_ours(args):
     if args.only_mixed_large:
         if rank == 0:
             print(json.dumps({"mixed_large": run_mixed_large(dev)}), flush=True)
+        return
+    if args.only_krylov_more:
+        if rank == 0:
+            print(json.dumps({"krylov_more": run_krylov_more(not args.no_cpu)}), flush=True)
         return
     if args.only_csr_algebra:
         if rank == 0:
@@ -688,6 +753,7 @@ def run_ours(args):
     block_rhs = run_block_rhs(dev) if not args.skip_extras else None
     mixed_large = run_mixed_large(dev) if not args.skip_extras else None
     csr_algebra = run_csr_algebra(rank == 0 and not args.no_cpu) if not args.skip_extras else None
+    krylov_more = run_krylov_more(rank == 0 and not args.no_cpu) if not args.skip_extras else None
     serving = None
     if not args.skip_extras:
         serving = {"mixed_rainbow": run_serving("mixed", "rainbow", args.requests),
@@ -745,6 +811,7 @@ def run_ours(args):
             "block_rhs_64": block_rhs,
             "mixed_large": mixed_large,
             "csr_algebra": csr_algebra,
+            "krylov_more": krylov_more,
             "serving": serving,
             "roofline": roofline,
             "cpu_baseline": cpu,
@@ -773,6 +840,7 @@ def main():
     ap.add_argument("--only-block-rhs", action="store_true", help="only the 64 right-hand-side blocked batch")
     ap.add_argument("--only-mixed-large", action="store_true", help="only the 3D P1 L7 mixed-precision solves")
     ap.add_argument("--only-csr-algebra", action="store_true", help="only the CSR algebra leg (product, transpose, sum)")
+    ap.add_argument("--only-krylov-more", action="store_true", help="only the CR / MINRES / Hodge leg")
     ap.add_argument("--only-batched", action="store_true",
                     help="only the batched headline step (no single-solve, SpMV, CPU or extra legs)")
     ap.add_argument("--rhs-per-team", type=int, default=0,
