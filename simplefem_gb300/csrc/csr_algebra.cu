@@ -42,119 +42,116 @@ int grid_of(long long n) { return (int)std::max<long long>(1, (n + kAlgBlock - 1
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int kWarpsPerBlock = 4;
 constexpr int kWarpBlock = kWarpsPerBlock * 32;
-constexpr int kRowCap = 1024;   // entries of one row staged in shared memory per warp (12 KB)
+constexpr int kRowCap = 1024;   // (column, slot) entries of one row staged in shared memory per warp (8 KB)
 
 int warp_grid(long long rows) { return (int)std::max<long long>(1, (rows + kWarpsPerBlock - 1) / kWarpsPerBlock); }
 
-// Values travel through the sort as the two 32-bit halves of their bit patterns: every
-// move, select and shuffle stays on the 32-bit integer pipes (64-bit operations share
-// the GPU's narrow FP64 pipe), and a value is a zero exactly when its bits other than
-// the sign are all zero.
-__device__ __forceinline__ bool nonzero_halves(unsigned hi, unsigned lo) { return ((hi << 1) | lo) != 0u; }
+// The sort carries, for each entry, its column and a slot: the position of its value in a
+// value array that stays in place. Bit 31 of the slot marks a value known to be zero
+// (initially zero, or emptied by a merge). A merge with a zero operand moves slots
+// instead of values (x + 0 and 0 + x are x, up to the sign of a zero sum, and zeros are
+// dropped afterwards), so the pipeline is 32-bit integer work; only a merge of two
+// nonzeros adds, out of line and in the value array. A sum that cancels to zero keeps its
+// slot unflagged: adding into it later gives exactly the other operand, as the serial
+// sort does.
+constexpr int kZeroSlot = (int)0x80000000u;
 
-// r + x in FP64 where `add` is set, else r. Kept out of line: compiled inline, the add is
+// v[r] += v[x] where `add` is set. Kept out of line: compiled inline, the add is
 // if-converted and then occupies the FP64 pipe on every step of the sort.
-__device__ __noinline__ uint2 merge_add(bool add, uint2 r, uint2 x) {
-    if (!add) return r;
-    const double t = __hiloint2double((int)r.y, (int)r.x) + __hiloint2double((int)x.y, (int)x.x);
-    return make_uint2((unsigned)__double2loint(t), (unsigned)__double2hiint(t));
+__device__ __noinline__ void slot_add(bool add, double* v, int r, int x) {
+    if (add) v[r] = v[r] + v[x];
 }
 
-// The reference's per-row exchange sort (sparse/matcsr.cpp:601-622) on c[0, L), v[0, L),
-// run by one warp as a systolic pipeline. Pass p of the reference keeps a running
-// minimum (column, value) in a register, scans positions p+1.., merges equal columns
-// into it (zeroing the merged entry) and swaps smaller ones in; at its end the register
-// is stored at position p. Lane k runs pass i+k of a sweep of 32 passes, one step behind
-// lane k-1: it receives each element after lane k-1 has processed it and hands it on.
-// Every pass therefore sees every position in exactly the state the serial sort gives
-// it, and every sum is formed in the serial order, at about L*L/64 warp steps instead
-// of L*L/2 serial ones. The stream enters at lane 0 (a broadcast load one element
-// ahead) and leaves at lane 31; columns are >= 0, -1 marks no element.
-//
-// A merge where either value is zero is a select: x + 0 and 0 + x are x, up to the sign
-// of a zero sum, and zeros are dropped afterwards, so the kept entries are bit-identical.
-// Only merges of two nonzeros (a few percent of the steps) issue a warp-wide FP64 add.
-__device__ void warp_exchange_sort(int* c, uint2* v, int L, int lane) {
+// The reference's per-row exchange sort (sparse/matcsr.cpp:601-622) on the entries
+// cs[0, L) = (column, slot), values v[slot], run by one warp as a systolic pipeline. Pass p
+// of the reference keeps a running minimum (column, value) in a register, scans positions
+// p+1.., merges equal columns into it (zeroing the merged entry) and swaps smaller ones in;
+// at its end the register is stored at position p. Lane k runs pass i+k of a sweep of 32
+// passes, one step behind lane k-1: it receives each entry after lane k-1 has processed it
+// and hands it on. Every pass therefore sees every position in exactly the state the serial
+// sort gives it, and every sum is formed in the serial order, at about L*L/64 warp steps
+// instead of L*L/2 serial ones. The stream enters at lane 0 (a broadcast load one entry
+// ahead) and leaves at lane 31; columns are >= 0, -1 marks no entry.
+__device__ void warp_exchange_sort(int2* cs, double* v, int L, int lane) {
     for (int i = 0; i < L; i += 32) {
-        int rc = 0; unsigned rh = 0, rl = 0;          // register of pass i + lane
-        int pc = -1; unsigned ph = 0, pl = 0;         // element this lane hands on (-1: none)
-        int nc = c[i]; uint2 nv = v[i];               // next element of the stream (all lanes)
+        int rc = 0, rs = 0;                   // register of pass i + lane
+        int pc = -1, ps = 0;                  // entry this lane hands on (-1: none)
+        int2 nx = cs[i];                      // next entry of the stream (all lanes)
         const int steps = (L - i) + 31;
         for (int s = 0; s < steps; s++) {
             int xc = __shfl_up_sync(kFull, pc, 1);
-            unsigned xh = __shfl_up_sync(kFull, ph, 1);
-            unsigned xl = __shfl_up_sync(kFull, pl, 1);
-            if (lane == 0) { xc = nc; xl = nv.x; xh = nv.y; }
+            int xs = __shfl_up_sync(kFull, ps, 1);
+            if (lane == 0) { xc = nx.x; xs = nx.y; }
             const int q1 = i + s + 1;
-            if (q1 < L) { nc = c[q1]; nv = v[q1]; } else { nc = -1; }
+            if (q1 < L) nx = cs[q1]; else nx.x = -1;
             const bool valid = xc >= 0;
             const bool reg = valid && s == 2 * lane;          // position i + lane: the register
             const bool proc = valid && !reg;
             const bool eq = proc && xc == rc;
             const bool lt = proc && xc < rc;
-            const bool rnz = nonzero_halves(rh, rl), xnz = nonzero_halves(xh, xl);
-            const bool add = eq && rnz && xnz;
-            if (__any_sync(kFull, add)) {          // rare: a real call, so the add is not speculated
-                const uint2 t = merge_add(add, make_uint2(rl, rh), make_uint2(xl, xh));
-                rl = t.x; rh = t.y;
+            const bool rz = rs < 0, xz = xs < 0;
+            const bool add = eq && !rz && !xz;
+            if (__any_sync(kFull, add)) slot_add(add, v, rs, xs);   // rare: a real call
+            if (eq) {
+                if (rz) { const int t = rs; rs = xs; xs = t; }  // the register takes the value
+                else if (!xz) xs |= kZeroSlot;                  // the merged entry is now zero
             }
-            if (eq && !rnz) { rh = xh; rl = xl; }
-            if (eq) { xh = 0u; xl = 0u; }
             const int oc = lt ? rc : xc;
-            const unsigned oh = lt ? rh : xh, ol = lt ? rl : xl;
-            if (lt || reg) { rc = xc; rh = xh; rl = xl; }
+            const int os = lt ? rs : xs;
+            if (lt || reg) { rc = xc; rs = xs; }
             pc = proc ? oc : -1;
-            ph = oh; pl = ol;
+            ps = os;
             if (lane == 31) {
-                if (pc >= 0) { const int q = i + s - 31; c[q] = pc; v[q] = make_uint2(pl, ph); }
+                if (pc >= 0) cs[i + s - 31] = make_int2(pc, ps);
                 pc = -1;
             }
         }
-        if (i + lane < L) { c[i + lane] = rc; v[i + lane] = make_uint2(rl, rh); }
+        if (i + lane < L) cs[i + lane] = make_int2(rc, rs);
         __syncwarp();
     }
 }
 
-// The nonzeros of (c, v)[0, L) in order, written to (dc, dv) (which may be c, v
-// themselves: a write never passes the read position); returns their count. This is
-// the reference's zero bubble pass (:624-649), a stable partition of the nonzeros.
-__device__ int warp_keep_nonzeros(const int* c, const uint2* v, int L, int* dc, uint2* dv, int lane) {
+// The nonzero entries of the sorted row, in order, written to (dc, dv); returns their
+// count. This is the reference's zero bubble pass (:624-649), a stable partition.
+__device__ int warp_keep_nonzeros(const int2* cs, const double* v, int L, int* __restrict__ dc,
+                                  double* __restrict__ dv, int lane) {
     int k = 0;
     for (int base = 0; base < L; base += 32) {
         const int q = base + lane;
-        int cq = 0; uint2 vq = make_uint2(0u, 0u);
-        if (q < L) { cq = c[q]; vq = v[q]; }
-        const bool keep = q < L && nonzero_halves(vq.y, vq.x);
+        int2 e = make_int2(0, kZeroSlot);
+        if (q < L) e = cs[q];
+        double val = 0.0;
+        if (e.y >= 0) val = v[e.y];
+        const bool keep = e.y >= 0 && ((__double_as_longlong(val) << 1) != 0);
         const unsigned m = __ballot_sync(kFull, keep);
-        __syncwarp();
-        if (keep) { const int d = k + __popc(m & ((1u << lane) - 1u)); dc[d] = cq; dv[d] = vq; }
+        if (keep) { const int d = k + __popc(m & ((1u << lane) - 1u)); dc[d] = e.x; dv[d] = val; }
         k += __popc(m);
-        __syncwarp();
     }
     return k;
 }
 
-// One warp per row: sort and merge (in shared memory when the row fits), keep the
-// nonzeros at the row's start; cnt[r] = their count. Values are handled as bit patterns.
+// One warp per row: the row's entries get slots (zero values flagged), are sorted and
+// merged (the (column, slot) stream in shared memory when the row fits, else in the global
+// scratch `cs`; the values stay in V, where only merges of two nonzeros and the final pass
+// touch them), and the nonzeros are written to (Co, Vo) from the row's start; cnt[r] =
+// their count.
 __global__ void __launch_bounds__(kWarpBlock)
-compress_rows_kernel(int rows, const int* __restrict__ A, int* C, double* Vd, int* __restrict__ cnt) {
-    __shared__ int sc[kWarpsPerBlock][kRowCap];
-    __shared__ uint2 sv[kWarpsPerBlock][kRowCap];
-    uint2* V = reinterpret_cast<uint2*>(Vd);
+compress_rows_kernel(int rows, const int* __restrict__ A, const int* __restrict__ C, double* V, int2* cs,
+                     int* __restrict__ Co, double* __restrict__ Vo, int* __restrict__ cnt) {
+    __shared__ int2 scs[kWarpsPerBlock][kRowCap];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int r = blockIdx.x * kWarpsPerBlock + w;
     if (r >= rows) return;
     const int lo = A[r], L = A[r + 1] - lo;
-    int k;
-    if (L <= kRowCap) {
-        for (int q = lane; q < L; q += 32) { sc[w][q] = C[lo + q]; sv[w][q] = V[lo + q]; }
-        __syncwarp();
-        warp_exchange_sort(sc[w], sv[w], L, lane);
-        k = warp_keep_nonzeros(sc[w], sv[w], L, C + lo, V + lo, lane);
-    } else {
-        warp_exchange_sort(C + lo, V + lo, L, lane);
-        k = warp_keep_nonzeros(C + lo, V + lo, L, C + lo, V + lo, lane);
+    int2* rcs = L <= kRowCap ? scs[w] : cs + lo;
+    double* rv = V + lo;
+    for (int q = lane; q < L; q += 32) {
+        const int zero = ((__double_as_longlong(rv[q]) << 1) == 0) ? kZeroSlot : 0;
+        rcs[q] = make_int2(C[lo + q], q | zero);
     }
+    __syncwarp();
+    warp_exchange_sort(rcs, rv, L, lane);
+    const int k = warp_keep_nonzeros(rcs, rv, L, Co + lo, Vo + lo, lane);
     if (lane == 0) cnt[r] = k;
 }
 
@@ -474,12 +471,18 @@ bool csr_ok(int rows, int cols, const int* A, const int* C) {
 // Compress the rows laid out at (dA, dC, dV), compact them into (oA, oC, oV) on the device.
 int compress_and_compact(DevArena& m, cudaStream_t s, int rows, int* dA, int* dC, double* dV, int*& oA, int*& oC,
                          double*& oV, int& nnz_out) {
-    int *cnt = nullptr, *off = nullptr, *scr = nullptr;
+    int *cnt = nullptr, *off = nullptr, *scr = nullptr, *Co = nullptr, total = 0;
+    int2* cs = nullptr;
+    double* Vo = nullptr;
+    FEEC_TRY(cudaMemcpyAsync(&total, dA + rows, sizeof(int), cudaMemcpyDeviceToHost, s));
+    FEEC_TRY(cudaStreamSynchronize(s));
     FEEC_TRY(m.alloc(cnt, (size_t)rows + 1)); FEEC_TRY(m.alloc(off, (size_t)rows + 1));
     FEEC_TRY(m.alloc(scr, scan_scratch_ints(rows + 1)));
+    FEEC_TRY(m.alloc(cs, (size_t)std::max(total, 1))); FEEC_TRY(m.alloc(Co, (size_t)std::max(total, 1)));
+    FEEC_TRY(m.alloc(Vo, (size_t)std::max(total, 1)));
     FEEC_TRY(cudaMemsetAsync(cnt + rows, 0, sizeof(int), s));
     note_launch();
-    compress_rows_kernel<<<warp_grid(rows), kWarpBlock, 0, s>>>(rows, dA, dC, dV, cnt);
+    compress_rows_kernel<<<warp_grid(rows), kWarpBlock, 0, s>>>(rows, dA, dC, dV, cs, Co, Vo, cnt);
     FEEC_TRY(cudaGetLastError());
     FEEC_TRY(launch_exclusive_scan(rows + 1, cnt, off, scr, s));
     FEEC_TRY(cudaMemcpyAsync(&nnz_out, off + rows, sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -488,7 +491,7 @@ int compress_and_compact(DevArena& m, cudaStream_t s, int rows, int* dA, int* dC
     FEEC_TRY(m.alloc(oV, (size_t)std::max(nnz_out, 1)));
     if (rows == 0) FEEC_TRY(cudaMemsetAsync(oA, 0, sizeof(int), s));
     note_launch();
-    compact_rows_kernel<<<warp_grid(rows), kWarpBlock, 0, s>>>(rows, dA, cnt, off, dC, dV, oC, oV, oA);
+    compact_rows_kernel<<<warp_grid(rows), kWarpBlock, 0, s>>>(rows, dA, cnt, off, Co, Vo, oC, oV, oA);
     FEEC_TRY(cudaGetLastError());
     return FEEC_OK;
 }
