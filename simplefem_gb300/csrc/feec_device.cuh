@@ -70,21 +70,27 @@ __device__ __forceinline__ bool wait_counter(DeviceStatus* st, unsigned long lon
     return true;
 }
 
+// Arrival at a grid barrier: a release reduction (no return value to wait for) that
+// publishes every write the block made before it (the preceding __syncthreads orders the
+// other threads' writes before this thread's release).
+__device__ __forceinline__ void arrive_release(unsigned long long* p) {
+    asm volatile("red.release.gpu.global.add.u64 [%0], 1;" ::"l"(p) : "memory");
+}
+
 // Grid-wide barrier for a cooperatively launched grid. `epoch` is the number of
-// barriers this block has passed (identical in every block). Returns false if
-// the wait gave up (time or poll limit) or another block gave up; the caller
-// must then leave the kernel without touching shared state again.
+// barriers this block has passed (identical in every block). Arrival is a release
+// reduction and the wait an acquire load (wait_counter), so no separate fences are
+// needed; the __syncthreads on either side carry the ordering to the block's other
+// threads. Returns false if the wait gave up (time or poll limit) or another block gave
+// up; the caller must then leave the kernel without touching shared state again.
 __device__ __forceinline__ bool grid_barrier(DeviceStatus* st, unsigned long long& epoch, int site) {
     __shared__ int s_ok;
     __syncthreads();
     if (threadIdx.x == 0) {
         epoch += 1;
         const unsigned long long target = epoch * (unsigned long long)(gridDim.x * gridDim.y);
-        __threadfence();
-        atomicAdd(&st->barrier, 1ull);
-        const int ok = wait_counter(st, target, site, kWaitNanos) ? 1 : 0;
-        __threadfence();
-        s_ok = ok;
+        arrive_release(&st->barrier);
+        s_ok = wait_counter(st, target, site, kWaitNanos) ? 1 : 0;
     }
     __syncthreads();
     return s_ok != 0;
