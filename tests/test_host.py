@@ -147,3 +147,50 @@ def test_uniform_vector_reproducible(built):
     a = workloads.uniform_vector(7, 1000)
     b = workloads.uniform_vector(7, 1000)
     assert np.array_equal(a, b) and a.min() >= -1.0 and a.max() < 1.0 and abs(a.mean()) < 0.1
+
+
+def test_algebra_and_solver_entry_points_check_arguments_on_the_host(built):
+    """The CSR algebra, the COO product, CR/MINRES/Chebyshev and the Hodge solvers refuse
+    invalid arguments on the host, before any device work (FEEC_BADARG without a GPU)."""
+    from simplefem_gb300 import _native
+    L = _native.gpu()
+    BAD = _native.FEEC_BADARG
+    A = np.array([0, 2, 3], np.int32); C = np.array([0, 1, 1], np.int32); V = np.ones(3)
+    Cbad = np.array([0, 5, 1], np.int32); Abad = np.array([0, 3, 2], np.int32)
+    oA = np.empty(8, np.int32); oC = np.empty(16, np.int32); oV = np.empty(16)
+    nnz = ctypes.c_int(0); cnt = ctypes.c_longlong(0)
+    assert L.feec_csr_add(2, 2, A, Cbad, V, A, C, V, 1.0, 1.0, oA, oC, oV, ctypes.byref(nnz)) == BAD
+    assert L.feec_csr_add(2, 2, Abad, C, V, A, C, V, 1.0, 1.0, oA, oC, oV, ctypes.byref(nnz)) == BAD
+    assert L.feec_csr_multiply(2, 2, 2, A, Cbad, V, A, C, V, oA, oC, oV, ctypes.byref(nnz)) == BAD
+    assert L.feec_csr_transpose(2, 2, A, Cbad, V, oA, oC, oV, ctypes.byref(nnz)) == BAD
+    r = np.array([0, 3], np.int32); c = np.array([0, 1], np.int32)
+    assert L.feec_coo_to_csr(2, 2, 2, r, c, np.ones(2), oA, oC, oV, ctypes.byref(nnz)) == BAD
+    assert L.feec_coo_multiply(2, 2, 2, 2, r, c, np.ones(2), 2, c, c, np.ones(2), oC, oC.copy(), oV,
+                               ctypes.byref(cnt)) == BAD
+    size = ctypes.c_longlong(0)
+    assert L.feec_coo_multiply_size(2, 2, np.array([0, 1], np.int32), 2, np.array([0, 1], np.int32),
+                                    ctypes.byref(size)) == _native.FEEC_OK and size.value == 2
+    info = _native.FeecSolveInfo()
+    x = np.zeros(2); res = np.zeros(2); b = np.ones(2)
+    for fn in (L.feec_cr_csr, L.feec_cr_csr_textbook, L.feec_minres_csr):
+        assert fn(0, x, b, A, C, V, res, 1e-10, -3, ctypes.byref(info)) == BAD          # N > 0 (:1699)
+        assert fn(2, x, b, A, C, V, res, 0.0, -3, ctypes.byref(info)) == BAD            # precision > 0
+    assert L.feec_chebyshev_diag(2, x, b, A, C, V, res, 0.0, -3, np.ones(2), 0.5, 2.0, ctypes.byref(info)) == BAD
+    args = [2, 0, x, b] + [A, C, V] * 4 + [res, 1e-10, -3, 1e-12, -3, ctypes.byref(info)]
+    for name in ("feec_hodge_cr_csr", "feec_hodge_cr_csr_diagonal", "feec_hodge_cr_csr_ssor",
+                 "feec_hodge_cr_csr_textbook"):
+        assert getattr(L, name)(*args) == BAD                                          # L > 0 (:76-77)
+    assert L.feec_hodge_herzog_soodhalter(0, 2, x, x.copy(), b, b, *([A, C, V] * 4), 1e-10, -3,
+                                          None, None, None, None, None, None, 1e-12, -3, ctypes.byref(info)) == BAD
+
+
+def test_python_surface_checks_shapes(built):
+    from simplefem_gb300 import MatrixCSR, MatrixCSRAddition, MatrixCSRMultiplication, SparseMatrix
+    with pytest.raises(ValueError):
+        SparseMatrix(2, 2, [0, 1], [0], [1.0])
+    X = MatrixCSR(2, 3, [0, 1, 2], [0, 2], [1.0, 2.0])
+    Y = MatrixCSR(2, 2, [0, 1, 2], [0, 1], [1.0, 2.0])
+    with pytest.raises(ValueError):
+        MatrixCSRAddition(X, Y)
+    with pytest.raises(ValueError):
+        MatrixCSRMultiplication(X, Y)
