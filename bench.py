@@ -36,7 +36,7 @@ WORKLOAD_NAME = "3D P2 Lagrange stiffness+mass, unit cube (6 tets) refined 5x: N
                 "Rainbow SSOR-PCG omega=1.0, x0=0, b~U[-1,1] seeded, 1e-10 true relative residual"
 METRIC = "solves/s at 1e-10 rel. residual (3D P2 L5, Rainbow SSOR-PCG), mixed FP32/FP64"
 PRECISION = 1e-10
-DRAM_OVER_ALGORITHMIC_K4_T512 = 0.919
+DRAM_OVER_ALGORITHMIC_K4_T512 = 0.901
 
 
 def max_over_ranks(x, device=None):
@@ -685,14 +685,14 @@ def run_ours(args):
         kernel_name = f"batched_solve_kernel<float,{K_TEAM},true,{tuned['team_threads']}>"
     # DRAM traffic of this kernel configuration from one ncu capture (dram__bytes_read.sum +
     # dram__bytes_write.sum) on the operator refined 4x (profiles/batched_solve_3d_p2_l4.md):
-    # 0.919 x its algorithmic bytes; a full-size launch (about 2.6 s) is not captured, so the
+    # 0.901 x its algorithmic bytes; a full-size launch (about 2.6 s) is not captured, so the
     # traffic of this launch is that ratio times its algorithmic bytes
     traffic = None
     if (K_TEAM, tuned["team_threads"], tuned["team_blocks"]) == (4, 512, 1) and DRAM_OVER_ALGORITHMIC_K4_T512:
         traffic = DRAM_OVER_ALGORITHMIC_K4_T512 * per_step_bytes
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": traffic, "kernel": kernel_name, "launches_per_step": 1,
-                "traffic_source": "ncu DRAM bytes / algorithmic bytes = 0.919 measured on the 4x-refined operator "
+                "traffic_source": "ncu DRAM bytes / algorithmic bytes = 0.901 measured on the 4x-refined operator "
                                   "(profiles/batched_solve_3d_p2_l4.md), applied to this launch" if traffic else None,
                 "bytes_per_launch": per_step_bytes, "ms_per_launch": total_ms / args.steps,
                 "peak_kind": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)"}
