@@ -2,8 +2,9 @@
  * ORACLE — test infrastructure, not product code.
  *
  * A plain-C restatement of the FEEC++ reference algorithms on the sparse CSR
- * Krylov path, used only as the checker by tests/, __graft_entry__.smoke() and
- * bench.py's CPU-baseline / reference legs. Nothing in the product library
+ * Krylov path and the CSR algebra and block solvers around it, used only to compare
+ * results against by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline /
+ * reference legs. Nothing in the product library
  * links, loads or calls this file.
  *
  * Every function follows the cited reference lines statement by statement,

@@ -3,7 +3,7 @@
 ctypes binding of ``oracle/_build/libfeec_oracle.so`` (the plain-C restatement of the
 reference's CSR Krylov path, ``oracle/feec_oracle.c``). Only ``tests/``,
 ``__graft_entry__.smoke()`` and ``bench.py`` (CPU-baseline and reference legs) import
-this module, and only as the checker or the timed CPU baseline.
+this module, and only to compare results against or as the timed CPU baseline.
 """
 from __future__ import annotations
 
