@@ -508,6 +508,52 @@ def run_krylov_more(with_cpu, hodge=True):
     return out
 
 
+def run_small(with_cpu):
+    """The drop-ins on the reference's own CPU-sized case, 2D P1 refined 6x (N = 4,225):
+    host arrays in and out, median of 5 calls, beside the oracle at one thread (the
+    reference's plain CG is only correct at one thread, its SSOR sweeps are serial)."""
+    import simplefem_gb300 as S
+    from simplefem_gb300 import workloads
+    oracle = None
+    if with_cpu:
+        from oracle import oracle
+        oracle.set_threads(1)
+    A, C, V = workloads.lattice_matrix(2, 1, 6, 0)
+    n = len(A) - 1
+    b = workloads.uniform_vector(2024, n)
+    mat = S.MatrixCSR(n, n, A, C, V)
+    diag = mat.getDiagonal().raw()
+    rb = S.Rainbow(mat)
+    rbo = (rb.num_colors, rb.F, rb.B, rb.R)
+    calls = {
+        "cg": (lambda x, r: S.ConjugateGradientSolverCSR(n, x, b, A, C, V, r, 1e-10, -3),
+               None if oracle is None else (lambda: oracle.cg(A, C, V, b, precision=1e-10))),
+        "ssor": (lambda x, r: S.ConjugateGradientSolverCSR_SSOR(n, x, b, A, C, V, r, 1e-10, -3, diag, 1.0),
+                 None if oracle is None else (lambda: oracle.cg_ssor(A, C, V, b, diag, 1.0, precision=1e-10))),
+        "rainbow": (lambda x, r: S.ConjugateGradientSolverCSR_Rainbow(n, x, b, A, C, V, r, 1e-10, -3, diag, 1.0,
+                                                                      *rbo),
+                    None if oracle is None else (lambda: oracle.cg_rainbow(A, C, V, b, diag, rbo, 1.0,
+                                                                           precision=1e-10))),
+    }
+    out = {"workload": f"2D P1 refined 6x, N={n}, nnz={len(C)}, {rb.num_colors} colors, precision 1e-10"}
+    for name, (gpu, cpu) in calls.items():
+        wall, dev_ms, K = [], [], 0
+        for _ in range(6):
+            x = np.zeros(n); r = np.zeros(n)
+            t0 = time.perf_counter()
+            K = gpu(x, r)
+            wall.append(1000.0 * (time.perf_counter() - t0))
+            dev_ms.append(S.last_info()["device_ms"])
+        leg = {"iterations": K, "call_ms": float(np.median(wall[1:])), "device_ms": float(np.median(dev_ms[1:]))}
+        if cpu is not None:
+            ts = []
+            for _ in range(5):
+                t0 = time.perf_counter(); K_o, _, _ = cpu(); ts.append(1000.0 * (time.perf_counter() - t0))
+            leg.update({"cpu_ms": float(np.median(ts)), "cpu_iterations": K_o, "cpu_cores": 1})
+        out[name] = leg
+    return out
+
+
 def run_serving(mode, method, count=200, rate=200.0, slots=24, budget=120 * 10**9):
     """Poisson-arrival request stream through the continuous-batching server."""
     from simplefem_gb300 import workloads
@@ -572,6 +618,10 @@ def run_ours(args):
     if args.only_mixed_large:
         if rank == 0:
             print(json.dumps({"mixed_large": run_mixed_large(dev)}), flush=True)
+        return
+    if args.only_small:
+        if rank == 0:
+            print(json.dumps({"small": run_small(not args.no_cpu)}), flush=True)
         return
     if args.only_krylov_more:
         if rank == 0:
@@ -803,6 +853,7 @@ def run_ours(args):
     mixed_large = run_mixed_large(dev) if not args.skip_extras else None
     csr_algebra = run_csr_algebra(rank == 0 and not args.no_cpu) if not args.skip_extras else None
     krylov_more = run_krylov_more(rank == 0 and not args.no_cpu) if not args.skip_extras else None
+    small = run_small(rank == 0 and not args.no_cpu) if not args.skip_extras else None
     serving = None
     if not args.skip_extras:
         serving = {"mixed_rainbow": run_serving("mixed", "rainbow", args.requests),
@@ -875,6 +926,7 @@ def run_ours(args):
             "mixed_large": mixed_large,
             "csr_algebra": csr_algebra,
             "krylov_more": krylov_more,
+            "small_dropins": small,
             "serving": serving,
             "roofline": roofline,
             "cpu_baseline": cpu,
@@ -905,6 +957,7 @@ def main():
     ap.add_argument("--only-mixed-large", action="store_true", help="only the 3D P1 L7 mixed-precision solves")
     ap.add_argument("--only-csr-algebra", action="store_true", help="only the CSR algebra leg (product, transpose, sum)")
     ap.add_argument("--only-krylov-more", action="store_true", help="only the CR / MINRES / Hodge leg")
+    ap.add_argument("--only-small", action="store_true", help="only the drop-ins on 2D P1 L6 (N = 4,225)")
     ap.add_argument("--only-batched", action="store_true",
                     help="only the batched headline step (no single-solve, SpMV, CPU or extra legs)")
     ap.add_argument("--rhs-per-team", type=int, default=0,

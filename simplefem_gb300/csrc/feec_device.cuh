@@ -84,6 +84,10 @@ __device__ __forceinline__ void arrive_release(unsigned long long* p) {
 // threads. Returns false if the wait gave up (time or poll limit) or another block gave
 // up; the caller must then leave the kernel without touching shared state again.
 __device__ __forceinline__ bool grid_barrier(DeviceStatus* st, unsigned long long& epoch, int site) {
+    if (gridDim.x * gridDim.y == 1) {   // a one-block grid (small systems): the block barrier suffices
+        __syncthreads();
+        return true;
+    }
     __shared__ int s_ok;
     __syncthreads();
     if (threadIdx.x == 0) {
