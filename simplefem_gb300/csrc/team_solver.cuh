@@ -75,7 +75,7 @@ __device__ __forceinline__ void load_k(const T* p, T (&v)[K]) {
 // first (all independent, coalesced across the warp), then the CH gathers are
 // issued together, then the FMAs run; padded slots are predicated off.
 template <typename T, int K>
-struct Chunk { static constexpr int value = sizeof(T) == 8 ? ((K >= 2) ? 1 : 4) : (K >= 8 ? 2 : ((K >= 4) ? 2 : 4)); };
+struct Chunk { static constexpr int value = sizeof(T) == 8 ? ((K >= 2) ? 2 : 4) : (K >= 8 ? 2 : ((K >= 4) ? 2 : 4)); };
 
 template <typename T, typename TV, int CH>
 __device__ __forceinline__ void load_entries(const int* __restrict__ sci, const TV* __restrict__ sval, long long off,
