@@ -194,3 +194,14 @@ def test_python_surface_checks_shapes(built):
         MatrixCSRAddition(X, Y)
     with pytest.raises(ValueError):
         MatrixCSRMultiplication(X, Y)
+
+
+def test_public_header_compiles_as_c_and_cpp():
+    """include/feec_gpu.h is plain C (the boundary a cgo / FFI / C caller includes)."""
+    import shutil
+    header = os.path.join(ROOT, "include", "feec_gpu.h")
+    if shutil.which("gcc"):
+        subprocess.run(["gcc", "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror", "-fsyntax-only", "-x", "c",
+                        header], check=True)
+    if shutil.which("g++"):
+        subprocess.run(["g++", "-std=c++14", "-Wall", "-Werror", "-fsyntax-only", "-x", "c++", header], check=True)

@@ -140,3 +140,49 @@ def test_oracle_hodge_herzog_soodhalter_bitexact(O):
                                float(g["precision"]), float(g["inner_precision"]))
         assert K == int(g[case + "_K"]), case
         assert np.array_equal(xA, g[case + "_xA"]) and np.array_equal(xC, g[case + "_xC"]), case
+
+
+def test_oracle_algebra_and_solvers_agree_with_independent_references(O):
+    """Beyond the pins: the oracle's CSR algebra against scipy.sparse, and its further
+    drivers and block solvers against dense solves (independent arithmetic)."""
+    sp = pytest.importorskip("scipy.sparse")
+    g = load_golden("fem2d_p2_l4_coef")
+    A, C, V = g["A"], g["C"], g["V"]
+    n = len(A) - 1
+    M = sp.csr_matrix((V, C, A), shape=(n, n))
+    rng = np.random.default_rng(7)
+    V2 = V * rng.uniform(0.5, 1.5, len(V))
+    M2 = sp.csr_matrix((V2, C, A), shape=(n, n))
+    for (Ao, Co, Vo), ref in ((O.csr_add(A, C, V, A, C, V2, 0.3, -1.7), 0.3 * M - 1.7 * M2),
+                              (O.csr_multiply(A, C, V, A, C, V2), M @ M2),
+                              (O.csr_transpose(A, C, V2, n), M2.T.tocsr())):
+        got = sp.csr_matrix((Vo, Co, Ao), shape=ref.shape)
+        assert abs(got - ref).max() <= 1e-12 * abs(ref).max()
+    r, c, v = sp.find(M)
+    rr, cc, vv = O.coo_multiply(n, (r.astype(np.int32), c.astype(np.int32), v),
+                                (r.astype(np.int32), c.astype(np.int32), v))
+    P = sp.csr_matrix((vv, (rr, cc)), shape=(n, n))
+    assert abs(P - M @ M).max() <= 1e-12 * abs(M @ M).max()
+    # further drivers against a dense solve (the operator is SPD)
+    b = g["b"]
+    xs = np.linalg.solve(M.toarray(), b)
+    d = M.diagonal()
+    ev = np.linalg.eigvalsh((M.multiply(1.0 / np.sqrt(np.outer(d, d)))).toarray())
+    for K, x, _ in (O.cr(A, C, V, b, precision=1e-12), O.minres(A, C, V, b, precision=1e-12),
+                    O.chebyshev(A, C, V, b, 1.0 / d, 0.99 * ev[0], 1.01 * ev[-1], precision=1e-12)):
+        assert 0 < K < n and np.linalg.norm(x - xs) <= 1e-6 * np.linalg.norm(xs)
+    # Hodge: conjugate residuals on B A^-1 Bt + C, and the block MINRES on [[-A, Bt], [B, C]]
+    h = load_golden("hodge")
+    Mh = lambda k: (h[k + "_A"], h[k + "_C"], h[k + "_V"])  # noqa: E731
+    L, N = len(h["A_A"]) - 1, len(h["C_A"]) - 1
+    Ad = sp.csr_matrix((h["A_V"], h["A_C"], h["A_A"]), shape=(L, L)).toarray()
+    Bd = sp.csr_matrix((h["B_V"], h["B_C"], h["B_A"]), shape=(N, L)).toarray()
+    Cd = sp.csr_matrix((h["C_V"], h["C_C"], h["C_A"]), shape=(N, N)).toarray()
+    xs = np.linalg.solve(Bd @ np.linalg.solve(Ad, Bd.T) + Cd, h["b"])
+    K, x, _ = O.hodge_cr(2, Mh("A"), Mh("B"), Mh("Bt"), Mh("C"), h["b"], precision=1e-12, inner_precision=1e-14)
+    assert np.linalg.norm(x - xs) <= 1e-6 * np.linalg.norm(xs)
+    Kb = np.block([[-Ad, Bd.T], [Bd, Cd]])
+    zs = np.linalg.solve(Kb, np.concatenate([h["hhs_bA"], h["hhs_bC"]]))
+    K, xA, xC = O.hodge_hs(Mh("A"), Mh("B"), Mh("Bt"), Mh("C"), h["hhs_bA"], h["hhs_bC"], Mh("A"), Mh("C"),
+                           1e-12, 1e-14)
+    assert np.linalg.norm(np.concatenate([xA, xC]) - zs) <= 1e-6 * np.linalg.norm(zs)
