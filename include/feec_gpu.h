@@ -357,6 +357,15 @@ int feec_batch_create(feec_batch** batch, int nsys, feec_system* const* systems,
                       double* const* x, const double* const* b, double precision, int max_iter,
                       int team_threads, void* stream);
 int feec_batch_run(feec_batch* batch, feec_solve_info* infos, double* device_ms);
+/* feec_batch_run in two halves, so that one host thread can overlap other work (the
+ * next batch's uploads, the last batch's downloads on its own streams) with a replay:
+ * feec_batch_launch enqueues the replay after the work already on the caller's stream
+ * and returns at once; feec_batch_finish waits for it and fills infos and *device_ms
+ * as feec_batch_run does. x and b of the batch must not be touched in between. A
+ * second launch before the finish, or a finish without a launch, is FEEC_BADARG.
+ * Several batches (over separate x, b) may be in flight at the same time. */
+int feec_batch_launch(feec_batch* batch);
+int feec_batch_finish(feec_batch* batch, feec_solve_info* infos, double* device_ms);
 int feec_batch_destroy(feec_batch* batch);
 
 /* y = scaling * A * x with device pointers (MatrixCSR::apply on a resident matrix),

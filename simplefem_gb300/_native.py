@@ -120,6 +120,8 @@ def gpu():
         L.feec_batch_create.argtypes = [ctypes.POINTER(_vp), _ip, ctypes.POINTER(_vp), _ip, _ip, ctypes.POINTER(_vp),
                                          ctypes.POINTER(_vp), _dp, _ip, _ip, _vp]
         L.feec_batch_run.argtypes = [_vp, _infop, ctypes.POINTER(ctypes.c_double)]
+        L.feec_batch_launch.argtypes = [_vp]
+        L.feec_batch_finish.argtypes = [_vp, _infop, ctypes.POINTER(ctypes.c_double)]
         L.feec_batch_destroy.argtypes = [_vp]
         L.feec_system_set_launch.argtypes = [_vp, _ip, _ip]
         L.feec_system_memory.argtypes = [_vp, ctypes.POINTER(ctypes.c_size_t)]

@@ -519,6 +519,8 @@ struct feec_batch {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     BatchResult* dres = nullptr;
+    BatchResult* hres = nullptr;          // pinned: the result copy of a launch is asynchronous
+    bool pending = false;                 // launched and not yet finished
     int nresults = 0;
     double precision = 0.0;
     int teams = 0;
@@ -546,6 +548,7 @@ int feec_batch_create(feec_batch** out, int nsys, feec_system* const* systems, i
                 cudaStreamSynchronize(p->stream);
                 if (p->own_stream) cudaStreamDestroy(p->stream);
                 if (p->ev_in) cudaEventDestroy(p->ev_in);
+                if (p->hres) cudaFreeHost(p->hres);
                 delete p;
                 p = nullptr;
             }
@@ -633,23 +636,37 @@ int feec_batch_create(feec_batch** out, int nsys, feec_system* const* systems, i
     FEEC_TRY(cudaGraphInstantiate(&bt->exec, bt->graph, 0));
     FEEC_TRY(cudaEventCreate(&bt->e0));
     FEEC_TRY(cudaEventCreate(&bt->e1));
+    FEEC_TRY(cudaMallocHost(&bt->hres, sizeof(BatchResult) * (size_t)nsys));
     bt->nresults = nsys;
     cleanup.keep = true;
     *out = bt;
     return FEEC_OK;
 }
 
-int feec_batch_run(feec_batch* bt, feec_solve_info* infos, double* device_ms) {
-    if (!bt) return FEEC_BADARG;
+int feec_batch_launch(feec_batch* bt) {
+    if (!bt || bt->pending) return FEEC_BADARG;
     FEEC_TRY(cudaEventRecord(bt->ev_in, bt->user_stream));     // inputs written on the caller's stream
     FEEC_TRY(cudaStreamWaitEvent(bt->stream, bt->ev_in, 0));
     FEEC_TRY(cudaEventRecord(bt->e0, bt->stream));
     FEEC_TRY(cudaGraphLaunch(bt->exec, bt->stream));
     note_launch();
-    FEEC_TRY(cudaEventRecord(bt->e1, bt->stream));
-    std::vector<BatchResult> res((size_t)bt->nresults);
-    FEEC_TRY(cudaMemcpyAsync(res.data(), bt->dres, sizeof(BatchResult) * bt->nresults, cudaMemcpyDeviceToHost, bt->stream));
+    cudaError_t e = cudaEventRecord(bt->e1, bt->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(bt->hres, bt->dres, sizeof(BatchResult) * bt->nresults, cudaMemcpyDeviceToHost,
+                            bt->stream);
+    if (e != cudaSuccess) {                                      // the replay is in flight: let it end
+        cudaStreamSynchronize(bt->stream);
+        return cuda_status(e);
+    }
+    bt->pending = true;
+    return FEEC_OK;
+}
+
+int feec_batch_finish(feec_batch* bt, feec_solve_info* infos, double* device_ms) {
+    if (!bt || !bt->pending) return FEEC_BADARG;
+    bt->pending = false;
     FEEC_TRY(cudaStreamSynchronize(bt->stream));
+    std::vector<BatchResult> res(bt->hres, bt->hres + bt->nresults);
     float ms = 0.0f;
     cudaEventElapsedTime(&ms, bt->e0, bt->e1);
     if (bt->mode == FEEC_MODE_MIXED) {
@@ -663,6 +680,12 @@ int feec_batch_run(feec_batch* bt, feec_solve_info* infos, double* device_ms) {
     return worst;
 }
 
+int feec_batch_run(feec_batch* bt, feec_solve_info* infos, double* device_ms) {
+    const int st = feec_batch_launch(bt);
+    if (st != FEEC_OK) return st;
+    return feec_batch_finish(bt, infos, device_ms);
+}
+
 int feec_batch_destroy(feec_batch* bt) {
     if (!bt) return FEEC_OK;
     cudaStreamSynchronize(bt->stream);
@@ -674,6 +697,7 @@ int feec_batch_destroy(feec_batch* bt) {
     cudaStreamSynchronize(bt->stream);
     if (bt->ev_in) cudaEventDestroy(bt->ev_in);
     if (bt->own_stream) cudaStreamDestroy(bt->stream);
+    if (bt->hres) cudaFreeHost(bt->hres);
     delete bt;
     return FEEC_OK;
 }

@@ -188,6 +188,21 @@ class Batch:
             raise _native.FeecError(st, "feec_batch_run")
         return [i.as_dict() for i in infos], ms.value
 
+    def launch(self):
+        """Enqueue a replay after the work on the current stream and return at once
+        (the first half of ``run``); ``finish`` waits for it. ``bs`` and ``xs`` must not
+        be touched in between."""
+        _native.check(self._lib.feec_batch_launch(self._h), "feec_batch_launch")
+
+    def finish(self, raise_on_error=True) -> tuple:
+        """Wait for the replay ``launch`` enqueued; returns what ``run`` returns."""
+        infos = (_native.FeecSolveInfo * self.n)()
+        ms = ctypes.c_double(0.0)
+        st = self._lib.feec_batch_finish(self._h, infos, ctypes.byref(ms))
+        if raise_on_error and st not in (_native.FEEC_OK, _native.FEEC_MAXITER, _native.FEEC_BREAKDOWN):
+            raise _native.FeecError(st, "feec_batch_finish")
+        return [i.as_dict() for i in infos], ms.value
+
     def close(self):
         if getattr(self, "_h", None):
             self._lib.feec_batch_destroy(self._h)

@@ -150,6 +150,55 @@ def test_graph_captured_batch_replays(cuda):
         s.close()
 
 
+@pytest.mark.parametrize("mode", ["fp64", "mixed"])
+def test_graph_batch_launch_finish_double_buffered(cuda, mode):
+    """The two halves of a replay (feec_batch_launch / feec_batch_finish): two batches over
+    separate right-hand sides of the same systems are in flight at once from one host
+    thread, each reaches 1e-10 with the solution and iteration count of a synchronous
+    replay of the same inputs, and a second launch before the finish or a finish without
+    a launch is refused."""
+    torch = cuda
+    from simplefem_gb300 import _native, workloads
+    from simplefem_gb300.system import Batch
+    specs = [(2, 1, 4, 31), (2, 2, 3, 32), (2, 1, 5, 33), (2, 2, 4, 34)]
+    systems, mats = [], []
+    for (d, r, L, seed) in specs:
+        s, M = _prepared(d, r, L, seed)
+        systems.append(s); mats.append(M)
+
+    def buffers(seed):
+        bs = [torch.from_numpy(workloads.uniform_vector(seed + i, s.n)).cuda() for i, s in enumerate(systems)]
+        return bs, [torch.zeros(s.n, dtype=torch.float64, device="cuda") for s in systems]
+
+    (bs0, xs0), (bs1, xs1) = buffers(700), buffers(800)
+    b0 = Batch(systems, bs0, xs0, method="rainbow", mode=mode, precision=1e-10)
+    b1 = Batch(systems, bs1, xs1, method="rainbow", mode=mode, precision=1e-10)
+    with pytest.raises(_native.FeecError):
+        b0.finish()                                   # nothing launched yet
+    b0.launch()
+    with pytest.raises(_native.FeecError):
+        b0.launch()                                   # the first replay is still pending
+    b1.launch()
+    infos0, ms0 = b0.finish()
+    infos1, ms1 = b1.finish()
+    assert ms0 > 0 and ms1 > 0
+    got = [[x.cpu().numpy() for x in xs0], [x.cpu().numpy() for x in xs1]]
+    # the same inputs through synchronous replays, one batch at a time
+    for (bt, bs, xs, infos, x_async) in ((b0, bs0, xs0, infos0, got[0]), (b1, bs1, xs1, infos1, got[1])):
+        for x in xs:
+            x.zero_()
+        infos_sync, _ = bt.run()
+        for i, M in enumerate(mats):
+            b = bs[i].cpu().numpy(); x_sync = xs[i].cpu().numpy()
+            assert infos[i]["status"] == 0
+            assert np.linalg.norm(b - M @ x_async[i]) / np.linalg.norm(b) <= 1e-10
+            assert abs(infos[i]["iterations"] - infos_sync[i]["iterations"]) <= max(1, 0.02 * infos_sync[i]["iterations"])
+            assert np.linalg.norm(x_async[i] - x_sync) <= 1e-9 * np.linalg.norm(x_sync)
+    b0.close(); b1.close()
+    for s in systems:
+        s.close()
+
+
 @pytest.mark.parametrize("mode,k,blocks", [("mixed", 4, 4), ("mixed", 2, 8), ("mixed", 1, 2), ("fp64", 2, 4),
                                            ("fp64", 1, 16), ("mixed", 8, 4)])
 def test_cluster_teams_reach_tolerance(cuda, mode, k, blocks):
