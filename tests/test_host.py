@@ -182,6 +182,11 @@ def test_algebra_and_solver_entry_points_check_arguments_on_the_host(built):
         assert getattr(L, name)(*args) == BAD                                          # L > 0 (:76-77)
     assert L.feec_hodge_herzog_soodhalter(0, 2, x, x.copy(), b, b, *([A, C, V] * 4), 1e-10, -3,
                                           None, None, None, None, None, None, 1e-12, -3, ctypes.byref(info)) == BAD
+    # the batch replay halves refuse a missing batch before touching the device
+    ms = ctypes.c_double(0.0)
+    assert L.feec_batch_launch(None) == BAD
+    assert L.feec_batch_finish(None, ctypes.byref(info), ctypes.byref(ms)) == BAD
+    assert L.feec_batch_run(None, ctypes.byref(info), ctypes.byref(ms)) == BAD
 
 
 def test_python_surface_checks_shapes(built):
