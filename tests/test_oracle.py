@@ -186,3 +186,50 @@ def test_oracle_algebra_and_solvers_agree_with_independent_references(O):
     K, xA, xC = O.hodge_hs(Mh("A"), Mh("B"), Mh("Bt"), Mh("C"), h["hhs_bA"], h["hhs_bC"], Mh("A"), Mh("C"),
                            1e-12, 1e-14)
     assert np.linalg.norm(np.concatenate([xA, xC]) - zs) <= 1e-6 * np.linalg.norm(zs)
+
+
+@pytest.mark.parametrize("shape", [(7, 5, 9), (1, 1, 1), (6, 0, 4), (0, 3, 2), (40, 33, 17)])
+def test_oracle_rectangular_and_empty_algebra_against_scipy(O, shape):
+    """Rectangular, empty-inner and zero-row shapes, random sparse operands with duplicated
+    columns inside rows, exact cancellations and explicit zeros: the oracle's sum, product,
+    transpose and COO -> CSR agree with scipy.sparse (structure free of zeros, as the
+    reference compresses them away)."""
+    sp = pytest.importorskip("scipy.sparse")
+    m, k, n = shape
+    rng = np.random.default_rng(m * 1000 + k * 10 + n)
+
+    def rand_csr(r, c, dens):
+        if r == 0 or c == 0:
+            return np.zeros(r + 1, np.int32), np.zeros(0, np.int32), np.zeros(0)
+        lens = rng.binomial(max(1, int(c * dens * 2)), 0.5, r)
+        A = np.concatenate([[0], np.cumsum(lens)]).astype(np.int32)
+        C = rng.integers(0, c, A[-1]).astype(np.int32)
+        V = rng.integers(-3, 4, A[-1]).astype(np.float64)      # integers: exact cancellations, zeros
+        return A, C, V
+
+    def dense(A, C, V, r, c):
+        D = np.zeros((r, c))
+        for i in range(r):
+            for j in range(A[i], A[i + 1]):
+                D[i, C[j]] += V[j]
+        return D
+
+    def check(got, D):
+        A, C, V = got
+        assert A[0] == 0 and np.all(np.diff(A) >= 0) and A[-1] == len(C) == len(V)
+        assert np.all(V != 0)
+        for i in range(len(A) - 1):
+            assert np.all(np.diff(C[A[i]:A[i + 1]]) > 0)     # sorted, merged rows
+        np.testing.assert_array_equal(dense(A, C, V, len(A) - 1, D.shape[1]), D)
+
+    X1, X2, Y = rand_csr(m, k, 0.4), rand_csr(m, k, 0.3), rand_csr(k, n, 0.4)
+    D1, D2, DY = dense(*X1, m, k), dense(*X2, m, k), dense(*Y, k, n)
+    check(O.csr_add(*X1, *X2, 2.0, -1.0), 2.0 * D1 - D2)
+    check(O.csr_multiply(*X1, *Y), D1 @ DY)
+    check(O.csr_transpose(*X1, k), D1.T)
+    r = rng.integers(0, max(m, 1), 3 * m).astype(np.int32) if m else np.zeros(0, np.int32)
+    c = rng.integers(0, max(k, 1), 3 * m).astype(np.int32) if m else np.zeros(0, np.int32)
+    v = rng.integers(-2, 3, 3 * m).astype(np.float64) if m else np.zeros(0)
+    if k:
+        ref = sp.coo_matrix((v, (r, c)), shape=(m, k)).toarray()
+        check(O.coo_to_csr(m, r, c, v), ref)
