@@ -30,6 +30,24 @@ def _ptr(t):
     return ctypes.c_void_p(t.data_ptr()) if t is not None else None
 
 
+def _device_array(t, name, shape, dtypes=("float64",)):
+    """Pointer to a contiguous CUDA tensor of the given shape and an accepted dtype; any
+    other argument is a ValueError before the library sees it (a host or mis-sized buffer
+    handed to a kernel as a device array would be read out of bounds)."""
+    if not (hasattr(t, "is_cuda") and hasattr(t, "data_ptr")):
+        raise ValueError(f"{name}: {type(t).__name__}, expected a CUDA tensor")
+    dt = str(t.dtype).replace("torch.", "")
+    if dt not in dtypes:
+        raise ValueError(f"{name}: dtype {dt}, expected {' or '.join(dtypes)}")
+    if tuple(t.shape) != tuple(shape):
+        raise ValueError(f"{name}: shape {tuple(t.shape)}, expected {tuple(shape)}")
+    if not t.is_contiguous():
+        raise ValueError(f"{name}: not contiguous")
+    if not t.is_cuda:
+        raise ValueError(f"{name}: not a CUDA tensor")
+    return ctypes.c_void_p(t.data_ptr())
+
+
 def _stream():
     torch = _torch()
     return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
@@ -76,7 +94,9 @@ class System:
               raise_on_error=True) -> dict:
         """Solve A x = b with device tensors b, x (float64, length n); x is the initial guess."""
         info = _native.FeecSolveInfo()
-        st = self._lib.feec_system_solve(self._h, METHODS[method], MODES[mode], _ptr(x), _ptr(b), _ptr(residual),
+        xp, bp = _device_array(x, "x", (self.n,)), _device_array(b, "b", (self.n,))
+        rp = None if residual is None else _device_array(residual, "residual", (self.n,))
+        st = self._lib.feec_system_solve(self._h, METHODS[method], MODES[mode], xp, bp, rp,
                                          float(precision), int(max_iter), info, _stream())
         out = info.as_dict()
         out["status_name"] = _native.STATUS.get(st, str(st))
@@ -90,8 +110,9 @@ class System:
         """Solve A X[j] = B[j] for every row j of the (nrhs, n) float64 device tensors B, X
         (X holds the initial guesses) with the batched engine; one dict per column."""
         nrhs = int(B.shape[0])
+        Bp, Xp = _device_array(B, "B", (nrhs, self.n)), _device_array(X, "X", (nrhs, self.n))
         infos = (_native.FeecSolveInfo * nrhs)()
-        st = self._lib.feec_system_solve_batch(self._h, METHODS[method], MODES[mode], nrhs, _ptr(X), _ptr(B),
+        st = self._lib.feec_system_solve_batch(self._h, METHODS[method], MODES[mode], nrhs, Xp, Bp,
                                                float(precision), int(max_iter), int(rhs_per_team), infos, _stream())
         if raise_on_error and st not in (_native.FEEC_OK, _native.FEEC_MAXITER, _native.FEEC_BREAKDOWN):
             raise _native.FeecError(st, "feec_system_solve_batch")
@@ -116,10 +137,13 @@ class System:
 
     def apply(self, x, y, scaling=1.0):
         """y = scaling * A x for device tensors (float64, or float32 on the FP32 values)."""
-        if x.dtype.itemsize == 4:
-            st = self._lib.feec_system_apply_f32(self._h, _ptr(x), _ptr(y), float(scaling), _stream())
+        dt = (str(getattr(x, "dtype", "")).replace("torch.", ""),)
+        xp = _device_array(x, "x", (self.n,), ("float64", "float32"))
+        yp = _device_array(y, "y", (self.n,), dt)
+        if dt == ("float32",):
+            st = self._lib.feec_system_apply_f32(self._h, xp, yp, float(scaling), _stream())
         else:
-            st = self._lib.feec_system_apply(self._h, _ptr(x), _ptr(y), float(scaling), _stream())
+            st = self._lib.feec_system_apply(self._h, xp, yp, float(scaling), _stream())
         _native.check(st, "feec_system_apply")
 
     def set_launch(self, blocks=0, lanes=0):
@@ -143,14 +167,23 @@ class System:
             pass
 
 
+def _system_vectors(systems, bs, xs):
+    """Host arrays of system handles and of the x, b device pointers (one per system)."""
+    n = len(systems)
+    if n == 0 or len(bs) != n or len(xs) != n:
+        raise ValueError(f"{n} systems, {len(bs)} right-hand sides, {len(xs)} solutions: expected one each")
+    hs = (ctypes.c_void_p * n)(*[s._h for s in systems])
+    xp = (ctypes.c_void_p * n)(*[_device_array(x, f"xs[{i}]", (s.n,)).value for i, (s, x) in enumerate(zip(systems, xs))])
+    bp = (ctypes.c_void_p * n)(*[_device_array(b, f"bs[{i}]", (s.n,)).value for i, (s, b) in enumerate(zip(systems, bs))])
+    return hs, xp, bp
+
+
 def solve_many(systems, bs, xs, method="rainbow", mode="mixed", precision=1e-10, max_iter=0,
                raise_on_error=True) -> list:
     """One batched launch over many systems, one right-hand side each (device tensors)."""
     lib = _native.gpu()
     n = len(systems)
-    hs = (ctypes.c_void_p * n)(*[s._h for s in systems])
-    xp = (ctypes.c_void_p * n)(*[x.data_ptr() for x in xs])
-    bp = (ctypes.c_void_p * n)(*[b.data_ptr() for b in bs])
+    hs, xp, bp = _system_vectors(systems, bs, xs)
     infos = (_native.FeecSolveInfo * n)()
     st = lib.feec_solve_many(n, hs, METHODS[method], MODES[mode], xp, bp, float(precision), int(max_iter), infos,
                              _stream())
@@ -170,9 +203,7 @@ class Batch:
         self._lib = _native.gpu()
         n = len(systems)
         self.systems, self.bs, self.xs = systems, bs, xs
-        hs = (ctypes.c_void_p * n)(*[s._h for s in systems])
-        xp = (ctypes.c_void_p * n)(*[x.data_ptr() for x in xs])
-        bp = (ctypes.c_void_p * n)(*[b.data_ptr() for b in bs])
+        hs, xp, bp = _system_vectors(systems, bs, xs)
         h = ctypes.c_void_p()
         st = self._lib.feec_batch_create(ctypes.byref(h), n, hs, METHODS[method], MODES[mode], xp, bp,
                                          float(precision), int(max_iter), int(team_threads), _stream())

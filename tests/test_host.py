@@ -210,3 +210,30 @@ def test_public_header_compiles_as_c_and_cpp():
                         header], check=True)
     if shutil.which("g++"):
         subprocess.run(["g++", "-std=c++14", "-Wall", "-Werror", "-fsyntax-only", "-x", "c++", header], check=True)
+
+
+def test_device_arrays_are_checked_before_the_library():
+    """The System / Batch / solve_many mirror refuses host tensors, wrong dtypes, wrong
+    shapes and non-contiguous views with a ValueError before any pointer reaches a kernel."""
+    torch = pytest.importorskip("torch")
+    from simplefem_gb300.system import _device_array, _system_vectors
+    with pytest.raises(ValueError, match="dtype"):
+        _device_array(torch.zeros(4, dtype=torch.float32), "x", (4,))
+    with pytest.raises(ValueError, match="ndarray, expected a CUDA tensor"):
+        _device_array(np.zeros(4), "x", (4,))
+    with pytest.raises(ValueError, match="shape"):
+        _device_array(torch.zeros(5, dtype=torch.float64), "x", (4,))
+    with pytest.raises(ValueError, match="shape"):
+        _device_array(torch.zeros((4, 3), dtype=torch.float64), "B", (3, 4))
+    with pytest.raises(ValueError, match="contiguous"):
+        _device_array(torch.zeros((4, 3), dtype=torch.float64).t(), "B", (3, 4))
+    with pytest.raises(ValueError, match="CUDA"):
+        _device_array(torch.zeros(4, dtype=torch.float64), "x", (4,))
+
+    class _Sys:
+        n, _h = 4, None
+    with pytest.raises(ValueError, match="one each"):
+        _system_vectors([_Sys(), _Sys()], [torch.zeros(4, dtype=torch.float64)] * 2, [])
+    with pytest.raises(ValueError, match=r"xs\[0\]: shape"):
+        _system_vectors([_Sys(), _Sys()], [torch.zeros(4, dtype=torch.float64)] * 2,
+                        [torch.zeros(3, dtype=torch.float64), torch.zeros(4, dtype=torch.float64)])
