@@ -33,8 +33,27 @@ def _vec(a, name, n=None, writable=False):
     return a
 
 
-def _ints(a, name):
-    return np.ascontiguousarray(a, np.int32)
+def _ints(a, name, n=None):
+    a = np.ascontiguousarray(a, np.int32)
+    if n is not None and (a.ndim != 1 or a.shape[0] < n):
+        raise ValueError(f"{name} has {a.shape[0] if a.ndim == 1 else a.shape} entries, expected {n}")
+    return a
+
+
+def _coloring(N, num_colors, F, B, R):
+    """Rainbow's F (color of each row), B (color offsets) and R (rows by color) arrays."""
+    return _ints(F, "F", N), _ints(B, "B", int(num_colors) + 1), _ints(R, "R", N)
+
+
+def _csr(rows, csrrows, csrcolumns, csrvalues, name=""):
+    """The CSR arrays of a matrix with `rows` rows, checked to be as long as the row
+    pointers say (the library reads rows + 1 pointers and A[rows] columns and values
+    through the raw pointers); the pointers' contents are validated by the library."""
+    A = _ints(csrrows, name + "rows", int(rows) + 1)
+    nnz = int(A[int(rows)]) if int(rows) >= 0 else 0
+    if nnz < 0:
+        raise ValueError(f"{name}rows[{int(rows)}] = {nnz} is negative")
+    return A, _ints(csrcolumns, name + "columns", nnz), _vec(csrvalues, name + "values", nnz)
 
 
 _DONE = (_native.FEEC_OK, _native.FEEC_BREAKDOWN, _native.FEEC_SMALL_ENERGY, _native.FEEC_MAXITER)
@@ -51,9 +70,10 @@ def _finish(status, info, where):
 def ConjugateGradientSolverCSR(N, x, b, csrrows, csrcolumns, csrvalues, residual, precision, print_modulo=-3):
     """GPU replacement of ConjugateGradientSolverCSR (solver/sparsesolver.cpp:26-201)."""
     x = _vec(x, "x", N, True); residual = _vec(residual, "residual", N, True)
+    csr = _csr(N, csrrows, csrcolumns, csrvalues)
     info = _native.FeecSolveInfo()
-    st = _native.gpu().feec_cg_csr(int(N), x, _vec(b, "b", N), _ints(csrrows, "A"), _ints(csrcolumns, "C"),
-                                   _vec(csrvalues, "V"), residual, float(precision), int(print_modulo), info)
+    st = _native.gpu().feec_cg_csr(int(N), x, _vec(b, "b", N), *csr, residual, float(precision), int(print_modulo),
+                                   info)
     return _finish(st, info, "ConjugateGradientSolverCSR")
 
 
@@ -61,9 +81,9 @@ def ConjugateGradientSolverCSR_SSOR(N, x, b, csrrows, csrcolumns, csrvalues, res
                                     diagonal, omega):
     """GPU replacement of ConjugateGradientSolverCSR_SSOR (solver/sparsesolver.cpp:446-724)."""
     x = _vec(x, "x", N, True); residual = _vec(residual, "residual", N, True)
+    csr = _csr(N, csrrows, csrcolumns, csrvalues)
     info = _native.FeecSolveInfo()
-    st = _native.gpu().feec_cg_csr_ssor(int(N), x, _vec(b, "b", N), _ints(csrrows, "A"), _ints(csrcolumns, "C"),
-                                        _vec(csrvalues, "V"), residual, float(precision), int(print_modulo),
+    st = _native.gpu().feec_cg_csr_ssor(int(N), x, _vec(b, "b", N), *csr, residual, float(precision), int(print_modulo),
                                         _vec(diagonal, "diagonal", N), float(omega), info)
     return _finish(st, info, "ConjugateGradientSolverCSR_SSOR")
 
@@ -72,11 +92,11 @@ def ConjugateGradientSolverCSR_Rainbow(N, x, b, csrrows, csrcolumns, csrvalues, 
                                        diagonal, omega, num_colors, F, B, R):
     """GPU replacement of ConjugateGradientSolverCSR_Rainbow (solver/sparsesolver.cpp:1002-1335)."""
     x = _vec(x, "x", N, True); residual = _vec(residual, "residual", N, True)
+    csr = _csr(N, csrrows, csrcolumns, csrvalues)
     info = _native.FeecSolveInfo()
-    st = _native.gpu().feec_cg_csr_rainbow(int(N), x, _vec(b, "b", N), _ints(csrrows, "A"), _ints(csrcolumns, "C"),
-                                           _vec(csrvalues, "V"), residual, float(precision), int(print_modulo),
-                                           _vec(diagonal, "diagonal", N), float(omega), int(num_colors),
-                                           _ints(F, "F"), _ints(B, "B"), _ints(R, "R"), info)
+    st = _native.gpu().feec_cg_csr_rainbow(int(N), x, _vec(b, "b", N), *csr, residual, float(precision),
+                                           int(print_modulo), _vec(diagonal, "diagonal", N), float(omega),
+                                           int(num_colors), *_coloring(N, num_colors, F, B, R), info)
     return _finish(st, info, "ConjugateGradientSolverCSR_Rainbow")
 
 
@@ -85,9 +105,9 @@ def ConjugateGradientSolverCSR_SSOR_Eisenstat(N, x, b, csrrows, csrcolumns, csrv
     """GPU replacement of ConjugateGradientSolverCSR_SSOR_Eisenstat (solver/sparsesolver.cpp:726-995);
     `residual` receives the residual of the L-solved system, as in the reference."""
     x = _vec(x, "x", N, True); residual = _vec(residual, "residual", N, True)
+    csr = _csr(N, csrrows, csrcolumns, csrvalues)
     info = _native.FeecSolveInfo()
-    st = _native.gpu().feec_cg_csr_ssor_eisenstat(int(N), x, _vec(b, "b", N), _ints(csrrows, "A"),
-                                                  _ints(csrcolumns, "C"), _vec(csrvalues, "V"), residual,
+    st = _native.gpu().feec_cg_csr_ssor_eisenstat(int(N), x, _vec(b, "b", N), *csr, residual,
                                                   float(precision), int(print_modulo), _vec(diagonal, "diagonal", N),
                                                   float(omega), info)
     return _finish(st, info, "ConjugateGradientSolverCSR_SSOR_Eisenstat")
@@ -97,12 +117,12 @@ def ConjugateGradientSolverCSR_Eisenstat_Rainbow(N, x, b, csrrows, csrcolumns, c
                                                  print_modulo, diagonal, omega, num_colors, F, B, R):
     """GPU replacement of ConjugateGradientSolverCSR_Eisenstat_Rainbow (solver/sparsesolver.cpp:1338-1645)."""
     x = _vec(x, "x", N, True); residual = _vec(residual, "residual", N, True)
+    csr = _csr(N, csrrows, csrcolumns, csrvalues)
     info = _native.FeecSolveInfo()
-    st = _native.gpu().feec_cg_csr_eisenstat_rainbow(int(N), x, _vec(b, "b", N), _ints(csrrows, "A"),
-                                                     _ints(csrcolumns, "C"), _vec(csrvalues, "V"), residual,
+    st = _native.gpu().feec_cg_csr_eisenstat_rainbow(int(N), x, _vec(b, "b", N), *csr, residual,
                                                      float(precision), int(print_modulo),
                                                      _vec(diagonal, "diagonal", N), float(omega), int(num_colors),
-                                                     _ints(F, "F"), _ints(B, "B"), _ints(R, "R"), info)
+                                                     *_coloring(N, num_colors, F, B, R), info)
     return _finish(st, info, "ConjugateGradientSolverCSR_Eisenstat_Rainbow")
 
 
@@ -110,9 +130,9 @@ def ConjugateGradientSolverCSR_DiagonalPreconditioner(N, x, b, csrrows, csrcolum
                                                       print_modulo, precon):
     """GPU replacement of ConjugateGradientSolverCSR_DiagonalPreconditioner (solver/sparsesolver.cpp:221-416)."""
     x = _vec(x, "x", N, True); residual = _vec(residual, "residual", N, True)
+    csr = _csr(N, csrrows, csrcolumns, csrvalues)
     info = _native.FeecSolveInfo()
-    st = _native.gpu().feec_cg_csr_diagonal_precon(int(N), x, _vec(b, "b", N), _ints(csrrows, "A"),
-                                                   _ints(csrcolumns, "C"), _vec(csrvalues, "V"), residual,
+    st = _native.gpu().feec_cg_csr_diagonal_precon(int(N), x, _vec(b, "b", N), *csr, residual,
                                                    float(precision), int(print_modulo), _vec(precon, "precon", N),
                                                    info)
     return _finish(st, info, "ConjugateGradientSolverCSR_DiagonalPreconditioner")
@@ -120,8 +140,9 @@ def ConjugateGradientSolverCSR_DiagonalPreconditioner(N, x, b, csrrows, csrcolum
 
 def _plain(fn, where, N, x, b, csrrows, csrcolumns, csrvalues, residual, precision, print_modulo):
     x = _vec(x, "x", N, True); residual = _vec(residual, "residual", N, True)
+    csr = _csr(N, csrrows, csrcolumns, csrvalues)
     info = _native.FeecSolveInfo()
-    st = fn(int(N), x, _vec(b, "b", N), _ints(csrrows, "A"), _ints(csrcolumns, "C"), _vec(csrvalues, "V"), residual,
+    st = fn(int(N), x, _vec(b, "b", N), *csr, residual,
             float(precision), int(print_modulo), info)
     return _finish(st, info, where)
 
@@ -149,10 +170,11 @@ def ChebyshevIteration_DiagonalPreconditioner(N, x, b, csrrows, csrcolumns, csrv
                                               print_modulo, precon, lower, upper):
     """GPU replacement of ChebyshevIteration_DiagonalPreconditioner (solver/sparsesolver.cpp:2428-2590)."""
     x = _vec(x, "x", N, True); residual = _vec(residual, "residual", N, True)
+    csr = _csr(N, csrrows, csrcolumns, csrvalues)
     info = _native.FeecSolveInfo()
-    st = _native.gpu().feec_chebyshev_diag(int(N), x, _vec(b, "b", N), _ints(csrrows, "A"), _ints(csrcolumns, "C"),
-                                           _vec(csrvalues, "V"), residual, float(precision), int(print_modulo),
-                                           _vec(precon, "precon", N), float(lower), float(upper), info)
+    st = _native.gpu().feec_chebyshev_diag(int(N), x, _vec(b, "b", N), *csr, residual, float(precision),
+                                           int(print_modulo), _vec(precon, "precon", N), float(lower), float(upper),
+                                           info)
     return _finish(st, info, "ChebyshevIteration_DiagonalPreconditioner")
 
 
@@ -160,8 +182,8 @@ def _hodge(entry, where, N, L, x, b, A, B, Bt, C, residual, precision, print_mod
            inner_print_modulo):
     x = _vec(x, "x", N, True); residual = _vec(residual, "residual", N, True)
     mats = []
-    for name, M in (("A", A), ("B", B), ("Bt", Bt), ("C", C)):
-        mats += [_ints(M[0], name + "rows"), _ints(M[1], name + "columns"), _vec(M[2], name + "values")]
+    for name, rows, M in (("A", L, A), ("B", N, B), ("Bt", L, Bt), ("C", N, C)):
+        mats += [*_csr(rows, *M, name=name)]
     info = _native.FeecSolveInfo()
     st = getattr(_native.gpu(), entry)(int(N), int(L), x, _vec(b, "b", N), *mats, residual, float(precision),
                                        int(print_modulo), float(inner_precision), int(inner_print_modulo), info)
@@ -206,20 +228,20 @@ def HodgeHerzogSoodhalterMethod(dimension_A, dimension_C, x_A, x_C, b_A, b_C, A,
     dA, dC = int(dimension_A), int(dimension_C)
     x_A = _vec(x_A, "x_A", dA, True); x_C = _vec(x_C, "x_C", dC, True)
     mats = []
-    for name, M in (("A", A), ("B", B), ("Bt", Bt), ("C", C)):
-        mats += [_ints(M[0], name + "rows"), _ints(M[1], name + "columns"), _vec(M[2], name + "values")]
+    for name, rows, M in (("A", dA, A), ("B", dC, B), ("Bt", dA, Bt), ("C", dC, C)):
+        mats += [*_csr(rows, *M, name=name)]
     keep = []
 
-    def opt(P, name):
+    def opt(P, name, rows):
         if P is None:
             return [None, None, None]
-        r, c, v = _ints(P[0], name + "rows"), _ints(P[1], name + "columns"), _vec(P[2], name + "values")
+        r, c, v = _csr(rows, *P, name=name)
         keep.extend([r, c, v])
         return [r.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), c.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
                 v.ctypes.data_as(ctypes.POINTER(ctypes.c_double))]
     info = _native.FeecSolveInfo()
     st = _native.gpu().feec_hodge_herzog_soodhalter(dA, dC, x_A, x_C, _vec(b_A, "b_A", dA), _vec(b_C, "b_C", dC),
-                                                    *mats, float(precision), int(print_modulo), *opt(PA, "PA"),
-                                                    *opt(PC, "PC"), float(inneriteration_precision),
+                                                    *mats, float(precision), int(print_modulo), *opt(PA, "PA", dA),
+                                                    *opt(PC, "PC", dC), float(inneriteration_precision),
                                                     int(inneriteration_print_modulo), info)
     return _finish(st, info, "HodgeHerzogSoodhalterMethod")

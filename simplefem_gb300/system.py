@@ -173,8 +173,10 @@ def _system_vectors(systems, bs, xs):
     if n == 0 or len(bs) != n or len(xs) != n:
         raise ValueError(f"{n} systems, {len(bs)} right-hand sides, {len(xs)} solutions: expected one each")
     hs = (ctypes.c_void_p * n)(*[s._h for s in systems])
-    xp = (ctypes.c_void_p * n)(*[_device_array(x, f"xs[{i}]", (s.n,)).value for i, (s, x) in enumerate(zip(systems, xs))])
-    bp = (ctypes.c_void_p * n)(*[_device_array(b, f"bs[{i}]", (s.n,)).value for i, (s, b) in enumerate(zip(systems, bs))])
+    xp = (ctypes.c_void_p * n)(*[_device_array(x, f"xs[{i}]", (s.n,)).value
+                                  for i, (s, x) in enumerate(zip(systems, xs))])
+    bp = (ctypes.c_void_p * n)(*[_device_array(b, f"bs[{i}]", (s.n,)).value
+                                  for i, (s, b) in enumerate(zip(systems, bs))])
     return hs, xp, bp
 
 

@@ -237,3 +237,41 @@ def test_device_arrays_are_checked_before_the_library():
     with pytest.raises(ValueError, match=r"xs\[0\]: shape"):
         _system_vectors([_Sys(), _Sys()], [torch.zeros(4, dtype=torch.float64)] * 2,
                         [torch.zeros(3, dtype=torch.float64), torch.zeros(4, dtype=torch.float64)])
+
+
+def test_raw_pointer_mirror_checks_array_lengths(built):
+    """The raw-pointer drivers read N + 1 row pointers, A[N] columns and values, and the
+    Rainbow arrays through their pointers: NumPy arrays shorter than that are a ValueError
+    in the Python mirror (the library would read past them on the host)."""
+    import simplefem_gb300 as S
+    n = 3
+    A = np.array([0, 1, 2, 3], np.int32); C = np.array([0, 1, 2], np.int32); V = np.ones(3)
+    x, r, b = np.zeros(n), np.zeros(n), np.ones(n)
+    with pytest.raises(ValueError, match="columns has 2 entries, expected 3"):
+        S.ConjugateGradientSolverCSR(n, x, b, A, C[:2], V, r, 1e-10, -3)
+    with pytest.raises(ValueError, match="values has 2 entries, expected 3"):
+        S.MINRESCSR(n, x, b, A, C, V[:2], r, 1e-10, -3)
+    with pytest.raises(ValueError, match="rows has 3 entries, expected 4"):
+        S.ConjugateResidualSolverCSR(n, x, b, A[:3], C, V, r, 1e-10, -3)
+    with pytest.raises(ValueError, match="R has 2 entries, expected 3"):
+        S.ConjugateGradientSolverCSR_Rainbow(n, x, b, A, C, V, r, 1e-10, -3, np.ones(n), 1.0, 1,
+                                             np.zeros(n, np.int32), np.array([0, 3], np.int32),
+                                             np.array([2, 1], np.int32))
+    with pytest.raises(ValueError, match="B has 1 entries, expected 2"):
+        S.ConjugateGradientSolverCSR_Eisenstat_Rainbow(n, x, b, A, C, V, r, 1e-10, -3, np.ones(n), 1.0, 1,
+                                                       np.zeros(n, np.int32), np.array([0], np.int32),
+                                                       np.array([2, 1, 0], np.int32))
+    # Hodge: B has N rows, Bt has L rows
+    L = 2
+    Ah = (np.array([0, 1, 2], np.int32), np.array([0, 1], np.int32), np.ones(2))
+    Bh = (np.array([0, 1, 2, 3], np.int32), np.array([0, 1, 0], np.int32), np.ones(3))
+    Bth = (np.array([0, 2, 3], np.int32), np.array([0, 2, 1], np.int32), np.ones(3))
+    with pytest.raises(ValueError, match="Btrows has 2 entries, expected 3"):
+        S.HodgeConjugateResidualSolverCSR_diagonal(n, L, x, b, Ah, Bh, (Bth[0][:2], Bth[1], Bth[2]), (A, C, V), r,
+                                                   1e-10, -3, 1e-12)
+    with pytest.raises(ValueError, match="Bcolumns has 2 entries, expected 3"):
+        S.HodgeConjugateResidualSolverCSR_textbook(n, L, x, b, Ah, (Bh[0], Bh[1][:2], Bh[2]), Bth, (A, C, V), r,
+                                                   1e-10, -3, 1e-12)
+    with pytest.raises(ValueError, match="PArows has 2 entries, expected 3"):
+        S.HodgeHerzogSoodhalterMethod(L, n, np.zeros(L), np.zeros(n), np.ones(L), b, Ah, Bh, Bth, (A, C, V),
+                                      1e-10, -3, (Ah[0][:2], Ah[1], Ah[2]), None, 1e-12)
