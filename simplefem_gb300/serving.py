@@ -15,6 +15,7 @@ import threading
 import numpy as np
 
 from . import _native
+from .solver import _csr, _vec
 
 METHODS = {"cg": _native.METHOD_CG, "rainbow": _native.METHOD_RAINBOW}
 MODES = {"fp64": _native.MODE_FP64, "mixed": _native.MODE_MIXED}
@@ -57,9 +58,15 @@ class Server:
         self._lock = threading.Lock()
 
     def submit(self, A, C, V, b, precision=1e-10) -> int:
-        A = np.ascontiguousarray(A, np.int32); C = np.ascontiguousarray(C, np.int32)
-        V = np.ascontiguousarray(V, np.float64); b = np.ascontiguousarray(b, np.float64)
-        x = np.zeros(len(A) - 1)
+        """Queue A x = b. The host CSR arrays and right-hand side are read by a worker thread
+        after this call returns: they are kept alive here until the request is polled, and
+        must not be changed before then."""
+        n = len(A) - 1
+        if n < 1:
+            raise ValueError("a request needs at least one row")
+        A, C, V = _csr(n, A, C, V)
+        b = _vec(b, "b", n)
+        x = np.zeros(n)
         rid = ctypes.c_longlong(0)
         p = lambda a: a.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
         with self._lock:

@@ -275,3 +275,17 @@ def test_raw_pointer_mirror_checks_array_lengths(built):
     with pytest.raises(ValueError, match="PArows has 2 entries, expected 3"):
         S.HodgeHerzogSoodhalterMethod(L, n, np.zeros(L), np.zeros(n), np.ones(L), b, Ah, Bh, Bth, (A, C, V),
                                       1e-10, -3, (Ah[0][:2], Ah[1], Ah[2]), None, 1e-12)
+
+
+def test_server_submit_checks_arrays_before_queueing(built):
+    """A request's CSR arrays and right-hand side are read later by a worker thread: arrays
+    shorter than the row pointers say are refused at submit with a ValueError."""
+    from simplefem_gb300.serving import Server
+    srv = object.__new__(Server)                       # no device here: only the host checks run
+    A = np.array([0, 1, 2], np.int32); C = np.array([0, 1], np.int32); V = np.ones(2)
+    with pytest.raises(ValueError, match="at least one row"):
+        srv.submit(np.array([0], np.int32), C[:0], V[:0], np.ones(0))
+    with pytest.raises(ValueError, match="columns has 1 entries, expected 2"):
+        srv.submit(A, C[:1], V, np.ones(2))
+    with pytest.raises(ValueError, match="b has 1 entries, expected 2"):
+        srv.submit(A, C, V, np.ones(1))
