@@ -68,7 +68,8 @@ class MatrixCSR:
 
     def check(self):
         """Structural invariants of MatrixCSR::check (sparse/matcsr.cpp:178-194)."""
-        if self.A.shape[0] != self.rows + 1 or self.C.shape[0] != self.V.shape[0]:
+        if (self.A.ndim != 1 or self.A.shape[0] != self.rows + 1 or self.C.shape[0] != self.V.shape[0]
+                or int(self.A[self.rows]) != self.C.shape[0]):
             raise ValueError("MatrixCSR: array sizes do not match the dimensions")
         st = _native.gpu().feec_csr_check(self.rows, self.columns, self.A, self.C, self.V)
         if st != _native.FEEC_OK:

@@ -103,6 +103,8 @@ def test_csr_check_rejects_bad_arrays(built):
         MatrixCSR(2, 2, [0, 1, 2], [0, 2], [1.0, 1.0])          # column out of range
     with pytest.raises(ValueError):
         MatrixCSR(2, 2, [0, 1, 2], [0, 1], [1.0, np.nan])       # non-finite value
+    with pytest.raises(ValueError):
+        MatrixCSR(2, 2, [0, 1, 3], [0, 1], [1.0, 1.0])          # A[rows] beyond the stored entries
 
 
 def test_solver_argument_checks_fail_like_asserts(built):
