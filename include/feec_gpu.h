@@ -11,6 +11,12 @@
  * pointers (the reference's raw-pointer convention) and copy to and from the
  * GPU inside the call; the feec_system_* entry points keep a matrix resident
  * on the GPU and take device pointers.
+ *
+ * Threads: the host entry points are reentrant like the reference's functions
+ * (each call owns its device scratch; calls from several host threads are
+ * ordered on CUDA's default stream). A feec_system or feec_batch handle is used
+ * by one host thread at a time. A feec_server may be used from any number of
+ * threads (its queue is locked inside).
  */
 #ifndef FEEC_GPU_H
 #define FEEC_GPU_H
