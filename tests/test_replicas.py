@@ -63,3 +63,26 @@ def test_single_process_needs_no_process_group():
     import bench
     assert bench.max_over_ranks(3.5) == 3.5
     assert bench.whole_job_rate(10, 1, 2.0) == 5.0
+
+
+def test_reference_arm_prints_the_contract_line():
+    """`bench.py --impl reference` at N = 1: one JSON line with the arm's own metric, unit and
+    config, whole solves of the headline workload timed on the host cores (the oracle's
+    restatement of the reference's Rainbow SSOR-PCG), and zero-copy e2e."""
+    import json
+    import subprocess
+    sys.path.insert(0, ROOT)
+    import bench
+    out = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--steps", "1",
+                          "--warmup", "0"], cwd=ROOT, capture_output=True, text=True, timeout=600, check=True)
+    lines = [ln for ln in out.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["metric"] == bench.METRIC and d["unit"] == "solves/s"
+    assert d["n_gpus"] == 1 and d["steps"] == 1 and d["warmup"] == 3          # W is raised to 3
+    assert d["higher_is_better"] is True and d["config"]["workload"] == bench.WORKLOAD_NAME
+    assert d["value"] > 0 and d["ms_per_step"] == pytest.approx(1000.0 / d["value"])
+    cb = d["cpu_baseline"]
+    assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == d["value"] and cb["sample"]
+    assert d["e2e"] == {"value": d["value"], "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+    assert d["config"]["iterations"] > 0
