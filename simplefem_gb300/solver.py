@@ -28,6 +28,8 @@ def _vec(a, name, n=None, writable=False):
         if writable:
             raise TypeError(f"{name} must be a C-contiguous float64 numpy array (it is written in place)")
         a = np.ascontiguousarray(a, np.float64)
+    if a.ndim != 1:
+        raise ValueError(f"{name} must be one-dimensional, not of shape {a.shape}")
     if n is not None and a.shape[0] < n:
         raise ValueError(f"{name} has {a.shape[0]} entries, expected {n}")
     return a

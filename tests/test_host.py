@@ -253,6 +253,8 @@ def test_raw_pointer_mirror_checks_array_lengths(built):
         S.ConjugateGradientSolverCSR(n, x, b, A, C[:2], V, r, 1e-10, -3)
     with pytest.raises(ValueError, match="values has 2 entries, expected 3"):
         S.MINRESCSR(n, x, b, A, C, V[:2], r, 1e-10, -3)
+    with pytest.raises(ValueError, match="x must be one-dimensional"):
+        S.ConjugateGradientSolverCSR(n, np.zeros((n, 1)), b, A, C, V, r, 1e-10, -3)
     with pytest.raises(ValueError, match="rows has 3 entries, expected 4"):
         S.ConjugateResidualSolverCSR(n, x, b, A[:3], C, V, r, 1e-10, -3)
     with pytest.raises(ValueError, match="R has 2 entries, expected 3"):
