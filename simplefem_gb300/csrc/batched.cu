@@ -539,17 +539,12 @@ int feec_batch_create(feec_batch** out, int nsys, feec_system* const* systems, i
     *out = nullptr;
     feec_batch* bt = new (std::nothrow) feec_batch();
     if (!bt) return FEEC_OOM;
-    struct Cleanup {
+    struct Cleanup {                      // a failed create releases whatever it made
         feec_batch*& p;
         bool keep = false;
         ~Cleanup() {
             if (!keep && p) {
-                p->mem.release();
-                cudaStreamSynchronize(p->stream);
-                if (p->own_stream) cudaStreamDestroy(p->stream);
-                if (p->ev_in) cudaEventDestroy(p->ev_in);
-                if (p->hres) cudaFreeHost(p->hres);
-                delete p;
+                feec_batch_destroy(p);
                 p = nullptr;
             }
         }
