@@ -79,36 +79,41 @@ extern "C" int feec_cg_csr_noalloc(int N, double* x, const double* b, const int*
         *info = feec_solve_info{};
         info->true_relres = -1.0;
         info->outer_iterations = 1;
+        info->error_estimate = -1.0;
     }
-    if (N <= 0 || !x || !b || !A || !C || !V || !residual || !(precision > 0.0)) return FEEC_BADARG;
+    // every early return records its code in info->status as well
+    auto fail = [info](int code) {
+        if (info) info->status = code;
+        return code;
+    };
+    if (N <= 0 || !x || !b || !A || !C || !V || !residual || !(precision > 0.0)) return fail(FEEC_BADARG);
     if (N > kNoAllocMaxRows) {
         std::fprintf(stderr, "feec_cg_csr_noalloc: N = %d exceeds the fixed scratch capacity of %d rows\n", N,
                      kNoAllocMaxRows);
-        if (info) info->status = FEEC_BADARG;
-        return FEEC_BADARG;
+        return fail(FEEC_BADARG);
     }
     NoAllocScratch* sc = nullptr;
     int st = noalloc_scratch(sc);
-    if (st != FEEC_OK) return st;
+    if (st != FEEC_OK) return fail(st);
     cudaStream_t s = (cudaStream_t)stream;
 
     // structural check of the caller's CSR before any kernel indexes through it
     int nnz = -1;
     cudaError_t e = cudaMemcpyAsync(&nnz, A + N, sizeof(int), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    if (e != cudaSuccess) return noalloc_cuda(e);
-    if (nnz < 0) return FEEC_BADARG;
+    if (e != cudaSuccess) return fail(noalloc_cuda(e));
+    if (nnz < 0) return fail(FEEC_BADARG);
     int bad = 0;
     if ((e = cudaMemsetAsync(&sc->bad, 0, sizeof(int), s)) != cudaSuccess ||
         (e = launch_validate_csr(N, nnz, A, C, &sc->bad, s)) != cudaSuccess ||
         (e = launch_sum_sq_f64(N, b, &sc->bnorm2, s)) != cudaSuccess)
-        return noalloc_cuda(e);
+        return fail(noalloc_cuda(e));
     double bnorm2 = 0.0;
     if ((e = cudaMemcpyAsync(&bad, &sc->bad, sizeof(int), cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
         (e = cudaMemcpyAsync(&bnorm2, &sc->bnorm2, sizeof(double), cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
         (e = cudaStreamSynchronize(s)) != cudaSuccess)
-        return noalloc_cuda(e);
-    if (bad) return FEEC_BADARG;
+        return fail(noalloc_cuda(e));
+    if (bad) return fail(FEEC_BADARG);
 
     // tolerance exactly as solver/sparsesolver.cpp:45-48 (norm summed on the device)
     const double kFloor = 1.490116119384765625e-08;
@@ -116,7 +121,7 @@ extern "C" int feec_cg_csr_noalloc(int N, double* x, const double* b, const int*
     if (!(tolerance >= kFloor)) tolerance = tolerance != tolerance ? tolerance : kFloor;
 
     // the status words (barrier counter, abort flag, status) must start at zero
-    if ((e = cudaMemsetAsync(&sc->st, 0, sizeof(DeviceStatus), s)) != cudaSuccess) return noalloc_cuda(e);
+    if ((e = cudaMemsetAsync(&sc->st, 0, sizeof(DeviceStatus), s)) != cudaSuccess) return fail(noalloc_cuda(e));
 
     CgArgs<double> a{};
     a.n = N; a.rp = A; a.ci = C; a.val = V; a.b = b; a.x = x; a.r = residual; a.d = sc->d; a.q = sc->q;
@@ -131,11 +136,11 @@ extern "C" int feec_cg_csr_noalloc(int N, double* x, const double* b, const int*
     shape.threads = 512;
     const int maxb = max_coresident_blocks(0, 0, shape.lanes, shape.threads);
     if (maxb > kNoAllocMaxBlocks) shape.blocks = kNoAllocMaxBlocks;
-    if ((e = launch_cg<double>(a, shape, s)) != cudaSuccess) return noalloc_cuda(e);
+    if ((e = launch_cg<double>(a, shape, s)) != cudaSuccess) return fail(noalloc_cuda(e));
     DeviceStatus hs{};
     if ((e = cudaMemcpyAsync(&hs, &sc->st, sizeof(DeviceStatus), cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
         (e = cudaStreamSynchronize(s)) != cudaSuccess)
-        return noalloc_cuda(e);
+        return fail(noalloc_cuda(e));
     if (info) {
         info->status = hs.status;
         info->iterations = hs.iterations;
