@@ -59,6 +59,45 @@ def test_dropin_exports_reference_mangled_names(built):
         assert mangled in out, mangled
 
 
+REF_SOLVER_OBJECT = os.path.join(ROOT, "oracle", "_ref", "solver.o")
+
+
+@pytest.mark.skipif(not os.path.exists(REF_SOLVER_OBJECT),
+                    reason="the reference's own solver object is built only where its sources are mounted")
+def test_dropin_exports_the_reference_objects_csr_solver_names(built):
+    """Every CSR Krylov driver the reference's compiled solver module defines (its own
+    object file, oracle/_ref/solver.o) is exported by the shim under the same symbol,
+    and the shim exports nothing else of that family."""
+    from simplefem_gb300 import build
+    family = re.compile(r"(CSR|MINRES|Chebyshev|Hodge)")
+
+    def defined(cmd):
+        out = subprocess.run(cmd, capture_output=True, text=True, check=True).stdout
+        return {ln.split()[-1] for ln in out.splitlines()
+                if len(ln.split()) == 3 and ln.split()[1] == "T" and family.search(ln.split()[-1])}
+
+    ref = defined(["nm", "--defined-only", REF_SOLVER_OBJECT])
+    shim = defined(["nm", "-D", "--defined-only", build.lib_path("libfeec_dropin.so")])
+    assert ref, "no CSR drivers found in the reference object"
+    assert shim == ref, (sorted(ref - shim), sorted(shim - ref))
+
+
+def test_shim_aborts_like_a_checked_build_when_no_gpu_is_usable(built, tmp_path):
+    """A C++ caller linked against the shim alone: where no GPU is usable the C ABI
+    returns FEEC_NO_DEVICE and the shim prints it and aborts (it never falls back to
+    the CPU). On a GPU machine this runs the same driver's argument-check abort."""
+    import torch
+    from test_gpu_dropin_shim import build_driver, write_input
+    g = load_golden("lap5_n8")
+    exe = build_driver(tmp_path)
+    inp, outp = str(tmp_path / "in.bin"), str(tmp_path / "out.bin")
+    has_gpu = torch.cuda.is_available()
+    write_input(inp, g, precision=-1.0 if has_gpu else None)
+    res = subprocess.run([exe, inp, outp], capture_output=True, text=True, timeout=120)
+    assert res.returncode == -6, (res.returncode, res.stderr)
+    assert "ConjugateGradientSolverCSR:" in res.stderr
+
+
 @pytest.mark.parametrize("name", golden_names())
 def test_rainbow_bitexact_against_reference(built, name):
     from simplefem_gb300 import MatrixCSR, Rainbow
