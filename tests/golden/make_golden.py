@@ -1,7 +1,8 @@
 """Writes the golden fixtures in this directory from the FEEC++ reference itself.
 
 Runs ``oracle/_ref/ref_harness`` (the unmodified reference modules linked with a small
-driver, built by ``make -C oracle -f Makefile.ref``) and stores, per case, one
+driver, built by ``make -C oracle -f Makefile.ref`` with FEEC_REFERENCE_DIR naming the
+reference sources) and stores, per case, one
 compressed ``.npz`` holding:
 
 * the matrix exactly as the reference assembles it (``A``, ``C``, ``V``; plus ``pos``,
@@ -93,7 +94,7 @@ def spectral_bounds(m):
 
 def main():
     if not os.path.exists(HARNESS):
-        sys.exit("build the reference harness first: make -C oracle -f Makefile.ref")
+        sys.exit("build the reference harness first: FEEC_REFERENCE_DIR=<reference sources> make -C oracle -f Makefile.ref")
     with tempfile.TemporaryDirectory() as tmp:
         t = lambda name: os.path.join(tmp, name)  # noqa: E731
         for name, spec, seed, omegas in CASES:

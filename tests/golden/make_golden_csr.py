@@ -49,7 +49,7 @@ def first_rows(m, k):
 
 def main():
     if not os.path.exists(HARNESS):
-        sys.exit("build the reference harness first: make -C oracle -f Makefile.ref")
+        sys.exit("build the reference harness first: FEEC_REFERENCE_DIR=<reference sources> make -C oracle -f Makefile.ref")
     out = {}
     with tempfile.TemporaryDirectory() as tmp:
         t = lambda name: os.path.join(tmp, name)  # noqa: E731

@@ -46,7 +46,7 @@ def run(*args):
 
 def main():
     if not os.path.exists(HARNESS):
-        sys.exit("build the reference harness first: make -C oracle -f Makefile.ref")
+        sys.exit("build the reference harness first: FEEC_REFERENCE_DIR=<reference sources> make -C oracle -f Makefile.ref")
     out = {}
     rng = np.random.default_rng(4242)
     with tempfile.TemporaryDirectory() as tmp:
