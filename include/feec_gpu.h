@@ -16,7 +16,9 @@
  * (each call owns its device scratch; calls from several host threads are
  * ordered on CUDA's default stream). A feec_system or feec_batch handle is used
  * by one host thread at a time. A feec_server may be used from any number of
- * threads (its queue is locked inside).
+ * threads (its queue is locked inside). The one exception is
+ * feec_cg_csr_noalloc: all its calls share one fixed device scratch array, so
+ * the caller must serialise calls whose GPU work could overlap.
  */
 #ifndef FEEC_GPU_H
 #define FEEC_GPU_H
@@ -79,6 +81,9 @@ typedef struct feec_solve_info {
     int fp64_fallback;       /* MIXED: 1 if FP32 inner solves stagnated (operator too       */
                              /* ill-conditioned for FP32) and the solve finished in FP64    */
     int reserved;
+    double error_estimate;   /* MIXED: estimated ||x - x*|| / ||x*|| from the measured      */
+                             /* error-to-residual amplification of the outer corrections;   */
+                             /* the solve keeps it <= 10 x precision; -1 if not estimated   */
 } feec_solve_info;
 
 /* ---------------------------------------------------------------------------
@@ -398,7 +403,8 @@ int feec_system_destroy(feec_system* sys);
  * (larger N returns FEEC_BADARG). All calls share that array: calls that overlap
  * on the GPU race and must be serialised by the caller. The first call on a
  * device looks up the array's address; make it before any stream capture.
- * max_iter <= 0 means N; `stream` is a cudaStream_t (NULL = legacy default). */
+ * max_iter <= 0 means N; `stream` is a cudaStream_t (NULL = legacy default).
+ * Every return, early ones included, also stores its code in info->status. */
 int feec_cg_csr_noalloc(int N, double* x, const double* b,
                         const int* A, const int* C, const double* V,
                         double* residual, double precision, int max_iter,
@@ -428,6 +434,7 @@ typedef struct feec_request_result {
     double t_submit_ms;      /* host steady-clock times since the server started    */
     double t_start_ms;       /* solve launched (after admission and set-up)         */
     double t_end_ms;         /* solution copied back                                */
+    double error_estimate;   /* mixed: estimated relative error of x (-1: none)     */
 } feec_request_result;
 
 int feec_server_create(feec_server** srv, size_t hbm_budget_bytes, int slots, int method, int mode);

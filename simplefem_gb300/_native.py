@@ -31,6 +31,7 @@ class FeecSolveInfo(ctypes.Structure):
         ("lanes_per_row", ctypes.c_int),
         ("fp64_fallback", ctypes.c_int),
         ("reserved", ctypes.c_int),
+        ("error_estimate", ctypes.c_double),
     ]
 
     def as_dict(self):

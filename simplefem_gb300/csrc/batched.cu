@@ -219,6 +219,7 @@ int rescue_stagnated(cudaStream_t st, const std::vector<feec_system*>& systems, 
         d.iterations += r2[k].iterations;
         d.outer += r2[k].outer;
         d.relres = r2[k].relres;
+        d.err_est = r2[k].err_est;
         d.fp64_fallback = 1;
     }
     if (extra_ms) *extra_ms += ms;
@@ -243,6 +244,7 @@ void fill_infos(const std::vector<BatchResult>& res, double precision, float ms,
             f.lanes_per_row = 1;
             f.grid_blocks = grid;
             f.fp64_fallback = res[i].fp64_fallback;
+            f.error_estimate = res[i].err_est;
         }
     }
 }

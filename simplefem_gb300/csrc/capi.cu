@@ -166,6 +166,7 @@ void zero_info(feec_solve_info* info) {
     std::memset(info, 0, sizeof(*info));
     info->true_relres = -1.0;
     info->outer_iterations = 1;
+    info->error_estimate = -1.0;
 }
 
 const char* method_title(int method) {
@@ -250,6 +251,7 @@ int solve_core(feec_system* s, int method, int mode, double* xx, const double* b
     int K_total = 0, outer = 0, status = FEEC_OK;
     double final_norm = 0.0;
     int fell_back = 0;
+    double err_estimate = -1.0;      // MIXED: estimated relative error of x (-1: not estimated)
     DeviceStatus hs{};
 
     // FP64 solve from the current iterate s->x: run with the recursive-residual rule, then
@@ -372,18 +374,34 @@ int solve_core(feec_system* s, int method, int mode, double* xx, const double* b
         double rn2 = 0.0;
         double stall_limit = 0.0;        // residual norm above which the last outer step stagnated
         bool stagnated = false;
+        // Error control. A small residual does not make a small error: what the FP32 inner
+        // solves leave behind is mostly smooth, low-eigenvalue error, which A shrinks the most.
+        // Each outer step measures how large its correction was against the residual it
+        // corrected (the correction c_k approximates the error of x_k), which gives the
+        // error-to-residual amplification of this operator; the solve then also asks
+        // amplification x relative residual <= err_target before it stops, and sizes its last
+        // inner solve for both bars. At most one step is added for the error bar alone.
+        const double err_target = kErrorPerResidual * precision;
+        double amp = 0.0;                // largest measured amplification (steps after the first)
+        bool err_step = false;           // the last step was taken for the error bar alone
         for (outer = 0; outer < max_outer; outer++) {
             st = true_residual(s, s->b, s->x, s->r, rn2, permuted);
             if (st != FEEC_OK) return st;
             const double rn = std::sqrt(rn2);
             final_norm = rn;
             if (!(rn == rn)) { status = FEEC_BREAKDOWN; break; }
-            if (rn <= tolerance) { status = FEEC_OK; break; }
+            const double relres = bnorm > 0.0 ? rn / bnorm : 0.0;
+            if (rn <= tolerance) {
+                if (err_step || amp == 0.0 || amp * relres <= err_target) { status = FEEC_OK; break; }
+                err_step = true;
+            } else if (err_step) {
+                break;   // the error-bar step lost the residual bar: leave it to the final check
+            }
             // An inner solve that gained less than half the digits it was asked for means the
             // operator is too ill-conditioned for FP32 arithmetic (condition number times the
             // FP32 unit roundoff near 1e-2 or above): finish in FP64 from the current iterate,
             // with a fresh budget of max_iter iterations.
-            if (outer > 0 && rn > stall_limit) { stagnated = true; break; }
+            if (outer > 0 && !err_step && rn > stall_limit) { stagnated = true; break; }
             if (K_total >= max_iter) { status = FEEC_MAXITER; break; }
             const double inv = 1.0 / rn;
             const double scal_h[2] = {inv, rn};
@@ -395,8 +413,11 @@ int solve_core(feec_system* s, int method, int mode, double* xx, const double* b
             FEEC_TRY(cudaMemsetAsync(s->m32, 0, sizeof(float) * n, s->stream));
             FEEC_TRY(cudaMemsetAsync(s->q32, 0, sizeof(float) * n, s->stream));
             FEEC_TRY(cudaMemsetAsync(s->r32, 0, sizeof(float) * n, s->stream));
-            // do not over-solve the last step: ask only for the reduction still needed (with margin)
-            const double need = 0.3 * tolerance / rn;
+            // do not over-solve the last step: ask only for the reduction still needed (with
+            // margin) to meet the residual bar and, once an amplification is known, the error bar
+            double target = tolerance;
+            if (amp > 0.0) target = std::min(target, err_target * bnorm / amp);
+            const double need = 0.3 * target / rn;
             const double eta = std::max(inner_eta, need);
             stall_limit = rn * std::sqrt(eta);
             float ms = 0.0f;
@@ -429,9 +450,16 @@ int solve_core(feec_system* s, int method, int mode, double* xx, const double* b
                 FEEC_TRY(launch_eisenstat<float>(a, shape, s->stream));
             }
             FEEC_TRY(cudaEventRecord(s->ev1, s->stream));
-            FEEC_TRY(launch_update_x(n, nullptr, s->x32, s->scal + 3, s->x, s->stream));
+            FEEC_TRY(launch_update_x_norms(n, s->x32, s->scal + 3, s->x, s->partials, s->scal + 4, s->stream));
+            double norms2[2] = {0.0, 0.0};   // ||correction||^2, ||x||^2
+            FEEC_TRY(cudaMemcpyAsync(norms2, s->scal + 4, sizeof(norms2), cudaMemcpyDeviceToHost, s->stream));
             FEEC_TRY(cudaEventSynchronize(s->ev1));
             FEEC_TRY(cudaEventElapsedTime(&ms, s->ev0, s->ev1));
+            FEEC_TRY(cudaStreamSynchronize(s->stream));
+            // the first step starts from x = 0 (its correction is the whole solution); later
+            // corrections measure the error of the iterate they corrected
+            if (outer > 0 && norms2[1] > 0.0 && relres > 0.0)
+                amp = std::max(amp, std::sqrt(norms2[0] / norms2[1]) / relres);
             ms_total += ms;
             st = read_status(s, hs);
             if (st != FEEC_OK) return st;
@@ -451,6 +479,7 @@ int solve_core(feec_system* s, int method, int mode, double* xx, const double* b
         if (st != FEEC_OK) return st;
         final_norm = std::sqrt(rn2b);
         if (status == FEEC_OK && final_norm > tolerance) status = FEEC_MAXITER;
+        if (amp > 0.0 && !fell_back && bnorm > 0.0) err_estimate = amp * final_norm / bnorm;
     }
 
     // results back to the caller's numbering
@@ -463,6 +492,7 @@ int solve_core(feec_system* s, int method, int mode, double* xx, const double* b
         info->outer_iterations = outer;
         info->num_colors = cg_family ? 0 : s->num_levels;
         info->fp64_fallback = fell_back;
+        info->error_estimate = err_estimate;
         info->tolerance = (mode == FEEC_MODE_REFERENCE) ? tolerance : precision;
         info->final_norm = final_norm;
         info->device_ms = ms_total;

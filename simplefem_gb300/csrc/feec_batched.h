@@ -40,6 +40,7 @@ struct BatchResult {
     int status, iterations, outer;
     int fp64_fallback;        // set on the host when a stagnated column was finished in FP64
     double relres;
+    double err_est;           // mixed: estimated relative error of x (-1: not estimated)
 };
 
 struct BatchArgs {

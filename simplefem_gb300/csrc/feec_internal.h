@@ -15,6 +15,10 @@ namespace feec {
 
 struct DeviceStatus;
 
+// Mixed precision stops only when its estimated relative solution error is at most this
+// many times the requested relative residual (1e-9 at a request of 1e-10).
+constexpr double kErrorPerResidual = 10.0;
+
 // ---------------------------------------------------------------------------
 // Persistent solver arguments (all pointers are device pointers).
 // ---------------------------------------------------------------------------
@@ -102,6 +106,11 @@ cudaError_t launch_sweep_factors(int n, const double* diag, double omega, double
 // Mixed precision helpers.
 cudaError_t launch_scaled_cast(int n, const double* r, const double* inv_norm_dev, float* r32, cudaStream_t s);
 cudaError_t launch_update_x(int n, const int* perm, const float* c32, const double* norm_dev, double* x, cudaStream_t s);
+// x += (*norm_dev) c32 (unpermuted) and out2[0] = ||correction||^2, out2[1] = ||x||^2
+// (deterministic: per-block partials in `partials`, at least update_norm_blocks(n) x 2)
+cudaError_t launch_update_x_norms(int n, const float* c32, const double* norm_dev, double* x, double* partials,
+                                  double* out2, cudaStream_t s);
+int update_norm_blocks(int n);
 void note_launch();
 
 // Host integer preprocessing (coloring.cpp).

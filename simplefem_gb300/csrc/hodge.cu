@@ -256,6 +256,7 @@ int hodge_cr(int variant, int N, int L, double* x, const double* b, const int* A
     if (info) {
         *info = feec_solve_info{};
         info->true_relres = -1.0;
+        info->error_estimate = -1.0;
         info->outer_iterations = 1;
     }
     // the reference asserts these (:76-94)
@@ -428,6 +429,7 @@ int hodge_hs(int dA, int dC, double* x_A, double* x_C, const double* b_A, const 
     if (info) {
         *info = feec_solve_info{};
         info->true_relres = -1.0;
+        info->error_estimate = -1.0;
         info->outer_iterations = 1;
     }
     // the reference asserts these (:1142-1159)

@@ -384,6 +384,7 @@ void clear_info(feec_solve_info* info) {
     std::memset(info, 0, sizeof(*info));
     info->true_relres = -1.0;
     info->outer_iterations = 1;
+    info->error_estimate = -1.0;
 }
 
 int more_dropin(int kind, int N, double* x, const double* b, const int* A, const int* C, const double* V,

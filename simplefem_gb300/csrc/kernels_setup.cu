@@ -186,6 +186,28 @@ __global__ void update_x_kernel(int n, const int* __restrict__ perm, const float
     if (i < n) x[perm ? perm[i] : i] += (*norm) * (double)c32[i];
 }
 
+// The same update, plus per-block partial sums of the squared correction and of the
+// squared new iterate (partials[blk] and partials[gridDim.x + blk]): the defect
+// correction's error estimate compares the size of each correction with the solution.
+__global__ void update_x_norms_kernel(int n, const float* __restrict__ c32, const double* __restrict__ norm,
+                                      double* __restrict__ x, double* __restrict__ partials) {
+    const double s = *norm;
+    double cc = 0.0, xx = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const double c = s * (double)c32[i];
+        const double xn = x[i] + c;
+        x[i] = xn;
+        cc += c * c;
+        xx += xn * xn;
+    }
+    double v[2] = {cc, xx};
+    block_reduce<double, 2>(v);
+    if (threadIdx.x == 0) {
+        partials[blockIdx.x] = v[0];
+        partials[gridDim.x + blockIdx.x] = v[1];
+    }
+}
+
 // SELL-32 block lengths of each slice: the longest L, E and U part over its rows.
 // lsplit == null: the whole row is one block (U), for the unpreconditioned CG.
 __global__ void sell_lengths_kernel(int nslices, const int* __restrict__ row0, const int* __restrict__ nrow,
@@ -467,6 +489,20 @@ cudaError_t launch_sweep_factors(int n, const double* diag, double omega, double
 
 cudaError_t launch_scaled_cast(int n, const double* r, const double* inv_norm_dev, float* r32, cudaStream_t s) {
     return launch(scaled_cast_kernel, grid_for(n, kBlock), kBlock, s, n, r, inv_norm_dev, r32);
+}
+
+int update_norm_blocks(int n) {
+    const int g = grid_for(n, kBlock);
+    return g < 1024 ? (g < 1 ? 1 : g) : 1024;
+}
+
+cudaError_t launch_update_x_norms(int n, const float* c32, const double* norm_dev, double* x, double* partials,
+                                  double* out2, cudaStream_t s) {
+    const int g = update_norm_blocks(n);
+    cudaError_t e = launch(update_x_norms_kernel, g, kBlock, s, n, c32, norm_dev, x, partials);
+    if (e == cudaSuccess) e = launch(sum_kernel, 1, 1024, s, g, partials, out2, 0);
+    if (e == cudaSuccess) e = launch(sum_kernel, 1, 1024, s, g, partials + g, out2 + 1, 0);
+    return e;
 }
 
 cudaError_t launch_update_x(int n, const int* perm, const float* c32, const double* norm_dev, double* x, cudaStream_t s) {

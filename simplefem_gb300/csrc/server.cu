@@ -139,6 +139,7 @@ int serve_one(feec_server* srv, const Request& rq, cudaStream_t stream, feec_req
         res.true_relres = info.true_relres;
         res.cluster_blocks = -info.grid_blocks;   // negative: whole-GPU persistent grid
         res.fp64_fallback = info.fp64_fallback;
+        res.error_estimate = info.error_estimate;
         return st;
     }
     st = sell_prepare(s, rainbow ? FEEC_METHOD_RAINBOW : FEEC_METHOD_CG);
@@ -228,6 +229,7 @@ int serve_one(feec_server* srv, const Request& rq, cudaStream_t stream, feec_req
     res.true_relres = hr.relres;
     res.cluster_blocks = blocks;
     res.fp64_fallback = hr.fp64_fallback;
+    res.error_estimate = hr.err_est;
     return hr.status;
 }
 
@@ -303,6 +305,9 @@ int feec_server_create(feec_server** out, size_t hbm_budget_bytes, int slots, in
 int feec_server_submit(feec_server* srv, int N, const int* A, const int* C, const double* V, const double* b,
                        double* x, double precision, long long* id) {
     if (!srv || N <= 0 || !A || !C || !V || !b || !x || !(precision > 0.0)) return FEEC_BADARG;
+    // row pointers must start at 0 and end at a non-negative entry count before the
+    // footprint estimate reads A[N] (a negative count would wrap to a huge size)
+    if (A[0] != 0 || A[N] < 0) return FEEC_BADARG;
     Request rq;
     rq.n = N; rq.A = A; rq.C = C; rq.V = V; rq.b = b; rq.x = x; rq.precision = precision;
     rq.bytes = estimate_bytes(N, A[N]);

@@ -345,8 +345,10 @@ __device__ __forceinline__ void for_slices_dot(const Team& team, const SellView&
 template <typename T, int K>
 struct TeamControl {
     double bnorm2[K], relres[K], stall[K], rnorm[K], eta2[K], zr[K], rr[K], rr0[K];
+    double amp[K];   // largest measured error-to-residual amplification of column j (0: none yet)
     int iters[K], outer[K], status[K];
     T alpha[K], beta[K], inv[K];
+    int err_step;    // bit j: column j's last outer step was taken for the error bar alone
     int done;        // bit j: column j finished (converged, failed or absent)
     int active;      // bit j: column j still iterating in the current inner solve
     int all_done;
@@ -717,11 +719,18 @@ __device__ void team_solve(Team& team, const BatchArgs& args, const BatchItem& i
             for (int j = 0; j < K; j++) {
                 ctl.bnorm2[j] = o[j];
                 ctl.iters[j] = 0; ctl.outer[j] = 0; ctl.status[j] = FEEC_MAXITER; ctl.relres[j] = -1.0;
-                ctl.stall[j] = 0.0;
+                ctl.stall[j] = 0.0; ctl.amp[j] = 0.0;
                 if (j >= kk) ctl.done |= 1 << j;
             }
+            ctl.err_step = 0;
         }
     }
+    // Error control (as in the single-system mixed solver): a correction approximates the
+    // error of the iterate it corrects, so its size against that iterate's residual measures
+    // the operator's error-to-residual amplification; a column stops only when also
+    // amplification x relative residual <= kErrorPerResidual x precision, and its last inner
+    // solve is sized for both bars. At most one outer step is added for the error bar alone.
+    const double err_target = kErrorPerResidual * args.precision;
 
     for (int outer = 0; outer < args.max_outer; outer++) {
         // ---- FP64 true residual r64 = b - A x and its norm ----
@@ -752,17 +761,25 @@ __device__ void team_solve(Team& team, const BatchArgs& args, const BatchItem& i
                 for (int j = 0; j < kk; j++) {
                     const double bn = sqrt(ctl.bnorm2[j]);
                     const double rn = sqrt(rn2[j]);
+                    const double rel = bn > 0.0 ? rn / bn : 0.0;
+                    const bool errs = ctl.err_step >> j & 1;
                     if (!(done >> j & 1)) {
                         int st = -1;
                         if (!(rn == rn)) st = FEEC_BREAKDOWN;
-                        else if (rn <= args.precision * bn) st = FEEC_OK;
+                        else if (rn <= args.precision * bn) {
+                            if (errs || ctl.amp[j] == 0.0 || ctl.amp[j] * rel <= err_target) st = FEEC_OK;
+                            else ctl.err_step |= 1 << j;
+                        } else if (errs) st = FEEC_MAXITER;   // the error-bar step lost the residual bar
                         else if (args.stall_check && ctl.outer[j] > 0 && rn > ctl.stall[j]) st = kStatusStagnated;
                         else if (ctl.iters[j] >= args.max_iter) st = FEEC_MAXITER;
                         if (st >= 0) { done |= 1 << j; ctl.status[j] = st; }
                     }
-                    ctl.relres[j] = bn > 0.0 ? rn / bn : 0.0;
-                    // inner target: the reduction still needed (with margin), never below eta
-                    const double need = args.inner_margin * args.precision * bn / (rn > 0.0 ? rn : 1.0);
+                    ctl.relres[j] = rel;
+                    // inner target: the reduction still needed (with margin) for the residual bar
+                    // and, once an amplification is known, the error bar; never below eta
+                    double target = args.precision * bn;
+                    if (ctl.amp[j] > 0.0 && err_target * bn / ctl.amp[j] < target) target = err_target * bn / ctl.amp[j];
+                    const double need = args.inner_margin * target / (rn > 0.0 ? rn : 1.0);
                     const double eta = need > args.inner_eta ? need : args.inner_eta;
                     const bool live = !(done >> j & 1);
                     ctl.inv[j] = live && rn > 0.0 ? (T)(1.0 / rn) : T(0);
@@ -783,21 +800,37 @@ __device__ void team_solve(Team& team, const BatchArgs& args, const BatchItem& i
             inner_eisenstat<T, K>(team, S, args, ctl, val, wd, sd, r64, r, d, z, m, q, c);
         else
             inner_cg<T, K>(team, S, args, ctl, val, r64, r, d, q, c);
-        // x += ||r|| c in FP64 (rnorm is 0 for finished columns)
+        // x += ||r|| c in FP64 (rnorm is 0 for finished columns), with the squared norms of
+        // the corrections and of the new iterates for the error control
         {
-            double rnorm[K];
+            double rnorm[K], nn[2 * K], nsum[2 * K];
             #pragma unroll
-            for (int j = 0; j < K; j++) rnorm[j] = ctl.rnorm[j];
+            for (int j = 0; j < K; j++) { rnorm[j] = ctl.rnorm[j]; nn[j] = 0.0; nn[K + j] = 0.0; }
             const int done = ctl.done;
             for (int i = team.tid(); i < n; i += team.nthreads())
                 #pragma unroll
                 for (int j = 0; j < K; j++) {
                     const long long p = (long long)i * K + j;
-                    if (!(done >> j & 1)) xp[p] += rnorm[j] * (double)c[p];
+                    if (!(done >> j & 1)) {
+                        const double cj = rnorm[j] * (double)c[p];
+                        const double xn = xp[p] + cj;
+                        xp[p] = xn;
+                        nn[j] += cj * cj;
+                        nn[K + j] += xn * xn;
+                    }
+                }
+            team.template sum<double, 2 * K>(nn, nsum);
+            if (leader)
+                for (int j = 0; j < K; j++) {
+                    if (ctl.done >> j & 1) continue;
+                    // the first step starts from x = 0 (its correction is the whole solution)
+                    if (ctl.outer[j] > 0 && nsum[K + j] > 0.0 && ctl.relres[j] > 0.0) {
+                        const double a = sqrt(nsum[j] / nsum[K + j]) / ctl.relres[j];
+                        if (a > ctl.amp[j]) ctl.amp[j] = a;
+                    }
+                    ctl.outer[j]++;
                 }
         }
-        if (leader)
-            for (int j = 0; j < K; j++) if (!(ctl.done >> j & 1)) ctl.outer[j]++;
     }
     // scatter x back to the caller's numbering and report
     team.sync();
@@ -814,6 +847,7 @@ __device__ void team_solve(Team& team, const BatchArgs& args, const BatchItem& i
             args.results[slot].iterations = ctl.iters[j];
             args.results[slot].outer = ctl.outer[j];
             args.results[slot].relres = ctl.relres[j];
+            args.results[slot].err_est = ctl.amp[j] > 0.0 ? ctl.amp[j] * ctl.relres[j] : -1.0;
         }
     }
 }

@@ -26,7 +26,7 @@ class RequestResult(ctypes.Structure):
         ("id", ctypes.c_longlong), ("n", ctypes.c_int), ("status", ctypes.c_int), ("iterations", ctypes.c_int),
         ("outer_iterations", ctypes.c_int), ("cluster_blocks", ctypes.c_int), ("fp64_fallback", ctypes.c_int),
         ("true_relres", ctypes.c_double), ("t_submit_ms", ctypes.c_double), ("t_start_ms", ctypes.c_double),
-        ("t_end_ms", ctypes.c_double),
+        ("t_end_ms", ctypes.c_double), ("error_estimate", ctypes.c_double),
     ]
 
 

@@ -1,0 +1,136 @@
+"""Mixed precision (FP32 inner solves inside FP64 defect correction) at the sizes of the
+benchmark configurations: every result must reach the requested FP64 relative residual
+1e-10 AND be within 1e-9 (relative, 2-norm) of a tight FP64 oracle solve.
+
+The tight oracle is the oracle's restatement of the reference's Rainbow SSOR-PCG
+(solver/sparsesolver.cpp:1002-1335) run on the scaled system A (s x) = s b, with s so
+large that the reference's absolute floor of 2^-26 (base/base.hpp:127-128) does not
+bind, to a relative precision of 1e-13; dividing by s gives x. Its own error is about
+1e-12 on these operators, far below the 1e-9 bar.
+
+Cases (the configurations' operators):
+* 3D P1 refined 6 times (N = 274,625), the inner sizing operator of the mixed
+  configuration: single solves on the whole GPU (Rainbow and plain CG) and a batch;
+* a sample of the 512 uneven systems of the batched configuration (2D P1/P2 refined
+  3-7 times, coefficient mass), solved together in one batched launch;
+* 2D P2 refined 7 times with coefficient mass (N = 66,049): 64 right-hand sides in
+  one blocked batch, a sample of the columns checked.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+ERR_BAR = 1e-9
+PRECISION = 1e-10
+
+
+def _tight(A, C, V, b, diag, rb):
+    from oracle import oracle
+    bn = float(np.linalg.norm(b))
+    s = max(1.0, 10.0 * 2.0 ** -26 / (1e-13 * bn))
+    oracle.set_threads(oracle.max_threads())
+    _, x, _ = oracle.cg_rainbow(A, C, V, s * np.asarray(b), diag, rb, 1.0, precision=1e-13)
+    return x / s
+
+
+def _system(dim, r, L, coef_seed=0):
+    import simplefem_gb300 as S
+    from simplefem_gb300 import workloads
+    from simplefem_gb300.system import System
+    A, C, V = workloads.lattice_matrix(dim, r, L, coef_seed)
+    n = len(A) - 1
+    mat = S.MatrixCSR(n, n, A, C, V)
+    rb = S.Rainbow(mat)
+    diag = mat.getDiagonal().raw()
+    sysm = System(A, C, V)
+    sysm.set_rainbow(diag, 1.0, rb.num_colors, rb.F, rb.B, rb.R)
+    return sysm, (A, C, V, diag, (rb.num_colors, rb.F, rb.B, rb.R))
+
+
+def _check(x, b, ops, info, what):
+    import scipy.sparse as sp
+    A, C, V, diag, rb = ops
+    n = len(A) - 1
+    M = sp.csr_matrix((V, C, A), shape=(n, n))
+    relres = np.linalg.norm(b - M @ x) / np.linalg.norm(b)
+    assert info["status"] == 0 and relres <= PRECISION, (what, info, relres)
+    xt = _tight(A, C, V, b, diag, rb)
+    err = np.linalg.norm(x - xt) / np.linalg.norm(xt)
+    assert err <= ERR_BAR, (what, err, info)
+    return err
+
+
+@pytest.mark.parametrize("method", ["rainbow", "cg"])
+def test_mixed_single_solve_3d_p1_l6_meets_error_bar(cuda, method):
+    torch = cuda
+    from simplefem_gb300 import workloads
+    sysm, ops = _system(3, 1, 6)
+    n = sysm.n
+    b = workloads.uniform_vector(77, n)
+    x = torch.zeros(n, dtype=torch.float64, device="cuda")
+    info = sysm.solve(torch.from_numpy(b).cuda(), x, method=method, mode="mixed", precision=PRECISION)
+    assert info["fp64_fallback"] == 0
+    err = _check(x.cpu().numpy(), b, ops, info, method)
+    # the solver's own estimate is reported and sits at or under its bar
+    assert 0.0 < info["error_estimate"] <= 10.0 * PRECISION, info
+    assert err <= 10.0 * max(info["error_estimate"], 1e-12), (err, info["error_estimate"])
+    sysm.close()
+
+
+def test_mixed_batch_3d_p1_l6_meets_error_bar(cuda):
+    torch = cuda
+    from simplefem_gb300 import workloads
+    sysm, ops = _system(3, 1, 6)
+    n = sysm.n
+    nrhs = 8
+    Bh = np.stack([workloads.uniform_vector(300 + j, n) for j in range(nrhs)])
+    X = torch.zeros((nrhs, n), dtype=torch.float64, device="cuda")
+    infos = sysm.solve_batch(torch.from_numpy(Bh).cuda(), X, method="rainbow", mode="mixed", precision=PRECISION)
+    Xh = X.cpu().numpy()
+    for j in (0, 5):
+        _check(Xh[j], Bh[j], ops, infos[j], ("batch column", j))
+    for j in range(nrhs):
+        assert 0.0 < infos[j]["error_estimate"] <= 10.0 * PRECISION, (j, infos[j])
+    sysm.close()
+
+
+def test_mixed_uneven_sample_meets_error_bar(cuda):
+    torch = cuda
+    from simplefem_gb300 import workloads
+    from simplefem_gb300.system import solve_many
+    specs = workloads.batched_uneven_systems(512, 4242)
+    # every refinement level and both degrees of the configuration, largest systems included
+    pick, seen = [], set()
+    for i, sp_ in enumerate(specs):
+        key = (sp_["r"], sp_["L"])
+        if key not in seen:
+            seen.add(key)
+            pick.append(i)
+    systems, opss, bs, xs, bh = [], [], [], [], []
+    for i in pick:
+        sysm, ops = _system(**specs[i])
+        b = workloads.uniform_vector(77 + i, sysm.n)
+        systems.append(sysm); opss.append(ops); bh.append(b)
+        bs.append(torch.from_numpy(b).cuda())
+        xs.append(torch.zeros(sysm.n, dtype=torch.float64, device="cuda"))
+    infos = solve_many(systems, bs, xs, method="rainbow", mode="mixed", precision=PRECISION)
+    for k, i in enumerate(pick):
+        _check(xs[k].cpu().numpy(), bh[k], opss[k], infos[k], ("uneven system", i, specs[i]))
+    for s in systems:
+        s.close()
+
+
+def test_mixed_block_64_rhs_2d_p2_l7_meets_error_bar(cuda):
+    torch = cuda
+    from simplefem_gb300 import workloads
+    sysm, ops = _system(2, 2, 7, 1)
+    n = sysm.n
+    nrhs = 64
+    Bh = np.stack([workloads.uniform_vector(4000 + j, n) for j in range(nrhs)])
+    X = torch.zeros((nrhs, n), dtype=torch.float64, device="cuda")
+    infos = sysm.solve_batch(torch.from_numpy(Bh).cuda(), X, method="rainbow", mode="mixed", precision=PRECISION)
+    Xh = X.cpu().numpy()
+    for j in (0, 31, 63):
+        _check(Xh[j], Bh[j], ops, infos[j], ("block column", j))
+    sysm.close()
