@@ -625,7 +625,7 @@ def run_ours(args):
         return
     if args.only_krylov_more:
         if rank == 0:
-            print(json.dumps({"krylov_more": run_krylov_more(not args.no_cpu, hodge=not args.skip_extras)}), flush=True)
+            print(json.dumps({"krylov_more": run_krylov_more(not args.no_cpu)}), flush=True)
         return
     if args.only_csr_algebra:
         if rank == 0:
@@ -650,6 +650,31 @@ def run_ours(args):
     sysm.set_rainbow(diag, 1.0, rb.num_colors, rb.F, rb.B, rb.R)
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)   # 256 MB > L2 (129 MB)
     stream = torch.cuda.current_stream()
+    if args.only_single:
+        # one solve at a time on the whole GPU (the persistent drop-in kernels), `--steps` solves
+        # per method after `--warmup` untimed ones; L2 flushed before each
+        out = {"workload": f"3D P2 refined {args.level}x, N={n}, nnz={nnz}"}
+        for method, mode in (("rainbow", "reference"), ("cg", "reference"), ("rainbow", "mixed"), ("cg", "fp64")):
+            ms, infos = [], []
+            for k in range(args.warmup + args.steps):
+                b = torch.from_numpy(workloads.uniform_vector(9000 + k, n)).to(dev)
+                x = torch.zeros(n, dtype=torch.float64, device=dev)
+                flush.zero_()
+                torch.cuda.synchronize()
+                e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                info = sysm.solve(b, x, method=method, mode=mode, precision=PRECISION)
+                e1.record(stream)
+                torch.cuda.synchronize()
+                if k >= args.warmup:
+                    ms.append(e0.elapsed_time(e1)); infos.append(info)
+            out[f"{method}_{mode}"] = {"ms": float(np.median(ms)), "iterations": int(np.median([i["iterations"] for i in infos])),
+                                       "device_ms": float(np.median([i["device_ms"] for i in infos])),
+                                       "grid_blocks": infos[0]["grid_blocks"], "lanes_per_row": infos[0]["lanes_per_row"]}
+        if rank == 0:
+            print(json.dumps({"single": out}), flush=True)
+        sysm.close()
+        return
     B_RHS = args.batch
     if args.rhs_per_team > 0:
         # a fixed launch configuration (profiling captures: the kernel launches are then exactly
@@ -753,11 +778,25 @@ def run_ours(args):
     # stream while the current batch solves (solve_batch releases the GIL and runs on the
     # compute stream). Every step's copies are inside the timed region; the first upload and
     # the last download are not overlapped.
-    E2E_STEPS = min(3, args.steps)
+    E2E_STEPS = args.steps                                 # the same number of batches as `value`
     hB = [torch.empty((B_RHS, n), dtype=torch.float64).pin_memory() for _ in range(2)]
     hX = [torch.empty((B_RHS, n), dtype=torch.float64).pin_memory() for _ in range(2)]
     for k in range(2):
         hB[k].copy_(torch.from_numpy(rhs_block(500 + k, B_RHS)))
+
+    # ---------------- accuracy of the last timed batch (untimed) ----------------
+    # a sample of its columns against FP64 plain CG solves on the GPU to 1e-13 true relative
+    # residual (their own error is about 1e-12 here)
+    sample = list(range(0, B_RHS, max(1, B_RHS // 8)))[:8]
+    errs = []
+    for j in sample:
+        xt = torch.zeros(n, dtype=torch.float64, device=dev)
+        sysm.solve(Bdev[j], xt, method="cg", mode="fp64", precision=1e-13)
+        errs.append(float((Xdev[j] - xt).norm() / xt.norm()))
+    accuracy = {"columns": len(sample), "rel_error_max": max(errs), "rel_error_median": float(np.median(errs)),
+                "error_estimate_max": max(i["error_estimate"] for i in infos_all[-1]),
+                "reference": "FP64 plain CG on the GPU to 1e-13 true relative residual"}
+
     Bd = [Bdev, torch.empty_like(Bdev)]
     Xd = [Xdev, torch.empty_like(Xdev)]
     copy_stream = torch.cuda.Stream()
@@ -796,6 +835,9 @@ def run_ours(args):
     e2e_total = time.perf_counter() - t0
     e2e_per = [e2e_total / E2E_STEPS] * E2E_STEPS
     e2e_value = whole_job_rate(B_RHS * len(e2e_per), world, max_over_ranks(sum(e2e_per), dev))
+    e2e = {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": 8 * n * B_RHS,
+           "d2h_bytes_per_step": 8 * n * B_RHS, "steps": E2E_STEPS, "ms_per_step": 1000.0 * e2e_total / E2E_STEPS,
+           "copies": "double-buffered on a copy stream, overlapped with the neighbouring batches' solves"}
 
     if args.only_batched:
         if rank == 0:
@@ -803,17 +845,35 @@ def run_ours(args):
                               "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
                               "config": {"workload": f"3D P2 refined {args.level}x, N={n}, nnz={nnz}",
                                          "batch": B_RHS, "rhs_per_team": K_TEAM, "autotuner": tuned},
-                              "inner_iterations": int(np.median(inner_iters)), "roofline": roofline,
-                              "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": 8 * n * B_RHS,
-                                      "d2h_bytes_per_step": 8 * n * B_RHS,
-                                      "ms_per_step": [1000.0 * t for t in e2e_per],
-                                      "copies": "double-buffered on a copy stream, overlapped with the "
-                                                "neighbouring batches' solves"},
+                              "inner_iterations": int(np.median(inner_iters)),
+                              "outer_iterations": int(np.median(outer_iters)), "accuracy": accuracy,
+                              "roofline": roofline, "e2e": e2e,
                               "gpu_launches": int(launches), "clocks": clock_info}), flush=True)
         sysm.close()
         if world > 1:
             dist.destroy_process_group()
         return
+
+    # ---------------- like for like: the same 1216 solves by the batched FP64 engine ----------------
+    tuned64 = sysm.tune_batch("rainbow", "fp64", nrhs_hint=B_RHS)
+    fp64_batch_ms = []
+    for rep in range(3):
+        Bdev.copy_(torch.from_numpy(rhs_block(args.warmup + rep, B_RHS)))
+        Xdev.zero_()
+        flush.zero_()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        infos64 = sysm.solve_batch(Bdev, Xdev, method="rainbow", mode="fp64", precision=PRECISION)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        assert all(i["status"] == 0 and 0 <= i["true_relres"] <= PRECISION for i in infos64), "FP64 batch missed"
+        if rep > 0:
+            fp64_batch_ms.append(e0.elapsed_time(e1))
+    fp64_batched = {"solves_per_s": B_RHS / (float(np.median(fp64_batch_ms)) / 1000.0),
+                    "ms_per_batch": float(np.median(fp64_batch_ms)), "config": tuned64,
+                    "iterations_median": int(np.median([i["iterations"] for i in infos64]))}
+    del Bd, Xd, hB, hX
 
     # ---------------- single-solve latency (whole GPU per solve) and the FP64 baselines ----------------
     def single(method, mode, count, seed):
@@ -840,26 +900,25 @@ def run_ours(args):
     # drop-in host-pointer call (matrix uploaded inside the call, as the reference signature implies)
     b0 = workloads.uniform_vector(6000, n)
     dropin = []
-    for step in range(2):
+    for step in range(3):
         xh = np.zeros(n); res = np.zeros(n)
         t0 = time.perf_counter()
         S.ConjugateGradientSolverCSR_Rainbow(n, xh, b0, A, C, V, res, PRECISION, -3, diag, 1.0,
                                              rb.num_colors, rb.F, rb.B, rb.R)
-        dropin.append(time.perf_counter() - t0)
+        if step > 0:
+            dropin.append(time.perf_counter() - t0)
+    dropin_K = S.last_info()["iterations"]
 
     spmv = run_spmv(dev)
-    uneven = run_batched_uneven(dev) if not args.skip_extras else None
-    block_rhs = run_block_rhs(dev) if not args.skip_extras else None
-    mixed_large = run_mixed_large(dev) if not args.skip_extras else None
-    csr_algebra = run_csr_algebra(rank == 0 and not args.no_cpu) if not args.skip_extras else None
-    krylov_more = run_krylov_more(rank == 0 and not args.no_cpu) if not args.skip_extras else None
-    small = run_small(rank == 0 and not args.no_cpu) if not args.skip_extras else None
-    serving = None
-    if not args.skip_extras:
-        serving = {"mixed_rainbow": run_serving("mixed", "rainbow", args.requests),
-                   "fp64_cg": run_serving("fp64", "cg", args.requests),
-                   "mixed_rainbow_at_5_per_s": run_serving("mixed", "rainbow", 100, rate=5.0),
-                   "fp64_cg_at_5_per_s": run_serving("fp64", "cg", 100, rate=5.0)}
+    extras = {}
+    if args.full:
+        extras = {"batched_uneven": run_batched_uneven(dev), "block_rhs_64": run_block_rhs(dev),
+                  "mixed_large": run_mixed_large(dev),
+                  "csr_algebra": run_csr_algebra(rank == 0 and not args.no_cpu),
+                  "krylov_more": run_krylov_more(rank == 0 and not args.no_cpu),
+                  "small_dropins": run_small(rank == 0 and not args.no_cpu),
+                  "serving": {"mixed_rainbow": run_serving("mixed", "rainbow", args.requests),
+                              "fp64_cg": run_serving("fp64", "cg", args.requests)}}
 
     # CPU baseline: the oracle restatement of the reference Rainbow-PCG on the host cores, one solve
     cpu = None
@@ -893,6 +952,23 @@ def run_ours(args):
         return len(ms_list) / (sum(ms_list) / 1000.0)
 
     if rank == 0:
+        rb64_ms = float(np.median(rb64))
+        cg64_ms = float(np.median(cg64))
+        dropin_ms = 1000 * float(np.median(dropin))
+        cpu_ms = 1000.0 / cpu["value"] if cpu else None
+        # the same-config comparisons, compact and last on the line
+        like = {
+            "mixed_batched_solves_per_s": value,
+            "fp64_batched_solves_per_s": fp64_batched["solves_per_s"],
+            "mixed_over_fp64_batched": value / fp64_batched["solves_per_s"],
+            "mixed_batched_over_fp64_plain_cg_single": value / (1000.0 / cg64_ms),
+            "fp64_rainbow_gpu_single_ms": rb64_ms,
+            "fp64_rainbow_dropin_host_call_ms": dropin_ms,
+            "fp64_rainbow_cpu_ms": cpu_ms,
+            "dropin_device_speedup_vs_cpu": (cpu_ms / rb64_ms) if cpu_ms else None,
+            "dropin_host_call_speedup_vs_cpu": (cpu_ms / dropin_ms) if cpu_ms else None,
+            "mixed_rel_error_max_vs_fp64": accuracy["rel_error_max"],
+        }
         line = {
             "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -911,30 +987,26 @@ def run_ours(args):
             "inner_iterations": int(np.median(inner_iters)), "outer_iterations": int(np.median(outer_iters)),
             "true_relres_max": max(i["true_relres"] for i in flat),
             "single_solve_mixed": {"solves_per_s": rate(mixed1), "ms": float(np.median(mixed1)),
-                                   "iterations": int(np.median([i["iterations"] for i in mixed1_i]))},
-            "fp64_plain_cg": {"solves_per_s": rate(cg64), "ms": float(np.median(cg64)),
+                                   "iterations": int(np.median([i["iterations"] for i in mixed1_i])),
+                                   "error_estimate": float(np.median([i["error_estimate"] for i in mixed1_i]))},
+            "fp64_batched_rainbow": fp64_batched,
+            "fp64_plain_cg": {"solves_per_s": rate(cg64), "ms": cg64_ms,
                               "iterations": int(np.median([i["iterations"] for i in cg64_i])),
                               "note": "plain FP64 CG on the whole GPU, stop at true relres 1e-10"},
-            "fp64_rainbow_reference_rule": {"solves_per_s": rate(rb64), "ms": float(np.median(rb64)),
+            "fp64_rainbow_reference_rule": {"solves_per_s": rate(rb64), "ms": rb64_ms,
                                             "iterations": int(np.median([i["iterations"] for i in rb64_i]))},
             "fp64_eisenstat_rainbow_reference_rule": {"solves_per_s": rate(eis64), "ms": float(np.median(eis64)),
                                                       "iterations": int(np.median([i["iterations"] for i in eis64_i]))},
-            "dropin_host_call_ms": 1000 * float(np.median(dropin)),
+            "dropin_host_call": {"ms": dropin_ms, "iterations": dropin_K},
             "spmv": spmv,
-            "batched_uneven": uneven,
-            "block_rhs_64": block_rhs,
-            "mixed_large": mixed_large,
-            "csr_algebra": csr_algebra,
-            "krylov_more": krylov_more,
-            "small_dropins": small,
-            "serving": serving,
+            **extras,
+            "accuracy": accuracy,
             "roofline": roofline,
             "cpu_baseline": cpu,
-            "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": 8 * n * B_RHS,
-                    "d2h_bytes_per_step": 8 * n * B_RHS, "ms_per_step": [1000.0 * t for t in e2e_per],
-                    "copies": "double-buffered on a copy stream, overlapped with the neighbouring batches' solves"},
+            "e2e": e2e,
             "gpu_launches": int(launches),
             "clocks": clock_info,
+            "like_for_like": like,
         }
         print(json.dumps(line), flush=True)
     sysm.close()
@@ -958,6 +1030,8 @@ def main():
     ap.add_argument("--only-csr-algebra", action="store_true", help="only the CSR algebra leg (product, transpose, sum)")
     ap.add_argument("--only-krylov-more", action="store_true", help="only the CR / MINRES / Hodge leg")
     ap.add_argument("--only-small", action="store_true", help="only the drop-ins on 2D P1 L6 (N = 4,225)")
+    ap.add_argument("--only-single", action="store_true",
+                    help="only single solves on the whole GPU (drop-in persistent kernels) on the headline operator")
     ap.add_argument("--only-batched", action="store_true",
                     help="only the batched headline step (no single-solve, SpMV, CPU or extra legs)")
     ap.add_argument("--rhs-per-team", type=int, default=0,
@@ -968,7 +1042,9 @@ def main():
                     help="refinement level of the 3D P2 headline operator (5 = the benchmark; smaller only for "
                          "profiling captures)")
     ap.add_argument("--requests", type=int, default=200, help="requests in the serving stream")
-    ap.add_argument("--skip-extras", action="store_true", help="skip the uneven-batch and serving legs")
+    ap.add_argument("--full", action="store_true",
+                    help="also run the side legs (uneven batch, 64-RHS block, 3D P1 L7 mixed, CSR algebra, further "
+                         "drivers, small drop-ins, serving); each has its own --only-* switch as well")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
