@@ -28,7 +28,7 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr", "-Xc
               "-I" + INCLUDE, "-I" + CSRC]
 CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-Wall", "-Wextra", "-I" + INCLUDE, "-I" + CSRC]
 
-GPU_SOURCES = ["kernels_krylov.cu", "kernels_eisenstat.cu", "kernels_setup.cu", "capi.cu", "coloring.cpp", "noalloc.cu", "kernels_batched.cu", "batched.cu", "kernels_cluster.cu", "kernels_cluster_batched.cu", "server.cu", "selftest.cu", "csr_algebra.cu", "kernels_krylov_more.cu", "hodge.cu"]
+GPU_SOURCES = ["kernels_krylov.cu", "kernels_eisenstat.cu", "kernels_setup.cu", "capi.cu", "coloring.cpp", "noalloc.cu", "kernels_batched.cu", "batched.cu", "kernels_cluster.cu", "kernels_cluster_batched.cu", "server.cu", "selftest.cu", "csr_algebra.cu", "kernels_krylov_more.cu", "hodge.cu", "kernels_small.cu"]
 
 
 def nvcc() -> str:

@@ -153,8 +153,21 @@ PcgArgs<T> make_pcg_args(feec_system* s, T* x, T* r, T* d, T* z, T* m, T* q, con
 
 int timed_launch_pcg64(feec_system* s, const PcgArgs<double>& a, LaunchShape& shape, float& ms) {
     FEEC_TRY(reset_status(s));
+    // Systems whose three gathered vectors fit one block's shared memory run in one block
+    // (2D P1 refined 6 times: the index-order SSOR sweeps are 258 dependent level phases
+    // per iteration, which one block with shared-memory vectors turns into block barriers
+    // and shared-memory round trips).
+    const bool small = s->user_blocks <= 0 && s->user_lanes <= 0 && a.n <= pcg_smem_max_rows();
     FEEC_TRY(cudaEventRecord(s->ev0, s->stream));
-    FEEC_TRY(launch_pcg<double>(a, shape, s->stream));
+    if (small) {
+        const double avg = (double)s->nnz / (double)(a.n > 0 ? a.n : 1);
+        shape.lanes = avg <= 10.0 ? 1 : avg <= 20.0 ? 2 : avg <= 40.0 ? 4 : 8;
+        shape.blocks = 1;
+        shape.threads = 256;
+        FEEC_TRY(launch_pcg_smem(a, shape.lanes, s->stream));
+    } else {
+        FEEC_TRY(launch_pcg<double>(a, shape, s->stream));
+    }
     FEEC_TRY(cudaEventRecord(s->ev1, s->stream));
     FEEC_TRY(cudaEventSynchronize(s->ev1));
     FEEC_TRY(cudaEventElapsedTime(&ms, s->ev0, s->ev1));
@@ -217,12 +230,13 @@ int solve_core(feec_system* s, int method, int mode, double* xx, const double* b
 
     LaunchShape shape;
     shape.lanes = s->lanes;
-    // Measured on GB300 (3D P2 operator, 28 entries per row): the FP64 persistent
-    // solvers issue FP64 at 2 lanes/clk/SM, so per-row reductions across lanes and
-    // per-group epilogues cost more than they save; one thread per row is fastest for
-    // plain FP64 CG and 4 lanes per row for the sweeps of the preconditioned solvers
-    // (8 for their FP32 inner solves).
-    if (cg_family && mode != FEEC_MODE_MIXED) shape.lanes = 1;
+    // Measured on GB300 (3D P2 operator, 28 entries per row, two 512-thread blocks per
+    // SM): the FP64 persistent solvers issue FP64 at 2 lanes/clk/SM, so wide per-row
+    // reductions and per-group epilogues cost more than they save; 2 lanes per row are
+    // fastest for plain FP64 CG (42.7 ms against 50.4 with 1, and 47.3 with 1 lane on one
+    // block per SM) and 4 for the sweeps of the preconditioned solvers (50.2 ms against
+    // 56.3 with 8 and 76.0 with 16; 8 for their FP32 inner solves).
+    if (cg_family && mode != FEEC_MODE_MIXED) shape.lanes = 2;
     else {
         const int cap = (mode == FEEC_MODE_MIXED && method != FEEC_METHOD_CG) ? 8 : 4;
         if (shape.lanes > cap) shape.lanes = cap;

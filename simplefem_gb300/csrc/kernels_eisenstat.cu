@@ -40,7 +40,7 @@ __device__ __forceinline__ T seg_dot_guarded(const int* __restrict__ ci, const T
             if (__ldg(&wd[c]) != T(0)) s = fma(__ldg(&v[j]), x[c], s);
         }
     } else {
-        for (int j = lo + lane; j < hi; j += LANES) s = fma(__ldg(&v[j]), x[__ldg(&ci[j])], s);
+        s = seg_accumulate<T, LANES>(ci, v, x, lo + lane, hi, s);
     }
     #pragma unroll
     for (int off = LANES / 2; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off, LANES);

@@ -77,7 +77,7 @@ __device__ __forceinline__ T seg_dot_pre(const RowRef<T, LANES>& R, const int* _
     #pragma unroll
     for (int t = 0; t < PF; t++)
         if (R.a + lane + t * LANES < R.e) s = fma(R.v[t], x[R.c[t]], s);
-    for (int j = R.a + lane + PF * LANES; j < R.e; j += LANES) s = fma(__ldg(&v[j]), x[__ldg(&ci[j])], s);
+    s = seg_accumulate<T, LANES>(ci, v, x, R.a + lane + PF * LANES, R.e, s);
     #pragma unroll
     for (int off = LANES / 2; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off, LANES);
     return s;
@@ -111,7 +111,7 @@ __device__ __forceinline__ void rows_pipelined(const PcgArgs<T>& a, int lo, int 
 // Plain CG
 // ---------------------------------------------------------------------------
 template <typename T, int LANES>
-__global__ void __launch_bounds__(kThreads) cg_persistent(CgArgs<T> a) {
+__global__ void __launch_bounds__(kThreads, 2) cg_persistent(CgArgs<T> a) {
     using AT = AccT<T>;
     using Acc = typename AT::type;
     unsigned long long epoch = 0;

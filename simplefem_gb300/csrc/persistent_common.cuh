@@ -18,11 +18,36 @@ constexpr double kMachineEpsilon = 2.220446049250313080847263336181640625e-16;  
         for (int row = _base + (int)((threadIdx.x & 31) / LANES), _once = 1; _once; _once = 0)      \
             for (bool active = row < (hi); _once; _once = 0)
 
+// Accumulates s += v[j] * x[ci[j]] for j = j0, j0 + LANES, ... < hi in that order, four
+// strides at a time: the four column indices and values are requested together, then the
+// four gathers, so a long row costs two memory round trips per four strides instead of
+// two per stride. The terms and their order are those of the one-stride loop.
+template <typename T, int LANES>
+__device__ __forceinline__ T seg_accumulate(const int* __restrict__ ci, const T* __restrict__ v, const T* x, int j0,
+                                            int hi, T s) {
+    for (int j = j0; j < hi; j += 4 * LANES) {
+        int c[4];
+        T w[4];
+        #pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const int k = j + u * LANES;
+            c[u] = k < hi ? __ldg(&ci[k]) : -1;
+            w[u] = k < hi ? __ldg(&v[k]) : T(0);
+        }
+        T g[4];
+        #pragma unroll
+        for (int u = 0; u < 4; u++) g[u] = c[u] >= 0 ? x[c[u]] : T(0);
+        #pragma unroll
+        for (int u = 0; u < 4; u++)
+            if (c[u] >= 0) s = fma(w[u], g[u], s);
+    }
+    return s;
+}
+
 template <typename T, int LANES>
 __device__ __forceinline__ T seg_dot(const int* __restrict__ ci, const T* __restrict__ v, const T* x, int lo, int hi,
                                      int lane) {
-    T s = T(0);
-    for (int j = lo + lane; j < hi; j += LANES) s = fma(__ldg(&v[j]), x[__ldg(&ci[j])], s);
+    T s = seg_accumulate<T, LANES>(ci, v, x, lo + lane, hi, T(0));
     #pragma unroll
     for (int off = LANES / 2; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off, LANES);
     return s;

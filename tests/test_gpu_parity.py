@@ -290,3 +290,28 @@ def test_system_apply_sell_matches_reference(cuda, name):
         sysm.apply(x, y, 0.7)
         assert np.max(np.abs(y.cpu().numpy() - ref)) <= 1e-13 * np.max(np.abs(ref))
     sysm.close()
+
+
+@pytest.mark.parametrize("method", ["ssor", "rainbow"])
+def test_one_block_shared_memory_solver_matches_grid_solver(cuda, method):
+    """Small systems run the reference-rule SSOR / Rainbow PCG in one block with the
+    gathered vectors in shared memory; a launch-shape override sends the same solve to
+    the grid-wide persistent kernel. Both follow the reference: same K (+-1), same x."""
+    torch = cuda
+    from simplefem_gb300 import workloads
+    sysm, (A, C, V) = _system(2, 1, 6, method)
+    n = sysm.n
+    b = torch.from_numpy(workloads.uniform_vector(31, n)).cuda()
+    xs = []
+    infos = []
+    for override in (False, True):
+        if override:
+            sysm.set_launch(16, 4)
+        x = torch.zeros(n, dtype=torch.float64, device="cuda")
+        infos.append(sysm.solve(b, x, method=method, mode="reference", precision=1e-10))
+        xs.append(x.cpu().numpy())
+    assert infos[0]["grid_blocks"] == 1 and infos[1]["grid_blocks"] == 16, infos
+    assert infos[0]["status"] == 0 and infos[1]["status"] == 0
+    assert abs(infos[0]["iterations"] - infos[1]["iterations"]) <= 1, infos
+    assert np.linalg.norm(xs[0] - xs[1]) / np.linalg.norm(xs[1]) < 1e-11
+    sysm.close()
