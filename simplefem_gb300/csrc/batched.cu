@@ -162,10 +162,13 @@ int run_batch_results(cudaStream_t st, const std::vector<feec_system*>& systems,
     BatchArgs a{};
     a.systems = dviews; a.items = ditems; a.nitems = (int)items.size(); a.next_item = dnext; a.results = dres;
     a.precision = precision;
-    a.inner_eta = is_float ? 2e-5 : 1e-30;
+    // reliable-update factor (FP32: replace the residual whenever z.r has fallen by its
+    // square; FP64: only when the target is reached); the autotuner's trials (max_outer > 0)
+    // run a fixed iteration count without replacements
+    a.inner_eta = (is_float && max_outer <= 0) ? kReliableDelta : 1e-30;
     a.inner_margin = is_float ? 0.3 : 1.0;   // FP64 recursion tracks the true residual closely
     a.max_iter = max_iter;
-    a.max_outer = max_outer > 0 ? max_outer : (is_float ? 12 : 4);
+    a.max_outer = max_outer > 0 ? max_outer : kMaxReplacements;
     a.stall_check = (is_float && stall_check) ? 1 : 0;
     cudaEvent_t e0, e1;
     FEEC_TRY(cudaEventCreate(&e0));
@@ -607,10 +610,10 @@ int feec_batch_create(feec_batch** out, int nsys, feec_system* const* systems, i
     BatchArgs a{};
     a.systems = dviews; a.items = ditems; a.nitems = nsys; a.next_item = dnext; a.results = bt->dres;
     a.precision = precision;
-    a.inner_eta = is_float ? 2e-5 : 1e-30;
+    a.inner_eta = is_float ? kReliableDelta : 1e-30;
     a.inner_margin = is_float ? 0.3 : 1.0;
     a.max_iter = max_iter > 0 ? max_iter : maxn;
-    a.max_outer = is_float ? 12 : 4;
+    a.max_outer = kMaxReplacements;
     a.stall_check = is_float;
     bt->method = method; bt->mode = mode; bt->max_iter = a.max_iter;
     bt->systems = sys;

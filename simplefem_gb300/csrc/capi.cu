@@ -380,24 +380,32 @@ int solve_core(feec_system* s, int method, int mode, double* xx, const double* b
         st = run_fp64(mode);
         if (st != FEEC_OK) return st;
     } else {
-        // MIXED: FP64 defect correction around an FP32 inner solve (compensated FP32 dots).
+        // MIXED: FP32 inner iterations (compensated FP32 dots) with reliable updates around
+        // them: the FP64 solution and true residual are kept beside the FP32 recursion, and a
+        // segment ends when z.r (r.r for CG) has fallen by kReliableDelta^2 or far enough for
+        // the target; the correction then goes into x in FP64, the FP64 true residual
+        // replaces the recursive one (scaled to unit norm), and the next segment keeps the
+        // search direction (rescaled, beta against the previous rho) instead of restarting
+        // the Krylov recurrence as plain defect correction does.
         if (method == FEEC_METHOD_CG && !s->V32) return FEEC_BADARG;
         if (method != FEEC_METHOD_CG && !s->val32) return FEEC_BADARG;
-        const double inner_eta = 2e-5;   // relative reduction asked of one inner solve
-        const int max_outer = 12;
+        const int max_outer = kMaxReplacements;
+        const double delta2 = kReliableDelta * kReliableDelta;
         double rn2 = 0.0;
-        double stall_limit = 0.0;        // residual norm above which the last outer step stagnated
+        double stall_limit = 0.0;        // residual norm above which the last segment stagnated
         bool stagnated = false;
         // Error control. A small residual does not make a small error: what the FP32 inner
-        // solves leave behind is mostly smooth, low-eigenvalue error, which A shrinks the most.
-        // Each outer step measures how large its correction was against the residual it
-        // corrected (the correction c_k approximates the error of x_k), which gives the
-        // error-to-residual amplification of this operator; the solve then also asks
-        // amplification x relative residual <= err_target before it stops, and sizes its last
-        // inner solve for both bars. At most one step is added for the error bar alone.
+        // iterations leave behind is mostly smooth, low-eigenvalue error, which A shrinks the
+        // most. Each segment measures how large its correction was against the residual it
+        // corrected (the correction approximates the error of the iterate it corrected),
+        // which gives the error-to-residual amplification of this operator; the solve then
+        // also asks amplification x relative residual <= err_target before it stops, and
+        // sizes each segment's target for both bars.
         const double err_target = kErrorPerResidual * precision;
-        double amp = 0.0;                // largest measured amplification (steps after the first)
-        bool err_step = false;           // the last step was taken for the error bar alone
+        double amp = 0.0;                // largest measured amplification (segments after the first)
+        bool err_step = false;           // the residual bar is met, the error bar not yet
+        bool have_dir = false;           // a search direction to keep from the last segment
+        double zr_prev = 0.0, rn_prev = 0.0;
         for (outer = 0; outer < max_outer; outer++) {
             st = true_residual(s, s->b, s->x, s->r, rn2, permuted);
             if (st != FEEC_OK) return st;
@@ -406,34 +414,42 @@ int solve_core(feec_system* s, int method, int mode, double* xx, const double* b
             if (!(rn == rn)) { status = FEEC_BREAKDOWN; break; }
             const double relres = bnorm > 0.0 ? rn / bnorm : 0.0;
             if (rn <= tolerance) {
-                if (err_step || amp == 0.0 || amp * relres <= err_target) { status = FEEC_OK; break; }
+                // stop at the error bar, or when the residual no longer falls (the FP64
+                // residual's own rounding floor) after the bar was first missed
+                const bool floor = err_step && rn > 0.3 * rn_prev;
+                if (amp == 0.0 || amp * relres <= err_target || floor || K_total >= max_iter) {
+                    status = FEEC_OK;
+                    break;
+                }
                 err_step = true;
-            } else if (err_step) {
-                break;   // the error-bar step lost the residual bar: leave it to the final check
             }
-            // An inner solve that gained less than half the digits it was asked for means the
-            // operator is too ill-conditioned for FP32 arithmetic (condition number times the
-            // FP32 unit roundoff near 1e-2 or above): finish in FP64 from the current iterate,
-            // with a fresh budget of max_iter iterations.
-            if (outer > 0 && !err_step && rn > stall_limit) { stagnated = true; break; }
+            // A segment whose true residual gained less than half the digits its recursion
+            // promised means the operator is too ill-conditioned for FP32 arithmetic
+            // (condition number times the FP32 unit roundoff near 1e-2 or above): finish in
+            // FP64 from the current iterate, with a fresh budget of max_iter iterations.
+            if (outer > 0 && rn > stall_limit && rn > tolerance) { stagnated = true; break; }
             if (K_total >= max_iter) { status = FEEC_MAXITER; break; }
+            const double scale = (have_dir && rn > 0.0) ? rn_prev / rn : 1.0;
             const double inv = 1.0 / rn;
             const double scal_h[2] = {inv, rn};
             FEEC_TRY(cudaMemcpyAsync(s->scal + 2, scal_h, sizeof(scal_h), cudaMemcpyHostToDevice, s->stream));
             FEEC_TRY(launch_scaled_cast(n, s->r, s->scal + 2, s->b32, s->stream));
             FEEC_TRY(cudaMemsetAsync(s->x32, 0, sizeof(float) * n, s->stream));
-            FEEC_TRY(cudaMemsetAsync(s->d32, 0, sizeof(float) * n, s->stream));
-            FEEC_TRY(cudaMemsetAsync(s->z32, 0, sizeof(float) * n, s->stream));
-            FEEC_TRY(cudaMemsetAsync(s->m32, 0, sizeof(float) * n, s->stream));
-            FEEC_TRY(cudaMemsetAsync(s->q32, 0, sizeof(float) * n, s->stream));
-            FEEC_TRY(cudaMemsetAsync(s->r32, 0, sizeof(float) * n, s->stream));
-            // do not over-solve the last step: ask only for the reduction still needed (with
-            // margin) to meet the residual bar and, once an amplification is known, the error bar
+            if (!have_dir) {
+                FEEC_TRY(cudaMemsetAsync(s->d32, 0, sizeof(float) * n, s->stream));
+                FEEC_TRY(cudaMemsetAsync(s->z32, 0, sizeof(float) * n, s->stream));
+                FEEC_TRY(cudaMemsetAsync(s->m32, 0, sizeof(float) * n, s->stream));
+                FEEC_TRY(cudaMemsetAsync(s->q32, 0, sizeof(float) * n, s->stream));
+                FEEC_TRY(cudaMemsetAsync(s->r32, 0, sizeof(float) * n, s->stream));
+            }
+            // the segment's target: the residual bar and, once an amplification is known, the
+            // error bar (with margin), or a fall of kReliableDelta, whichever comes first
+            // (the larger of the two factors)
             double target = tolerance;
             if (amp > 0.0) target = std::min(target, err_target * bnorm / amp);
             const double need = 0.3 * target / rn;
-            const double eta = std::max(inner_eta, need);
-            stall_limit = rn * std::sqrt(eta);
+            const double f = std::max(delta2, need * need);
+            stall_limit = rn * std::sqrt(std::sqrt(f));
             float ms = 0.0f;
             FEEC_TRY(reset_status(s));
             FEEC_TRY(cudaEventRecord(s->ev0, s->stream));
@@ -441,15 +457,15 @@ int solve_core(feec_system* s, int method, int mode, double* xx, const double* b
                 CgArgs<float> a{};
                 a.n = n; a.rp = s->A; a.ci = s->C; a.val = s->V32; a.b = s->b32; a.x = s->x32; a.r = s->r32;
                 a.d = s->d32; a.q = s->q32;
-                a.tol2 = eta * eta;
+                a.tol2 = f;                       // r starts at unit norm: a relative fall of f in r.r
                 a.max_iter = max_iter - K_total;
                 a.partials = s->partials; a.st = s->st;
+                a.keep_dir = have_dir ? 1 : 0; a.zr_prev = zr_prev; a.scale = scale;
                 FEEC_TRY(launch_cg<float>(a, shape, s->stream));
             } else {
                 // The inner multicolor / index-order SSOR-PCG runs in Eisenstat's formulation:
                 // the same preconditioned iterates, but an iteration is one backward and one
-                // forward sweep over the strict parts, with no SpMV over full rows. It stops
-                // when z.r has fallen by eta^2; the FP64 outer loop checks the true residual.
+                // forward sweep over the strict parts, with no SpMV over full rows.
                 if (!s->w32) {
                     HomeStreamScope home(s);
                     FEEC_TRY(s->work.alloc(s->w32, (size_t)n));
@@ -459,8 +475,9 @@ int solve_core(feec_system* s, int method, int mode, double* xx, const double* b
                 a.dg = s->diag32; a.w = s->w32;
                 a.guard_restart = a.guard_iter = s->zero_diag_rows > 0;
                 a.use_zr_rule = 0;
-                a.rr_stop = eta * eta;
+                a.rr_stop = f;
                 a.max_iter = max_iter - K_total;
+                a.keep_dir = have_dir ? 1 : 0; a.zr_prev = zr_prev; a.scale = scale;
                 FEEC_TRY(launch_eisenstat<float>(a, shape, s->stream));
             }
             FEEC_TRY(cudaEventRecord(s->ev1, s->stream));
@@ -470,16 +487,20 @@ int solve_core(feec_system* s, int method, int mode, double* xx, const double* b
             FEEC_TRY(cudaEventSynchronize(s->ev1));
             FEEC_TRY(cudaEventElapsedTime(&ms, s->ev0, s->ev1));
             FEEC_TRY(cudaStreamSynchronize(s->stream));
-            // the first step starts from x = 0 (its correction is the whole solution); later
-            // corrections measure the error of the iterate they corrected
-            if (outer > 0 && norms2[1] > 0.0 && relres > 0.0)
-                amp = std::max(amp, std::sqrt(norms2[0] / norms2[1]) / relres);
             ms_total += ms;
             st = read_status(s, hs);
             if (st != FEEC_OK) return st;
             K_total += hs.iterations;
+            // the first segment starts from the initial guess (its correction is the
+            // solution); a later one measures the error of the iterate it corrected
+            if (outer > 0 && norms2[1] > 0.0 && relres > 0.0)
+                amp = std::max(amp, std::sqrt(norms2[0] / norms2[1]) / relres);
             if (hs.status == FEEC_TIMEOUT) { status = FEEC_TIMEOUT; break; }
             if (hs.status == FEEC_BREAKDOWN && hs.iterations == 0) { status = FEEC_BREAKDOWN; break; }
+            // a breakdown or an empty segment restarts the direction next time
+            have_dir = hs.status == FEEC_OK && hs.iterations > 0;
+            zr_prev = hs.extra[0];
+            rn_prev = rn;
         }
         if (outer == max_outer) status = FEEC_MAXITER;
         if (stagnated) {

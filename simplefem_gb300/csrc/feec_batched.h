@@ -43,6 +43,12 @@ struct BatchResult {
     double err_est;           // mixed: estimated relative error of x (-1: not estimated)
 };
 
+// Reliable updates of the mixed-precision team solver: the FP32 recursion's residual is
+// replaced by the FP64 true residual whenever its preconditioned norm has fallen by this
+// factor since the last replacement; a column gets at most kMaxReplacements replacements.
+constexpr double kReliableDelta = 0.05;
+constexpr int kMaxReplacements = 64;
+
 struct BatchArgs {
     const SellView* systems;
     const BatchItem* items;
@@ -50,10 +56,10 @@ struct BatchArgs {
     int* next_item;           // work queue head (zeroed before the launch)
     BatchResult* results;
     double precision;         // stop when ||b - A x|| <= precision ||b|| (FP64)
-    double inner_eta;         // relative reduction asked of one inner solve
-    double inner_margin;      // the last inner solve aims at margin * (reduction still needed)
-    int max_iter;             // inner iterations per column, summed over outer steps
-    int max_outer;
+    double inner_eta;         // reliable-update factor (kReliableDelta; 1e-30: replace only at the target)
+    double inner_margin;      // a segment aims at margin * (the residual target)
+    int max_iter;             // inner iterations per column, summed over all segments
+    int max_outer;            // residual replacements per column
     int stall_check;          // 1: stop a column whose last inner solve gained less than half
                               // the digits asked (status kStatusStagnated; the host finishes it in FP64)
 };

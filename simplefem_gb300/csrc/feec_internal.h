@@ -38,6 +38,12 @@ struct CgArgs {
     // null: z = precon * r, rows with precon == 0 are skipped, the stop test is on z.r
     const T* precon;
     T* z;
+    // reliable updates of the mixed-precision solver: keep_dir = 1 keeps the search
+    // direction d of the previous segment, forming d = r + beta d with beta =
+    // r.r / (zr_prev * scale) after the restart (scale = old over new residual scale);
+    // the kernel leaves its last rho_prev in st->extra[0]
+    int keep_dir;
+    double zr_prev, scale;
 };
 
 template <typename T>
@@ -64,6 +70,11 @@ struct PcgArgs {
     T* w;                // the sweeps' combined vector (auxiliary + technical)
     int guard_restart;   // skip entries whose column has D == 0 in the restart sweeps
     int guard_iter;      // ... and in the iteration sweeps (index-order variant)
+    // reliable updates (Eisenstat kernel, mixed precision): keep_dir = 1 keeps the direction d
+    // of the previous segment (d = z + beta d with beta = z.r / (zr_prev * scale) after the
+    // restart); the kernel leaves its last rho_prev in st->extra[0]
+    int keep_dir;
+    double zr_prev, scale;
 };
 
 struct LaunchShape {

@@ -86,13 +86,14 @@ __global__ void __launch_bounds__(kThreads, 2) eisenstat_persistent(PcgArgs<T> a
         }
         if (!grid_barrier(a.st, epoch, 31)) return;
     }
+    const bool keep = a.keep_dir != 0;
     Acc azr = AT::zero();
     for (int i = tid; i < n; i += nthr) {
         if (__ldg(&a.wd[i]) == T(0)) continue;
         const T ri = a.r[i];
         const T zi = ri * __ldg(&a.sd[i]);
         a.z[i] = zi;
-        a.d[i] = zi;
+        if (!keep) a.d[i] = zi;
         azr = AT::add(azr, zi * ri);
     }
     write_partials<T>(p_zr, azr);
@@ -101,10 +102,13 @@ __global__ void __launch_bounds__(kThreads, 2) eisenstat_persistent(PcgArgs<T> a
     grid_sum<1>(p_zr, one);
     double z_r = one[0];
     const double z_r0 = z_r;
+    double z_r_prev = z_r;
 
     int K = 0;
     int status = FEEC_MAXITER;
-    T beta = T(0);
+    // a kept direction (reliable update) continues the recurrence: the first backward sweep
+    // forms d = z + beta d with beta against the previous segment's rho, rescaled
+    T beta = keep ? (T)(z_r / (a.zr_prev * a.scale)) : T(0);
     while (K < a.max_iter) {
         if (threadIdx.x == 0) {
             if (a.print_modulo > 0 && K % a.print_modulo == 0 && blockIdx.x == 0)
@@ -127,7 +131,7 @@ __global__ void __launch_bounds__(kThreads, 2) eisenstat_persistent(PcgArgs<T> a
                     const T w = __ldg(&a.wd[i]);
                     if (w != T(0)) {
                         T dv = a.d[i];
-                        if (K > 0) { dv = a.z[i] + beta * dv; a.d[i] = dv; }                // :990-997
+                        if (K > 0 || keep) { dv = a.z[i] + beta * dv; a.d[i] = dv; }        // :990-997
                         a.m[i] = (dv - s) * w;
                     }
                 }
@@ -188,10 +192,12 @@ __global__ void __launch_bounds__(kThreads, 2) eisenstat_persistent(PcgArgs<T> a
         if (threadIdx.x == 0) s_scal[1] = one[0] / z_r;
         __syncthreads();
         beta = (T)s_scal[1];
+        z_r_prev = z_r;
         z_r = one[0];
         K++;
     }
     finish(a.st, status, K, z_r, 0.0);
+    if (blockIdx.x == 0 && threadIdx.x == 0) a.st->extra[0] = z_r_prev;
 }
 
 template <typename T>

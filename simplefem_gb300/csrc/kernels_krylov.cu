@@ -144,7 +144,7 @@ __global__ void __launch_bounds__(kThreads, 2) cg_persistent(CgArgs<T> a) {
             } else {
                 const T ri = __ldg(&a.b[i]) - s;
                 a.r[i] = ri;
-                a.d[i] = ri;
+                if (!a.keep_dir) a.d[i] = ri;
                 acc = AT::add(acc, ri * ri);
             }
         }
@@ -154,6 +154,14 @@ __global__ void __launch_bounds__(kThreads, 2) cg_persistent(CgArgs<T> a) {
     double rr[1];
     grid_sum<1>(p_rr, rr);
     double r_r = rr[0];
+    double r_r_prev = r_r;
+    if (a.keep_dir && !pc) {
+        // reliable update: the previous segment's direction continues the recurrence,
+        // d = r + beta d with beta against its rho, rescaled to the new residual scale
+        const T beta0 = (T)(r_r / (a.zr_prev * a.scale));
+        for (int i = tid; i < n; i += nthr) a.d[i] = a.r[i] + beta0 * a.d[i];
+        if (!grid_barrier(a.st, epoch, 5)) return;
+    }
 
     // Scalar control (stop tests, alpha, beta) is evaluated by thread 0 only and
     // broadcast through shared memory: FP64 issues at 2 lanes/clk/SM on this part,
@@ -223,6 +231,7 @@ __global__ void __launch_bounds__(kThreads, 2) cg_persistent(CgArgs<T> a) {
         if (threadIdx.x == 0) s_scal[1] = r_r_new / r_r;                               // :175-183
         __syncthreads();
         const T beta = (T)s_scal[1];
+        r_r_prev = r_r;
         r_r = r_r_new;
         if (pc) {
             for (int i = tid; i < n; i += nthr)
@@ -234,6 +243,7 @@ __global__ void __launch_bounds__(kThreads, 2) cg_persistent(CgArgs<T> a) {
         K++;
     }
     finish(a.st, status, K, r_r, d_Ad);
+    if (blockIdx.x == 0 && threadIdx.x == 0) a.st->extra[0] = r_r_prev;
 }
 
 // ---------------------------------------------------------------------------

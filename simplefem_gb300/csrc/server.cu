@@ -172,10 +172,10 @@ int serve_one(feec_server* srv, const Request& rq, cudaStream_t stream, feec_req
     BatchArgs a{};
     a.systems = dview; a.items = ditem; a.nitems = 1; a.next_item = nullptr; a.results = dres;
     a.precision = rq.precision;
-    a.inner_eta = is_float ? 2e-5 : 1e-30;
+    a.inner_eta = is_float ? kReliableDelta : 1e-30;
     a.inner_margin = is_float ? 0.3 : 1.0;
     a.max_iter = rq.n;
-    a.max_outer = is_float ? 12 : 4;
+    a.max_outer = kMaxReplacements;
     a.stall_check = is_float;
     // cluster size from the work per iteration: about 0.25 M stored entries per block
     const long long nnz = view.nslices > 0 ? s->nnz : 0;
@@ -205,7 +205,7 @@ int serve_one(feec_server* srv, const Request& rq, cudaStream_t stream, feec_req
         a.inner_eta = 1e-30;
         a.inner_margin = 1.0;
         a.max_iter = rq.n;
-        a.max_outer = 4;
+        a.max_outer = kMaxReplacements;
         a.stall_check = 0;
         int b64 = std::min(blocks, cluster_max_blocks(0, rainbow));
         int q2 = 1;

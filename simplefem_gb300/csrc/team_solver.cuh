@@ -344,165 +344,169 @@ __device__ __forceinline__ void for_slices_dot(const Team& team, const SellView&
 // the bookkeeping out of registers leaves them to the slice loops.
 template <typename T, int K>
 struct TeamControl {
-    double bnorm2[K], relres[K], stall[K], rnorm[K], eta2[K], zr[K], rr[K], rr0[K];
-    double amp[K];   // largest measured error-to-residual amplification of column j (0: none yet)
+    double bnorm2[K], relres[K], stall[K], rnorm[K], zr[K];
+    double zr_prev[K];   // rho of the previous iteration: the denominator of the last beta
+    double thr[K];       // the column asks for a residual replacement once zr < thr
+    double amp[K];       // largest measured error-to-residual amplification of column j (0: none yet)
+    double scale[K];     // rnorm of the previous segment over rnorm of this one (direction rescaling)
     int iters[K], outer[K], status[K];
     T alpha[K], beta[K], inv[K];
-    int err_step;    // bit j: column j's last outer step was taken for the error bar alone
+    int err_step;    // bit j: column j met the residual bar but not yet the error bar
+    int fresh;       // bit j: column j starts a new direction (first segment or after a breakdown)
+    int broke;       // bit j: column j's last iteration broke down (its direction restarts)
     int done;        // bit j: column j finished (converged, failed or absent)
-    int active;      // bit j: column j still iterating in the current inner solve
+    int active;      // bit j: column j iterates in this segment
+    int trig;        // bit j: column j asked for the residual replacement that ends the segment
     int all_done;
 };
 
-// Leader's stop test of the inner solve for the columns in `mask`: the monitored
-// quantity has fallen below eta^2 times its start value, or the iteration budget is used.
-template <typename T, int K>
-__device__ __forceinline__ int inner_active(const TeamControl<T, K>& ctl, int mask, int max_iter) {
-    int act = 0;
-    for (int j = 0; j < K; j++)
-        if ((mask >> j & 1) && !(ctl.rr[j] < ctl.eta2[j] * ctl.rr0[j]) && ctl.iters[j] < max_iter) act |= 1 << j;
-    return act;
+// ---------------------------------------------------------------------------
+// Mixed precision with reliable updates (residual replacement). The inner iteration runs
+// in T (FP32 in mixed precision) on the residual equation scaled to unit norm; the FP64
+// solution x and the FP64 true residual r64 = b - A x are kept beside it. A segment ends
+// when a column's preconditioned residual measure z.r has fallen by delta^2 since the
+// segment began (or far enough to meet its target): then the segment's correction is
+// added to x in FP64 (x += ||r64|| c), the true residual is recomputed in FP64, scaled to
+// unit norm and put in place of the recursive one — but the search direction is kept,
+// rescaled to the new scale, and beta is taken against the previous iteration's rho, so
+// the Krylov recurrence carries on instead of restarting (a restart per outer step, as
+// in plain defect correction, cost about half again as many iterations). The FP32
+// recursion cannot drift far from the true residual between replacements, and the
+// answer's accuracy is that of the FP64 residual.
+// ---------------------------------------------------------------------------
+
+// Plain CG (ConjugateGradientSolverCSR, solver/sparsesolver.cpp:26-201) on the scaled
+// residual equation: the transform is r = r64 / ||r64|| (z = r); a fresh column starts
+// from d = 0, so its first d = r + beta d is r.
+template <typename T, int K, typename Team>
+__device__ void cg_transform(Team& team, const SellView& S, TeamControl<T, K>& ctl, const double* r64, T* r, T* d,
+                             T* c, double (&zr)[K]) {
+    using AT = AccT<T>;
+    using Acc = typename AT::type;
+    const int n = S.n;
+    Acc arr[K];
+    #pragma unroll
+    for (int j = 0; j < K; j++) arr[j] = AT::zero();
+    T inv[K];
+    #pragma unroll
+    for (int j = 0; j < K; j++) inv[j] = ctl.inv[j];
+    const int fresh = ctl.fresh;
+    for (int i = team.tid(); i < n; i += team.nthreads()) {
+        #pragma unroll
+        for (int j = 0; j < K; j++) {
+            const long long p = (long long)i * K + j;
+            const T rv = (T)(r64[p] * (double)inv[j]);
+            r[p] = rv; c[p] = T(0);
+            if (fresh >> j & 1) d[p] = T(0);
+            arr[j] = AT::add(arr[j], rv * rv);
+        }
+    }
+    team.template sum<T, K>(arr, zr);
 }
 
-// Plain CG inner solve (ConjugateGradientSolverCSR, solver/sparsesolver.cpp:26-201), K columns
-// in lockstep: q = A d, then x/r updates, then d = r + beta d. Stops on the recursive r.r.
+// One CG iteration for the active columns: d = r + beta d, q = A d, alpha = r.r / d.q,
+// c += alpha d, r -= alpha q; the new r.r comes back in rr.
 template <typename T, int K, typename Team>
-__device__ void inner_cg(Team& team, const SellView& S, const BatchArgs& args, TeamControl<T, K>& ctl, const T* val,
-                         const double* r64, T* r, T* d, T* q, T* c) {
+__device__ void cg_iterate(Team& team, const SellView& S, TeamControl<T, K>& ctl, const T* val, T* r, T* d, T* q,
+                           T* c, double (&rr)[K]) {
     using AT = AccT<T>;
     using Acc = typename AT::type;
     const int n = S.n;
     const int lane = threadIdx.x & 31;
     const bool leader = threadIdx.x == 0;
-    Acc arr[K];
-    #pragma unroll
-    for (int j = 0; j < K; j++) arr[j] = AT::zero();
     {
-        T inv[K];
+        T beta[K];
         #pragma unroll
-        for (int j = 0; j < K; j++) inv[j] = ctl.inv[j];
+        for (int j = 0; j < K; j++) beta[j] = ctl.beta[j];
         for (int i = team.tid(); i < n; i += team.nthreads()) {
+            T rv[K], dv[K];
+            load_k_stream<T, K>(r + (long long)i * K, rv);
+            load_k_stream<T, K>(d + (long long)i * K, dv);
             #pragma unroll
-            for (int j = 0; j < K; j++) {
-                const long long p = (long long)i * K + j;
-                const T rv = (T)(r64[p] * (double)inv[j]);
-                r[p] = rv; c[p] = T(0); d[p] = rv;
-                arr[j] = AT::add(arr[j], rv * rv);
-            }
+            for (int j = 0; j < K; j++) dv[j] = rv[j] + beta[j] * dv[j];
+            store_row<T, K>(d, i, dv);
         }
     }
+    team.sync();
+    Acc adq[K];
+    #pragma unroll
+    for (int j = 0; j < K; j++) adq[j] = AT::zero();
+    for_slices_dot<T, T, K, kBlockFull>(team, S, 0, S.nslices, val, d,
+        [&](const SliceMeta& M) {
+            RowState<T, K> p;
+            p.row = M.row0 + lane; p.act = lane < M.nrow;
+            load_row<T, K>(d, p.row, p.act, p.a);
+            return p;
+        },
+        [&](const SliceMeta&, const RowState<T, K>& p, const T (&sum)[K]) {
+            if (p.act) {
+                #pragma unroll
+                for (int j = 0; j < K; j++) adq[j] = AT::add(adq[j], p.a[j] * sum[j]);
+                store_row<T, K>(q, p.row, sum);
+            }
+        });
     {
-        double o[K];
-        team.template sum<T, K>(arr, o);
+        double dq[K];
+        team.template sum<T, K>(adq, dq);
         if (leader) {
-            for (int j = 0; j < K; j++) { ctl.zr[j] = o[j]; ctl.rr[j] = o[j]; ctl.rr0[j] = 1.0; }
-            ctl.active = inner_active<T, K>(ctl, ~ctl.done, args.max_iter);
+            int act = ctl.active;
+            for (int j = 0; j < K; j++) {
+                T a = T(0);
+                if (act >> j & 1) {
+                    const double zr = ctl.zr[j];
+                    if (!(dq[j] > 0.0) || !(zr >= 0.0) || !isfinite(dq[j]) || !isfinite(zr)) {
+                        act &= ~(1 << j);
+                        ctl.broke |= 1 << j;
+                    } else {
+                        a = (T)(zr / dq[j]);
+                    }
+                }
+                ctl.alpha[j] = a;
+            }
+            ctl.active = act;
         }
     }
     __syncthreads();
-    while (ctl.active) {
-        Acc adq[K];
+    Acc arr[K];
+    T alpha[K];
+    #pragma unroll
+    for (int j = 0; j < K; j++) { alpha[j] = ctl.alpha[j]; arr[j] = AT::zero(); }
+    for (int i = team.tid(); i < n; i += team.nthreads())
         #pragma unroll
-        for (int j = 0; j < K; j++) adq[j] = AT::zero();
-        for_slices_dot<T, T, K, kBlockFull>(team, S, 0, S.nslices, val, d,
-            [&](const SliceMeta& M) {
-                RowState<T, K> p;
-                p.row = M.row0 + lane; p.act = lane < M.nrow;
-                load_row<T, K>(d, p.row, p.act, p.a);
-                return p;
-            },
-            [&](const SliceMeta&, const RowState<T, K>& p, const T (&sum)[K]) {
-                if (p.act) {
-                    #pragma unroll
-                    for (int j = 0; j < K; j++) adq[j] = AT::add(adq[j], p.a[j] * sum[j]);
-                    store_row<T, K>(q, p.row, sum);
-                }
-            });
-        {
-            double dq[K];
-            team.template sum<T, K>(adq, dq);
-            if (leader) {
-                int act = ctl.active;
-                for (int j = 0; j < K; j++) {
-                    T a = T(0);
-                    if (act >> j & 1) {
-                        const double zr = ctl.zr[j];
-                        if (!(dq[j] > 0.0) || !(zr >= 0.0) || !isfinite(dq[j]) || !isfinite(zr)) act &= ~(1 << j);
-                        else a = (T)(zr / dq[j]);
-                    }
-                    ctl.alpha[j] = a;
-                }
-                ctl.active = act;
-            }
+        for (int j = 0; j < K; j++) {
+            const long long p = (long long)i * K + j;
+            c[p] += alpha[j] * d[p];
+            const T rv = r[p] - alpha[j] * q[p];
+            r[p] = rv;
+            arr[j] = AT::add(arr[j], rv * rv);
         }
-        __syncthreads();
-        T alpha[K];
-        #pragma unroll
-        for (int j = 0; j < K; j++) { alpha[j] = ctl.alpha[j]; arr[j] = AT::zero(); }
-        for (int i = team.tid(); i < n; i += team.nthreads())
-            #pragma unroll
-            for (int j = 0; j < K; j++) {
-                const long long p = (long long)i * K + j;
-                c[p] += alpha[j] * d[p];
-                const T rv = r[p] - alpha[j] * q[p];
-                r[p] = rv;
-                arr[j] = AT::add(arr[j], rv * rv);
-            }
-        {
-            double o[K];
-            team.template sum<T, K>(arr, o);
-            if (leader) {
-                const int was = ctl.active;
-                for (int j = 0; j < K; j++) {
-                    T b = T(0);
-                    if (was >> j & 1) {
-                        b = (T)(o[j] / ctl.zr[j]);
-                        ctl.zr[j] = o[j]; ctl.rr[j] = o[j];
-                        ctl.iters[j]++;
-                    }
-                    ctl.beta[j] = b;
-                }
-                ctl.active = inner_active<T, K>(ctl, was, args.max_iter);
-            }
-        }
-        __syncthreads();
-        {
-            T beta[K];
-            #pragma unroll
-            for (int j = 0; j < K; j++) beta[j] = ctl.beta[j];
-            for (int i = team.tid(); i < n; i += team.nthreads()) {
-                T rv[K], dv[K];
-                load_k_stream<T, K>(r + (long long)i * K, rv);
-                load_k_stream<T, K>(d + (long long)i * K, dv);
-                #pragma unroll
-                for (int j = 0; j < K; j++) dv[j] = rv[j] + beta[j] * dv[j];
-                store_row<T, K>(d, i, dv);
-            }
-        }
-        team.sync();
-    }
+    team.template sum<T, K>(arr, rr);
 }
 
-// Multicolor SSOR-PCG inner solve in Eisenstat's formulation
+// Multicolor SSOR-PCG in Eisenstat's formulation
 // (ConjugateGradientSolverCSR_Eisenstat_Rainbow, solver/sparsesolver.cpp:1338-1645): the
 // same preconditioned iterates as the Rainbow solver (:1002-1335) in exact arithmetic, but
 // an iteration is one backward and one forward sweep over the strict parts — no SpMV
 // over full rows — so each stored entry is read and gathered once per iteration instead
 // of twice. Vectors (interleaved [row][K]): r = L-solved residual, d = direction,
 // z = S r, m = technical (backward sweep), q = auxiliary (forward sweep), c = solution.
-// With sd = D (2 - w) / w, the reference's (2/w - 1) D equals sd. The previous
-// iteration's d = z + beta d runs inside the backward sweep (a row's d is read only by
-// the row itself). Stops on z.r relative to its start value.
+// With sd = D (2 - w) / w, the reference's (2/w - 1) D equals sd. A direction update
+// d = z + beta d runs inside the backward sweep (a row's d is read only by the row itself).
+
+// The transform of a (new) residual: auxiliary = r64 / ||r64||, r = L-solve of it,
+// z = S r, c = 0; a fresh column also starts its direction, d = z. `init` (the first
+// segment): every work vector starts at 0, so rows the sweeps skip (D == 0) hold 0
+// wherever a gather reads them.
 template <typename T, int K, typename Team>
-__device__ void inner_eisenstat(Team& team, const SellView& S, const BatchArgs& args, TeamControl<T, K>& ctl,
-                                const T* val, const T* wd, const T* sd, const double* r64, T* r, T* d, T* z, T* m,
-                                T* q, T* c) {
+__device__ void eis_transform(Team& team, const SellView& S, TeamControl<T, K>& ctl, const T* val, const T* wd,
+                              const T* sd, const double* r64, T* r, T* d, T* z, T* m, T* q, T* c, bool init,
+                              double (&zr)[K]) {
     using AT = AccT<T>;
     using Acc = typename AT::type;
     const int n = S.n;
     const int lane = threadIdx.x & 31;
-    const bool leader = threadIdx.x == 0;
-    {   // restart from c = 0: auxiliary = r64 / ||r64||
+    const int fresh = ctl.fresh;
+    {
         T inv[K];
         #pragma unroll
         for (int j = 0; j < K; j++) inv[j] = ctl.inv[j];
@@ -511,7 +515,8 @@ __device__ void inner_eisenstat(Team& team, const SellView& S, const BatchArgs& 
             for (int j = 0; j < K; j++) {
                 const long long p = (long long)i * K + j;
                 q[p] = (T)(r64[p] * (double)inv[j]);
-                r[p] = T(0); c[p] = T(0); d[p] = T(0); z[p] = T(0); m[p] = T(0);
+                c[p] = T(0);
+                if (init) { r[p] = T(0); d[p] = T(0); z[p] = T(0); m[p] = T(0); }
             }
         }
     }
@@ -519,7 +524,7 @@ __device__ void inner_eisenstat(Team& team, const SellView& S, const BatchArgs& 
     Acc azr[K];
     #pragma unroll
     for (int j = 0; j < K; j++) azr[j] = AT::zero();
-    for (int col = 0; col < S.ncolors; col++) {                  // L-solve of the residual, z = S r, d = z
+    for (int col = 0; col < S.ncolors; col++) {
         for_slices_dot<T, T, K, kBlockL>(team, S, __ldg(&S.color_slice[col]), __ldg(&S.color_slice[col + 1]), val, r,
             [&](const SliceMeta& M) {
                 RowState<T, K> p;
@@ -527,163 +532,150 @@ __device__ void inner_eisenstat(Team& team, const SellView& S, const BatchArgs& 
                 p.w = p.act ? __ldg(&wd[p.row]) : T(0);
                 p.sdv = p.act ? __ldg(&sd[p.row]) : T(0);
                 load_row<T, K>(q, p.row, p.act, p.a);
+                if (fresh) load_row<T, K>(d, p.row, p.act, p.b);
                 return p;
             },
             [&](const SliceMeta&, const RowState<T, K>& p, const T (&sum)[K]) {
                 if (p.act && p.w != T(0)) {
-                    T rv[K], zv[K];
+                    T rv[K], zv[K], dv[K];
                     #pragma unroll
                     for (int j = 0; j < K; j++) {
                         rv[j] = (p.a[j] - sum[j]) * p.w;
                         zv[j] = rv[j] * p.sdv;
                         azr[j] = AT::add(azr[j], zv[j] * rv[j]);
+                        dv[j] = (fresh >> j & 1) ? zv[j] : p.b[j];
                     }
                     store_row<T, K>(r, p.row, rv);
                     store_row<T, K>(z, p.row, zv);
-                    store_row<T, K>(d, p.row, zv);
+                    if (fresh) store_row<T, K>(d, p.row, dv);
+                }
+            });
+        team.sync();
+    }
+    team.template sum<T, K>(azr, zr);
+}
+
+// One iteration for the active columns. `update_d`: the backward sweep first forms
+// d = z + beta d (skipped when every active column is fresh: the transform set d = z).
+template <typename T, int K, typename Team>
+__device__ void eis_iterate(Team& team, const SellView& S, TeamControl<T, K>& ctl, const T* val, const T* wd,
+                            const T* sd, T* r, T* d, T* z, T* m, T* q, T* c, bool update_d, double (&zr_new)[K]) {
+    using AT = AccT<T>;
+    using Acc = typename AT::type;
+    const int n = S.n;
+    const int lane = threadIdx.x & 31;
+    const bool leader = threadIdx.x == 0;
+    {   // backward sweep: technical = (d - U technical) w / D, with d = z + beta d first
+        T beta[K];
+        #pragma unroll
+        for (int j = 0; j < K; j++) beta[j] = ctl.beta[j];
+        for (int col = S.ncolors - 1; col >= 0; col--) {
+            for_slices_dot<T, T, K, kBlockU>(team, S, __ldg(&S.color_slice[col]), __ldg(&S.color_slice[col + 1]),
+                                             val, m,
+                [&](const SliceMeta& M) {
+                    RowState<T, K> p;
+                    p.row = M.row0 + lane; p.act = lane < M.nrow;
+                    p.w = p.act ? __ldg(&wd[p.row]) : T(0);
+                    load_row<T, K>(d, p.row, p.act, p.a);
+                    if (update_d) load_row<T, K>(z, p.row, p.act, p.b);
+                    return p;
+                },
+                [&](const SliceMeta&, const RowState<T, K>& p, const T (&sum)[K]) {
+                    if (p.act && p.w != T(0)) {
+                        T dv[K], mv[K];
+                        #pragma unroll
+                        for (int j = 0; j < K; j++) {
+                            dv[j] = update_d ? p.b[j] + beta[j] * p.a[j] : p.a[j];
+                            mv[j] = (dv[j] - sum[j]) * p.w;
+                        }
+                        if (update_d) store_row<T, K>(d, p.row, dv);
+                        store_row<T, K>(m, p.row, mv);
+                    }
+                });
+            team.sync();
+        }
+    }
+    Acc dad[K];
+    #pragma unroll
+    for (int j = 0; j < K; j++) dad[j] = AT::zero();
+    for (int col = 0; col < S.ncolors; col++) {              // forward sweep: auxiliary, d.(aux + tech)
+        for_slices_dot<T, T, K, kBlockL>(team, S, __ldg(&S.color_slice[col]), __ldg(&S.color_slice[col + 1]), val, q,
+            [&](const SliceMeta& M) {
+                RowState<T, K> p;
+                p.row = M.row0 + lane; p.act = lane < M.nrow;
+                p.w = p.act ? __ldg(&wd[p.row]) : T(0);
+                p.sdv = p.act ? __ldg(&sd[p.row]) : T(0);
+                load_row<T, K>(d, p.row, p.act, p.a);
+                load_row<T, K>(m, p.row, p.act, p.b);
+                return p;
+            },
+            [&](const SliceMeta&, const RowState<T, K>& p, const T (&sum)[K]) {
+                if (p.act && p.w != T(0)) {
+                    T av[K];
+                    #pragma unroll
+                    for (int j = 0; j < K; j++) {
+                        av[j] = (p.a[j] - p.sdv * p.b[j] - sum[j]) * p.w;
+                        dad[j] = AT::add(dad[j], (av[j] + p.b[j]) * p.a[j]);
+                    }
+                    store_row<T, K>(q, p.row, av);
                 }
             });
         team.sync();
     }
     {
-        double o[K];
-        team.template sum<T, K>(azr, o);
+        double dq[K];
+        team.template sum<T, K>(dad, dq);
         if (leader) {
-            for (int j = 0; j < K; j++) { ctl.zr[j] = o[j]; ctl.rr[j] = o[j]; ctl.rr0[j] = o[j] > 0.0 ? o[j] : 1.0; }
-            ctl.active = inner_active<T, K>(ctl, ~ctl.done, args.max_iter);
+            int act = ctl.active;
+            for (int j = 0; j < K; j++) {
+                T a = T(0);
+                if (act >> j & 1) {
+                    const double zr = ctl.zr[j];
+                    if (!(dq[j] > 0.0) || !(zr >= 0.0) || !isfinite(dq[j]) || !isfinite(zr)) {
+                        act &= ~(1 << j);
+                        ctl.broke |= 1 << j;
+                    } else {
+                        a = (T)(zr / dq[j]);
+                    }
+                }
+                ctl.alpha[j] = a;
+            }
+            ctl.active = act;
         }
     }
     __syncthreads();
-    bool first = true;
-    while (ctl.active) {
-        {   // backward sweep: technical = (d - U technical) w / D, with d = z + beta d first
-            T beta[K];
-            #pragma unroll
-            for (int j = 0; j < K; j++) beta[j] = ctl.beta[j];
-            for (int col = S.ncolors - 1; col >= 0; col--) {
-                for_slices_dot<T, T, K, kBlockU>(team, S, __ldg(&S.color_slice[col]), __ldg(&S.color_slice[col + 1]),
-                                                 val, m,
-                    [&](const SliceMeta& M) {
-                        RowState<T, K> p;
-                        p.row = M.row0 + lane; p.act = lane < M.nrow;
-                        p.w = p.act ? __ldg(&wd[p.row]) : T(0);
-                        load_row<T, K>(d, p.row, p.act, p.a);
-                        if (!first) load_row<T, K>(z, p.row, p.act, p.b);
-                        return p;
-                    },
-                    [&](const SliceMeta&, const RowState<T, K>& p, const T (&sum)[K]) {
-                        if (p.act && p.w != T(0)) {
-                            T dv[K], mv[K];
-                            #pragma unroll
-                            for (int j = 0; j < K; j++) {
-                                dv[j] = first ? p.a[j] : p.b[j] + beta[j] * p.a[j];
-                                mv[j] = (dv[j] - sum[j]) * p.w;
-                            }
-                            if (!first) store_row<T, K>(d, p.row, dv);
-                            store_row<T, K>(m, p.row, mv);
-                        }
-                    });
-                team.sync();
-            }
-        }
-        Acc dad[K];
+    Acc azr[K];
+    {   // update: c += alpha technical, r -= alpha (auxiliary + technical), z = S r, z.r
+        T alpha[K];
         #pragma unroll
-        for (int j = 0; j < K; j++) dad[j] = AT::zero();
-        for (int col = 0; col < S.ncolors; col++) {              // forward sweep: auxiliary, d.(aux + tech)
-            for_slices_dot<T, T, K, kBlockL>(team, S, __ldg(&S.color_slice[col]), __ldg(&S.color_slice[col + 1]), val, q,
-                [&](const SliceMeta& M) {
-                    RowState<T, K> p;
-                    p.row = M.row0 + lane; p.act = lane < M.nrow;
-                    p.w = p.act ? __ldg(&wd[p.row]) : T(0);
-                    p.sdv = p.act ? __ldg(&sd[p.row]) : T(0);
-                    load_row<T, K>(d, p.row, p.act, p.a);
-                    load_row<T, K>(m, p.row, p.act, p.b);
-                    return p;
-                },
-                [&](const SliceMeta&, const RowState<T, K>& p, const T (&sum)[K]) {
-                    if (p.act && p.w != T(0)) {
-                        T av[K];
-                        #pragma unroll
-                        for (int j = 0; j < K; j++) {
-                            av[j] = (p.a[j] - p.sdv * p.b[j] - sum[j]) * p.w;
-                            dad[j] = AT::add(dad[j], (av[j] + p.b[j]) * p.a[j]);
-                        }
-                        store_row<T, K>(q, p.row, av);
-                    }
-                });
-            team.sync();
-        }
-        {
-            double dq[K];
-            team.template sum<T, K>(dad, dq);
-            if (leader) {
-                int act = ctl.active;
-                for (int j = 0; j < K; j++) {
-                    T a = T(0);
-                    if (act >> j & 1) {
-                        const double zr = ctl.zr[j];
-                        if (!(dq[j] > 0.0) || !(zr >= 0.0) || !isfinite(dq[j]) || !isfinite(zr)) act &= ~(1 << j);
-                        else a = (T)(zr / dq[j]);
-                    }
-                    ctl.alpha[j] = a;
-                }
-                ctl.active = act;
-            }
-        }
-        __syncthreads();
-        {   // update: c += alpha technical, r -= alpha (auxiliary + technical), z = S r, z.r
-            T alpha[K];
+        for (int j = 0; j < K; j++) { alpha[j] = ctl.alpha[j]; azr[j] = AT::zero(); }
+        for (int i = team.tid(); i < n; i += team.nthreads()) {
+            const T w = __ldg(&wd[i]);
+            if (w == T(0)) continue;
+            const T sdv = __ldg(&sd[i]);
+            T cv[K], mv[K], qv[K], rv[K], zv[K];
+            load_k_stream<T, K>(c + (long long)i * K, cv);
+            load_k_stream<T, K>(m + (long long)i * K, mv);
+            load_k_stream<T, K>(q + (long long)i * K, qv);
+            load_k_stream<T, K>(r + (long long)i * K, rv);
             #pragma unroll
-            for (int j = 0; j < K; j++) { alpha[j] = ctl.alpha[j]; azr[j] = AT::zero(); }
-            for (int i = team.tid(); i < n; i += team.nthreads()) {
-                const T w = __ldg(&wd[i]);
-                if (w == T(0)) continue;
-                const T sdv = __ldg(&sd[i]);
-                T cv[K], mv[K], qv[K], rv[K], zv[K];
-                load_k_stream<T, K>(c + (long long)i * K, cv);
-                load_k_stream<T, K>(m + (long long)i * K, mv);
-                load_k_stream<T, K>(q + (long long)i * K, qv);
-                load_k_stream<T, K>(r + (long long)i * K, rv);
-                #pragma unroll
-                for (int j = 0; j < K; j++) {
-                    cv[j] += alpha[j] * mv[j];
-                    rv[j] -= alpha[j] * (qv[j] + mv[j]);
-                    zv[j] = rv[j] * sdv;
-                    azr[j] = AT::add(azr[j], zv[j] * rv[j]);
-                }
-                store_row<T, K>(c, i, cv);
-                store_row<T, K>(r, i, rv);
-                store_row<T, K>(z, i, zv);
+            for (int j = 0; j < K; j++) {
+                cv[j] += alpha[j] * mv[j];
+                rv[j] -= alpha[j] * (qv[j] + mv[j]);
+                zv[j] = rv[j] * sdv;
+                azr[j] = AT::add(azr[j], zv[j] * rv[j]);
             }
+            store_row<T, K>(c, i, cv);
+            store_row<T, K>(r, i, rv);
+            store_row<T, K>(z, i, zv);
         }
-        {
-            double o[K];
-            team.template sum<T, K>(azr, o);
-            if (leader) {
-                const int was = ctl.active;
-                for (int j = 0; j < K; j++) {
-                    T b = T(0);
-                    if (was >> j & 1) {
-                        b = (T)(o[j] / ctl.zr[j]);
-                        ctl.zr[j] = o[j]; ctl.rr[j] = o[j];
-                        ctl.iters[j]++;
-                    }
-                    ctl.beta[j] = b;
-                }
-                ctl.active = inner_active<T, K>(ctl, was, args.max_iter);
-            }
-        }
-        __syncthreads();
-        first = false;
-        team.sync();
     }
+    team.template sum<T, K>(azr, zr_new);
 }
 
 // One team solves work item `it` completely.
 template <typename T, int K, bool RAINBOW, typename Team>
 __device__ void team_solve(Team& team, const BatchArgs& args, const BatchItem& it) {
-    using AT = AccT<T>;
-    using Acc = typename AT::type;
     const SellView S = args.systems[it.system];
     const int n = S.n;
     const int lane = threadIdx.x & 31;
@@ -719,20 +711,21 @@ __device__ void team_solve(Team& team, const BatchArgs& args, const BatchItem& i
             for (int j = 0; j < K; j++) {
                 ctl.bnorm2[j] = o[j];
                 ctl.iters[j] = 0; ctl.outer[j] = 0; ctl.status[j] = FEEC_MAXITER; ctl.relres[j] = -1.0;
-                ctl.stall[j] = 0.0; ctl.amp[j] = 0.0;
+                ctl.stall[j] = 0.0; ctl.amp[j] = 0.0; ctl.rnorm[j] = 0.0; ctl.scale[j] = 1.0; ctl.zr_prev[j] = 1.0;
+                ctl.beta[j] = T(0);
                 if (j >= kk) ctl.done |= 1 << j;
             }
-            ctl.err_step = 0;
+            ctl.err_step = 0; ctl.fresh = (1 << K) - 1; ctl.broke = 0; ctl.trig = 0;
         }
     }
-    // Error control (as in the single-system mixed solver): a correction approximates the
-    // error of the iterate it corrects, so its size against that iterate's residual measures
-    // the operator's error-to-residual amplification; a column stops only when also
-    // amplification x relative residual <= kErrorPerResidual x precision, and its last inner
-    // solve is sized for both bars. At most one outer step is added for the error bar alone.
+    // Error control: a correction approximates the error of the iterate it corrects, so its
+    // size against that iterate's residual measures the operator's error-to-residual
+    // amplification; a column stops only when also amplification x relative residual <=
+    // kErrorPerResidual x precision, and its replacement target is sized for both bars.
     const double err_target = kErrorPerResidual * args.precision;
+    const double delta2 = args.inner_eta * args.inner_eta;   // reliable-update factor, squared
 
-    for (int outer = 0; outer < args.max_outer; outer++) {
+    for (int seg = 0; ; seg++) {
         // ---- FP64 true residual r64 = b - A x and its norm ----
         team.sync();
         {
@@ -755,53 +748,118 @@ __device__ void team_solve(Team& team, const BatchArgs& args, const BatchItem& i
                     }
                 });
             team.template sum<double, K>(a2, rn2);
-            // stop tests and the next inner target per column
+            // stop tests and the scale of the next segment per column
             if (leader) {
                 int done = ctl.done;
                 for (int j = 0; j < kk; j++) {
                     const double bn = sqrt(ctl.bnorm2[j]);
                     const double rn = sqrt(rn2[j]);
                     const double rel = bn > 0.0 ? rn / bn : 0.0;
-                    const bool errs = ctl.err_step >> j & 1;
                     if (!(done >> j & 1)) {
                         int st = -1;
+                        const bool budget = ctl.iters[j] >= args.max_iter || ctl.outer[j] >= args.max_outer;
                         if (!(rn == rn)) st = FEEC_BREAKDOWN;
                         else if (rn <= args.precision * bn) {
-                            if (errs || ctl.amp[j] == 0.0 || ctl.amp[j] * rel <= err_target) st = FEEC_OK;
+                            // stop at the error bar, or when the residual no longer falls (the FP64
+                            // residual's own rounding floor) after the bar was first missed
+                            const bool floor = (ctl.err_step >> j & 1) && rn > 0.3 * ctl.rnorm[j];
+                            if (ctl.amp[j] == 0.0 || ctl.amp[j] * rel <= err_target || budget || floor) st = FEEC_OK;
                             else ctl.err_step |= 1 << j;
-                        } else if (errs) st = FEEC_MAXITER;   // the error-bar step lost the residual bar
-                        else if (args.stall_check && ctl.outer[j] > 0 && rn > ctl.stall[j]) st = kStatusStagnated;
-                        else if (ctl.iters[j] >= args.max_iter) st = FEEC_MAXITER;
+                        } else if (args.stall_check && seg > 0 && (ctl.trig >> j & 1) && rn > ctl.stall[j]) {
+                            st = kStatusStagnated;   // FP32 cannot follow: the host finishes it in FP64
+                        } else if (budget) st = FEEC_MAXITER;
                         if (st >= 0) { done |= 1 << j; ctl.status[j] = st; }
                     }
                     ctl.relres[j] = rel;
-                    // inner target: the reduction still needed (with margin) for the residual bar
-                    // and, once an amplification is known, the error bar; never below eta
-                    double target = args.precision * bn;
-                    if (ctl.amp[j] > 0.0 && err_target * bn / ctl.amp[j] < target) target = err_target * bn / ctl.amp[j];
-                    const double need = args.inner_margin * target / (rn > 0.0 ? rn : 1.0);
-                    const double eta = need > args.inner_eta ? need : args.inner_eta;
                     const bool live = !(done >> j & 1);
+                    // direction rescaling to the new scale, folded into the next beta
+                    ctl.scale[j] = (live && rn > 0.0 && ctl.rnorm[j] > 0.0) ? ctl.rnorm[j] / rn : 1.0;
                     ctl.inv[j] = live && rn > 0.0 ? (T)(1.0 / rn) : T(0);
                     ctl.rnorm[j] = live ? rn : 0.0;
-                    ctl.eta2[j] = eta * eta;
-                    ctl.stall[j] = rn * sqrt(eta);   // the next residual must gain half the digits asked
+                    if (ctl.broke >> j & 1) ctl.fresh |= 1 << j;   // a broken-down direction restarts
                 }
-                for (int j = kk; j < K; j++) { ctl.inv[j] = T(0); ctl.rnorm[j] = 0.0; ctl.eta2[j] = 0.0; }
+                for (int j = kk; j < K; j++) { ctl.inv[j] = T(0); ctl.rnorm[j] = 0.0; }
+                ctl.broke = 0;
+                ctl.trig = 0;
                 ctl.done = done;
+                ctl.fresh &= ~done;
                 ctl.all_done = done == (1 << K) - 1;
             }
         }
         __syncthreads();
         if (ctl.all_done) break;
 
-        // ---- inner solve: A c = r64 / ||r64|| in T, from c = 0 ----
-        if constexpr (RAINBOW)
-            inner_eisenstat<T, K>(team, S, args, ctl, val, wd, sd, r64, r, d, z, m, q, c);
-        else
-            inner_cg<T, K>(team, S, args, ctl, val, r64, r, d, q, c);
-        // x += ||r|| c in FP64 (rnorm is 0 for finished columns), with the squared norms of
-        // the corrections and of the new iterates for the error control
+        // ---- transform the new residual; beta against the previous rho (kept direction) ----
+        {
+            double zr[K];
+            if constexpr (RAINBOW)
+                eis_transform<T, K>(team, S, ctl, val, wd, sd, r64, r, d, z, m, q, c, seg == 0, zr);
+            else
+                cg_transform<T, K>(team, S, ctl, r64, r, d, c, zr);
+            if (leader) {
+                const int done = ctl.done;
+                for (int j = 0; j < K; j++) {
+                    const bool live = !(done >> j & 1);
+                    T b = T(0);
+                    if (live && !(ctl.fresh >> j & 1) && ctl.zr_prev[j] > 0.0)
+                        b = (T)(zr[j] / (ctl.zr_prev[j] * ctl.scale[j]));
+                    ctl.beta[j] = b;
+                    ctl.zr[j] = zr[j];
+                    // the segment ends once z.r has fallen by delta^2 or far enough for the target
+                    // (the residual bar and, once an amplification is known, the error bar),
+                    // whichever comes first: the larger of the two factors
+                    const double bn = sqrt(ctl.bnorm2[j]);
+                    double target = args.precision * bn;
+                    if (ctl.amp[j] > 0.0 && err_target * bn / ctl.amp[j] < target) target = err_target * bn / ctl.amp[j];
+                    const double rn = ctl.rnorm[j];
+                    const double need = rn > 0.0 ? args.inner_margin * target / rn : 0.0;
+                    const double f = need * need > delta2 ? need * need : delta2;
+                    ctl.thr[j] = live ? zr[j] * f : 0.0;
+                    // the next true residual must gain at least half the digits z.r promised
+                    ctl.stall[j] = rn * sqrt(sqrt(f > 0.0 ? f : 1.0));
+                }
+                ctl.active = ~done & ((1 << K) - 1);
+            }
+        }
+        __syncthreads();
+
+        // ---- iterate until a column asks for a replacement ----
+        // a fresh column's d = z was set by the transform; the others form d = z + beta d in
+        // the first backward sweep (fresh columns then have beta = 0 and d = z: the same d)
+        bool update_d = true;
+        if constexpr (RAINBOW) update_d = (ctl.fresh & ctl.active) != ctl.active;
+        while (true) {
+            double zr_new[K];
+            if constexpr (RAINBOW)
+                eis_iterate<T, K>(team, S, ctl, val, wd, sd, r, d, z, m, q, c, update_d, zr_new);
+            else
+                cg_iterate<T, K>(team, S, ctl, val, r, d, q, c, zr_new);
+            update_d = true;
+            if (leader) {
+                ctl.fresh = 0;   // every thread read it before the iteration's barriers
+                const int was = ctl.active;
+                int trig = 0;
+                for (int j = 0; j < K; j++) {
+                    T b = T(0);
+                    if (was >> j & 1) {
+                        b = (T)(zr_new[j] / ctl.zr[j]);
+                        ctl.zr_prev[j] = ctl.zr[j];
+                        ctl.zr[j] = zr_new[j];
+                        ctl.iters[j]++;
+                        if (!(zr_new[j] >= ctl.thr[j]) || ctl.iters[j] >= args.max_iter) trig |= 1 << j;
+                    } else if (!(ctl.done >> j & 1)) {
+                        trig |= 1 << j;   // broke down: replace its residual and restart its direction
+                    }
+                    ctl.beta[j] = b;
+                }
+                ctl.trig = trig;
+            }
+            __syncthreads();
+            if (ctl.trig) break;
+            team.sync();
+        }
+
+        // ---- x += ||r64|| c in FP64, with the norms of the corrections and the new iterates ----
         {
             double rnorm[K], nn[2 * K], nsum[2 * K];
             #pragma unroll
@@ -823,8 +881,9 @@ __device__ void team_solve(Team& team, const BatchArgs& args, const BatchItem& i
             if (leader)
                 for (int j = 0; j < K; j++) {
                     if (ctl.done >> j & 1) continue;
-                    // the first step starts from x = 0 (its correction is the whole solution)
-                    if (ctl.outer[j] > 0 && nsum[K + j] > 0.0 && ctl.relres[j] > 0.0) {
+                    // the first segment starts from the initial guess (its correction is the
+                    // solution); a later one measures the error of the iterate it corrected
+                    if (ctl.outer[j] > 0 && nsum[K + j] > 0.0 && ctl.relres[j] > 0.0 && (ctl.trig >> j & 1)) {
                         const double a = sqrt(nsum[j] / nsum[K + j]) / ctl.relres[j];
                         if (a > ctl.amp[j]) ctl.amp[j] = a;
                     }
