@@ -18,6 +18,7 @@
 #include <condition_variable>
 #include <cstring>
 #include <deque>
+#include <memory>
 #include <mutex>
 #include <new>
 #include <thread>
@@ -49,6 +50,35 @@ struct Request {
     clock_type::time_point t_submit;
 };
 
+// The reference's Rainbow coloring (sparse/rainbow.cpp:14-130) depends on the sparsity
+// pattern only. A serving process sees the same operators again and again, so colorings
+// are kept per pattern, keyed by the row count and a 64-bit hash of the row pointers and
+// column indices; a request whose pattern is known skips the greedy coloring.
+struct Coloring {
+    int nc = 0;
+    std::vector<int> F, B, R;
+};
+
+unsigned long long pattern_hash(int n, const int* A, const int* C) {
+    unsigned long long h = 0x243F6A8885A308D3ull ^ (unsigned long long)n;
+    auto mix = [&h](const int* p, size_t count) {
+        size_t i = 0;
+        for (; i + 2 <= count; i += 2) {
+            unsigned long long w;
+            std::memcpy(&w, p + i, sizeof(w));
+            h = (h ^ w) * 0x9E3779B97F4A7C15ull;
+            h ^= h >> 29;
+        }
+        if (i < count) {
+            h = (h ^ (unsigned long long)(unsigned)p[i]) * 0x9E3779B97F4A7C15ull;
+            h ^= h >> 29;
+        }
+    };
+    mix(A, (size_t)n + 1);
+    mix(C, (size_t)A[n]);
+    return h;
+}
+
 size_t estimate_bytes(int n, long long nnz) {
     // original CSR + FP32 values, permuted [L|E|U] copy (FP64 + FP32), SELL copy with
     // padding (int + FP32 + FP64), row arrays, solver vectors
@@ -74,6 +104,9 @@ struct feec_server {
     std::vector<std::thread> workers;
     bool stop = false;
     long long next_id = 1;
+    std::mutex color_mu;               // colorings by pattern (see Coloring), oldest dropped first
+    std::deque<std::pair<unsigned long long, std::shared_ptr<const Coloring>>> colorings;
+    static constexpr size_t kMaxColorings = 64;
     long long submitted = 0, finished = 0;
     clock_type::time_point t0;
 };
@@ -92,16 +125,31 @@ int serve_one(feec_server* srv, const Request& rq, cudaStream_t stream, feec_req
     struct Guard { feec_system* s; ~Guard() { feec_system_destroy(s); } } guard{s};
     const bool rainbow = srv->method == FEEC_METHOD_RAINBOW;
     if (rainbow) {
-        // the reference's Rainbow ordering (sparse/rainbow.cpp:14-130) and the diagonal
-        std::vector<int> F((size_t)rq.n), B((size_t)rq.n + 1), R((size_t)rq.n);
-        int nc = 0;
-        st = feec_rainbow(rq.n, rq.A, rq.C, &nc, F.data(), B.data(), R.data());
-        if (st != FEEC_OK) return st;
+        // the reference's Rainbow ordering (sparse/rainbow.cpp:14-130), from the cache when
+        // this pattern was colored before, and the diagonal
+        const unsigned long long key = pattern_hash(rq.n, rq.A, rq.C);
+        std::shared_ptr<const Coloring> col;
+        {
+            std::lock_guard<std::mutex> lk(srv->color_mu);
+            for (const auto& e : srv->colorings)
+                if (e.first == key && (int)e.second->F.size() == rq.n) { col = e.second; break; }
+        }
+        if (!col) {
+            auto c = std::make_shared<Coloring>();
+            c->F.resize((size_t)rq.n); c->B.resize((size_t)rq.n + 1); c->R.resize((size_t)rq.n);
+            st = feec_rainbow(rq.n, rq.A, rq.C, &c->nc, c->F.data(), c->B.data(), c->R.data());
+            if (st != FEEC_OK) return st;
+            c->B.resize((size_t)c->nc + 1);
+            col = c;
+            std::lock_guard<std::mutex> lk(srv->color_mu);
+            srv->colorings.emplace_back(key, col);
+            if (srv->colorings.size() > feec_server::kMaxColorings) srv->colorings.pop_front();
+        }
         std::vector<double> diag((size_t)rq.n, 0.0);
         for (int r = 0; r < rq.n; r++)
             for (int k = rq.A[r]; k < rq.A[r + 1]; k++)
                 if (rq.C[k] == r) diag[r] += rq.V[k];
-        st = feec_system_set_rainbow(s, diag.data(), 1.0, nc, F.data(), B.data(), R.data(), 1);
+        st = feec_system_set_rainbow(s, diag.data(), 1.0, col->nc, col->F.data(), col->B.data(), col->R.data(), 1);
         if (st != FEEC_OK) return st;
     }
     const int is_float = srv->mode == FEEC_MODE_MIXED;

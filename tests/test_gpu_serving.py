@@ -103,3 +103,64 @@ def test_oversized_request_is_rejected(cuda):
     with pytest.raises(FeecError):
         srv.submit(A, C, V, b, 1e-10)
     srv.close()
+
+
+def _laplace_1d(n):
+    """tridiag(-1, 2, -1): condition number about 3.6e6 at n = 3000, too ill-conditioned
+    for FP32 arithmetic, so a mixed-precision request finishes in FP64."""
+    M = sp.diags([-np.ones(n - 1), 2.0 * np.ones(n), -np.ones(n - 1)], [-1, 0, 1]).tocsr()
+    M.sort_indices()
+    return M.indptr.astype(np.int32), M.indices.astype(np.int32), M.data.astype(np.float64)
+
+
+def test_whole_gpu_and_fp64_fallback_requests_same_alone_and_in_mix(cuda):
+    """A request above the whole-GPU threshold (3D P1 refined 6 times, 4.0 M stored
+    entries: the persistent solver on every SM) and one whose FP32 iterations stagnate
+    (finished in FP64) give the same solution alone and in a mix of cluster requests,
+    and each reaches its tolerance."""
+    from simplefem_gb300 import workloads
+    from simplefem_gb300.serving import Server
+    big = _problem(3, 1, 6, 11)
+    A1, C1, V1 = _laplace_1d(3000)
+    b1 = workloads.uniform_vector(7, 3000)
+    cases = [(big, 1e-10), ((A1, C1, V1, b1), 1e-8)]
+    alone = []
+    for prob, tol in cases:
+        srv = Server(hbm_budget_bytes=20 * 10**9, slots=1)
+        srv.submit(*prob, tol)
+        assert srv.wait(600)
+        alone.append(srv.poll()[0])
+        srv.close()
+    assert alone[0]["cluster_blocks"] < 0, alone[0]          # whole-GPU persistent grid
+    assert alone[1]["fp64_fallback"] == 1, alone[1]
+    mix = Server(hbm_budget_bytes=60 * 10**9, slots=8)
+    for spec in SPECS[:4]:
+        mix.submit(*_problem(*spec), 1e-10)
+    ids = [mix.submit(*prob, tol) for prob, tol in cases]
+    for spec in SPECS[4:8]:
+        mix.submit(*_problem(*spec), 1e-10)
+    assert mix.wait(900)
+    res = {r["id"]: r for r in mix.poll()}
+    assert len(res) == 10 and all(r["status"] == 0 for r in res.values())
+    for (prob, tol), rid, a in zip(cases, ids, alone):
+        r = res[rid]
+        assert r["cluster_blocks"] == a["cluster_blocks"] and r["fp64_fallback"] == a["fp64_fallback"], (r, a)
+        diff = np.linalg.norm(r["x"] - a["x"]) / np.linalg.norm(a["x"])
+        assert diff <= 1e-9, diff
+        assert _relres(*prob, r["x"]) <= tol
+    mix.close()
+
+
+def test_repeated_pattern_reuses_its_coloring(cuda):
+    """The same operator submitted twice (a coloring cached by pattern the second time)
+    gives the same solution both times."""
+    from simplefem_gb300.serving import Server
+    A, C, V, b = _problem(3, 2, 3, 5)
+    srv = Server(hbm_budget_bytes=10 * 10**9, slots=1)
+    srv.submit(A, C, V, b, 1e-10)
+    srv.submit(A, C, V, b, 1e-10)
+    assert srv.wait(300)
+    res = srv.poll()
+    assert len(res) == 2 and all(r["status"] == 0 for r in res)
+    assert np.array_equal(res[0]["x"], res[1]["x"])
+    srv.close()
