@@ -380,17 +380,20 @@ int solve_core(feec_system* s, int method, int mode, double* xx, const double* b
         st = run_fp64(mode);
         if (st != FEEC_OK) return st;
     } else {
-        // MIXED: FP32 inner iterations (compensated FP32 dots) with reliable updates around
-        // them: the FP64 solution and true residual are kept beside the FP32 recursion, and a
-        // segment ends when z.r (r.r for CG) has fallen by kReliableDelta^2 or far enough for
-        // the target; the correction then goes into x in FP64, the FP64 true residual
-        // replaces the recursive one (scaled to unit norm), and the next segment keeps the
-        // search direction (rescaled, beta against the previous rho) instead of restarting
-        // the Krylov recurrence as plain defect correction does.
+        // MIXED: FP32 inner iterations (compensated FP32 dots) in segments: the FP64 solution
+        // and true residual are kept beside the FP32 recursion, and a segment ends when z.r
+        // (r.r for CG) has fallen by the square of kReliableDelta (kRestartEta for CG) or far
+        // enough for the target; the correction then goes into x in FP64 and the FP64 true
+        // residual replaces the recursive one (scaled to unit norm). The multicolor SSOR-PCG
+        // keeps its search direction across the replacement (rescaled, beta against the
+        // previous rho: reliable updates) instead of restarting the Krylov recurrence; plain
+        // CG restarts (plain defect correction), see kRestartEta.
         if (method == FEEC_METHOD_CG && !s->V32) return FEEC_BADARG;
         if (method != FEEC_METHOD_CG && !s->val32) return FEEC_BADARG;
         const int max_outer = kMaxReplacements;
-        const double delta2 = kReliableDelta * kReliableDelta;
+        const bool keep_dirs = method != FEEC_METHOD_CG;   // plain CG restarts each segment
+        const double seg = keep_dirs ? kReliableDelta : kRestartEta;
+        const double delta2 = seg * seg;
         double rn2 = 0.0;
         double stall_limit = 0.0;        // residual norm above which the last segment stagnated
         bool stagnated = false;
@@ -399,8 +402,8 @@ int solve_core(feec_system* s, int method, int mode, double* xx, const double* b
         // most. Each segment measures how large its correction was against the residual it
         // corrected (the correction approximates the error of the iterate it corrected),
         // which gives the error-to-residual amplification of this operator; the solve then
-        // also asks amplification x relative residual <= err_target before it stops, and
-        // sizes each segment's target for both bars.
+        // also asks max(amplification, kAmpFloor) x relative residual <= err_target before
+        // it stops, and sizes each segment's target for both bars.
         const double err_target = kErrorPerResidual * precision;
         double amp = 0.0;                // largest measured amplification (segments after the first)
         bool err_step = false;           // the residual bar is met, the error bar not yet
@@ -417,7 +420,7 @@ int solve_core(feec_system* s, int method, int mode, double* xx, const double* b
                 // stop at the error bar, or when the residual no longer falls (the FP64
                 // residual's own rounding floor) after the bar was first missed
                 const bool floor = err_step && rn > 0.3 * rn_prev;
-                if (amp == 0.0 || amp * relres <= err_target || floor || K_total >= max_iter) {
+                if (std::max(amp, kAmpFloor) * relres <= err_target || floor || K_total >= max_iter) {
                     status = FEEC_OK;
                     break;
                 }
@@ -445,8 +448,7 @@ int solve_core(feec_system* s, int method, int mode, double* xx, const double* b
             // the segment's target: the residual bar and, once an amplification is known, the
             // error bar (with margin), or a fall of kReliableDelta, whichever comes first
             // (the larger of the two factors)
-            double target = tolerance;
-            if (amp > 0.0) target = std::min(target, err_target * bnorm / amp);
+            const double target = std::min(tolerance, err_target * bnorm / std::max(amp, kAmpFloor));
             const double need = 0.3 * target / rn;
             const double f = std::max(delta2, need * need);
             stall_limit = rn * std::sqrt(std::sqrt(f));
@@ -498,7 +500,7 @@ int solve_core(feec_system* s, int method, int mode, double* xx, const double* b
             if (hs.status == FEEC_TIMEOUT) { status = FEEC_TIMEOUT; break; }
             if (hs.status == FEEC_BREAKDOWN && hs.iterations == 0) { status = FEEC_BREAKDOWN; break; }
             // a breakdown or an empty segment restarts the direction next time
-            have_dir = hs.status == FEEC_OK && hs.iterations > 0;
+            have_dir = keep_dirs && hs.status == FEEC_OK && hs.iterations > 0;
             zr_prev = hs.extra[0];
             rn_prev = rn;
         }

@@ -18,6 +18,11 @@ struct DeviceStatus;
 // Mixed precision stops only when its estimated relative solution error is at most this
 // many times the requested relative residual (1e-9 at a request of 1e-10).
 constexpr double kErrorPerResidual = 10.0;
+// The amplification assumed until a larger one is measured: the stopping residual is at most
+// kErrorPerResidual x precision / max(measured amplification, kAmpFloor). Measured on the
+// benchmark operators (2D P2, 3D P1 and P2, 4,913 to 2.1 M unknowns), the final error of a
+// mixed solve was at most 43 times its relative residual.
+constexpr double kAmpFloor = 100.0;
 
 // ---------------------------------------------------------------------------
 // Persistent solver arguments (all pointers are device pointers).

@@ -86,14 +86,17 @@ __device__ __forceinline__ double small_dot(const SmallRow& R, const PcgArgs<dou
 
 // Walks the row slots [lo, hi) of one phase (LANES lanes per row; the trip count is uniform
 // across each warp for the shuffles). `cur` holds the group's first row, loaded ahead;
-// each later row is loaded while the one before it is processed.
+// each later row is loaded while the one before it is processed. A warp without a row in
+// the phase branches around the body: a level holds a few dozen rows, and GB300 issues a
+// warp's FP64 instruction for 16 cycles of the SM's FP64 pipe even with every lane masked
+// (the idle warps' masked FP64 work was a third of the kernel's time).
 template <int KIND, int LANES, typename F>
 __device__ __forceinline__ void small_phase(const PcgArgs<double>& a, int lo, int hi, SmallRow cur, F&& body) {
     constexpr int groups = kSmallThreads / LANES;
     const int g = threadIdx.x / LANES;
     for (int base = lo; base < hi; base += groups) {
         const SmallRow nxt = small_row<KIND, LANES>(a, base + groups + g, hi);
-        body(cur);
+        if (__any_sync(0xffffffffu, cur.i >= 0)) body(cur);
         cur = nxt;
     }
 }

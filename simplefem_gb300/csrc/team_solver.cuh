@@ -718,10 +718,11 @@ __device__ void team_solve(Team& team, const BatchArgs& args, const BatchItem& i
             ctl.err_step = 0; ctl.fresh = (1 << K) - 1; ctl.broke = 0; ctl.trig = 0;
         }
     }
-    // Error control: a correction approximates the error of the iterate it corrects, so its
-    // size against that iterate's residual measures the operator's error-to-residual
-    // amplification; a column stops only when also amplification x relative residual <=
-    // kErrorPerResidual x precision, and its replacement target is sized for both bars.
+    // Error control (mixed precision): a correction approximates the error of the iterate it
+    // corrects, so its size against that iterate's residual measures the operator's
+    // error-to-residual amplification; a column stops only when also max(amplification,
+    // kAmpFloor) x relative residual <= kErrorPerResidual x precision, and each segment's
+    // target is sized for both bars.
     const double err_target = kErrorPerResidual * args.precision;
     const double delta2 = args.inner_eta * args.inner_eta;   // reliable-update factor, squared
 
@@ -763,7 +764,8 @@ __device__ void team_solve(Team& team, const BatchArgs& args, const BatchItem& i
                             // stop at the error bar, or when the residual no longer falls (the FP64
                             // residual's own rounding floor) after the bar was first missed
                             const bool floor = (ctl.err_step >> j & 1) && rn > 0.3 * ctl.rnorm[j];
-                            if (ctl.amp[j] == 0.0 || ctl.amp[j] * rel <= err_target || budget || floor) st = FEEC_OK;
+                            const double amp = ctl.amp[j] > kAmpFloor ? ctl.amp[j] : kAmpFloor;
+                            if (!args.err_control || amp * rel <= err_target || budget || floor) st = FEEC_OK;
                             else ctl.err_step |= 1 << j;
                         } else if (args.stall_check && seg > 0 && (ctl.trig >> j & 1) && rn > ctl.stall[j]) {
                             st = kStatusStagnated;   // FP32 cannot follow: the host finishes it in FP64
@@ -776,7 +778,8 @@ __device__ void team_solve(Team& team, const BatchArgs& args, const BatchItem& i
                     ctl.scale[j] = (live && rn > 0.0 && ctl.rnorm[j] > 0.0) ? ctl.rnorm[j] / rn : 1.0;
                     ctl.inv[j] = live && rn > 0.0 ? (T)(1.0 / rn) : T(0);
                     ctl.rnorm[j] = live ? rn : 0.0;
-                    if (ctl.broke >> j & 1) ctl.fresh |= 1 << j;   // a broken-down direction restarts
+                    // a broken-down direction restarts, and so does every direction without reliable updates
+                    if ((ctl.broke >> j & 1) || !args.keep_dir) ctl.fresh |= 1 << j;
                 }
                 for (int j = kk; j < K; j++) { ctl.inv[j] = T(0); ctl.rnorm[j] = 0.0; }
                 ctl.broke = 0;
@@ -810,7 +813,10 @@ __device__ void team_solve(Team& team, const BatchArgs& args, const BatchItem& i
                     // whichever comes first: the larger of the two factors
                     const double bn = sqrt(ctl.bnorm2[j]);
                     double target = args.precision * bn;
-                    if (ctl.amp[j] > 0.0 && err_target * bn / ctl.amp[j] < target) target = err_target * bn / ctl.amp[j];
+                    if (args.err_control) {
+                        const double amp = ctl.amp[j] > kAmpFloor ? ctl.amp[j] : kAmpFloor;
+                        if (err_target * bn / amp < target) target = err_target * bn / amp;
+                    }
                     const double rn = ctl.rnorm[j];
                     const double need = rn > 0.0 ? args.inner_margin * target / rn : 0.0;
                     const double f = need * need > delta2 ? need * need : delta2;
