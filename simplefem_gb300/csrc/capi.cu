@@ -394,6 +394,7 @@ int solve_core(feec_system* s, int method, int mode, double* xx, const double* b
         const bool keep_dirs = method != FEEC_METHOD_CG;   // plain CG restarts each segment
         const double seg = keep_dirs ? kReliableDelta : kRestartEta;
         const double delta2 = seg * seg;
+        const double first2 = kRestartEta * kRestartEta;   // see kReliableDelta
         double rn2 = 0.0;
         double stall_limit = 0.0;        // residual norm above which the last segment stagnated
         bool stagnated = false;
@@ -450,7 +451,7 @@ int solve_core(feec_system* s, int method, int mode, double* xx, const double* b
             // (the larger of the two factors)
             const double target = std::min(tolerance, err_target * bnorm / std::max(amp, kAmpFloor));
             const double need = 0.3 * target / rn;
-            const double f = std::max(delta2, need * need);
+            const double f = std::max(outer == 0 ? first2 : delta2, need * need);
             stall_limit = rn * std::sqrt(std::sqrt(f));
             float ms = 0.0f;
             FEEC_TRY(reset_status(s));
@@ -516,7 +517,8 @@ int solve_core(feec_system* s, int method, int mode, double* xx, const double* b
         if (st != FEEC_OK) return st;
         final_norm = std::sqrt(rn2b);
         if (status == FEEC_OK && final_norm > tolerance) status = FEEC_MAXITER;
-        if (amp > 0.0 && !fell_back && bnorm > 0.0) err_estimate = amp * final_norm / bnorm;
+        // the bound the stop rule enforced: max(amplification, kAmpFloor) x relative residual
+        if (!fell_back && bnorm > 0.0) err_estimate = std::max(amp, kAmpFloor) * final_norm / bnorm;
     }
 
     // results back to the caller's numbering

@@ -51,6 +51,11 @@ struct BatchResult {
 // each replaced residual too much for a kept direction (measured on the 3D P2 operator
 // refined 5 times: 4,757 iterations kept against 1,297 restarted). A column gets at most
 // kMaxReplacements replacements.
+// Every mixed solve's first segment asks for the full fall of kRestartEta, as one step of
+// plain defect correction does: an operator too ill-conditioned for FP32 arithmetic shows
+// there (its true residual gains less than half the digits) and is finished in FP64,
+// where short segments would let the FP32 recursion creep on for many times the
+// iterations (measured: 16,253 on the 1D Laplacian of 3,000 unknowns).
 constexpr double kReliableDelta = 0.01;
 constexpr double kRestartEta = 2e-5;
 constexpr int kMaxReplacements = 64;
@@ -63,6 +68,7 @@ struct BatchArgs {
     BatchResult* results;
     double precision;         // stop when ||b - A x|| <= precision ||b|| (FP64)
     double inner_eta;         // segment factor (kReliableDelta / kRestartEta; 1e-30: only at the target)
+    double first_eta;         // segment factor of a column's first segment (kRestartEta in mixed precision)
     int keep_dir;             // 1: keep the search direction across replacements (reliable updates)
     int err_control;          // 1: also stop only at the error bar (mixed precision)
     double inner_margin;      // a segment aims at margin * (the residual target)

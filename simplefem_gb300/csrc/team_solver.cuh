@@ -724,7 +724,8 @@ __device__ void team_solve(Team& team, const BatchArgs& args, const BatchItem& i
     // kAmpFloor) x relative residual <= kErrorPerResidual x precision, and each segment's
     // target is sized for both bars.
     const double err_target = kErrorPerResidual * args.precision;
-    const double delta2 = args.inner_eta * args.inner_eta;   // reliable-update factor, squared
+    const double delta2 = args.inner_eta * args.inner_eta;   // segment factor, squared
+    const double first2 = args.first_eta * args.first_eta;   // ... of a column's first segment
 
     for (int seg = 0; ; seg++) {
         // ---- FP64 true residual r64 = b - A x and its norm ----
@@ -819,7 +820,8 @@ __device__ void team_solve(Team& team, const BatchArgs& args, const BatchItem& i
                     }
                     const double rn = ctl.rnorm[j];
                     const double need = rn > 0.0 ? args.inner_margin * target / rn : 0.0;
-                    const double f = need * need > delta2 ? need * need : delta2;
+                    const double seg_f = ctl.outer[j] == 0 ? first2 : delta2;
+                    const double f = need * need > seg_f ? need * need : seg_f;
                     ctl.thr[j] = live ? zr[j] * f : 0.0;
                     // the next true residual must gain at least half the digits z.r promised
                     ctl.stall[j] = rn * sqrt(sqrt(f > 0.0 ? f : 1.0));
@@ -912,7 +914,9 @@ __device__ void team_solve(Team& team, const BatchArgs& args, const BatchItem& i
             args.results[slot].iterations = ctl.iters[j];
             args.results[slot].outer = ctl.outer[j];
             args.results[slot].relres = ctl.relres[j];
-            args.results[slot].err_est = ctl.amp[j] > 0.0 ? ctl.amp[j] * ctl.relres[j] : -1.0;
+            // the bound the stop rule enforced: max(amplification, kAmpFloor) x relative residual
+            const double amp = ctl.amp[j] > kAmpFloor ? ctl.amp[j] : kAmpFloor;
+            args.results[slot].err_est = args.err_control ? amp * ctl.relres[j] : -1.0;
         }
     }
 }
