@@ -95,8 +95,9 @@ template <typename T> cudaError_t launch_pcg(const PcgArgs<T>& a, LaunchShape& s
 template <typename T> cudaError_t launch_eisenstat(const PcgArgs<T>& a, LaunchShape& shape, cudaStream_t s);
 // FP64 SSOR / multicolor SSOR PCG in one block with the gathered vectors in shared memory
 // (kernels_small.cu), for systems of at most pcg_smem_max_rows() rows.
-cudaError_t launch_pcg_smem(const PcgArgs<double>& a, int lanes, cudaStream_t s);
+cudaError_t launch_pcg_smem(const PcgArgs<double>& a, int lanes, int threads, cudaStream_t s);
 int pcg_smem_max_rows();
+int pcg_smem_threads(int max_phase_rows, int lanes);
 // Largest co-resident grid for the given kernel family and lane count.
 int max_coresident_blocks(int family, int is_float, int lanes, int threads);
 int pick_lanes(double avg_nnz_per_row);

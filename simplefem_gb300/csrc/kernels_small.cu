@@ -22,7 +22,6 @@
 namespace feec {
 namespace {
 
-constexpr int kSmallThreads = 256;
 constexpr int kSmallPF = 4;   // entries of a row segment prefetched per lane
 constexpr int kRing = 4;      // rows (product) or phases (sweeps) loaded ahead per group
 
@@ -90,9 +89,9 @@ __device__ __forceinline__ double small_dot(const SmallRow& R, const PcgArgs<dou
 // the phase branches around the body: a level holds a few dozen rows, and GB300 issues a
 // warp's FP64 instruction for 16 cycles of the SM's FP64 pipe even with every lane masked
 // (the idle warps' masked FP64 work was a third of the kernel's time).
-template <int KIND, int LANES, typename F>
+template <int KIND, int LANES, int THREADS, typename F>
 __device__ __forceinline__ void small_phase(const PcgArgs<double>& a, int lo, int hi, SmallRow cur, F&& body) {
-    constexpr int groups = kSmallThreads / LANES;
+    constexpr int groups = THREADS / LANES;
     const int g = threadIdx.x / LANES;
     for (int base = lo; base < hi; base += groups) {
         const SmallRow nxt = small_row<KIND, LANES>(a, base + groups + g, hi);
@@ -103,9 +102,9 @@ __device__ __forceinline__ void small_phase(const PcgArgs<double>& a, int lo, in
 
 // Rows [lo, hi) without dependences between them (the full-row product): each group keeps
 // kRing of its rows in flight.
-template <int KIND, int LANES, typename F>
+template <int KIND, int LANES, int THREADS, typename F>
 __device__ __forceinline__ void small_rows_ring(const PcgArgs<double>& a, int lo, int hi, F&& body) {
-    constexpr int groups = kSmallThreads / LANES;
+    constexpr int groups = THREADS / LANES;
     const int g = threadIdx.x / LANES;
     SmallRow buf[kRing];
     #pragma unroll
@@ -137,7 +136,7 @@ __device__ __forceinline__ SmallRow sweep_first(const PcgArgs<double>& a, int p)
 // A sweep of dependent phases, one block barrier after each: the group's first row in phase
 // p + kRing is loaded while phase p runs, so a phase waits for its shared-memory gathers and
 // the barrier only. `ring` arrives holding the first kRing phases.
-template <int KIND, int LANES, typename F>
+template <int KIND, int LANES, int THREADS, typename F>
 __device__ __forceinline__ void small_sweep(const PcgArgs<double>& a, SmallRow (&ring)[kRing], F&& body) {
     const int nph = KIND == kSmForward ? a.nf : a.nbw;
     for (int p0 = 0; p0 < nph; p0 += kRing) {
@@ -147,7 +146,7 @@ __device__ __forceinline__ void small_sweep(const PcgArgs<double>& a, SmallRow (
             if (p < nph) {   // uniform
                 const int lo = KIND == kSmForward ? __ldg(&a.fptr[p]) : __ldg(&a.bptr[p]);
                 const int hi = KIND == kSmForward ? __ldg(&a.fptr[p + 1]) : __ldg(&a.bptr[p + 1]);
-                small_phase<KIND, LANES>(a, lo, hi, ring[k], body);
+                small_phase<KIND, LANES, THREADS>(a, lo, hi, ring[k], body);
                 ring[k] = sweep_first<KIND, LANES>(a, p + kRing);
                 __syncthreads();
             }
@@ -166,8 +165,8 @@ __device__ __forceinline__ double small_block_sum(double v) {
     return out;
 }
 
-template <int LANES>
-__global__ void __launch_bounds__(kSmallThreads) pcg_smem_kernel(PcgArgs<double> a) {
+template <int LANES, int THREADS>
+__global__ void __launch_bounds__(THREADS) pcg_smem_kernel(PcgArgs<double> a) {
     extern __shared__ double smem[];
     const int n = a.n;
     double* sdv = smem;          // d
@@ -175,11 +174,11 @@ __global__ void __launch_bounds__(kSmallThreads) pcg_smem_kernel(PcgArgs<double>
     double* szv = smem + 2 * n;  // z
     const int lane = threadIdx.x & (LANES - 1);
     const int g = threadIdx.x / LANES;
-    constexpr int groups = kSmallThreads / LANES;
+    constexpr int groups = THREADS / LANES;
     __shared__ double s_scal[2];
     __shared__ int s_ctl;
 
-    for (int i = threadIdx.x; i < 3 * n; i += kSmallThreads) smem[i] = 0.0;   // work vectors start at 0
+    for (int i = threadIdx.x; i < 3 * n; i += THREADS) smem[i] = 0.0;   // work vectors start at 0
     __syncthreads();
 
     // ---- restart (sparsesolver.cpp:506-588): r = b - A x for rows with D != 0 ----
@@ -255,7 +254,7 @@ __global__ void __launch_bounds__(kSmallThreads) pcg_smem_kernel(PcgArgs<double>
         if (s_ctl) { status = FEEC_OK; break; }
 
         double adq = 0.0;                                                            // :614-628
-        small_rows_ring<kSmFull, LANES>(a, 0, n, [&](const SmallRow& R) {
+        small_rows_ring<kSmFull, LANES, THREADS>(a, 0, n, [&](const SmallRow& R) {
             const double s = small_dot<LANES>(R, a, sdv);
             if (R.i >= 0 && lane == 0) {
                 const double qi = (R.w != 0.0) ? s : 0.0;
@@ -279,7 +278,7 @@ __global__ void __launch_bounds__(kSmallThreads) pcg_smem_kernel(PcgArgs<double>
 
         const double alpha = s_scal[0];
         arr = 0.0;
-        small_sweep<kSmForward, LANES>(a, ring, [&](const SmallRow& R) {             // :640-667
+        small_sweep<kSmForward, LANES, THREADS>(a, ring, [&](const SmallRow& R) {             // :640-667
             const double s = small_dot<LANES>(R, a, smv);
             if (R.i >= 0 && lane == 0 && R.w != 0.0) {
                 a.x[R.i] = R.x + alpha * sdv[R.i];
@@ -292,7 +291,7 @@ __global__ void __launch_bounds__(kSmallThreads) pcg_smem_kernel(PcgArgs<double>
         double azr2 = 0.0;
         #pragma unroll
         for (int k = 0; k < kRing; k++) ring[k] = sweep_first<kSmBackward, LANES>(a, k);
-        small_sweep<kSmBackward, LANES>(a, ring, [&](const SmallRow& R) {            // :670-699
+        small_sweep<kSmBackward, LANES, THREADS>(a, ring, [&](const SmallRow& R) {            // :670-699
             const double s = small_dot<LANES>(R, a, szv);
             if (R.i >= 0 && lane == 0 && R.w != 0.0) {
                 const double mi = smv[R.i] * R.s;
@@ -301,34 +300,41 @@ __global__ void __launch_bounds__(kSmallThreads) pcg_smem_kernel(PcgArgs<double>
                 szv[R.i] = zi;
             }
         });
-        for (int i = threadIdx.x; i < n; i += kSmallThreads)                           // z.r, :690-697
+        for (int i = threadIdx.x; i < n; i += THREADS)                           // z.r, :690-697
             if (__ldg(&a.wd[i]) != 0.0) azr2 += szv[i] * a.r[i];
         // the block sums' barriers order x, r and z before the direction update and the next product
         const double z_r_new = small_block_sum(azr2);
         r_r = small_block_sum(arr);
         const double beta = z_r_new / z_r;                                             // :701-706
         z_r = z_r_new;
-        for (int i = threadIdx.x; i < n; i += kSmallThreads)
+        for (int i = threadIdx.x; i < n; i += THREADS)
             if (__ldg(&a.wd[i]) != 0.0) sdv[i] = szv[i] + beta * sdv[i];
         __syncthreads();
         K++;
     }
     // the work vectors go back to global memory (callers may read d, z, m after a solve)
-    for (int i = threadIdx.x; i < n; i += kSmallThreads) { a.d[i] = sdv[i]; a.m[i] = smv[i]; a.z[i] = szv[i]; }
+    for (int i = threadIdx.x; i < n; i += THREADS) { a.d[i] = sdv[i]; a.m[i] = smv[i]; a.z[i] = szv[i]; }
     finish(a.st, status, K, z_r, r_r);
 }
 
 size_t smem_bytes(int n) { return (size_t)3 * (size_t)n * sizeof(double); }
 
-template <int LANES>
+template <int LANES, int THREADS>
 cudaError_t launch_small(const PcgArgs<double>& a, cudaStream_t s) {
     const size_t bytes = smem_bytes(a.n);
-    cudaError_t e = cudaFuncSetAttribute(pcg_smem_kernel<LANES>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaError_t e = cudaFuncSetAttribute(pcg_smem_kernel<LANES, THREADS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)bytes);
     if (e != cudaSuccess) return e;
     note_launch();
-    pcg_smem_kernel<LANES><<<1, kSmallThreads, bytes, s>>>(a);
+    pcg_smem_kernel<LANES, THREADS><<<1, THREADS, bytes, s>>>(a);
     return cudaGetLastError();
+}
+
+template <int LANES>
+cudaError_t launch_small_threads(const PcgArgs<double>& a, int threads, cudaStream_t s) {
+    if (threads <= 64) return launch_small<LANES, 64>(a, s);
+    if (threads <= 128) return launch_small<LANES, 128>(a, s);
+    return launch_small<LANES, 256>(a, s);
 }
 
 }  // namespace
@@ -341,13 +347,21 @@ int pcg_smem_max_rows() {
     return (optin - static_bytes) / (3 * (int)sizeof(double));
 }
 
-cudaError_t launch_pcg_smem(const PcgArgs<double>& a, int lanes, cudaStream_t s) {
+// The block is as wide as the widest sweep phase needs (64, 128 or 256 threads): a phase's
+// cost is its instruction path and barrier, which grow with the warps that take part, and
+// the index-order levels hold a few dozen rows.
+int pcg_smem_threads(int max_phase_rows, int lanes) {
+    const long long need = (long long)max_phase_rows * lanes;
+    return need <= 64 ? 64 : need <= 128 ? 128 : 256;
+}
+
+cudaError_t launch_pcg_smem(const PcgArgs<double>& a, int lanes, int threads, cudaStream_t s) {
     if (a.n <= 0 || a.n > pcg_smem_max_rows()) return cudaErrorInvalidValue;
     switch (lanes) {
-        case 1: return launch_small<1>(a, s);
-        case 2: return launch_small<2>(a, s);
-        case 4: return launch_small<4>(a, s);
-        default: return launch_small<8>(a, s);
+        case 1: return launch_small_threads<1>(a, threads, s);
+        case 2: return launch_small_threads<2>(a, threads, s);
+        case 4: return launch_small_threads<4>(a, threads, s);
+        default: return launch_small_threads<8>(a, threads, s);
     }
 }
 
