@@ -501,7 +501,9 @@ int solve_core(feec_system* s, int method, int mode, double* xx, const double* b
             if (hs.status == FEEC_TIMEOUT) { status = FEEC_TIMEOUT; break; }
             if (hs.status == FEEC_BREAKDOWN && hs.iterations == 0) { status = FEEC_BREAKDOWN; break; }
             // a breakdown or an empty segment restarts the direction next time
-            have_dir = keep_dirs && hs.status == FEEC_OK && hs.iterations > 0;
+            // (and the long first segment's direction, whose recursion drifted too far from the
+            // true residual to fit the replaced one)
+            have_dir = keep_dirs && outer > 0 && hs.status == FEEC_OK && hs.iterations > 0;
             zr_prev = hs.extra[0];
             rn_prev = rn;
         }

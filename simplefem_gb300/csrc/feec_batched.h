@@ -55,7 +55,10 @@ struct BatchResult {
 // plain defect correction does: an operator too ill-conditioned for FP32 arithmetic shows
 // there (its true residual gains less than half the digits) and is finished in FP64,
 // where short segments would let the FP32 recursion creep on for many times the
-// iterations (measured: 16,253 on the 1D Laplacian of 3,000 unknowns).
+// iterations (measured: 16,253 on the 1D Laplacian of 3,000 unknowns). The second segment
+// starts a fresh direction: after the long first one the recursion has drifted too far
+// from the true residual for its direction to fit (measured: kept, 2,675 iterations on the
+// 3D P1 operator refined 7 times).
 constexpr double kReliableDelta = 0.01;
 constexpr double kRestartEta = 2e-5;
 constexpr int kMaxReplacements = 64;

@@ -779,8 +779,10 @@ __device__ void team_solve(Team& team, const BatchArgs& args, const BatchItem& i
                     ctl.scale[j] = (live && rn > 0.0 && ctl.rnorm[j] > 0.0) ? ctl.rnorm[j] / rn : 1.0;
                     ctl.inv[j] = live && rn > 0.0 ? (T)(1.0 / rn) : T(0);
                     ctl.rnorm[j] = live ? rn : 0.0;
-                    // a broken-down direction restarts, and so does every direction without reliable updates
-                    if ((ctl.broke >> j & 1) || !args.keep_dir) ctl.fresh |= 1 << j;
+                    // a broken-down direction restarts, and so does every direction without reliable
+                    // updates, and the direction of the long first segment: its recursion drifted too
+                    // far from the true residual for the direction to fit the replaced residual
+                    if ((ctl.broke >> j & 1) || !args.keep_dir || ctl.outer[j] <= 1) ctl.fresh |= 1 << j;
                 }
                 for (int j = kk; j < K; j++) { ctl.inv[j] = T(0); ctl.rnorm[j] = 0.0; }
                 ctl.broke = 0;
