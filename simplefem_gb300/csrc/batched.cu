@@ -162,13 +162,10 @@ int run_batch_results(cudaStream_t st, const std::vector<feec_system*>& systems,
     BatchArgs a{};
     a.systems = dviews; a.items = ditems; a.nitems = (int)items.size(); a.next_item = dnext; a.results = dres;
     a.precision = precision;
-    // reliable-update factor (FP32: replace the residual whenever z.r has fallen by its
-    // square; FP64: only when the target is reached); the autotuner's trials (max_outer > 0)
-    // run a fixed iteration count without replacements
-    const bool rb = method == FEEC_METHOD_RAINBOW;
-    a.inner_eta = (is_float && max_outer <= 0) ? (rb ? kReliableDelta : kRestartEta) : 1e-30;
-    a.first_eta = (is_float && max_outer <= 0) ? kRestartEta : 1e-30;
-    a.keep_dir = rb ? 1 : 0;
+    // segment factor (FP32: a fresh inner solve asks for a fall of kRestartEta or what the
+    // target still needs; FP64: only the target); the autotuner's trials (max_outer > 0) run
+    // a fixed iteration count in one segment
+    a.inner_eta = (is_float && max_outer <= 0) ? kRestartEta : 1e-30;
     a.err_control = (is_float && max_outer <= 0) ? 1 : 0;
     a.inner_margin = is_float ? 0.3 : 1.0;   // FP64 recursion tracks the true residual closely
     a.max_iter = max_iter;
@@ -614,9 +611,7 @@ int feec_batch_create(feec_batch** out, int nsys, feec_system* const* systems, i
     BatchArgs a{};
     a.systems = dviews; a.items = ditems; a.nitems = nsys; a.next_item = dnext; a.results = bt->dres;
     a.precision = precision;
-    a.inner_eta = is_float ? (method == FEEC_METHOD_RAINBOW ? kReliableDelta : kRestartEta) : 1e-30;
-    a.first_eta = is_float ? kRestartEta : 1e-30;
-    a.keep_dir = method == FEEC_METHOD_RAINBOW ? 1 : 0;
+    a.inner_eta = is_float ? kRestartEta : 1e-30;
     a.err_control = is_float ? 1 : 0;
     a.inner_margin = is_float ? 0.3 : 1.0;
     a.max_iter = max_iter > 0 ? max_iter : maxn;

@@ -43,24 +43,17 @@ struct BatchResult {
     double err_est;           // mixed: estimated relative error of x (-1: not estimated)
 };
 
-// Mixed precision, segment by segment. Multicolor SSOR-PCG uses reliable updates: the
-// FP32 recursion's residual is replaced by the FP64 true residual whenever its
-// preconditioned norm has fallen by kReliableDelta since the last replacement, and the
-// search direction is kept. Plain CG restarts instead (each segment a fresh FP32 solve to
-// a fall of kRestartEta): without a preconditioner the FP32 operator's rounding perturbs
-// each replaced residual too much for a kept direction (measured on the 3D P2 operator
-// refined 5 times: 4,757 iterations kept against 1,297 restarted). A column gets at most
-// kMaxReplacements replacements.
-// Every mixed solve's first segment asks for the full fall of kRestartEta, as one step of
-// plain defect correction does: an operator too ill-conditioned for FP32 arithmetic shows
-// there (its true residual gains less than half the digits) and is finished in FP64,
-// where short segments would let the FP32 recursion creep on for many times the
-// iterations (measured: 16,253 on the 1D Laplacian of 3,000 unknowns). The second segment
-// starts a fresh direction: after the long first one the recursion has drifted too far
-// from the true residual for its direction to fit (measured: kept, 2,675 iterations on the
-// 3D P1 operator refined 7 times).
-constexpr double kReliableDelta = 0.01;
+// Mixed precision, segment by segment: each segment is a fresh FP32 inner solve of the
+// residual equation to a fall of kRestartEta (or what the target still needs), after which
+// the FP64 true residual is recomputed (plain defect correction). The whole-GPU solver
+// keeps the multicolor SSOR-PCG's search direction across replacements after the first
+// segment (reliable updates) with segments of kReliableDelta: 3D P2 refined 5 times,
+// 39.2 ms against 46.5 restarted. The batched engine restarts: its columns run in
+// lockstep, and kept directions gained 2.5 % there. An operator too ill-conditioned for
+// FP32 arithmetic shows in the first segment (its true residual gains less than half the
+// digits asked) and is finished in FP64. A column gets at most kMaxReplacements segments.
 constexpr double kRestartEta = 2e-5;
+constexpr double kReliableDelta = 0.01;
 constexpr int kMaxReplacements = 64;
 
 struct BatchArgs {
@@ -70,9 +63,7 @@ struct BatchArgs {
     int* next_item;           // work queue head (zeroed before the launch)
     BatchResult* results;
     double precision;         // stop when ||b - A x|| <= precision ||b|| (FP64)
-    double inner_eta;         // segment factor (kReliableDelta / kRestartEta; 1e-30: only at the target)
-    double first_eta;         // segment factor of a column's first segment (kRestartEta in mixed precision)
-    int keep_dir;             // 1: keep the search direction across replacements (reliable updates)
+    double inner_eta;         // segment factor (kRestartEta; 1e-30: only the target)
     int err_control;          // 1: also stop only at the error bar (mixed precision)
     double inner_margin;      // a segment aims at margin * (the residual target)
     int max_iter;             // inner iterations per column, summed over all segments

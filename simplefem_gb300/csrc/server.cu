@@ -220,9 +220,7 @@ int serve_one(feec_server* srv, const Request& rq, cudaStream_t stream, feec_req
     BatchArgs a{};
     a.systems = dview; a.items = ditem; a.nitems = 1; a.next_item = nullptr; a.results = dres;
     a.precision = rq.precision;
-    a.inner_eta = is_float ? (rainbow ? kReliableDelta : kRestartEta) : 1e-30;
-    a.first_eta = is_float ? kRestartEta : 1e-30;
-    a.keep_dir = rainbow ? 1 : 0;
+    a.inner_eta = is_float ? kRestartEta : 1e-30;
     a.err_control = is_float ? 1 : 0;
     a.inner_margin = is_float ? 0.3 : 1.0;
     a.max_iter = rq.n;
@@ -254,7 +252,6 @@ int serve_one(feec_server* srv, const Request& rq, cudaStream_t stream, feec_req
         FEEC_TRY(cudaMemcpyAsync(ditem, &it, sizeof(it), cudaMemcpyHostToDevice, stream));
         FEEC_TRY(cudaMemsetAsync(dres, 0, sizeof(BatchResult), stream));
         a.inner_eta = 1e-30;
-        a.first_eta = 1e-30;
         a.err_control = 0;
         a.inner_margin = 1.0;
         a.max_iter = rq.n;

@@ -345,15 +345,11 @@ __device__ __forceinline__ void for_slices_dot(const Team& team, const SellView&
 template <typename T, int K>
 struct TeamControl {
     double bnorm2[K], relres[K], stall[K], rnorm[K], zr[K];
-    double zr_prev[K];   // rho of the previous iteration: the denominator of the last beta
-    double thr[K];       // the column asks for a residual replacement once zr < thr
+    double thr[K];       // the column's segment ends once zr < thr
     double amp[K];       // largest measured error-to-residual amplification of column j (0: none yet)
-    double scale[K];     // rnorm of the previous segment over rnorm of this one (direction rescaling)
     int iters[K], outer[K], status[K];
     T alpha[K], beta[K], inv[K];
     int err_step;    // bit j: column j met the residual bar but not yet the error bar
-    int fresh;       // bit j: column j starts a new direction (first segment or after a breakdown)
-    int broke;       // bit j: column j's last iteration broke down (its direction restarts)
     int done;        // bit j: column j finished (converged, failed or absent)
     int active;      // bit j: column j iterates in this segment
     int trig;        // bit j: column j asked for the residual replacement that ends the segment
@@ -361,23 +357,20 @@ struct TeamControl {
 };
 
 // ---------------------------------------------------------------------------
-// Mixed precision with reliable updates (residual replacement). The inner iteration runs
-// in T (FP32 in mixed precision) on the residual equation scaled to unit norm; the FP64
-// solution x and the FP64 true residual r64 = b - A x are kept beside it. A segment ends
-// when a column's preconditioned residual measure z.r has fallen by delta^2 since the
-// segment began (or far enough to meet its target): then the segment's correction is
-// added to x in FP64 (x += ||r64|| c), the true residual is recomputed in FP64, scaled to
-// unit norm and put in place of the recursive one — but the search direction is kept,
-// rescaled to the new scale, and beta is taken against the previous iteration's rho, so
-// the Krylov recurrence carries on instead of restarting (a restart per outer step, as
-// in plain defect correction, cost about half again as many iterations). The FP32
-// recursion cannot drift far from the true residual between replacements, and the
-// answer's accuracy is that of the FP64 residual.
+// Mixed precision: FP64 defect correction around FP32 inner solves. The FP64 solution x and
+// true residual r64 = b - A x are kept beside the inner iteration, which runs in T (FP32 in
+// mixed precision) on the residual equation scaled to unit norm, A c = r64 / ||r64||, from
+// c = 0 with a fresh Krylov recurrence. A segment ends when the column's preconditioned
+// residual measure z.r has fallen by the square of args.inner_eta or far enough for its
+// target; the correction is added to x in FP64 (x += ||r64|| c) and the true residual is
+// recomputed. (Reliable updates, keeping the direction across the replacement, gained 2.5 %
+// here at 1,216 columns in lockstep — any column's replacement ends every column's
+// segment — and are used by the whole-GPU single-system solver only.)
 // ---------------------------------------------------------------------------
 
 // Plain CG (ConjugateGradientSolverCSR, solver/sparsesolver.cpp:26-201) on the scaled
-// residual equation: the transform is r = r64 / ||r64|| (z = r); a fresh column starts
-// from d = 0, so its first d = r + beta d is r.
+// residual equation: the restart is r = r64 / ||r64|| (z = r), c = 0, and d = 0, so the first
+// d = r + beta d (beta = 0) is r.
 template <typename T, int K, typename Team>
 __device__ void cg_transform(Team& team, const SellView& S, TeamControl<T, K>& ctl, const double* r64, T* r, T* d,
                              T* c, double (&zr)[K]) {
@@ -390,14 +383,12 @@ __device__ void cg_transform(Team& team, const SellView& S, TeamControl<T, K>& c
     T inv[K];
     #pragma unroll
     for (int j = 0; j < K; j++) inv[j] = ctl.inv[j];
-    const int fresh = ctl.fresh;
     for (int i = team.tid(); i < n; i += team.nthreads()) {
         #pragma unroll
         for (int j = 0; j < K; j++) {
             const long long p = (long long)i * K + j;
             const T rv = (T)(r64[p] * (double)inv[j]);
-            r[p] = rv; c[p] = T(0);
-            if (fresh >> j & 1) d[p] = T(0);
+            r[p] = rv; c[p] = T(0); d[p] = T(0);
             arr[j] = AT::add(arr[j], rv * rv);
         }
     }
@@ -454,12 +445,8 @@ __device__ void cg_iterate(Team& team, const SellView& S, TeamControl<T, K>& ctl
                 T a = T(0);
                 if (act >> j & 1) {
                     const double zr = ctl.zr[j];
-                    if (!(dq[j] > 0.0) || !(zr >= 0.0) || !isfinite(dq[j]) || !isfinite(zr)) {
-                        act &= ~(1 << j);
-                        ctl.broke |= 1 << j;
-                    } else {
-                        a = (T)(zr / dq[j]);
-                    }
+                    if (!(dq[j] > 0.0) || !(zr >= 0.0) || !isfinite(dq[j]) || !isfinite(zr)) act &= ~(1 << j);
+                    else a = (T)(zr / dq[j]);
                 }
                 ctl.alpha[j] = a;
             }
@@ -493,10 +480,9 @@ __device__ void cg_iterate(Team& team, const SellView& S, TeamControl<T, K>& ctl
 // With sd = D (2 - w) / w, the reference's (2/w - 1) D equals sd. A direction update
 // d = z + beta d runs inside the backward sweep (a row's d is read only by the row itself).
 
-// The transform of a (new) residual: auxiliary = r64 / ||r64||, r = L-solve of it,
-// z = S r, c = 0; a fresh column also starts its direction, d = z. `init` (the first
-// segment): every work vector starts at 0, so rows the sweeps skip (D == 0) hold 0
-// wherever a gather reads them.
+// The restart of a segment: auxiliary = r64 / ||r64||, r = L-solve of it, z = S r, d = z,
+// c = 0. `init` (the first segment): every work vector starts at 0, so rows the sweeps skip
+// (D == 0) hold 0 wherever a gather reads them.
 template <typename T, int K, typename Team>
 __device__ void eis_transform(Team& team, const SellView& S, TeamControl<T, K>& ctl, const T* val, const T* wd,
                               const T* sd, const double* r64, T* r, T* d, T* z, T* m, T* q, T* c, bool init,
@@ -505,7 +491,6 @@ __device__ void eis_transform(Team& team, const SellView& S, TeamControl<T, K>& 
     using Acc = typename AT::type;
     const int n = S.n;
     const int lane = threadIdx.x & 31;
-    const int fresh = ctl.fresh;
     {
         T inv[K];
         #pragma unroll
@@ -532,22 +517,20 @@ __device__ void eis_transform(Team& team, const SellView& S, TeamControl<T, K>& 
                 p.w = p.act ? __ldg(&wd[p.row]) : T(0);
                 p.sdv = p.act ? __ldg(&sd[p.row]) : T(0);
                 load_row<T, K>(q, p.row, p.act, p.a);
-                if (fresh) load_row<T, K>(d, p.row, p.act, p.b);
                 return p;
             },
             [&](const SliceMeta&, const RowState<T, K>& p, const T (&sum)[K]) {
                 if (p.act && p.w != T(0)) {
-                    T rv[K], zv[K], dv[K];
+                    T rv[K], zv[K];
                     #pragma unroll
                     for (int j = 0; j < K; j++) {
                         rv[j] = (p.a[j] - sum[j]) * p.w;
                         zv[j] = rv[j] * p.sdv;
                         azr[j] = AT::add(azr[j], zv[j] * rv[j]);
-                        dv[j] = (fresh >> j & 1) ? zv[j] : p.b[j];
                     }
                     store_row<T, K>(r, p.row, rv);
                     store_row<T, K>(z, p.row, zv);
-                    if (fresh) store_row<T, K>(d, p.row, dv);
+                    store_row<T, K>(d, p.row, zv);
                 }
             });
         team.sync();
@@ -556,7 +539,7 @@ __device__ void eis_transform(Team& team, const SellView& S, TeamControl<T, K>& 
 }
 
 // One iteration for the active columns. `update_d`: the backward sweep first forms
-// d = z + beta d (skipped when every active column is fresh: the transform set d = z).
+// d = z + beta d (not in a segment's first iteration, whose d = z the restart set).
 template <typename T, int K, typename Team>
 __device__ void eis_iterate(Team& team, const SellView& S, TeamControl<T, K>& ctl, const T* val, const T* wd,
                             const T* sd, T* r, T* d, T* z, T* m, T* q, T* c, bool update_d, double (&zr_new)[K]) {
@@ -631,12 +614,8 @@ __device__ void eis_iterate(Team& team, const SellView& S, TeamControl<T, K>& ct
                 T a = T(0);
                 if (act >> j & 1) {
                     const double zr = ctl.zr[j];
-                    if (!(dq[j] > 0.0) || !(zr >= 0.0) || !isfinite(dq[j]) || !isfinite(zr)) {
-                        act &= ~(1 << j);
-                        ctl.broke |= 1 << j;
-                    } else {
-                        a = (T)(zr / dq[j]);
-                    }
+                    if (!(dq[j] > 0.0) || !(zr >= 0.0) || !isfinite(dq[j]) || !isfinite(zr)) act &= ~(1 << j);
+                    else a = (T)(zr / dq[j]);
                 }
                 ctl.alpha[j] = a;
             }
@@ -711,11 +690,11 @@ __device__ void team_solve(Team& team, const BatchArgs& args, const BatchItem& i
             for (int j = 0; j < K; j++) {
                 ctl.bnorm2[j] = o[j];
                 ctl.iters[j] = 0; ctl.outer[j] = 0; ctl.status[j] = FEEC_MAXITER; ctl.relres[j] = -1.0;
-                ctl.stall[j] = 0.0; ctl.amp[j] = 0.0; ctl.rnorm[j] = 0.0; ctl.scale[j] = 1.0; ctl.zr_prev[j] = 1.0;
+                ctl.stall[j] = 0.0; ctl.amp[j] = 0.0; ctl.rnorm[j] = 0.0;
                 ctl.beta[j] = T(0);
                 if (j >= kk) ctl.done |= 1 << j;
             }
-            ctl.err_step = 0; ctl.fresh = (1 << K) - 1; ctl.broke = 0; ctl.trig = 0;
+            ctl.err_step = 0; ctl.trig = 0;
         }
     }
     // Error control (mixed precision): a correction approximates the error of the iterate it
@@ -725,7 +704,6 @@ __device__ void team_solve(Team& team, const BatchArgs& args, const BatchItem& i
     // target is sized for both bars.
     const double err_target = kErrorPerResidual * args.precision;
     const double delta2 = args.inner_eta * args.inner_eta;   // segment factor, squared
-    const double first2 = args.first_eta * args.first_eta;   // ... of a column's first segment
 
     for (int seg = 0; ; seg++) {
         // ---- FP64 true residual r64 = b - A x and its norm ----
@@ -775,27 +753,19 @@ __device__ void team_solve(Team& team, const BatchArgs& args, const BatchItem& i
                     }
                     ctl.relres[j] = rel;
                     const bool live = !(done >> j & 1);
-                    // direction rescaling to the new scale, folded into the next beta
-                    ctl.scale[j] = (live && rn > 0.0 && ctl.rnorm[j] > 0.0) ? ctl.rnorm[j] / rn : 1.0;
                     ctl.inv[j] = live && rn > 0.0 ? (T)(1.0 / rn) : T(0);
                     ctl.rnorm[j] = live ? rn : 0.0;
-                    // a broken-down direction restarts, and so does every direction without reliable
-                    // updates, and the direction of the long first segment: its recursion drifted too
-                    // far from the true residual for the direction to fit the replaced residual
-                    if ((ctl.broke >> j & 1) || !args.keep_dir || ctl.outer[j] <= 1) ctl.fresh |= 1 << j;
                 }
                 for (int j = kk; j < K; j++) { ctl.inv[j] = T(0); ctl.rnorm[j] = 0.0; }
-                ctl.broke = 0;
                 ctl.trig = 0;
                 ctl.done = done;
-                ctl.fresh &= ~done;
                 ctl.all_done = done == (1 << K) - 1;
             }
         }
         __syncthreads();
         if (ctl.all_done) break;
 
-        // ---- transform the new residual; beta against the previous rho (kept direction) ----
+        // ---- restart the inner iteration on the new residual ----
         {
             double zr[K];
             if constexpr (RAINBOW)
@@ -806,10 +776,7 @@ __device__ void team_solve(Team& team, const BatchArgs& args, const BatchItem& i
                 const int done = ctl.done;
                 for (int j = 0; j < K; j++) {
                     const bool live = !(done >> j & 1);
-                    T b = T(0);
-                    if (live && !(ctl.fresh >> j & 1) && ctl.zr_prev[j] > 0.0)
-                        b = (T)(zr[j] / (ctl.zr_prev[j] * ctl.scale[j]));
-                    ctl.beta[j] = b;
+                    ctl.beta[j] = T(0);
                     ctl.zr[j] = zr[j];
                     // the segment ends once z.r has fallen by delta^2 or far enough for the target
                     // (the residual bar and, once an amplification is known, the error bar),
@@ -822,8 +789,7 @@ __device__ void team_solve(Team& team, const BatchArgs& args, const BatchItem& i
                     }
                     const double rn = ctl.rnorm[j];
                     const double need = rn > 0.0 ? args.inner_margin * target / rn : 0.0;
-                    const double seg_f = ctl.outer[j] == 0 ? first2 : delta2;
-                    const double f = need * need > seg_f ? need * need : seg_f;
+                    const double f = need * need > delta2 ? need * need : delta2;
                     ctl.thr[j] = live ? zr[j] * f : 0.0;
                     // the next true residual must gain at least half the digits z.r promised
                     ctl.stall[j] = rn * sqrt(sqrt(f > 0.0 ? f : 1.0));
@@ -833,11 +799,8 @@ __device__ void team_solve(Team& team, const BatchArgs& args, const BatchItem& i
         }
         __syncthreads();
 
-        // ---- iterate until a column asks for a replacement ----
-        // a fresh column's d = z was set by the transform; the others form d = z + beta d in
-        // the first backward sweep (fresh columns then have beta = 0 and d = z: the same d)
-        bool update_d = true;
-        if constexpr (RAINBOW) update_d = (ctl.fresh & ctl.active) != ctl.active;
+        // ---- iterate until a column's segment ends (the restart set d = z) ----
+        bool update_d = false;
         while (true) {
             double zr_new[K];
             if constexpr (RAINBOW)
@@ -845,27 +808,26 @@ __device__ void team_solve(Team& team, const BatchArgs& args, const BatchItem& i
             else
                 cg_iterate<T, K>(team, S, ctl, val, r, d, q, c, zr_new);
             update_d = true;
+            // a column whose z.r met its threshold (or whose budget ran out, or that broke
+            // down) stops iterating; the segment ends when every column has stopped
             if (leader) {
-                ctl.fresh = 0;   // every thread read it before the iteration's barriers
                 const int was = ctl.active;
-                int trig = 0;
+                int act = was;
                 for (int j = 0; j < K; j++) {
                     T b = T(0);
                     if (was >> j & 1) {
                         b = (T)(zr_new[j] / ctl.zr[j]);
-                        ctl.zr_prev[j] = ctl.zr[j];
                         ctl.zr[j] = zr_new[j];
                         ctl.iters[j]++;
-                        if (!(zr_new[j] >= ctl.thr[j]) || ctl.iters[j] >= args.max_iter) trig |= 1 << j;
-                    } else if (!(ctl.done >> j & 1)) {
-                        trig |= 1 << j;   // broke down: replace its residual and restart its direction
+                        if (!(zr_new[j] >= ctl.thr[j]) || ctl.iters[j] >= args.max_iter) act &= ~(1 << j);
                     }
+                    if (!(act >> j & 1) && !(ctl.done >> j & 1)) ctl.trig |= 1 << j;
                     ctl.beta[j] = b;
                 }
-                ctl.trig = trig;
+                ctl.active = act;
             }
             __syncthreads();
-            if (ctl.trig) break;
+            if (!ctl.active) break;
             team.sync();
         }
 
