@@ -36,7 +36,7 @@ WORKLOAD_NAME = "3D P2 Lagrange stiffness+mass, unit cube (6 tets) refined 5x: N
                 "Rainbow SSOR-PCG omega=1.0, x0=0, b~U[-1,1] seeded, 1e-10 true relative residual"
 METRIC = "solves/s at 1e-10 rel. residual (3D P2 L5, Rainbow SSOR-PCG), mixed FP32/FP64"
 PRECISION = 1e-10
-DRAM_OVER_ALGORITHMIC_K4_T512 = 0.901
+DRAM_OVER_ALGORITHMIC_L5_K4_T512 = None   # set from the full-size capture
 
 
 def max_over_ranks(x, device=None):
@@ -742,34 +742,41 @@ def run_ours(args):
     outer_team_b = 12 * nnz + 4 * (n + 1) + 4 * (nnz - n) + 4 * (n + 1)
     outer_col_b = 96 * n
     per_step_bytes = 0
+    shared_bytes = 0      # the same with the operator counted once per iteration of the whole batch
     for infos in infos_all:
         its = [i["iterations"] for i in infos]
         outs = [i["outer_iterations"] for i in infos]
         for t0 in range(teams):
             cols = range(t0 * K_TEAM, min(B_RHS, (t0 + 1) * K_TEAM))
             team_it = max(its[j] for j in cols)
-            per_step_bytes += team_it * mat_b + sum(its[j] for j in cols) * vec_b
-            per_step_bytes += (max(outs[j] for j in cols) + 1) * outer_team_b + \
-                sum(outs[j] + 1 for j in cols) * outer_col_b
+            vec_outer = sum(its[j] for j in cols) * vec_b + sum(outs[j] + 1 for j in cols) * outer_col_b
+            per_step_bytes += team_it * mat_b + (max(outs[j] for j in cols) + 1) * outer_team_b + vec_outer
+            shared_bytes += vec_outer
+        shared_bytes += max(its) * mat_b + (max(outs) + 1) * outer_team_b
     per_step_bytes /= len(infos_all)
+    shared_bytes /= len(infos_all)
     peak, peak_kind = measured_peaks()
     achieved = per_step_bytes / (total_ms / args.steps / 1000.0) / 1e9
+    achieved_shared = shared_bytes / (total_ms / args.steps / 1000.0) / 1e9
     if tuned["team_blocks"] > 1:
         kernel_name = f"cluster_batched_kernel<float,{K_TEAM},true> ({tuned['team_blocks']}-block clusters)"
     else:
         kernel_name = f"batched_solve_kernel<float,{K_TEAM},true,{tuned['team_threads']}>"
-    # DRAM traffic of this kernel configuration from one ncu capture (dram__bytes_read.sum +
-    # dram__bytes_write.sum) on the operator refined 4x (profiles/batched_solve_3d_p2_l4.md):
-    # 0.901 x its algorithmic bytes; a full-size launch (about 2.6 s) is not captured, so the
-    # traffic of this launch is that ratio times its algorithmic bytes
+    # DRAM traffic of this kernel configuration from one full-size ncu capture (one pass:
+    # dram__bytes_read.sum + dram__bytes_write.sum; profiles/batched_solve_3d_p2_l5.md), as a
+    # ratio to the algorithmic bytes of the captured launch, applied to this launch
     traffic = None
-    if (K_TEAM, tuned["team_threads"], tuned["team_blocks"]) == (4, 512, 1) and DRAM_OVER_ALGORITHMIC_K4_T512:
-        traffic = DRAM_OVER_ALGORITHMIC_K4_T512 * per_step_bytes
+    if (K_TEAM, tuned["team_threads"], tuned["team_blocks"]) == (4, 512, 1) and DRAM_OVER_ALGORITHMIC_L5_K4_T512:
+        traffic = DRAM_OVER_ALGORITHMIC_L5_K4_T512 * per_step_bytes
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": traffic, "kernel": kernel_name, "launches_per_step": 1,
-                "traffic_source": "ncu DRAM bytes / algorithmic bytes = 0.901 measured on the 4x-refined operator "
-                                  "(profiles/batched_solve_3d_p2_l4.md), applied to this launch" if traffic else None,
+                "traffic_source": f"ncu DRAM bytes / algorithmic bytes = {DRAM_OVER_ALGORITHMIC_L5_K4_T512} measured "
+                                  "on this workload (profiles/batched_solve_3d_p2_l5.md), applied to this launch"
+                                  if traffic else None,
                 "bytes_per_launch": per_step_bytes, "ms_per_launch": total_ms / args.steps,
+                "shared_operator": {"bytes_per_launch": shared_bytes, "achieved": achieved_shared,
+                                    "frac": achieved_shared / peak,
+                                    "note": "operator counted once per iteration of the whole batch"},
                 "peak_kind": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)"}
 
     # ---------------- e2e: pinned host B -> device, batched solve, device X -> pinned host ----------------
