@@ -731,14 +731,14 @@ def run_ours(args):
     # roofline of the batched kernel: algorithmic bytes over its event-timed duration. The
     # Rainbow inner solve is Eisenstat's formulation: per team iteration the strict lower and
     # strict upper parts are read once (FP32 value + int32 column) with two sweeps' row
-    # bounds, plus 5 per-row FP32 factors (wd three times, sd twice); per right-hand side and
-    # iteration 16 FP32 vector streams (backward: d, z in, d, m out, m gathered; forward:
-    # d, m in, q out, q gathered; update: c, m, q, r in, c, r, z out). Per outer step: the
+    # bounds, plus 6 per-row FP32 factors (wd and sd three times each); per right-hand side
+    # and iteration 15 FP32 vector streams (backward: d, r in, d, m out, m gathered;
+    # forward: d, m in, q out, q gathered; update: c, m, q, r in, c, r out). Per segment: the
     # FP64 residual (whole matrix, FP64) and the L-solve of the restart per team, and 96
     # bytes per row and right-hand side (residual 24, restart 32, L-solve 20, x update 20).
     teams = (B_RHS + K_TEAM - 1) // K_TEAM
-    mat_b = 8 * (nnz - n) + 8 * (n + 1) + 5 * 4 * n
-    vec_b = 16 * 4 * n
+    mat_b = 8 * (nnz - n) + 8 * (n + 1) + 6 * 4 * n
+    vec_b = 15 * 4 * n
     outer_team_b = 12 * nnz + 4 * (n + 1) + 4 * (nnz - n) + 4 * (n + 1)
     outer_col_b = 96 * n
     per_step_bytes = 0

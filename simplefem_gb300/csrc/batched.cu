@@ -151,9 +151,8 @@ int run_batch_results(cudaStream_t st, const std::vector<feec_system*>& systems,
         for (int j = 0; j < kBatchMaxK; j++) { it.b[j] = jb.b[j]; it.x[j] = jb.x[j]; }
         FEEC_TRY(tmp.alloc(it.xp, len)); FEEC_TRY(tmp.alloc(it.bp, len)); FEEC_TRY(tmp.alloc(it.r64, len));
         char* w = nullptr;
-        FEEC_TRY(tmp.alloc(w, 6 * len * tsz));
-        it.r = w; it.d = w + len * tsz; it.z = w + 2 * len * tsz; it.m = w + 3 * len * tsz; it.q = w + 4 * len * tsz;
-        it.c = w + 5 * len * tsz;
+        FEEC_TRY(tmp.alloc(w, 5 * len * tsz));
+        it.r = w; it.d = w + len * tsz; it.m = w + 2 * len * tsz; it.q = w + 3 * len * tsz; it.c = w + 4 * len * tsz;
     }
     FEEC_TRY(cudaMemcpyAsync(dviews, views.data(), sizeof(SellView) * views.size(), cudaMemcpyHostToDevice, st));
     FEEC_TRY(cudaMemcpyAsync(ditems, items.data(), sizeof(BatchItem) * items.size(), cudaMemcpyHostToDevice, st));
@@ -601,9 +600,8 @@ int feec_batch_create(feec_batch** out, int nsys, feec_system* const* systems, i
         it.b[0] = b[i]; it.x[0] = x[i];
         FEEC_TRY(M.alloc(it.xp, len)); FEEC_TRY(M.alloc(it.bp, len)); FEEC_TRY(M.alloc(it.r64, len));
         char* w = nullptr;
-        FEEC_TRY(M.alloc(w, 6 * len * tsz));
-        it.r = w; it.d = w + len * tsz; it.z = w + 2 * len * tsz; it.m = w + 3 * len * tsz; it.q = w + 4 * len * tsz;
-        it.c = w + 5 * len * tsz;
+        FEEC_TRY(M.alloc(w, 5 * len * tsz));
+        it.r = w; it.d = w + len * tsz; it.m = w + 2 * len * tsz; it.q = w + 3 * len * tsz; it.c = w + 4 * len * tsz;
     }
     FEEC_TRY(cudaMemcpyAsync(dviews, views.data(), sizeof(SellView) * views.size(), cudaMemcpyHostToDevice, bt->stream));
     FEEC_TRY(cudaMemcpyAsync(ditems, items.data(), sizeof(BatchItem) * items.size(), cudaMemcpyHostToDevice, bt->stream));

@@ -33,7 +33,7 @@ struct BatchItem {
     const double* b[kBatchMaxK];   // caller right-hand sides (caller numbering)
     double* x[kBatchMaxK];         // caller solutions (caller numbering; in: initial guess)
     double* xp; double* bp; double* r64;                 // n*K FP64 workspace
-    void* r; void* d; void* z; void* m; void* q; void* c;  // n*K inner workspace (float or double)
+    void* r; void* d; void* m; void* q; void* c;  // n*K inner workspace (float or double)
 };
 
 struct BatchResult {

@@ -205,10 +205,9 @@ int serve_one(feec_server* srv, const Request& rq, cudaStream_t stream, feec_req
     FEEC_TRY(mem.alloc(b, n)); FEEC_TRY(mem.alloc(x, n));
     BatchItem it{};
     FEEC_TRY(mem.alloc(it.xp, n)); FEEC_TRY(mem.alloc(it.bp, n)); FEEC_TRY(mem.alloc(it.r64, n));
-    FEEC_TRY(mem.alloc(w, 6 * n * tsz));
+    FEEC_TRY(mem.alloc(w, 5 * n * tsz));
     FEEC_TRY(mem.alloc(dview, 1)); FEEC_TRY(mem.alloc(ditem, 1)); FEEC_TRY(mem.alloc(dres, 1));
-    it.r = w; it.d = w + n * tsz; it.z = w + 2 * n * tsz; it.m = w + 3 * n * tsz; it.q = w + 4 * n * tsz;
-    it.c = w + 5 * n * tsz;
+    it.r = w; it.d = w + n * tsz; it.m = w + 2 * n * tsz; it.q = w + 3 * n * tsz; it.c = w + 4 * n * tsz;
     it.system = 0; it.nrhs = 1; it.first_result = 0;
     it.b[0] = b; it.x[0] = x;
     const SellView view = sell_view(s, rainbow ? FEEC_METHOD_RAINBOW : FEEC_METHOD_CG);
@@ -246,9 +245,9 @@ int serve_one(feec_server* srv, const Request& rq, cudaStream_t stream, feec_req
         // finish in FP64 from the current iterate on the device; the workspace grows to FP64
         // within the bytes the admission estimate counted for this request.
         char* w64 = nullptr;
-        FEEC_TRY(mem.alloc(w64, 6 * n * sizeof(double)));
+        FEEC_TRY(mem.alloc(w64, 5 * n * sizeof(double)));
         const size_t d = n * sizeof(double);
-        it.r = w64; it.d = w64 + d; it.z = w64 + 2 * d; it.m = w64 + 3 * d; it.q = w64 + 4 * d; it.c = w64 + 5 * d;
+        it.r = w64; it.d = w64 + d; it.m = w64 + 2 * d; it.q = w64 + 3 * d; it.c = w64 + 4 * d;
         FEEC_TRY(cudaMemcpyAsync(ditem, &it, sizeof(it), cudaMemcpyHostToDevice, stream));
         FEEC_TRY(cudaMemsetAsync(dres, 0, sizeof(BatchResult), stream));
         a.inner_eta = 1e-30;

@@ -476,7 +476,9 @@ __device__ void cg_iterate(Team& team, const SellView& S, TeamControl<T, K>& ctl
 // an iteration is one backward and one forward sweep over the strict parts — no SpMV
 // over full rows — so each stored entry is read and gathered once per iteration instead
 // of twice. Vectors (interleaved [row][K]): r = L-solved residual, d = direction,
-// z = S r, m = technical (backward sweep), q = auxiliary (forward sweep), c = solution.
+// m = technical (backward sweep), q = auxiliary (forward sweep), c = solution. z = S r is
+// not stored: the backward sweep forms it from r and the row factor (one FP32 vector
+// stream less per column and iteration).
 // With sd = D (2 - w) / w, the reference's (2/w - 1) D equals sd. A direction update
 // d = z + beta d runs inside the backward sweep (a row's d is read only by the row itself).
 
@@ -485,7 +487,7 @@ __device__ void cg_iterate(Team& team, const SellView& S, TeamControl<T, K>& ctl
 // (D == 0) hold 0 wherever a gather reads them.
 template <typename T, int K, typename Team>
 __device__ void eis_transform(Team& team, const SellView& S, TeamControl<T, K>& ctl, const T* val, const T* wd,
-                              const T* sd, const double* r64, T* r, T* d, T* z, T* m, T* q, T* c, bool init,
+                              const T* sd, const double* r64, T* r, T* d, T* m, T* q, T* c, bool init,
                               double (&zr)[K]) {
     using AT = AccT<T>;
     using Acc = typename AT::type;
@@ -501,7 +503,7 @@ __device__ void eis_transform(Team& team, const SellView& S, TeamControl<T, K>& 
                 const long long p = (long long)i * K + j;
                 q[p] = (T)(r64[p] * (double)inv[j]);
                 c[p] = T(0);
-                if (init) { r[p] = T(0); d[p] = T(0); z[p] = T(0); m[p] = T(0); }
+                if (init) { r[p] = T(0); d[p] = T(0); m[p] = T(0); }
             }
         }
     }
@@ -529,7 +531,6 @@ __device__ void eis_transform(Team& team, const SellView& S, TeamControl<T, K>& 
                         azr[j] = AT::add(azr[j], zv[j] * rv[j]);
                     }
                     store_row<T, K>(r, p.row, rv);
-                    store_row<T, K>(z, p.row, zv);
                     store_row<T, K>(d, p.row, zv);
                 }
             });
@@ -542,7 +543,7 @@ __device__ void eis_transform(Team& team, const SellView& S, TeamControl<T, K>& 
 // d = z + beta d (not in a segment's first iteration, whose d = z the restart set).
 template <typename T, int K, typename Team>
 __device__ void eis_iterate(Team& team, const SellView& S, TeamControl<T, K>& ctl, const T* val, const T* wd,
-                            const T* sd, T* r, T* d, T* z, T* m, T* q, T* c, bool update_d, double (&zr_new)[K]) {
+                            const T* sd, T* r, T* d, T* m, T* q, T* c, bool update_d, double (&zr_new)[K]) {
     using AT = AccT<T>;
     using Acc = typename AT::type;
     const int n = S.n;
@@ -560,7 +561,10 @@ __device__ void eis_iterate(Team& team, const SellView& S, TeamControl<T, K>& ct
                     p.row = M.row0 + lane; p.act = lane < M.nrow;
                     p.w = p.act ? __ldg(&wd[p.row]) : T(0);
                     load_row<T, K>(d, p.row, p.act, p.a);
-                    if (update_d) load_row<T, K>(z, p.row, p.act, p.b);
+                    if (update_d) {
+                        p.sdv = p.act ? __ldg(&sd[p.row]) : T(0);
+                        load_row<T, K>(r, p.row, p.act, p.b);
+                    }
                     return p;
                 },
                 [&](const SliceMeta&, const RowState<T, K>& p, const T (&sum)[K]) {
@@ -568,7 +572,7 @@ __device__ void eis_iterate(Team& team, const SellView& S, TeamControl<T, K>& ct
                         T dv[K], mv[K];
                         #pragma unroll
                         for (int j = 0; j < K; j++) {
-                            dv[j] = update_d ? p.b[j] + beta[j] * p.a[j] : p.a[j];
+                            dv[j] = update_d ? p.b[j] * p.sdv + beta[j] * p.a[j] : p.a[j];
                             mv[j] = (dv[j] - sum[j]) * p.w;
                         }
                         if (update_d) store_row<T, K>(d, p.row, dv);
@@ -624,7 +628,7 @@ __device__ void eis_iterate(Team& team, const SellView& S, TeamControl<T, K>& ct
     }
     __syncthreads();
     Acc azr[K];
-    {   // update: c += alpha technical, r -= alpha (auxiliary + technical), z = S r, z.r
+    {   // update: c += alpha technical, r -= alpha (auxiliary + technical), z.r with z = S r
         T alpha[K];
         #pragma unroll
         for (int j = 0; j < K; j++) { alpha[j] = ctl.alpha[j]; azr[j] = AT::zero(); }
@@ -646,7 +650,6 @@ __device__ void eis_iterate(Team& team, const SellView& S, TeamControl<T, K>& ct
             }
             store_row<T, K>(c, i, cv);
             store_row<T, K>(r, i, rv);
-            store_row<T, K>(z, i, zv);
         }
     }
     team.template sum<T, K>(azr, zr_new);
@@ -663,7 +666,7 @@ __device__ void team_solve(Team& team, const BatchArgs& args, const BatchItem& i
     const T* wd = sel_wd<T>(S);
     const T* sd = sel_sd<T>(S);
     double* xp = it.xp; double* bp = it.bp; double* r64 = it.r64;
-    T* r = (T*)it.r; T* d = (T*)it.d; T* z = (T*)it.z; T* m = (T*)it.m; T* q = (T*)it.q; T* c = (T*)it.c;
+    T* r = (T*)it.r; T* d = (T*)it.d; T* m = (T*)it.m; T* q = (T*)it.q; T* c = (T*)it.c;
     __shared__ TeamControl<T, K> ctl;
     const bool leader = threadIdx.x == 0;
 
@@ -769,7 +772,7 @@ __device__ void team_solve(Team& team, const BatchArgs& args, const BatchItem& i
         {
             double zr[K];
             if constexpr (RAINBOW)
-                eis_transform<T, K>(team, S, ctl, val, wd, sd, r64, r, d, z, m, q, c, seg == 0, zr);
+                eis_transform<T, K>(team, S, ctl, val, wd, sd, r64, r, d, m, q, c, seg == 0, zr);
             else
                 cg_transform<T, K>(team, S, ctl, r64, r, d, c, zr);
             if (leader) {
@@ -804,7 +807,7 @@ __device__ void team_solve(Team& team, const BatchArgs& args, const BatchItem& i
         while (true) {
             double zr_new[K];
             if constexpr (RAINBOW)
-                eis_iterate<T, K>(team, S, ctl, val, wd, sd, r, d, z, m, q, c, update_d, zr_new);
+                eis_iterate<T, K>(team, S, ctl, val, wd, sd, r, d, m, q, c, update_d, zr_new);
             else
                 cg_iterate<T, K>(team, S, ctl, val, r, d, q, c, zr_new);
             update_d = true;
