@@ -36,7 +36,7 @@ WORKLOAD_NAME = "3D P2 Lagrange stiffness+mass, unit cube (6 tets) refined 5x: N
                 "Rainbow SSOR-PCG omega=1.0, x0=0, b~U[-1,1] seeded, 1e-10 true relative residual"
 METRIC = "solves/s at 1e-10 rel. residual (3D P2 L5, Rainbow SSOR-PCG), mixed FP32/FP64"
 PRECISION = 1e-10
-DRAM_OVER_ALGORITHMIC_L5_K4_T512 = 1.316   # profiles/batched_solve_3d_p2_l5.md
+DRAM_OVER_ALGORITHMIC_L5_K4_T512 = 1.304   # profiles/batched_solve_3d_p2_l5.md
 
 
 def max_over_ranks(x, device=None):
