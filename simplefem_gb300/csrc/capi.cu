@@ -409,6 +409,16 @@ int solve_core(feec_system* s, int method, int mode, double* xx, const double* b
         double amp = 0.0;                // largest measured amplification (segments after the first)
         bool err_step = false;           // the residual bar is met, the error bar not yet
         bool have_dir = false;           // a search direction to keep from the last segment
+        bool keep_live = keep_dirs;      // cleared once a kept direction stops paying
+        // Iterations per decade of z.r fall of the restarted segments (the largest seen). A
+        // kept direction stays consistent with the replaced residual only while the FP32
+        // recursion's drift within a segment is small against that residual; on operators
+        // whose condition number times the FP32 unit roundoff nears 1e-2 it is not, and the
+        // kept segments slow down without bound (2D P1 refined 10 times: 0.7 k, 1.1 k, 14 k,
+        // 60 k, 258 k iterations for the same 0.01 fall). A kept segment is therefore given
+        // at most kKeptSegmentSlack times the restarted rate for its fall; one that runs out
+        // ends there, and every later segment restarts.
+        double restart_rate = 0.0;
         double zr_prev = 0.0, rn_prev = 0.0;
         for (outer = 0; outer < max_outer; outer++) {
             st = true_residual(s, s->b, s->x, s->r, rn2, permuted);
@@ -453,6 +463,12 @@ int solve_core(feec_system* s, int method, int mode, double* xx, const double* b
             const double need = 0.3 * target / rn;
             const double f = std::max(outer == 0 ? first2 : delta2, need * need);
             stall_limit = rn * std::sqrt(std::sqrt(f));
+            const double decades = std::max(1.0, -std::log10(f));
+            int seg_budget = max_iter - K_total;
+            if (have_dir && restart_rate > 0.0) {
+                const double cap = kKeptSegmentSlack * restart_rate * decades + 32.0;
+                if (cap < (double)seg_budget) seg_budget = (int)cap;
+            }
             float ms = 0.0f;
             FEEC_TRY(reset_status(s));
             FEEC_TRY(cudaEventRecord(s->ev0, s->stream));
@@ -461,7 +477,7 @@ int solve_core(feec_system* s, int method, int mode, double* xx, const double* b
                 a.n = n; a.rp = s->A; a.ci = s->C; a.val = s->V32; a.b = s->b32; a.x = s->x32; a.r = s->r32;
                 a.d = s->d32; a.q = s->q32;
                 a.tol2 = f;                       // r starts at unit norm: a relative fall of f in r.r
-                a.max_iter = max_iter - K_total;
+                a.max_iter = seg_budget;
                 a.partials = s->partials; a.st = s->st;
                 a.keep_dir = have_dir ? 1 : 0; a.zr_prev = zr_prev; a.scale = scale;
                 FEEC_TRY(launch_cg<float>(a, shape, s->stream));
@@ -479,7 +495,7 @@ int solve_core(feec_system* s, int method, int mode, double* xx, const double* b
                 a.guard_restart = a.guard_iter = s->zero_diag_rows > 0;
                 a.use_zr_rule = 0;
                 a.rr_stop = f;
-                a.max_iter = max_iter - K_total;
+                a.max_iter = seg_budget;
                 a.keep_dir = have_dir ? 1 : 0; a.zr_prev = zr_prev; a.scale = scale;
                 FEEC_TRY(launch_eisenstat<float>(a, shape, s->stream));
             }
@@ -500,10 +516,19 @@ int solve_core(feec_system* s, int method, int mode, double* xx, const double* b
                 amp = std::max(amp, std::sqrt(norms2[0] / norms2[1]) / relres);
             if (hs.status == FEEC_TIMEOUT) { status = FEEC_TIMEOUT; break; }
             if (hs.status == FEEC_BREAKDOWN && hs.iterations == 0) { status = FEEC_BREAKDOWN; break; }
+            if (!have_dir && hs.status == FEEC_OK && hs.iterations > 0)
+                restart_rate = std::max(restart_rate, hs.iterations / decades);
+            if (have_dir && hs.status == FEEC_MAXITER && hs.iterations >= seg_budget &&
+                seg_budget < max_iter - (K_total - hs.iterations)) {
+                // a kept segment that ran out of its share: restart from here on; its true
+                // residual only has to fall (it did not reach the fall it was asked for)
+                keep_live = false;
+                stall_limit = rn;
+            }
             // a breakdown or an empty segment restarts the direction next time
             // (and the long first segment's direction, whose recursion drifted too far from the
             // true residual to fit the replaced one)
-            have_dir = keep_dirs && outer > 0 && hs.status == FEEC_OK && hs.iterations > 0;
+            have_dir = keep_live && outer > 0 && hs.status == FEEC_OK && hs.iterations > 0;
             zr_prev = hs.extra[0];
             rn_prev = rn;
         }

@@ -54,6 +54,9 @@ struct BatchResult {
 // digits asked) and is finished in FP64. A column gets at most kMaxReplacements segments.
 constexpr double kRestartEta = 2e-5;
 constexpr double kReliableDelta = 0.01;
+// A kept-direction segment may take this many times the iterations per decade of z.r fall
+// that the restarted segments of the same solve took (the whole-GPU solver).
+constexpr double kKeptSegmentSlack = 2.0;
 constexpr int kMaxReplacements = 64;
 
 struct BatchArgs {

@@ -134,3 +134,30 @@ def test_mixed_block_64_rhs_2d_p2_l7_meets_error_bar(cuda):
     for j in (0, 31, 63):
         _check(Xh[j], Bh[j], ops, infos[j], ("block column", j))
     sysm.close()
+
+
+def test_mixed_kept_directions_stay_bounded_on_ill_conditioned_operator(cuda):
+    """2D P1 refined 10 times (N = 1,050,625; condition number x FP32 roundoff near 1e-2) at a
+    request of 1e-12 on one block per SM: kept-direction FP32 segments slow down without bound
+    here (one such solve took 426,392 iterations), so each gets a bounded share of the
+    restarted rate and the solve restarts once one runs out. The whole mixed solve must stay
+    within 5x the FP64 solve's iterations (it takes about 3x) and meet the residual and error
+    bars."""
+    torch = cuda
+    from simplefem_gb300 import workloads
+    sysm, ops = _system(2, 1, 10, 1)
+    n = sysm.n
+    b = workloads.uniform_vector(1429455515942280814, n)
+    bd = torch.from_numpy(b).cuda()
+    sysm.set_launch(torch.cuda.get_device_properties(0).multi_processor_count, 0)
+    x = torch.zeros(n, dtype=torch.float64, device="cuda")
+    info = sysm.solve(bd, x, method="rainbow", mode="mixed", precision=1e-12, max_iter=50000)   # bounds the test's time
+    sysm.set_launch(0, 0)
+    x64 = torch.zeros(n, dtype=torch.float64, device="cuda")
+    info64 = sysm.solve(bd, x64, method="rainbow", mode="fp64", precision=1e-12)
+    assert info["status"] == 0 and info["true_relres"] <= 1e-12, info
+    assert info["iterations"] <= 5 * info64["iterations"], (info["iterations"], info64["iterations"])
+    # the FP64 solve at 1e-12 is within about 3e-11 of the solution (amplification ~30)
+    err = float(torch.linalg.norm(x - x64) / torch.linalg.norm(x64))
+    assert err <= ERR_BAR, (err, info)
+    sysm.close()
