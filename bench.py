@@ -240,7 +240,9 @@ def run_batched_uneven(dev, count=512, reps=3):
     out = {"systems": count, "n_min": min(s.n for s in systems), "n_max": max(s.n for s in systems),
            "unknowns_total": sum(s.n for s in systems)}
     for mode, method in (("mixed", "rainbow"), ("fp64", "rainbow"), ("fp64", "cg")):
-        bs = [torch.empty(s.n, dtype=torch.float64, device=dev) for s in systems]
+        # the first right-hand sides are in place before the batch is made: a mixed batch
+        # solves them once each way at creation to pick its inner precision
+        bs = [torch.from_numpy(workloads.uniform_vector(i, s.n)).to(dev) for i, s in enumerate(systems)]
         xs = [torch.zeros(s.n, dtype=torch.float64, device=dev) for s in systems]
         batch = Batch(systems, bs, xs, method=method, mode=mode, precision=PRECISION)
         times = []
@@ -256,7 +258,8 @@ def run_batched_uneven(dev, count=512, reps=3):
         batch.close()
         t = float(np.median(times))
         out[f"{mode}_{method}"] = {"ms_per_batch": t, "solves_per_s": count / (t / 1000.0),
-                                   "iterations_median": int(np.median([i["iterations"] for i in infos]))}
+                                   "iterations_median": int(np.median([i["iterations"] for i in infos])),
+                                   "inner_fp64": int(infos[0]["inner_fp64"])}
     for s in systems:
         s.close()
     return out

@@ -80,7 +80,8 @@ typedef struct feec_solve_info {
     int lanes_per_row;       /* CSR lanes per row used by the SpMV and sweeps              */
     int fp64_fallback;       /* MIXED: 1 if FP32 inner solves stagnated (operator too       */
                              /* ill-conditioned for FP32) and the solve finished in FP64    */
-    int reserved;
+    int inner_fp64;          /* MIXED: 1 if the inner iterations ran in FP64 because a       */
+                             /* reusable batch measured them faster (feec_batch_create)      */
     double error_estimate;   /* MIXED: estimated ||x - x*|| / ||x*|| from the measured      */
                              /* error-to-residual amplification of the outer corrections;   */
                              /* the solve keeps it <= 10 x precision; -1 if not estimated   */
@@ -362,7 +363,9 @@ int feec_solve_many(int nsys, feec_system* const* systems, int method, int mode,
  * x[i], b[i] that stay valid for the batch's lifetime; x holds the initial guess
  * on every run). Everything is set up once and the launch sequence is captured in
  * a CUDA graph; feec_batch_run replays it and fills infos[i] (host, nsys entries,
- * may be NULL) and *device_ms. team_threads 0 = 256. */
+ * may be NULL) and *device_ms. team_threads 0 = 256. In FEEC_MODE_MIXED the create
+ * call solves the batch once with FP32 and once with FP64 inner iterations (x is
+ * restored afterwards) and keeps the faster; infos[i].inner_fp64 reports it. */
 typedef struct feec_batch feec_batch;
 int feec_batch_create(feec_batch** batch, int nsys, feec_system* const* systems, int method, int mode,
                       double* const* x, const double* const* b, double precision, int max_iter,

@@ -30,7 +30,7 @@ class FeecSolveInfo(ctypes.Structure):
         ("grid_blocks", ctypes.c_int),
         ("lanes_per_row", ctypes.c_int),
         ("fp64_fallback", ctypes.c_int),
-        ("reserved", ctypes.c_int),
+        ("inner_fp64", ctypes.c_int),
         ("error_estimate", ctypes.c_double),
     ]
 

@@ -230,7 +230,7 @@ int rescue_stagnated(cudaStream_t st, const std::vector<feec_system*>& systems, 
 }
 
 void fill_infos(const std::vector<BatchResult>& res, double precision, float ms, int grid, feec_solve_info* infos,
-                int& worst) {
+                int& worst, int inner_fp64 = 0) {
     worst = FEEC_OK;
     for (size_t i = 0; i < res.size(); i++) {
         if (res[i].status != FEEC_OK && worst == FEEC_OK) worst = res[i].status;
@@ -247,6 +247,7 @@ void fill_infos(const std::vector<BatchResult>& res, double precision, float ms,
             f.lanes_per_row = 1;
             f.grid_blocks = grid;
             f.fp64_fallback = res[i].fp64_fallback;
+            f.inner_fp64 = inner_fp64;
             f.error_estimate = res[i].err_est;
         }
     }
@@ -532,6 +533,7 @@ struct feec_batch {
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     // for the FP64 finish of stagnated systems (mixed precision only)
     int method = 0, mode = 0, max_iter = 0;
+    int inner_fp64 = 0;                   // mixed: the FP64 graph measured faster at creation
     std::vector<feec_system*> systems;
     std::vector<Job> jobs;
 };
@@ -575,7 +577,9 @@ int feec_batch_create(feec_batch** out, int nsys, feec_system* const* systems, i
         maxn = std::max(maxn, sys[i]->n);
     }
     const int is_float = mode == FEEC_MODE_MIXED;
-    const size_t tsz = is_float ? sizeof(float) : sizeof(double);
+    // FP64-sized workspace in both modes: a mixed batch also captures and times the FP64
+    // iteration (below)
+    const size_t tsz = sizeof(double);
     // largest systems first
     std::vector<int> order((size_t)nsys);
     std::iota(order.begin(), order.end(), 0);
@@ -623,21 +627,91 @@ int feec_batch_create(feec_batch** out, int nsys, feec_system* const* systems, i
         bt->jobs.push_back(jb);
     }
     const int threads = team_threads > 0 ? team_threads : 256;
-    bt->teams = std::min(nsys, batched_resident_teams(is_float, 1, method == FEEC_METHOD_RAINBOW, threads));
-    // capture the launch sequence once (batched_resident_teams above already set the
-    // kernel's attributes, so nothing but stream work happens while capturing)
-    FEEC_TRY(cudaStreamBeginCapture(bt->stream, cudaStreamCaptureModeRelaxed));
-    cudaMemsetAsync(dnext, 0, sizeof(int), bt->stream);
-    cudaMemsetAsync(bt->dres, 0, sizeof(BatchResult) * nsys, bt->stream);
-    const cudaError_t le = launch_batched(a, is_float, 1, method == FEEC_METHOD_RAINBOW, threads, bt->teams, bt->stream);
-    const cudaError_t ce = cudaStreamEndCapture(bt->stream, &bt->graph);
-    if (le != cudaSuccess) return cuda_status(le);
-    if (ce != cudaSuccess) return cuda_status(ce);
-    FEEC_TRY(cudaGraphInstantiate(&bt->exec, bt->graph, 0));
+    const bool rainbow = method == FEEC_METHOD_RAINBOW;
+    bt->teams = std::min(nsys, batched_resident_teams(is_float, 1, rainbow, threads));
+    const int teams64 = std::min(nsys, batched_resident_teams(0, 1, rainbow, threads));
+    // capture a launch sequence (batched_resident_teams above already set the kernels'
+    // attributes, so nothing but stream work happens while capturing)
+    auto capture = [&](const BatchArgs& args, int f, int teams, cudaGraph_t& g, cudaGraphExec_t& ex) -> int {
+        FEEC_TRY(cudaStreamBeginCapture(bt->stream, cudaStreamCaptureModeRelaxed));
+        cudaMemsetAsync(dnext, 0, sizeof(int), bt->stream);
+        cudaMemsetAsync(bt->dres, 0, sizeof(BatchResult) * nsys, bt->stream);
+        const cudaError_t le = launch_batched(args, f, 1, rainbow, threads, teams, bt->stream);
+        const cudaError_t ce = cudaStreamEndCapture(bt->stream, &g);
+        if (le != cudaSuccess) return cuda_status(le);
+        if (ce != cudaSuccess) return cuda_status(ce);
+        FEEC_TRY(cudaGraphInstantiate(&ex, g, 0));
+        return FEEC_OK;
+    };
+    int st = capture(a, is_float, bt->teams, bt->graph, bt->exec);
+    if (st != FEEC_OK) return st;
     FEEC_TRY(cudaEventCreate(&bt->e0));
     FEEC_TRY(cudaEventCreate(&bt->e1));
     FEEC_TRY(cudaMallocHost(&bt->hres, sizeof(BatchResult) * (size_t)nsys));
     bt->nresults = nsys;
+    if (is_float) {
+        // FP32 storage pays where the batch is bound by memory traffic; for batches of small
+        // systems the FP32 segments' extra iterations can cost more than it saves (512 2D
+        // systems of 81 to 66,049 unknowns: 580 solves/s mixed against 706 in FP64). The
+        // batch is replayed once each way from the same initial guess (the FP32 run
+        // including the FP64 finish of stagnated systems), x is put back, and the faster
+        // graph is kept; results report it in inner_fp64.
+        BatchArgs a64 = a;
+        a64.inner_eta = 1e-30;
+        a64.err_control = 0;
+        a64.inner_margin = 1.0;
+        a64.stall_check = 0;
+        cudaGraph_t g64 = nullptr;
+        cudaGraphExec_t ex64 = nullptr;
+        struct GraphGuard {
+            cudaGraph_t& g; cudaGraphExec_t& ex;
+            ~GraphGuard() { if (ex) cudaGraphExecDestroy(ex); if (g) cudaGraphDestroy(g); }
+        } gguard{g64, ex64};
+        st = capture(a64, 0, teams64, g64, ex64);
+        if (st != FEEC_OK) return st;
+        std::vector<size_t> off((size_t)nsys + 1, 0);
+        for (int i = 0; i < nsys; i++) off[i + 1] = off[i] + (size_t)sys[i]->n;
+        double* xsave = nullptr;
+        FEEC_TRY(M.alloc(xsave, off[nsys]));
+        for (int i = 0; i < nsys; i++)
+            FEEC_TRY(cudaMemcpyAsync(xsave + off[i], x[i], sizeof(double) * sys[i]->n, cudaMemcpyDeviceToDevice,
+                                     bt->stream));
+        auto restore = [&]() -> int {
+            for (int i = 0; i < nsys; i++)
+                FEEC_TRY(cudaMemcpyAsync(x[i], xsave + off[i], sizeof(double) * sys[i]->n, cudaMemcpyDeviceToDevice,
+                                         bt->stream));
+            return FEEC_OK;
+        };
+        auto trial = [&](cudaGraphExec_t ex, bool f32, float& ms) -> int {
+            FEEC_TRY(cudaEventRecord(bt->e0, bt->stream));
+            FEEC_TRY(cudaGraphLaunch(ex, bt->stream));
+            note_launch();
+            FEEC_TRY(cudaEventRecord(bt->e1, bt->stream));
+            FEEC_TRY(cudaMemcpyAsync(bt->hres, bt->dres, sizeof(BatchResult) * nsys, cudaMemcpyDeviceToHost,
+                                     bt->stream));
+            FEEC_TRY(cudaStreamSynchronize(bt->stream));
+            FEEC_TRY(cudaEventElapsedTime(&ms, bt->e0, bt->e1));
+            if (f32) {
+                std::vector<BatchResult> res(bt->hres, bt->hres + nsys);
+                const int e = rescue_stagnated(bt->stream, bt->systems, bt->jobs, method, precision, a.max_iter,
+                                               res, &ms);
+                if (e != FEEC_OK) return e;
+            }
+            return FEEC_OK;
+        };
+        float t32 = 0.0f, t64 = 0.0f;
+        if ((st = trial(bt->exec, true, t32)) != FEEC_OK) return st;
+        if ((st = restore()) != FEEC_OK) return st;
+        if ((st = trial(ex64, false, t64)) != FEEC_OK) return st;
+        if ((st = restore()) != FEEC_OK) return st;
+        FEEC_TRY(cudaStreamSynchronize(bt->stream));
+        if (t64 < t32) {
+            std::swap(bt->graph, g64);
+            std::swap(bt->exec, ex64);   // the guard destroys the FP32 graph
+            bt->teams = teams64;
+            bt->inner_fp64 = 1;
+        }
+    }
     cleanup.keep = true;
     *out = bt;
     return FEEC_OK;
@@ -669,14 +743,14 @@ int feec_batch_finish(feec_batch* bt, feec_solve_info* infos, double* device_ms)
     std::vector<BatchResult> res(bt->hres, bt->hres + bt->nresults);
     float ms = 0.0f;
     cudaEventElapsedTime(&ms, bt->e0, bt->e1);
-    if (bt->mode == FEEC_MODE_MIXED) {
+    if (bt->mode == FEEC_MODE_MIXED && !bt->inner_fp64) {
         const int st = rescue_stagnated(bt->stream, bt->systems, bt->jobs, bt->method, bt->precision, bt->max_iter,
                                         res, &ms);
         if (st != FEEC_OK) return st;
     }
     if (device_ms) *device_ms = ms;
     int worst = FEEC_OK;
-    fill_infos(res, bt->precision, ms, bt->teams, infos, worst);
+    fill_infos(res, bt->precision, ms, bt->teams, infos, worst, bt->inner_fp64);
     return worst;
 }
 

@@ -163,7 +163,7 @@ int timed_launch_pcg64(feec_system* s, const PcgArgs<double>& a, LaunchShape& sh
         const double avg = (double)s->nnz / (double)(a.n > 0 ? a.n : 1);
         shape.lanes = avg <= 10.0 ? 1 : avg <= 20.0 ? 2 : avg <= 40.0 ? 4 : 8;
         shape.blocks = 1;
-        shape.threads = pcg_smem_threads(s->max_phase_rows, shape.lanes);
+        shape.threads = pcg_smem_warp_sweeps(a.n, a.nf, a.nbw) ? 256 : pcg_smem_threads(s->max_phase_rows, shape.lanes);
         FEEC_TRY(launch_pcg_smem(a, shape.lanes, shape.threads, s->stream));
     } else {
         FEEC_TRY(launch_pcg<double>(a, shape, s->stream));

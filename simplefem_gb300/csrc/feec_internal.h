@@ -98,6 +98,7 @@ template <typename T> cudaError_t launch_eisenstat(const PcgArgs<T>& a, LaunchSh
 cudaError_t launch_pcg_smem(const PcgArgs<double>& a, int lanes, int threads, cudaStream_t s);
 int pcg_smem_max_rows();
 int pcg_smem_threads(int max_phase_rows, int lanes);
+bool pcg_smem_warp_sweeps(int n, int nf, int nbw);   // one warp walks the sweeps (256-thread block)
 // Largest co-resident grid for the given kernel family and lane count.
 int max_coresident_blocks(int family, int is_float, int lanes, int threads);
 int pick_lanes(double avg_nnz_per_row);

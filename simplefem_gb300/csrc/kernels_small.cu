@@ -11,7 +11,9 @@
 // phases ahead: a phase costs a few shared-memory accesses and one __syncthreads. The
 // arithmetic and its order per row are those of pcg_persistent (same preconditioner,
 // same stopping rule, same skipped rows); only the dot products are summed by one block
-// instead of a grid, and the backward sweep's z.r is summed after the sweep.
+// instead of a grid, and the backward sweep's z.r is summed after the sweep. When the
+// phases average at most 64 rows (index-order levels), one warp walks each sweep with a
+// __syncwarp between phases and the rest of the block joins in between the sweeps.
 #include <cmath>
 #include <cstdio>
 
@@ -154,6 +156,123 @@ __device__ __forceinline__ void small_sweep(const PcgArgs<double>& a, SmallRow (
     }
 }
 
+// ---- sweeps by one warp, for phases of a few dozen rows ----
+// Index-order SSOR levels hold a few dozen rows (2D P1 refined 6 times: 129 levels of 33
+// rows on average), so a level costs its latency. One warp walks a sweep's phases with a
+// __syncwarp between them instead of a block barrier; lane l takes rows l, l + 32, l + 64
+// of a phase and sums each row's triangular part in CSR order (one lane per row, the
+// order of the reference's loop). A barrier orders memory, so row data loaded into
+// registers ahead of it still has to arrive before the barrier completes: the row bounds
+// therefore sit in shared memory for the whole solve, and each phase's entries and sweep
+// factors are copied into a shared-memory ring kStages - 1 phases ahead with cp.async,
+// which barriers do not wait for. The base of a row (r in the forward sweep, the scaled m
+// in the backward sweep) is in shared memory too: the x, r update writes r into z's
+// storage, which holds nothing live until the backward sweep writes z.
+constexpr int kStageE = 4;      // entries of a row's triangular part staged (the rest: direct loads)
+constexpr int kStageSlots = 3;  // rows per lane per phase staged (phases of up to 96 rows)
+constexpr int kStages = 4;      // ring depth: phases in flight
+
+struct StagedRow {              // one lane's copy of one row's sweep data, 64 bytes
+    double v[kStageE];
+    int c[kStageE];
+    double w;
+    double pad;
+};
+constexpr int kStageBytes = kStageSlots * 32 * (int)sizeof(StagedRow);
+
+struct SweepIndex {             // row bounds in shared memory
+    const int* rp; const int* lsplit; const int* usplit; const int* brows;
+};
+
+__device__ __forceinline__ void cp_async4(void* dst, const void* src) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async8(void* dst, const void* src) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+// Row of slot k in a phase, and its triangular segment [a, e).
+template <int KIND>
+__device__ __forceinline__ int sweep_row(const SweepIndex& ix, int k, int& a, int& e) {
+    if (KIND == kSmBackward) {
+        const int i = ix.brows[k];
+        a = ix.usplit[i]; e = ix.rp[i + 1];
+        return i;
+    }
+    a = ix.rp[k]; e = ix.lsplit[k];
+    return k;
+}
+
+// Copies the lane's rows of phase p into stage `st` (one commit group, possibly empty).
+template <int KIND>
+__device__ __forceinline__ void stage_phase(const PcgArgs<double>& a, const SweepIndex& ix, const int* ptr, int nph,
+                                            int p, StagedRow* st, int lane) {
+    if (p < nph) {
+        const int lo = ptr[p], hi = ptr[p + 1];
+        #pragma unroll
+        for (int t = 0; t < kStageSlots; t++) {
+            const int k = lo + lane + 32 * t;
+            if (k < hi) {
+                int ra, re;
+                const int i = sweep_row<KIND>(ix, k, ra, re);
+                StagedRow& d = st[t * 32 + lane];
+                cp_async8(&d.w, &a.wd[i]);
+                #pragma unroll
+                for (int u = 0; u < kStageE; u++)
+                    if (ra + u < re) { cp_async4(&d.c[u], &a.ci[ra + u]); cp_async8(&d.v[u], &a.val[ra + u]); }
+            }
+        }
+    }
+    cp_async_commit();
+}
+
+// A whole sweep by the calling warp: x[i] = (base[i] - sum_j A_ij x[j]) * w over each row's
+// triangular part, phase after phase.
+template <int KIND>
+__device__ __forceinline__ void warp_sweep(const PcgArgs<double>& a, const SweepIndex& ix, const int* ptr, int nph,
+                                           double* x, const double* base, StagedRow* ring) {
+    const int lane = threadIdx.x & 31;
+    #pragma unroll
+    for (int q = 0; q < kStages - 1; q++) stage_phase<KIND>(a, ix, ptr, nph, q, ring + q * (kStageBytes / 64), lane);
+    for (int p = 0; p < nph; p++) {
+        stage_phase<KIND>(a, ix, ptr, nph, p + kStages - 1, ring + ((p + kStages - 1) % kStages) * (kStageBytes / 64),
+                          lane);
+        cp_async_wait<kStages - 1>();   // this lane's copies of phase p have landed
+        const StagedRow* st = ring + (p % kStages) * (kStageBytes / 64);
+        const int lo = ptr[p], hi = ptr[p + 1];
+        #pragma unroll
+        for (int t = 0; t < kStageSlots; t++) {
+            const int k = lo + lane + 32 * t;
+            if (k < hi) {
+                int ra, re;
+                const int i = sweep_row<KIND>(ix, k, ra, re);
+                const StagedRow& d = st[t * 32 + lane];
+                double s = 0.0;
+                #pragma unroll
+                for (int u = 0; u < kStageE; u++)
+                    if (ra + u < re) s = fma(d.v[u], x[d.c[u]], s);
+                for (int j = ra + kStageE; j < re; j++) s = fma(__ldg(&a.val[j]), x[__ldg(&a.ci[j])], s);
+                if (d.w != 0.0) x[i] = (base[i] - s) * d.w;
+            }
+        }
+        for (int k = lo + lane + 32 * kStageSlots; k < hi; k += 32) {   // rows past the staged slots
+            int ra, re;
+            const int i = sweep_row<KIND>(ix, k, ra, re);
+            double s = 0.0;
+            for (int j = ra; j < re; j++) s = fma(__ldg(&a.val[j]), x[__ldg(&a.ci[j])], s);
+            const double w = __ldg(&a.wd[i]);
+            if (w != 0.0) x[i] = (base[i] - s) * w;
+        }
+        __syncwarp();   // this phase's results before the next phase gathers them
+    }
+    cp_async_wait<0>();
+}
+
 __device__ __forceinline__ double small_block_sum(double v) {
     double vv[1] = {v};
     block_reduce<double, 1>(vv);
@@ -165,7 +284,7 @@ __device__ __forceinline__ double small_block_sum(double v) {
     return out;
 }
 
-template <int LANES, int THREADS>
+template <int LANES, int THREADS, bool WARP>
 __global__ void __launch_bounds__(THREADS) pcg_smem_kernel(PcgArgs<double> a) {
     extern __shared__ double smem[];
     const int n = a.n;
@@ -179,6 +298,32 @@ __global__ void __launch_bounds__(THREADS) pcg_smem_kernel(PcgArgs<double> a) {
     __shared__ int s_ctl;
 
     for (int i = threadIdx.x; i < 3 * n; i += THREADS) smem[i] = 0.0;   // work vectors start at 0
+    StagedRow* stage_ring = nullptr;
+    SweepIndex ix{};
+    const int* sfptr = nullptr;
+    const int* sbptr = nullptr;
+    if constexpr (WARP) {
+        // the staging ring and the row bounds of both sweeps follow the vectors
+        stage_ring = reinterpret_cast<StagedRow*>(smem + 3 * n);
+        int* si = reinterpret_cast<int*>(reinterpret_cast<char*>(stage_ring) + kStages * kStageBytes);
+        int* srp = si;
+        int* sls = srp + n + 1;
+        int* sus = sls + n;
+        int* sbr = sus + n;
+        int* sfp = sbr + n;
+        int* sbp = sfp + a.nf + 1;
+        for (int i = threadIdx.x; i <= n; i += THREADS) srp[i] = __ldg(&a.rp[i]);
+        for (int i = threadIdx.x; i < n; i += THREADS) {
+            sls[i] = __ldg(&a.lsplit[i]);
+            sus[i] = __ldg(&a.usplit[i]);
+            sbr[i] = __ldg(&a.brows[i]);
+        }
+        for (int i = threadIdx.x; i <= a.nf; i += THREADS) sfp[i] = __ldg(&a.fptr[i]);
+        for (int i = threadIdx.x; i <= a.nbw; i += THREADS) sbp[i] = __ldg(&a.bptr[i]);
+        ix = SweepIndex{srp, sls, sus, sbr};
+        sfptr = sfp;
+        sbptr = sbp;
+    }
     __syncthreads();
 
     // ---- restart (sparsesolver.cpp:506-588): r = b - A x for rows with D != 0 ----
@@ -194,45 +339,62 @@ __global__ void __launch_bounds__(THREADS) pcg_smem_kernel(PcgArgs<double> a) {
         if (act && lane == 0 && __ldg(&a.wd[i]) != 0.0) {
             const double ri = __ldg(&a.b[i]) - s;
             a.r[i] = ri;
+            if constexpr (WARP) szv[i] = ri;   // the forward sweep's base
             arr += ri * ri;
         }
     }
     __syncthreads();   // orders the r writes before the sweeps read them
-    for (int p = 0; p < a.nf; p++) {                          // forward sweep
-        const int lo_r = __ldg(&a.fptr[p]), hi_r = __ldg(&a.fptr[p + 1]);
-        for (int base = lo_r; base < hi_r; base += groups) {
-            const int i = base + g;
-            const bool act = i < hi_r;
-            const SmallRow R = small_row<kSmForward, LANES>(a, i, hi_r);
-            const double s = small_dot<LANES>(R, a, smv);
-            if (act && lane == 0) {
-                const double w = __ldg(&a.wd[i]);
-                if (w != 0.0) smv[i] = (a.r[i] - s) * w;
-            }
-        }
-        __syncthreads();
-    }
     double azr = 0.0;
-    for (int p = 0; p < a.nbw; p++) {                         // scale + backward sweep
-        const int lo_r = __ldg(&a.bptr[p]), hi_r = __ldg(&a.bptr[p + 1]);
-        for (int base = lo_r; base < hi_r; base += groups) {
-            const int k = base + g;
-            const bool act = k < hi_r;
-            const SmallRow R = small_row<kSmBackward, LANES>(a, k, hi_r);
-            const double s = small_dot<LANES>(R, a, szv);
-            if (act && lane == 0) {
-                const double w = __ldg(&a.wd[R.i]);
-                if (w != 0.0) {
-                    const double mi = smv[R.i] * __ldg(&a.sd[R.i]);
-                    smv[R.i] = mi;
-                    const double zi = (mi - s) * w;
-                    szv[R.i] = zi;
-                    sdv[R.i] = zi;
-                    azr += zi * a.r[R.i];
+    if constexpr (WARP) {
+        if (threadIdx.x < 32) warp_sweep<kSmForward>(a, ix, sfptr, a.nf, smv, szv, stage_ring);
+        __syncthreads();
+        for (int i = threadIdx.x; i < n; i += THREADS)
+            if (__ldg(&a.wd[i]) != 0.0) smv[i] *= __ldg(&a.sd[i]);
+        __syncthreads();
+        if (threadIdx.x < 32) warp_sweep<kSmBackward>(a, ix, sbptr, a.nbw, szv, smv, stage_ring);
+        __syncthreads();
+        for (int i = threadIdx.x; i < n; i += THREADS)
+            if (__ldg(&a.wd[i]) != 0.0) {
+                const double zi = szv[i];
+                sdv[i] = zi;
+                azr += zi * a.r[i];
+            }
+    } else {
+        for (int p = 0; p < a.nf; p++) {                          // forward sweep
+            const int lo_r = __ldg(&a.fptr[p]), hi_r = __ldg(&a.fptr[p + 1]);
+            for (int base = lo_r; base < hi_r; base += groups) {
+                const int i = base + g;
+                const bool act = i < hi_r;
+                const SmallRow R = small_row<kSmForward, LANES>(a, i, hi_r);
+                const double s = small_dot<LANES>(R, a, smv);
+                if (act && lane == 0) {
+                    const double w = __ldg(&a.wd[i]);
+                    if (w != 0.0) smv[i] = (a.r[i] - s) * w;
                 }
             }
+            __syncthreads();
         }
-        __syncthreads();
+        for (int p = 0; p < a.nbw; p++) {                         // scale + backward sweep
+            const int lo_r = __ldg(&a.bptr[p]), hi_r = __ldg(&a.bptr[p + 1]);
+            for (int base = lo_r; base < hi_r; base += groups) {
+                const int k = base + g;
+                const bool act = k < hi_r;
+                const SmallRow R = small_row<kSmBackward, LANES>(a, k, hi_r);
+                const double s = small_dot<LANES>(R, a, szv);
+                if (act && lane == 0) {
+                    const double w = __ldg(&a.wd[R.i]);
+                    if (w != 0.0) {
+                        const double mi = smv[R.i] * __ldg(&a.sd[R.i]);
+                        smv[R.i] = mi;
+                        const double zi = (mi - s) * w;
+                        szv[R.i] = zi;
+                        sdv[R.i] = zi;
+                        azr += zi * a.r[R.i];
+                    }
+                }
+            }
+            __syncthreads();
+        }
     }
     double z_r = small_block_sum(azr);
     double r_r = small_block_sum(arr);
@@ -263,8 +425,10 @@ __global__ void __launch_bounds__(THREADS) pcg_smem_kernel(PcgArgs<double> a) {
             }
         });
         d_Ad = small_block_sum(adq);    // its barriers also order q before the forward sweep reads it
-        #pragma unroll
-        for (int k = 0; k < kRing; k++) ring[k] = sweep_first<kSmForward, LANES>(a, k);
+        if constexpr (!WARP) {
+            #pragma unroll
+            for (int k = 0; k < kRing; k++) ring[k] = sweep_first<kSmForward, LANES>(a, k);
+        }
         if (threadIdx.x == 0) {
             int ctl = 0;
             if (!isfinite(z_r) || z_r < 0.0 || !isfinite(d_Ad) || d_Ad < 0.0) ctl = 1;
@@ -278,28 +442,48 @@ __global__ void __launch_bounds__(THREADS) pcg_smem_kernel(PcgArgs<double> a) {
 
         const double alpha = s_scal[0];
         arr = 0.0;
-        small_sweep<kSmForward, LANES, THREADS>(a, ring, [&](const SmallRow& R) {             // :640-667
-            const double s = small_dot<LANES>(R, a, smv);
-            if (R.i >= 0 && lane == 0 && R.w != 0.0) {
-                a.x[R.i] = R.x + alpha * sdv[R.i];
-                const double ri = R.r - alpha * R.q;
-                a.r[R.i] = ri;
-                arr += ri * ri;
-                smv[R.i] = (ri - s) * R.w;
-            }
-        });
+        if constexpr (WARP) {
+            // :640-667, the update of x and r first (rows with D != 0), then the sweep
+            for (int i = threadIdx.x; i < n; i += THREADS)
+                if (__ldg(&a.wd[i]) != 0.0) {
+                    a.x[i] = a.x[i] + alpha * sdv[i];
+                    const double ri = a.r[i] - alpha * a.q[i];
+                    a.r[i] = ri;
+                    szv[i] = ri;   // the forward sweep's base (z's storage is free until the backward sweep)
+                    arr += ri * ri;
+                }
+            __syncthreads();
+            if (threadIdx.x < 32) warp_sweep<kSmForward>(a, ix, sfptr, a.nf, smv, szv, stage_ring);
+            __syncthreads();
+            for (int i = threadIdx.x; i < n; i += THREADS)                            // :670-699
+                if (__ldg(&a.wd[i]) != 0.0) smv[i] *= __ldg(&a.sd[i]);
+            __syncthreads();
+            if (threadIdx.x < 32) warp_sweep<kSmBackward>(a, ix, sbptr, a.nbw, szv, smv, stage_ring);
+            __syncthreads();
+        } else {
+            small_sweep<kSmForward, LANES, THREADS>(a, ring, [&](const SmallRow& R) {             // :640-667
+                const double s = small_dot<LANES>(R, a, smv);
+                if (R.i >= 0 && lane == 0 && R.w != 0.0) {
+                    a.x[R.i] = R.x + alpha * sdv[R.i];
+                    const double ri = R.r - alpha * R.q;
+                    a.r[R.i] = ri;
+                    arr += ri * ri;
+                    smv[R.i] = (ri - s) * R.w;
+                }
+            });
+            #pragma unroll
+            for (int k = 0; k < kRing; k++) ring[k] = sweep_first<kSmBackward, LANES>(a, k);
+            small_sweep<kSmBackward, LANES, THREADS>(a, ring, [&](const SmallRow& R) {            // :670-699
+                const double s = small_dot<LANES>(R, a, szv);
+                if (R.i >= 0 && lane == 0 && R.w != 0.0) {
+                    const double mi = smv[R.i] * R.s;
+                    smv[R.i] = mi;
+                    const double zi = (mi - s) * R.w;
+                    szv[R.i] = zi;
+                }
+            });
+        }
         double azr2 = 0.0;
-        #pragma unroll
-        for (int k = 0; k < kRing; k++) ring[k] = sweep_first<kSmBackward, LANES>(a, k);
-        small_sweep<kSmBackward, LANES, THREADS>(a, ring, [&](const SmallRow& R) {            // :670-699
-            const double s = small_dot<LANES>(R, a, szv);
-            if (R.i >= 0 && lane == 0 && R.w != 0.0) {
-                const double mi = smv[R.i] * R.s;
-                smv[R.i] = mi;
-                const double zi = (mi - s) * R.w;
-                szv[R.i] = zi;
-            }
-        });
         for (int i = threadIdx.x; i < n; i += THREADS)                           // z.r, :690-697
             if (__ldg(&a.wd[i]) != 0.0) azr2 += szv[i] * a.r[i];
         // the block sums' barriers order x, r and z before the direction update and the next product
@@ -319,22 +503,28 @@ __global__ void __launch_bounds__(THREADS) pcg_smem_kernel(PcgArgs<double> a) {
 
 size_t smem_bytes(int n) { return (size_t)3 * (size_t)n * sizeof(double); }
 
-template <int LANES, int THREADS>
+// The one-warp sweeps also hold the staging ring and the row bounds of both sweeps.
+size_t smem_bytes_warp(int n, int nf, int nbw) {
+    return smem_bytes(n) + (size_t)kStages * kStageBytes + sizeof(int) * ((size_t)4 * n + 1 + (size_t)nf + 1 + nbw + 1);
+}
+
+template <int LANES, int THREADS, bool WARP>
 cudaError_t launch_small(const PcgArgs<double>& a, cudaStream_t s) {
-    const size_t bytes = smem_bytes(a.n);
-    cudaError_t e = cudaFuncSetAttribute(pcg_smem_kernel<LANES, THREADS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)bytes);
+    const size_t bytes = WARP ? smem_bytes_warp(a.n, a.nf, a.nbw) : smem_bytes(a.n);
+    cudaError_t e = cudaFuncSetAttribute(pcg_smem_kernel<LANES, THREADS, WARP>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
     if (e != cudaSuccess) return e;
     note_launch();
-    pcg_smem_kernel<LANES, THREADS><<<1, THREADS, bytes, s>>>(a);
+    pcg_smem_kernel<LANES, THREADS, WARP><<<1, THREADS, bytes, s>>>(a);
     return cudaGetLastError();
 }
 
 template <int LANES>
-cudaError_t launch_small_threads(const PcgArgs<double>& a, int threads, cudaStream_t s) {
-    if (threads <= 64) return launch_small<LANES, 64>(a, s);
-    if (threads <= 128) return launch_small<LANES, 128>(a, s);
-    return launch_small<LANES, 256>(a, s);
+cudaError_t launch_small_threads(const PcgArgs<double>& a, int threads, bool warp_sweeps, cudaStream_t s) {
+    if (warp_sweeps) return launch_small<LANES, 256, true>(a, s);
+    if (threads <= 64) return launch_small<LANES, 64, false>(a, s);
+    if (threads <= 128) return launch_small<LANES, 128, false>(a, s);
+    return launch_small<LANES, 256, false>(a, s);
 }
 
 }  // namespace
@@ -355,13 +545,25 @@ int pcg_smem_threads(int max_phase_rows, int lanes) {
     return need <= 64 ? 64 : need <= 128 ? 128 : 256;
 }
 
+// Sweeps by one warp when the phases average at most 64 rows (index-order SSOR levels)
+// and the staging ring and row bounds fit beside the vectors; by the whole block otherwise
+// (multicolor phases of hundreds of rows).
+bool pcg_smem_warp_sweeps(int n, int nf, int nbw) {
+    if (nf <= 0 || n > 64 * nf) return false;
+    int dev = 0, optin = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return false;
+    if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) return false;
+    return smem_bytes_warp(n, nf, nbw) + 2048 <= (size_t)optin;   // 2048: block reductions and scalars
+}
+
 cudaError_t launch_pcg_smem(const PcgArgs<double>& a, int lanes, int threads, cudaStream_t s) {
     if (a.n <= 0 || a.n > pcg_smem_max_rows()) return cudaErrorInvalidValue;
+    const bool warp = pcg_smem_warp_sweeps(a.n, a.nf, a.nbw);
     switch (lanes) {
-        case 1: return launch_small_threads<1>(a, threads, s);
-        case 2: return launch_small_threads<2>(a, threads, s);
-        case 4: return launch_small_threads<4>(a, threads, s);
-        default: return launch_small_threads<8>(a, threads, s);
+        case 1: return launch_small_threads<1>(a, threads, warp, s);
+        case 2: return launch_small_threads<2>(a, threads, warp, s);
+        case 4: return launch_small_threads<4>(a, threads, warp, s);
+        default: return launch_small_threads<8>(a, threads, warp, s);
     }
 }
 

@@ -108,7 +108,11 @@ def test_many_systems_and_graph_batch_fall_back_only_where_needed(cuda):
         else:
             infos = solve_many(systems, bs, xs, method="rainbow", mode="mixed", precision=TOL, max_iter=MAX_IT)
         assert [i["status"] for i in infos] == [0, 0], infos
-        assert [i["fp64_fallback"] for i in infos] == [1, 0], infos
+        if use_graph and infos[0]["inner_fp64"]:
+            # the reusable batch measured FP64 inner iterations faster at creation
+            assert [i["inner_fp64"] for i in infos] == [1, 1], infos
+        else:
+            assert [i["fp64_fallback"] for i in infos] == [1, 0], infos
         assert _relres(M1, bh[0], xs[0].cpu().numpy()) <= TOL
         assert _relres(M2, bh[1], xs[1].cpu().numpy()) <= TOL
     for s in systems:
