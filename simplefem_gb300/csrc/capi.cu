@@ -158,13 +158,25 @@ int timed_launch_pcg64(feec_system* s, const PcgArgs<double>& a, LaunchShape& sh
     // per iteration, which one block with shared-memory vectors turns into block barriers
     // and shared-memory round trips).
     const bool small = s->user_blocks <= 0 && s->user_lanes <= 0 && a.n <= pcg_smem_max_rows();
+    const bool warp = small && pcg_smem_warp_sweeps(a.n, a.nf, a.nbw);
+    PcgArgs<double> ax = a;
+    if (warp) {
+        // per-row sweep records in sweep order, rebuilt for every solve (they hold omega / D)
+        if (!s->sweep_rec) {
+            HomeStreamScope home(s);
+            FEEC_TRY(s->work.alloc(s->sweep_rec, sweep_record_bytes(a.n)));
+        }
+        FEEC_TRY(launch_build_sweep_records(a, s->sweep_rec, s->stream));
+        ax.sweep_fwd = s->sweep_rec;
+        ax.sweep_bwd = s->sweep_rec + sweep_record_bytes(a.n) / 2;
+    }
     FEEC_TRY(cudaEventRecord(s->ev0, s->stream));
     if (small) {
         const double avg = (double)s->nnz / (double)(a.n > 0 ? a.n : 1);
         shape.lanes = avg <= 10.0 ? 1 : avg <= 20.0 ? 2 : avg <= 40.0 ? 4 : 8;
         shape.blocks = 1;
-        shape.threads = pcg_smem_warp_sweeps(a.n, a.nf, a.nbw) ? 256 : pcg_smem_threads(s->max_phase_rows, shape.lanes);
-        FEEC_TRY(launch_pcg_smem(a, shape.lanes, shape.threads, s->stream));
+        shape.threads = warp ? 256 : pcg_smem_threads(s->max_phase_rows, shape.lanes);
+        FEEC_TRY(launch_pcg_smem(ax, shape.lanes, shape.threads, s->stream));
     } else {
         FEEC_TRY(launch_pcg<double>(a, shape, s->stream));
     }

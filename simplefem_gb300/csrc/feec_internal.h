@@ -49,6 +49,10 @@ struct CgArgs {
     // the kernel leaves its last rho_prev in st->extra[0]
     int keep_dir;
     double zr_prev, scale;
+    // one-block solver with one-warp sweeps (kernels_small.cu): per-row sweep records in
+    // forward and backward sweep order, built by launch_build_sweep_records
+    const void* sweep_fwd;
+    const void* sweep_bwd;
 };
 
 template <typename T>
@@ -80,6 +84,10 @@ struct PcgArgs {
     // restart); the kernel leaves its last rho_prev in st->extra[0]
     int keep_dir;
     double zr_prev, scale;
+    // one-block solver with one-warp sweeps (kernels_small.cu): per-row sweep records in
+    // forward and backward sweep order, built by launch_build_sweep_records
+    const void* sweep_fwd;
+    const void* sweep_bwd;
 };
 
 struct LaunchShape {
@@ -99,6 +107,8 @@ cudaError_t launch_pcg_smem(const PcgArgs<double>& a, int lanes, int threads, cu
 int pcg_smem_max_rows();
 int pcg_smem_threads(int max_phase_rows, int lanes);
 bool pcg_smem_warp_sweeps(int n, int nf, int nbw);   // one warp walks the sweeps (256-thread block)
+size_t sweep_record_bytes(int n);                   // both sweeps' records of an n-row system
+cudaError_t launch_build_sweep_records(const PcgArgs<double>& a, void* recs, cudaStream_t s);
 // Largest co-resident grid for the given kernel family and lane count.
 int max_coresident_blocks(int family, int is_float, int lanes, int threads);
 int pick_lanes(double avg_nnz_per_row);

@@ -95,6 +95,7 @@ struct feec_system {
     double *x = nullptr, *r = nullptr, *d = nullptr, *z = nullptr, *m = nullptr, *q = nullptr, *b = nullptr;
     double* w = nullptr;               // Eisenstat solvers only: auxiliary + technical
     float* w32 = nullptr;              // ... FP32 copy for the mixed-precision inner solves
+    char* sweep_rec = nullptr;         // one-block solver: per-row sweep records (both sweeps)
     int zero_diag_rows = 0;            // rows with D == 0 in the prepared layout (the sweeps skip them)
     double* precon = nullptr;          // diagonal preconditioner of FEEC_METHOD_DIAGONAL (original numbering)
     float *x32 = nullptr, *r32 = nullptr, *d32 = nullptr, *z32 = nullptr, *m32 = nullptr, *q32 = nullptr, *b32 = nullptr;

@@ -158,119 +158,108 @@ __device__ __forceinline__ void small_sweep(const PcgArgs<double>& a, SmallRow (
 
 // ---- sweeps by one warp, for phases of a few dozen rows ----
 // Index-order SSOR levels hold a few dozen rows (2D P1 refined 6 times: 129 levels of 33
-// rows on average), so a level costs its latency. One warp walks a sweep's phases with a
-// __syncwarp between them instead of a block barrier; lane l takes rows l, l + 32, l + 64
-// of a phase and sums each row's triangular part in CSR order (one lane per row, the
-// order of the reference's loop). A barrier orders memory, so row data loaded into
-// registers ahead of it still has to arrive before the barrier completes: the row bounds
-// therefore sit in shared memory for the whole solve, and each phase's entries and sweep
-// factors are copied into a shared-memory ring kStages - 1 phases ahead with cp.async,
-// which barriers do not wait for. The base of a row (r in the forward sweep, the scaled m
-// in the backward sweep) is in shared memory too: the x, r update writes r into z's
-// storage, which holds nothing live until the backward sweep writes z.
-constexpr int kStageE = 4;      // entries of a row's triangular part staged (the rest: direct loads)
-constexpr int kStageSlots = 3;  // rows per lane per phase staged (phases of up to 96 rows)
-constexpr int kStages = 4;      // ring depth: phases in flight
-
-struct StagedRow {              // one lane's copy of one row's sweep data, 64 bytes
-    double v[kStageE];
-    int c[kStageE];
-    double w;
+// rows on average), so a level costs the latency of one warp's instruction path. One warp
+// walks a sweep's phases with a __syncwarp between them instead of a block barrier; lane
+// l takes rows l, l + 32, l + 64 of a phase and sums each row's triangular part in CSR
+// order (one lane per row, the order of the reference's loop). Each row of a sweep has a
+// 64-byte record in sweep order (row, first three columns and values of its triangular
+// part, sweep factor), so a phase's records are one contiguous range: the warp copies the
+// ranges of the next phases into a shared-memory ring with 16-byte cp.async copies, which
+// the barriers do not wait for (a barrier orders memory: row data loaded into registers
+// ahead of it would still have to arrive before it completes). The base of a row (r in
+// the forward sweep, the scaled m in the backward sweep) is in shared memory: the x, r
+// update writes r into z's storage, which holds nothing live until the backward sweep.
+struct SweepRecord {    // 64 bytes
+    int i, a, cnt;      // row, start and length of its triangular segment
+    int c[3];           // first three columns (0 past cnt)
+    double v[3];        // first three values (0 past cnt)
+    double w;           // sweep factor
     double pad;
 };
-constexpr int kStageBytes = kStageSlots * 32 * (int)sizeof(StagedRow);
+constexpr int kStageSlots = 3;                    // rows per lane per phase staged (phases of up to 96 rows)
+constexpr int kStages = 4;                        // ring depth: phases in flight
+constexpr int kStageRows = kStageSlots * 32;
+constexpr int kRingDoubles = kStages * kStageRows * (int)sizeof(SweepRecord) / 8;
 
-struct SweepIndex {             // row bounds in shared memory
-    const int* rp; const int* lsplit; const int* usplit; const int* brows;
-};
-
-__device__ __forceinline__ void cp_async4(void* dst, const void* src) {
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
     const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
-}
-__device__ __forceinline__ void cp_async8(void* dst, const void* src) {
-    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src) : "memory");
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src) : "memory");
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
-// Row of slot k in a phase, and its triangular segment [a, e).
-template <int KIND>
-__device__ __forceinline__ int sweep_row(const SweepIndex& ix, int k, int& a, int& e) {
-    if (KIND == kSmBackward) {
-        const int i = ix.brows[k];
-        a = ix.usplit[i]; e = ix.rp[i + 1];
-        return i;
-    }
-    a = ix.rp[k]; e = ix.lsplit[k];
-    return k;
-}
-
-// Copies the lane's rows of phase p into stage `st` (one commit group, possibly empty).
-template <int KIND>
-__device__ __forceinline__ void stage_phase(const PcgArgs<double>& a, const SweepIndex& ix, const int* ptr, int nph,
-                                            int p, StagedRow* st, int lane) {
+// Copies the records of phase p (at most kStageRows of them) into `st` (one commit group,
+// possibly empty).
+__device__ __forceinline__ void stage_phase(const SweepRecord* rec, const int* ptr, int nph, int p, SweepRecord* st,
+                                            int lane) {
     if (p < nph) {
-        const int lo = ptr[p], hi = ptr[p + 1];
-        #pragma unroll
-        for (int t = 0; t < kStageSlots; t++) {
-            const int k = lo + lane + 32 * t;
-            if (k < hi) {
-                int ra, re;
-                const int i = sweep_row<KIND>(ix, k, ra, re);
-                StagedRow& d = st[t * 32 + lane];
-                cp_async8(&d.w, &a.wd[i]);
-                #pragma unroll
-                for (int u = 0; u < kStageE; u++)
-                    if (ra + u < re) { cp_async4(&d.c[u], &a.ci[ra + u]); cp_async8(&d.v[u], &a.val[ra + u]); }
-            }
-        }
+        const int lo = ptr[p];
+        const int rows = min(ptr[p + 1] - lo, kStageRows);
+        const char* src = reinterpret_cast<const char*>(rec + lo);
+        char* dst = reinterpret_cast<char*>(st);
+        for (int q = lane; q < 4 * rows; q += 32) cp_async16(dst + 16 * q, src + 16 * q);
     }
     cp_async_commit();
 }
 
-// A whole sweep by the calling warp: x[i] = (base[i] - sum_j A_ij x[j]) * w over each row's
-// triangular part, phase after phase.
-template <int KIND>
-__device__ __forceinline__ void warp_sweep(const PcgArgs<double>& a, const SweepIndex& ix, const int* ptr, int nph,
-                                           double* x, const double* base, StagedRow* ring) {
+__device__ __forceinline__ void sweep_record(const SweepRecord& R, const PcgArgs<double>& a, double* x,
+                                             const double* base) {
+    double s = 0.0;
+    #pragma unroll
+    for (int u = 0; u < 3; u++)
+        if (u < R.cnt) s = fma(R.v[u], x[R.c[u]], s);
+    for (int j = R.a + 3; j < R.a + R.cnt; j++) s = fma(__ldg(&a.val[j]), x[__ldg(&a.ci[j])], s);
+    if (R.w != 0.0) x[R.i] = (base[R.i] - s) * R.w;
+}
+
+// A whole sweep by the calling warp over the records `rec` (in sweep order, phases
+// [ptr[p], ptr[p + 1])): x[i] = (base[i] - sum_j A_ij x[j]) * w.
+__device__ __forceinline__ void warp_sweep(const PcgArgs<double>& a, const SweepRecord* rec, const int* ptr, int nph,
+                                           double* x, const double* base, SweepRecord* ring) {
     const int lane = threadIdx.x & 31;
     #pragma unroll
-    for (int q = 0; q < kStages - 1; q++) stage_phase<KIND>(a, ix, ptr, nph, q, ring + q * (kStageBytes / 64), lane);
+    for (int q = 0; q < kStages - 1; q++) stage_phase(rec, ptr, nph, q, ring + q * kStageRows, lane);
     for (int p = 0; p < nph; p++) {
-        stage_phase<KIND>(a, ix, ptr, nph, p + kStages - 1, ring + ((p + kStages - 1) % kStages) * (kStageBytes / 64),
-                          lane);
-        cp_async_wait<kStages - 1>();   // this lane's copies of phase p have landed
-        const StagedRow* st = ring + (p % kStages) * (kStageBytes / 64);
+        stage_phase(rec, ptr, nph, p + kStages - 1, ring + ((p + kStages - 1) % kStages) * kStageRows, lane);
+        cp_async_wait<kStages - 1>();   // this lane's copies of phase p have landed ...
+        __syncwarp();                   // ... and every other lane's
+        const SweepRecord* st = ring + (p % kStages) * kStageRows;
         const int lo = ptr[p], hi = ptr[p + 1];
         #pragma unroll
         for (int t = 0; t < kStageSlots; t++) {
-            const int k = lo + lane + 32 * t;
-            if (k < hi) {
-                int ra, re;
-                const int i = sweep_row<KIND>(ix, k, ra, re);
-                const StagedRow& d = st[t * 32 + lane];
-                double s = 0.0;
-                #pragma unroll
-                for (int u = 0; u < kStageE; u++)
-                    if (ra + u < re) s = fma(d.v[u], x[d.c[u]], s);
-                for (int j = ra + kStageE; j < re; j++) s = fma(__ldg(&a.val[j]), x[__ldg(&a.ci[j])], s);
-                if (d.w != 0.0) x[i] = (base[i] - s) * d.w;
-            }
+            const int k = lane + 32 * t;
+            if (lo + k < hi) sweep_record(st[k], a, x, base);
         }
-        for (int k = lo + lane + 32 * kStageSlots; k < hi; k += 32) {   // rows past the staged slots
-            int ra, re;
-            const int i = sweep_row<KIND>(ix, k, ra, re);
-            double s = 0.0;
-            for (int j = ra; j < re; j++) s = fma(__ldg(&a.val[j]), x[__ldg(&a.ci[j])], s);
-            const double w = __ldg(&a.wd[i]);
-            if (w != 0.0) x[i] = (base[i] - s) * w;
-        }
+        for (int k = lo + lane + kStageRows; k < hi; k += 32) sweep_record(rec[k], a, x, base);   // past the ring
         __syncwarp();   // this phase's results before the next phase gathers them
     }
     cp_async_wait<0>();
+    __syncwarp();
+}
+
+// One record per row of each sweep: forward slot k is row k (the phases are row ranges),
+// backward slot k is row brows[k].
+__global__ void build_sweep_records(PcgArgs<double> a, SweepRecord* fwd, SweepRecord* bwd) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= a.n) return;
+    #pragma unroll
+    for (int dir = 0; dir < 2; dir++) {
+        const int i = dir == 0 ? k : __ldg(&a.brows[k]);
+        const int lo = dir == 0 ? __ldg(&a.rp[i]) : __ldg(&a.usplit[i]);
+        const int hi = dir == 0 ? __ldg(&a.lsplit[i]) : __ldg(&a.rp[i + 1]);
+        SweepRecord R;
+        R.i = i; R.a = lo; R.cnt = hi - lo;
+        #pragma unroll
+        for (int u = 0; u < 3; u++) {
+            const bool ok = lo + u < hi;
+            R.c[u] = ok ? __ldg(&a.ci[lo + u]) : 0;
+            R.v[u] = ok ? __ldg(&a.val[lo + u]) : 0.0;
+        }
+        R.w = __ldg(&a.wd[i]);
+        R.pad = 0.0;
+        (dir == 0 ? fwd : bwd)[k] = R;
+    }
 }
 
 __device__ __forceinline__ double small_block_sum(double v) {
@@ -286,41 +275,30 @@ __device__ __forceinline__ double small_block_sum(double v) {
 
 template <int LANES, int THREADS, bool WARP>
 __global__ void __launch_bounds__(THREADS) pcg_smem_kernel(PcgArgs<double> a) {
-    extern __shared__ double smem[];
+    extern __shared__ __align__(16) double smem[];
     const int n = a.n;
-    double* sdv = smem;          // d
-    double* smv = smem + n;      // m
-    double* szv = smem + 2 * n;  // z
+    double* vec = WARP ? smem + kRingDoubles : smem;   // one-warp sweeps: the staging ring first
+    double* sdv = vec;           // d
+    double* smv = vec + n;       // m
+    double* szv = vec + 2 * n;   // z
     const int lane = threadIdx.x & (LANES - 1);
     const int g = threadIdx.x / LANES;
     constexpr int groups = THREADS / LANES;
     __shared__ double s_scal[2];
     __shared__ int s_ctl;
 
-    for (int i = threadIdx.x; i < 3 * n; i += THREADS) smem[i] = 0.0;   // work vectors start at 0
-    StagedRow* stage_ring = nullptr;
-    SweepIndex ix{};
+    for (int i = threadIdx.x; i < 3 * n; i += THREADS) vec[i] = 0.0;   // work vectors start at 0
+    SweepRecord* stage_ring = reinterpret_cast<SweepRecord*>(smem);
+    const SweepRecord* frec = reinterpret_cast<const SweepRecord*>(a.sweep_fwd);
+    const SweepRecord* brec = reinterpret_cast<const SweepRecord*>(a.sweep_bwd);
     const int* sfptr = nullptr;
     const int* sbptr = nullptr;
     if constexpr (WARP) {
-        // the staging ring and the row bounds of both sweeps follow the vectors
-        stage_ring = reinterpret_cast<StagedRow*>(smem + 3 * n);
-        int* si = reinterpret_cast<int*>(reinterpret_cast<char*>(stage_ring) + kStages * kStageBytes);
-        int* srp = si;
-        int* sls = srp + n + 1;
-        int* sus = sls + n;
-        int* sbr = sus + n;
-        int* sfp = sbr + n;
+        // the phase bounds of both sweeps follow the vectors
+        int* sfp = reinterpret_cast<int*>(vec + 3 * n);
         int* sbp = sfp + a.nf + 1;
-        for (int i = threadIdx.x; i <= n; i += THREADS) srp[i] = __ldg(&a.rp[i]);
-        for (int i = threadIdx.x; i < n; i += THREADS) {
-            sls[i] = __ldg(&a.lsplit[i]);
-            sus[i] = __ldg(&a.usplit[i]);
-            sbr[i] = __ldg(&a.brows[i]);
-        }
         for (int i = threadIdx.x; i <= a.nf; i += THREADS) sfp[i] = __ldg(&a.fptr[i]);
         for (int i = threadIdx.x; i <= a.nbw; i += THREADS) sbp[i] = __ldg(&a.bptr[i]);
-        ix = SweepIndex{srp, sls, sus, sbr};
         sfptr = sfp;
         sbptr = sbp;
     }
@@ -346,12 +324,12 @@ __global__ void __launch_bounds__(THREADS) pcg_smem_kernel(PcgArgs<double> a) {
     __syncthreads();   // orders the r writes before the sweeps read them
     double azr = 0.0;
     if constexpr (WARP) {
-        if (threadIdx.x < 32) warp_sweep<kSmForward>(a, ix, sfptr, a.nf, smv, szv, stage_ring);
+        if (threadIdx.x < 32) warp_sweep(a, frec, sfptr, a.nf, smv, szv, stage_ring);
         __syncthreads();
         for (int i = threadIdx.x; i < n; i += THREADS)
             if (__ldg(&a.wd[i]) != 0.0) smv[i] *= __ldg(&a.sd[i]);
         __syncthreads();
-        if (threadIdx.x < 32) warp_sweep<kSmBackward>(a, ix, sbptr, a.nbw, szv, smv, stage_ring);
+        if (threadIdx.x < 32) warp_sweep(a, brec, sbptr, a.nbw, szv, smv, stage_ring);
         __syncthreads();
         for (int i = threadIdx.x; i < n; i += THREADS)
             if (__ldg(&a.wd[i]) != 0.0) {
@@ -453,12 +431,12 @@ __global__ void __launch_bounds__(THREADS) pcg_smem_kernel(PcgArgs<double> a) {
                     arr += ri * ri;
                 }
             __syncthreads();
-            if (threadIdx.x < 32) warp_sweep<kSmForward>(a, ix, sfptr, a.nf, smv, szv, stage_ring);
+            if (threadIdx.x < 32) warp_sweep(a, frec, sfptr, a.nf, smv, szv, stage_ring);
             __syncthreads();
             for (int i = threadIdx.x; i < n; i += THREADS)                            // :670-699
                 if (__ldg(&a.wd[i]) != 0.0) smv[i] *= __ldg(&a.sd[i]);
             __syncthreads();
-            if (threadIdx.x < 32) warp_sweep<kSmBackward>(a, ix, sbptr, a.nbw, szv, smv, stage_ring);
+            if (threadIdx.x < 32) warp_sweep(a, brec, sbptr, a.nbw, szv, smv, stage_ring);
             __syncthreads();
         } else {
             small_sweep<kSmForward, LANES, THREADS>(a, ring, [&](const SmallRow& R) {             // :640-667
@@ -503,9 +481,9 @@ __global__ void __launch_bounds__(THREADS) pcg_smem_kernel(PcgArgs<double> a) {
 
 size_t smem_bytes(int n) { return (size_t)3 * (size_t)n * sizeof(double); }
 
-// The one-warp sweeps also hold the staging ring and the row bounds of both sweeps.
+// The one-warp sweeps also hold the staging ring and the phase bounds of both sweeps.
 size_t smem_bytes_warp(int n, int nf, int nbw) {
-    return smem_bytes(n) + (size_t)kStages * kStageBytes + sizeof(int) * ((size_t)4 * n + 1 + (size_t)nf + 1 + nbw + 1);
+    return smem_bytes(n) + (size_t)kRingDoubles * 8 + sizeof(int) * ((size_t)nf + 1 + (size_t)nbw + 1);
 }
 
 template <int LANES, int THREADS, bool WARP>
@@ -556,9 +534,18 @@ bool pcg_smem_warp_sweeps(int n, int nf, int nbw) {
     return smem_bytes_warp(n, nf, nbw) + 2048 <= (size_t)optin;   // 2048: block reductions and scalars
 }
 
+size_t sweep_record_bytes(int n) { return (size_t)2 * (size_t)n * sizeof(SweepRecord); }
+
+cudaError_t launch_build_sweep_records(const PcgArgs<double>& a, void* recs, cudaStream_t s) {
+    SweepRecord* fwd = reinterpret_cast<SweepRecord*>(recs);
+    note_launch();
+    build_sweep_records<<<(a.n + 255) / 256, 256, 0, s>>>(a, fwd, fwd + a.n);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_pcg_smem(const PcgArgs<double>& a, int lanes, int threads, cudaStream_t s) {
     if (a.n <= 0 || a.n > pcg_smem_max_rows()) return cudaErrorInvalidValue;
-    const bool warp = pcg_smem_warp_sweeps(a.n, a.nf, a.nbw);
+    const bool warp = pcg_smem_warp_sweeps(a.n, a.nf, a.nbw) && a.sweep_fwd && a.sweep_bwd;
     switch (lanes) {
         case 1: return launch_small_threads<1>(a, threads, warp, s);
         case 2: return launch_small_threads<2>(a, threads, warp, s);
