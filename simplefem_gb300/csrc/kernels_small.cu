@@ -165,8 +165,9 @@ __device__ __forceinline__ void small_sweep(const PcgArgs<double>& a, SmallRow (
 // 64-byte record in sweep order (row, first three columns and values of its triangular
 // part, sweep factor), so a phase's records are one contiguous range: the warp copies the
 // ranges of the next phases into a shared-memory ring with 16-byte cp.async copies, which
-// the barriers do not wait for (a barrier orders memory: row data loaded into registers
-// ahead of it would still have to arrive before it completes). The base of a row (r in
+// the barriers do not wait for (row data loaded into registers ahead of the barriers did
+// not shorten the phases: the barriers' memory ordering holds the warp until it arrives).
+// The base of a row (r in
 // the forward sweep, the scaled m in the backward sweep) is in shared memory: the x, r
 // update writes r into z's storage, which holds nothing live until the backward sweep.
 struct SweepRecord {    // 64 bytes
