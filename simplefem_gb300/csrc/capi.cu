@@ -147,6 +147,7 @@ PcgArgs<T> make_pcg_args(feec_system* s, T* x, T* r, T* d, T* z, T* m, T* q, con
     a.n = s->n; a.rp = s->rp; a.ci = s->ci; a.val = val; a.lsplit = s->lsplit; a.usplit = s->usplit;
     a.wd = wd; a.sd = sd; a.b = b; a.x = x; a.r = r; a.d = d; a.z = z; a.m = m; a.q = q;
     a.nf = s->nf; a.fptr = s->fptr; a.nbw = s->nbw; a.bptr = s->bptr; a.brows = s->brows;
+    a.fsplit = s->fsplit; a.bsplit = s->bsplit;
     a.omega = s->omega; a.partials = s->partials; a.st = s->st;
     return a;
 }
@@ -602,6 +603,7 @@ int build_layout(feec_system* s, int method, const double* diag_dev, double omeg
         FEEC_TRY(M.alloc(s->wd, n)); FEEC_TRY(M.alloc(s->sd, n)); FEEC_TRY(M.alloc(s->wd32, n)); FEEC_TRY(M.alloc(s->sd32, n));
     }
     // schedules (small, reallocated per preparation)
+    s->fsplit = nullptr; s->bsplit = nullptr;
     FEEC_TRY(M.alloc(s->fptr, fptr.size())); FEEC_TRY(M.alloc(s->bptr, bptr.size())); FEEC_TRY(M.alloc(s->brows, brows.size()));
     FEEC_TRY(cudaMemcpyAsync(s->perm, perm_host, sizeof(int) * n, cudaMemcpyHostToDevice, st));
     FEEC_TRY(cudaMemcpyAsync(s->fptr, fptr.data(), sizeof(int) * fptr.size(), cudaMemcpyHostToDevice, st));
@@ -768,14 +770,12 @@ int feec_system_set_rainbow(feec_system* s, const double* diagonal, double omega
     }
     // Inside a color the rows are independent, so their order is free: sort them by row
     // length (stable, longest first) so that 32-row slices hold rows of equal length.
-    {
-        std::vector<int> hA((size_t)n + 1);
-        FEEC_TRY(cudaMemcpyAsync(hA.data(), s->A, sizeof(int) * (n + 1), cudaMemcpyDeviceToHost, s->stream));
-        FEEC_TRY(cudaStreamSynchronize(s->stream));
-        for (int c = 0; c < num_colors; c++)
-            std::stable_sort(hR.begin() + hB[c], hR.begin() + hB[c + 1],
-                             [&](int a, int b) { return hA[a + 1] - hA[a] > hA[b + 1] - hA[b]; });
-    }
+    std::vector<int> hA((size_t)n + 1);
+    FEEC_TRY(cudaMemcpyAsync(hA.data(), s->A, sizeof(int) * (n + 1), cudaMemcpyDeviceToHost, s->stream));
+    FEEC_TRY(cudaStreamSynchronize(s->stream));
+    for (int c = 0; c < num_colors; c++)
+        std::stable_sort(hR.begin() + hB[c], hR.begin() + hB[c + 1],
+                         [&](int a, int b) { return hA[a + 1] - hA[a] > hA[b + 1] - hA[b]; });
     // forward phases: colors ascending (rows are renumbered color by color, so ranges are contiguous);
     // backward phases: colors descending
     std::vector<int> fptr(hB.begin(), hB.end());
@@ -792,6 +792,22 @@ int feec_system_set_rainbow(feec_system* s, const double* diagonal, double omega
     FEEC_TRY(cudaMemcpyAsync(Fd, F, sizeof(int) * n, kind, s->stream));
     FEEC_TRY(cudaMemcpyAsync(Dd, diagonal, sizeof(double) * n, kind, s->stream));
     st = build_layout(s, FEEC_METHOD_RAINBOW, Dd, omega, hR.data(), Fd, fptr, bptr, brows, num_colors);
+    if (st == FEEC_OK) {
+        // each color's rows are longest first: where its long rows end, in both sweeps' order
+        std::vector<int> fsplit((size_t)num_colors), bsplit((size_t)num_colors);
+        for (int c = 0; c < num_colors; c++) {
+            int k = hB[c];
+            while (k < hB[c + 1] && hA[hR[k] + 1] - hA[hR[k]] > kLongRowEntries) k++;
+            fsplit[c] = k;
+            const int p = num_colors - 1 - c;   // backward phase of color c: slots bptr[p].. hold rows hB[c]..
+            bsplit[p] = bptr[p] + (k - hB[c]);
+        }
+        DevArena& M = s->mem;
+        FEEC_TRY(M.alloc(s->fsplit, fsplit.size() + 1));
+        FEEC_TRY(M.alloc(s->bsplit, bsplit.size() + 1));
+        FEEC_TRY(cudaMemcpyAsync(s->fsplit, fsplit.data(), sizeof(int) * fsplit.size(), cudaMemcpyHostToDevice, s->stream));
+        FEEC_TRY(cudaMemcpyAsync(s->bsplit, bsplit.data(), sizeof(int) * bsplit.size(), cudaMemcpyHostToDevice, s->stream));
+    }
     tmp.release();
     cudaStreamSynchronize(s->stream);
     return st;

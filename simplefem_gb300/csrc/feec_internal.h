@@ -65,6 +65,9 @@ struct PcgArgs {
     T* x; T* r; T* d; T* z; T* m; T* q;
     int nf; const int* fptr;                      // forward phases: rows [fptr[p], fptr[p+1])
     int nbw; const int* bptr; const int* brows;   // backward phases: rows brows[bptr[p] .. bptr[p+1])
+    // multicolor layouts (rows of a color longest first): the long rows of forward phase p
+    // are [fptr[p], fsplit[p]), of backward phase p the slots [bptr[p], bsplit[p]); null otherwise
+    const int* fsplit; const int* bsplit;
     double omega;
     double tol2;         // reference rule: stop when |z.r| < tol2 (if use_zr_rule)
     double rr_stop;      // stop when the recursive r.r < rr_stop (if > 0); Eisenstat: when z.r < rr_stop * (z.r at the start)
@@ -89,6 +92,10 @@ struct PcgArgs {
     const void* sweep_fwd;
     const void* sweep_bwd;
 };
+
+// Rows with more stored entries than this count as long in a multicolor layout: the
+// persistent sweeps give them more lanes (the phase bounds fsplit / bsplit).
+constexpr int kLongRowEntries = 32;
 
 struct LaunchShape {
     int blocks = 0;

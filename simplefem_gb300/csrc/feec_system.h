@@ -88,6 +88,7 @@ struct feec_system {
     double* wd = nullptr; double* sd = nullptr; float* wd32 = nullptr; float* sd32 = nullptr;
     int nf = 0; int* fptr = nullptr;
     int nbw = 0; int* bptr = nullptr; int* brows = nullptr;
+    int* fsplit = nullptr; int* bsplit = nullptr;   // multicolor: end of each phase's long rows
     double omega = 1.0;
     int num_levels = 0;
     // workspace (FP64 permuted vectors + FP32 inner vectors)

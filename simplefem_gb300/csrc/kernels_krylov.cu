@@ -14,6 +14,7 @@
 // mixed-precision mode (FP32 storage, FP32 arithmetic, compensated FP32 dots).
 #include <cmath>
 #include <cstdio>
+#include <type_traits>
 
 #include "feec_device.cuh"
 #include "feec_internal.h"
@@ -104,6 +105,30 @@ __device__ __forceinline__ void rows_pipelined(const PcgArgs<T>& a, int lo, int 
         const RowRef<T, LANES> nxt = row_ref<KIND, LANES>(a, k + stride, hi);
         body(cur);
         cur = nxt;
+    }
+}
+
+// Rows [lo, hi) of a multicolor phase whose rows are sorted longest first, [lo, sp) being
+// the long ones: the long rows get LL lanes each (the first warps of the grid), the rest LS
+// lanes each (the warps after them), so that no row group walks more than a few strides
+// of its row. A phase lasts as long as its slowest row group: with LS lanes for every row,
+// the longest rows of a color (65 entries on 3D P2) took several dependent rounds of index
+// loads and gathers while the other warps waited at the barrier. body(lanes, row, active,
+// lane in group) is called with std::integral_constant lanes, uniformly across each warp.
+template <int LS, int LL, typename F>
+__device__ __forceinline__ void split_rows(int lo, int sp, int hi, F&& body) {
+    const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) / 32);
+    const int nwarps = (int)(gridDim.x * blockDim.x / 32);
+    const int wl = (sp - lo + (32 / LL) - 1) / (32 / LL);   // warps the long rows take
+    for (int w = warp; w < wl; w += nwarps) {
+        const int i = lo + w * (32 / LL) + (int)((threadIdx.x & 31) / LL);
+        body(std::integral_constant<int, LL>{}, i, i < sp, (int)(threadIdx.x & (LL - 1)));
+    }
+    int w = warp - wl % nwarps;
+    if (w < 0) w += nwarps;
+    for (; sp + w * (32 / LS) < hi; w += nwarps) {
+        const int i = sp + w * (32 / LS) + (int)((threadIdx.x & 31) / LS);
+        body(std::integral_constant<int, LS>{}, i, i < hi, (int)(threadIdx.x & (LS - 1)));
     }
 }
 
@@ -324,6 +349,7 @@ __global__ void __launch_bounds__(kThreads, 2) pcg_persistent(PcgArgs<T> a) {
     int status = FEEC_MAXITER;
     double d_Ad = 0.0;
     RowRef<T, LANES> pf = row_ref<kRowsFull, LANES>(a, group_first<LANES>(0), n);
+    constexpr int LL = LANES > kLongLanes ? LANES : kLongLanes;   // long rows of multicolor phases
     while (K < a.max_iter) {
         if (threadIdx.x == 0) {
             if (a.print_modulo > 0 && K % a.print_modulo == 0 && blockIdx.x == 0)
@@ -366,6 +392,48 @@ __global__ void __launch_bounds__(kThreads, 2) pcg_persistent(PcgArgs<T> a) {
 
         const T alpha = (T)s_scal[0];
         arr = AT::zero();
+        if (a.fsplit) {
+            // multicolor phases with long rows first: split lane counts (split_rows)
+            for (int p = 0; p < a.nf; p++) {                                           // :1230-1261
+                const int lo_r = __ldg(&a.fptr[p]), sp_r = __ldg(&a.fsplit[p]), hi_r = __ldg(&a.fptr[p + 1]);
+                split_rows<LANES, LL>(lo_r, sp_r, hi_r, [&](auto L, int i, bool act, int ln) {
+                    constexpr int LN = decltype(L)::value;
+                    const int lo = act ? __ldg(&a.rp[i]) : 0, hi = act ? __ldg(&a.lsplit[i]) : 0;
+                    // the row's own values are requested before its entries' gathers
+                    T w = T(0), xi = T(0), di = T(0), ri0 = T(0), qi = T(0);
+                    if (act && ln == 0) { w = __ldg(&a.wd[i]); xi = a.x[i]; di = a.d[i]; ri0 = a.r[i]; qi = a.q[i]; }
+                    const T s = seg_dot<T, LN>(a.ci, a.val, a.m, lo, hi, ln);
+                    if (act && ln == 0 && w != T(0)) {
+                        a.x[i] = xi + alpha * di;
+                        const T ri = ri0 - alpha * qi;
+                        a.r[i] = ri;
+                        arr = AT::add(arr, ri * ri);
+                        a.m[i] = (ri - s) * w;
+                    }
+                });
+                if (!grid_barrier(a.st, epoch, 15)) return;
+            }
+            azr = AT::zero();
+            for (int p = 0; p < a.nbw; p++) {                                          // :1263-1307
+                const int lo_r = __ldg(&a.bptr[p]), sp_r = __ldg(&a.bsplit[p]), hi_r = __ldg(&a.bptr[p + 1]);
+                split_rows<LANES, LL>(lo_r, sp_r, hi_r, [&](auto L, int k, bool act, int ln) {
+                    constexpr int LN = decltype(L)::value;
+                    const int i = act ? __ldg(&a.brows[k]) : 0;
+                    const int lo = act ? __ldg(&a.usplit[i]) : 0, hi = act ? __ldg(&a.rp[i + 1]) : 0;
+                    T w = T(0), m0 = T(0), sdi = T(0), ri = T(0);
+                    if (act && ln == 0) { w = __ldg(&a.wd[i]); m0 = a.m[i]; sdi = __ldg(&a.sd[i]); ri = a.r[i]; }
+                    const T s = seg_dot<T, LN>(a.ci, a.val, a.z, lo, hi, ln);
+                    if (act && ln == 0 && w != T(0)) {
+                        const T mi = m0 * sdi;
+                        a.m[i] = mi;
+                        const T zi = (mi - s) * w;
+                        a.z[i] = zi;
+                        azr = AT::add(azr, zi * ri);
+                    }
+                });
+                if (p + 1 < a.nbw && !grid_barrier(a.st, epoch, 16)) return;
+            }
+        } else {
         for (int p = 0; p < a.nf; p++) {                                               // :1230-1261
             rows_pipelined<LANES, kRowsL>(a, flo, fhi, pf, [&](const RowRef<T, LANES>& R) {
                 const bool act = R.i >= 0;
@@ -411,6 +479,7 @@ __global__ void __launch_bounds__(kThreads, 2) pcg_persistent(PcgArgs<T> a) {
                 pf = row_ref<kRowsBackwardU, LANES>(a, group_first<LANES>(hi_r), __ldg(&a.bptr[p + 2]));
                 if (!grid_barrier(a.st, epoch, 16)) return;
             }
+        }
         }
         pf = row_ref<kRowsFull, LANES>(a, group_first<LANES>(0), n);
         write_partials2<T>(p_zr, azr, arr);

@@ -8,6 +8,7 @@
 namespace feec {
 
 constexpr int kThreads = 512;
+constexpr int kLongLanes = 16;   // lanes per row for the long rows of a multicolor phase (split_rows)
 constexpr double kMachineEpsilon = 2.220446049250313080847263336181640625e-16;  // base/base.hpp:123
 
 // Iterate rows [lo, hi) with LANES lanes per row; the loop trip count is
