@@ -80,8 +80,10 @@ typedef struct feec_solve_info {
     int lanes_per_row;       /* CSR lanes per row used by the SpMV and sweeps              */
     int fp64_fallback;       /* MIXED: 1 if FP32 inner solves stagnated (operator too       */
                              /* ill-conditioned for FP32) and the solve finished in FP64    */
-    int inner_fp64;          /* MIXED: 1 if the inner iterations ran in FP64 because a       */
-                             /* reusable batch measured them faster (feec_batch_create)      */
+    int inner_fp64;          /* MIXED: 1 if the inner iterations ran in FP64: a reusable     */
+                             /* batch measured them faster (feec_batch_create), or a system  */
+                             /* solving on the whole GPU did (its first solve runs FP32,     */
+                             /* its second FP64, later ones the faster per decade of fall)   */
     double error_estimate;   /* MIXED: estimated ||x - x*|| / ||x*|| from the measured      */
                              /* error-to-residual amplification of the outer corrections;   */
                              /* the solve keeps it <= 10 x precision; -1 if not estimated   */

@@ -241,6 +241,19 @@ int solve_core(feec_system* s, int method, int mode, double* xx, const double* b
     double tolerance = tol_override > 0.0 ? tol_override : std::max(precision * bnorm, kDesiredPrecision);
     if (mode != FEEC_MODE_REFERENCE) tolerance = precision * bnorm;
 
+    // MIXED on the whole GPU: a system measures its first solve with FP32 inner iterations
+    // and its second with FP64 ones (device time per decade of residual fall) and keeps the
+    // faster for later solves of the same method. The phases of a single solve are latency-
+    // bound, so FP32 storage may not pay for its extra iterations (3D P1 refined 7 times:
+    // 223 ms against 168 in FP64); the result reports the choice in inner_fp64.
+    const int pick_slot = method == FEEC_METHOD_CG ? 0 : 1;
+    bool inner64 = false;
+    if (mode == FEEC_MODE_MIXED) {
+        const int pick = s->mixed_pick[pick_slot];
+        inner64 = pick == 2 || (pick == 0 && s->mixed_rate[pick_slot][0] > 0.0);
+    }
+    const int shape_mode = inner64 ? FEEC_MODE_FP64 : mode;
+
     LaunchShape shape;
     shape.lanes = s->lanes;
     // Measured on GB300 (3D P2 operator, 28 entries per row, two 512-thread blocks per
@@ -249,9 +262,9 @@ int solve_core(feec_system* s, int method, int mode, double* xx, const double* b
     // fastest for plain FP64 CG (42.7 ms against 50.4 with 1, and 47.3 with 1 lane on one
     // block per SM) and 4 for the sweeps of the preconditioned solvers (50.2 ms against
     // 56.3 with 8 and 76.0 with 16; 8 for their FP32 inner solves).
-    if (cg_family && mode != FEEC_MODE_MIXED) shape.lanes = 2;
+    if (cg_family && shape_mode != FEEC_MODE_MIXED) shape.lanes = 2;
     else {
-        const int cap = (mode == FEEC_MODE_MIXED && method != FEEC_METHOD_CG) ? 8 : 4;
+        const int cap = (shape_mode == FEEC_MODE_MIXED && method != FEEC_METHOD_CG) ? 8 : 4;
         if (shape.lanes > cap) shape.lanes = cap;
     }
     if (shape.lanes == 1 || shape.lanes == 4 || shape.lanes == 8) {
@@ -392,6 +405,15 @@ int solve_core(feec_system* s, int method, int mode, double* xx, const double* b
     if (mode == FEEC_MODE_REFERENCE || mode == FEEC_MODE_FP64) {
         st = run_fp64(mode);
         if (st != FEEC_OK) return st;
+    } else if (inner64) {
+        // MIXED with FP64 inner iterations: the residual bar tightened so that the error bar
+        // holds for amplifications up to kAmpFloor (kAmpFloor x relative residual <=
+        // kErrorPerResidual x precision), the bound reported as the estimate
+        tolerance = precision * bnorm * kErrorPerResidual / kAmpFloor;
+        st = run_fp64(FEEC_MODE_FP64);
+        if (st != FEEC_OK) return st;
+        if (bnorm > 0.0) err_estimate = kAmpFloor * final_norm / bnorm;
+        tolerance = precision * bnorm;
     } else {
         // MIXED: FP32 inner iterations (compensated FP32 dots) in segments: the FP64 solution
         // and true residual are kept beside the FP32 recursion, and a segment ends when z.r
@@ -561,6 +583,13 @@ int solve_core(feec_system* s, int method, int mode, double* xx, const double* b
         if (!fell_back && bnorm > 0.0) err_estimate = std::max(amp, kAmpFloor) * final_norm / bnorm;
     }
 
+    if (mode == FEEC_MODE_MIXED && s->mixed_pick[pick_slot] == 0 && status == FEEC_OK && final_norm > 0.0 &&
+        bnorm > 0.0) {
+        const double decades = std::max(1.0, std::log10(bnorm / final_norm));
+        s->mixed_rate[pick_slot][inner64 ? 1 : 0] = ms_total / decades;
+        if (inner64) s->mixed_pick[pick_slot] = s->mixed_rate[pick_slot][1] < s->mixed_rate[pick_slot][0] ? 2 : 1;
+    }
+
     // results back to the caller's numbering
     FEEC_TRY(launch_scatter_f64(n, perm, s->x, xx, s->stream));
     if (res) FEEC_TRY(launch_scatter_f64(n, perm, s->r, res, s->stream));
@@ -571,6 +600,7 @@ int solve_core(feec_system* s, int method, int mode, double* xx, const double* b
         info->outer_iterations = outer;
         info->num_colors = cg_family ? 0 : s->num_levels;
         info->fp64_fallback = fell_back;
+        info->inner_fp64 = inner64 ? 1 : 0;
         info->error_estimate = err_estimate;
         info->tolerance = (mode == FEEC_MODE_REFERENCE) ? tolerance : precision;
         info->final_norm = final_norm;
@@ -638,6 +668,8 @@ int build_layout(feec_system* s, int method, const double* diag_dev, double omeg
     s->omega = omega;
     s->num_levels = num_levels;
     s->prepared = method;
+    s->mixed_pick[1] = 0;   // a new layout measures its inner precision again
+    s->mixed_rate[1][0] = s->mixed_rate[1][1] = 0.0;
     s->sell[1].ready = false;   // the Rainbow-order SELL copy follows the new ordering
     return FEEC_OK;
 }

@@ -97,6 +97,10 @@ struct feec_system {
     double* w = nullptr;               // Eisenstat solvers only: auxiliary + technical
     float* w32 = nullptr;              // ... FP32 copy for the mixed-precision inner solves
     char* sweep_rec = nullptr;         // one-block solver: per-row sweep records (both sweeps)
+    // MIXED on the whole GPU, per method slot (0: plain CG, 1: preconditioned): 0 = not yet
+    // measured, 1 = FP32 inner iterations, 2 = FP64; device ms per decade of residual fall
+    int mixed_pick[2] = {0, 0};
+    double mixed_rate[2][2] = {{0.0, 0.0}, {0.0, 0.0}};
     int zero_diag_rows = 0;            // rows with D == 0 in the prepared layout (the sweeps skip them)
     double* precon = nullptr;          // diagonal preconditioner of FEEC_METHOD_DIAGONAL (original numbering)
     float *x32 = nullptr, *r32 = nullptr, *d32 = nullptr, *z32 = nullptr, *m32 = nullptr, *q32 = nullptr, *b32 = nullptr;

@@ -161,3 +161,26 @@ def test_mixed_kept_directions_stay_bounded_on_ill_conditioned_operator(cuda):
     err = float(torch.linalg.norm(x - x64) / torch.linalg.norm(x64))
     assert err <= ERR_BAR, (err, info)
     sysm.close()
+
+
+def test_mixed_whole_gpu_solves_measure_both_inner_precisions(cuda):
+    """On the whole GPU, a system's first mixed solve runs FP32 inner iterations and its
+    second FP64 ones; later solves keep the faster per decade of residual fall and report it
+    in inner_fp64. Every one of them meets the residual bar and the error bar against the
+    tight oracle, and reports an error estimate."""
+    torch = cuda
+    from simplefem_gb300 import workloads
+    sysm, ops = _system(3, 1, 5)
+    n = sysm.n
+    infos = []
+    for k in range(3):
+        b = workloads.uniform_vector(500 + k, n)
+        x = torch.zeros(n, dtype=torch.float64, device="cuda")
+        info = sysm.solve(torch.from_numpy(b).cuda(), x, method="rainbow", mode="mixed", precision=PRECISION)
+        _check(x.cpu().numpy(), b, ops, info, ("solve", k))
+        assert info["error_estimate"] > 0.0, info
+        infos.append(info)
+    assert [i["inner_fp64"] for i in infos[:2]] == [0, 1], infos
+    assert infos[2]["inner_fp64"] in (0, 1)
+    assert infos[1]["fp64_fallback"] == 0
+    sysm.close()
