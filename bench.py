@@ -453,13 +453,14 @@ def run_krylov_more(with_cpu, hodge=True):
     """The further drop-in drivers through their host-pointer entry points (upload inside the
     call): conjugate residuals and MINRES beside plain CG on the 3D P1 operator refined 6x,
     and the Hodge conjugate residual solver (inner SSOR-PCG) on a block system. The CPU
-    column is the oracle restatement (serial, as the reference's loops run per thread)."""
+    column is the oracle restatement with the reference's OpenMP loops, on every host core."""
     import simplefem_gb300 as S
     from simplefem_gb300 import workloads
     oracle = None
+    cores = os.cpu_count() or 1
     if with_cpu:
         from oracle import oracle
-        oracle.set_threads(1)
+        oracle.set_threads(cores)
     A, C, V = workloads.lattice_matrix(3, 1, 6, 0)
     n = len(A) - 1
     b = workloads.uniform_vector(17, n)
@@ -487,7 +488,7 @@ def run_krylov_more(with_cpu, hodge=True):
         if ofn is not None:
             t0 = time.perf_counter()
             K_o, _, _ = ofn(A, C, V, b, precision=1e-10)
-            leg.update({"cpu_ms": 1000.0 * (time.perf_counter() - t0), "cpu_iterations": K_o, "cpu_cores": 1})
+            leg.update({"cpu_ms": 1000.0 * (time.perf_counter() - t0), "cpu_iterations": K_o, "cpu_cores": cores})
         out[name] = leg
     if not hodge:
         return out
@@ -516,7 +517,8 @@ def run_krylov_more(with_cpu, hodge=True):
         if oracle is not None:
             t0 = time.perf_counter()
             K_o, _, _ = oracle.hodge_cr(variant, Am, Bm, Btm, Cm, bh, precision=1e-8, inner_precision=1e-10)
-            leg.update({"cpu_ms": 1000.0 * (time.perf_counter() - t0), "cpu_outer_iterations": K_o, "cpu_cores": 1})
+            leg.update({"cpu_ms": 1000.0 * (time.perf_counter() - t0), "cpu_outer_iterations": K_o,
+                        "cpu_cores": cores})
         out[key] = leg
     return out
 

@@ -821,7 +821,8 @@ int oracle_coo_to_csr(int rows, long long count, const int* r, const int* c, con
 }
 
 /* solver/sparsesolver.cpp:1687-1915, ConjugateResidualSolverCSR (and the arithmetically
- * identical _textbook variant, :1918-2156); returns K. */
+ * identical _textbook variant, :1918-2156); returns K. The loops carry the reference's
+ * OpenMP clauses (:1751, :1768, :1836, :1859): identical bits at one thread. */
 int oracle_cr(int N, double* x, const double* b, const int* A, const int* C, const double* V,
               double* res, double precision, int print_modulo)
 {
@@ -837,12 +838,14 @@ int oracle_cr(int N, double* x, const double* b, const int* A, const int* C, con
     int K = 0;
     while (K < N) {
         if (K == 0) {                                         /* :1749-1790 */
+            #pragma omp parallel for
             for (int c = 0; c < N; c++) {
                 res[c] = b[c];
                 for (int d = A[c]; d < A[c + 1]; d++) res[c] -= V[d] * x[C[d]];
                 dir[c] = res[c];
             }
             Ad_r = 0.0; Ad_Ad = 0.0;
+            #pragma omp parallel for reduction(+:Ad_r,Ad_Ad)
             for (int c = 0; c < N; c++) {
                 Adir[c] = 0.0;
                 for (int e = A[c]; e < A[c + 1]; e++) Adir[c] += V[e] * dir[C[e]];
@@ -857,6 +860,7 @@ int oracle_cr(int N, double* x, const double* b, const int* A, const int* C, con
         if (sqrt(fabs(Ad_Ad)) < ORACLE_MACHINE_EPSILON) break;
         const double alpha = Ad_r / Ad_Ad;                    /* :1840-1865 */
         double new_Ar_r = 0.0;
+        #pragma omp parallel for reduction(+:new_Ar_r)
         for (int c = 0; c < N; c++) {
             vil[c] = 0.0;
             for (int d = A[c]; d < A[c + 1]; d++) vil[c] += V[d] * Adir[C[d]];
@@ -867,6 +871,7 @@ int oracle_cr(int N, double* x, const double* b, const int* A, const int* C, con
         }
         const double beta = new_Ar_r / Ad_r;                  /* :1867-1882 */
         Ad_Ad = 0.0;
+        #pragma omp parallel for reduction(+:Ad_Ad)
         for (int c = 0; c < N; c++) {
             dir[c] = res[c] + beta * dir[c];
             Adir[c] = Ares[c] + beta * Adir[c];
@@ -879,7 +884,8 @@ int oracle_cr(int N, double* x, const double* b, const int* A, const int* C, con
     return K;
 }
 
-/* solver/sparsesolver.cpp:2159-2425, MINRESCSR; returns K (res = b - A x at the end). */
+/* solver/sparsesolver.cpp:2159-2425, MINRESCSR; returns K (res = b - A x at the end). The
+ * loops carry the reference's OpenMP clauses (:2238, :2259, :2289, :2305, :2320, :2336). */
 int oracle_minres(int N, double* x, const double* b, const int* A, const int* C, const double* V,
                   double* res, double precision, int print_modulo)
 {
@@ -898,12 +904,14 @@ int oracle_minres(int N, double* x, const double* b, const int* A, const int* C,
     while (K < N) {
         if (K == 0) {                                         /* :2233-2283 */
             double gamma_sq = 0.0;
+            #pragma omp parallel for reduction(+:gamma_sq)
             for (int c = 0; c < N; c++) {
                 v0[c] = 0.0; w0[c] = 0.0; v1[c] = b[c]; w1[c] = 0.0;
                 for (int d = A[c]; d < A[c + 1]; d++) v1[c] -= V[d] * x[C[d]];
                 gamma_sq += v1[c] * v1[c];
             }
             gamma = sqrt(gamma_sq);
+            #pragma omp parallel for
             for (int c = 0; c < N; c++) v1[c] /= gamma;
             s0 = s1 = 0.0;
             c0 = c1 = 1.0;
@@ -911,17 +919,20 @@ int oracle_minres(int N, double* x, const double* b, const int* A, const int* C,
         }
         if (fabs(eta) < tolerance) break;                     /* :2290-2293 */
         double delta = 0.0;                                   /* :2297-2313 */
+        #pragma omp parallel for reduction(+:delta)
         for (int c = 0; c < N; c++) {
             p[c] = 0.0;
             for (int d = A[c]; d < A[c + 1]; d++) p[c] += V[d] * v1[C[d]];
             delta += p[c] * v1[c];
         }
         double gamma_n_sq = 0.0;                              /* :2317-2330 */
+        #pragma omp parallel for reduction(+:gamma_n_sq)
         for (int c = 0; c < N; c++) {
             vn[c] = p[c] - delta * v1[c] - gamma * v0[c];
             gamma_n_sq += vn[c] * vn[c];
         }
         const double gamma_n = sqrt(gamma_n_sq);
+        #pragma omp parallel for
         for (int c = 0; c < N; c++) vn[c] /= gamma_n;
         const double alpha_0 = c1 * delta - c0 * s1 * gamma; /* :2338-2349 */
         const double alpha_1 = sqrt(alpha_0 * alpha_0 + gamma_n * gamma_n);
@@ -929,6 +940,7 @@ int oracle_minres(int N, double* x, const double* b, const int* A, const int* C,
         const double alpha_3 = s0 * gamma;
         const double cn = alpha_0 / alpha_1;
         const double sn = gamma_n / alpha_1;
+        #pragma omp parallel for
         for (int c = 0; c < N; c++) {                         /* :2353-2360 */
             wn[c] = (v1[c] - alpha_2 * w1[c] - alpha_3 * w0[c]) / alpha_1;
             x[c] = x[c] + cn * eta * wn[c];
@@ -1013,7 +1025,8 @@ int oracle_chebyshev(int N, double* x, const double* b, const int* A, const int*
  * diagonal, :76-91; HodgeConjugateResidualSolverCSR_diagonal), 1 SSOR with omega = 1
  * (:500-516; _SSOR and HodgeConjugateResidualSolverCSR), 2 plain CG (_textbook). The inner
  * solve of each restart starts from zero, those of the iterations from the previous inner
- * solution (:253-277). Returns K. */
+ * solution (:253-277). Returns K. The loops carry the reference's OpenMP clauses (:126,
+ * :162, :186, :206, :230, :298, :322, :357): identical bits at one thread. */
 int oracle_hodge_cr(int variant, int N, int L, double* x, const double* b,
                     const int* Ar, const int* Ac, const double* Av, const int* Br, const int* Bc, const double* Bv,
                     const int* Btr, const int* Btc, const double* Btv, const int* Cr, const int* Cc, const double* Cv,
@@ -1035,6 +1048,7 @@ int oracle_hodge_cr(int variant, int N, int L, double* x, const double* b,
     if (!dir || !Mdir || !Mres || !vil || !aux1 || !aux2 || !auxR || !diag) {
         free(dir); free(Mdir); free(Mres); free(vil); free(aux1); free(aux2); free(auxR); free(diag); return -1;
     }
+    #pragma omp parallel for
     for (int c = 0; c < L; c++) {                             /* :76-91 / :500-516 */
         diag[c] = 0.;
         for (int d = Ar[c]; d < Ar[c + 1]; d++) if (Ac[d] == c) diag[c] += Av[d];
@@ -1050,12 +1064,14 @@ int oracle_hodge_cr(int variant, int N, int L, double* x, const double* b,
     int K = 0;
     while (K < N) {
         if (K == 0) {                                         /* :107-200 */
+            #pragma omp parallel for
             for (int c = 0; c < L; c++) {
                 aux1[c] = 0.;
                 for (int d = Btr[c]; d < Btr[c + 1]; d++) aux1[c] += Btv[d] * x[Btc[d]];
             }
             for (int c = 0; c < L; c++) aux2[c] = 0.;
             HODGE_INNER(aux2, aux1);
+            #pragma omp parallel for
             for (int c = 0; c < N; c++) {
                 res[c] = b[c];
                 for (int d = Br[c]; d < Br[c + 1]; d++) res[c] -= sign_A * Bv[d] * aux2[Bc[d]];
@@ -1063,12 +1079,14 @@ int oracle_hodge_cr(int variant, int N, int L, double* x, const double* b,
                 dir[c] = res[c];
             }
             Md_r = 0.; Md_Md = 0.;
+            #pragma omp parallel for
             for (int c = 0; c < L; c++) {
                 aux1[c] = 0;
                 for (int d = Btr[c]; d < Btr[c + 1]; d++) aux1[c] += Btv[d] * dir[Btc[d]];
             }
             for (int c = 0; c < L; c++) aux2[c] = 0.;
             HODGE_INNER(aux2, aux1);
+            #pragma omp parallel for reduction(+:Md_r,Md_Md)
             for (int c = 0; c < N; c++) {
                 Mdir[c] = 0.;
                 for (int d = Br[c]; d < Br[c + 1]; d++) Mdir[c] += sign_A * Bv[d] * aux2[Bc[d]];
@@ -1084,11 +1102,13 @@ int oracle_hodge_cr(int variant, int N, int L, double* x, const double* b,
         if (sqrt(fabs(Md_Md)) < ORACLE_MACHINE_EPSILON) break;
         const double alpha = Md_r / Md_Md;                    /* :242-300 */
         double new_Mr_r = 0.;
+        #pragma omp parallel for
         for (int c = 0; c < L; c++) {
             aux1[c] = 0.;
             for (int d = Btr[c]; d < Btr[c + 1]; d++) aux1[c] += Btv[d] * Mdir[Btc[d]];
         }
         HODGE_INNER(aux2, aux1);
+        #pragma omp parallel for reduction(+:new_Mr_r)
         for (int c = 0; c < N; c++) {
             vil[c] = 0.;
             for (int d = Br[c]; d < Br[c + 1]; d++) vil[c] += sign_A * Bv[d] * aux2[Bc[d]];
@@ -1100,6 +1120,7 @@ int oracle_hodge_cr(int variant, int N, int L, double* x, const double* b,
         }
         const double beta = new_Mr_r / Md_r;                  /* :302-318 */
         Md_Md = 0.;
+        #pragma omp parallel for reduction(+:Md_Md)
         for (int c = 0; c < N; c++) {
             dir[c] = res[c] + beta * dir[c];
             Mdir[c] = Mres[c] + beta * Mdir[c];
