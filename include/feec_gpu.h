@@ -450,6 +450,18 @@ int feec_server_create(feec_server** srv, size_t hbm_budget_bytes, int slots, in
 int feec_server_submit(feec_server* srv, int N, const int* A, const int* C, const double* V,
                        const double* b, double* x, double precision, long long* id);
 
+/* Resident operators, for streams of right-hand sides on the same matrices: the matrix
+ * is uploaded and prepared once (coloring, layouts) in the calling thread, its estimated
+ * footprint reserved in the budget (FEEC_OOM if it does not fit beside what runs now),
+ * and *op identifies it. Requests submitted against it carry only their right-hand side
+ * and solution (host b, x valid until reported) and share the prepared matrix; a request
+ * on the whole-GPU solver also keeps the system's measured mixed-precision choice from
+ * one request to the next. An operator can be removed once no request on it is queued or
+ * running (FEEC_BADARG otherwise). */
+int feec_server_add_operator(feec_server* srv, int N, const int* A, const int* C, const double* V, int* op);
+int feec_server_submit_rhs(feec_server* srv, int op, const double* b, double* x, double precision, long long* id);
+int feec_server_remove_operator(feec_server* srv, int op);
+
 /* Moves up to max_out finished requests into out; *nout receives their number. */
 int feec_server_poll(feec_server* srv, feec_request_result* out, int max_out, int* nout);
 

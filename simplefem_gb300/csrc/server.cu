@@ -18,6 +18,7 @@
 #include <condition_variable>
 #include <cstring>
 #include <deque>
+#include <map>
 #include <memory>
 #include <mutex>
 #include <new>
@@ -39,10 +40,24 @@ namespace {
 
 using clock_type = std::chrono::steady_clock;
 
+// A resident operator: uploaded and prepared once (layouts, coloring, SELL copy), then
+// shared by the requests submitted against it. Cluster-solved requests only read its
+// layouts; whole-GPU requests run on its system one at a time (the server's big lane).
+struct Operator {
+    int id = 0;
+    feec_system* s = nullptr;
+    cudaStream_t home = nullptr;   // the system's creation stream: owns its persistent allocations
+    int n = 0;
+    long long nnz = 0;
+    size_t bytes = 0;       // counted against the budget while the operator is registered
+    int users = 0;          // requests queued or running on it (under feec_server::mu)
+};
+
 struct Request {
     long long id = 0;
     int n = 0;
     const int* A = nullptr; const int* C = nullptr; const double* V = nullptr;
+    std::shared_ptr<Operator> op;   // set: solve against a resident operator (A, C, V unused)
     const double* b = nullptr;
     double* x = nullptr;
     double precision = 1e-10;
@@ -85,6 +100,10 @@ size_t estimate_bytes(int n, long long nnz) {
     return (size_t)(nnz * (12 + 4 + 16 + 16 * 5 / 4)) + (size_t)n * 200 + (32u << 20);
 }
 
+// A request against a resident operator: its own right-hand side, solution and workspace
+// (FP64 x, b, residual and five inner vectors).
+size_t estimate_rhs_bytes(int n) { return (size_t)n * 80 + (1u << 20); }
+
 }  // namespace
 
 struct feec_server {
@@ -107,6 +126,8 @@ struct feec_server {
     std::mutex color_mu;               // colorings by pattern (see Coloring), oldest dropped first
     std::deque<std::pair<unsigned long long, std::shared_ptr<const Coloring>>> colorings;
     static constexpr size_t kMaxColorings = 64;
+    std::map<int, std::shared_ptr<Operator>> ops;   // resident operators (under mu)
+    int next_op = 1;
     long long submitted = 0, finished = 0;
     clock_type::time_point t0;
 };
@@ -117,27 +138,33 @@ double ms_since(const feec_server* srv, clock_type::time_point t) {
     return std::chrono::duration<double, std::milli>(t - srv->t0).count();
 }
 
-// Sets up and solves one request on `stream`; fills `res`.
-int serve_one(feec_server* srv, const Request& rq, cudaStream_t stream, feec_request_result& res) {
+// Uploads a request's (or a resident operator's) matrix and prepares it for the server's
+// method: the Rainbow coloring from the cache when the pattern was seen before.
+int prepare_system(feec_server* srv, int n, const int* A, const int* C, const double* V, cudaStream_t stream,
+                   feec_system** out) {
     feec_system* s = nullptr;
-    int st = feec_system_create(&s, rq.n, rq.A, rq.C, rq.V, 1, stream);
+    int st = feec_system_create(&s, n, A, C, V, 1, stream);
     if (st != FEEC_OK) return st;
-    struct Guard { feec_system* s; ~Guard() { feec_system_destroy(s); } } guard{s};
+    struct Guard {
+        feec_system*& s;
+        bool keep = false;
+        ~Guard() { if (!keep) feec_system_destroy(s); }
+    } guard{s};
     const bool rainbow = srv->method == FEEC_METHOD_RAINBOW;
     if (rainbow) {
         // the reference's Rainbow ordering (sparse/rainbow.cpp:14-130), from the cache when
         // this pattern was colored before, and the diagonal
-        const unsigned long long key = pattern_hash(rq.n, rq.A, rq.C);
+        const unsigned long long key = pattern_hash(n, A, C);
         std::shared_ptr<const Coloring> col;
         {
             std::lock_guard<std::mutex> lk(srv->color_mu);
             for (const auto& e : srv->colorings)
-                if (e.first == key && (int)e.second->F.size() == rq.n) { col = e.second; break; }
+                if (e.first == key && (int)e.second->F.size() == n) { col = e.second; break; }
         }
         if (!col) {
             auto c = std::make_shared<Coloring>();
-            c->F.resize((size_t)rq.n); c->B.resize((size_t)rq.n + 1); c->R.resize((size_t)rq.n);
-            st = feec_rainbow(rq.n, rq.A, rq.C, &c->nc, c->F.data(), c->B.data(), c->R.data());
+            c->F.resize((size_t)n); c->B.resize((size_t)n + 1); c->R.resize((size_t)n);
+            st = feec_rainbow(n, A, C, &c->nc, c->F.data(), c->B.data(), c->R.data());
             if (st != FEEC_OK) return st;
             c->B.resize((size_t)c->nc + 1);
             col = c;
@@ -145,13 +172,22 @@ int serve_one(feec_server* srv, const Request& rq, cudaStream_t stream, feec_req
             srv->colorings.emplace_back(key, col);
             if (srv->colorings.size() > feec_server::kMaxColorings) srv->colorings.pop_front();
         }
-        std::vector<double> diag((size_t)rq.n, 0.0);
-        for (int r = 0; r < rq.n; r++)
-            for (int k = rq.A[r]; k < rq.A[r + 1]; k++)
-                if (rq.C[k] == r) diag[r] += rq.V[k];
+        std::vector<double> diag((size_t)n, 0.0);
+        for (int r = 0; r < n; r++)
+            for (int k = A[r]; k < A[r + 1]; k++)
+                if (C[k] == r) diag[r] += V[k];
         st = feec_system_set_rainbow(s, diag.data(), 1.0, col->nc, col->F.data(), col->B.data(), col->R.data(), 1);
         if (st != FEEC_OK) return st;
     }
+    guard.keep = true;
+    *out = s;
+    return FEEC_OK;
+}
+
+// Solves one request on the prepared system `s` on `stream`; fills `res`.
+int solve_on(feec_server* srv, feec_system* s, const Request& rq, cudaStream_t stream, feec_request_result& res) {
+    int st = FEEC_OK;
+    const bool rainbow = srv->method == FEEC_METHOD_RAINBOW;
     const int is_float = srv->mode == FEEC_MODE_MIXED;
     cudaEvent_t done_ev = nullptr;
     FEEC_TRY(cudaEventCreateWithFlags(&done_ev, cudaEventBlockingSync | cudaEventDisableTiming));
@@ -282,6 +318,16 @@ int serve_one(feec_server* srv, const Request& rq, cudaStream_t stream, feec_req
     return hr.status;
 }
 
+// Sets up (unless the request names a resident operator) and solves one request.
+int serve_one(feec_server* srv, const Request& rq, cudaStream_t stream, feec_request_result& res) {
+    if (rq.op) return solve_on(srv, rq.op->s, rq, stream, res);
+    feec_system* s = nullptr;
+    const int st = prepare_system(srv, rq.n, rq.A, rq.C, rq.V, stream, &s);
+    if (st != FEEC_OK) return st;
+    struct Guard { feec_system* s; ~Guard() { feec_system_destroy(s); } } guard{s};
+    return solve_on(srv, s, rq, stream, res);
+}
+
 void worker_loop(feec_server* srv) {
     cudaSetDevice(srv->device);
     cudaStream_t stream = nullptr;
@@ -318,6 +364,7 @@ void worker_loop(feec_server* srv) {
             srv->in_use -= rq.bytes;
             srv->inflight--;
             srv->finished++;
+            if (rq.op) rq.op->users--;
             srv->done.push_back(res);
         }
         srv->cv.notify_all();
@@ -374,6 +421,91 @@ int feec_server_submit(feec_server* srv, int N, const int* A, const int* C, cons
     return FEEC_OK;
 }
 
+int feec_server_add_operator(feec_server* srv, int N, const int* A, const int* C, const double* V, int* op) {
+    if (!srv || N <= 0 || !A || !C || !V || !op) return FEEC_BADARG;
+    if (A[0] != 0 || A[N] < 0) return FEEC_BADARG;
+    auto o = std::make_shared<Operator>();
+    o->n = N;
+    o->nnz = A[N];
+    o->bytes = estimate_bytes(N, A[N]);
+    {
+        std::lock_guard<std::mutex> lk(srv->mu);
+        if (srv->stop) return FEEC_BADARG;
+        // resident bytes are reserved at once: they must fit beside what is running now
+        if (srv->in_use.load() + o->bytes > srv->budget) return FEEC_OOM;
+        srv->in_use += o->bytes;
+        size_t cur = srv->in_use.load(), pk = srv->peak.load();
+        while (cur > pk && !srv->peak.compare_exchange_weak(pk, cur)) {}
+    }
+    auto give_back = [&] {
+        std::lock_guard<std::mutex> lk(srv->mu);
+        srv->in_use -= o->bytes;
+        srv->cv.notify_all();
+    };
+    if (cudaStreamCreateWithFlags(&o->home, cudaStreamNonBlocking) != cudaSuccess) { give_back(); return FEEC_CUDA_ERROR; }
+    int st = prepare_system(srv, N, A, C, V, o->home, &o->s);
+    // cluster-solved requests share the SELL copy: built here, before any of them reads it
+    if (st == FEEC_OK && (long long)o->nnz < srv->big_nnz)
+        st = sell_prepare(o->s, srv->method == FEEC_METHOD_RAINBOW ? FEEC_METHOD_RAINBOW : FEEC_METHOD_CG);
+    cudaStreamSynchronize(o->home);
+    if (st != FEEC_OK) {
+        if (o->s) feec_system_destroy(o->s);
+        cudaStreamDestroy(o->home);
+        give_back();
+        return st;
+    }
+    std::lock_guard<std::mutex> lk(srv->mu);
+    o->id = srv->next_op++;
+    srv->ops[o->id] = o;
+    *op = o->id;
+    return FEEC_OK;
+}
+
+int feec_server_submit_rhs(feec_server* srv, int op, const double* b, double* x, double precision, long long* id) {
+    if (!srv || !b || !x || !(precision > 0.0)) return FEEC_BADARG;
+    Request rq;
+    {
+        std::lock_guard<std::mutex> lk(srv->mu);
+        if (srv->stop) return FEEC_BADARG;
+        auto it = srv->ops.find(op);
+        if (it == srv->ops.end()) return FEEC_BADARG;
+        rq.op = it->second;
+        rq.n = rq.op->n;
+        rq.b = b; rq.x = x; rq.precision = precision;
+        rq.bytes = estimate_rhs_bytes(rq.n);
+        rq.t_submit = clock_type::now();
+        if (rq.bytes > srv->budget) return FEEC_OOM;
+        rq.op->users++;
+        rq.id = srv->next_id++;
+        srv->queue.push_back(rq);
+        srv->submitted++;
+    }
+    srv->cv.notify_all();
+    if (id) *id = rq.id;
+    return FEEC_OK;
+}
+
+int feec_server_remove_operator(feec_server* srv, int op) {
+    if (!srv) return FEEC_BADARG;
+    std::shared_ptr<Operator> o;
+    {
+        std::lock_guard<std::mutex> lk(srv->mu);
+        auto it = srv->ops.find(op);
+        if (it == srv->ops.end() || it->second->users > 0) return FEEC_BADARG;
+        o = it->second;
+        srv->ops.erase(it);
+    }
+    feec_system_destroy(o->s);
+    o->s = nullptr;
+    cudaStreamDestroy(o->home);
+    {
+        std::lock_guard<std::mutex> lk(srv->mu);
+        srv->in_use -= o->bytes;
+    }
+    srv->cv.notify_all();
+    return FEEC_OK;
+}
+
 int feec_server_poll(feec_server* srv, feec_request_result* out, int max_out, int* nout) {
     if (!srv || !nout || (max_out > 0 && !out)) return FEEC_BADARG;
     std::lock_guard<std::mutex> lk(srv->mu);
@@ -410,6 +542,11 @@ int feec_server_destroy(feec_server* srv) {
     }
     srv->cv.notify_all();
     for (auto& t : srv->workers) t.join();
+    for (auto& e : srv->ops) {
+        feec_system_destroy(e.second->s);
+        cudaStreamDestroy(e.second->home);
+    }
+    srv->ops.clear();
     delete srv;
     return FEEC_OK;
 }

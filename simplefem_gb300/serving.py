@@ -42,6 +42,9 @@ def _declare(L):
     L.feec_server_stats.argtypes = [vp, ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(ctypes.c_size_t),
                                     ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_longlong)]
     L.feec_server_destroy.argtypes = [vp]
+    L.feec_server_add_operator.argtypes = [vp, ctypes.c_int, vp, vp, vp, ctypes.POINTER(ctypes.c_int)]
+    L.feec_server_submit_rhs.argtypes = [vp, ctypes.c_int, vp, vp, ctypes.c_double, ctypes.POINTER(ctypes.c_longlong)]
+    L.feec_server_remove_operator.argtypes = [vp, ctypes.c_int]
     L._feec_server_declared = True
     return L
 
@@ -55,6 +58,7 @@ class Server:
         _native.check(st, "feec_server_create")
         self._h = h
         self._live = {}          # id -> arrays kept alive until the request finishes
+        self._ops = {}           # resident operator id -> rows
         self._lock = threading.Lock()
 
     def submit(self, A, C, V, b, precision=1e-10) -> int:
@@ -75,6 +79,43 @@ class Server:
             _native.check(st, "feec_server_submit")
             self._live[rid.value] = (A, C, V, b, x)
         return rid.value
+
+    def add_operator(self, A, C, V) -> int:
+        """Upload and prepare a matrix once (coloring, layouts); returns its operator id for
+        submit_rhs. Its footprint is reserved in the budget until remove_operator."""
+        n = len(A) - 1
+        if n < 1:
+            raise ValueError("an operator needs at least one row")
+        A, C, V = _csr(n, A, C, V)
+        op = ctypes.c_int(0)
+        p = lambda a: a.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
+        _native.check(self._lib.feec_server_add_operator(self._h, n, p(A), p(C), p(V), ctypes.byref(op)),
+                      "feec_server_add_operator")
+        with self._lock:
+            self._ops[op.value] = n
+        return op.value
+
+    def submit_rhs(self, op, b, precision=1e-10) -> int:
+        """Queue A x = b against a resident operator. The right-hand side is read by a worker
+        thread after this call returns: it is kept alive here until the request is polled."""
+        with self._lock:
+            n = self._ops.get(op)
+        if n is None:
+            raise ValueError(f"unknown operator {op}")
+        b = _vec(b, "b", n)
+        x = np.zeros(n)
+        rid = ctypes.c_longlong(0)
+        p = lambda a: a.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
+        with self._lock:
+            st = self._lib.feec_server_submit_rhs(self._h, int(op), p(b), p(x), float(precision), ctypes.byref(rid))
+            _native.check(st, "feec_server_submit_rhs")
+            self._live[rid.value] = (None, None, None, b, x)
+        return rid.value
+
+    def remove_operator(self, op) -> None:
+        _native.check(self._lib.feec_server_remove_operator(self._h, int(op)), "feec_server_remove_operator")
+        with self._lock:
+            self._ops.pop(op, None)
 
     def poll(self, max_out=1024) -> list:
         buf = (RequestResult * max_out)()

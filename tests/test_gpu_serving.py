@@ -164,3 +164,55 @@ def test_repeated_pattern_reuses_its_coloring(cuda):
     assert len(res) == 2 and all(r["status"] == 0 for r in res)
     assert np.array_equal(res[0]["x"], res[1]["x"])
     srv.close()
+
+
+def test_resident_operators_serve_right_hand_sides(cuda):
+    """Resident operators: a matrix added once serves many right-hand sides, several of them
+    in flight at the same time on the cluster path, and a large one (above the whole-GPU
+    threshold) on the whole-GPU solver; every result reaches its tolerance and equals the
+    one-request-one-matrix path's (1e-9). The operator's bytes are held while it is
+    registered; removing it with requests outstanding is refused, afterwards it works and
+    the bytes come back."""
+    from simplefem_gb300 import _native, workloads
+    from simplefem_gb300.serving import Server
+    A, C, V, _ = _problem(3, 2, 4, 51)
+    Ab, Cb, Vb = workloads.lattice_matrix(2, 1, 10, 1)      # 7.3 M entries: whole-GPU solver
+    srv = Server(hbm_budget_bytes=60 * 10**9, slots=6)
+    before = srv.stats()["bytes_in_use"]
+    op = srv.add_operator(A, C, V)
+    opb = srv.add_operator(Ab, Cb, Vb)
+    assert srv.stats()["bytes_in_use"] > before
+    rhs = {}
+    for k in range(8):
+        b = workloads.uniform_vector(600 + k, len(A) - 1)
+        rhs[srv.submit_rhs(op, b, 1e-10)] = (A, C, V, b, 1e-10)
+    for k in range(2):
+        b = workloads.uniform_vector(700 + k, len(Ab) - 1)
+        rhs[srv.submit_rhs(opb, b, 1e-10)] = (Ab, Cb, Vb, b, 1e-10)
+    with pytest.raises(_native.FeecError):
+        srv.remove_operator(op)                              # requests outstanding
+    assert srv.wait(600)
+    res = {r["id"]: r for r in srv.poll()}
+    assert len(res) == len(rhs)
+    for rid, (A_, C_, V_, b, tol) in rhs.items():
+        r = res[rid]
+        assert r["status"] == 0, r
+        assert _relres(A_, C_, V_, b, r["x"]) <= tol, r
+    big = [res[rid] for rid, v in rhs.items() if v[0] is Ab]
+    assert all(r["cluster_blocks"] < 0 for r in big), big       # negative: the whole-GPU grid
+    # the same right-hand side through the one-request-one-matrix path
+    rid0 = next(iter(rhs))
+    A_, C_, V_, b, tol = rhs[rid0]
+    ref = Server(hbm_budget_bytes=10 * 10**9, slots=1)
+    ref.submit(A_, C_, V_, b, tol)
+    assert ref.wait(300)
+    x_ref = ref.poll()[0]["x"]
+    ref.close()
+    x = res[rid0]["x"]
+    assert np.linalg.norm(x - x_ref) <= 1e-9 * np.linalg.norm(x_ref)
+    srv.remove_operator(op)
+    srv.remove_operator(opb)
+    assert srv.stats()["bytes_in_use"] == before
+    with pytest.raises(ValueError):
+        srv.submit_rhs(op, np.ones(len(A) - 1), 1e-10)        # removed
+    srv.close()
