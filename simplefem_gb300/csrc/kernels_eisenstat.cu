@@ -87,6 +87,7 @@ __global__ void __launch_bounds__(kThreads, 2) eisenstat_persistent(PcgArgs<T> a
         if (!grid_barrier(a.st, epoch, 31)) return;
     }
     const bool keep = a.keep_dir != 0;
+    constexpr int LL = LANES > kLongLanes ? LANES : kLongLanes;   // long rows of multicolor phases
     Acc azr = AT::zero();
     for (int i = tid; i < n; i += nthr) {
         if (__ldg(&a.wd[i]) == T(0)) continue;
@@ -120,14 +121,16 @@ __global__ void __launch_bounds__(kThreads, 2) eisenstat_persistent(PcgArgs<T> a
         __syncthreads();
         if (s_ctl) { status = FEEC_OK; break; }
 
-        // backward sweep (:870-884 / :1506-1530), with the previous iteration's d = z + beta d
+        // backward sweep (:870-884 / :1506-1530), with the previous iteration's d = z + beta d;
+        // in multicolor layouts each color's long rows get LL lanes (split_rows)
         for (int p = 0; p < a.nbw; p++) {
             const int lo_r = __ldg(&a.bptr[p]), hi_r = __ldg(&a.bptr[p + 1]);
-            FEEC_FOR_ROW_GROUPS(lo_r, hi_r, k, act) {
+            auto brow = [&](auto L, int k, bool act, int ln) {
+                constexpr int LN = decltype(L)::value;
                 const int i = act ? __ldg(&a.brows[k]) : 0;
                 const int lo = act ? __ldg(&a.usplit[i]) : 0, hi = act ? __ldg(&a.rp[i + 1]) : 0;
-                const T s = seg_dot_guarded<T, LANES>(a.ci, a.val, a.m, a.wd, lo, hi, lane, g_iter);
-                if (act && lane == 0) {
+                const T s = seg_dot_guarded<T, LN>(a.ci, a.val, a.m, a.wd, lo, hi, ln, g_iter);
+                if (act && ln == 0) {
                     const T w = __ldg(&a.wd[i]);
                     if (w != T(0)) {
                         T dv = a.d[i];
@@ -135,6 +138,11 @@ __global__ void __launch_bounds__(kThreads, 2) eisenstat_persistent(PcgArgs<T> a
                         a.m[i] = (dv - s) * w;
                     }
                 }
+            };
+            if (a.bsplit) {
+                split_rows<LANES, LL>(lo_r, __ldg(&a.bsplit[p]), hi_r, brow);
+            } else {
+                FEEC_FOR_ROW_GROUPS(lo_r, hi_r, k, act) brow(std::integral_constant<int, LANES>{}, k, act, lane);
             }
             if (!grid_barrier(a.st, epoch, 33)) return;
         }
@@ -142,10 +150,11 @@ __global__ void __launch_bounds__(kThreads, 2) eisenstat_persistent(PcgArgs<T> a
         Acc dad = AT::zero();
         for (int p = 0; p < a.nf; p++) {
             const int lo_r = __ldg(&a.fptr[p]), hi_r = __ldg(&a.fptr[p + 1]);
-            FEEC_FOR_ROW_GROUPS(lo_r, hi_r, i, act) {
+            auto frow = [&](auto L, int i, bool act, int ln) {
+                constexpr int LN = decltype(L)::value;
                 const int lo = act ? __ldg(&a.rp[i]) : 0, hi = act ? __ldg(&a.lsplit[i]) : 0;
-                const T s = seg_dot_guarded<T, LANES>(a.ci, a.val, a.q, a.wd, lo, hi, lane, g_iter);
-                if (act && lane == 0) {
+                const T s = seg_dot_guarded<T, LN>(a.ci, a.val, a.q, a.wd, lo, hi, ln, g_iter);
+                if (act && ln == 0) {
                     const T w = __ldg(&a.wd[i]);
                     if (w != T(0)) {
                         const T dv = a.d[i], tv = a.m[i];
@@ -156,6 +165,11 @@ __global__ void __launch_bounds__(kThreads, 2) eisenstat_persistent(PcgArgs<T> a
                         dad = AT::add(dad, cv * dv);
                     }
                 }
+            };
+            if (a.fsplit) {
+                split_rows<LANES, LL>(lo_r, __ldg(&a.fsplit[p]), hi_r, frow);
+            } else {
+                FEEC_FOR_ROW_GROUPS(lo_r, hi_r, i, act) frow(std::integral_constant<int, LANES>{}, i, act, lane);
             }
             if (p + 1 < a.nf && !grid_barrier(a.st, epoch, 34)) return;
         }

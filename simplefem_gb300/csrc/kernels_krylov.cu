@@ -108,30 +108,6 @@ __device__ __forceinline__ void rows_pipelined(const PcgArgs<T>& a, int lo, int 
     }
 }
 
-// Rows [lo, hi) of a multicolor phase whose rows are sorted longest first, [lo, sp) being
-// the long ones: the long rows get LL lanes each (the first warps of the grid), the rest LS
-// lanes each (the warps after them), so that no row group walks more than a few strides
-// of its row. A phase lasts as long as its slowest row group: with LS lanes for every row,
-// the longest rows of a color (65 entries on 3D P2) took several dependent rounds of index
-// loads and gathers while the other warps waited at the barrier. body(lanes, row, active,
-// lane in group) is called with std::integral_constant lanes, uniformly across each warp.
-template <int LS, int LL, typename F>
-__device__ __forceinline__ void split_rows(int lo, int sp, int hi, F&& body) {
-    const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) / 32);
-    const int nwarps = (int)(gridDim.x * blockDim.x / 32);
-    const int wl = (sp - lo + (32 / LL) - 1) / (32 / LL);   // warps the long rows take
-    for (int w = warp; w < wl; w += nwarps) {
-        const int i = lo + w * (32 / LL) + (int)((threadIdx.x & 31) / LL);
-        body(std::integral_constant<int, LL>{}, i, i < sp, (int)(threadIdx.x & (LL - 1)));
-    }
-    int w = warp - wl % nwarps;
-    if (w < 0) w += nwarps;
-    for (; sp + w * (32 / LS) < hi; w += nwarps) {
-        const int i = sp + w * (32 / LS) + (int)((threadIdx.x & 31) / LS);
-        body(std::integral_constant<int, LS>{}, i, i < hi, (int)(threadIdx.x & (LS - 1)));
-    }
-}
-
 // ---------------------------------------------------------------------------
 // Plain CG
 // ---------------------------------------------------------------------------
